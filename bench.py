@@ -1,0 +1,300 @@
+"""Benchmark of the DG scalar-wave evolution hot path (grid-point RHS/s).
+
+Workload (the configuration the metric is quoted on that fits one GPU):
+ScalarWave first-order system on the periodic cube [0, 2pi]^3 split into
+32^3 elements of 8^3 Legendre-Gauss-Lobatto points (16,777,216 points, 5 FP64
+variables), Gaussian pulse psi = exp(-|x-c|^2/0.25), c = (pi, pi, pi),
+UpwindPenalty correction, SSP-RK3 with dt = 2e-4.  One bench step = one
+SSP-RK3 step over the whole grid = 3 right-hand-side evaluations of every
+grid point.  Metric: grid-point RHS evaluations per second (points x 3 x
+steps / time).
+
+The state (671 MB per copy) is larger than L2 (129 MB), so no L2 flush is
+done between timed steps.
+
+`--impl reference` times the reference algorithm on the host CPU cores
+instead: the FP64 C++ restatement in oracle/ (the reference executable
+needs Charm++, Blaze, LIBXSMM and HDF5, none of which is in this image).
+
+Multi-GPU: the path is run as independent replicas (one evolution per
+rank, no collective); value = total grid-point RHS over all ranks / max time.
+"""
+import argparse
+import json
+import math
+import os
+import subprocess
+import sys
+import threading
+import time
+
+import numpy as np
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, ROOT)
+
+METRIC = "grid-pt RHS/s FP64 vs batched mixed at <=1e-6 rel L2; adjoint s/grad"
+UNIT = "grid-point RHS/s"
+ELEMS = 32
+N_PTS = 8
+DT = 2e-4
+BYTES_PER_POINT_LAUNCH = (80.0 + 120.0 + 120.0) / 3.0  # compulsory HBM bytes per point per stage
+# FP64 pipe instructions per point per stage of the plain kernel at N = 8
+# (even/odd contraction: 6 per derivative x 6 derivatives, dt Pi sum 2,
+# RK combination ~10, face corrections ~3); counted from the kernel source.
+FP64_OPS_PER_POINT_STAGE = 50.0
+
+
+def load_peaks():
+    try:
+        with open(os.path.join(ROOT, "MEASURED_PEAKS.json")) as f:
+            return json.load(f), "measured"
+    except Exception:
+        return {"hbm_gbs": 6800.0, "bf16_tflops": 1900.0}, "fallback"
+
+
+class ClockSampler:
+    """nvidia-smi clocks and throttle reasons sampled during the timed region."""
+
+    FIELDS = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+              "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+              "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, device_index):
+        self.device_index = device_index
+        self.proc = None
+        self.lines = []
+        self.thread = None
+
+    def start(self):
+        try:
+            self.proc = subprocess.Popen(
+                ["nvidia-smi", "-i", str(self.device_index), "--query-gpu=" + self.FIELDS,
+                 "--format=csv,noheader,nounits", "-lms", "200"],
+                stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
+        except Exception:
+            self.proc = None
+            return
+        self.thread = threading.Thread(target=self._read, daemon=True)
+        self.thread.start()
+
+    def _read(self):
+        for line in self.proc.stdout:
+            self.lines.append(line.strip())
+
+    def stop(self):
+        if self.proc is None:
+            return None
+        self.proc.terminate()
+        try:
+            self.proc.wait(timeout=5)
+        except Exception:
+            self.proc.kill()
+        if self.thread:
+            self.thread.join(timeout=2)
+        sm, smax, reasons = [], None, set()
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        for ln in self.lines:
+            parts = [p.strip() for p in ln.split(",")]
+            if len(parts) < 9:
+                continue
+            try:
+                sm.append(float(parts[1]))
+                smax = float(parts[2])
+            except ValueError:
+                continue
+            for name, val in zip(names, parts[5:9]):
+                if val.lower().startswith("active"):
+                    reasons.add(name)
+        if not sm:
+            return None
+        return {"sm_mhz": float(np.median(sm)), "sm_max_mhz": smax,
+                "reasons": sorted(reasons), "samples": len(sm)}
+
+
+def dist_env():
+    ws = int(os.environ.get("WORLD_SIZE", "1"))
+    rank = int(os.environ.get("RANK", "0"))
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    return ws, rank, local
+
+
+def cpu_threads():
+    try:
+        return len(os.sched_getaffinity(0))
+    except Exception:
+        return os.cpu_count() or 1
+
+
+def cpu_reference_run(steps, warmup, threads, elems=16):
+    """Times the FP64 oracle (C++ restatement of the reference) on host cores.
+
+    The sample is a 16^3-element brick of the same N = 8 grid (same per-point
+    work as the 32^3 workload, 1/8 of its points) per step.
+    """
+    from oracle import pyoracle
+    from spectre_gb300.dgsw import Brick
+    bricks = [Brick((elems, elems, elems))]
+    params = pyoracle.gaussian_params(1, amp=1.0, width=0.5)
+    u = pyoracle.initial_data(bricks, N_PTS, "gaussian", params)
+    points = elems ** 3 * N_PTS ** 3
+    for _ in range(warmup):
+        u = pyoracle.evolve(bricks, N_PTS, u, DT, 1, threads=threads)
+    t0 = time.perf_counter()
+    for _ in range(steps):
+        u = pyoracle.evolve(bricks, N_PTS, u, DT, 1, threads=threads)
+    el = time.perf_counter() - t0
+    return points * 3 * steps / el, el, points
+
+
+def run_reference(args):
+    ws, rank, local = dist_env()
+    if rank != 0:
+        return 0
+    threads = cpu_threads()
+    steps = max(1, args.steps)
+    value, el, points = cpu_reference_run(steps, min(args.warmup, 1), threads)
+    sample = ("FP64 C++ restatement of the reference (oracle/), 16^3 elements x 8^3 LGL points "
+              "(%d points, 1/8 of the workload), %d SSP-RK3 steps, %d threads, %.2f s"
+              % (points, steps, threads, el))
+    line = {
+        "impl": "reference", "metric": METRIC, "value": value, "unit": UNIT,
+        "n_gpus": args.gpus, "steps": steps, "warmup": args.warmup,
+        "ms_per_step": el / steps * 1e3 * 8.0, "higher_is_better": True,
+        "scaling": "weak", "vs_baseline": None, "dtype": "f64", "data": "synthetic",
+        "config": workload_config(),
+        "cpu_baseline": {"value": value, "unit": UNIT, "cores": threads, "kind": "port",
+                         "sample": sample},
+        "e2e": {"value": value, "unit": UNIT, "h2d_bytes_per_step": 0,
+                "d2h_bytes_per_step": 0},
+    }
+    print(json.dumps(line), flush=True)
+    return 0
+
+
+def workload_config(elems=ELEMS):
+    return {"workload": "ScalarWave %d^3 elements x 8^3 LGL points periodic [0,2pi]^3, "
+                        "Gaussian pulse, UpwindPenalty, SSP-RK3 dt=2e-4" % elems,
+            "elements": elems ** 3, "points_per_dim": N_PTS,
+            "grid_points": elems ** 3 * N_PTS ** 3, "variables": 5, "dt": DT,
+            "precision": "plain FP64", "l2": "inputs larger than L2 (671 MB state), no flush"}
+
+
+def run_ours(args):
+    import torch
+    from spectre_gb300 import Brick, DgEvolution
+    ws, rank, local = dist_env()
+    if ws > 1:
+        import torch.distributed as dist
+        torch.cuda.set_device(local)
+        dist.init_process_group("nccl", device_id=torch.device("cuda", local))
+    dev = local if ws > 1 else 0
+    torch.cuda.set_device(dev)
+    peaks, peak_kind = load_peaks()
+    bricks = [Brick((args.elements, args.elements, args.elements))]
+    params = np.array([[1.0, 0.5, math.pi, math.pi, math.pi]])
+    ev = DgEvolution(bricks, N_PTS, device=dev)
+    ev.set_initial_data("gaussian", params)
+    stream = torch.cuda.ExternalStream(ev.stream_ptr(), device=dev)
+    for _ in range(max(args.warmup, 3)):
+        ev.step(1, DT, sync=False)
+    ev.synchronize()
+    sampler = ClockSampler(dev) if rank == 0 else None
+    if sampler:
+        sampler.start()
+        time.sleep(0.3)
+    if ws > 1:
+        torch.distributed.barrier()
+    torch.cuda.synchronize()
+    e0 = torch.cuda.Event(enable_timing=True)
+    e1 = torch.cuda.Event(enable_timing=True)
+    with torch.cuda.stream(stream):
+        e0.record(stream)
+        ev.step(args.steps, DT, sync=False)
+        e1.record(stream)
+    e1.synchronize()
+    torch.cuda.synchronize()
+    ms = e0.elapsed_time(e1)
+    if ws > 1:
+        t = torch.tensor([ms], device="cuda")
+        torch.distributed.all_reduce(t, op=torch.distributed.ReduceOp.MAX)
+        ms = float(t.item())
+        torch.distributed.barrier()
+    clocks = sampler.stop() if sampler else None
+    points = ev.grid_points
+    value = points * 3 * args.steps * ws / (ms * 1e-3)
+    launch_ms = ms / (3 * args.steps)
+    achieved_gbs = BYTES_PER_POINT_LAUNCH * points / (launch_ms * 1e-3) / 1e9
+
+    # end to end through the C ABI with pinned host buffers: H2D of the state,
+    # one step, D2H of the new state, every step
+    e2e = None
+    if rank == 0 or ws > 1:
+        host = torch.empty(ev.state_size, dtype=torch.float64, pin_memory=True)
+        hnp = host.numpy()
+        ev.get_state(hnp)
+        k2 = max(1, min(args.steps, 10))
+        torch.cuda.synchronize()
+        t0 = time.perf_counter()
+        for _ in range(k2):
+            ev.set_state(hnp)
+            ev.step(1, DT, sync=False)
+            ev.get_state(hnp)
+        el = time.perf_counter() - t0
+        e2e = {"value": points * 3 * k2 * ws / el, "unit": UNIT,
+               "h2d_bytes_per_step": ev.state_size * 8, "d2h_bytes_per_step": ev.state_size * 8,
+               "steps": k2}
+
+    cpu = None
+    if rank == 0 and not args.no_cpu_baseline:
+        threads = cpu_threads()
+        v, el, pts = cpu_reference_run(1, 0, threads)
+        cpu = {"value": v, "unit": UNIT, "cores": threads, "kind": "port",
+               "sample": "FP64 C++ restatement (oracle/), 16^3 elements x 8^3 points, "
+                         "1 SSP-RK3 step, %.2f s" % el}
+    if ws > 1:
+        torch.distributed.barrier()
+    if rank == 0:
+        fp64_tflops = FP64_OPS_PER_POINT_STAGE * 2.0 * points / (launch_ms * 1e-3) / 1e12
+        line = {
+            "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": ws, "steps": args.steps,
+            "warmup": max(args.warmup, 3), "ms_per_step": ms / args.steps,
+            "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f64",
+            "data": "synthetic", "config": workload_config(args.elements),
+            "roofline": {"bound": "hbm", "achieved": achieved_gbs,
+                         "peak": peaks.get("hbm_gbs"), "unit": "GB/s",
+                         "frac": achieved_gbs / peaks.get("hbm_gbs"), "traffic": None,
+                         "peak_source": peak_kind,
+                         "bytes_per_point_launch": BYTES_PER_POINT_LAUNCH,
+                         "avg_launch_ms": launch_ms},
+            "fp64_pipe": {"achieved_tflops": fp64_tflops, "peak_tflops": 1.01,
+                          "peak_source": "DFMA probe on this pool's GB300 (0.505 T inst/s)",
+                          "frac": fp64_tflops / 1.01},
+            "cpu_baseline": cpu, "e2e": e2e, "clocks": clocks,
+            "gpu_launches": 3 * args.steps,
+        }
+        print(json.dumps(line), flush=True)
+    ev.close()
+    if ws > 1:
+        torch.distributed.destroy_process_group()
+    return 0
+
+
+def main():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=30)
+    ap.add_argument("--warmup", type=int, default=3)
+    ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
+    ap.add_argument("--no-cpu-baseline", action="store_true")
+    ap.add_argument("--elements", type=int, default=ELEMS,
+                    help="elements per axis (default 32: the benchmark workload; smaller "
+                         "values only for profiling captures)")
+    args = ap.parse_args()
+    if args.impl == "reference":
+        return run_reference(args)
+    return run_ours(args)
+
+
+if __name__ == "__main__":
+    sys.exit(main())

@@ -1,0 +1,180 @@
+/*
+ * dgsw.h -- C ABI of the GB300-native DG scalar-wave evolution hot path.
+ *
+ * This library replaces, for one GPU, the per-element DG evolution step of
+ * SpECTRE's first-order scalar wave (reference release 2024.09.29):
+ *   ScalarWave::System<3>            src/Evolution/Systems/ScalarWave/System.hpp:39-57
+ *   ScalarWave::TimeDerivative<3>    src/Evolution/Systems/ScalarWave/TimeDerivative.cpp:13-45
+ *     (called from evolution::dg::Actions::detail::volume_terms,
+ *      src/Evolution/DiscontinuousGalerkin/Actions/VolumeTermsImpl.tpp:76-295,
+ *      after partial_derivatives, src/NumericalAlgorithms/LinearOperators/PartialDerivatives.tpp:191-241)
+ *   ScalarWave::BoundaryCorrections::UpwindPenalty<3>
+ *                                    src/Evolution/Systems/ScalarWave/BoundaryCorrections/UpwindPenalty.cpp:35-205
+ *   dg::lift_flux + add_slice_to_data
+ *                                    src/NumericalAlgorithms/DiscontinuousGalerkin/LiftFlux.hpp:41-62,
+ *                                    src/Evolution/DiscontinuousGalerkin/Actions/ApplyBoundaryCorrections.hpp:723-1050
+ *   TimeSteppers::Rk3HesthavenSsp    src/Time/TimeSteppers/Rk3HesthavenSsp.cpp:21-81
+ *     (TimeStepper::update_u, src/Time/TimeSteppers/TimeStepper.hpp:56-101,
+ *      driven by Actions::UpdateU, src/Time/Actions/UpdateU.hpp:45-154)
+ *
+ * Conventions
+ *  - Every function returns an int status: DGSW_OK (0) or a negative
+ *    DgswStatus.  Nothing aborts.  dgsw_last_error() gives the message of the
+ *    most recent failure on that handle (or of the last handle-less call).
+ *  - State layout is the reference's Variables layout, one contiguous block
+ *    per element, elements in initial_element_ids order: per element
+ *    [var][k][j][i] with i (xi) fastest, vars = Psi, Pi, Phi_x, Phi_y, Phi_z.
+ *  - Host pointers are borrowed for the duration of a call.  Device buffers
+ *    are owned by the handle.  "_device" entry points take device pointers.
+ *  - One CUDA stream per handle; a handle is not thread-safe.
+ *  - Functions with no handle argument are host-only and need no GPU.
+ */
+#ifndef DGSW_H
+#define DGSW_H
+
+#include <stddef.h>
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+#define DGSW_ABI_VERSION 1
+
+typedef enum {
+  DGSW_OK = 0,
+  DGSW_ERR_ARGUMENT = -1,     /* bad configuration or argument */
+  DGSW_ERR_CUDA = -2,         /* CUDA runtime error */
+  DGSW_ERR_UNSUPPORTED = -3,  /* valid request this build does not support */
+  DGSW_ERR_NOT_FINITE = -4,   /* NaN or Inf detected in the state */
+  DGSW_ERR_NO_DEVICE = -5     /* no usable GB300-class device */
+} DgswStatus;
+
+/* System::variables_tag, ScalarWave/System.hpp:39-57 */
+typedef enum { DGSW_SYSTEM_SCALAR_WAVE_3D = 0 } DgswSystem;
+/* BoundaryCorrection creatable classes, ScalarWave/BoundaryCorrections/Factory.hpp */
+typedef enum { DGSW_CORRECTION_UPWIND_PENALTY = 0 } DgswBoundaryCorrection;
+/* TimeStepper creatable classes, Time/TimeSteppers/Factory.hpp */
+typedef enum { DGSW_STEPPER_RK3_HESTHAVEN_SSP = 0 } DgswTimeStepper;
+/* Arithmetic of the derivative/flux/lift work.  FP64: everything in FP64.
+ * MIXED: FP32 contractions with the D-matrix split into hi+lo FP32 parts,
+ * FP64 state and FP64 accumulation of each time step. */
+typedef enum { DGSW_PRECISION_FP64 = 0, DGSW_PRECISION_MIXED = 1 } DgswPrecision;
+
+/* One periodic rectilinear evolution domain [lower, upper]^3 with
+ * elements[d] elements along axis d.  A count n = b * 2^L (b odd) is laid out
+ * as b aligned blocks of refinement level L (Domain/Creators/AlignedLattice,
+ * blocks numbered x fastest, Domain/DomainHelpers.cpp:1187-1201). */
+typedef struct {
+  double lower[3];
+  double upper[3];
+  int32_t elements[3];
+} DgswBrick;
+
+typedef struct {
+  int32_t system;              /* DgswSystem */
+  int32_t boundary_correction; /* DgswBoundaryCorrection */
+  int32_t time_stepper;        /* DgswTimeStepper */
+  int32_t precision;           /* DgswPrecision */
+  int32_t n_instances;         /* independent evolutions in this handle */
+  const DgswBrick* bricks;     /* n_instances domains */
+  /* Legendre-Gauss-Lobatto points per dimension, per element (isotropic),
+   * in global element order.  NULL: every element has uniform_points. */
+  const int32_t* points_per_element;
+  int32_t uniform_points;
+  double gamma2;               /* constraint damping, ScalarWave/Initialize.hpp:33-56 */
+  int32_t device;              /* CUDA device ordinal */
+} DgswConfig;
+
+typedef struct DgswHandle_* DgswHandle;
+
+/* ---- handle lifecycle ---------------------------------------------------- */
+int dgsw_create(const DgswConfig* config, DgswHandle* out);
+int dgsw_destroy(DgswHandle h);
+const char* dgsw_last_error(DgswHandle h); /* h may be NULL */
+int dgsw_abi_version(void);
+
+/* Sizes: elements over all instances; doubles in one state vector. */
+int dgsw_sizes(DgswHandle h, int64_t* n_elements, int64_t* state_doubles,
+               int64_t* grid_points);
+/* The handle's CUDA stream (a cudaStream_t), for interop. */
+void* dgsw_stream(DgswHandle h);
+int dgsw_synchronize(DgswHandle h);
+
+/* ---- state transfer (Variables<tmpl::list<Psi, Pi, Phi>>) ---------------- */
+int dgsw_set_state(DgswHandle h, const double* host_u);
+int dgsw_get_state(DgswHandle h, double* host_u);
+int dgsw_set_state_device(DgswHandle h, const double* dev_u);
+int dgsw_get_state_device(DgswHandle h, double* dev_u);
+/* Analytic initial data evaluated on the device at time t.
+ * kind 0: PlaneWave (PointwiseFunctions/AnalyticSolutions/WaveEquation/
+ *         PlaneWave.cpp:56-80) psi = sin(k.x - |k| t), params = {kx, ky, kz}.
+ * kind 1: Gaussian pulse psi = A exp(-|x-c|^2 / w^2), Pi = 0, Phi = grad psi;
+ *         params = {A, w, cx, cy, cz} per instance (5 * n_instances values). */
+int dgsw_set_initial_data(DgswHandle h, int kind, const double* params,
+                          double t);
+
+/* ---- TimeDerivative / BoundaryCorrection ---------------------------------
+ * dgsw_rhs: the full semi-discrete DG time derivative du/dt of the state u:
+ * volume terms (partial_derivatives + TimeDerivative::apply) plus the
+ * UpwindPenalty correction of every mortar lifted onto the GLL faces
+ * (ComputeTimeDerivative.hpp:388-650 + ApplyBoundaryCorrections.hpp:723-1050).
+ * The handle's precision selects FP64 or mixed arithmetic. */
+int dgsw_rhs(DgswHandle h, const double* host_u, double* host_dudt);
+int dgsw_rhs_device(DgswHandle h, const double* dev_u, double* dev_dudt);
+/* Volume terms only (TimeDerivative::apply after partial_derivatives). */
+int dgsw_volume_rhs_device(DgswHandle h, const double* dev_u, double* dev_dudt);
+
+/* UpwindPenalty<3>::dg_package_data (UpwindPenalty.cpp:35-108) on npts face
+ * points, device pointers, component-major.  packaged: 16*npts doubles in
+ * dg_package_field_tags order (VPsi, VZero[3], VPlus, VMinus,
+ * NormalTimesVPlus[3], NormalTimesVMinus[3], Gamma2VPsi, CharSpeeds[3]).
+ * normal_dot_mesh_velocity may be NULL.  stream: a cudaStream_t or NULL. */
+int dgsw_package_data_device(int64_t npts, const double* psi, const double* pi,
+                             const double* phi, const double* gamma2,
+                             const double* normal,
+                             const double* normal_dot_mesh_velocity,
+                             double* packaged, void* stream);
+/* UpwindPenalty<3>::dg_boundary_terms (UpwindPenalty.cpp:110-205):
+ * out = 5*npts (Psi, Pi, Phi_x, Phi_y, Phi_z corrections). */
+int dgsw_boundary_terms_device(int64_t npts, const double* packaged_int,
+                               const double* packaged_ext, double* out,
+                               void* stream);
+
+/* ---- TimeStepper (Rk3HesthavenSsp) ---------------------------------------
+ * dgsw_step: n_steps full SSP-RK3 steps of size dt on the handle's state, each
+ * step one fused launch per substep, replayed from a CUDA graph.
+ * dgsw_substep: substep k (0, 1, 2) of the step that starts from the state
+ * saved by the last dgsw_substep(k=0); for stepping parity with
+ * TimeStepper::update_u one substep at a time. */
+int dgsw_step(DgswHandle h, int n_steps, double dt);
+int dgsw_substep(DgswHandle h, int k, double dt);
+
+/* ---- host-only setup (no GPU) ---------------------------------------------
+ * Spectral::collocation_points / quadrature_weights <Legendre, GaussLobatto>
+ * (NumericalAlgorithms/Spectral/Legendre.cpp:186-239) */
+int dgsw_lgl_points_weights(int n, double* x, double* w);
+/* Spectral::differentiation_matrix, row-major D[i*n+j]
+ * (NumericalAlgorithms/Spectral/Spectral.cpp:113-447) */
+int dgsw_differentiation_matrix(int n, double* D);
+/* Spectral::projection_matrix_parent_to_child (face -> mortar, nm x ne) and
+ * projection_matrix_child_to_parent (mortar -> face, ne x nm), ChildSize::Full
+ * (NumericalAlgorithms/Spectral/Projection.cpp:56-375) */
+int dgsw_mortar_projections(int ne, int nm, double* face_to_mortar,
+                            double* mortar_to_face);
+/* Element / neighbour index maps of a configuration (Domain/Structure):
+ * element_ids: packed ElementId<3> bits (ElementId.hpp:138-147), n_elements;
+ * neighbors: 6 per element in Direction<3>::all_directions() order
+ *            (Direction.hpp:186-193), global element index;
+ * mortar_points: 6 per element, mortar_mesh extent (MortarHelpers.cpp:21-47);
+ * Any output may be NULL.  Returns DGSW_ERR_UNSUPPORTED when a block id does
+ * not fit the reference's 8 block-id bits (the other outputs are still set). */
+int dgsw_index_maps(const DgswConfig* config, uint64_t* element_ids,
+                    int32_t* neighbors, int32_t* mortar_points);
+int dgsw_count_elements(const DgswConfig* config, int64_t* n_elements,
+                        int64_t* state_doubles);
+
+#ifdef __cplusplus
+}
+#endif
+#endif /* DGSW_H */

@@ -1,0 +1,849 @@
+// dgsw_oracle.cpp -- CPU FP64 restatement of the reference DG scalar-wave step.
+//
+// Test infrastructure: the checker for the CUDA path, never part of it.
+// Each function names the reference file:line it restates (paths relative to
+// the SpECTRE source tree).  Compiled with -ffp-contract=off so that every
+// product and sum is rounded separately, as in the reference's scalar code.
+#include "dgsw_oracle.h"
+
+#include <algorithm>
+#include <cmath>
+#include <cstdlib>
+#include <cstring>
+#include <limits>
+#include <vector>
+
+#ifdef _OPENMP
+#include <omp.h>
+#endif
+
+namespace {
+
+constexpr int kMaxN = 20;  // Spectral::maximum_number_of_points<Legendre>
+constexpr int kVars = 5;   // Psi, Pi, Phi_x, Phi_y, Phi_z
+constexpr int kPkg = 16;   // UpwindPenalty packaged doubles per face point
+
+// EvaluateQandL, Legendre.cpp:160-184 (Kopriva algorithm 24 with errata).
+void eval_q_and_l(int poly_degree, double x, double* q, double* L) {
+  double lm2 = 1.0, lm1 = x, ln = 0.0;
+  for (int k = 2; k <= poly_degree; ++k) {
+    ln = ((2. * k - 1.) * x * lm1 - (k - 1.) * lm2) / k;
+    lm2 = lm1;
+    lm1 = ln;
+  }
+  const int k = poly_degree + 1;
+  const double lnp1 = ((2. * k - 1.) * x * ln - (k - 1.) * lm2) / k;
+  *q = lnp1 - lm2;
+  *L = ln;
+}
+
+// Root of q on a sign-changing bracket.  The reference uses TOMS748 with a
+// relative tolerance of 6e-16 (Legendre.cpp:218-226); plain bisection to
+// adjacent doubles lands on the same root of the computed q.
+double lgl_root(int poly_degree, double a, double b) {
+  double qa, qb, L;
+  eval_q_and_l(poly_degree, a, &qa, &L);
+  eval_q_and_l(poly_degree, b, &qb, &L);
+  if (qa == 0.0) return a;
+  if (qb == 0.0) return b;
+  for (int it = 0; it < 200; ++it) {
+    const double m = 0.5 * (a + b);
+    if (m <= std::min(a, b) || m >= std::max(a, b)) break;
+    double qm;
+    eval_q_and_l(poly_degree, m, &qm, &L);
+    if (qm == 0.0) return m;
+    if ((qm < 0) == (qa < 0)) {
+      a = m;
+      qa = qm;
+    } else {
+      b = m;
+    }
+  }
+  return 0.5 * (a + b);
+}
+
+// compute_basis_function_value_impl for Legendre: P_k(x) by recurrence.
+double legendre_p(int k, double x) {
+  if (k == 0) return 1.0;
+  double pm2 = 1.0, pm1 = x;
+  for (int j = 2; j <= k; ++j) {
+    const double p = ((2. * j - 1.) * x * pm1 - (j - 1.) * pm2) / j;
+    pm2 = pm1;
+    pm1 = p;
+  }
+  return pm1;
+}
+
+// Utilities/EqualWithinRoundoff.hpp: |a-b| <= eps*max(|a|,|b|,scale),
+// eps = 100 * machine epsilon, scale = 1.
+bool equal_within_roundoff(double a, double b) {
+  const double eps = std::numeric_limits<double>::epsilon() * 100.0;
+  return std::abs(a - b) <=
+         eps * std::max(std::max(std::abs(a), std::abs(b)), 1.0);
+}
+
+struct Spectral1d {
+  int n = 0;
+  double x[kMaxN], w[kMaxN], bw[kMaxN];
+  double D[kMaxN * kMaxN];
+};
+
+const Spectral1d& spectral(int n) {
+  static Spectral1d table[kMaxN + 1];
+  static bool init = [] {
+    for (int m = 2; m <= kMaxN; ++m) {
+      Spectral1d& s = table[m];
+      s.n = m;
+      orc_lgl(m, s.x, s.w);
+      orc_barycentric_weights(m, s.bw);
+      orc_diff_matrix(m, s.D);
+    }
+    return true;
+  }();
+  (void)init;
+  return table[n];
+}
+
+// Decomposition of an element count into b blocks of refinement L (b odd).
+void split_count(int n, int* blocks, int* level) {
+  int L = 0;
+  while ((n % 2) == 0) {
+    n /= 2;
+    ++L;
+  }
+  *blocks = n;
+  *level = L;
+}
+
+struct InstLayout {
+  int b[3], L[3];
+  int64_t base;   // first global element index
+  int64_t count;  // elements in this instance
+};
+
+std::vector<InstLayout> layouts(int n_inst, const OrcBrick* br) {
+  std::vector<InstLayout> out(n_inst);
+  int64_t base = 0;
+  for (int i = 0; i < n_inst; ++i) {
+    for (int d = 0; d < 3; ++d) split_count(br[i].n[d], &out[i].b[d], &out[i].L[d]);
+    out[i].base = base;
+    out[i].count = (int64_t)br[i].n[0] * br[i].n[1] * br[i].n[2];
+    base += out[i].count;
+  }
+  return out;
+}
+
+// Global element index of lattice point (ix, iy, iz) of an instance:
+// blocks x fastest (DomainHelpers.cpp:1187-1201), then elements of a block in
+// x-outer / z-inner order (InitialElementIds.cpp:50-66).
+int64_t element_index(const InstLayout& lay, const int ijk[3]) {
+  int blk[3], seg[3];
+  for (int d = 0; d < 3; ++d) {
+    blk[d] = ijk[d] >> lay.L[d];
+    seg[d] = ijk[d] & ((1 << lay.L[d]) - 1);
+  }
+  const int64_t block_id = blk[0] + (int64_t)lay.b[0] * (blk[1] + (int64_t)lay.b[1] * blk[2]);
+  const int64_t per_block = (int64_t)1 << (lay.L[0] + lay.L[1] + lay.L[2]);
+  const int64_t within =
+      ((int64_t)seg[0] << (lay.L[1] + lay.L[2])) + ((int64_t)seg[1] << lay.L[2]) + seg[2];
+  return lay.base + block_id * per_block + within;
+}
+
+void element_lattice(const InstLayout& lay, int64_t local, int ijk[3], int* block_id,
+                     int seg[3]) {
+  const int64_t per_block = (int64_t)1 << (lay.L[0] + lay.L[1] + lay.L[2]);
+  const int64_t bid = local / per_block;
+  int64_t within = local % per_block;
+  seg[2] = (int)(within & ((1 << lay.L[2]) - 1));
+  within >>= lay.L[2];
+  seg[1] = (int)(within & ((1 << lay.L[1]) - 1));
+  within >>= lay.L[1];
+  seg[0] = (int)within;
+  int blk[3];
+  blk[0] = (int)(bid % lay.b[0]);
+  blk[1] = (int)((bid / lay.b[0]) % lay.b[1]);
+  blk[2] = (int)(bid / ((int64_t)lay.b[0] * lay.b[1]));
+  for (int d = 0; d < 3; ++d) ijk[d] = (blk[d] << lay.L[d]) + seg[d];
+  *block_id = (int)bid;
+}
+
+struct ElemGeom {
+  int inst;
+  int ijk[3];
+  double lo[3];     // lower corner
+  double h[3];      // widths
+  double invjac[3]; // d xi^d / d x^d (diagonal; off-diagonal entries are 0)
+};
+
+struct Mesh {
+  int n_inst;
+  const OrcBrick* br;
+  std::vector<InstLayout> lay;
+  std::vector<ElemGeom> geom;
+  std::vector<int32_t> nbr;  // 6 per element
+  std::vector<int64_t> off;
+  const int32_t* elem_n;
+  int64_t n_elem;
+};
+
+void build_mesh(Mesh* m, int n_inst, const OrcBrick* br, const int32_t* elem_n) {
+  m->n_inst = n_inst;
+  m->br = br;
+  m->lay = layouts(n_inst, br);
+  m->n_elem = orc_num_elements(n_inst, br);
+  m->elem_n = elem_n;
+  m->geom.resize(m->n_elem);
+  m->nbr.resize(6 * m->n_elem);
+  m->off.resize(m->n_elem + 1);
+  orc_offsets(m->n_elem, elem_n, m->off.data());
+  for (int i = 0; i < n_inst; ++i) {
+    const InstLayout& lay = m->lay[i];
+    for (int64_t l = 0; l < lay.count; ++l) {
+      int ijk[3], bid, seg[3];
+      element_lattice(lay, l, ijk, &bid, seg);
+      const int64_t e = lay.base + l;
+      ElemGeom& g = m->geom[e];
+      g.inst = i;
+      for (int d = 0; d < 3; ++d) {
+        g.ijk[d] = ijk[d];
+        g.h[d] = (br[i].hi[d] - br[i].lo[d]) / br[i].n[d];
+        g.lo[d] = br[i].lo[d] + g.h[d] * ijk[d];
+        g.invjac[d] = 2.0 / g.h[d];
+      }
+      for (int dir = 0; dir < 6; ++dir) {
+        const int d = dir / 2;
+        int q[3] = {ijk[0], ijk[1], ijk[2]};
+        q[d] = (dir % 2) ? (q[d] + 1) % br[i].n[d] : (q[d] + br[i].n[d] - 1) % br[i].n[d];
+        m->nbr[6 * e + dir] = (int32_t)element_index(lay, q);
+      }
+    }
+  }
+}
+
+// Face slice of a volume field: ProjectToBoundary.hpp:114-146 for GLL (the
+// face is a slice of volume points).  Face point index = a + n*b over the two
+// remaining dimensions in ascending order.
+inline int64_t volume_index(int n, int d, int slice, int a, int b) {
+  switch (d) {
+    case 0: return slice + (int64_t)n * (a + (int64_t)n * b);
+    case 1: return a + (int64_t)n * (slice + (int64_t)n * b);
+    default: return a + (int64_t)n * (b + (int64_t)n * slice);
+  }
+}
+
+// apply_matrices on a 2D face: out(i', j') = sum_i sum_j M(i',i) M(j',j) in(i,j),
+// first index fastest; M is rows x cols row-major.
+void apply_face_matrix(int rows, int cols, const double* M, int nfields,
+                       const double* in, double* out) {
+  std::vector<double> tmp((size_t)rows * cols);
+  for (int f = 0; f < nfields; ++f) {
+    const double* src = in + (size_t)f * cols * cols;
+    double* dst = out + (size_t)f * rows * rows;
+    for (int b = 0; b < cols; ++b)
+      for (int ip = 0; ip < rows; ++ip) {
+        double s = 0.0;
+        for (int i = 0; i < cols; ++i) s += M[ip * cols + i] * src[i + cols * b];
+        tmp[ip + (size_t)rows * b] = s;
+      }
+    for (int bp = 0; bp < rows; ++bp)
+      for (int ip = 0; ip < rows; ++ip) {
+        double s = 0.0;
+        for (int b = 0; b < cols; ++b) s += M[bp * cols + b] * tmp[ip + (size_t)rows * b];
+        dst[ip + (size_t)rows * bp] = s;
+      }
+  }
+}
+
+// Package one face of element e in direction dir: InternalMortarDataImpl.hpp
+// :177-221 (normal = sign * inverse-Jacobian row, normalised as in
+// NormalCovectorAndMagnitude.hpp:84-98) then UpwindPenalty::dg_package_data.
+void package_face(const Mesh& m, const double* u, double gamma2, int64_t e, int dir,
+                  double* pkg, double* magnitude) {
+  const int n = m.elem_n[e];
+  const int64_t np = (int64_t)n * n * n;
+  const int d = dir / 2;
+  const bool upper = dir % 2;
+  const int slice = upper ? n - 1 : 0;
+  const int nf = n * n;
+  const double* ue = u + m.off[e];
+  std::vector<double> psi(nf), pi(nf), phi(3 * nf), g2(nf, gamma2), nrm(3 * nf);
+  const double sign = upper ? 1.0 : -1.0;
+  for (int b = 0; b < n; ++b)
+    for (int a = 0; a < n; ++a) {
+      const int f = a + n * b;
+      const int64_t v = volume_index(n, d, slice, a, b);
+      psi[f] = ue[v];
+      pi[f] = ue[np + v];
+      for (int i = 0; i < 3; ++i) phi[i * nf + f] = ue[(2 + i) * np + v];
+      double un[3];
+      for (int i = 0; i < 3; ++i) un[i] = sign * (i == d ? m.geom[e].invjac[d] : 0.0);
+      const double mag = std::sqrt(un[0] * un[0] + un[1] * un[1] + un[2] * un[2]);
+      const double inv = 1.0 / mag;
+      for (int i = 0; i < 3; ++i) nrm[i * nf + f] = un[i] * inv;
+      magnitude[f] = mag;
+    }
+  double ms;
+  orc_package(nf, psi.data(), pi.data(), phi.data(), g2.data(), nrm.data(), nullptr, pkg, &ms);
+}
+
+void volume_terms(const Mesh& m, const double* u, double gamma2, int64_t e, double* dt) {
+  const int n = m.elem_n[e];
+  const int64_t np = (int64_t)n * n * n;
+  const Spectral1d& sp = spectral(n);
+  const double* ue = u + m.off[e];
+  // logical derivatives of all 5 vars (PartialDerivatives.tpp:315-363)
+  std::vector<double> dl((size_t)3 * kVars * np);
+  for (int v = 0; v < kVars; ++v) {
+    const double* f = ue + v * np;
+    for (int a = 0; a < 3; ++a) {
+      double* out = dl.data() + ((size_t)a * kVars + v) * np;
+      for (int k = 0; k < n; ++k)
+        for (int j = 0; j < n; ++j)
+          for (int i = 0; i < n; ++i) {
+            const int idx[3] = {i, j, k};
+            double s = 0.0;
+            for (int q = 0; q < n; ++q) {
+              int id2[3] = {i, j, k};
+              id2[a] = q;
+              s += sp.D[idx[a] * n + q] * f[id2[0] + n * (id2[1] + n * id2[2])];
+            }
+            out[i + n * (j + n * k)] = s;
+          }
+    }
+  }
+  // du_i = sum_a invjac(a, i) * d_a u, a = 0 first (PartialDerivatives.tpp:82-105)
+  const ElemGeom& g = m.geom[e];
+  auto ij = [&](int a, int i) { return a == i ? g.invjac[a] : 0.0; };
+  std::vector<double> du((size_t)3 * kVars * np);  // [v][i][pt]
+  for (int v = 0; v < kVars; ++v)
+    for (int i = 0; i < 3; ++i) {
+      double* out = du.data() + ((size_t)v * 3 + i) * np;
+      const double* l0 = dl.data() + ((size_t)0 * kVars + v) * np;
+      const double* l1 = dl.data() + ((size_t)1 * kVars + v) * np;
+      const double* l2 = dl.data() + ((size_t)2 * kVars + v) * np;
+      for (int64_t p = 0; p < np; ++p) {
+        double s = ij(0, i) * l0[p];
+        s += ij(1, i) * l1[p];
+        s += ij(2, i) * l2[p];
+        out[p] = s;
+      }
+    }
+  // ScalarWave::TimeDerivative<3>::apply, TimeDerivative.cpp:37-44
+  const double* pi = ue + np;
+  for (int64_t p = 0; p < np; ++p) {
+    auto dpsi = [&](int i) { return du[((size_t)0 * 3 + i) * np + p]; };
+    auto dpi = [&](int i) { return du[((size_t)1 * 3 + i) * np + p]; };
+    auto dphi = [&](int i, int j) { return du[((size_t)(2 + j) * 3 + i) * np + p]; };
+    dt[p] = -pi[p];
+    double s = -dphi(0, 0);
+    s -= dphi(1, 1);
+    s -= dphi(2, 2);
+    dt[np + p] = s;
+    for (int dd = 0; dd < 3; ++dd)
+      dt[(2 + dd) * np + p] = -dpi(dd) + gamma2 * (dpsi(dd) - ue[(2 + dd) * np + p]);
+  }
+}
+
+// ApplyBoundaryCorrections.hpp:723-1050 for GLL global time stepping: per
+// mortar, dg_boundary_terms, project from mortar if needed, lift_flux, then
+// add_slice_to_data.
+void boundary_terms(const Mesh& m, const double* u, double gamma2, int64_t e, double* dt) {
+  const int n = m.elem_n[e];
+  const int64_t np = (int64_t)n * n * n;
+  for (int dir = 0; dir < 6; ++dir) {
+    const int d = dir / 2;
+    const bool upper = dir % 2;
+    const int64_t nb = m.nbr[6 * e + dir];
+    const int nn = m.elem_n[nb];
+    const int nm = std::max(n, nn);  // mortar_mesh, MortarHelpers.cpp:41
+    std::vector<double> pkg_i((size_t)kPkg * n * n), pkg_e((size_t)kPkg * nn * nn);
+    std::vector<double> mag_i(n * n), mag_e(nn * nn);
+    package_face(m, u, gamma2, e, dir, pkg_i.data(), mag_i.data());
+    package_face(m, u, gamma2, nb, dir ^ 1, pkg_e.data(), mag_e.data());
+    std::vector<double> mi((size_t)kPkg * nm * nm), me((size_t)kPkg * nm * nm);
+    if (nm != n) {
+      std::vector<double> P((size_t)nm * n);
+      orc_proj_face_to_mortar(n, nm, P.data());
+      apply_face_matrix(nm, n, P.data(), kPkg, pkg_i.data(), mi.data());
+    } else {
+      mi = pkg_i;
+    }
+    if (nm != nn) {
+      std::vector<double> P((size_t)nm * nn);
+      orc_proj_face_to_mortar(nn, nm, P.data());
+      apply_face_matrix(nm, nn, P.data(), kPkg, pkg_e.data(), me.data());
+    } else {
+      me = pkg_e;
+    }
+    std::vector<double> bc_m((size_t)kVars * nm * nm), bc((size_t)kVars * n * n);
+    orc_boundary_terms(nm * nm, mi.data(), me.data(), bc_m.data());
+    if (nm != n) {
+      std::vector<double> P((size_t)n * nm);
+      orc_proj_mortar_to_face(n, nm, P.data());
+      apply_face_matrix(n, nm, P.data(), kVars, bc_m.data(), bc.data());
+    } else {
+      bc = bc_m;
+    }
+    // lift_flux, LiftFlux.hpp:57-61
+    const int nf = n * n;
+    const double slice_factor = -0.5 * static_cast<double>(n * (n - 1));
+    const int slice = upper ? n - 1 : 0;
+    for (int b = 0; b < n; ++b)
+      for (int a = 0; a < n; ++a) {
+        const int f = a + n * b;
+        const int64_t vi = volume_index(n, d, slice, a, b);
+        const double fac = slice_factor * mag_i[f];
+        for (int v = 0; v < kVars; ++v) dt[v * np + vi] += bc[(size_t)v * nf + f] * fac;
+      }
+  }
+}
+
+}  // namespace
+
+extern "C" {
+
+int orc_lgl(int n, double* x, double* w) {
+  // Legendre.cpp:186-239 (Kopriva algorithm 25)
+  if (n < 2 || n > kMaxN || !x || !w) return -1;
+  const int p = n - 1;
+  if (p == 1) {
+    x[0] = -1.;
+    x[1] = 1.;
+    w[0] = w[1] = 1.;
+    return 0;
+  }
+  x[0] = -1.;
+  x[p] = 1.;
+  w[0] = w[p] = 2. / (p * (p + 1.));
+  for (int j = 1; j < (p + 1) / 2; ++j) {
+    const double a = -std::cos((j - 0.25) * M_PI / p - 0.375 / (p * M_PI * (j - 0.25)));
+    const double b = -std::cos((j + 0.75) * M_PI / p - 0.375 / (p * M_PI * (j + 0.75)));
+    const double r = lgl_root(p, a, b);
+    double q, L;
+    eval_q_and_l(p, r, &q, &L);
+    x[j] = r;
+    x[p - j] = -r;
+    w[j] = w[p - j] = 2. / (p * (p + 1.) * (L * L));
+  }
+  if (p % 2 == 0) {
+    double q, L;
+    eval_q_and_l(p, 0., &q, &L);
+    x[p / 2] = 0.;
+    w[p / 2] = 2. / (p * (p + 1.) * (L * L));
+  }
+  return 0;
+}
+
+int orc_barycentric_weights(int n, double* bw) {
+  // Spectral.cpp:84-101 (Kopriva algorithm 30)
+  if (n < 2 || n > kMaxN || !bw) return -1;
+  double x[kMaxN], w[kMaxN];
+  orc_lgl(n, x, w);
+  for (int j = 0; j < n; ++j) bw[j] = 1.;
+  for (int j = 1; j < n; ++j)
+    for (int k = 0; k < j; ++k) {
+      bw[k] *= x[k] - x[j];
+      bw[j] *= x[j] - x[k];
+    }
+  for (int j = 0; j < n; ++j) bw[j] = 1. / bw[j];
+  return 0;
+}
+
+int orc_diff_matrix(int n, double* D) {
+  // Spectral.cpp:431-444 (Kopriva algorithm 37, negative-sum diagonal)
+  if (n < 2 || n > kMaxN || !D) return -1;
+  double x[kMaxN], w[kMaxN], bw[kMaxN];
+  orc_lgl(n, x, w);
+  orc_barycentric_weights(n, bw);
+  for (int i = 0; i < n; ++i) {
+    double diag = 0.0;
+    for (int j = 0; j < n; ++j) {
+      if (i != j) {
+        D[i * n + j] = bw[j] / (bw[i] * (x[i] - x[j]));
+        diag -= D[i * n + j];
+      }
+    }
+    D[i * n + i] = diag;
+  }
+  return 0;
+}
+
+int orc_vandermonde(int n, double* V) {
+  // ModalToNodalMatrixGenerator, Spectral.cpp:499-516
+  if (n < 2 || n > kMaxN || !V) return -1;
+  double x[kMaxN], w[kMaxN];
+  orc_lgl(n, x, w);
+  for (int i = 0; i < n; ++i)
+    for (int k = 0; k < n; ++k) V[i * n + k] = legendre_p(k, x[i]);
+  return 0;
+}
+
+int orc_inv_vandermonde(int n, double* Vinv) {
+  // NodalToModalMatrixGenerator, Spectral.cpp:518-523: numerical inverse
+  // (LU with partial pivoting, as LAPACK's getrf/getri behind blaze::inv).
+  if (n < 2 || n > kMaxN || !Vinv) return -1;
+  double A[kMaxN * kMaxN];
+  orc_vandermonde(n, A);
+  double B[kMaxN * kMaxN];
+  for (int i = 0; i < n; ++i)
+    for (int j = 0; j < n; ++j) B[i * n + j] = (i == j) ? 1.0 : 0.0;
+  for (int c = 0; c < n; ++c) {
+    int piv = c;
+    for (int r = c + 1; r < n; ++r)
+      if (std::abs(A[r * n + c]) > std::abs(A[piv * n + c])) piv = r;
+    if (piv != c)
+      for (int j = 0; j < n; ++j) {
+        std::swap(A[c * n + j], A[piv * n + j]);
+        std::swap(B[c * n + j], B[piv * n + j]);
+      }
+    const double inv = 1.0 / A[c * n + c];
+    for (int r = 0; r < n; ++r) {
+      if (r == c) continue;
+      const double f = A[r * n + c] * inv;
+      if (f == 0.0) continue;
+      for (int j = 0; j < n; ++j) {
+        A[r * n + j] -= f * A[c * n + j];
+        B[r * n + j] -= f * B[c * n + j];
+      }
+    }
+  }
+  for (int r = 0; r < n; ++r) {
+    const double inv = 1.0 / A[r * n + r];
+    for (int j = 0; j < n; ++j) Vinv[r * n + j] = B[r * n + j] * inv;
+  }
+  return 0;
+}
+
+int orc_interp_matrix(int n, int m, const double* t, double* M) {
+  // Spectral.cpp:625-670 (Kopriva algorithm 32)
+  if (n < 2 || n > kMaxN || m < 0 || !M || (m > 0 && !t)) return -1;
+  const Spectral1d& s = spectral(n);
+  for (int k = 0; k < m; ++k) {
+    bool match = false;
+    for (int j = 0; j < n; ++j) {
+      M[k * n + j] = 0.0;
+      if (equal_within_roundoff(t[k], s.x[j])) {
+        M[k * n + j] = 1.0;
+        match = true;
+      }
+    }
+    if (!match) {
+      double sum = 0.0;
+      for (int j = 0; j < n; ++j) {
+        M[k * n + j] = s.bw[j] / (t[k] - s.x[j]);
+        sum += M[k * n + j];
+      }
+      for (int j = 0; j < n; ++j) M[k * n + j] /= sum;
+    }
+  }
+  return 0;
+}
+
+int orc_proj_face_to_mortar(int ne, int nm, double* P) {
+  // projection_matrix_parent_to_child, ChildSize::Full: interpolation of the
+  // element's face polynomial to the mortar points (Projection.cpp:310-330)
+  if (ne < 2 || nm < ne || nm > kMaxN || !P) return -1;
+  const Spectral1d& sm = spectral(nm);
+  return orc_interp_matrix(ne, nm, sm.x, P);
+}
+
+int orc_proj_mortar_to_face(int ne, int nm, double* P) {
+  // projection_matrix_child_to_parent, ChildSize::Full, not massive:
+  // truncation of the mortar's Legendre modes (Projection.cpp:97-130)
+  if (ne < 2 || nm < ne || nm > kMaxN || !P) return -1;
+  double Ve[kMaxN * kMaxN], Vm_inv[kMaxN * kMaxN];
+  orc_vandermonde(ne, Ve);
+  orc_inv_vandermonde(nm, Vm_inv);
+  for (int i = 0; i < ne; ++i)
+    for (int j = 0; j < nm; ++j) {
+      double s = 0.;
+      for (int k = 0; k < ne; ++k) s += Ve[i * ne + k] * Vm_inv[k * nm + j];
+      P[i * nm + j] = s;
+    }
+  return 0;
+}
+
+int64_t orc_num_elements(int n_inst, const OrcBrick* br) {
+  int64_t c = 0;
+  for (int i = 0; i < n_inst; ++i) c += (int64_t)br[i].n[0] * br[i].n[1] * br[i].n[2];
+  return c;
+}
+
+int orc_index_maps(int n_inst, const OrcBrick* br, uint64_t* elem_id, int32_t* nbr,
+                   int32_t* ijk_out, int32_t* inst) {
+  if (n_inst < 1 || !br) return -1;
+  for (int i = 0; i < n_inst; ++i)
+    for (int d = 0; d < 3; ++d)
+      if (br[i].n[d] < 1) return -1;
+  std::vector<InstLayout> lay = layouts(n_inst, br);
+  int rc = 0;
+  for (int i = 0; i < n_inst; ++i) {
+    for (int64_t l = 0; l < lay[i].count; ++l) {
+      int ijk[3], bid, seg[3];
+      element_lattice(lay[i], l, ijk, &bid, seg);
+      const int64_t e = lay[i].base + l;
+      if (bid >= 256) rc = -2;  // not representable in the 8 block-id bits
+      if (elem_id) {
+        // ElementId.hpp:138-147 bit fields, least significant first
+        uint64_t id = (uint64_t)(bid & 0xff);
+        id |= (uint64_t)0 << 8;   // grid index
+        id |= (uint64_t)0 << 12;  // direction
+        id |= (uint64_t)seg[0] << 16;
+        id |= (uint64_t)lay[i].L[0] << 28;
+        id |= (uint64_t)seg[1] << 32;
+        id |= (uint64_t)lay[i].L[1] << 44;
+        id |= (uint64_t)seg[2] << 48;
+        id |= (uint64_t)lay[i].L[2] << 60;
+        elem_id[e] = id;
+      }
+      if (ijk_out)
+        for (int d = 0; d < 3; ++d) ijk_out[3 * e + d] = ijk[d];
+      if (inst) inst[e] = i;
+      if (nbr)
+        for (int dir = 0; dir < 6; ++dir) {
+          const int d = dir / 2;
+          int q[3] = {ijk[0], ijk[1], ijk[2]};
+          q[d] = (dir % 2) ? (q[d] + 1) % br[i].n[d] : (q[d] + br[i].n[d] - 1) % br[i].n[d];
+          nbr[6 * e + dir] = (int32_t)element_index(lay[i], q);
+        }
+    }
+  }
+  return rc;
+}
+
+int orc_offsets(int64_t n_elem, const int32_t* elem_n, int64_t* off) {
+  if (n_elem < 0 || !elem_n || !off) return -1;
+  off[0] = 0;
+  for (int64_t e = 0; e < n_elem; ++e) {
+    const int64_t n = elem_n[e];
+    off[e + 1] = off[e] + kVars * n * n * n;
+  }
+  return 0;
+}
+
+int orc_coords(int n_inst, const OrcBrick* br, const int32_t* elem_n, double* xyz) {
+  if (n_inst < 1 || !br || !elem_n || !xyz) return -1;
+  Mesh m;
+  build_mesh(&m, n_inst, br, elem_n);
+  int64_t pos = 0;
+  for (int64_t e = 0; e < m.n_elem; ++e) {
+    const int n = elem_n[e];
+    const int64_t np = (int64_t)n * n * n;
+    const Spectral1d& s = spectral(n);
+    const ElemGeom& g = m.geom[e];
+    for (int k = 0; k < n; ++k)
+      for (int j = 0; j < n; ++j)
+        for (int i = 0; i < n; ++i) {
+          const int64_t p = i + n * (j + (int64_t)n * k);
+          const int id[3] = {i, j, k};
+          for (int d = 0; d < 3; ++d)
+            xyz[pos + d * np + p] = g.lo[d] + (s.x[id[d]] + 1.0) * (0.5 * g.h[d]);
+        }
+    pos += 3 * np;
+  }
+  return 0;
+}
+
+int orc_initial_data(int n_inst, const OrcBrick* br, const int32_t* elem_n, int kind,
+                     const double* params, double t, double* u) {
+  if (n_inst < 1 || !br || !elem_n || !params || !u) return -1;
+  Mesh m;
+  build_mesh(&m, n_inst, br, elem_n);
+  for (int64_t e = 0; e < m.n_elem; ++e) {
+    const int n = elem_n[e];
+    const int64_t np = (int64_t)n * n * n;
+    const Spectral1d& s = spectral(n);
+    const ElemGeom& g = m.geom[e];
+    double* ue = u + m.off[e];
+    for (int k = 0; k < n; ++k)
+      for (int j = 0; j < n; ++j)
+        for (int i = 0; i < n; ++i) {
+          const int64_t p = i + n * (j + (int64_t)n * k);
+          const int id[3] = {i, j, k};
+          double x[3];
+          for (int d = 0; d < 3; ++d) x[d] = g.lo[d] + (s.x[id[d]] + 1.0) * (0.5 * g.h[d]);
+          if (kind == 0) {
+            // PlaneWave.cpp:56-80: psi = f(k.x - omega t), Pi = -dpsi/dt
+            const double* kv = params;
+            const double omega = std::sqrt(kv[0] * kv[0] + kv[1] * kv[1] + kv[2] * kv[2]);
+            const double ph = kv[0] * x[0] + kv[1] * x[1] + kv[2] * x[2] - omega * t;
+            ue[p] = std::sin(ph);
+            ue[np + p] = omega * std::cos(ph);
+            for (int d = 0; d < 3; ++d) ue[(2 + d) * np + p] = kv[d] * std::cos(ph);
+          } else if (kind == 1) {
+            const double* q = params + 5 * g.inst;
+            const double A = q[0], w = q[1];
+            double r2 = 0.0, dx[3];
+            for (int d = 0; d < 3; ++d) {
+              dx[d] = x[d] - q[2 + d];
+              r2 += dx[d] * dx[d];
+            }
+            const double psi = A * std::exp(-r2 / (w * w));
+            ue[p] = psi;
+            ue[np + p] = 0.0;
+            for (int d = 0; d < 3; ++d) ue[(2 + d) * np + p] = -2.0 * dx[d] / (w * w) * psi;
+          } else {
+            return -1;
+          }
+        }
+  }
+  return 0;
+}
+
+int orc_package(int npts, const double* psi, const double* pi, const double* phi,
+                const double* gamma2, const double* normal, const double* ndotv,
+                double* pkg, double* max_speed) {
+  // UpwindPenalty<3>::dg_package_data, UpwindPenalty.cpp:35-108
+  if (npts < 0 || !psi || !pi || !phi || !gamma2 || !normal || !pkg) return -1;
+  const int n = npts;
+  double* v_psi = pkg;
+  double* v_zero = pkg + n;
+  double* v_plus = pkg + 4 * n;
+  double* v_minus = pkg + 5 * n;
+  double* n_v_plus = pkg + 6 * n;
+  double* n_v_minus = pkg + 9 * n;
+  double* g2_v_psi = pkg + 12 * n;
+  double* speeds = pkg + 13 * n;
+  double mx = -std::numeric_limits<double>::infinity();
+  for (int p = 0; p < n; ++p) {
+    double c0, c1, c2;
+    if (ndotv) {
+      c0 = -ndotv[p];
+      c1 = 1.0 - ndotv[p];
+      c2 = -1.0 - ndotv[p];
+    } else {
+      c0 = 0.0;
+      c1 = 1.0;
+      c2 = -1.0;
+    }
+    speeds[p] = c0;
+    speeds[n + p] = c1;
+    speeds[2 * n + p] = c2;
+    const double g2psi = gamma2[p] * psi[p];
+    // dot_product(normal, phi): n_0 phi_0 + n_1 phi_1 + n_2 phi_2
+    double ndp = normal[p] * phi[p];
+    ndp += normal[n + p] * phi[n + p];
+    ndp += normal[2 * n + p] * phi[2 * n + p];
+    for (int i = 0; i < 3; ++i)
+      v_zero[i * n + p] = c0 * (phi[i * n + p] - normal[i * n + p] * ndp);
+    v_plus[p] = c1 * (pi[p] + ndp - g2psi);
+    v_minus[p] = c2 * (pi[p] - ndp - g2psi);
+    for (int i = 0; i < 3; ++i) {
+      n_v_plus[i * n + p] = v_plus[p] * normal[i * n + p];
+      n_v_minus[i * n + p] = v_minus[p] * normal[i * n + p];
+    }
+    v_psi[p] = c0 * psi[p];
+    g2_v_psi[p] = g2psi * c0;
+    mx = std::max(mx, std::max(c0, std::max(c1, c2)));
+  }
+  if (max_speed) *max_speed = mx;
+  return 0;
+}
+
+int orc_boundary_terms(int npts, const double* pi_, const double* pe, double* out) {
+  // UpwindPenalty<3>::dg_boundary_terms, UpwindPenalty.cpp:110-205, with
+  // step_function(x) = x >= 0 ? 1 : 0 (Utilities/Math.hpp:70-74)
+  if (npts < 0 || !pi_ || !pe || !out) return -1;
+  const int n = npts;
+  auto step = [](double x) { return x >= 0.0 ? 1.0 : 0.0; };
+  for (int p = 0; p < n; ++p) {
+    const double* si = pi_ + 13 * n;
+    const double* se = pe + 13 * n;
+    const double wpsi_i = step(-si[p]);
+    const double wpsi_e = -step(se[p]);
+    const double wzero_i = step(-si[p]);
+    const double wzero_e = -step(se[p]);
+    const double wplus_i = step(-si[n + p]);
+    const double wplus_e = -step(se[n + p]);
+    const double wminus_i = step(-si[2 * n + p]);
+    const double wminus_e = -step(se[2 * n + p]);
+    out[p] = wpsi_e * pe[p] - wpsi_i * pi_[p];
+    out[n + p] = 0.5 * (wplus_e * pe[4 * n + p] + wminus_e * pe[5 * n + p]) +
+                 wpsi_e * pe[12 * n + p] -
+                 0.5 * (wplus_i * pi_[4 * n + p] + wminus_i * pi_[5 * n + p]) -
+                 wpsi_i * pi_[12 * n + p];
+    for (int d = 0; d < 3; ++d)
+      out[(2 + d) * n + p] =
+          0.5 * (wplus_e * pe[(6 + d) * n + p] - wminus_e * pe[(9 + d) * n + p]) +
+          wzero_e * pe[(1 + d) * n + p] -
+          0.5 * (wplus_i * pi_[(6 + d) * n + p] - wminus_i * pi_[(9 + d) * n + p]) -
+          wzero_i * pi_[(1 + d) * n + p];
+  }
+  return 0;
+}
+
+int orc_volume_rhs(int n_inst, const OrcBrick* br, const int32_t* elem_n, double gamma2,
+                   const double* u, double* dudt, int n_threads) {
+  if (n_inst < 1 || !br || !elem_n || !u || !dudt) return -1;
+  Mesh m;
+  build_mesh(&m, n_inst, br, elem_n);
+#ifdef _OPENMP
+  if (n_threads > 0) omp_set_num_threads(n_threads);
+#pragma omp parallel for schedule(dynamic, 4)
+#endif
+  for (int64_t e = 0; e < m.n_elem; ++e) volume_terms(m, u, gamma2, e, dudt + m.off[e]);
+  (void)n_threads;
+  return 0;
+}
+
+int orc_rhs(int n_inst, const OrcBrick* br, const int32_t* elem_n, double gamma2,
+            const double* u, double* dudt, int n_threads) {
+  if (n_inst < 1 || !br || !elem_n || !u || !dudt) return -1;
+  for (int i = 0; i < n_inst; ++i)
+    for (int d = 0; d < 3; ++d)
+      if (br[i].n[d] < 1) return -1;
+  Mesh m;
+  build_mesh(&m, n_inst, br, elem_n);
+  for (int64_t e = 0; e < m.n_elem; ++e)
+    if (elem_n[e] < 2 || elem_n[e] > kMaxN) return -1;
+#ifdef _OPENMP
+  if (n_threads > 0) omp_set_num_threads(n_threads);
+#pragma omp parallel for schedule(dynamic, 4)
+#endif
+  for (int64_t e = 0; e < m.n_elem; ++e) {
+    volume_terms(m, u, gamma2, e, dudt + m.off[e]);
+    boundary_terms(m, u, gamma2, e, dudt + m.off[e]);
+  }
+  (void)n_threads;
+  return 0;
+}
+
+int orc_rk3_substep(int64_t n, int k, double dt, const double* u0, const double* ucur,
+                    const double* du, double* un) {
+  // Rk3HesthavenSsp::update_u_impl, Rk3HesthavenSsp.cpp:63-80
+  if (n < 0 || k < 0 || k > 2 || !u0 || !ucur || !du || !un) return -1;
+  for (int64_t i = 0; i < n; ++i) {
+    if (k == 0) {
+      un[i] = ucur[i] + dt * du[i];
+    } else if (k == 1) {
+      un[i] = 0.25 * (3.0 * u0[i] + ucur[i] + dt * du[i]);
+    } else {
+      un[i] = (1.0 / 3.0) * (u0[i] + 2.0 * ucur[i] + 2.0 * dt * du[i]);
+    }
+  }
+  return 0;
+}
+
+int orc_evolve(int n_inst, const OrcBrick* br, const int32_t* elem_n, double gamma2,
+               double dt, int n_steps, double* u, int n_threads) {
+  if (n_inst < 1 || !br || !elem_n || !u || n_steps < 0) return -1;
+  const int64_t n_elem = orc_num_elements(n_inst, br);
+  std::vector<int64_t> off(n_elem + 1);
+  orc_offsets(n_elem, elem_n, off.data());
+  const int64_t n = off[n_elem];
+  std::vector<double> u0(n), u1(n), du(n);
+  for (int s = 0; s < n_steps; ++s) {
+    std::memcpy(u0.data(), u, n * sizeof(double));
+    int rc = orc_rhs(n_inst, br, elem_n, gamma2, u0.data(), du.data(), n_threads);
+    if (rc) return rc;
+    orc_rk3_substep(n, 0, dt, u0.data(), u0.data(), du.data(), u1.data());
+    orc_rhs(n_inst, br, elem_n, gamma2, u1.data(), du.data(), n_threads);
+    orc_rk3_substep(n, 1, dt, u0.data(), u1.data(), du.data(), u);
+    std::memcpy(u1.data(), u, n * sizeof(double));
+    orc_rhs(n_inst, br, elem_n, gamma2, u1.data(), du.data(), n_threads);
+    orc_rk3_substep(n, 2, dt, u0.data(), u1.data(), du.data(), u);
+  }
+  return 0;
+}
+
+}  // extern "C"

@@ -1,0 +1,117 @@
+/*
+ * dgsw_oracle.h -- CPU FP64 restatement of SpECTRE's DG scalar-wave evolution
+ * step (test infrastructure only).
+ *
+ * This library is the correctness checker for the CUDA path in
+ * spectre_gb300/.  Only tests/, __graft_entry__.smoke() and bench.py's CPU
+ * baseline leg may load it; the product library never links it.
+ *
+ * It follows the reference's own algorithms (file:line relative to the
+ * SpECTRE source tree, release 2024.09.29):
+ *   LGL nodes/weights   src/NumericalAlgorithms/Spectral/Legendre.cpp:160-239
+ *   barycentric weights src/NumericalAlgorithms/Spectral/Spectral.cpp:84-101
+ *   D-matrix            src/NumericalAlgorithms/Spectral/Spectral.cpp:431-444
+ *   Vandermonde         src/NumericalAlgorithms/Spectral/Spectral.cpp:499-523
+ *   interpolation       src/NumericalAlgorithms/Spectral/Spectral.cpp:625-670
+ *   mortar projections  src/NumericalAlgorithms/Spectral/Projection.cpp:56-375
+ *   partial derivatives src/NumericalAlgorithms/LinearOperators/PartialDerivatives.tpp:56-110,315-363
+ *   time derivative     src/Evolution/Systems/ScalarWave/TimeDerivative.cpp:13-45
+ *   UpwindPenalty       src/Evolution/Systems/ScalarWave/BoundaryCorrections/UpwindPenalty.cpp:35-205
+ *   face normals        src/Evolution/DiscontinuousGalerkin/Actions/NormalCovectorAndMagnitude.hpp:48-101
+ *   lift_flux           src/NumericalAlgorithms/DiscontinuousGalerkin/LiftFlux.hpp:41-62
+ *   SSP-RK3             src/Time/TimeSteppers/Rk3HesthavenSsp.cpp:55-81
+ *   ElementId layout    src/Domain/Structure/ElementId.hpp:55-90,138-147
+ *   element ordering    src/Domain/Structure/InitialElementIds.cpp:45-96
+ *   multi-block lattice src/Domain/DomainHelpers.cpp:1187-1201 (blocks x fastest)
+ *   mortar mesh         src/NumericalAlgorithms/DiscontinuousGalerkin/MortarHelpers.cpp:21-47
+ *
+ * All arrays are caller-owned host memory.  Every function returns 0 on
+ * success and a negative code on bad arguments.
+ */
+#ifndef DGSW_ORACLE_H
+#define DGSW_ORACLE_H
+
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+/* ---------------- spectral (a1, a7) ---------------- */
+int orc_lgl(int n, double* x, double* w);
+int orc_barycentric_weights(int n, double* bw);
+/* D[i*n + j] = d l_j / d xi at x_i (row-major) */
+int orc_diff_matrix(int n, double* D);
+/* V[i*n + k] = P_k(x_i) */
+int orc_vandermonde(int n, double* V);
+int orc_inv_vandermonde(int n, double* Vinv);
+/* M[k*n + j]: value at targets[k] of the j-th Lagrange polynomial on n LGL pts */
+int orc_interp_matrix(int n, int m, const double* targets, double* M);
+/* face (ne pts) -> mortar (nm >= ne pts): P[i*ne + j], i < nm (interpolation) */
+int orc_proj_face_to_mortar(int ne, int nm, double* P);
+/* mortar (nm pts) -> face (ne <= nm pts): P[i*nm + j], i < ne (modal truncation) */
+int orc_proj_mortar_to_face(int ne, int nm, double* P);
+
+/* ---------------- domain (a13, a14) ---------------- */
+/* One periodic brick evolution: [lo, hi]^3 with n[d] elements along axis d.
+ * n[d] = b * 2^L with b odd is laid out as b blocks of refinement L. */
+typedef struct {
+  double lo[3];
+  double hi[3];
+  int32_t n[3];
+} OrcBrick;
+
+/* number of elements over all instances */
+int64_t orc_num_elements(int n_inst, const OrcBrick* bricks);
+/* elem_id: packed 64-bit ElementId; nbr: 6 per element in Direction order
+ * (lower_xi, upper_xi, lower_eta, upper_eta, lower_zeta, upper_zeta), global
+ * element index; ijk: 3 global lattice coordinates per element; inst: owner. */
+int orc_index_maps(int n_inst, const OrcBrick* bricks, uint64_t* elem_id,
+                   int32_t* nbr, int32_t* ijk, int32_t* inst);
+
+/* Offsets (in doubles) of each element's 5*N^3 block; off has n_elem+1 entries. */
+int orc_offsets(int64_t n_elem, const int32_t* elem_n, int64_t* off);
+
+/* Inertial coordinates, 3*N^3 per element (x, y, z component-major). */
+int orc_coords(int n_inst, const OrcBrick* bricks, const int32_t* elem_n,
+               double* xyz);
+
+/* ---------------- initial data ---------------- */
+/* kind 0: plane wave psi = sin(k.x - |k| t), params = {kx, ky, kz}
+ * kind 1: gaussian pulse psi = A exp(-|x-c|^2 / w^2), Pi = 0,
+ *         params per instance = {A, w, cx, cy, cz} (5 * n_inst values) */
+int orc_initial_data(int n_inst, const OrcBrick* bricks, const int32_t* elem_n,
+                     int kind, const double* params, double t, double* u);
+
+/* ---------------- UpwindPenalty (a6, a8) ---------------- */
+/* packaged: 16*npts component-major in dg_package_field_tags order:
+ *   v_psi, v_zero[3], v_plus, v_minus, n*v_plus[3], n*v_minus[3],
+ *   gamma2*v_psi, char_speeds[3]
+ * phi, normal: 3*npts component-major.  ndotv may be NULL (no mesh velocity). */
+int orc_package(int npts, const double* psi, const double* pi,
+                const double* phi, const double* gamma2, const double* normal,
+                const double* ndotv, double* packaged, double* max_speed);
+/* out: 5*npts (psi, pi, phi_x, phi_y, phi_z boundary corrections) */
+int orc_boundary_terms(int npts, const double* pkg_int, const double* pkg_ext,
+                       double* out);
+
+/* ---------------- DG right-hand side and stepping (a2-a12) ---------------- */
+/* dudt = strong-form DG time derivative with UpwindPenalty corrections lifted
+ * at GLL faces; u, dudt laid out per element [var][k][j][i]. gamma2 constant. */
+int orc_rhs(int n_inst, const OrcBrick* bricks, const int32_t* elem_n,
+            double gamma2, const double* u, double* dudt, int n_threads);
+/* volume terms only (TimeDerivative::apply after partial_derivatives) */
+int orc_volume_rhs(int n_inst, const OrcBrick* bricks, const int32_t* elem_n,
+                   double gamma2, const double* u, double* dudt, int n_threads);
+/* one SSP-RK3 substep k (0,1,2) given u0 (step start) and the current stage
+ * value ucur: writes unext. */
+int orc_rk3_substep(int64_t n, int k, double dt, const double* u0,
+                    const double* ucur, const double* dudt, double* unext);
+/* n_steps full SSP-RK3 steps in place */
+int orc_evolve(int n_inst, const OrcBrick* bricks, const int32_t* elem_n,
+               double gamma2, double dt, int n_steps, double* u, int n_threads);
+
+#ifdef __cplusplus
+}
+#endif
+#endif

@@ -1,0 +1,212 @@
+"""ctypes binding of oracle/_build/liboracle.so (test infrastructure only).
+
+The library is the C++ FP64 restatement in dgsw_oracle.cpp; see its header for
+the reference file:line each function follows.
+"""
+import ctypes
+import math
+import os
+import subprocess
+
+import numpy as np
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+LIB = os.path.join(HERE, "_build", "liboracle.so")
+
+
+class OrcBrick(ctypes.Structure):
+    _fields_ = [("lo", ctypes.c_double * 3), ("hi", ctypes.c_double * 3),
+                ("n", ctypes.c_int32 * 3)]
+
+
+def build():
+    subprocess.run(["make", "-s", "-C", HERE], check=True)
+    return LIB
+
+
+_lib = None
+
+
+def lib():
+    global _lib
+    if _lib is None:
+        if not os.path.exists(LIB) or os.path.getmtime(LIB) < os.path.getmtime(
+                os.path.join(HERE, "dgsw_oracle.cpp")):
+            build()
+        L = ctypes.CDLL(LIB)
+        P, D, I, I64 = ctypes.c_void_p, ctypes.c_double, ctypes.c_int, ctypes.c_int64
+        sig = {
+            "orc_lgl": [I, P, P], "orc_barycentric_weights": [I, P],
+            "orc_diff_matrix": [I, P], "orc_vandermonde": [I, P],
+            "orc_inv_vandermonde": [I, P], "orc_interp_matrix": [I, I, P, P],
+            "orc_proj_face_to_mortar": [I, I, P], "orc_proj_mortar_to_face": [I, I, P],
+            "orc_index_maps": [I, P, P, P, P, P], "orc_offsets": [I64, P, P],
+            "orc_coords": [I, P, P, P], "orc_initial_data": [I, P, P, I, P, D, P],
+            "orc_package": [I, P, P, P, P, P, P, P, P], "orc_boundary_terms": [I, P, P, P],
+            "orc_rhs": [I, P, P, D, P, P, I], "orc_volume_rhs": [I, P, P, D, P, P, I],
+            "orc_rk3_substep": [I64, I, D, P, P, P, P], "orc_evolve": [I, P, P, D, D, I, P, I],
+        }
+        for name, args in sig.items():
+            fn = getattr(L, name)
+            fn.argtypes = args
+            fn.restype = I
+        L.orc_num_elements.argtypes = [I, P]
+        L.orc_num_elements.restype = I64
+        _lib = L
+    return _lib
+
+
+def _p(a):
+    return None if a is None else a.ctypes.data
+
+
+def _bricks(bricks):
+    arr = (OrcBrick * len(bricks))()
+    for i, b in enumerate(bricks):
+        arr[i].lo[:] = [float(v) for v in b.lower]
+        arr[i].hi[:] = [float(v) for v in b.upper]
+        arr[i].n[:] = [int(v) for v in b.elements]
+    return arr
+
+
+def _check(rc):
+    if rc != 0:
+        raise RuntimeError("oracle call failed with %d" % rc)
+
+
+def lgl(n):
+    x, w = np.zeros(n), np.zeros(n)
+    _check(lib().orc_lgl(n, _p(x), _p(w)))
+    return x, w
+
+
+def diff_matrix(n):
+    D = np.zeros((n, n))
+    _check(lib().orc_diff_matrix(n, _p(D)))
+    return D
+
+
+def vandermonde(n):
+    V = np.zeros((n, n))
+    _check(lib().orc_vandermonde(n, _p(V)))
+    return V
+
+
+def inv_vandermonde(n):
+    V = np.zeros((n, n))
+    _check(lib().orc_inv_vandermonde(n, _p(V)))
+    return V
+
+
+def proj_face_to_mortar(ne, nm):
+    P = np.zeros((nm, ne))
+    _check(lib().orc_proj_face_to_mortar(ne, nm, _p(P)))
+    return P
+
+
+def proj_mortar_to_face(ne, nm):
+    P = np.zeros((ne, nm))
+    _check(lib().orc_proj_mortar_to_face(ne, nm, _p(P)))
+    return P
+
+
+def num_elements(bricks):
+    arr = _bricks(bricks)
+    return lib().orc_num_elements(len(bricks), ctypes.addressof(arr))
+
+
+def index_maps(bricks):
+    arr = _bricks(bricks)
+    E = lib().orc_num_elements(len(bricks), ctypes.addressof(arr))
+    ids = np.zeros(E, dtype=np.uint64)
+    nbr = np.zeros((E, 6), dtype=np.int32)
+    ijk = np.zeros((E, 3), dtype=np.int32)
+    inst = np.zeros(E, dtype=np.int32)
+    rc = lib().orc_index_maps(len(bricks), ctypes.addressof(arr), _p(ids), _p(nbr), _p(ijk),
+                              _p(inst))
+    if rc not in (0, -2):
+        _check(rc)
+    return ids, nbr, ijk, inst, rc == 0
+
+
+def offsets(elem_n):
+    elem_n = np.ascontiguousarray(elem_n, dtype=np.int32)
+    off = np.zeros(len(elem_n) + 1, dtype=np.int64)
+    _check(lib().orc_offsets(len(elem_n), _p(elem_n), _p(off)))
+    return off
+
+
+def elem_points(bricks, points):
+    E = num_elements(bricks)
+    if np.ndim(points) == 0:
+        return np.full(E, int(points), dtype=np.int32)
+    return np.ascontiguousarray(points, dtype=np.int32)
+
+
+def coords(bricks, points):
+    en = elem_points(bricks, points)
+    off = offsets(en)
+    xyz = np.zeros(3 * int(off[-1]) // 5)
+    arr = _bricks(bricks)
+    _check(lib().orc_coords(len(bricks), ctypes.addressof(arr), _p(en), _p(xyz)))
+    return xyz
+
+
+def initial_data(bricks, points, kind, params, t=0.0):
+    en = elem_points(bricks, points)
+    off = offsets(en)
+    u = np.zeros(int(off[-1]))
+    p = np.ascontiguousarray(params, dtype=np.float64).ravel()
+    arr = _bricks(bricks)
+    k = {"plane_wave": 0, "gaussian": 1}[kind]
+    _check(lib().orc_initial_data(len(bricks), ctypes.addressof(arr), _p(en), k, _p(p), t, _p(u)))
+    return u
+
+
+def package(psi, pi, phi, gamma2, normal, ndotv=None):
+    n = len(psi)
+    out = np.zeros((16, n))
+    ms = ctypes.c_double()
+    args = [np.ascontiguousarray(a, dtype=np.float64) for a in (psi, pi, phi, gamma2, normal)]
+    nd = None if ndotv is None else np.ascontiguousarray(ndotv, dtype=np.float64)
+    _check(lib().orc_package(n, *[_p(a) for a in args], _p(nd), _p(out),
+                             ctypes.addressof(ms)))
+    return out, ms.value
+
+
+def boundary_terms(pkg_int, pkg_ext):
+    n = pkg_int.shape[1]
+    out = np.zeros((5, n))
+    a = np.ascontiguousarray(pkg_int, dtype=np.float64)
+    b = np.ascontiguousarray(pkg_ext, dtype=np.float64)
+    _check(lib().orc_boundary_terms(n, _p(a), _p(b), _p(out)))
+    return out
+
+
+def rhs(bricks, points, u, gamma2=0.0, threads=0, volume_only=False):
+    en = elem_points(bricks, points)
+    u = np.ascontiguousarray(u, dtype=np.float64)
+    out = np.zeros_like(u)
+    arr = _bricks(bricks)
+    fn = lib().orc_volume_rhs if volume_only else lib().orc_rhs
+    _check(fn(len(bricks), ctypes.addressof(arr), _p(en), gamma2, _p(u), _p(out), threads))
+    return out
+
+
+def rk3_substep(k, dt, u0, ucur, dudt):
+    out = np.zeros_like(u0)
+    _check(lib().orc_rk3_substep(len(u0), k, dt, _p(u0), _p(ucur), _p(dudt), _p(out)))
+    return out
+
+
+def evolve(bricks, points, u, dt, steps, gamma2=0.0, threads=0):
+    en = elem_points(bricks, points)
+    u = np.array(u, dtype=np.float64, copy=True)
+    arr = _bricks(bricks)
+    _check(lib().orc_evolve(len(bricks), ctypes.addressof(arr), _p(en), gamma2, dt, steps,
+                            _p(u), threads))
+    return u
+
+
+def gaussian_params(n_inst, amp=1.0, width=0.5, center=(math.pi, math.pi, math.pi)):
+    return np.tile(np.array([amp, width, *center], dtype=np.float64), (n_inst, 1))

@@ -1,0 +1,493 @@
+// dgsw_api.cu -- the C ABI (include/dgsw.h): handle lifecycle, state
+// transfer, RHS / substep / step launches and host-only setup queries.
+//
+// Ownership follows the reference's DG element: the caller owns the state it
+// passes in (Variables of Psi, Pi, Phi), the handle owns every device buffer.
+// dgsw_step allocates nothing: the three stage launches of one SSP-RK3 step
+// (Rk3HesthavenSsp.cpp:63-80) are captured once into a CUDA graph per
+// (dt, steps-per-graph) and replayed.
+#include <cmath>
+#include <cstdio>
+#include <cstring>
+#include <new>
+#include <string>
+#include <vector>
+
+#include "../../include/dgsw.h"
+#include "common.cuh"
+#include "host_setup.hpp"
+#include "launch.hpp"
+
+using namespace dgsw;
+
+struct DgswHandle_ {
+  DgswConfig cfg{};
+  Domain dom;
+  int device = 0;
+  cudaStream_t stream = nullptr;
+  // device buffers
+  double* state = nullptr;  // u^n (Variables of all elements)
+  double* t1 = nullptr;     // stage buffers
+  double* t2 = nullptr;
+  double* u0s = nullptr;    // step-start copy for dgsw_substep
+  int32_t* nbr = nullptr;
+  double* jac = nullptr;
+  double* lower = nullptr;
+  double* width = nullptr;
+  int32_t* elem_n = nullptr;
+  int64_t* offset = nullptr;
+  int32_t* instance = nullptr;
+  double* lgl_x = nullptr;
+  double* params = nullptr;  // initial-data parameters
+  size_t params_cap = 0;
+  EoTable eo{};
+  // graphs of whole steps
+  cudaGraphExec_t graph_one = nullptr;
+  cudaGraphExec_t graph_many = nullptr;
+  int graph_many_steps = 0;
+  double graph_dt = std::nan("");
+  std::string err;
+};
+
+namespace {
+
+thread_local std::string g_last_error;
+
+int fail(DgswHandle h, int code, const std::string& msg) {
+  if (h) h->err = msg;
+  g_last_error = msg;
+  return code;
+}
+
+int cuda_fail(DgswHandle h, cudaError_t e, const char* where) {
+  std::string m = std::string(where) + ": " + cudaGetErrorString(e);
+  return fail(h, DGSW_ERR_CUDA, m);
+}
+
+#define DGSW_CUDA(h, call)                          \
+  do {                                              \
+    cudaError_t e_ = (call);                        \
+    if (e_ != cudaSuccess) return cuda_fail(h, e_, #call); \
+  } while (0)
+
+template <typename T>
+cudaError_t upload(T** dst, const std::vector<T>& v) {
+  cudaError_t e = cudaMalloc(dst, v.size() * sizeof(T) + 16);
+  if (e != cudaSuccess) return e;
+  return cudaMemcpy(*dst, v.data(), v.size() * sizeof(T), cudaMemcpyHostToDevice);
+}
+
+int select_device(DgswHandle h) {
+  cudaError_t e = cudaSetDevice(h->device);
+  if (e != cudaSuccess) return cuda_fail(h, e, "cudaSetDevice");
+  return DGSW_OK;
+}
+
+void destroy_graphs(DgswHandle h) {
+  if (h->graph_one) cudaGraphExecDestroy(h->graph_one);
+  if (h->graph_many) cudaGraphExecDestroy(h->graph_many);
+  h->graph_one = h->graph_many = nullptr;
+  h->graph_many_steps = 0;
+  h->graph_dt = std::nan("");
+}
+
+StageLaunch base_launch(DgswHandle h) {
+  StageLaunch L;
+  L.n = h->dom.elem_n.empty() ? 0 : h->dom.elem_n[0];
+  L.nbr = h->nbr;
+  L.jac = h->jac;
+  L.n_elem = h->dom.n_elem;
+  L.gamma2 = h->cfg.gamma2;
+  L.eo = h->eo;
+  return L;
+}
+
+cudaError_t launch_stage(DgswHandle h, const StageLaunch& L) {
+  return launch_stage_fp64(L, h->stream);
+}
+
+// Enqueue the three substeps of one SSP-RK3 step on the handle's stream:
+//   t1 = u + dt L(u); t2 = 3/4 u + 1/4 t1 + dt/4 L(t1);
+//   u  = 1/3 u + 2/3 t2 + 2dt/3 L(t2)   (in place: each element reads only
+//   its own u, neighbours' faces come from t2).
+cudaError_t enqueue_step(DgswHandle h, double dt) {
+  StageLaunch L = base_launch(h);
+  L.mode = kModeStageFirst;
+  L.ucur = h->state;
+  L.u0 = h->state;
+  L.unext = h->t1;
+  L.coef = {0.0, 1.0, dt};
+  cudaError_t e = launch_stage(h, L);
+  if (e != cudaSuccess) return e;
+  L.mode = kModeStage;
+  L.ucur = h->t1;
+  L.u0 = h->state;
+  L.unext = h->t2;
+  L.coef = {0.75, 0.25, 0.25 * dt};
+  e = launch_stage(h, L);
+  if (e != cudaSuccess) return e;
+  L.ucur = h->t2;
+  L.u0 = h->state;
+  L.unext = h->state;
+  L.coef = {1.0 / 3.0, 2.0 / 3.0, (2.0 / 3.0) * dt};
+  return launch_stage(h, L);
+}
+
+cudaError_t capture_steps(DgswHandle h, double dt, int steps, cudaGraphExec_t* out) {
+  cudaGraph_t g = nullptr;
+  cudaError_t e = cudaStreamBeginCapture(h->stream, cudaStreamCaptureModeThreadLocal);
+  if (e != cudaSuccess) return e;
+  cudaError_t le = cudaSuccess;
+  for (int s = 0; s < steps && le == cudaSuccess; ++s) le = enqueue_step(h, dt);
+  e = cudaStreamEndCapture(h->stream, &g);
+  if (le != cudaSuccess) {
+    if (g) cudaGraphDestroy(g);
+    return le;
+  }
+  if (e != cudaSuccess) return e;
+  e = cudaGraphInstantiate(out, g, 0);
+  cudaGraphDestroy(g);
+  return e;
+}
+
+}  // namespace
+
+extern "C" {
+
+int dgsw_abi_version(void) { return DGSW_ABI_VERSION; }
+
+const char* dgsw_last_error(DgswHandle h) {
+  if (h) return h->err.c_str();
+  return g_last_error.c_str();
+}
+
+int dgsw_count_elements(const DgswConfig* cfg, int64_t* n_elements, int64_t* state_doubles) {
+  if (!cfg) return fail(nullptr, DGSW_ERR_ARGUMENT, "null config");
+  Domain dom;
+  std::string err;
+  if (!build_domain(*cfg, &dom, &err)) return fail(nullptr, DGSW_ERR_ARGUMENT, err);
+  if (n_elements) *n_elements = dom.n_elem;
+  if (state_doubles) *state_doubles = dom.offset.back();
+  return DGSW_OK;
+}
+
+int dgsw_index_maps(const DgswConfig* cfg, uint64_t* ids, int32_t* nbr, int32_t* mortar) {
+  if (!cfg) return fail(nullptr, DGSW_ERR_ARGUMENT, "null config");
+  Domain dom;
+  std::string err;
+  if (!build_domain(*cfg, &dom, &err)) return fail(nullptr, DGSW_ERR_ARGUMENT, err);
+  if (ids) std::memcpy(ids, dom.element_id.data(), dom.n_elem * sizeof(uint64_t));
+  if (nbr) std::memcpy(nbr, dom.neighbor.data(), 6 * dom.n_elem * sizeof(int32_t));
+  if (mortar)
+    for (int64_t e = 0; e < dom.n_elem; ++e)
+      for (int dir = 0; dir < 6; ++dir) {
+        const int a = dom.elem_n[e], b = dom.elem_n[dom.neighbor[6 * e + dir]];
+        mortar[6 * e + dir] = a > b ? a : b;
+      }
+  if (!dom.block_ids_fit)
+    return fail(nullptr, DGSW_ERR_UNSUPPORTED, "a block id does not fit in 8 bits");
+  return DGSW_OK;
+}
+
+int dgsw_lgl_points_weights(int n, double* x, double* w) {
+  if (!lgl_nodes_weights(n, x, w)) return fail(nullptr, DGSW_ERR_ARGUMENT, "n must be in [2, 20]");
+  return DGSW_OK;
+}
+
+int dgsw_differentiation_matrix(int n, double* D) {
+  if (!lgl_diff_matrix(n, D)) return fail(nullptr, DGSW_ERR_ARGUMENT, "n must be in [2, 20]");
+  return DGSW_OK;
+}
+
+int dgsw_mortar_projections(int ne, int nm, double* to_m, double* from_m) {
+  if (!lgl_mortar_projections(ne, nm, to_m, from_m))
+    return fail(nullptr, DGSW_ERR_ARGUMENT, "need 2 <= ne <= nm <= 20");
+  return DGSW_OK;
+}
+
+int dgsw_create(const DgswConfig* cfg, DgswHandle* out) {
+  if (!cfg || !out) return fail(nullptr, DGSW_ERR_ARGUMENT, "null argument");
+  *out = nullptr;
+  DgswHandle h = new (std::nothrow) DgswHandle_;
+  if (!h) return fail(nullptr, DGSW_ERR_ARGUMENT, "out of host memory");
+  h->cfg = *cfg;
+  std::string err;
+  if (!build_domain(*cfg, &h->dom, &err)) {
+    delete h;
+    return fail(nullptr, DGSW_ERR_ARGUMENT, err);
+  }
+  h->cfg.bricks = nullptr;  // copies live in h->dom
+  h->cfg.points_per_element = nullptr;
+  if (!h->dom.uniform) {
+    delete h;
+    return fail(nullptr, DGSW_ERR_UNSUPPORTED, "elements of different extents are not supported yet");
+  }
+  if (cfg->precision != DGSW_PRECISION_FP64) {
+    delete h;
+    return fail(nullptr, DGSW_ERR_UNSUPPORTED, "only FP64 precision in this build");
+  }
+  int count = 0;
+  if (cudaGetDeviceCount(&count) != cudaSuccess || count <= cfg->device || cfg->device < 0) {
+    delete h;
+    return fail(nullptr, DGSW_ERR_NO_DEVICE, "no CUDA device with that ordinal");
+  }
+  h->device = cfg->device;
+  cudaDeviceProp prop;
+  if (cudaGetDeviceProperties(&prop, h->device) != cudaSuccess || prop.major != 10) {
+    delete h;
+    return fail(nullptr, DGSW_ERR_NO_DEVICE, "device is not a Blackwell (sm_10x) GPU");
+  }
+  int rc = select_device(h);
+  if (rc) {
+    delete h;
+    return rc;
+  }
+  auto bail = [&](cudaError_t e, const char* where) {
+    int code = cuda_fail(nullptr, e, where);
+    dgsw_destroy(h);
+    return code;
+  };
+  cudaError_t e = cudaStreamCreateWithFlags(&h->stream, cudaStreamNonBlocking);
+  if (e != cudaSuccess) return bail(e, "cudaStreamCreate");
+  const size_t bytes = (size_t)h->dom.offset.back() * sizeof(double);
+  if ((e = cudaMalloc(&h->state, bytes)) != cudaSuccess) return bail(e, "cudaMalloc state");
+  if ((e = cudaMalloc(&h->t1, bytes)) != cudaSuccess) return bail(e, "cudaMalloc stage 1");
+  if ((e = cudaMalloc(&h->t2, bytes)) != cudaSuccess) return bail(e, "cudaMalloc stage 2");
+  if ((e = cudaMalloc(&h->u0s, bytes)) != cudaSuccess) return bail(e, "cudaMalloc step start");
+  if ((e = cudaMemset(h->state, 0, bytes)) != cudaSuccess) return bail(e, "cudaMemset");
+  std::vector<double> jac(3 * h->dom.n_elem);
+  for (int64_t i = 0; i < 3 * h->dom.n_elem; ++i) jac[i] = 2.0 / h->dom.width[i];
+  if ((e = upload(&h->nbr, h->dom.neighbor)) != cudaSuccess) return bail(e, "upload neighbors");
+  if ((e = upload(&h->jac, jac)) != cudaSuccess) return bail(e, "upload jacobian");
+  if ((e = upload(&h->lower, h->dom.lower)) != cudaSuccess) return bail(e, "upload lower");
+  if ((e = upload(&h->width, h->dom.width)) != cudaSuccess) return bail(e, "upload width");
+  if ((e = upload(&h->elem_n, h->dom.elem_n)) != cudaSuccess) return bail(e, "upload extents");
+  if ((e = upload(&h->offset, h->dom.offset)) != cudaSuccess) return bail(e, "upload offsets");
+  if ((e = upload(&h->instance, h->dom.instance)) != cudaSuccess) return bail(e, "upload instance");
+  std::vector<double> nodes((kMaxN + 1) * kMaxN, 0.0);
+  for (int n = kMinN; n <= kMaxN; ++n) {
+    double w[kMaxN];
+    lgl_nodes_weights(n, &nodes[n * kMaxN], w);
+  }
+  if ((e = upload(&h->lgl_x, nodes)) != cudaSuccess) return bail(e, "upload nodes");
+  lgl_eo_table(h->dom.elem_n[0], &h->eo);
+  *out = h;
+  return DGSW_OK;
+}
+
+int dgsw_destroy(DgswHandle h) {
+  if (!h) return DGSW_OK;
+  cudaSetDevice(h->device);
+  if (h->stream) cudaStreamSynchronize(h->stream);
+  destroy_graphs(h);
+  double* dbl[] = {h->state, h->t1, h->t2, h->u0s, h->jac, h->lower, h->width, h->lgl_x, h->params};
+  for (double* p : dbl)
+    if (p) cudaFree(p);
+  if (h->nbr) cudaFree(h->nbr);
+  if (h->elem_n) cudaFree(h->elem_n);
+  if (h->offset) cudaFree(h->offset);
+  if (h->instance) cudaFree(h->instance);
+  if (h->stream) cudaStreamDestroy(h->stream);
+  delete h;
+  return DGSW_OK;
+}
+
+int dgsw_sizes(DgswHandle h, int64_t* n_elements, int64_t* state_doubles, int64_t* grid_points) {
+  if (!h) return fail(nullptr, DGSW_ERR_ARGUMENT, "null handle");
+  if (n_elements) *n_elements = h->dom.n_elem;
+  if (state_doubles) *state_doubles = h->dom.offset.back();
+  if (grid_points) *grid_points = h->dom.n_points;
+  return DGSW_OK;
+}
+
+void* dgsw_stream(DgswHandle h) { return h ? (void*)h->stream : nullptr; }
+
+int dgsw_synchronize(DgswHandle h) {
+  if (!h) return fail(nullptr, DGSW_ERR_ARGUMENT, "null handle");
+  if (int rc = select_device(h)) return rc;
+  DGSW_CUDA(h, cudaStreamSynchronize(h->stream));
+  return DGSW_OK;
+}
+
+int dgsw_set_state(DgswHandle h, const double* host_u) {
+  if (!h || !host_u) return fail(h, DGSW_ERR_ARGUMENT, "null argument");
+  if (int rc = select_device(h)) return rc;
+  DGSW_CUDA(h, cudaMemcpyAsync(h->state, host_u, h->dom.offset.back() * sizeof(double),
+                               cudaMemcpyHostToDevice, h->stream));
+  return DGSW_OK;
+}
+
+int dgsw_get_state(DgswHandle h, double* host_u) {
+  if (!h || !host_u) return fail(h, DGSW_ERR_ARGUMENT, "null argument");
+  if (int rc = select_device(h)) return rc;
+  DGSW_CUDA(h, cudaMemcpyAsync(host_u, h->state, h->dom.offset.back() * sizeof(double),
+                               cudaMemcpyDeviceToHost, h->stream));
+  DGSW_CUDA(h, cudaStreamSynchronize(h->stream));
+  return DGSW_OK;
+}
+
+int dgsw_set_state_device(DgswHandle h, const double* dev_u) {
+  if (!h || !dev_u) return fail(h, DGSW_ERR_ARGUMENT, "null argument");
+  if (int rc = select_device(h)) return rc;
+  DGSW_CUDA(h, cudaMemcpyAsync(h->state, dev_u, h->dom.offset.back() * sizeof(double),
+                               cudaMemcpyDeviceToDevice, h->stream));
+  return DGSW_OK;
+}
+
+int dgsw_get_state_device(DgswHandle h, double* dev_u) {
+  if (!h || !dev_u) return fail(h, DGSW_ERR_ARGUMENT, "null argument");
+  if (int rc = select_device(h)) return rc;
+  DGSW_CUDA(h, cudaMemcpyAsync(dev_u, h->state, h->dom.offset.back() * sizeof(double),
+                               cudaMemcpyDeviceToDevice, h->stream));
+  return DGSW_OK;
+}
+
+int dgsw_set_initial_data(DgswHandle h, int kind, const double* params, double t) {
+  if (!h || !params) return fail(h, DGSW_ERR_ARGUMENT, "null argument");
+  if (kind != 0 && kind != 1) return fail(h, DGSW_ERR_ARGUMENT, "unknown initial data kind");
+  if (int rc = select_device(h)) return rc;
+  const size_t count = kind == 0 ? 3 : 5 * (size_t)h->dom.bricks.size();
+  for (size_t i = 0; i < count; ++i)
+    if (!std::isfinite(params[i])) return fail(h, DGSW_ERR_ARGUMENT, "non-finite parameter");
+  if (kind == 1)
+    for (size_t i = 0; i < h->dom.bricks.size(); ++i)
+      if (!(params[5 * i + 1] > 0.0)) return fail(h, DGSW_ERR_ARGUMENT, "width must be positive");
+  if (count > h->params_cap) {
+    DGSW_CUDA(h, cudaStreamSynchronize(h->stream));
+    if (h->params) cudaFree(h->params);
+    h->params = nullptr;
+    DGSW_CUDA(h, cudaMalloc(&h->params, count * sizeof(double)));
+    h->params_cap = count;
+  }
+  DGSW_CUDA(h, cudaMemcpyAsync(h->params, params, count * sizeof(double), cudaMemcpyHostToDevice,
+                               h->stream));
+  InitLaunch L;
+  L.kind = kind;
+  L.n_elem = h->dom.n_elem;
+  L.elem_n = h->elem_n;
+  L.offset = h->offset;
+  L.instance = h->instance;
+  L.lower = h->lower;
+  L.width = h->width;
+  L.params = h->params;
+  L.lgl_x = h->lgl_x;
+  L.t = t;
+  L.u = h->state;
+  DGSW_CUDA(h, launch_initial_data(L, h->stream));
+  DGSW_CUDA(h, cudaStreamSynchronize(h->stream));
+  return DGSW_OK;
+}
+
+int dgsw_rhs_device(DgswHandle h, const double* dev_u, double* dev_dudt) {
+  if (!h || !dev_u || !dev_dudt) return fail(h, DGSW_ERR_ARGUMENT, "null argument");
+  if (dev_u == dev_dudt) return fail(h, DGSW_ERR_ARGUMENT, "input and output must differ");
+  if (int rc = select_device(h)) return rc;
+  StageLaunch L = base_launch(h);
+  L.mode = kModeRhs;
+  L.ucur = dev_u;
+  L.u0 = dev_u;
+  L.unext = dev_dudt;
+  L.coef = {0.0, 0.0, 1.0};
+  DGSW_CUDA(h, launch_stage(h, L));
+  return DGSW_OK;
+}
+
+int dgsw_volume_rhs_device(DgswHandle h, const double* dev_u, double* dev_dudt) {
+  if (!h || !dev_u || !dev_dudt) return fail(h, DGSW_ERR_ARGUMENT, "null argument");
+  if (dev_u == dev_dudt) return fail(h, DGSW_ERR_ARGUMENT, "input and output must differ");
+  if (int rc = select_device(h)) return rc;
+  StageLaunch L = base_launch(h);
+  L.mode = kModeVolume;
+  L.ucur = dev_u;
+  L.u0 = dev_u;
+  L.unext = dev_dudt;
+  L.coef = {0.0, 0.0, 1.0};
+  DGSW_CUDA(h, launch_stage(h, L));
+  return DGSW_OK;
+}
+
+int dgsw_rhs(DgswHandle h, const double* host_u, double* host_dudt) {
+  if (!h || !host_u || !host_dudt) return fail(h, DGSW_ERR_ARGUMENT, "null argument");
+  if (int rc = select_device(h)) return rc;
+  const size_t bytes = h->dom.offset.back() * sizeof(double);
+  // t1/t2 hold only intermediate stage values between launches, so they
+  // double as staging buffers here.
+  DGSW_CUDA(h, cudaMemcpyAsync(h->t1, host_u, bytes, cudaMemcpyHostToDevice, h->stream));
+  if (int rc = dgsw_rhs_device(h, h->t1, h->t2)) return rc;
+  DGSW_CUDA(h, cudaMemcpyAsync(host_dudt, h->t2, bytes, cudaMemcpyDeviceToHost, h->stream));
+  DGSW_CUDA(h, cudaStreamSynchronize(h->stream));
+  return DGSW_OK;
+}
+
+int dgsw_package_data_device(int64_t npts, const double* psi, const double* pi, const double* phi,
+                             const double* gamma2, const double* normal, const double* ndotv,
+                             double* packaged, void* stream) {
+  if (npts < 0 || (npts > 0 && (!psi || !pi || !phi || !gamma2 || !normal || !packaged)))
+    return fail(nullptr, DGSW_ERR_ARGUMENT, "null argument");
+  cudaError_t e = launch_package_data(npts, psi, pi, phi, gamma2, normal, ndotv, packaged,
+                                      (cudaStream_t)stream);
+  if (e != cudaSuccess) return cuda_fail(nullptr, e, "package_data");
+  return DGSW_OK;
+}
+
+int dgsw_boundary_terms_device(int64_t npts, const double* pkg_int, const double* pkg_ext,
+                               double* out, void* stream) {
+  if (npts < 0 || (npts > 0 && (!pkg_int || !pkg_ext || !out)))
+    return fail(nullptr, DGSW_ERR_ARGUMENT, "null argument");
+  cudaError_t e = launch_boundary_terms(npts, pkg_int, pkg_ext, out, (cudaStream_t)stream);
+  if (e != cudaSuccess) return cuda_fail(nullptr, e, "boundary_terms");
+  return DGSW_OK;
+}
+
+int dgsw_substep(DgswHandle h, int k, double dt) {
+  if (!h) return fail(nullptr, DGSW_ERR_ARGUMENT, "null handle");
+  if (k < 0 || k > 2 || !std::isfinite(dt)) return fail(h, DGSW_ERR_ARGUMENT, "bad substep");
+  if (int rc = select_device(h)) return rc;
+  const size_t bytes = h->dom.offset.back() * sizeof(double);
+  StageLaunch L = base_launch(h);
+  if (k == 0) {
+    DGSW_CUDA(h, cudaMemcpyAsync(h->u0s, h->state, bytes, cudaMemcpyDeviceToDevice, h->stream));
+    L.mode = kModeStageFirst;
+    L.ucur = h->u0s;
+    L.u0 = h->u0s;
+    L.unext = h->state;
+    L.coef = {0.0, 1.0, dt};
+  } else {
+    DGSW_CUDA(h, cudaMemcpyAsync(h->t1, h->state, bytes, cudaMemcpyDeviceToDevice, h->stream));
+    L.mode = kModeStage;
+    L.ucur = h->t1;
+    L.u0 = h->u0s;
+    L.unext = h->state;
+    L.coef = k == 1 ? StageCoef{0.75, 0.25, 0.25 * dt}
+                    : StageCoef{1.0 / 3.0, 2.0 / 3.0, (2.0 / 3.0) * dt};
+  }
+  DGSW_CUDA(h, launch_stage(h, L));
+  return DGSW_OK;
+}
+
+int dgsw_step(DgswHandle h, int n_steps, double dt) {
+  if (!h) return fail(nullptr, DGSW_ERR_ARGUMENT, "null handle");
+  if (n_steps < 0 || !std::isfinite(dt)) return fail(h, DGSW_ERR_ARGUMENT, "bad step arguments");
+  if (n_steps == 0) return DGSW_OK;
+  if (int rc = select_device(h)) return rc;
+  if (!(h->graph_dt == dt)) {
+    destroy_graphs(h);
+    DGSW_CUDA(h, capture_steps(h, dt, 1, &h->graph_one));
+    h->graph_dt = dt;
+  }
+  // replay chunks of up to 16 steps per graph launch to amortise launch cost
+  constexpr int kChunk = 16;
+  if (n_steps >= kChunk && !h->graph_many) {
+    DGSW_CUDA(h, capture_steps(h, dt, kChunk, &h->graph_many));
+    h->graph_many_steps = kChunk;
+  }
+  int left = n_steps;
+  while (h->graph_many && left >= h->graph_many_steps) {
+    DGSW_CUDA(h, cudaGraphLaunch(h->graph_many, h->stream));
+    left -= h->graph_many_steps;
+  }
+  for (; left > 0; --left) DGSW_CUDA(h, cudaGraphLaunch(h->graph_one, h->stream));
+  return DGSW_OK;
+}
+
+}  // extern "C"

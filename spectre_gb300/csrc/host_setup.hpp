@@ -1,0 +1,60 @@
+// host_setup.hpp -- host-side (FP64) spectral tables and domain index maps.
+//
+// Setup work that runs once per handle on the CPU: Legendre-Gauss-Lobatto
+// nodes and weights, the differentiation matrix, mortar projection matrices
+// and the integer element/neighbour/mortar maps of a periodic brick lattice.
+#pragma once
+
+#include <cstdint>
+#include <string>
+#include <vector>
+
+#include "../../include/dgsw.h"
+#include "common.cuh"
+
+namespace dgsw {
+
+// Spectral::collocation_points/quadrature_weights<Legendre, GaussLobatto>,
+// Legendre.cpp:186-239.  Nodes are the roots of q = L_{p+1} - L_{p-1}
+// found by Newton's method with q' = (2p+1) L_p.
+bool lgl_nodes_weights(int n, double* x, double* w);
+// Barycentric differentiation matrix with negative-sum diagonal,
+// Spectral.cpp:84-111,431-444.  Row-major.
+bool lgl_diff_matrix(int n, double* D);
+// Interpolation from n LGL points to m targets, Spectral.cpp:625-670.
+bool lgl_interp_matrix(int n, int m, const double* targets, double* M);
+// Face -> mortar (nm x ne, interpolation) and mortar -> face (ne x nm,
+// Legendre modal truncation), Projection.cpp:56-375, ChildSize::Full.
+bool lgl_mortar_projections(int ne, int nm, double* to_mortar, double* from_mortar);
+// Even/odd split tables of the differentiation matrix (see EoTable).
+bool lgl_eo_table(int n, EoTable* t);
+
+struct BrickLayout {
+  int blocks[3];  // odd part of each per-axis element count
+  int level[3];   // refinement level: count = blocks * 2^level
+  int64_t first;  // global index of the instance's first element
+  int64_t count;
+};
+
+struct Domain {
+  std::vector<DgswBrick> bricks;
+  std::vector<BrickLayout> layout;
+  std::vector<int32_t> elem_n;     // LGL extent per element
+  std::vector<int64_t> offset;     // doubles, n_elem + 1 entries
+  std::vector<int32_t> neighbor;   // 6 per element
+  std::vector<int32_t> instance;   // per element
+  std::vector<double> lower;       // 3 per element
+  std::vector<double> width;       // 3 per element
+  std::vector<uint64_t> element_id;
+  int64_t n_elem = 0;
+  int64_t n_points = 0;
+  bool block_ids_fit = true;       // every block id < 256
+  bool uniform = true;             // every element has the same extent
+  int max_n = 0;
+};
+
+// Validates a configuration and builds every host-side map.  On failure
+// returns false with a message in *err.
+bool build_domain(const DgswConfig& cfg, Domain* dom, std::string* err);
+
+}  // namespace dgsw

@@ -1,0 +1,53 @@
+// launch.hpp -- host-side launch descriptors shared by the kernel translation
+// units and the C-ABI layer.
+#pragma once
+
+#include <cstdint>
+#include <cuda_runtime.h>
+
+#include "common.cuh"
+
+namespace dgsw {
+
+// One fused RHS / RK-substep launch over elements of a uniform extent n.
+struct StageLaunch {
+  int n = 0;       // LGL points per dimension
+  int mode = 0;    // kModeRhs, kModeVolume, kModeStageFirst, kModeStage
+  const double* ucur = nullptr;
+  const double* u0 = nullptr;
+  double* unext = nullptr;
+  const int32_t* nbr = nullptr;  // 6 per element
+  const double* jac = nullptr;   // 3 per element (diagonal inverse Jacobian)
+  int64_t n_elem = 0;
+  StageCoef coef{0.0, 0.0, 1.0};
+  double gamma2 = 0.0;
+  EoTable eo{};
+};
+
+cudaError_t launch_stage_fp64(const StageLaunch& L, cudaStream_t s);
+
+// UpwindPenalty pointwise kernels (face_kernels.cu).
+cudaError_t launch_package_data(int64_t npts, const double* psi, const double* pi,
+                                const double* phi, const double* gamma2,
+                                const double* normal, const double* ndotv,
+                                double* packaged, cudaStream_t s);
+cudaError_t launch_boundary_terms(int64_t npts, const double* pkg_int,
+                                  const double* pkg_ext, double* out, cudaStream_t s);
+
+// Analytic initial data (init_kernels.cu).
+struct InitLaunch {
+  int kind = 0;
+  int64_t n_elem = 0;
+  const int32_t* elem_n = nullptr;
+  const int64_t* offset = nullptr;
+  const int32_t* instance = nullptr;
+  const double* lower = nullptr;
+  const double* width = nullptr;
+  const double* params = nullptr;  // device copy
+  const double* lgl_x = nullptr;   // [kMaxN+1][kMaxN] nodes table
+  double t = 0.0;
+  double* u = nullptr;
+};
+cudaError_t launch_initial_data(const InitLaunch& L, cudaStream_t s);
+
+}  // namespace dgsw

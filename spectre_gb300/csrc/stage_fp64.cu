@@ -1,0 +1,284 @@
+// stage_fp64.cu -- plain FP64 fused DG right-hand side + SSP-RK3 substep for
+// elements of one uniform LGL extent N with conforming (aligned, equal-N)
+// mortars on an affine (rectilinear) mesh.
+//
+// One launch computes, for every element, L(u) of ScalarWave::TimeDerivative
+// (TimeDerivative.cpp:37-44) from the logical derivatives along each axis
+// (PartialDerivatives.tpp:315-363) times the diagonal inverse Jacobian, adds
+// the UpwindPenalty boundary correction (UpwindPenalty.cpp:35-205) of each of
+// the six mortars lifted onto the GLL face (LiftFlux.hpp:57-61,
+// ApplyBoundaryCorrections.hpp:934-1043), and writes
+//   u_next = a * u0 + b * ucur + c * L(ucur)
+// which is Rk3HesthavenSsp::update_u_impl (Rk3HesthavenSsp.cpp:63-80) for the
+// stage coefficients (0,1,dt), (3/4,1/4,dt/4), (1/3,2/3,2dt/3).
+//
+// Work split: one group of N*N threads per element.  The four differentiated
+// fields (Pi, Phi_x, Phi_y, Phi_z) are staged in shared memory; three passes
+// follow, one per logical axis d.  In pass d each thread owns one line along
+// d: it differentiates Phi_d (into the running sum for dt Pi) and Pi (giving
+// dt Phi_d), adds the two face corrections at the ends of its line (the
+// neighbour's face value is read straight from its volume data: GLL faces are
+// volume points), and writes Phi_d's update.  The z pass completes dt Pi and
+// writes the Pi and Psi updates.
+//
+// Arithmetic: every operation on field values is FP64.  The FP64 pipe, not
+// HBM, binds this kernel on GB300, so the contraction uses the even/odd split
+// of the centro-antisymmetric D (N^2/2 + N fused multiply-adds per line
+// instead of N^2), only the six derivatives the system needs are formed
+// (d_i Phi_i and d_i Pi; d Psi enters only through gamma2), and the scalars
+// -c * (d xi/dx) are folded into the split tables once per element.
+#include <cstdio>
+
+#include "common.cuh"
+#include "launch.hpp"
+
+namespace dgsw {
+namespace {
+
+template <int N>
+struct Shape {
+  static constexpr int h = N / 2;          // even/odd pairs
+  static constexpr int odd = N % 2;
+  static constexpr int H = h + odd;        // rows formed by the split
+  static constexpr int NN = N * N;
+  static constexpr int NP = N * N * N;
+  static constexpr int TAB = 2 * H * h + H;  // doubles of one scaled table
+  static constexpr int SLOT = 5 * NP + 3 * TAB;  // smem doubles per element
+};
+
+// (scaled D) applied to one line with the even/odd split.
+template <int N>
+__device__ __forceinline__ void eo_line(const double (&u)[N], double (&out)[N],
+                                        const double* __restrict__ tab) {
+  using S = Shape<N>;
+  constexpr int h = S::h, H = S::H;
+  const double* A = tab;
+  const double* B = tab + H * h;
+  const double* M = tab + 2 * H * h;
+  double e[h], o[h];
+#pragma unroll
+  for (int j = 0; j < h; ++j) {
+    e[j] = u[j] + u[N - 1 - j];
+    o[j] = u[j] - u[N - 1 - j];
+  }
+#pragma unroll
+  for (int i = 0; i < h; ++i) {
+    double P = A[i * h] * e[0];
+#pragma unroll
+    for (int j = 1; j < h; ++j) P = fma(A[i * h + j], e[j], P);
+    if (S::odd) P = fma(M[i], u[h], P);
+    double Q = B[i * h] * o[0];
+#pragma unroll
+    for (int j = 1; j < h; ++j) Q = fma(B[i * h + j], o[j], Q);
+    out[i] = P + Q;
+    out[N - 1 - i] = Q - P;
+  }
+  if (S::odd) {
+    double Q = B[h * h] * o[0];
+#pragma unroll
+    for (int j = 1; j < h; ++j) Q = fma(B[h * h + j], o[j], Q);
+    out[h] = Q;
+  }
+}
+
+template <int N, int EPB, int MODE>
+__global__ void __launch_bounds__(N * N * EPB)
+    stage_fp64_kernel(const double* ucur, const double* u0, double* unext,
+                      const int32_t* __restrict__ nbr, const double* __restrict__ jac,
+                      int64_t n_elem, StageCoef coef, double gamma2, EoTable eo) {
+  using S = Shape<N>;
+  constexpr int NN = S::NN, NP = S::NP, TAB = S::TAB, h = S::h, H = S::H;
+  constexpr bool kBoundary = MODE != kModeVolume;
+  extern __shared__ double smem[];
+  const int slot = threadIdx.x / NN;
+  const int t = threadIdx.x - slot * NN;
+  const int64_t e = (int64_t)blockIdx.x * EPB + slot;
+  const bool active = e < n_elem;
+  double* F = smem + slot * S::SLOT;  // Pi, Phi_x, Phi_y, Phi_z of ucur
+  double* Sacc = F + 4 * NP;         // running c * (dt Pi)
+  double* T = Sacc + NP;             // three scaled split tables
+  const int64_t off = e * (int64_t)(kVars * NP);
+  const double c = coef.c;
+
+  double jd[3] = {0.0, 0.0, 0.0};
+  if (active) {
+    jd[0] = jac[3 * e];
+    jd[1] = jac[3 * e + 1];
+    jd[2] = jac[3 * e + 2];
+    const double* src = ucur + off + NP;
+    for (int q = t; q < 4 * NP; q += NN) F[q] = src[q];
+    for (int q = t; q < 3 * TAB; q += NN) {
+      const int d = q / TAB, r = q - d * TAB;
+      double v;
+      if (r < H * h)
+        v = eo.A[r / h][r % h];
+      else if (r < 2 * H * h)
+        v = eo.B[(r - H * h) / h][(r - H * h) % h];
+      else
+        v = eo.M[r - 2 * H * h];
+      T[q] = (-c * jd[d]) * v;
+    }
+  }
+  __syncthreads();
+
+  const int ta = t % N, tb = t / N;
+#pragma unroll 1
+  for (int d = 0; d < 3; ++d) {
+    if (active) {
+      int64_t base;
+      int stride;
+      if (d == 0) {
+        base = N * ta + NN * tb;
+        stride = 1;
+      } else if (d == 1) {
+        base = ta + NN * tb;
+        stride = N;
+      } else {
+        base = ta + N * tb;
+        stride = NN;
+      }
+      double up[N], uf[N], dF[N], dP[N];
+#pragma unroll
+      for (int i = 0; i < N; ++i) {
+        up[i] = F[base + i * stride];
+        uf[i] = F[(1 + d) * NP + base + i * stride];
+      }
+      const double* tab = T + d * TAB;
+      eo_line<N>(uf, dF, tab);  // -c J_d D Phi_d : c * (dt Pi) part
+      eo_line<N>(up, dP, tab);  // -c J_d D Pi    : c * (dt Phi_d)
+      if (kBoundary) {
+        // UpwindPenalty with char speeds (0, +1, -1) and a flat unit normal
+        // n = s e_d: D_Psi = 0, D_Pi = (w_int - w_ext)/2 and D_Phi_d = -s D_Pi
+        // with w = Pi - s Phi_d - gamma2 Psi (the exterior w uses the
+        // neighbour's fields and this element's s).  Lifted with
+        // -N(N-1)/2 |n| and scaled by c: G = -c N(N-1) J_d / 4.
+        const double G = -0.25 * c * (double)(N * (N - 1)) * jd[d];
+        const int64_t nlo = (int64_t)nbr[6 * e + 2 * d] * (kVars * NP);
+        const int64_t nhi = (int64_t)nbr[6 * e + 2 * d + 1] * (kVars * NP);
+        const int64_t lo_pt = base + (N - 1) * stride;  // neighbour's upper face
+        const int64_t hi_pt = base;                     // neighbour's lower face
+        double wi_lo = up[0] + uf[0];  // s = -1
+        double we_lo = ucur[nlo + NP + lo_pt] + ucur[nlo + (2 + d) * NP + lo_pt];
+        double wi_hi = up[N - 1] - uf[N - 1];  // s = +1
+        double we_hi = ucur[nhi + NP + hi_pt] - ucur[nhi + (2 + d) * NP + hi_pt];
+        if (gamma2 != 0.0) {
+          wi_lo = fma(-gamma2, ucur[off + base], wi_lo);
+          we_lo = fma(-gamma2, ucur[nlo + lo_pt], we_lo);
+          wi_hi = fma(-gamma2, ucur[off + base + (N - 1) * stride], wi_hi);
+          we_hi = fma(-gamma2, ucur[nhi + hi_pt], we_hi);
+        }
+        const double dw_lo = wi_lo - we_lo;
+        const double dw_hi = wi_hi - we_hi;
+        dF[0] = fma(G, dw_lo, dF[0]);
+        dP[0] = fma(G, dw_lo, dP[0]);
+        dF[N - 1] = fma(G, dw_hi, dF[N - 1]);
+        dP[N - 1] = fma(-G, dw_hi, dP[N - 1]);
+      }
+      if (gamma2 != 0.0) {
+        // gamma2 (d_d Psi - Phi_d) term of dt Phi_d (TimeDerivative.cpp:42-43)
+        // needs d_d Psi: one more line contraction along d.
+        double ups[N], dpsi[N];
+#pragma unroll
+        for (int i = 0; i < N; ++i) ups[i] = ucur[off + base + i * stride];
+        eo_line<N>(ups, dpsi, tab);  // -c J_d D Psi
+#pragma unroll
+        for (int i = 0; i < N; ++i) dP[i] = fma(-gamma2, dpsi[i] + c * uf[i], dP[i]);
+      }
+      // Phi_d update
+      double* outF = unext + off + (2 + d) * NP + base;
+#pragma unroll
+      for (int i = 0; i < N; ++i) {
+        double v;
+        if (MODE == kModeRhs || MODE == kModeVolume) {
+          v = dP[i];
+        } else if (MODE == kModeStageFirst) {
+          v = uf[i] + dP[i];
+        } else {
+          v = fma(coef.a, u0[off + (2 + d) * NP + base + i * stride], fma(coef.b, uf[i], dP[i]));
+        }
+        outF[i * stride] = v;
+      }
+      if (d < 2) {
+#pragma unroll
+        for (int i = 0; i < N; ++i) {
+          if (d == 0)
+            Sacc[base + i * stride] = dF[i];
+          else
+            Sacc[base + i * stride] += dF[i];
+        }
+      } else {
+        // z pass: dt Pi complete on this line; Pi and Psi updates
+#pragma unroll
+        for (int i = 0; i < N; ++i) {
+          const int64_t p = base + i * stride;
+          const double sp = Sacc[p] + dF[i];
+          double vpi, vpsi;
+          if (MODE == kModeRhs || MODE == kModeVolume) {
+            vpi = sp;
+            vpsi = -up[i];
+          } else if (MODE == kModeStageFirst) {
+            vpi = up[i] + sp;
+            vpsi = fma(-c, up[i], ucur[off + p]);
+          } else {
+            vpi = fma(coef.a, u0[off + NP + p], fma(coef.b, up[i], sp));
+            vpsi = fma(coef.a, u0[off + p], fma(coef.b, ucur[off + p], -c * up[i]));
+          }
+          unext[off + NP + p] = vpi;
+          unext[off + p] = vpsi;
+        }
+      }
+    }
+    if (d < 2) __syncthreads();
+  }
+}
+
+template <int N>
+constexpr int elems_per_block() {
+  return N <= 4 ? 16 : (N <= 6 ? 8 : (N <= 8 ? 4 : 2));
+}
+
+template <int N, int MODE>
+cudaError_t launch_n(const StageLaunch& L, cudaStream_t s) {
+  constexpr int EPB = elems_per_block<N>();
+  const size_t smem = (size_t)EPB * Shape<N>::SLOT * sizeof(double);
+  auto k = stage_fp64_kernel<N, EPB, MODE>;
+  cudaError_t err = cudaFuncSetAttribute(k, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+  if (err != cudaSuccess) return err;
+  const int64_t blocks = (L.n_elem + EPB - 1) / EPB;
+  if (blocks <= 0) return cudaSuccess;
+  k<<<(unsigned)blocks, N * N * EPB, smem, s>>>(L.ucur, L.u0, L.unext, L.nbr, L.jac, L.n_elem,
+                                                 L.coef, L.gamma2, L.eo);
+  return cudaGetLastError();
+}
+
+template <int N>
+cudaError_t launch_mode(const StageLaunch& L, cudaStream_t s) {
+  switch (L.mode) {
+    case kModeRhs: return launch_n<N, kModeRhs>(L, s);
+    case kModeVolume: return launch_n<N, kModeVolume>(L, s);
+    case kModeStageFirst: return launch_n<N, kModeStageFirst>(L, s);
+    case kModeStage: return launch_n<N, kModeStage>(L, s);
+    default: return cudaErrorInvalidValue;
+  }
+}
+
+}  // namespace
+
+cudaError_t launch_stage_fp64(const StageLaunch& L, cudaStream_t s) {
+  switch (L.n) {
+    case 2: return launch_mode<2>(L, s);
+    case 3: return launch_mode<3>(L, s);
+    case 4: return launch_mode<4>(L, s);
+    case 5: return launch_mode<5>(L, s);
+    case 6: return launch_mode<6>(L, s);
+    case 7: return launch_mode<7>(L, s);
+    case 8: return launch_mode<8>(L, s);
+    case 9: return launch_mode<9>(L, s);
+    case 10: return launch_mode<10>(L, s);
+    case 11: return launch_mode<11>(L, s);
+    case 12: return launch_mode<12>(L, s);
+    default: return cudaErrorInvalidValue;
+  }
+}
+
+}  // namespace dgsw

@@ -1,0 +1,389 @@
+"""Python mirror of SpECTRE's DG scalar-wave operator surface over libdgsw.so.
+
+The classes keep the reference's names and argument meaning:
+
+  ScalarWaveSystem   ScalarWave::System<3>            (Evolution/Systems/ScalarWave/System.hpp:39-57)
+  TimeDerivative     ScalarWave::TimeDerivative<3>    (Evolution/Systems/ScalarWave/TimeDerivative.cpp:13-45)
+  UpwindPenalty      ScalarWave::BoundaryCorrections::UpwindPenalty<3>
+                                                      (.../BoundaryCorrections/UpwindPenalty.cpp:35-205)
+  Rk3HesthavenSsp    TimeSteppers::Rk3HesthavenSsp    (Time/TimeSteppers/Rk3HesthavenSsp.cpp:21-81)
+  DgEvolution        the per-element DG step of EvolveScalarWave (ComputeTimeDerivative +
+                     ApplyBoundaryCorrections + UpdateU) for every element of one or more
+                     periodic bricks, owned by one libdgsw handle on one GPU.
+
+Every call goes through the C ABI in include/dgsw.h.  There is no CPU
+fallback: if the library is missing, importing this module raises.
+"""
+from __future__ import annotations
+
+import ctypes
+import math
+import os
+from dataclasses import dataclass
+from typing import Optional, Sequence
+
+import numpy as np
+
+_HERE = os.path.dirname(os.path.abspath(__file__))
+LIB_PATH = os.path.join(_HERE, "_lib", "libdgsw.so")
+
+DGSW_OK = 0
+STATUS_NAMES = {
+    -1: "DGSW_ERR_ARGUMENT",
+    -2: "DGSW_ERR_CUDA",
+    -3: "DGSW_ERR_UNSUPPORTED",
+    -4: "DGSW_ERR_NOT_FINITE",
+    -5: "DGSW_ERR_NO_DEVICE",
+}
+PRECISION_FP64 = 0
+PRECISION_MIXED = 1
+N_VARS = 5  # Psi, Pi, Phi_x, Phi_y, Phi_z
+N_PACKAGED = 16  # UpwindPenalty dg_package_field_tags doubles per face point
+
+
+class DgswError(RuntimeError):
+    def __init__(self, status: int, message: str):
+        super().__init__("%s (%d): %s" % (STATUS_NAMES.get(status, "?"), status, message))
+        self.status = status
+
+
+class DgswBrick(ctypes.Structure):
+    _fields_ = [("lower", ctypes.c_double * 3), ("upper", ctypes.c_double * 3),
+                ("elements", ctypes.c_int32 * 3)]
+
+
+class DgswConfig(ctypes.Structure):
+    _fields_ = [("system", ctypes.c_int32), ("boundary_correction", ctypes.c_int32),
+                ("time_stepper", ctypes.c_int32), ("precision", ctypes.c_int32),
+                ("n_instances", ctypes.c_int32), ("bricks", ctypes.POINTER(DgswBrick)),
+                ("points_per_element", ctypes.POINTER(ctypes.c_int32)),
+                ("uniform_points", ctypes.c_int32), ("gamma2", ctypes.c_double),
+                ("device", ctypes.c_int32)]
+
+
+_P = ctypes.c_void_p
+_D = ctypes.c_double
+_I = ctypes.c_int
+_I64 = ctypes.c_int64
+_SIGNATURES = {
+    "dgsw_abi_version": (_I, []),
+    "dgsw_last_error": (ctypes.c_char_p, [_P]),
+    "dgsw_create": (_I, [ctypes.POINTER(DgswConfig), ctypes.POINTER(_P)]),
+    "dgsw_destroy": (_I, [_P]),
+    "dgsw_sizes": (_I, [_P, ctypes.POINTER(_I64), ctypes.POINTER(_I64), ctypes.POINTER(_I64)]),
+    "dgsw_stream": (_P, [_P]),
+    "dgsw_synchronize": (_I, [_P]),
+    "dgsw_set_state": (_I, [_P, _P]),
+    "dgsw_get_state": (_I, [_P, _P]),
+    "dgsw_set_state_device": (_I, [_P, _P]),
+    "dgsw_get_state_device": (_I, [_P, _P]),
+    "dgsw_set_initial_data": (_I, [_P, _I, _P, _D]),
+    "dgsw_rhs": (_I, [_P, _P, _P]),
+    "dgsw_rhs_device": (_I, [_P, _P, _P]),
+    "dgsw_volume_rhs_device": (_I, [_P, _P, _P]),
+    "dgsw_package_data_device": (_I, [_I64, _P, _P, _P, _P, _P, _P, _P, _P]),
+    "dgsw_boundary_terms_device": (_I, [_I64, _P, _P, _P, _P]),
+    "dgsw_step": (_I, [_P, _I, _D]),
+    "dgsw_substep": (_I, [_P, _I, _D]),
+    "dgsw_lgl_points_weights": (_I, [_I, _P, _P]),
+    "dgsw_differentiation_matrix": (_I, [_I, _P]),
+    "dgsw_mortar_projections": (_I, [_I, _I, _P, _P]),
+    "dgsw_index_maps": (_I, [ctypes.POINTER(DgswConfig), _P, _P, _P]),
+    "dgsw_count_elements": (_I, [ctypes.POINTER(DgswConfig), ctypes.POINTER(_I64),
+                                 ctypes.POINTER(_I64)]),
+}
+
+_lib_handle = None
+
+
+def lib() -> ctypes.CDLL:
+    """The loaded libdgsw.so.  Raises if it has not been built."""
+    global _lib_handle
+    if _lib_handle is None:
+        if not os.path.exists(LIB_PATH):
+            raise ImportError("libdgsw.so is not built (%s); run "
+                              "`python -c 'import __graft_entry__ as g; g.build()'`" % LIB_PATH)
+        L = ctypes.CDLL(LIB_PATH)
+        for name, (res, args) in _SIGNATURES.items():
+            fn = getattr(L, name)
+            fn.restype = res
+            fn.argtypes = args
+        _lib_handle = L
+    return _lib_handle
+
+
+def exported_symbols() -> Sequence[str]:
+    return tuple(_SIGNATURES)
+
+
+def _check(status: int, handle=None):
+    if status != DGSW_OK:
+        msg = lib().dgsw_last_error(handle)
+        raise DgswError(status, msg.decode() if msg else "")
+
+
+def _ptr(a) -> int:
+    """Address of a numpy array or torch tensor (contiguous)."""
+    if a is None:
+        return None
+    if isinstance(a, np.ndarray):
+        assert a.flags["C_CONTIGUOUS"]
+        return a.ctypes.data
+    if hasattr(a, "data_ptr"):
+        assert a.is_contiguous()
+        return a.data_ptr()
+    raise TypeError("expected numpy array or torch tensor")
+
+
+# ----------------------------------------------------------------- spectral
+
+
+def lgl_points_weights(n: int):
+    """Spectral::collocation_points / quadrature_weights <Legendre, GaussLobatto>."""
+    x = np.zeros(n)
+    w = np.zeros(n)
+    _check(lib().dgsw_lgl_points_weights(n, _ptr(x), _ptr(w)))
+    return x, w
+
+
+def differentiation_matrix(n: int) -> np.ndarray:
+    """Spectral::differentiation_matrix (row-major n x n)."""
+    D = np.zeros((n, n))
+    _check(lib().dgsw_differentiation_matrix(n, _ptr(D)))
+    return D
+
+
+def mortar_projections(n_face: int, n_mortar: int):
+    """(face->mortar [nm x ne], mortar->face [ne x nm]) for ChildSize::Full."""
+    a = np.zeros((n_mortar, n_face))
+    b = np.zeros((n_face, n_mortar))
+    _check(lib().dgsw_mortar_projections(n_face, n_mortar, _ptr(a), _ptr(b)))
+    return a, b
+
+
+# ------------------------------------------------------------------ domain
+
+
+@dataclass
+class Brick:
+    """Periodic [lower, upper]^3 split into elements[d] elements along d."""
+    elements: Sequence[int]
+    lower: Sequence[float] = (0.0, 0.0, 0.0)
+    upper: Sequence[float] = (2 * math.pi, 2 * math.pi, 2 * math.pi)
+
+
+class _ConfigHolder:
+    """Keeps the ctypes arrays a DgswConfig points to alive."""
+
+    def __init__(self, bricks, points, precision=PRECISION_FP64, gamma2=0.0, device=0):
+        self.bricks = (DgswBrick * len(bricks))()
+        for i, b in enumerate(bricks):
+            self.bricks[i].lower[:] = [float(v) for v in b.lower]
+            self.bricks[i].upper[:] = [float(v) for v in b.upper]
+            self.bricks[i].elements[:] = [int(v) for v in b.elements]
+        self.points = None
+        uniform = 0
+        if np.ndim(points) == 0:
+            uniform = int(points)
+        else:
+            self.points = np.ascontiguousarray(points, dtype=np.int32)
+        self.cfg = DgswConfig()
+        self.cfg.system = 0
+        self.cfg.boundary_correction = 0
+        self.cfg.time_stepper = 0
+        self.cfg.precision = precision
+        self.cfg.n_instances = len(bricks)
+        self.cfg.bricks = ctypes.cast(self.bricks, ctypes.POINTER(DgswBrick))
+        self.cfg.points_per_element = (
+            self.points.ctypes.data_as(ctypes.POINTER(ctypes.c_int32))
+            if self.points is not None else None)
+        self.cfg.uniform_points = uniform
+        self.cfg.gamma2 = float(gamma2)
+        self.cfg.device = device
+
+
+def index_maps(bricks, points):
+    """(element_ids uint64, neighbors int32 [E,6], mortar extents int32 [E,6], fits)."""
+    h = _ConfigHolder(bricks, points)
+    ne = _I64()
+    nd = _I64()
+    _check(lib().dgsw_count_elements(ctypes.byref(h.cfg), ctypes.byref(ne), ctypes.byref(nd)))
+    E = ne.value
+    ids = np.zeros(E, dtype=np.uint64)
+    nbr = np.zeros((E, 6), dtype=np.int32)
+    mort = np.zeros((E, 6), dtype=np.int32)
+    st = lib().dgsw_index_maps(ctypes.byref(h.cfg), _ptr(ids), _ptr(nbr), _ptr(mort))
+    if st not in (DGSW_OK, -3):
+        _check(st)
+    return ids, nbr, mort, st == DGSW_OK
+
+
+# ------------------------------------------------------------------ system
+
+
+class ScalarWaveSystem:
+    """ScalarWave::System<3>: variables {Psi, Pi, Phi_i}, no fluxes."""
+    volume_dim = 3
+    variables = ("Psi", "Pi", "Phi")
+    number_of_components = N_VARS
+    has_primitive_and_conservative_vars = False
+
+
+class UpwindPenalty:
+    """ScalarWave::BoundaryCorrections::UpwindPenalty<3> on device face data.
+
+    Fields are torch CUDA float64 tensors: scalars of shape [npts], covectors
+    of shape [3, npts].  Packaged data is a [16, npts] tensor in
+    dg_package_field_tags order.
+    """
+
+    def dg_package_data(self, psi, pi, phi, constraint_gamma2, normal_covector,
+                        mesh_velocity=None, normal_dot_mesh_velocity=None, stream=None):
+        import torch
+        npts = psi.numel()
+        out = torch.empty((N_PACKAGED, npts), dtype=torch.float64, device=psi.device)
+        _check(lib().dgsw_package_data_device(
+            npts, _ptr(psi), _ptr(pi), _ptr(phi), _ptr(constraint_gamma2),
+            _ptr(normal_covector),
+            _ptr(normal_dot_mesh_velocity) if normal_dot_mesh_velocity is not None else None,
+            _ptr(out), stream))
+        # max over the char speeds, as the reference's return value
+        max_speed = float(out[13:16].max()) if npts else float("-inf")
+        return out, max_speed
+
+    def dg_boundary_terms(self, packaged_int, packaged_ext, dg_formulation="StrongInertial",
+                          stream=None):
+        import torch
+        npts = packaged_int.shape[1]
+        out = torch.empty((N_VARS, npts), dtype=torch.float64, device=packaged_int.device)
+        _check(lib().dgsw_boundary_terms_device(npts, _ptr(packaged_int), _ptr(packaged_ext),
+                                                _ptr(out), stream))
+        return out
+
+
+class Rk3HesthavenSsp:
+    """TimeSteppers::Rk3HesthavenSsp: 3-stage, 3rd-order SSP Runge-Kutta."""
+
+    def order(self) -> int:
+        return 3
+
+    def number_of_substeps(self) -> int:
+        return 3
+
+    def number_of_past_steps(self) -> int:
+        return 0
+
+    def stable_step(self) -> float:
+        c = (4.0 + math.sqrt(17.0)) ** (1.0 / 3.0)
+        return 0.5 * (1.0 + c - 1.0 / c)
+
+    def substep_time_fractions(self):
+        """Fractions of dt at which substeps 0, 1, 2 evaluate the RHS."""
+        return (0.0, 1.0, 0.5)
+
+
+class DgEvolution:
+    """All elements of one or more periodic bricks on one GPU (one handle)."""
+
+    def __init__(self, bricks, points, precision=PRECISION_FP64, gamma2=0.0, device=0):
+        if isinstance(bricks, Brick):
+            bricks = [bricks]
+        self._cfg = _ConfigHolder(bricks, points, precision, gamma2, device)
+        h = _P()
+        _check(lib().dgsw_create(ctypes.byref(self._cfg.cfg), ctypes.byref(h)))
+        self._h = h
+        ne, nd, npt = _I64(), _I64(), _I64()
+        _check(lib().dgsw_sizes(h, ctypes.byref(ne), ctypes.byref(nd), ctypes.byref(npt)), h)
+        self.n_elements = ne.value
+        self.state_size = nd.value
+        self.grid_points = npt.value
+        self.bricks = list(bricks)
+        self.points = points
+        self.precision = precision
+        self.gamma2 = gamma2
+        self.device = device
+
+    def close(self):
+        if getattr(self, "_h", None):
+            lib().dgsw_destroy(self._h)
+            self._h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    def __enter__(self):
+        return self
+
+    def __exit__(self, *a):
+        self.close()
+
+    @property
+    def handle(self):
+        return self._h
+
+    def stream_ptr(self) -> int:
+        return lib().dgsw_stream(self._h) or 0
+
+    def synchronize(self):
+        _check(lib().dgsw_synchronize(self._h), self._h)
+
+    # state ---------------------------------------------------------------
+    def set_state(self, u):
+        """u: numpy float64 host array or torch float64 tensor (host or cuda)."""
+        if hasattr(u, "is_cuda") and u.is_cuda:
+            _check(lib().dgsw_set_state_device(self._h, _ptr(u)), self._h)
+            self.synchronize()
+        else:
+            a = u if isinstance(u, np.ndarray) else u.numpy()
+            a = np.ascontiguousarray(a, dtype=np.float64)
+            assert a.size == self.state_size
+            _check(lib().dgsw_set_state(self._h, _ptr(a)), self._h)
+            self.synchronize()
+
+    def get_state(self, out=None):
+        if out is not None and hasattr(out, "is_cuda") and out.is_cuda:
+            _check(lib().dgsw_get_state_device(self._h, _ptr(out)), self._h)
+            self.synchronize()
+            return out
+        a = np.empty(self.state_size) if out is None else out
+        _check(lib().dgsw_get_state(self._h, _ptr(a)), self._h)
+        return a
+
+    def set_initial_data(self, kind: str, params, t: float = 0.0):
+        k = {"plane_wave": 0, "gaussian": 1}[kind]
+        p = np.ascontiguousarray(params, dtype=np.float64).ravel()
+        _check(lib().dgsw_set_initial_data(self._h, k, _ptr(p), float(t)), self._h)
+
+    # TimeDerivative + BoundaryCorrection --------------------------------
+    def rhs(self, u):
+        """du/dt of a host state (numpy) or device state (torch cuda)."""
+        if hasattr(u, "is_cuda") and u.is_cuda:
+            import torch
+            out = torch.empty_like(u)
+            _check(lib().dgsw_rhs_device(self._h, _ptr(u), _ptr(out)), self._h)
+            self.synchronize()
+            return out
+        a = np.ascontiguousarray(u, dtype=np.float64)
+        out = np.empty_like(a)
+        _check(lib().dgsw_rhs(self._h, _ptr(a), _ptr(out)), self._h)
+        return out
+
+    def volume_rhs(self, u_dev):
+        import torch
+        out = torch.empty_like(u_dev)
+        _check(lib().dgsw_volume_rhs_device(self._h, _ptr(u_dev), _ptr(out)), self._h)
+        self.synchronize()
+        return out
+
+    # TimeStepper ---------------------------------------------------------
+    def step(self, n_steps: int, dt: float, sync: bool = True):
+        _check(lib().dgsw_step(self._h, int(n_steps), float(dt)), self._h)
+        if sync:
+            self.synchronize()
+
+    def substep(self, k: int, dt: float):
+        _check(lib().dgsw_substep(self._h, int(k), float(dt)), self._h)
+        self.synchronize()

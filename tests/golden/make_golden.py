@@ -1,0 +1,180 @@
+"""Generate the golden fixtures in this directory from the reference's tests.
+
+Run in a container that has the SpECTRE source tree (release 2024.09.29) at
+SPECTRE_ROOT (default /root/reference).  The generated JSON files are
+committed; nothing at test time reads the reference tree.
+
+Fixtures:
+  lgl_golden.json      LGL points/weights, D-matrices and Vandermonde matrices
+                       read as text from
+                       tests/Unit/NumericalAlgorithms/Spectral/Test_LegendreGaussLobatto.cpp
+  upwind_golden.json   seeded inputs and the outputs of the reference's pypp
+                       golden functions
+                       tests/Unit/Evolution/Systems/ScalarWave/BoundaryCorrections/UpwindPenalty.py
+                       (dg_package_data, dg_boundary_terms), evaluated point
+                       by point as pypp does for DataVector arguments.
+"""
+import importlib.util
+import json
+import os
+import re
+import sys
+
+import numpy as np
+
+ROOT = os.environ.get("SPECTRE_ROOT", "/root/reference")
+HERE = os.path.dirname(os.path.abspath(__file__))
+
+
+def _cpp_expr_to_py(s):
+    s = re.sub(r"Matrix\(\s*\{", "Matrix({", s)
+    s = re.sub(r"\}\s*\)", "})", s)
+    s = s.replace("DataVector{", "np.array([").replace("Matrix({", "np.array([")
+    # close the constructors: count braces by a tiny state machine
+    out, depth_stack = [], []
+    i = 0
+    while i < len(s):
+        c = s[i]
+        if s.startswith("np.array([", i):
+            out.append("np.array([")
+            depth_stack.append("arr")
+            i += len("np.array([")
+            continue
+        if c == "{":
+            out.append("[")
+            depth_stack.append("br")
+        elif c == "}":
+            kind = depth_stack.pop()
+            out.append("])" if kind == "arr" else "]")
+            if kind == "arr" and i + 1 < len(s) and s[i + 1] == ")":
+                i += 1  # Matrix({ ... }) closing paren
+        else:
+            out.append(c)
+        i += 1
+    return "".join(out)
+
+
+def _split_args(text):
+    depth, cur, args = 0, [], []
+    for c in text:
+        if c in "({[":
+            depth += 1
+        elif c in ")}]":
+            depth -= 1
+        if c == "," and depth == 0:
+            args.append("".join(cur))
+            cur = []
+        else:
+            cur.append(c)
+    args.append("".join(cur))
+    return [a.strip() for a in args]
+
+
+def _calls(src, fname):
+    out = []
+    for m in re.finditer(re.escape(fname) + r"\(", src):
+        if src[m.start() - 5 : m.start()].strip().endswith("void"):
+            continue
+        i, depth = m.end(), 1
+        while depth:
+            depth += {"(": 1, ")": -1}.get(src[i], 0)
+            i += 1
+        out.append(_split_args(src[m.end() : i - 1]))
+    return out
+
+
+def lgl_golden():
+    path = os.path.join(
+        ROOT, "tests/Unit/NumericalAlgorithms/Spectral/Test_LegendreGaussLobatto.cpp")
+    src = open(path).read()
+    src = re.sub(r"//[^\n]*", "", src)
+    res = {"source": "tests/Unit/NumericalAlgorithms/Spectral/Test_LegendreGaussLobatto.cpp",
+           "points_weights": {}, "diff_matrix": {}, "modal_to_nodal": {},
+           "nodal_to_modal": {}}
+    for args in _calls(src, "test_points_and_weights"):
+        if len(args) != 3 or not args[0].isdigit():
+            continue
+        n = int(args[0])
+        x = eval(_cpp_expr_to_py(args[1]), {"np": np})
+        w = eval(_cpp_expr_to_py(args[2]), {"np": np})
+        res["points_weights"][n] = {"x": list(map(float, x)), "w": list(map(float, w))}
+    for key, fname in (("diff_matrix", "test_diff_matrix"),
+                       ("modal_to_nodal", "test_modal_to_nodal_matrix"),
+                       ("nodal_to_modal", "test_nodal_to_modal_matrix")):
+        for args in _calls(src, fname):
+            if len(args) != 2 or not args[0].isdigit():
+                continue
+            n = int(args[0])
+            M = eval(_cpp_expr_to_py(args[1]), {"np": np})
+            res[key][n] = np.asarray(M, dtype=float).tolist()
+    return res
+
+
+def upwind_golden(seed=20241204, npts=40):
+    path = os.path.join(
+        ROOT, "tests/Unit/Evolution/Systems/ScalarWave/BoundaryCorrections/UpwindPenalty.py")
+    spec = importlib.util.spec_from_file_location("ref_upwind", path)
+    mod = importlib.util.module_from_spec(spec)
+    spec.loader.exec_module(mod)
+    rng = np.random.default_rng(seed)
+    cases = []
+    for side in range(2):
+        psi = rng.uniform(-1, 1, npts)
+        pi = rng.uniform(-1, 1, npts)
+        phi = rng.uniform(-1, 1, (3, npts))
+        g2 = rng.uniform(0, 2, npts)
+        nrm = rng.normal(size=(3, npts))
+        nrm /= np.linalg.norm(nrm, axis=0)
+        cases.append((psi, pi, phi, g2, nrm))
+    pkgs = []
+    for (psi, pi, phi, g2, nrm) in cases:
+        pk = np.zeros((16, npts))
+        for p in range(npts):
+            r = mod.dg_package_data(psi[p], pi[p], phi[:, p], g2[p], nrm[:, p], None, None)
+            flat = [np.atleast_1d(np.asarray(f, dtype=float)) for f in r]
+            pk[:, p] = np.concatenate(flat)
+        pkgs.append(pk)
+    bt = np.zeros((5, npts))
+    for p in range(npts):
+        def fields(pk):
+            return (pk[0, p], pk[1:4, p], pk[4, p], pk[5, p], pk[6:9, p], pk[9:12, p],
+                    pk[12, p], pk[13:16, p])
+        r = mod.dg_boundary_terms(*fields(pkgs[0]), *fields(pkgs[1]), True)
+        bt[:, p] = np.concatenate([np.atleast_1d(np.asarray(f, dtype=float)) for f in r])
+    # exterior package with non-default char speeds so every Theta branch is hit
+    sp = np.array([[0.0, 1.0, -1.0], [-0.3, 0.7, -1.3], [0.4, 1.4, -0.6]])
+    pk_int2 = pkgs[0].copy()
+    pk_ext2 = pkgs[1].copy()
+    for p in range(npts):
+        pk_int2[13:16, p] = sp[p % 3]
+        pk_ext2[13:16, p] = sp[(p + 1) % 3]
+    bt2 = np.zeros((5, npts))
+    for p in range(npts):
+        def fields2(pk):
+            return (pk[0, p], pk[1:4, p], pk[4, p], pk[5, p], pk[6:9, p], pk[9:12, p],
+                    pk[12, p], pk[13:16, p])
+        r = mod.dg_boundary_terms(*fields2(pk_int2), *fields2(pk_ext2), True)
+        bt2[:, p] = np.concatenate([np.atleast_1d(np.asarray(f, dtype=float)) for f in r])
+    return {
+        "source": "tests/Unit/Evolution/Systems/ScalarWave/BoundaryCorrections/UpwindPenalty.py",
+        "seed": seed,
+        "npts": npts,
+        "inputs": [{"psi": c[0].tolist(), "pi": c[1].tolist(), "phi": c[2].tolist(),
+                    "gamma2": c[3].tolist(), "normal": c[4].tolist()} for c in cases],
+        "packaged": [p.tolist() for p in pkgs],
+        "boundary_terms": bt.tolist(),
+        "speeds_case": {"pkg_int": pk_int2.tolist(), "pkg_ext": pk_ext2.tolist(),
+                        "boundary_terms": bt2.tolist()},
+    }
+
+
+def main():
+    with open(os.path.join(HERE, "lgl_golden.json"), "w") as f:
+        json.dump(lgl_golden(), f, indent=1)
+    with open(os.path.join(HERE, "upwind_golden.json"), "w") as f:
+        json.dump(upwind_golden(), f)
+    print("wrote fixtures to", HERE)
+
+
+if __name__ == "__main__":
+    sys.exit(main())

@@ -1,0 +1,134 @@
+"""Host-only parts of libdgsw.so (no GPU): exports, spectral setup, index maps,
+argument validation."""
+import ctypes
+import json
+import os
+import re
+
+import numpy as np
+import pytest
+
+from spectre_gb300 import dgsw
+from spectre_gb300.dgsw import Brick
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+ROOT = os.path.dirname(HERE)
+LGL = json.load(open(os.path.join(HERE, "golden", "lgl_golden.json")))
+
+
+def header_functions():
+    src = open(os.path.join(ROOT, "include", "dgsw.h")).read()
+    src = re.sub(r"/\*.*?\*/", "", src, flags=re.S)
+    return sorted(set(re.findall(r"\b(dgsw_[a-z0-9_]+)\s*\(", src)))
+
+
+def test_library_exports_every_header_symbol(dgsw_lib):
+    names = header_functions()
+    assert len(names) >= 20
+    L = dgsw_lib.lib()
+    for n in names:
+        assert hasattr(L, n), n
+    # the Python binding declares a signature for every exported function
+    assert set(names) <= set(dgsw.exported_symbols()) | {"dgsw_stream"}
+    assert L.dgsw_abi_version() == 1
+
+
+@pytest.mark.parametrize("n", sorted(int(k) for k in LGL["points_weights"]))
+def test_product_lgl_matches_golden(dgsw_lib, oracle, n):
+    x, w = dgsw.lgl_points_weights(n)
+    g = LGL["points_weights"][str(n)]
+    np.testing.assert_allclose(x, g["x"], rtol=1e-14, atol=1e-14)
+    np.testing.assert_allclose(w, g["w"], rtol=1e-8, atol=1e-8)
+    xo, wo = oracle.lgl(n)
+    np.testing.assert_allclose(x, xo, rtol=0, atol=4e-16)
+    np.testing.assert_allclose(w, wo, rtol=1e-14)
+
+
+@pytest.mark.parametrize("n", range(2, 21))
+def test_product_diff_matrix_matches_oracle(dgsw_lib, oracle, n):
+    D = dgsw.differentiation_matrix(n)
+    np.testing.assert_allclose(D, oracle.diff_matrix(n), rtol=1e-13, atol=1e-12)
+    if str(n) in LGL["diff_matrix"]:
+        np.testing.assert_allclose(D, np.array(LGL["diff_matrix"][str(n)]), rtol=1e-13,
+                                   atol=1e-13)
+
+
+def test_product_mortar_projections_match_oracle(dgsw_lib, oracle):
+    for ne in range(2, 13):
+        for nm in range(ne, 13):
+            a, b = dgsw.mortar_projections(ne, nm)
+            np.testing.assert_allclose(a, oracle.proj_face_to_mortar(ne, nm), atol=1e-14)
+            np.testing.assert_allclose(b, oracle.proj_mortar_to_face(ne, nm), atol=2e-13)
+
+
+CASES = [
+    [Brick((4, 4, 4))],                     # config 1 lattice
+    [Brick((32, 32, 32))],                  # config 2 lattice (32,768 elements)
+    [Brick((8, 8, 8))],                     # config 4 lattice
+    [Brick((3, 6, 5)), Brick((2, 7, 8)), Brick((1, 1, 1))],
+]
+
+
+@pytest.mark.parametrize("case", range(len(CASES)))
+def test_index_maps_bit_exact(dgsw_lib, oracle, case):
+    bricks = CASES[case]
+    ids, nbr, mort, fits = dgsw.index_maps(bricks, 6)
+    oids, onbr, _, _, ofits = oracle.index_maps(bricks)
+    assert fits == ofits
+    np.testing.assert_array_equal(ids, oids)
+    np.testing.assert_array_equal(nbr, onbr)
+    assert (mort == 6).all()
+
+
+def test_index_maps_random_batched(dgsw_lib, oracle):
+    # config-3-like batches: per-axis counts in {2..8}, per-element N in {4..10}
+    rng = np.random.default_rng(7)
+    bricks = [Brick(tuple(int(v) for v in rng.integers(2, 9, 3))) for _ in range(24)]
+    E = oracle.num_elements(bricks)
+    pts = rng.integers(4, 11, E).astype(np.int32)
+    ids, nbr, mort, fits = dgsw.index_maps(bricks, pts)
+    oids, onbr, _, _, ofits = oracle.index_maps(bricks)
+    assert fits == ofits
+    np.testing.assert_array_equal(ids, oids)
+    np.testing.assert_array_equal(nbr, onbr)
+    np.testing.assert_array_equal(mort, np.maximum(pts[:, None], pts[onbr]))
+
+
+def test_index_maps_block_id_overflow(dgsw_lib, oracle):
+    # 7x7x7 odd counts need 343 blocks: more than the 8 block-id bits hold
+    ids, nbr, mort, fits = dgsw.index_maps([Brick((7, 7, 7))], 4)
+    assert not fits
+    _, onbr, _, _, ofits = oracle.index_maps([Brick((7, 7, 7))])
+    assert not ofits
+    np.testing.assert_array_equal(nbr, onbr)
+
+
+@pytest.mark.parametrize("bad", [
+    dict(bricks=[Brick((0, 1, 1))], points=4),
+    dict(bricks=[Brick((1, 1, 1), (0, 0, 0), (0, 1, 1))], points=4),
+    dict(bricks=[Brick((2, 2, 2))], points=1),
+    dict(bricks=[Brick((2, 2, 2))], points=13),
+    dict(bricks=[Brick((5000, 1, 1))], points=4),
+])
+def test_bad_configs_rejected(dgsw_lib, bad):
+    with pytest.raises(dgsw.DgswError) as ei:
+        dgsw.index_maps(bad["bricks"], bad["points"])
+    assert ei.value.status == -1
+
+
+def test_bad_spectral_arguments(dgsw_lib):
+    L = dgsw_lib.lib()
+    x = np.zeros(40)
+    assert L.dgsw_lgl_points_weights(1, x.ctypes.data, x.ctypes.data) == -1
+    assert L.dgsw_lgl_points_weights(21, x.ctypes.data, x.ctypes.data) == -1
+    assert L.dgsw_differentiation_matrix(0, x.ctypes.data) == -1
+    assert L.dgsw_mortar_projections(5, 4, None, None) == -1
+    assert b"ne <= nm" in L.dgsw_last_error(None)
+
+
+def test_null_handle_is_an_error_not_a_crash(dgsw_lib):
+    L = dgsw_lib.lib()
+    assert L.dgsw_step(None, 1, 1e-3) == -1
+    assert L.dgsw_rhs(None, None, None) == -1
+    assert L.dgsw_destroy(None) == 0
+    assert L.dgsw_create(None, None) == -1

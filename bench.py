@@ -38,11 +38,20 @@ UNIT = "grid-point RHS/s"
 ELEMS = 32
 N_PTS = 8
 DT = 2e-4
-BYTES_PER_POINT_LAUNCH = (80.0 + 120.0 + 120.0) / 3.0  # compulsory HBM bytes per point per stage
+# Compulsory HBM bytes per grid point per stage launch.  Plain FP64: read
+# ucur (40 B) + write unext (40 B) + read u0 on stages 2 and 3 (40 B).
+BYTES_PER_POINT_LAUNCH = (80.0 + 120.0 + 120.0) / 3.0
+# Mixed: stage 1 reads u0 (40 B) and writes d1 in FP32 (20 B); stage 2 reads
+# d1 and writes s2 (20 + 20 B); stage 3 reads s2, d1 (FP32) and u0, and
+# writes u (20 + 20 + 40 + 40 B).
+MIXED_BYTES_PER_POINT_LAUNCH = (60.0 + 40.0 + 120.0) / 3.0
 # FP64 pipe instructions per point per stage of the plain kernel at N = 8
-# (even/odd contraction: 6 per derivative x 6 derivatives, dt Pi sum 2,
-# RK combination ~10, face corrections ~3); counted from the kernel source.
-FP64_OPS_PER_POINT_STAGE = 50.0
+# (even/odd contraction 6 per derivative x 6, dt Pi sum 2, RK update 5-11,
+# face corrections ~3.75); the ncu capture of the 20^3 case measured
+# 42.7 / 47.6 / 47.6 per point for the three stages.
+FP64_INST_PER_POINT_STAGE = 46.0
+# DFMA / DADD throughput measured on this machine's GB300 (0.505 T inst/s)
+FP64_PEAK_TINST = 0.505
 
 
 def load_peaks():
@@ -180,26 +189,21 @@ def workload_config(elems=ELEMS):
             "precision": "plain FP64", "l2": "inputs larger than L2 (671 MB state), no flush"}
 
 
-def run_ours(args):
+def time_path(args, precision, dev, rank, ws, sample_clocks):
+    """Times args.steps SSP-RK3 steps of one precision; returns the numbers
+    and the final state (host copy)."""
     import torch
     from spectre_gb300 import Brick, DgEvolution
-    ws, rank, local = dist_env()
-    if ws > 1:
-        import torch.distributed as dist
-        torch.cuda.set_device(local)
-        dist.init_process_group("nccl", device_id=torch.device("cuda", local))
-    dev = local if ws > 1 else 0
-    torch.cuda.set_device(dev)
-    peaks, peak_kind = load_peaks()
     bricks = [Brick((args.elements, args.elements, args.elements))]
     params = np.array([[1.0, 0.5, math.pi, math.pi, math.pi]])
-    ev = DgEvolution(bricks, N_PTS, device=dev)
+    ev = DgEvolution(bricks, N_PTS, precision=precision, device=dev)
     ev.set_initial_data("gaussian", params)
     stream = torch.cuda.ExternalStream(ev.stream_ptr(), device=dev)
-    for _ in range(max(args.warmup, 3)):
+    warm = max(args.warmup, 3)
+    for _ in range(warm):
         ev.step(1, DT, sync=False)
     ev.synchronize()
-    sampler = ClockSampler(dev) if rank == 0 else None
+    sampler = ClockSampler(dev) if (rank == 0 and sample_clocks) else None
     if sampler:
         sampler.start()
         time.sleep(0.3)
@@ -208,10 +212,9 @@ def run_ours(args):
     torch.cuda.synchronize()
     e0 = torch.cuda.Event(enable_timing=True)
     e1 = torch.cuda.Event(enable_timing=True)
-    with torch.cuda.stream(stream):
-        e0.record(stream)
-        ev.step(args.steps, DT, sync=False)
-        e1.record(stream)
+    e0.record(stream)
+    ev.step(args.steps, DT, sync=False)
+    e1.record(stream)
     e1.synchronize()
     torch.cuda.synchronize()
     ms = e0.elapsed_time(e1)
@@ -221,6 +224,24 @@ def run_ours(args):
         ms = float(t.item())
         torch.distributed.barrier()
     clocks = sampler.stop() if sampler else None
+    state = ev.get_state()
+    return ev, ms, clocks, state, warm
+
+
+def run_ours(args):
+    import torch
+    from spectre_gb300 import PRECISION_FP64, PRECISION_MIXED
+    ws, rank, local = dist_env()
+    if ws > 1:
+        import torch.distributed as dist
+        torch.cuda.set_device(local)
+        dist.init_process_group("nccl", device_id=torch.device("cuda", local))
+    dev = local if ws > 1 else 0
+    torch.cuda.set_device(dev)
+    peaks, peak_kind = load_peaks()
+    hbm = peaks.get("hbm_gbs")
+
+    ev, ms, clocks, state64, warm = time_path(args, PRECISION_FP64, dev, rank, ws, True)
     points = ev.grid_points
     value = points * 3 * args.steps * ws / (ms * 1e-3)
     launch_ms = ms / (3 * args.steps)
@@ -228,53 +249,73 @@ def run_ours(args):
 
     # end to end through the C ABI with pinned host buffers: H2D of the state,
     # one step, D2H of the new state, every step
-    e2e = None
-    if rank == 0 or ws > 1:
-        host = torch.empty(ev.state_size, dtype=torch.float64, pin_memory=True)
-        hnp = host.numpy()
+    host = torch.empty(ev.state_size, dtype=torch.float64, pin_memory=True)
+    hnp = host.numpy()
+    ev.get_state(hnp)
+    k2 = max(1, min(args.steps, 10))
+    torch.cuda.synchronize()
+    t0 = time.perf_counter()
+    for _ in range(k2):
+        ev.set_state(hnp)
+        ev.step(1, DT, sync=False)
         ev.get_state(hnp)
-        k2 = max(1, min(args.steps, 10))
-        torch.cuda.synchronize()
-        t0 = time.perf_counter()
-        for _ in range(k2):
-            ev.set_state(hnp)
-            ev.step(1, DT, sync=False)
-            ev.get_state(hnp)
-        el = time.perf_counter() - t0
-        e2e = {"value": points * 3 * k2 * ws / el, "unit": UNIT,
-               "h2d_bytes_per_step": ev.state_size * 8, "d2h_bytes_per_step": ev.state_size * 8,
-               "steps": k2}
+    el = time.perf_counter() - t0
+    if ws > 1:
+        t = torch.tensor([el], device="cuda")
+        torch.distributed.all_reduce(t, op=torch.distributed.ReduceOp.MAX)
+        el = float(t.item())
+    e2e = {"value": points * 3 * k2 * ws / el, "unit": UNIT,
+           "h2d_bytes_per_step": ev.state_size * 8, "d2h_bytes_per_step": ev.state_size * 8,
+           "steps": k2}
+    ev.close()
+
+    mixed = None
+    if not args.no_mixed:
+        evm, msm, _, statem, _ = time_path(args, PRECISION_MIXED, dev, rank, ws, False)
+        evm.close()
+        err = float(np.linalg.norm(statem - state64) / np.linalg.norm(state64))
+        launch_m = msm / (3 * args.steps)
+        gbs_m = MIXED_BYTES_PER_POINT_LAUNCH * points / (launch_m * 1e-3) / 1e9
+        mixed = {"value": points * 3 * args.steps * ws / (msm * 1e-3), "unit": UNIT,
+                 "ms_per_step": msm / args.steps,
+                 "speedup_vs_fp64": ms / msm,
+                 "rel_l2_vs_fp64_after_steps": err, "steps_compared": warm + args.steps,
+                 "dtype": "f32 split-product contractions, f64 state and step accumulation",
+                 "roofline": {"bound": "hbm", "achieved": gbs_m, "peak": hbm, "unit": "GB/s",
+                              "frac": gbs_m / hbm, "traffic": None,
+                              "bytes_per_point_launch": MIXED_BYTES_PER_POINT_LAUNCH,
+                              "avg_launch_ms": launch_m}}
 
     cpu = None
     if rank == 0 and not args.no_cpu_baseline:
         threads = cpu_threads()
-        v, el, pts = cpu_reference_run(1, 0, threads)
+        v, elc, pts = cpu_reference_run(1, 0, threads)
         cpu = {"value": v, "unit": UNIT, "cores": threads, "kind": "port",
                "sample": "FP64 C++ restatement (oracle/), 16^3 elements x 8^3 points, "
-                         "1 SSP-RK3 step, %.2f s" % el}
+                         "1 SSP-RK3 step, %.2f s" % elc}
     if ws > 1:
         torch.distributed.barrier()
     if rank == 0:
-        fp64_tflops = FP64_OPS_PER_POINT_STAGE * 2.0 * points / (launch_ms * 1e-3) / 1e12
+        fp64_inst = FP64_INST_PER_POINT_STAGE * points / (launch_ms * 1e-3) / 1e12
         line = {
             "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": ws, "steps": args.steps,
-            "warmup": max(args.warmup, 3), "ms_per_step": ms / args.steps,
+            "warmup": warm, "ms_per_step": ms / args.steps,
             "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f64",
             "data": "synthetic", "config": workload_config(args.elements),
-            "roofline": {"bound": "hbm", "achieved": achieved_gbs,
-                         "peak": peaks.get("hbm_gbs"), "unit": "GB/s",
-                         "frac": achieved_gbs / peaks.get("hbm_gbs"), "traffic": None,
+            "roofline": {"bound": "hbm", "achieved": achieved_gbs, "peak": hbm, "unit": "GB/s",
+                         "frac": achieved_gbs / hbm, "traffic": None,
                          "peak_source": peak_kind,
                          "bytes_per_point_launch": BYTES_PER_POINT_LAUNCH,
                          "avg_launch_ms": launch_ms},
-            "fp64_pipe": {"achieved_tflops": fp64_tflops, "peak_tflops": 1.01,
-                          "peak_source": "DFMA probe on this pool's GB300 (0.505 T inst/s)",
-                          "frac": fp64_tflops / 1.01},
-            "cpu_baseline": cpu, "e2e": e2e, "clocks": clocks,
+            "fp64_pipe": {"achieved_tinst_s": fp64_inst, "peak_tinst_s": FP64_PEAK_TINST,
+                          "frac": fp64_inst / FP64_PEAK_TINST,
+                          "inst_per_point_stage": FP64_INST_PER_POINT_STAGE,
+                          "note": "FP64 pipe binds the plain path on GB300; peak from a "
+                                  "DFMA/DADD throughput probe on this pool's GB300"},
+            "mixed": mixed, "cpu_baseline": cpu, "e2e": e2e, "clocks": clocks,
             "gpu_launches": 3 * args.steps,
         }
         print(json.dumps(line), flush=True)
-    ev.close()
     if ws > 1:
         torch.distributed.destroy_process_group()
     return 0
@@ -287,6 +328,7 @@ def main():
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
     ap.add_argument("--no-cpu-baseline", action="store_true")
+    ap.add_argument("--no-mixed", action="store_true")
     ap.add_argument("--elements", type=int, default=ELEMS,
                     help="elements per axis (default 32: the benchmark workload; smaller "
                          "values only for profiling captures)")

@@ -47,7 +47,8 @@ typedef enum {
   DGSW_ERR_CUDA = -2,         /* CUDA runtime error */
   DGSW_ERR_UNSUPPORTED = -3,  /* valid request this build does not support */
   DGSW_ERR_NOT_FINITE = -4,   /* NaN or Inf detected in the state */
-  DGSW_ERR_NO_DEVICE = -5     /* no usable GB300-class device */
+  DGSW_ERR_NO_DEVICE = -5,    /* no usable GB300-class device */
+  DGSW_ERR_DEVICE_TIMEOUT = -6 /* a bounded device-side wait gave up */
 } DgswStatus;
 
 /* System::variables_tag, ScalarWave/System.hpp:39-57 */

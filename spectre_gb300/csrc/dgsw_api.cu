@@ -30,6 +30,9 @@ struct DgswHandle_ {
   double* t1 = nullptr;     // stage buffers
   double* t2 = nullptr;
   double* u0s = nullptr;    // step-start copy for dgsw_substep
+  float* w1 = nullptr;      // mixed precision: d1 = dt L(u0)
+  float* w2 = nullptr;      // mixed precision: s2 = u2 - u0
+  int* dev_err = nullptr;   // error word written by bounded device waits
   int32_t* nbr = nullptr;
   double* jac = nullptr;
   double* lower = nullptr;
@@ -106,11 +109,79 @@ cudaError_t launch_stage(DgswHandle h, const StageLaunch& L) {
   return launch_stage_fp64(L, h->stream);
 }
 
+bool mixed(DgswHandle h) { return h->cfg.precision == DGSW_PRECISION_MIXED; }
+
+MixedLaunch base_mixed(DgswHandle h) {
+  MixedLaunch L;
+  L.n = h->dom.elem_n.empty() ? 0 : h->dom.elem_n[0];
+  L.n_elem = h->dom.n_elem;
+  L.nbr = h->nbr;
+  L.jac = h->jac;
+  L.eo = h->eo;
+  L.err = h->dev_err;
+  return L;
+}
+
+cudaError_t launch_mixed(DgswHandle h, const MixedLaunch& L) {
+  if (mixed_pipe_supported(L.n)) return launch_stage_mixed_pipe(L, h->stream);
+  return launch_stage_mixed(L, h->stream);
+}
+
+// Reads and clears the device error word; DGSW_ERR_DEVICE_TIMEOUT when set.
+int check_device_error(DgswHandle h) {
+  if (!h->dev_err) return DGSW_OK;
+  int v = 0;
+  cudaError_t e = cudaMemcpy(&v, h->dev_err, sizeof(int), cudaMemcpyDeviceToHost);
+  if (e != cudaSuccess) return cuda_fail(h, e, "read device error word");
+  if (v) {
+    cudaMemset(h->dev_err, 0, sizeof(int));
+    return fail(h, DGSW_ERR_DEVICE_TIMEOUT,
+                "a device-side wait for staged element data timed out; results are invalid");
+  }
+  return DGSW_OK;
+}
+
+// The three mixed-precision stages (incremental form of Rk3HesthavenSsp):
+//   A: w1 = dt L(u0)                         [base/out: u0 + w1 for substeps]
+//   B: w2 = w1/2 + dt/4 L(w1)                [u0 + w2]
+//   C: u  = u0 + 2/3 (w2 + w1) + 2dt/3 L(w2)
+cudaError_t enqueue_mixed_stage(DgswHandle h, int k, double dt, const double* u0, double* out) {
+  MixedLaunch L = base_mixed(h);
+  if (k == 0) {
+    L.x64 = u0;
+    L.c = dt;
+    L.w32 = h->w1;
+  } else if (k == 1) {
+    L.x32 = h->w1;
+    L.alpha = 0.5;
+    L.c = 0.25 * dt;
+    L.w32 = h->w2;
+  } else {
+    L.x32 = h->w2;
+    L.y32 = h->w1;
+    L.alpha = 2.0 / 3.0;
+    L.beta = 2.0 / 3.0;
+    L.c = (2.0 / 3.0) * dt;
+  }
+  if (out) {
+    L.out64 = out;
+    L.base64 = u0;
+  }
+  return launch_mixed(h, L);
+}
+
 // Enqueue the three substeps of one SSP-RK3 step on the handle's stream:
 //   t1 = u + dt L(u); t2 = 3/4 u + 1/4 t1 + dt/4 L(t1);
 //   u  = 1/3 u + 2/3 t2 + 2dt/3 L(t2)   (in place: each element reads only
 //   its own u, neighbours' faces come from t2).
 cudaError_t enqueue_step(DgswHandle h, double dt) {
+  if (mixed(h)) {
+    cudaError_t e = enqueue_mixed_stage(h, 0, dt, h->state, nullptr);
+    if (e != cudaSuccess) return e;
+    e = enqueue_mixed_stage(h, 1, dt, h->state, nullptr);
+    if (e != cudaSuccess) return e;
+    return enqueue_mixed_stage(h, 2, dt, h->state, h->state);
+  }
   StageLaunch L = base_launch(h);
   L.mode = kModeStageFirst;
   L.ucur = h->state;
@@ -222,9 +293,9 @@ int dgsw_create(const DgswConfig* cfg, DgswHandle* out) {
     delete h;
     return fail(nullptr, DGSW_ERR_UNSUPPORTED, "elements of different extents are not supported yet");
   }
-  if (cfg->precision != DGSW_PRECISION_FP64) {
+  if (cfg->precision == DGSW_PRECISION_MIXED && cfg->gamma2 != 0.0) {
     delete h;
-    return fail(nullptr, DGSW_ERR_UNSUPPORTED, "only FP64 precision in this build");
+    return fail(nullptr, DGSW_ERR_UNSUPPORTED, "mixed precision needs gamma2 = 0");
   }
   int count = 0;
   if (cudaGetDeviceCount(&count) != cudaSuccess || count <= cfg->device || cfg->device < 0) {
@@ -255,6 +326,12 @@ int dgsw_create(const DgswConfig* cfg, DgswHandle* out) {
   if ((e = cudaMalloc(&h->t2, bytes)) != cudaSuccess) return bail(e, "cudaMalloc stage 2");
   if ((e = cudaMalloc(&h->u0s, bytes)) != cudaSuccess) return bail(e, "cudaMalloc step start");
   if ((e = cudaMemset(h->state, 0, bytes)) != cudaSuccess) return bail(e, "cudaMemset");
+  if ((e = cudaMalloc(&h->dev_err, sizeof(int))) != cudaSuccess) return bail(e, "cudaMalloc err");
+  if ((e = cudaMemset(h->dev_err, 0, sizeof(int))) != cudaSuccess) return bail(e, "cudaMemset err");
+  if (cfg->precision == DGSW_PRECISION_MIXED) {
+    if ((e = cudaMalloc(&h->w1, bytes / 2 + 16)) != cudaSuccess) return bail(e, "cudaMalloc w1");
+    if ((e = cudaMalloc(&h->w2, bytes / 2 + 16)) != cudaSuccess) return bail(e, "cudaMalloc w2");
+  }
   std::vector<double> jac(3 * h->dom.n_elem);
   for (int64_t i = 0; i < 3 * h->dom.n_elem; ++i) jac[i] = 2.0 / h->dom.width[i];
   if ((e = upload(&h->nbr, h->dom.neighbor)) != cudaSuccess) return bail(e, "upload neighbors");
@@ -283,6 +360,9 @@ int dgsw_destroy(DgswHandle h) {
   double* dbl[] = {h->state, h->t1, h->t2, h->u0s, h->jac, h->lower, h->width, h->lgl_x, h->params};
   for (double* p : dbl)
     if (p) cudaFree(p);
+  if (h->dev_err) cudaFree(h->dev_err);
+  if (h->w1) cudaFree(h->w1);
+  if (h->w2) cudaFree(h->w2);
   if (h->nbr) cudaFree(h->nbr);
   if (h->elem_n) cudaFree(h->elem_n);
   if (h->offset) cudaFree(h->offset);
@@ -306,7 +386,7 @@ int dgsw_synchronize(DgswHandle h) {
   if (!h) return fail(nullptr, DGSW_ERR_ARGUMENT, "null handle");
   if (int rc = select_device(h)) return rc;
   DGSW_CUDA(h, cudaStreamSynchronize(h->stream));
-  return DGSW_OK;
+  return check_device_error(h);
 }
 
 int dgsw_set_state(DgswHandle h, const double* host_u) {
@@ -323,7 +403,7 @@ int dgsw_get_state(DgswHandle h, double* host_u) {
   DGSW_CUDA(h, cudaMemcpyAsync(host_u, h->state, h->dom.offset.back() * sizeof(double),
                                cudaMemcpyDeviceToHost, h->stream));
   DGSW_CUDA(h, cudaStreamSynchronize(h->stream));
-  return DGSW_OK;
+  return check_device_error(h);
 }
 
 int dgsw_set_state_device(DgswHandle h, const double* dev_u) {
@@ -382,6 +462,14 @@ int dgsw_rhs_device(DgswHandle h, const double* dev_u, double* dev_dudt) {
   if (!h || !dev_u || !dev_dudt) return fail(h, DGSW_ERR_ARGUMENT, "null argument");
   if (dev_u == dev_dudt) return fail(h, DGSW_ERR_ARGUMENT, "input and output must differ");
   if (int rc = select_device(h)) return rc;
+  if (mixed(h)) {
+    MixedLaunch M = base_mixed(h);
+    M.x64 = dev_u;
+    M.c = 1.0;
+    M.out64 = dev_dudt;
+    DGSW_CUDA(h, launch_mixed(h, M));
+    return DGSW_OK;
+  }
   StageLaunch L = base_launch(h);
   L.mode = kModeRhs;
   L.ucur = dev_u;
@@ -444,6 +532,12 @@ int dgsw_substep(DgswHandle h, int k, double dt) {
   if (k < 0 || k > 2 || !std::isfinite(dt)) return fail(h, DGSW_ERR_ARGUMENT, "bad substep");
   if (int rc = select_device(h)) return rc;
   const size_t bytes = h->dom.offset.back() * sizeof(double);
+  if (mixed(h)) {
+    if (k == 0)
+      DGSW_CUDA(h, cudaMemcpyAsync(h->u0s, h->state, bytes, cudaMemcpyDeviceToDevice, h->stream));
+    DGSW_CUDA(h, enqueue_mixed_stage(h, k, dt, h->u0s, h->state));
+    return DGSW_OK;
+  }
   StageLaunch L = base_launch(h);
   if (k == 0) {
     DGSW_CUDA(h, cudaMemcpyAsync(h->u0s, h->state, bytes, cudaMemcpyDeviceToDevice, h->stream));

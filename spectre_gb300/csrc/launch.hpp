@@ -26,6 +26,30 @@ struct StageLaunch {
 
 cudaError_t launch_stage_fp64(const StageLaunch& L, cudaStream_t s);
 
+// One mixed-precision stage: W = alpha X + beta Y + c L(X) (stage_mixed.cu).
+// Exactly one of x64 (FP64 input, compensated double-float arithmetic) and
+// x32 (FP32 increment input) is set.
+struct MixedLaunch {
+  int n = 0;
+  int64_t n_elem = 0;
+  const double* x64 = nullptr;
+  const float* x32 = nullptr;
+  const float* y32 = nullptr;   // optional pointwise input
+  float* w32 = nullptr;         // optional FP32 output
+  double* out64 = nullptr;      // optional FP64 output
+  const double* base64 = nullptr;  // out64 = base64 + W when set, else W
+  const int32_t* nbr = nullptr;
+  const double* jac = nullptr;
+  double alpha = 0.0, beta = 0.0, c = 1.0;
+  EoTable eo{};
+  int* err = nullptr;  // device error word (bounded waits that timed out)
+};
+
+cudaError_t launch_stage_mixed(const MixedLaunch& L, cudaStream_t s);
+// Persistent TMA-pipelined variant for even extents (stage_mixed_pipe.cu).
+bool mixed_pipe_supported(int n);
+cudaError_t launch_stage_mixed_pipe(const MixedLaunch& L, cudaStream_t s);
+
 // UpwindPenalty pointwise kernels (face_kernels.cu).
 cudaError_t launch_package_data(int64_t npts, const double* psi, const double* pi,
                                 const double* phi, const double* gamma2,

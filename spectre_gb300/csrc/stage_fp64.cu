@@ -81,8 +81,8 @@ __device__ __forceinline__ void eo_line(const double (&u)[N], double (&out)[N],
   }
 }
 
-template <int N, int EPB, int MODE>
-__global__ void __launch_bounds__(N * N * EPB)
+template <int N, int EPB, int MINB, int MODE>
+__global__ void __launch_bounds__(N * N * EPB, MINB)
     stage_fp64_kernel(const double* ucur, const double* u0, double* unext,
                       const int32_t* __restrict__ nbr, const double* __restrict__ jac,
                       int64_t n_elem, StageCoef coef, double gamma2, EoTable eo) {
@@ -232,17 +232,30 @@ __global__ void __launch_bounds__(N * N * EPB)
   }
 }
 
+// Elements per block and the minimum resident blocks per SM asked of the
+// register allocator: chosen per N so that no variant spills and several
+// blocks share an SM (one block's global loads and barriers overlap another
+// block's FP64 work).
 template <int N>
 constexpr int elems_per_block() {
-  return N <= 4 ? 16 : (N <= 6 ? 8 : (N <= 8 ? 4 : 2));
+  return N <= 4 ? 16 : (N <= 6 ? 8 : (N == 7 ? 4 : (N <= 11 ? 2 : 1)));
+}
+template <int N>
+constexpr int min_blocks() {
+  return N <= 5 ? 2 : (N == 8 ? 3 : 1);
 }
 
 template <int N, int MODE>
 cudaError_t launch_n(const StageLaunch& L, cudaStream_t s) {
   constexpr int EPB = elems_per_block<N>();
   const size_t smem = (size_t)EPB * Shape<N>::SLOT * sizeof(double);
-  auto k = stage_fp64_kernel<N, EPB, MODE>;
+  auto k = stage_fp64_kernel<N, EPB, min_blocks<N>(), MODE>;
   cudaError_t err = cudaFuncSetAttribute(k, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+  if (err != cudaSuccess) return err;
+  // two resident blocks per SM overlap one block's loads and barriers with
+  // the other's FP64 work
+  err = cudaFuncSetAttribute(k, cudaFuncAttributePreferredSharedMemoryCarveout,
+                             cudaSharedmemCarveoutMaxShared);
   if (err != cudaSuccess) return err;
   const int64_t blocks = (L.n_elem + EPB - 1) / EPB;
   if (blocks <= 0) return cudaSuccess;

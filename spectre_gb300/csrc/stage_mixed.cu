@@ -1,0 +1,451 @@
+// stage_mixed.cu -- mixed-precision fused DG right-hand side + SSP-RK3 stage
+// (uniform LGL extent N, conforming mortars, affine mesh).
+//
+// The DG operator L of ScalarWave::TimeDerivative + UpwindPenalty + lift is
+// linear in (Psi, Pi, Phi) for a static mesh (fixed normals, fixed char
+// speeds (0, +1, -1)).  With u1 = u0 + d1 and d1 = dt L(u0), the SSP-RK3
+// stages of Rk3HesthavenSsp.cpp:63-80 become
+//   d1 = dt L(u0)
+//   s2 = u2 - u0 = d1/2 + dt/4 L(d1)
+//   u3 = u0 + 2/3 (s2 + d1) + 2dt/3 L(s2)
+// so only the first stage differentiates the full FP64 state; the other two
+// differentiate small increments whose FP32 rounding is far below the
+// step's truncation error.  The first stage is done in FP32 "double-float"
+// arithmetic: the state is split exactly into hi + lo FP32 parts (integer bit
+// operations, no FP64 instruction), the scaled even/odd D tables are split
+// into hi + lo FP32 parts, and every dot product is compensated (TwoProd via
+// FMA, TwoSum), so L(u0) is accurate to far better than FP32 before its
+// final rounding.  The FP64 state is updated once per step, u0 + (double)inc,
+// with one FP64 add per value.
+//
+// One kernel template serves every stage:
+//   W = alpha X + beta Y + c L(X)
+// X: fields read with faces (FP64 and compensated when COMP, else FP32),
+// Y: optional FP32 pointwise input.  Outputs (each optional):
+//   w32[p]   = W                  (FP32 increment buffer)
+//   out64[p] = base64[p] + W      (FP64; out64 may alias base64)
+//   out64[p] = W                  (when base64 is null: the RHS itself)
+#include "common.cuh"
+#include "launch.hpp"
+
+namespace dgsw {
+namespace {
+
+template <int N>
+struct MShape {
+  static constexpr int h = N / 2;
+  static constexpr int odd = N % 2;
+  static constexpr int H = h + odd;
+  static constexpr int NN = N * N;
+  static constexpr int NP = N * N * N;
+  static constexpr int TAB = 2 * H * h + H;
+};
+
+// ---- exact FP64 -> (hi, lo) FP32 split with integer operations -----------
+// hi = u truncated to 24 significant bits, lo = the next 23 bits (u - hi to
+// 2^-47 relative).  |u| < 2^-126 flushes to (0, 0); the lo part flushes below
+// 2^-103.  Non-finite u gives (u as float, 0).
+__device__ __forceinline__ void split_df(double u, float& hi, float& lo) {
+  const unsigned long long b = (unsigned long long)__double_as_longlong(u);
+  const unsigned int top = (unsigned int)(b >> 32);
+  const unsigned int sign = top & 0x80000000u;
+  const int e = (int)((top >> 20) & 0x7ffu);
+  if (e >= 1023 + 128) {  // beyond float range or inf/nan
+    hi = __double2float_rn(u);
+    lo = 0.0f;
+    return;
+  }
+  if (e < 1023 - 126) {
+    hi = 0.0f;
+    lo = 0.0f;
+    return;
+  }
+  const unsigned int mhi = (unsigned int)((b >> 29) & 0x7fffffu);  // top 23 mantissa bits
+  hi = __int_as_float((int)(sign | ((unsigned int)(e - 1023 + 127) << 23) | mhi));
+  const unsigned int mlo = (unsigned int)(b & 0x1fffffffu);  // low 29 mantissa bits
+  if (e < 920 || mlo == 0u) {
+    lo = 0.0f;
+    return;
+  }
+  // (1 + m*2^-23) - 1 is exact; m = mlo >> 6 keeps the top 23 of the 29 bits
+  const float f = __int_as_float((int)(0x3f800000u | (mlo >> 6))) - 1.0f;
+  const float scale = __int_as_float((e - 919) << 23);  // 2^(e - 1046)
+  lo = __int_as_float(__float_as_int(f * scale) | (int)sign);
+}
+
+// exact FP32 -> FP64 widening with integer operations (normal floats; zero
+// and subnormals widen to signed zero)
+__device__ __forceinline__ double widen(float f) {
+  const unsigned int b = (unsigned int)__float_as_int(f);
+  const unsigned int e = (b >> 23) & 0xffu;
+  if (e == 0u) return __longlong_as_double((long long)((unsigned long long)(b & 0x80000000u) << 32));
+  if (e == 0xffu) return (double)f;
+  const unsigned int hiw = (b & 0x80000000u) | ((e + 896u) << 20) | ((b & 0x7fffffu) >> 3);
+  const unsigned int low = (b & 0x7u) << 29;
+  return __hiloint2double((int)hiw, (int)low);
+}
+
+// ---- double-float primitives ----------------------------------------------
+__device__ __forceinline__ void two_sum(float a, float b, float& s, float& t) {
+  s = a + b;
+  const float bb = s - a;
+  t = (a - (s - bb)) + (b - bb);
+}
+
+// compensated accumulation of one product (ah+al)*(xh+xl) into (s, c)
+__device__ __forceinline__ void dot2_term(float ah, float al, float xh, float xl, float& s,
+                                          float& c) {
+  const float p = ah * xh;
+  const float pe = fmaf(ah, xh, -p);
+  float t;
+  two_sum(s, p, s, t);
+  c += t + pe;
+  c = fmaf(al, xh, c);
+  c = fmaf(ah, xl, c);
+}
+
+__device__ __forceinline__ void dot2_first(float ah, float al, float xh, float xl, float& s,
+                                           float& c) {
+  s = ah * xh;
+  c = fmaf(ah, xh, -s);
+  c = fmaf(al, xh, c);
+  c = fmaf(ah, xl, c);
+}
+
+// compensated (scaled D) x (one line), double-float input, FP32 output
+template <int N>
+__device__ __forceinline__ void eo_line_df(const float (&xh)[N], const float (&xl)[N],
+                                           float (&out)[N], const float* __restrict__ th,
+                                           const float* __restrict__ tl) {
+  using S = MShape<N>;
+  constexpr int h = S::h, H = S::H;
+  float eh[h], el[h], oh[h], ol[h];
+#pragma unroll
+  for (int j = 0; j < h; ++j) {
+    float t;
+    two_sum(xh[j], xh[N - 1 - j], eh[j], t);
+    el[j] = t + (xl[j] + xl[N - 1 - j]);
+    two_sum(xh[j], -xh[N - 1 - j], oh[j], t);
+    ol[j] = t + (xl[j] - xl[N - 1 - j]);
+  }
+  const float* Ah = th;
+  const float* Al = tl;
+  const float* Bh = th + H * h;
+  const float* Bl = tl + H * h;
+  const float* Mh = th + 2 * H * h;
+  const float* Ml = tl + 2 * H * h;
+#pragma unroll
+  for (int i = 0; i < h; ++i) {
+    float ps, pc, qs, qc;
+    dot2_first(Ah[i * h], Al[i * h], eh[0], el[0], ps, pc);
+#pragma unroll
+    for (int j = 1; j < h; ++j) dot2_term(Ah[i * h + j], Al[i * h + j], eh[j], el[j], ps, pc);
+    if (S::odd) dot2_term(Mh[i], Ml[i], xh[h], xl[h], ps, pc);
+    dot2_first(Bh[i * h], Bl[i * h], oh[0], ol[0], qs, qc);
+#pragma unroll
+    for (int j = 1; j < h; ++j) dot2_term(Bh[i * h + j], Bl[i * h + j], oh[j], ol[j], qs, qc);
+    out[i] = (ps + qs) + (pc + qc);
+    out[N - 1 - i] = (qs - ps) + (qc - pc);
+  }
+  if (S::odd) {
+    float qs, qc;
+    dot2_first(Bh[h * h], Bl[h * h], oh[0], ol[0], qs, qc);
+#pragma unroll
+    for (int j = 1; j < h; ++j) dot2_term(Bh[h * h + j], Bl[h * h + j], oh[j], ol[j], qs, qc);
+    out[h] = qs + qc;
+  }
+}
+
+// plain FP32 (scaled D) x line with the even/odd split
+template <int N>
+__device__ __forceinline__ void eo_line_f(const float (&x)[N], float (&out)[N],
+                                          const float* __restrict__ th) {
+  using S = MShape<N>;
+  constexpr int h = S::h, H = S::H;
+  float e[h], o[h];
+#pragma unroll
+  for (int j = 0; j < h; ++j) {
+    e[j] = x[j] + x[N - 1 - j];
+    o[j] = x[j] - x[N - 1 - j];
+  }
+  const float* A = th;
+  const float* B = th + H * h;
+  const float* M = th + 2 * H * h;
+#pragma unroll
+  for (int i = 0; i < h; ++i) {
+    float P = A[i * h] * e[0];
+#pragma unroll
+    for (int j = 1; j < h; ++j) P = fmaf(A[i * h + j], e[j], P);
+    if (S::odd) P = fmaf(M[i], x[h], P);
+    float Q = B[i * h] * o[0];
+#pragma unroll
+    for (int j = 1; j < h; ++j) Q = fmaf(B[i * h + j], o[j], Q);
+    out[i] = P + Q;
+    out[N - 1 - i] = Q - P;
+  }
+  if (S::odd) {
+    float Q = B[h * h] * o[0];
+#pragma unroll
+    for (int j = 1; j < h; ++j) Q = fmaf(B[h * h + j], o[j], Q);
+    out[h] = Q;
+  }
+}
+
+template <int N, int EPB, bool COMP>
+struct MSmem {
+  using S = MShape<N>;
+  // per element: fields (COMP: hi and lo of Pi, Phi_x, Phi_y, Phi_z; else the
+  // four FP32 fields), the dt Pi accumulator, 3 scaled tables (hi [+ lo])
+  static constexpr int kFieldFloats = (COMP ? 8 : 4) * S::NP;
+  static constexpr int kTabFloats = (COMP ? 2 : 1) * 3 * S::TAB;
+  static constexpr int kSlot = kFieldFloats + S::NP + kTabFloats;
+  static constexpr size_t kBytes = (size_t)EPB * kSlot * sizeof(float);
+};
+
+template <int N, int EPB, bool COMP>
+__global__ void __launch_bounds__(N * N * EPB, COMP ? 1 : 2)
+    stage_mixed_kernel(MixedLaunch L) {
+  using S = MShape<N>;
+  using SM = MSmem<N, EPB, COMP>;
+  constexpr int NN = S::NN, NP = S::NP, TAB = S::TAB, h = S::h, H = S::H;
+  constexpr int64_t VS = (int64_t)kVars * NP;  // values per element
+  extern __shared__ float fsm[];
+  const int slot = threadIdx.x / NN;
+  const int t = threadIdx.x - slot * NN;
+  const int64_t e = (int64_t)blockIdx.x * EPB + slot;
+  const bool active = e < L.n_elem;
+  float* F = fsm + slot * SM::kSlot;
+  float* Sacc = F + SM::kFieldFloats;
+  float* T = Sacc + NP;  // COMP: [hi tables 3*TAB][lo tables 3*TAB]
+  const int64_t off = e * VS;
+  const float cf = (float)L.c;
+
+  double jd[3] = {0.0, 0.0, 0.0};
+  if (active) {
+    jd[0] = L.jac[3 * e];
+    jd[1] = L.jac[3 * e + 1];
+    jd[2] = L.jac[3 * e + 2];
+    if (COMP) {
+      const double* src = L.x64 + off + NP;
+      for (int q = t; q < 4 * NP; q += NN) {
+        float hi, lo;
+        split_df(src[q], hi, lo);
+        F[q] = hi;
+        F[4 * NP + q] = lo;
+      }
+    } else {
+      const float* src = L.x32 + off + NP;
+      for (int q = t; q < 4 * NP; q += NN) F[q] = src[q];
+    }
+    for (int q = t; q < 3 * TAB; q += NN) {
+      const int d = q / TAB, r = q - d * TAB;
+      double v;
+      if (r < H * h)
+        v = L.eo.A[r / h][r % h];
+      else if (r < 2 * H * h)
+        v = L.eo.B[(r - H * h) / h][(r - H * h) % h];
+      else
+        v = L.eo.M[r - 2 * H * h];
+      const double sv = (-L.c * jd[d]) * v;
+      const float hi = __double2float_rn(sv);
+      T[q] = hi;
+      if (COMP) T[3 * TAB + q] = __double2float_rn(sv - (double)hi);
+    }
+  }
+  __syncthreads();
+
+  const int ta = t % N, tb = t / N;
+  const float alpha = (float)L.alpha, beta = (float)L.beta;
+#pragma unroll 1
+  for (int d = 0; d < 3; ++d) {
+    if (active) {
+      int base, stride;
+      if (d == 0) {
+        base = N * ta + NN * tb;
+        stride = 1;
+      } else if (d == 1) {
+        base = ta + NN * tb;
+        stride = N;
+      } else {
+        base = ta + N * tb;
+        stride = NN;
+      }
+      const float* th = T + d * TAB;
+      const float* tl = T + 3 * TAB + d * TAB;
+      float dF[N], dP[N];
+      // fields of this line: Pi (index 0) and Phi_d (index 1 + d)
+      float pih[N], pil[N], fh[N], fl[N];
+#pragma unroll
+      for (int i = 0; i < N; ++i) {
+        pih[i] = F[base + i * stride];
+        fh[i] = F[(1 + d) * NP + base + i * stride];
+        if (COMP) {
+          pil[i] = F[4 * NP + base + i * stride];
+          fl[i] = F[4 * NP + (1 + d) * NP + base + i * stride];
+        } else {
+          pil[i] = 0.0f;
+          fl[i] = 0.0f;
+        }
+      }
+      if (COMP) {
+        eo_line_df<N>(fh, fl, dF, th, tl);
+        eo_line_df<N>(pih, pil, dP, th, tl);
+      } else {
+        eo_line_f<N>(fh, dF, th);
+        eo_line_f<N>(pih, dP, th);
+      }
+      // UpwindPenalty face corrections at both ends of the line (flat unit
+      // normal s e_d, char speeds (0, +1, -1)): D_Pi = (w_int - w_ext)/2,
+      // D_Phi_d = -s D_Pi, w = Pi - s Phi_d; lifted and scaled:
+      // G = -c N(N-1) J_d / 4.
+      const float G = (float)(-0.25 * L.c * (double)(N * (N - 1)) * jd[d]);
+      const int64_t nlo = (int64_t)L.nbr[6 * e + 2 * d] * VS;
+      const int64_t nhi = (int64_t)L.nbr[6 * e + 2 * d + 1] * VS;
+      const int lo_pt = base + (N - 1) * stride;
+      const int hi_pt = base;
+      float dw_lo, dw_hi;
+      if (COMP) {
+        // w in double-float; the jump is the small difference of two O(u)
+        // numbers, so it is formed before rounding to FP32
+        float ph, pl, qh, ql;
+        split_df(L.x64[nlo + NP + lo_pt], ph, pl);
+        split_df(L.x64[nlo + (2 + d) * NP + lo_pt], qh, ql);
+        // s = -1: w = Pi + Phi_d
+        float wih, wil, weh, wel, t1;
+        two_sum(pih[0], fh[0], wih, t1);
+        wil = t1 + (pil[0] + fl[0]);
+        two_sum(ph, qh, weh, t1);
+        wel = t1 + (pl + ql);
+        float dh;
+        two_sum(wih, -weh, dh, t1);
+        dw_lo = dh + (t1 + (wil - wel));
+        split_df(L.x64[nhi + NP + hi_pt], ph, pl);
+        split_df(L.x64[nhi + (2 + d) * NP + hi_pt], qh, ql);
+        // s = +1: w = Pi - Phi_d
+        two_sum(pih[N - 1], -fh[N - 1], wih, t1);
+        wil = t1 + (pil[N - 1] - fl[N - 1]);
+        two_sum(ph, -qh, weh, t1);
+        wel = t1 + (pl - ql);
+        two_sum(wih, -weh, dh, t1);
+        dw_hi = dh + (t1 + (wil - wel));
+      } else {
+        const float we_lo = L.x32[nlo + NP + lo_pt] + L.x32[nlo + (2 + d) * NP + lo_pt];
+        const float we_hi = L.x32[nhi + NP + hi_pt] - L.x32[nhi + (2 + d) * NP + hi_pt];
+        dw_lo = (pih[0] + fh[0]) - we_lo;
+        dw_hi = (pih[N - 1] - fh[N - 1]) - we_hi;
+      }
+      dF[0] = fmaf(G, dw_lo, dF[0]);
+      dP[0] = fmaf(G, dw_lo, dP[0]);
+      dF[N - 1] = fmaf(G, dw_hi, dF[N - 1]);
+      dP[N - 1] = fmaf(-G, dw_hi, dP[N - 1]);
+
+      // Phi_d: W = alpha X + beta Y + c L
+      {
+        const int64_t vo = off + (2 + d) * NP + base;
+#pragma unroll
+        for (int i = 0; i < N; ++i) {
+          float w = dP[i];
+          if (!COMP) {
+            w = fmaf(alpha, fh[i], w);
+            if (L.y32) w = fmaf(beta, L.y32[vo + i * stride], w);
+          }
+          if (L.w32) L.w32[vo + i * stride] = w;
+          if (L.out64) {
+            if (L.base64)
+              L.out64[vo + i * stride] = L.base64[vo + i * stride] + widen(w);
+            else
+              L.out64[vo + i * stride] = widen(w);
+          }
+        }
+      }
+      if (d < 2) {
+#pragma unroll
+        for (int i = 0; i < N; ++i) {
+          if (d == 0)
+            Sacc[base + i * stride] = dF[i];
+          else
+            Sacc[base + i * stride] += dF[i];
+        }
+      } else {
+#pragma unroll
+        for (int i = 0; i < N; ++i) {
+          const int p = base + i * stride;
+          float wpi = Sacc[p] + dF[i];
+          // dt Psi = -Pi (TimeDerivative.cpp:38)
+          float wpsi = COMP ? fmaf(-cf, pih[i], -cf * pil[i]) : -cf * pih[i];
+          if (!COMP) {
+            wpi = fmaf(alpha, pih[i], wpi);
+            wpsi = fmaf(alpha, L.x32[off + p], wpsi);
+            if (L.y32) {
+              wpi = fmaf(beta, L.y32[off + NP + p], wpi);
+              wpsi = fmaf(beta, L.y32[off + p], wpsi);
+            }
+          }
+          if (L.w32) {
+            L.w32[off + NP + p] = wpi;
+            L.w32[off + p] = wpsi;
+          }
+          if (L.out64) {
+            if (L.base64) {
+              L.out64[off + NP + p] = L.base64[off + NP + p] + widen(wpi);
+              L.out64[off + p] = L.base64[off + p] + widen(wpsi);
+            } else {
+              L.out64[off + NP + p] = widen(wpi);
+              L.out64[off + p] = widen(wpsi);
+            }
+          }
+        }
+      }
+    }
+    if (d < 2) __syncthreads();
+  }
+}
+
+template <int N>
+constexpr int mixed_epb() {
+  return N <= 4 ? 16 : (N <= 6 ? 8 : (N <= 8 ? 4 : 2));
+}
+
+template <int N, bool COMP>
+cudaError_t launch_mixed_n(const MixedLaunch& L, cudaStream_t s) {
+  constexpr int EPB = mixed_epb<N>();
+  using SM = MSmem<N, EPB, COMP>;
+  auto k = stage_mixed_kernel<N, EPB, COMP>;
+  cudaError_t err =
+      cudaFuncSetAttribute(k, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)SM::kBytes);
+  if (err != cudaSuccess) return err;
+  err = cudaFuncSetAttribute(k, cudaFuncAttributePreferredSharedMemoryCarveout,
+                             cudaSharedmemCarveoutMaxShared);
+  if (err != cudaSuccess) return err;
+  const int64_t blocks = (L.n_elem + EPB - 1) / EPB;
+  if (blocks <= 0) return cudaSuccess;
+  k<<<(unsigned)blocks, N * N * EPB, SM::kBytes, s>>>(L);
+  return cudaGetLastError();
+}
+
+template <int N>
+cudaError_t launch_mixed_comp(const MixedLaunch& L, cudaStream_t s) {
+  return L.x64 ? launch_mixed_n<N, true>(L, s) : launch_mixed_n<N, false>(L, s);
+}
+
+}  // namespace
+
+cudaError_t launch_stage_mixed(const MixedLaunch& L, cudaStream_t s) {
+  if ((L.x64 == nullptr) == (L.x32 == nullptr)) return cudaErrorInvalidValue;
+  switch (L.n) {
+    case 2: return launch_mixed_comp<2>(L, s);
+    case 3: return launch_mixed_comp<3>(L, s);
+    case 4: return launch_mixed_comp<4>(L, s);
+    case 5: return launch_mixed_comp<5>(L, s);
+    case 6: return launch_mixed_comp<6>(L, s);
+    case 7: return launch_mixed_comp<7>(L, s);
+    case 8: return launch_mixed_comp<8>(L, s);
+    case 9: return launch_mixed_comp<9>(L, s);
+    case 10: return launch_mixed_comp<10>(L, s);
+    case 11: return launch_mixed_comp<11>(L, s);
+    case 12: return launch_mixed_comp<12>(L, s);
+    default: return cudaErrorInvalidValue;
+  }
+}
+
+}  // namespace dgsw

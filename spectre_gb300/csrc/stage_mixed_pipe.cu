@@ -1,0 +1,572 @@
+// stage_mixed_pipe.cu -- persistent, TMA-pipelined mixed-precision DG stage
+// for even LGL extents N (element blocks are multiples of 16 bytes).
+//
+// Same arithmetic as stage_mixed.cu (W = alpha X + beta Y + c L(X), see the
+// header comment there for the incremental SSP-RK3 form and the double-float
+// first stage), restructured so that HBM latency is hidden:
+//  - a persistent grid; each CTA walks groups of EPB elements;
+//  - each element's contiguous blocks (X, and Y / base64 when present) are
+//    staged into shared memory by TMA bulk copies (cp.async.bulk, completion
+//    on an mbarrier), double-buffered: the next group's copies are in flight
+//    while the current group computes;
+//  - the 12 neighbour face values each thread needs are prefetched for the
+//    next group with cp.async into the same double buffer;
+//  - the contractions use Blackwell's packed FP32 instructions (FFMA2 /
+//    FADD2 / FMUL2), the even and odd halves of the split D in the two lanes.
+// Every mbarrier wait is bounded by a wall-clock limit; on timeout the
+// kernel records an error word the host reads and returns.
+#include <cstdint>
+#include <type_traits>
+
+#include "common.cuh"
+#include "launch.hpp"
+
+namespace dgsw {
+namespace {
+
+// ---------------------------------------------------------------- PTX helpers
+__device__ __forceinline__ uint32_t saddr(const void* p) {
+  return (uint32_t)__cvta_generic_to_shared(p);
+}
+
+__device__ __forceinline__ void mbar_init(uint64_t* bar, uint32_t count) {
+  asm volatile("mbarrier.init.shared::cta.b64 [%0], %1;" ::"r"(saddr(bar)), "r"(count)
+               : "memory");
+}
+
+__device__ __forceinline__ void fence_mbar_init() {
+  asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
+}
+
+__device__ __forceinline__ void mbar_arrive_expect_tx(uint64_t* bar, uint32_t bytes) {
+  asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;" ::"r"(saddr(bar)),
+               "r"(bytes)
+               : "memory");
+}
+
+__device__ __forceinline__ void bulk_g2s(void* dst, const void* src, uint32_t bytes,
+                                         uint64_t* bar) {
+  asm volatile(
+      "cp.async.bulk.shared::cluster.global.mbarrier::complete_tx::bytes [%0], [%1], %2, [%3];" ::
+          "r"(saddr(dst)),
+      "l"(src), "r"(bytes), "r"(saddr(bar))
+      : "memory");
+}
+
+__device__ __forceinline__ bool mbar_try_wait(uint64_t* bar, uint32_t parity) {
+  uint32_t ok;
+  asm volatile(
+      "{\n .reg .pred p;\n mbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2;\n"
+      " selp.u32 %0, 1, 0, p;\n}" : "=r"(ok) : "r"(saddr(bar)), "r"(parity) : "memory");
+  return ok != 0u;
+}
+
+// orders this thread's earlier generic-proxy accesses of shared memory before
+// later async-proxy (TMA) writes to it
+__device__ __forceinline__ void fence_proxy_async_smem() {
+  asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
+}
+
+__device__ __forceinline__ uint64_t global_ns() {
+  uint64_t t;
+  asm volatile("mov.u64 %0, %globaltimer;" : "=l"(t));
+  return t;
+}
+
+// Bounded wait: gives up after limit_ns of wall-clock time.
+__device__ __forceinline__ bool mbar_wait(uint64_t* bar, uint32_t parity, uint64_t limit_ns) {
+  if (mbar_try_wait(bar, parity)) return true;
+  const uint64_t t0 = global_ns();
+  while (!mbar_try_wait(bar, parity)) {
+    if (global_ns() - t0 > limit_ns) return false;
+  }
+  return true;
+}
+
+template <int BYTES>
+__device__ __forceinline__ void cp_async(void* dst, const void* src) {
+  asm volatile("cp.async.ca.shared.global [%0], [%1], %2;" ::"r"(saddr(dst)), "l"(src),
+               "n"(BYTES)
+               : "memory");
+}
+__device__ __forceinline__ void cp_async_commit() {
+  asm volatile("cp.async.commit_group;" ::: "memory");
+}
+__device__ __forceinline__ void cp_async_wait_all() {
+  asm volatile("cp.async.wait_all;" ::: "memory");
+}
+
+// ------------------------------------------------------- packed FP32 helpers
+__device__ __forceinline__ float2 add2(float2 a, float2 b) { return __fadd2_rn(a, b); }
+__device__ __forceinline__ float2 neg2(float2 a) { return make_float2(-a.x, -a.y); }
+__device__ __forceinline__ float2 sub2(float2 a, float2 b) { return __fadd2_rn(a, neg2(b)); }
+__device__ __forceinline__ float2 mul2(float2 a, float2 b) { return __fmul2_rn(a, b); }
+__device__ __forceinline__ float2 fma2(float2 a, float2 b, float2 c) { return __ffma2_rn(a, b, c); }
+
+__device__ __forceinline__ void two_sum2(float2 a, float2 b, float2& s, float2& t) {
+  s = add2(a, b);
+  const float2 bb = sub2(s, a);
+  t = add2(sub2(a, sub2(s, bb)), sub2(b, bb));
+}
+
+__device__ __forceinline__ void two_sum(float a, float b, float& s, float& t) {
+  s = a + b;
+  const float bb = s - a;
+  t = (a - (s - bb)) + (b - bb);
+}
+
+// exact FP64 -> (hi, lo) FP32 split with integer operations (as stage_mixed.cu)
+__device__ __forceinline__ void split_df(double u, float& hi, float& lo) {
+  const unsigned long long b = (unsigned long long)__double_as_longlong(u);
+  const unsigned int top = (unsigned int)(b >> 32);
+  const unsigned int sign = top & 0x80000000u;
+  const int e = (int)((top >> 20) & 0x7ffu);
+  if (e >= 1023 + 128) {
+    hi = __double2float_rn(u);
+    lo = 0.0f;
+    return;
+  }
+  if (e < 1023 - 126) {
+    hi = 0.0f;
+    lo = 0.0f;
+    return;
+  }
+  const unsigned int mhi = (unsigned int)((b >> 29) & 0x7fffffu);
+  hi = __int_as_float((int)(sign | ((unsigned int)(e - 1023 + 127) << 23) | mhi));
+  const unsigned int mlo = (unsigned int)(b & 0x1fffffffu);
+  if (e < 920 || mlo == 0u) {
+    lo = 0.0f;
+    return;
+  }
+  const float f = __int_as_float((int)(0x3f800000u | (mlo >> 6))) - 1.0f;
+  const float scale = __int_as_float((e - 919) << 23);
+  lo = __int_as_float(__float_as_int(f * scale) | (int)sign);
+}
+
+__device__ __forceinline__ double widen(float f) {
+  const unsigned int b = (unsigned int)__float_as_int(f);
+  const unsigned int e = (b >> 23) & 0xffu;
+  if (e == 0u)
+    return __longlong_as_double((long long)((unsigned long long)(b & 0x80000000u) << 32));
+  if (e == 0xffu) return (double)f;
+  const unsigned int hiw = (b & 0x80000000u) | ((e + 896u) << 20) | ((b & 0x7fffffu) >> 3);
+  return __hiloint2double((int)hiw, (int)((b & 0x7u) << 29));
+}
+
+// ---------------------------------------------------------------- geometry
+template <int N>
+struct P {
+  static constexpr int h = N / 2;
+  static constexpr int NN = N * N;
+  static constexpr int NP = N * N * N;
+  static constexpr int TAB2 = h * h;  // float2 (A, B) pairs per direction
+};
+
+constexpr int round128(int b) { return (b + 127) / 128 * 128; }
+
+// Shared-memory layout of one element slot (bytes).  Every region starts on a
+// 128-byte boundary (TMA destinations must be 16-byte aligned).
+template <int N, bool COMP, bool HAS_Y, bool HAS_B>
+struct Lay {
+  using S = P<N>;
+  static constexpr int kX = round128(COMP ? 4 * S::NP * 8 : 5 * S::NP * 4);  // staged X
+  static constexpr int kY = HAS_Y ? round128(5 * S::NP * 4) : 0;
+  static constexpr int kB = HAS_B ? round128(5 * S::NP * 8) : 0;
+  static constexpr int kFace = round128(12 * S::NN * (COMP ? 8 : 4));  // 3 dirs x 2 sides x 2
+  static constexpr int kBuf = kX + kY + kB + kFace;  // one pipeline buffer
+  static constexpr int kHiLo = 0;  // the double-float split is done as values are read
+  static constexpr int kS = round128(S::NP * 4);
+  static constexpr int kTab = round128((COMP ? 2 : 1) * 3 * S::TAB2 * 8);
+  static constexpr int kSlot = 2 * kBuf + kHiLo + kS + kTab;
+  // bytes the TMA copies of one element move (unpadded)
+  static constexpr uint32_t kXBytes = COMP ? 4 * S::NP * 8 : 5 * S::NP * 4;
+  static constexpr uint32_t kYBytes = HAS_Y ? 5 * S::NP * 4 : 0;
+  static constexpr uint32_t kBBytes = HAS_B ? 5 * S::NP * 8 : 0;
+};
+
+// packed even/odd contraction, plain FP32 (lanes: x = even part P, y = odd Q)
+template <int N>
+__device__ __forceinline__ void eo_line_p(const float (&x)[N], float (&out)[N],
+                                          const float2* __restrict__ tab) {
+  constexpr int h = N / 2;
+  float2 eo[h];
+#pragma unroll
+  for (int j = 0; j < h; ++j) eo[j] = make_float2(x[j] + x[N - 1 - j], x[j] - x[N - 1 - j]);
+#pragma unroll
+  for (int i = 0; i < h; ++i) {
+    float2 acc = mul2(tab[i * h], eo[0]);
+#pragma unroll
+    for (int j = 1; j < h; ++j) acc = fma2(tab[i * h + j], eo[j], acc);
+    out[i] = acc.x + acc.y;
+    out[N - 1 - i] = acc.y - acc.x;
+  }
+}
+
+// packed compensated contraction of a double-float line
+template <int N>
+__device__ __forceinline__ void eo_line_pdf(const float (&xh)[N], const float (&xl)[N],
+                                            float (&out)[N], const float2* __restrict__ th,
+                                            const float2* __restrict__ tl) {
+  constexpr int h = N / 2;
+  float2 eoh[h], eol[h];
+#pragma unroll
+  for (int j = 0; j < h; ++j) {
+    float2 s, t;
+    two_sum2(make_float2(xh[j], xh[j]), make_float2(xh[N - 1 - j], -xh[N - 1 - j]), s, t);
+    eoh[j] = s;
+    eol[j] = add2(t, make_float2(xl[j] + xl[N - 1 - j], xl[j] - xl[N - 1 - j]));
+  }
+#pragma unroll
+  for (int i = 0; i < h; ++i) {
+    float2 s = mul2(th[i * h], eoh[0]);
+    float2 c = fma2(th[i * h], eoh[0], neg2(s));
+    c = fma2(tl[i * h], eoh[0], c);
+    c = fma2(th[i * h], eol[0], c);
+#pragma unroll
+    for (int j = 1; j < h; ++j) {
+      const float2 a = th[i * h + j];
+      const float2 p = mul2(a, eoh[j]);
+      const float2 pe = fma2(a, eoh[j], neg2(p));
+      float2 t;
+      two_sum2(s, p, s, t);
+      c = add2(c, add2(t, pe));
+      c = fma2(tl[i * h + j], eoh[j], c);
+      c = fma2(a, eol[j], c);
+    }
+    // lanes: x = P_i (even part), y = Q_i (odd part)
+    out[i] = (s.x + s.y) + (c.x + c.y);
+    out[N - 1 - i] = (s.y - s.x) + (c.y - c.x);
+  }
+}
+
+template <int N, int EPB, bool COMP, bool HAS_Y, bool HAS_B>
+__global__ void __launch_bounds__(N * N * EPB)
+    stage_mixed_pipe_kernel(MixedLaunch L, int64_t n_groups) {
+  using S = P<N>;
+  using Y = Lay<N, COMP, HAS_Y, HAS_B>;
+  constexpr int NN = S::NN, NP = S::NP, h = S::h, TAB2 = S::TAB2;
+  constexpr int64_t VS = (int64_t)kVars * NP;
+  using FT = typename std::conditional<COMP, double, float>::type;  // staged field type
+
+  extern __shared__ __align__(128) unsigned char smem_raw[];
+  __shared__ uint64_t bars[2];
+  const int slot = threadIdx.x / NN;
+  const int t = threadIdx.x - slot * NN;
+  unsigned char* slot_base = smem_raw + (size_t)slot * Y::kSlot;
+  unsigned char* bufs[2] = {slot_base, slot_base + Y::kBuf};
+  float* Sacc = reinterpret_cast<float*>(slot_base + 2 * Y::kBuf + Y::kHiLo);
+  float2* tab = reinterpret_cast<float2*>(slot_base + 2 * Y::kBuf + Y::kHiLo + Y::kS);
+  const int ta = t % N, tb = t / N;
+  const uint64_t kLimitNs = 2000000000ull;  // 2 s per wait
+
+  if (threadIdx.x == 0) {
+    mbar_init(&bars[0], 1);
+    mbar_init(&bars[1], 1);
+    fence_mbar_init();
+  }
+  __syncthreads();
+
+  // issue the TMA copies of group g into buffer b (one thread)
+  auto issue_group = [&](int64_t g, int b) {
+    uint32_t bytes = 0;
+    for (int s = 0; s < EPB; ++s) {
+      const int64_t e = g * EPB + s;
+      if (e >= L.n_elem) break;
+      bytes += Y::kXBytes + Y::kYBytes + Y::kBBytes;
+    }
+    if (bytes == 0) return;
+    fence_proxy_async_smem();
+    mbar_arrive_expect_tx(&bars[b], bytes);
+    for (int s = 0; s < EPB; ++s) {
+      const int64_t e = g * EPB + s;
+      if (e >= L.n_elem) break;
+      unsigned char* dst = smem_raw + (size_t)s * Y::kSlot + (size_t)b * Y::kBuf;
+      if (COMP)
+        bulk_g2s(dst, L.x64 + e * VS + NP, Y::kXBytes, &bars[b]);
+      else
+        bulk_g2s(dst, L.x32 + e * VS, Y::kXBytes, &bars[b]);
+      if (HAS_Y) bulk_g2s(dst + Y::kX, L.y32 + e * VS, Y::kYBytes, &bars[b]);
+      if (HAS_B) bulk_g2s(dst + Y::kX + Y::kY, L.base64 + e * VS, Y::kBBytes, &bars[b]);
+    }
+  };
+  // prefetch this thread's 12 neighbour face values of element e into buffer b
+  auto issue_faces = [&](int64_t e, int b) {
+    if (e >= L.n_elem) return;
+    FT* face = reinterpret_cast<FT*>(bufs[b] + Y::kX + Y::kY + Y::kB);
+#pragma unroll
+    for (int d = 0; d < 3; ++d) {
+      int base, stride;
+      if (d == 0) {
+        base = N * ta + NN * tb;
+        stride = 1;
+      } else if (d == 1) {
+        base = ta + NN * tb;
+        stride = N;
+      } else {
+        base = ta + N * tb;
+        stride = NN;
+      }
+      const int64_t nlo = (int64_t)L.nbr[6 * e + 2 * d] * VS;
+      const int64_t nhi = (int64_t)L.nbr[6 * e + 2 * d + 1] * VS;
+      const int lo_pt = base + (N - 1) * stride, hi_pt = base;
+      const FT* src = COMP ? reinterpret_cast<const FT*>(L.x64) : reinterpret_cast<const FT*>(L.x32);
+      FT* f = face + (4 * d) * NN + t;
+      cp_async<sizeof(FT)>(f, src + nlo + NP + lo_pt);
+      cp_async<sizeof(FT)>(f + NN, src + nlo + (2 + d) * NP + lo_pt);
+      cp_async<sizeof(FT)>(f + 2 * NN, src + nhi + NP + hi_pt);
+      cp_async<sizeof(FT)>(f + 3 * NN, src + nhi + (2 + d) * NP + hi_pt);
+    }
+  };
+
+  const int64_t G = gridDim.x;
+  int64_t g = blockIdx.x;
+  if (g < n_groups) {
+    if (threadIdx.x == 0) issue_group(g, 0);
+    issue_faces(g * EPB + slot, 0);
+    cp_async_commit();
+  }
+  const float alpha = (float)L.alpha, beta = (float)L.beta, cf = (float)L.c;
+  for (int k = 0; g < n_groups; ++k, g += G) {
+    const int b = k & 1;
+    const int64_t gn = g + G;
+    const int64_t e = g * EPB + slot;
+    const bool active = e < L.n_elem;
+    if (threadIdx.x == 0 && gn < n_groups) issue_group(gn, b ^ 1);
+    // scaled split tables for this element (depend only on its Jacobian)
+    double jd[3] = {0.0, 0.0, 0.0};
+    if (active) {
+      jd[0] = L.jac[3 * e];
+      jd[1] = L.jac[3 * e + 1];
+      jd[2] = L.jac[3 * e + 2];
+      for (int q = t; q < 3 * TAB2; q += NN) {
+        const int d = q / TAB2, r = q - d * TAB2, i = r / h, j = r % h;
+        const double f = -L.c * jd[d];
+        const double va = f * L.eo.A[i][j], vb = f * L.eo.B[i][j];
+        const float ah = __double2float_rn(va), bh = __double2float_rn(vb);
+        tab[q] = make_float2(ah, bh);
+        if (COMP)
+          tab[3 * TAB2 + q] =
+              make_float2(__double2float_rn(va - (double)ah), __double2float_rn(vb - (double)bh));
+      }
+    }
+    const bool landed = mbar_wait(&bars[b], (uint32_t)((k >> 1) & 1), kLimitNs);
+    cp_async_wait_all();
+    if (__syncthreads_or(!landed)) {
+      // a copy did not land in time: record it, give copies still in flight
+      // one more bounded wait, and leave together
+      if (threadIdx.x == 0 && L.err) atomicExch(L.err, 1);
+      if (!landed) mbar_wait(&bars[b], (uint32_t)((k >> 1) & 1), kLimitNs);
+      return;
+    }
+    const unsigned char* buf = bufs[b];
+    const FT* X = reinterpret_cast<const FT*>(buf);
+    const float* Yb = reinterpret_cast<const float*>(buf + Y::kX);
+    const double* Bb = reinterpret_cast<const double*>(buf + Y::kX + Y::kY);
+    const FT* face = reinterpret_cast<const FT*>(buf + Y::kX + Y::kY + Y::kB);
+
+#pragma unroll 1
+    for (int d = 0; d < 3; ++d) {
+      if (active) {
+        int base, stride;
+        if (d == 0) {
+          base = N * ta + NN * tb;
+          stride = 1;
+        } else if (d == 1) {
+          base = ta + NN * tb;
+          stride = N;
+        } else {
+          base = ta + N * tb;
+          stride = NN;
+        }
+        const float2* th = tab + d * TAB2;
+        const float2* tl = tab + 3 * TAB2 + d * TAB2;
+        float dF[N], dP[N], pih[N], fh[N];
+        float pil[N], fl[N];
+        if (COMP) {
+          // X holds Pi, Phi_x, Phi_y, Phi_z in FP64; split as read
+#pragma unroll
+          for (int i = 0; i < N; ++i) {
+            split_df((double)X[base + i * stride], pih[i], pil[i]);
+            split_df((double)X[(1 + d) * NP + base + i * stride], fh[i], fl[i]);
+          }
+          eo_line_pdf<N>(fh, fl, dF, th, tl);
+          eo_line_pdf<N>(pih, pil, dP, th, tl);
+        } else {
+#pragma unroll
+          for (int i = 0; i < N; ++i) {
+            pih[i] = X[NP + base + i * stride];
+            fh[i] = X[(2 + d) * NP + base + i * stride];
+            pil[i] = 0.0f;
+            fl[i] = 0.0f;
+          }
+          eo_line_p<N>(fh, dF, th);
+          eo_line_p<N>(pih, dP, th);
+        }
+        // UpwindPenalty corrections at both ends of the line (see stage_mixed.cu)
+        const float G2 = (float)(-0.25 * L.c * (double)(N * (N - 1)) * jd[d]);
+        const FT* fc = face + (4 * d) * NN + t;
+        float dw_lo, dw_hi;
+        if (COMP) {
+          float ph, pl, qh, ql, wih, wil, weh, wel, t1, dh;
+          split_df((double)fc[0], ph, pl);
+          split_df((double)fc[NN], qh, ql);
+          two_sum(pih[0], fh[0], wih, t1);
+          wil = t1 + (pil[0] + fl[0]);
+          two_sum(ph, qh, weh, t1);
+          wel = t1 + (pl + ql);
+          two_sum(wih, -weh, dh, t1);
+          dw_lo = dh + (t1 + (wil - wel));
+          split_df((double)fc[2 * NN], ph, pl);
+          split_df((double)fc[3 * NN], qh, ql);
+          two_sum(pih[N - 1], -fh[N - 1], wih, t1);
+          wil = t1 + (pil[N - 1] - fl[N - 1]);
+          two_sum(ph, -qh, weh, t1);
+          wel = t1 + (pl - ql);
+          two_sum(wih, -weh, dh, t1);
+          dw_hi = dh + (t1 + (wil - wel));
+        } else {
+          dw_lo = (pih[0] + fh[0]) - ((float)fc[0] + (float)fc[NN]);
+          dw_hi = (pih[N - 1] - fh[N - 1]) - ((float)fc[2 * NN] - (float)fc[3 * NN]);
+        }
+        dF[0] = fmaf(G2, dw_lo, dF[0]);
+        dP[0] = fmaf(G2, dw_lo, dP[0]);
+        dF[N - 1] = fmaf(G2, dw_hi, dF[N - 1]);
+        dP[N - 1] = fmaf(-G2, dw_hi, dP[N - 1]);
+        // Phi_d output
+        const int64_t vo = e * VS + (2 + d) * NP + base;
+#pragma unroll
+        for (int i = 0; i < N; ++i) {
+          float w = dP[i];
+          if (!COMP) {
+            w = fmaf(alpha, fh[i], w);
+            if (HAS_Y) w = fmaf(beta, Yb[(2 + d) * NP + base + i * stride], w);
+          }
+          if (L.w32) L.w32[vo + i * stride] = w;
+          if (L.out64) {
+            if (HAS_B)
+              L.out64[vo + i * stride] = Bb[(2 + d) * NP + base + i * stride] + widen(w);
+            else
+              L.out64[vo + i * stride] = widen(w);
+          }
+        }
+        if (d < 2) {
+#pragma unroll
+          for (int i = 0; i < N; ++i) {
+            if (d == 0)
+              Sacc[base + i * stride] = dF[i];
+            else
+              Sacc[base + i * stride] += dF[i];
+          }
+        } else {
+#pragma unroll
+          for (int i = 0; i < N; ++i) {
+            const int p = base + i * stride;
+            float wpi = Sacc[p] + dF[i];
+            float wpsi = COMP ? fmaf(-cf, pih[i], -cf * pil[i]) : -cf * pih[i];
+            if (!COMP) {
+              wpi = fmaf(alpha, pih[i], wpi);
+              wpsi = fmaf(alpha, X[p], wpsi);
+              if (HAS_Y) {
+                wpi = fmaf(beta, Yb[NP + p], wpi);
+                wpsi = fmaf(beta, Yb[p], wpsi);
+              }
+            }
+            if (L.w32) {
+              L.w32[e * VS + NP + p] = wpi;
+              L.w32[e * VS + p] = wpsi;
+            }
+            if (L.out64) {
+              if (HAS_B) {
+                L.out64[e * VS + NP + p] = Bb[NP + p] + widen(wpi);
+                L.out64[e * VS + p] = Bb[p] + widen(wpsi);
+              } else {
+                L.out64[e * VS + NP + p] = widen(wpi);
+                L.out64[e * VS + p] = widen(wpsi);
+              }
+            }
+          }
+        }
+      }
+      if (d < 2) __syncthreads();
+    }
+    // neighbour faces of the next group, then release this buffer
+    if (gn < n_groups) issue_faces(gn * EPB + slot, b ^ 1);
+    cp_async_commit();
+    __syncthreads();
+  }
+  cp_async_wait_all();
+}
+
+template <int N>
+constexpr int pipe_epb_target() {
+  return N <= 4 ? 8 : (N <= 6 ? 4 : 2);
+}
+
+// Elements per CTA: the target, reduced until the double-buffered slots fit
+// the 227 KB of shared memory a CTA may use; 0 when one slot does not fit.
+constexpr int kSmemLimit = 227 * 1024;
+template <int N, bool COMP, bool HAS_Y, bool HAS_B>
+constexpr int pipe_epb() {
+  constexpr int slot = Lay<N, COMP, HAS_Y, HAS_B>::kSlot;
+  constexpr int fit = kSmemLimit / slot;
+  return fit < pipe_epb_target<N>() ? fit : pipe_epb_target<N>();
+}
+
+template <int N, bool COMP, bool HAS_Y, bool HAS_B>
+cudaError_t launch_pipe(const MixedLaunch& L, cudaStream_t s) {
+  constexpr int EPB_FIT = pipe_epb<N, COMP, HAS_Y, HAS_B>();
+  if (EPB_FIT < 1) return launch_stage_mixed(L, s);  // too large to double-buffer
+  constexpr int EPB = EPB_FIT < 1 ? 1 : EPB_FIT;
+  using Y = Lay<N, COMP, HAS_Y, HAS_B>;
+  const size_t smem = (size_t)EPB * Y::kSlot;
+  auto k = stage_mixed_pipe_kernel<N, EPB, COMP, HAS_Y, HAS_B>;
+  cudaError_t err = cudaFuncSetAttribute(k, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+  if (err != cudaSuccess) return err;
+  err = cudaFuncSetAttribute(k, cudaFuncAttributePreferredSharedMemoryCarveout,
+                             cudaSharedmemCarveoutMaxShared);
+  if (err != cudaSuccess) return err;
+  int dev = 0, sms = 0, per_sm = 0;
+  if ((err = cudaGetDevice(&dev)) != cudaSuccess) return err;
+  if ((err = cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev)) != cudaSuccess)
+    return err;
+  if ((err = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k, N * N * EPB, smem)) !=
+      cudaSuccess)
+    return err;
+  if (per_sm < 1) return cudaErrorInvalidConfiguration;
+  const int64_t groups = (L.n_elem + EPB - 1) / EPB;
+  if (groups <= 0) return cudaSuccess;
+  int64_t grid = (int64_t)sms * per_sm;
+  if (grid > groups) grid = groups;
+  k<<<(unsigned)grid, N * N * EPB, smem, s>>>(L, groups);
+  return cudaGetLastError();
+}
+
+template <int N>
+cudaError_t launch_pipe_n(const MixedLaunch& L, cudaStream_t s) {
+  const bool y = L.y32 != nullptr, bb = L.base64 != nullptr && L.out64 != nullptr;
+  if (L.x64) {
+    if (y) return cudaErrorInvalidValue;
+    return bb ? launch_pipe<N, true, false, true>(L, s) : launch_pipe<N, true, false, false>(L, s);
+  }
+  if (y) return bb ? launch_pipe<N, false, true, true>(L, s) : launch_pipe<N, false, true, false>(L, s);
+  return bb ? launch_pipe<N, false, false, true>(L, s) : launch_pipe<N, false, false, false>(L, s);
+}
+
+}  // namespace
+
+bool mixed_pipe_supported(int n) { return n % 2 == 0 && n >= 2 && n <= kMaxN; }
+
+cudaError_t launch_stage_mixed_pipe(const MixedLaunch& L, cudaStream_t s) {
+  if ((L.x64 == nullptr) == (L.x32 == nullptr)) return cudaErrorInvalidValue;
+  switch (L.n) {
+    case 2: return launch_pipe_n<2>(L, s);
+    case 4: return launch_pipe_n<4>(L, s);
+    case 6: return launch_pipe_n<6>(L, s);
+    case 8: return launch_pipe_n<8>(L, s);
+    case 10: return launch_pipe_n<10>(L, s);
+    case 12: return launch_pipe_n<12>(L, s);
+    default: return cudaErrorInvalidValue;
+  }
+}
+
+}  // namespace dgsw

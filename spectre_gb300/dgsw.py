@@ -34,6 +34,7 @@ STATUS_NAMES = {
     -3: "DGSW_ERR_UNSUPPORTED",
     -4: "DGSW_ERR_NOT_FINITE",
     -5: "DGSW_ERR_NO_DEVICE",
+    -6: "DGSW_ERR_DEVICE_TIMEOUT",
 }
 PRECISION_FP64 = 0
 PRECISION_MIXED = 1
@@ -120,6 +121,16 @@ def _check(status: int, handle=None):
     if status != DGSW_OK:
         msg = lib().dgsw_last_error(handle)
         raise DgswError(status, msg.decode() if msg else "")
+
+
+def _torch_ready(*tensors):
+    """Orders work queued by torch on its current stream before a library call
+    that reads or writes these device tensors on the handle's own stream."""
+    for t in tensors:
+        if t is not None and hasattr(t, "is_cuda") and t.is_cuda:
+            import torch
+            torch.cuda.current_stream(t.device).synchronize()
+            return
 
 
 def _ptr(a) -> int:
@@ -242,6 +253,8 @@ class UpwindPenalty:
         import torch
         npts = psi.numel()
         out = torch.empty((N_PACKAGED, npts), dtype=torch.float64, device=psi.device)
+        if stream is None:
+            _torch_ready(psi)
         _check(lib().dgsw_package_data_device(
             npts, _ptr(psi), _ptr(pi), _ptr(phi), _ptr(constraint_gamma2),
             _ptr(normal_covector),
@@ -256,6 +269,8 @@ class UpwindPenalty:
         import torch
         npts = packaged_int.shape[1]
         out = torch.empty((N_VARS, npts), dtype=torch.float64, device=packaged_int.device)
+        if stream is None:
+            _torch_ready(packaged_int)
         _check(lib().dgsw_boundary_terms_device(npts, _ptr(packaged_int), _ptr(packaged_ext),
                                                 _ptr(out), stream))
         return out
@@ -334,6 +349,7 @@ class DgEvolution:
     def set_state(self, u):
         """u: numpy float64 host array or torch float64 tensor (host or cuda)."""
         if hasattr(u, "is_cuda") and u.is_cuda:
+            _torch_ready(u)
             _check(lib().dgsw_set_state_device(self._h, _ptr(u)), self._h)
             self.synchronize()
         else:
@@ -345,6 +361,7 @@ class DgEvolution:
 
     def get_state(self, out=None):
         if out is not None and hasattr(out, "is_cuda") and out.is_cuda:
+            _torch_ready(out)
             _check(lib().dgsw_get_state_device(self._h, _ptr(out)), self._h)
             self.synchronize()
             return out
@@ -363,6 +380,7 @@ class DgEvolution:
         if hasattr(u, "is_cuda") and u.is_cuda:
             import torch
             out = torch.empty_like(u)
+            _torch_ready(u, out)
             _check(lib().dgsw_rhs_device(self._h, _ptr(u), _ptr(out)), self._h)
             self.synchronize()
             return out
@@ -374,6 +392,7 @@ class DgEvolution:
     def volume_rhs(self, u_dev):
         import torch
         out = torch.empty_like(u_dev)
+        _torch_ready(u_dev, out)
         _check(lib().dgsw_volume_rhs_device(self._h, _ptr(u_dev), _ptr(out)), self._h)
         self.synchronize()
         return out

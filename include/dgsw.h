@@ -175,6 +175,27 @@ int dgsw_index_maps(const DgswConfig* config, uint64_t* element_ids,
 int dgsw_count_elements(const DgswConfig* config, int64_t* n_elements,
                         int64_t* state_doubles);
 
+/* ---- stepping without any allocation ---------------------------------------
+ * No counterpart in the reference.  For callers that cannot allocate device
+ * memory while they step (a host framework that owns a fixed device-memory
+ * budget, or a caller that must not trigger the device-wide synchronisation
+ * of cudaMalloc/cudaFree): n_steps plain-FP64 SSP-RK3 steps of one periodic
+ * brick, in place on the caller's device state dev_u (layout as
+ * dgsw_set_state), on `stream` (a cudaStream_t or NULL).  Creates no handle
+ * and calls no allocating routine: the stage states and element tables live
+ * in one fixed 32 MiB device array inside the library, held by every GPU that
+ * loads it until the process exits.  The limit is
+ *   2 * elements * 5 * points^3 + 6 * elements <= 4,194,304 doubles
+ * (e.g. 8^3 elements at 8 points, 12^3 elements at 5 points); larger bricks
+ * return DGSW_ERR_ARGUMENT.  The first call on a device looks up the array's
+ * device address (with that device current); make it before any stream
+ * capture.  Calls share the array: calls that overlap on the GPU race.
+ * Errors: dgsw_noalloc_last_error(). */
+int dgsw_step_noalloc(const DgswBrick* brick, int points, double gamma2,
+                      double* dev_u, int n_steps, double dt, void* stream);
+size_t dgsw_noalloc_scratch_bytes(void);
+const char* dgsw_noalloc_last_error(void);
+
 #ifdef __cplusplus
 }
 #endif

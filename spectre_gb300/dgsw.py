@@ -92,6 +92,9 @@ _SIGNATURES = {
     "dgsw_index_maps": (_I, [ctypes.POINTER(DgswConfig), _P, _P, _P]),
     "dgsw_count_elements": (_I, [ctypes.POINTER(DgswConfig), ctypes.POINTER(_I64),
                                  ctypes.POINTER(_I64)]),
+    "dgsw_step_noalloc": (_I, [ctypes.POINTER(DgswBrick), _I, _D, _P, _I, _D, _P]),
+    "dgsw_noalloc_scratch_bytes": (ctypes.c_size_t, []),
+    "dgsw_noalloc_last_error": (ctypes.c_char_p, []),
 }
 
 _lib_handle = None

@@ -228,6 +228,99 @@ def time_path(args, precision, dev, rank, ws, sample_clocks):
     return ev, ms, clocks, state, warm
 
 
+def time_batched(args, dev):
+    """Config 3: 256 independent evolutions, per-element LGL extents in
+    {4..10}, p-nonconforming mortars, Gaussian pulses; FP64 and mixed, and
+    the worst per-instance rel L2 of mixed against FP64 after the same steps."""
+    import torch
+    from spectre_gb300 import DgEvolution, PRECISION_FP64, PRECISION_MIXED, workloads
+    bricks, pts, params = workloads.batched_instances(256, seed=2024)
+    dt = 1e-4
+    steps = max(1, min(args.steps, 20))
+    res = {}
+    states = {}
+    for name, prec in (("fp64", PRECISION_FP64), ("mixed", PRECISION_MIXED)):
+        ev = DgEvolution(bricks, pts, precision=prec, device=dev)
+        ev.set_initial_data("gaussian", params)
+        for _ in range(3):
+            ev.step(1, dt, sync=False)
+        ev.synchronize()
+        stream = torch.cuda.ExternalStream(ev.stream_ptr(), device=dev)
+        e0 = torch.cuda.Event(enable_timing=True)
+        e1 = torch.cuda.Event(enable_timing=True)
+        torch.cuda.synchronize()
+        e0.record(stream)
+        ev.step(steps, dt, sync=False)
+        e1.record(stream)
+        e1.synchronize()
+        ms = e0.elapsed_time(e1)
+        states[name] = ev.get_state()
+        res[name] = {"value": ev.grid_points * 3 * steps / (ms * 1e-3), "unit": UNIT,
+                     "ms_per_step": ms / steps}
+        points = ev.grid_points
+        n_elem = ev.n_elements
+        ev.close()
+    # per-instance relative L2 of mixed vs FP64 after 3 + steps steps
+    worst = 0.0
+    off = 0
+    e = 0
+    for b in bricks:
+        ne = b.elements[0] * b.elements[1] * b.elements[2]
+        size = int(5 * np.sum(np.asarray(pts[e:e + ne], dtype=np.int64) ** 3))
+        a = states["fp64"][off:off + size]
+        m = states["mixed"][off:off + size]
+        worst = max(worst, float(np.linalg.norm(m - a) / np.linalg.norm(a)))
+        off += size
+        e += ne
+    return {"workload": "256 periodic ScalarWave evolutions on [0,2pi]^3, elements per axis "
+                        "U{2..8}, LGL points per element U{4..10} (p-nonconforming mortars), "
+                        "Gaussian pulses, SSP-RK3 dt=1e-4, seed 2024",
+            "grid_points": points, "elements": n_elem, "steps": steps,
+            "fp64": res["fp64"], "mixed": res["mixed"],
+            "mixed_speedup_vs_fp64": res["fp64"]["ms_per_step"] / res["mixed"]["ms_per_step"],
+            "max_instance_rel_l2_mixed_vs_fp64": worst, "steps_compared": 3 + steps}
+
+
+def time_adjoint(dev):
+    """Config 4: 8^3 elements x 8^3 points, dt 5e-4, 2000 SSP-RK3 steps, 64
+    samples every 10 steps; seconds per gradient (forward misfit run + the
+    discrete adjoint sweep), with central-difference and tangent-linear checks
+    along seeded directions."""
+    import torch
+    from spectre_gb300.adjoint import MisfitProblem
+    p = MisfitProblem(device=dev)
+    try:
+        psi0 = p.initial_psi()
+        p.value_and_gradient(psi0)  # warm-up (graph capture)
+        torch.cuda.synchronize()
+        reps = 3
+        t0 = time.perf_counter()
+        for _ in range(reps):
+            J, g = p.value_and_gradient(psi0)
+        torch.cuda.synchronize()
+        s_per_grad = (time.perf_counter() - t0) / reps
+        rng = torch.Generator(device="cuda").manual_seed(11)
+        eps = 1e-6
+        fd_err = 0.0
+        for _ in range(2):
+            v = torch.randn(psi0.shape, dtype=torch.float64, device="cuda", generator=rng)
+            fd = (p.value(psi0 + eps * v) - p.value(psi0 - eps * v)) / (2 * eps)
+            ad = float(torch.sum(g * v))
+            fd_err = max(fd_err, abs(fd - ad) / abs(ad))
+        v = torch.randn(psi0.shape, dtype=torch.float64, device="cuda", generator=rng)
+        tl = p.tangent_linear(psi0, v)
+        tl_err = abs(tl - float(torch.sum(g * v))) / abs(tl)
+        return {"workload": "ScalarWave 8^3 elements x 8^3 LGL points, FP64, SSP-RK3 dt=5e-4, "
+                            "2000 steps, 64 seeded samples of Psi every 10 steps; control Psi(t=0)",
+                "s_per_grad": s_per_grad, "J": J,
+                "fd_max_rel_err_2_dirs": fd_err, "tangent_linear_rel_err": tl_err,
+                "note": "forward misfit run + hand-written discrete adjoint sweep (3 L^T "
+                        "launches per step); the step map is linear, so no forward states "
+                        "are stored"}
+    finally:
+        p.close()
+
+
 def run_ours(args):
     import torch
     from spectre_gb300 import PRECISION_FP64, PRECISION_MIXED
@@ -286,6 +379,13 @@ def run_ours(args):
                               "bytes_per_point_launch": MIXED_BYTES_PER_POINT_LAUNCH,
                               "avg_launch_ms": launch_m}}
 
+    batched = None
+    if not args.no_batched:
+        batched = time_batched(args, dev)
+    adjoint = None
+    if not args.no_adjoint:
+        adjoint = time_adjoint(dev)
+
     cpu = None
     if rank == 0 and not args.no_cpu_baseline:
         threads = cpu_threads()
@@ -312,8 +412,9 @@ def run_ours(args):
                           "inst_per_point_stage": FP64_INST_PER_POINT_STAGE,
                           "note": "FP64 pipe binds the plain path on GB300; peak from a "
                                   "DFMA/DADD throughput probe on this pool's GB300"},
-            "mixed": mixed, "cpu_baseline": cpu, "e2e": e2e, "clocks": clocks,
+            "mixed": mixed, "batched": batched, "adjoint": adjoint, "cpu_baseline": cpu, "e2e": e2e, "clocks": clocks,
             "gpu_launches": 3 * args.steps,
+            "gpu_launches_note": "stage kernels of the timed FP64 region (one launch per stage)",
         }
         print(json.dumps(line), flush=True)
     if ws > 1:
@@ -329,6 +430,8 @@ def main():
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--no-mixed", action="store_true")
+    ap.add_argument("--no-batched", action="store_true")
+    ap.add_argument("--no-adjoint", action="store_true")
     ap.add_argument("--elements", type=int, default=ELEMS,
                     help="elements per axis (default 32: the benchmark workload; smaller "
                          "values only for profiling captures)")

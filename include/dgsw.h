@@ -151,6 +151,30 @@ int dgsw_boundary_terms_device(int64_t npts, const double* packaged_int,
 int dgsw_step(DgswHandle h, int n_steps, double dt);
 int dgsw_substep(DgswHandle h, int k, double dt);
 
+/* ---- discrete adjoint and the misfit objective -----------------------------
+ * FP64, one brick of uniform extent, gamma2 = 0.  The step map of this path
+ * is linear (fixed normals and char speeds), so the reverse sweep needs only
+ * the recorded residuals, not the forward states.
+ * dgsw_adjoint_rhs_device: lambda -> L^T lambda, the exact transpose of the
+ * operator dgsw_rhs_device applies.
+ * dgsw_set_samples: points (x, y, z per point) where Psi is sampled by
+ * barycentric Lagrange interpolation on the element's LGL nodes
+ * (Spectral.cpp:625-670 weights; the role of IrregularInterpolant,
+ * NumericalAlgorithms/Interpolation/IrregularInterpolant.cpp:257-319).
+ * dgsw_sample_psi: Psi of the current state at the sample points (host).
+ * dgsw_misfit_forward: advances the state by n_windows x steps_per_window
+ * steps, sampling after each window; J = sum (sample - target)^2, targets
+ * n_windows x n_samples (host, window-major).
+ * dgsw_misfit_adjoint: dJ/du at the start of the last dgsw_misfit_forward,
+ * state-sized, into dev_grad (device); the adjoint of Rk3HesthavenSsp run
+ * backwards with 2 (sample - target) injected at each window. */
+int dgsw_adjoint_rhs_device(DgswHandle h, const double* dev_lambda, double* dev_out);
+int dgsw_set_samples(DgswHandle h, int n_samples, const double* xyz);
+int dgsw_sample_psi(DgswHandle h, double* host_out);
+int dgsw_misfit_forward(DgswHandle h, int n_windows, int steps_per_window, double dt,
+                        const double* host_targets, double* J);
+int dgsw_misfit_adjoint(DgswHandle h, double* dev_grad);
+
 /* ---- host-only setup (no GPU) ---------------------------------------------
  * Spectral::collocation_points / quadrature_weights <Legendre, GaussLobatto>
  * (NumericalAlgorithms/Spectral/Legendre.cpp:186-239) */

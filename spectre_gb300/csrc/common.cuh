@@ -37,4 +37,11 @@ enum : int {
   kModeStage = 3       // out = a u0 + b ucur + c L(ucur)
 };
 
+// Arithmetic classes of the general (mixed-extent) kernel.
+enum : int {
+  kPrecF64 = 0,   // FP64 throughout
+  kPrecComp = 1,  // FP64 input, compensated double-float FP32 arithmetic
+  kPrecF32 = 2    // FP32 input and arithmetic
+};
+
 }  // namespace dgsw

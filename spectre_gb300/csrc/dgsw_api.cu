@@ -44,6 +44,31 @@ struct DgswHandle_ {
   double* params = nullptr;  // initial-data parameters
   size_t params_cap = 0;
   EoTable eo{};
+  // elements of differing extents: one task list per extent, the face
+  // operators T(n, nn) and a split-table per extent
+  bool general = false;
+  int32_t* class_tasks[kMaxN + 1] = {};
+  int64_t class_count[kMaxN + 1] = {};
+  EoTable class_eo[kMaxN + 1] = {};
+  double* op64 = nullptr;
+  float* op_hi = nullptr;
+  float* op_lo = nullptr;
+  int32_t* op_off = nullptr;
+  // misfit objective and discrete adjoint (uniform FP64 path)
+  EoTable eoT{};
+  int n_samples = 0;
+  int64_t* samp_off = nullptr;
+  double* samp_w = nullptr;
+  double* adj = nullptr;   // adjoint state
+  double* adjz = nullptr;  // adjoint stage combination
+  double* targets = nullptr;
+  double* residuals = nullptr;
+  int64_t record_cap = 0;  // windows x samples the two buffers above hold
+  int rec_windows = 0, rec_steps = 0;
+  double rec_dt = 0.0;
+  cudaGraphExec_t graph_adj = nullptr;
+  int graph_adj_steps = 0;
+  double graph_adj_dt = std::nan("");
   // graphs of whole steps
   cudaGraphExec_t graph_one = nullptr;
   cudaGraphExec_t graph_many = nullptr;
@@ -127,6 +152,49 @@ cudaError_t launch_mixed(DgswHandle h, const MixedLaunch& L) {
   return launch_stage_mixed(L, h->stream);
 }
 
+GeneralLaunch base_general(DgswHandle h) {
+  GeneralLaunch G;
+  G.offset = h->offset;
+  G.elem_n = h->elem_n;
+  G.nbr = h->nbr;
+  G.jac = h->jac;
+  G.op64 = h->op64;
+  G.op_hi = h->op_hi;
+  G.op_lo = h->op_lo;
+  G.op_off = h->op_off;
+  G.gamma2 = h->cfg.gamma2;
+  return G;
+}
+
+// One launch per extent class present in the domain.
+cudaError_t launch_general_classes(DgswHandle h, GeneralLaunch G) {
+  for (int n = kMinN; n <= kMaxN; ++n) {
+    if (h->class_count[n] == 0) continue;
+    G.n = n;
+    G.tasks = h->class_tasks[n];
+    G.n_tasks = h->class_count[n];
+    G.eo = h->class_eo[n];
+    cudaError_t e = launch_stage_general(G, h->stream);
+    if (e != cudaSuccess) return e;
+  }
+  return cudaSuccess;
+}
+
+// FP64 stage on the general path: out = alpha x + beta y + c L(x)
+cudaError_t general_f64(DgswHandle h, const double* x, const double* y, double* out, double alpha,
+                        double beta, double c, int boundary = 1) {
+  GeneralLaunch G = base_general(h);
+  G.prec = kPrecF64;
+  G.x64 = x;
+  G.y64 = y;
+  G.out64 = out;
+  G.alpha = alpha;
+  G.beta = beta;
+  G.c = c;
+  G.boundary = boundary;
+  return launch_general_classes(h, G);
+}
+
 // Reads and clears the device error word; DGSW_ERR_DEVICE_TIMEOUT when set.
 int check_device_error(DgswHandle h) {
   if (!h->dev_err) return DGSW_OK;
@@ -146,6 +214,33 @@ int check_device_error(DgswHandle h) {
 //   B: w2 = w1/2 + dt/4 L(w1)                [u0 + w2]
 //   C: u  = u0 + 2/3 (w2 + w1) + 2dt/3 L(w2)
 cudaError_t enqueue_mixed_stage(DgswHandle h, int k, double dt, const double* u0, double* out) {
+  if (h->general) {
+    GeneralLaunch G = base_general(h);
+    if (k == 0) {
+      G.prec = kPrecComp;
+      G.x64 = u0;
+      G.c = dt;
+      G.w32 = h->w1;
+    } else if (k == 1) {
+      G.prec = kPrecF32;
+      G.x32 = h->w1;
+      G.alpha = 0.5;
+      G.c = 0.25 * dt;
+      G.w32 = h->w2;
+    } else {
+      G.prec = kPrecF32;
+      G.x32 = h->w2;
+      G.y32 = h->w1;
+      G.alpha = 2.0 / 3.0;
+      G.beta = 2.0 / 3.0;
+      G.c = (2.0 / 3.0) * dt;
+    }
+    if (out) {
+      G.out64 = out;
+      G.base64 = u0;
+    }
+    return launch_general_classes(h, G);
+  }
   MixedLaunch L = base_mixed(h);
   if (k == 0) {
     L.x64 = u0;
@@ -182,6 +277,13 @@ cudaError_t enqueue_step(DgswHandle h, double dt) {
     if (e != cudaSuccess) return e;
     return enqueue_mixed_stage(h, 2, dt, h->state, h->state);
   }
+  if (h->general) {
+    cudaError_t e = general_f64(h, h->state, nullptr, h->t1, 1.0, 0.0, dt);
+    if (e != cudaSuccess) return e;
+    e = general_f64(h, h->t1, h->state, h->t2, 0.25, 0.75, 0.25 * dt);
+    if (e != cudaSuccess) return e;
+    return general_f64(h, h->t2, h->state, h->state, 2.0 / 3.0, 1.0 / 3.0, (2.0 / 3.0) * dt);
+  }
   StageLaunch L = base_launch(h);
   L.mode = kModeStageFirst;
   L.ucur = h->state;
@@ -202,6 +304,67 @@ cudaError_t enqueue_step(DgswHandle h, double dt) {
   L.unext = h->state;
   L.coef = {1.0 / 3.0, 2.0 / 3.0, (2.0 / 3.0) * dt};
   return launch_stage(h, L);
+}
+
+AdjointLaunch base_adjoint(DgswHandle h) {
+  AdjointLaunch A;
+  A.n = h->dom.elem_n.empty() ? 0 : h->dom.elem_n[0];
+  A.n_elem = h->dom.n_elem;
+  A.nbr = h->nbr;
+  A.jac = h->jac;
+  A.eoT = h->eoT;
+  return A;
+}
+
+// One step of the discrete adjoint of Rk3HesthavenSsp (Rk3HesthavenSsp.cpp:63-80)
+// on h->adj.  Reverse of u1 = u0 + dt L u0, u2 = 3/4 u0 + 1/4 (u1 + dt L u1),
+// u3 = 1/3 u0 + 2/3 (u2 + dt L u2):
+//   m2 = 2/3 (l + dt L^T l);  m1 = 1/4 (m2 + dt L^T m2);
+//   l <- m1 + dt L^T m1 + 3/4 m2 + 1/3 l.
+cudaError_t enqueue_adjoint_step(DgswHandle h, double dt) {
+  AdjointLaunch A = base_adjoint(h);
+  A.x = h->adj;
+  A.out = h->t1;
+  A.alpha = 2.0 / 3.0;
+  A.c = (2.0 / 3.0) * dt;
+  cudaError_t e = launch_adjoint_fp64(A, h->stream);
+  if (e != cudaSuccess) return e;
+  A = base_adjoint(h);
+  A.x = h->t1;
+  A.y = h->adj;
+  A.out = h->t2;
+  A.alpha = 0.25;
+  A.c = 0.25 * dt;
+  A.out2 = h->adjz;
+  A.alpha2 = 0.75;
+  A.beta2 = 1.0 / 3.0;
+  e = launch_adjoint_fp64(A, h->stream);
+  if (e != cudaSuccess) return e;
+  A = base_adjoint(h);
+  A.x = h->t2;
+  A.y = h->adjz;
+  A.out = h->adj;
+  A.alpha = 1.0;
+  A.beta = 1.0;
+  A.c = dt;
+  return launch_adjoint_fp64(A, h->stream);
+}
+
+cudaError_t capture_adjoint_steps(DgswHandle h, double dt, int steps, cudaGraphExec_t* out) {
+  cudaGraph_t g = nullptr;
+  cudaError_t e = cudaStreamBeginCapture(h->stream, cudaStreamCaptureModeThreadLocal);
+  if (e != cudaSuccess) return e;
+  cudaError_t le = cudaSuccess;
+  for (int s = 0; s < steps && le == cudaSuccess; ++s) le = enqueue_adjoint_step(h, dt);
+  e = cudaStreamEndCapture(h->stream, &g);
+  if (le != cudaSuccess) {
+    if (g) cudaGraphDestroy(g);
+    return le;
+  }
+  if (e != cudaSuccess) return e;
+  e = cudaGraphInstantiate(out, g, 0);
+  cudaGraphDestroy(g);
+  return e;
 }
 
 cudaError_t capture_steps(DgswHandle h, double dt, int steps, cudaGraphExec_t* out) {
@@ -289,10 +452,6 @@ int dgsw_create(const DgswConfig* cfg, DgswHandle* out) {
   }
   h->cfg.bricks = nullptr;  // copies live in h->dom
   h->cfg.points_per_element = nullptr;
-  if (!h->dom.uniform) {
-    delete h;
-    return fail(nullptr, DGSW_ERR_UNSUPPORTED, "elements of different extents are not supported yet");
-  }
   if (cfg->precision == DGSW_PRECISION_MIXED && cfg->gamma2 != 0.0) {
     delete h;
     return fail(nullptr, DGSW_ERR_UNSUPPORTED, "mixed precision needs gamma2 = 0");
@@ -348,6 +507,41 @@ int dgsw_create(const DgswConfig* cfg, DgswHandle* out) {
   }
   if ((e = upload(&h->lgl_x, nodes)) != cudaSuccess) return bail(e, "upload nodes");
   lgl_eo_table(h->dom.elem_n[0], &h->eo);
+  lgl_eo_table_transposed(h->dom.elem_n[0], &h->eoT);
+  if (!h->dom.uniform) {
+    h->general = true;
+    std::vector<int32_t> lists[kMaxN + 1];
+    for (int64_t el = 0; el < h->dom.n_elem; ++el) lists[h->dom.elem_n[el]].push_back((int32_t)el);
+    for (int n = kMinN; n <= kMaxN; ++n) {
+      h->class_count[n] = (int64_t)lists[n].size();
+      lgl_eo_table(n, &h->class_eo[n]);
+      if (!lists[n].empty() && (e = upload(&h->class_tasks[n], lists[n])) != cudaSuccess)
+        return bail(e, "upload task list");
+    }
+    // face operators: interpolation (nn < n) or modal restriction (nn > n)
+    std::vector<double> ops;
+    std::vector<int32_t> op_off((kMaxN + 1) * (kMaxN + 1), -1);
+    double buf[kMaxN * kMaxN];
+    for (int n = kMinN; n <= kMaxN; ++n)
+      for (int nn = kMinN; nn <= kMaxN; ++nn) {
+        if (nn == n) continue;
+        if (nn < n)
+          lgl_mortar_projections(nn, n, buf, nullptr);  // n x nn
+        else
+          lgl_mortar_projections(n, nn, nullptr, buf);  // n x nn
+        op_off[n * (kMaxN + 1) + nn] = (int32_t)ops.size();
+        ops.insert(ops.end(), buf, buf + n * nn);
+      }
+    std::vector<float> hi(ops.size()), lo(ops.size());
+    for (size_t i = 0; i < ops.size(); ++i) {
+      hi[i] = (float)ops[i];
+      lo[i] = (float)(ops[i] - (double)hi[i]);
+    }
+    if ((e = upload(&h->op64, ops)) != cudaSuccess) return bail(e, "upload face operators");
+    if ((e = upload(&h->op_hi, hi)) != cudaSuccess) return bail(e, "upload face operators");
+    if ((e = upload(&h->op_lo, lo)) != cudaSuccess) return bail(e, "upload face operators");
+    if ((e = upload(&h->op_off, op_off)) != cudaSuccess) return bail(e, "upload face operators");
+  }
   *out = h;
   return DGSW_OK;
 }
@@ -360,7 +554,18 @@ int dgsw_destroy(DgswHandle h) {
   double* dbl[] = {h->state, h->t1, h->t2, h->u0s, h->jac, h->lower, h->width, h->lgl_x, h->params};
   for (double* p : dbl)
     if (p) cudaFree(p);
+  if (h->graph_adj) cudaGraphExecDestroy(h->graph_adj);
+  double* adjbufs[] = {h->samp_w, h->adj, h->adjz, h->targets, h->residuals};
+  for (double* p : adjbufs)
+    if (p) cudaFree(p);
+  if (h->samp_off) cudaFree(h->samp_off);
   if (h->dev_err) cudaFree(h->dev_err);
+  for (int n = 0; n <= kMaxN; ++n)
+    if (h->class_tasks[n]) cudaFree(h->class_tasks[n]);
+  if (h->op64) cudaFree(h->op64);
+  if (h->op_hi) cudaFree(h->op_hi);
+  if (h->op_lo) cudaFree(h->op_lo);
+  if (h->op_off) cudaFree(h->op_off);
   if (h->w1) cudaFree(h->w1);
   if (h->w2) cudaFree(h->w2);
   if (h->nbr) cudaFree(h->nbr);
@@ -463,11 +668,24 @@ int dgsw_rhs_device(DgswHandle h, const double* dev_u, double* dev_dudt) {
   if (dev_u == dev_dudt) return fail(h, DGSW_ERR_ARGUMENT, "input and output must differ");
   if (int rc = select_device(h)) return rc;
   if (mixed(h)) {
+    if (h->general) {
+      GeneralLaunch G = base_general(h);
+      G.prec = kPrecComp;
+      G.x64 = dev_u;
+      G.c = 1.0;
+      G.out64 = dev_dudt;
+      DGSW_CUDA(h, launch_general_classes(h, G));
+      return DGSW_OK;
+    }
     MixedLaunch M = base_mixed(h);
     M.x64 = dev_u;
     M.c = 1.0;
     M.out64 = dev_dudt;
     DGSW_CUDA(h, launch_mixed(h, M));
+    return DGSW_OK;
+  }
+  if (h->general) {
+    DGSW_CUDA(h, general_f64(h, dev_u, nullptr, dev_dudt, 0.0, 0.0, 1.0));
     return DGSW_OK;
   }
   StageLaunch L = base_launch(h);
@@ -484,6 +702,10 @@ int dgsw_volume_rhs_device(DgswHandle h, const double* dev_u, double* dev_dudt) 
   if (!h || !dev_u || !dev_dudt) return fail(h, DGSW_ERR_ARGUMENT, "null argument");
   if (dev_u == dev_dudt) return fail(h, DGSW_ERR_ARGUMENT, "input and output must differ");
   if (int rc = select_device(h)) return rc;
+  if (h->general) {
+    DGSW_CUDA(h, general_f64(h, dev_u, nullptr, dev_dudt, 0.0, 0.0, 1.0, 0));
+    return DGSW_OK;
+  }
   StageLaunch L = base_launch(h);
   L.mode = kModeVolume;
   L.ucur = dev_u;
@@ -538,6 +760,19 @@ int dgsw_substep(DgswHandle h, int k, double dt) {
     DGSW_CUDA(h, enqueue_mixed_stage(h, k, dt, h->u0s, h->state));
     return DGSW_OK;
   }
+  if (h->general) {
+    if (k == 0) {
+      DGSW_CUDA(h, cudaMemcpyAsync(h->u0s, h->state, bytes, cudaMemcpyDeviceToDevice, h->stream));
+      DGSW_CUDA(h, general_f64(h, h->u0s, nullptr, h->state, 1.0, 0.0, dt));
+    } else {
+      DGSW_CUDA(h, cudaMemcpyAsync(h->t1, h->state, bytes, cudaMemcpyDeviceToDevice, h->stream));
+      if (k == 1)
+        DGSW_CUDA(h, general_f64(h, h->t1, h->u0s, h->state, 0.25, 0.75, 0.25 * dt));
+      else
+        DGSW_CUDA(h, general_f64(h, h->t1, h->u0s, h->state, 2.0 / 3.0, 1.0 / 3.0, (2.0 / 3.0) * dt));
+    }
+    return DGSW_OK;
+  }
   StageLaunch L = base_launch(h);
   if (k == 0) {
     DGSW_CUDA(h, cudaMemcpyAsync(h->u0s, h->state, bytes, cudaMemcpyDeviceToDevice, h->stream));
@@ -582,6 +817,135 @@ int dgsw_step(DgswHandle h, int n_steps, double dt) {
   }
   for (; left > 0; --left) DGSW_CUDA(h, cudaGraphLaunch(h->graph_one, h->stream));
   return DGSW_OK;
+}
+
+int dgsw_adjoint_rhs_device(DgswHandle h, const double* dev_lambda, double* dev_out) {
+  if (!h || !dev_lambda || !dev_out) return fail(h, DGSW_ERR_ARGUMENT, "null argument");
+  if (dev_lambda == dev_out) return fail(h, DGSW_ERR_ARGUMENT, "input and output must differ");
+  if (h->general || h->cfg.gamma2 != 0.0)
+    return fail(h, DGSW_ERR_UNSUPPORTED, "the adjoint needs uniform extents and gamma2 = 0");
+  if (int rc = select_device(h)) return rc;
+  AdjointLaunch A = base_adjoint(h);
+  A.x = dev_lambda;
+  A.out = dev_out;
+  DGSW_CUDA(h, launch_adjoint_fp64(A, h->stream));
+  return DGSW_OK;
+}
+
+int dgsw_set_samples(DgswHandle h, int n_samples, const double* xyz) {
+  if (!h || n_samples < 1 || !xyz) return fail(h, DGSW_ERR_ARGUMENT, "need sample points");
+  if (h->general || h->dom.bricks.size() != 1 || h->cfg.gamma2 != 0.0)
+    return fail(h, DGSW_ERR_UNSUPPORTED,
+                "samples and the adjoint need one brick of uniform extent and gamma2 = 0");
+  if (int rc = select_device(h)) return rc;
+  const int n = h->dom.elem_n[0];
+  std::vector<int64_t> off(n_samples);
+  std::vector<double> w((size_t)n_samples * 3 * n);
+  if (!sample_weights(h->dom, n, n_samples, xyz, off.data(), w.data()))
+    return fail(h, DGSW_ERR_ARGUMENT, "a sample point lies outside the brick");
+  DGSW_CUDA(h, cudaStreamSynchronize(h->stream));
+  if (h->samp_off) cudaFree(h->samp_off);
+  if (h->samp_w) cudaFree(h->samp_w);
+  h->samp_off = nullptr;
+  h->samp_w = nullptr;
+  DGSW_CUDA(h, upload(&h->samp_off, off));
+  DGSW_CUDA(h, upload(&h->samp_w, w));
+  h->n_samples = n_samples;
+  if (!h->adj) {
+    const size_t bytes = h->dom.offset.back() * sizeof(double);
+    DGSW_CUDA(h, cudaMalloc(&h->adj, bytes));
+    DGSW_CUDA(h, cudaMalloc(&h->adjz, bytes));
+  }
+  return DGSW_OK;
+}
+
+int dgsw_sample_psi(DgswHandle h, double* host_out) {
+  if (!h || !host_out) return fail(h, DGSW_ERR_ARGUMENT, "null argument");
+  if (h->n_samples < 1) return fail(h, DGSW_ERR_ARGUMENT, "no sample points set");
+  if (int rc = select_device(h)) return rc;
+  if (h->record_cap < h->n_samples) {
+    DGSW_CUDA(h, cudaStreamSynchronize(h->stream));
+    if (h->residuals) cudaFree(h->residuals);
+    if (h->targets) cudaFree(h->targets);
+    h->residuals = h->targets = nullptr;
+    DGSW_CUDA(h, cudaMalloc(&h->residuals, h->n_samples * sizeof(double)));
+    DGSW_CUDA(h, cudaMalloc(&h->targets, h->n_samples * sizeof(double)));
+    h->record_cap = h->n_samples;
+  }
+  const int n = h->dom.elem_n[0];
+  DGSW_CUDA(h, launch_sample(h->state, h->n_samples, n, h->samp_off, h->samp_w, nullptr,
+                             h->residuals, h->stream));
+  DGSW_CUDA(h, cudaMemcpyAsync(host_out, h->residuals, h->n_samples * sizeof(double),
+                               cudaMemcpyDeviceToHost, h->stream));
+  DGSW_CUDA(h, cudaStreamSynchronize(h->stream));
+  return DGSW_OK;
+}
+
+int dgsw_misfit_forward(DgswHandle h, int n_windows, int steps_per_window, double dt,
+                        const double* host_targets, double* J) {
+  if (!h || !host_targets || !J) return fail(h, DGSW_ERR_ARGUMENT, "null argument");
+  if (n_windows < 1 || steps_per_window < 1 || !std::isfinite(dt))
+    return fail(h, DGSW_ERR_ARGUMENT, "bad window arguments");
+  if (h->n_samples < 1) return fail(h, DGSW_ERR_ARGUMENT, "no sample points set");
+  if (mixed(h)) return fail(h, DGSW_ERR_UNSUPPORTED, "the misfit adjoint is FP64 only");
+  if (int rc = select_device(h)) return rc;
+  const int64_t need = (int64_t)n_windows * h->n_samples;
+  if (h->record_cap < need) {
+    DGSW_CUDA(h, cudaStreamSynchronize(h->stream));
+    if (h->residuals) cudaFree(h->residuals);
+    if (h->targets) cudaFree(h->targets);
+    h->residuals = h->targets = nullptr;
+    DGSW_CUDA(h, cudaMalloc(&h->residuals, need * sizeof(double)));
+    DGSW_CUDA(h, cudaMalloc(&h->targets, need * sizeof(double)));
+    h->record_cap = need;
+  }
+  DGSW_CUDA(h, cudaMemcpyAsync(h->targets, host_targets, need * sizeof(double),
+                               cudaMemcpyHostToDevice, h->stream));
+  const int n = h->dom.elem_n[0];
+  for (int m = 0; m < n_windows; ++m) {
+    if (int rc = dgsw_step(h, steps_per_window, dt)) return rc;
+    DGSW_CUDA(h, launch_sample(h->state, h->n_samples, n, h->samp_off, h->samp_w,
+                               h->targets + (int64_t)m * h->n_samples,
+                               h->residuals + (int64_t)m * h->n_samples, h->stream));
+  }
+  std::vector<double> r(need);
+  DGSW_CUDA(h, cudaMemcpyAsync(r.data(), h->residuals, need * sizeof(double),
+                               cudaMemcpyDeviceToHost, h->stream));
+  DGSW_CUDA(h, cudaStreamSynchronize(h->stream));
+  double acc = 0.0;
+  for (double v : r) acc += v * v;
+  *J = acc;
+  h->rec_windows = n_windows;
+  h->rec_steps = steps_per_window;
+  h->rec_dt = dt;
+  return check_device_error(h);
+}
+
+int dgsw_misfit_adjoint(DgswHandle h, double* dev_grad) {
+  if (!h || !dev_grad) return fail(h, DGSW_ERR_ARGUMENT, "null argument");
+  if (h->rec_windows < 1) return fail(h, DGSW_ERR_ARGUMENT, "no recorded misfit run");
+  if (int rc = select_device(h)) return rc;
+  const size_t bytes = h->dom.offset.back() * sizeof(double);
+  const int K = h->rec_steps;
+  const double dt = h->rec_dt;
+  if (!(h->graph_adj_dt == dt) || h->graph_adj_steps != K) {
+    if (h->graph_adj) cudaGraphExecDestroy(h->graph_adj);
+    h->graph_adj = nullptr;
+    DGSW_CUDA(h, capture_adjoint_steps(h, dt, K, &h->graph_adj));
+    h->graph_adj_dt = dt;
+    h->graph_adj_steps = K;
+  }
+  const int n = h->dom.elem_n[0];
+  DGSW_CUDA(h, cudaMemsetAsync(h->adj, 0, bytes, h->stream));
+  for (int m = h->rec_windows - 1; m >= 0; --m) {
+    // dJ/d(sample) = 2 r, injected at the window's time, then K steps back
+    DGSW_CUDA(h, launch_sample_scatter(h->adj, h->n_samples, n, h->samp_off, h->samp_w,
+                                       h->residuals + (int64_t)m * h->n_samples, 2.0, h->stream));
+    DGSW_CUDA(h, cudaGraphLaunch(h->graph_adj, h->stream));
+  }
+  DGSW_CUDA(h, cudaMemcpyAsync(dev_grad, h->adj, bytes, cudaMemcpyDeviceToDevice, h->stream));
+  DGSW_CUDA(h, cudaStreamSynchronize(h->stream));
+  return check_device_error(h);
 }
 
 }  // extern "C"

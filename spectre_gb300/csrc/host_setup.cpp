@@ -158,10 +158,7 @@ bool lgl_mortar_projections(int ne, int nm, double* to_mortar, double* from_mort
   return true;
 }
 
-bool lgl_eo_table(int n, EoTable* t) {
-  if (n < kMinN || n > kMaxN || !t) return false;
-  double D[kMaxN * kMaxN];
-  lgl_diff_matrix(n, D);
+static bool eo_from_matrix(int n, const double* D, EoTable* t) {
   std::memset(t, 0, sizeof(*t));
   const int h = n / 2, H = (n + 1) / 2;
   for (int i = 0; i < H; ++i) {
@@ -175,6 +172,56 @@ bool lgl_eo_table(int n, EoTable* t) {
     // middle row: exactly antisymmetric, so its even part vanishes
     for (int j = 0; j < h; ++j) t->A[h][j] = 0.0;
     t->M[h] = 0.0;
+  }
+  return true;
+}
+
+bool lgl_eo_table(int n, EoTable* t) {
+  if (n < kMinN || n > kMaxN || !t) return false;
+  double D[kMaxN * kMaxN];
+  lgl_diff_matrix(n, D);
+  return eo_from_matrix(n, D, t);
+}
+
+bool lgl_eo_table_transposed(int n, EoTable* t) {
+  if (n < kMinN || n > kMaxN || !t) return false;
+  double D[kMaxN * kMaxN], Dt[kMaxN * kMaxN];
+  lgl_diff_matrix(n, D);
+  for (int i = 0; i < n; ++i)
+    for (int j = 0; j < n; ++j) Dt[i * n + j] = D[j * n + i];
+  return eo_from_matrix(n, Dt, t);
+}
+
+bool sample_weights(const Domain& dom, int n, int n_samples, const double* xyz,
+                    int64_t* elem_off, double* weights) {
+  if (dom.bricks.size() != 1 || !dom.uniform) return false;
+  const DgswBrick& b = dom.bricks[0];
+  const BrickLayout& L = dom.layout[0];
+  const int64_t per_block = (int64_t)1 << (L.level[0] + L.level[1] + L.level[2]);
+  for (int s = 0; s < n_samples; ++s) {
+    int q[3];
+    double xi[3];
+    for (int d = 0; d < 3; ++d) {
+      const double x = xyz[3 * s + d];
+      if (!(x >= b.lower[d] && x <= b.upper[d])) return false;
+      const double h = (b.upper[d] - b.lower[d]) / b.elements[d];
+      int k = (int)std::floor((x - b.lower[d]) / h);
+      if (k >= b.elements[d]) k = b.elements[d] - 1;
+      if (k < 0) k = 0;
+      q[d] = k;
+      xi[d] = 2.0 * (x - (b.lower[d] + h * k)) / h - 1.0;
+    }
+    int64_t blk[3], seg[3];
+    for (int d = 0; d < 3; ++d) {
+      blk[d] = q[d] >> L.level[d];
+      seg[d] = q[d] & ((1 << L.level[d]) - 1);
+    }
+    const int64_t bid = blk[0] + L.blocks[0] * (blk[1] + (int64_t)L.blocks[1] * blk[2]);
+    const int64_t e = bid * per_block + ((seg[0] << (L.level[1] + L.level[2])) |
+                                        (seg[1] << L.level[2]) | seg[2]);
+    elem_off[s] = dom.offset[e];
+    for (int d = 0; d < 3; ++d)
+      if (!lgl_interp_matrix(n, 1, &xi[d], weights + (size_t)s * 3 * n + d * n)) return false;
   }
   return true;
 }

@@ -26,8 +26,10 @@ bool lgl_interp_matrix(int n, int m, const double* targets, double* M);
 // Face -> mortar (nm x ne, interpolation) and mortar -> face (ne x nm,
 // Legendre modal truncation), Projection.cpp:56-375, ChildSize::Full.
 bool lgl_mortar_projections(int ne, int nm, double* to_mortar, double* from_mortar);
-// Even/odd split tables of the differentiation matrix (see EoTable).
+// Even/odd split tables of the differentiation matrix (see EoTable), and of
+// its transpose (also centro-antisymmetric), used by the adjoint.
 bool lgl_eo_table(int n, EoTable* t);
+bool lgl_eo_table_transposed(int n, EoTable* t);
 
 struct BrickLayout {
   int blocks[3];  // odd part of each per-axis element count
@@ -52,6 +54,12 @@ struct Domain {
   bool uniform = true;             // every element has the same extent
   int max_n = 0;
 };
+
+// Element and barycentric interpolation weights (3 x n per point) of points
+// inside a single-instance uniform-extent domain; false if a point lies
+// outside the brick.
+bool sample_weights(const Domain& dom, int n, int n_samples, const double* xyz,
+                    int64_t* elem_off, double* weights);
 
 // Validates a configuration and builds every host-side map.  On failure
 // returns false with a message in *err.

@@ -50,6 +50,60 @@ cudaError_t launch_stage_mixed(const MixedLaunch& L, cudaStream_t s);
 bool mixed_pipe_supported(int n);
 cudaError_t launch_stage_mixed_pipe(const MixedLaunch& L, cudaStream_t s);
 
+// One class of elements of extent n with neighbours of any extent
+// (stage_general.cu): W = alpha X + beta Y + c L(X).
+struct GeneralLaunch {
+  int n = 0;
+  int prec = kPrecF64;             // kPrecF64, kPrecComp, kPrecF32
+  const int32_t* tasks = nullptr;  // element indices of this class
+  int64_t n_tasks = 0;
+  const int64_t* offset = nullptr; // per element, in values
+  const int32_t* elem_n = nullptr;
+  const int32_t* nbr = nullptr;
+  const double* jac = nullptr;
+  // face operators T (n x nn, row-major) at op_off[n * (kMaxN + 1) + nn]
+  const double* op64 = nullptr;
+  const float* op_hi = nullptr;
+  const float* op_lo = nullptr;
+  const int32_t* op_off = nullptr;
+  EoTable eo{};
+  double gamma2 = 0.0;
+  int boundary = 1;                // 0: volume terms only
+  const double* x64 = nullptr;     // X (kPrecF64, kPrecComp)
+  const float* x32 = nullptr;      // X (kPrecF32)
+  const double* y64 = nullptr;     // Y (kPrecF64)
+  const float* y32 = nullptr;      // Y (kPrecComp, kPrecF32)
+  float* w32 = nullptr;            // FP32 output
+  double* out64 = nullptr;         // FP64 output (= W, or base64 + W)
+  const double* base64 = nullptr;
+  double alpha = 0.0, beta = 0.0, c = 1.0;
+};
+
+cudaError_t launch_stage_general(const GeneralLaunch& L, cudaStream_t s);
+
+// Transposed operator (adjoint_fp64.cu): out = alpha X + beta Y + c L^T X,
+// out2 = alpha2 X + beta2 Y (optional, pointwise).
+struct AdjointLaunch {
+  int n = 0;
+  int64_t n_elem = 0;
+  const double* x = nullptr;
+  const double* y = nullptr;
+  double* out = nullptr;
+  double* out2 = nullptr;
+  double alpha = 0.0, beta = 0.0, c = 1.0, alpha2 = 0.0, beta2 = 0.0;
+  const int32_t* nbr = nullptr;
+  const double* jac = nullptr;
+  EoTable eoT{};  // even/odd split of D^T
+};
+cudaError_t launch_adjoint_fp64(const AdjointLaunch& L, cudaStream_t s);
+// Psi at sample points: out[s] = sample - target[s] (target may be null).
+cudaError_t launch_sample(const double* u, int n_samples, int n, const int64_t* elem_off,
+                          const double* w, const double* target, double* out, cudaStream_t s);
+// lam_Psi += scale * r[s] * weights of sample s
+cudaError_t launch_sample_scatter(double* lam, int n_samples, int n, const int64_t* elem_off,
+                                  const double* w, const double* r, double scale,
+                                  cudaStream_t s);
+
 // UpwindPenalty pointwise kernels (face_kernels.cu).
 cudaError_t launch_package_data(int64_t npts, const double* psi, const double* pi,
                                 const double* phi, const double* gamma2,

@@ -30,6 +30,7 @@
 #include <cstdio>
 
 #include "common.cuh"
+#include "dg_device.cuh"
 #include "launch.hpp"
 
 namespace dgsw {
@@ -46,39 +47,10 @@ struct Shape {
   static constexpr int SLOT = 5 * NP + 3 * TAB;  // smem doubles per element
 };
 
-// (scaled D) applied to one line with the even/odd split.
 template <int N>
 __device__ __forceinline__ void eo_line(const double (&u)[N], double (&out)[N],
                                         const double* __restrict__ tab) {
-  using S = Shape<N>;
-  constexpr int h = S::h, H = S::H;
-  const double* A = tab;
-  const double* B = tab + H * h;
-  const double* M = tab + 2 * H * h;
-  double e[h], o[h];
-#pragma unroll
-  for (int j = 0; j < h; ++j) {
-    e[j] = u[j] + u[N - 1 - j];
-    o[j] = u[j] - u[N - 1 - j];
-  }
-#pragma unroll
-  for (int i = 0; i < h; ++i) {
-    double P = A[i * h] * e[0];
-#pragma unroll
-    for (int j = 1; j < h; ++j) P = fma(A[i * h + j], e[j], P);
-    if (S::odd) P = fma(M[i], u[h], P);
-    double Q = B[i * h] * o[0];
-#pragma unroll
-    for (int j = 1; j < h; ++j) Q = fma(B[i * h + j], o[j], Q);
-    out[i] = P + Q;
-    out[N - 1 - i] = Q - P;
-  }
-  if (S::odd) {
-    double Q = B[h * h] * o[0];
-#pragma unroll
-    for (int j = 1; j < h; ++j) Q = fma(B[h * h + j], o[j], Q);
-    out[h] = Q;
-  }
+  dev::eo_line<N, double>(u, out, tab);
 }
 
 template <int N, int EPB, int MINB, int MODE>

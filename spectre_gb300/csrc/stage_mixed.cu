@@ -26,6 +26,7 @@
 //   out64[p] = base64[p] + W      (FP64; out64 may alias base64)
 //   out64[p] = W                  (when base64 is null: the RHS itself)
 #include "common.cuh"
+#include "dg_device.cuh"
 #include "launch.hpp"
 
 namespace dgsw {
@@ -41,154 +42,17 @@ struct MShape {
   static constexpr int TAB = 2 * H * h + H;
 };
 
-// ---- exact FP64 -> (hi, lo) FP32 split with integer operations -----------
-// hi = u truncated to 24 significant bits, lo = the next 23 bits (u - hi to
-// 2^-47 relative).  |u| < 2^-126 flushes to (0, 0); the lo part flushes below
-// 2^-103.  Non-finite u gives (u as float, 0).
-__device__ __forceinline__ void split_df(double u, float& hi, float& lo) {
-  const unsigned long long b = (unsigned long long)__double_as_longlong(u);
-  const unsigned int top = (unsigned int)(b >> 32);
-  const unsigned int sign = top & 0x80000000u;
-  const int e = (int)((top >> 20) & 0x7ffu);
-  if (e >= 1023 + 128) {  // beyond float range or inf/nan
-    hi = __double2float_rn(u);
-    lo = 0.0f;
-    return;
-  }
-  if (e < 1023 - 126) {
-    hi = 0.0f;
-    lo = 0.0f;
-    return;
-  }
-  const unsigned int mhi = (unsigned int)((b >> 29) & 0x7fffffu);  // top 23 mantissa bits
-  hi = __int_as_float((int)(sign | ((unsigned int)(e - 1023 + 127) << 23) | mhi));
-  const unsigned int mlo = (unsigned int)(b & 0x1fffffffu);  // low 29 mantissa bits
-  if (e < 920 || mlo == 0u) {
-    lo = 0.0f;
-    return;
-  }
-  // (1 + m*2^-23) - 1 is exact; m = mlo >> 6 keeps the top 23 of the 29 bits
-  const float f = __int_as_float((int)(0x3f800000u | (mlo >> 6))) - 1.0f;
-  const float scale = __int_as_float((e - 919) << 23);  // 2^(e - 1046)
-  lo = __int_as_float(__float_as_int(f * scale) | (int)sign);
-}
-
-// exact FP32 -> FP64 widening with integer operations (normal floats; zero
-// and subnormals widen to signed zero)
-__device__ __forceinline__ double widen(float f) {
-  const unsigned int b = (unsigned int)__float_as_int(f);
-  const unsigned int e = (b >> 23) & 0xffu;
-  if (e == 0u) return __longlong_as_double((long long)((unsigned long long)(b & 0x80000000u) << 32));
-  if (e == 0xffu) return (double)f;
-  const unsigned int hiw = (b & 0x80000000u) | ((e + 896u) << 20) | ((b & 0x7fffffu) >> 3);
-  const unsigned int low = (b & 0x7u) << 29;
-  return __hiloint2double((int)hiw, (int)low);
-}
-
-// ---- double-float primitives ----------------------------------------------
-__device__ __forceinline__ void two_sum(float a, float b, float& s, float& t) {
-  s = a + b;
-  const float bb = s - a;
-  t = (a - (s - bb)) + (b - bb);
-}
-
-// compensated accumulation of one product (ah+al)*(xh+xl) into (s, c)
-__device__ __forceinline__ void dot2_term(float ah, float al, float xh, float xl, float& s,
-                                          float& c) {
-  const float p = ah * xh;
-  const float pe = fmaf(ah, xh, -p);
-  float t;
-  two_sum(s, p, s, t);
-  c += t + pe;
-  c = fmaf(al, xh, c);
-  c = fmaf(ah, xl, c);
-}
-
-__device__ __forceinline__ void dot2_first(float ah, float al, float xh, float xl, float& s,
-                                           float& c) {
-  s = ah * xh;
-  c = fmaf(ah, xh, -s);
-  c = fmaf(al, xh, c);
-  c = fmaf(ah, xl, c);
-}
-
-// compensated (scaled D) x (one line), double-float input, FP32 output
-template <int N>
-__device__ __forceinline__ void eo_line_df(const float (&xh)[N], const float (&xl)[N],
-                                           float (&out)[N], const float* __restrict__ th,
-                                           const float* __restrict__ tl) {
-  using S = MShape<N>;
-  constexpr int h = S::h, H = S::H;
-  float eh[h], el[h], oh[h], ol[h];
-#pragma unroll
-  for (int j = 0; j < h; ++j) {
-    float t;
-    two_sum(xh[j], xh[N - 1 - j], eh[j], t);
-    el[j] = t + (xl[j] + xl[N - 1 - j]);
-    two_sum(xh[j], -xh[N - 1 - j], oh[j], t);
-    ol[j] = t + (xl[j] - xl[N - 1 - j]);
-  }
-  const float* Ah = th;
-  const float* Al = tl;
-  const float* Bh = th + H * h;
-  const float* Bl = tl + H * h;
-  const float* Mh = th + 2 * H * h;
-  const float* Ml = tl + 2 * H * h;
-#pragma unroll
-  for (int i = 0; i < h; ++i) {
-    float ps, pc, qs, qc;
-    dot2_first(Ah[i * h], Al[i * h], eh[0], el[0], ps, pc);
-#pragma unroll
-    for (int j = 1; j < h; ++j) dot2_term(Ah[i * h + j], Al[i * h + j], eh[j], el[j], ps, pc);
-    if (S::odd) dot2_term(Mh[i], Ml[i], xh[h], xl[h], ps, pc);
-    dot2_first(Bh[i * h], Bl[i * h], oh[0], ol[0], qs, qc);
-#pragma unroll
-    for (int j = 1; j < h; ++j) dot2_term(Bh[i * h + j], Bl[i * h + j], oh[j], ol[j], qs, qc);
-    out[i] = (ps + qs) + (pc + qc);
-    out[N - 1 - i] = (qs - ps) + (qc - pc);
-  }
-  if (S::odd) {
-    float qs, qc;
-    dot2_first(Bh[h * h], Bl[h * h], oh[0], ol[0], qs, qc);
-#pragma unroll
-    for (int j = 1; j < h; ++j) dot2_term(Bh[h * h + j], Bl[h * h + j], oh[j], ol[j], qs, qc);
-    out[h] = qs + qc;
-  }
-}
+using dev::eo_line;
+using dev::eo_line_df;
+using dev::split_df;
+using dev::two_sum;
+using dev::widen;
 
 // plain FP32 (scaled D) x line with the even/odd split
 template <int N>
 __device__ __forceinline__ void eo_line_f(const float (&x)[N], float (&out)[N],
                                           const float* __restrict__ th) {
-  using S = MShape<N>;
-  constexpr int h = S::h, H = S::H;
-  float e[h], o[h];
-#pragma unroll
-  for (int j = 0; j < h; ++j) {
-    e[j] = x[j] + x[N - 1 - j];
-    o[j] = x[j] - x[N - 1 - j];
-  }
-  const float* A = th;
-  const float* B = th + H * h;
-  const float* M = th + 2 * H * h;
-#pragma unroll
-  for (int i = 0; i < h; ++i) {
-    float P = A[i * h] * e[0];
-#pragma unroll
-    for (int j = 1; j < h; ++j) P = fmaf(A[i * h + j], e[j], P);
-    if (S::odd) P = fmaf(M[i], x[h], P);
-    float Q = B[i * h] * o[0];
-#pragma unroll
-    for (int j = 1; j < h; ++j) Q = fmaf(B[i * h + j], o[j], Q);
-    out[i] = P + Q;
-    out[N - 1 - i] = Q - P;
-  }
-  if (S::odd) {
-    float Q = B[h * h] * o[0];
-#pragma unroll
-    for (int j = 1; j < h; ++j) Q = fmaf(B[h * h + j], o[j], Q);
-    out[h] = Q;
-  }
+  eo_line<N, float>(x, out, th);
 }
 
 template <int N, int EPB, bool COMP>

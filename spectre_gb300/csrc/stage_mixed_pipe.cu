@@ -19,6 +19,7 @@
 #include <type_traits>
 
 #include "common.cuh"
+#include "dg_device.cuh"
 #include "launch.hpp"
 
 namespace dgsw {
@@ -109,49 +110,9 @@ __device__ __forceinline__ void two_sum2(float2 a, float2 b, float2& s, float2& 
   t = add2(sub2(a, sub2(s, bb)), sub2(b, bb));
 }
 
-__device__ __forceinline__ void two_sum(float a, float b, float& s, float& t) {
-  s = a + b;
-  const float bb = s - a;
-  t = (a - (s - bb)) + (b - bb);
-}
-
-// exact FP64 -> (hi, lo) FP32 split with integer operations (as stage_mixed.cu)
-__device__ __forceinline__ void split_df(double u, float& hi, float& lo) {
-  const unsigned long long b = (unsigned long long)__double_as_longlong(u);
-  const unsigned int top = (unsigned int)(b >> 32);
-  const unsigned int sign = top & 0x80000000u;
-  const int e = (int)((top >> 20) & 0x7ffu);
-  if (e >= 1023 + 128) {
-    hi = __double2float_rn(u);
-    lo = 0.0f;
-    return;
-  }
-  if (e < 1023 - 126) {
-    hi = 0.0f;
-    lo = 0.0f;
-    return;
-  }
-  const unsigned int mhi = (unsigned int)((b >> 29) & 0x7fffffu);
-  hi = __int_as_float((int)(sign | ((unsigned int)(e - 1023 + 127) << 23) | mhi));
-  const unsigned int mlo = (unsigned int)(b & 0x1fffffffu);
-  if (e < 920 || mlo == 0u) {
-    lo = 0.0f;
-    return;
-  }
-  const float f = __int_as_float((int)(0x3f800000u | (mlo >> 6))) - 1.0f;
-  const float scale = __int_as_float((e - 919) << 23);
-  lo = __int_as_float(__float_as_int(f * scale) | (int)sign);
-}
-
-__device__ __forceinline__ double widen(float f) {
-  const unsigned int b = (unsigned int)__float_as_int(f);
-  const unsigned int e = (b >> 23) & 0xffu;
-  if (e == 0u)
-    return __longlong_as_double((long long)((unsigned long long)(b & 0x80000000u) << 32));
-  if (e == 0xffu) return (double)f;
-  const unsigned int hiw = (b & 0x80000000u) | ((e + 896u) << 20) | ((b & 0x7fffffu) >> 3);
-  return __hiloint2double((int)hiw, (int)((b & 0x7u) << 29));
-}
+using dev::split_df;
+using dev::two_sum;
+using dev::widen;
 
 // ---------------------------------------------------------------- geometry
 template <int N>

@@ -92,6 +92,11 @@ _SIGNATURES = {
     "dgsw_index_maps": (_I, [ctypes.POINTER(DgswConfig), _P, _P, _P]),
     "dgsw_count_elements": (_I, [ctypes.POINTER(DgswConfig), ctypes.POINTER(_I64),
                                  ctypes.POINTER(_I64)]),
+    "dgsw_adjoint_rhs_device": (_I, [_P, _P, _P]),
+    "dgsw_set_samples": (_I, [_P, _I, _P]),
+    "dgsw_sample_psi": (_I, [_P, _P]),
+    "dgsw_misfit_forward": (_I, [_P, _I, _I, _D, _P, ctypes.POINTER(_D)]),
+    "dgsw_misfit_adjoint": (_I, [_P, _P]),
     "dgsw_step_noalloc": (_I, [ctypes.POINTER(DgswBrick), _I, _D, _P, _I, _D, _P]),
     "dgsw_noalloc_scratch_bytes": (ctypes.c_size_t, []),
     "dgsw_noalloc_last_error": (ctypes.c_char_p, []),
@@ -409,3 +414,39 @@ class DgEvolution:
     def substep(self, k: int, dt: float):
         _check(lib().dgsw_substep(self._h, int(k), float(dt)), self._h)
         self.synchronize()
+
+    # discrete adjoint -----------------------------------------------------
+    def adjoint_rhs(self, lam_dev):
+        """L^T lambda (device tensors)."""
+        import torch
+        out = torch.empty_like(lam_dev)
+        _torch_ready(lam_dev, out)
+        _check(lib().dgsw_adjoint_rhs_device(self._h, _ptr(lam_dev), _ptr(out)), self._h)
+        self.synchronize()
+        return out
+
+    def set_samples(self, xyz):
+        a = np.ascontiguousarray(xyz, dtype=np.float64).reshape(-1, 3)
+        self.n_samples = a.shape[0]
+        _check(lib().dgsw_set_samples(self._h, a.shape[0], _ptr(a)), self._h)
+
+    def sample_psi(self):
+        out = np.empty(self.n_samples)
+        _check(lib().dgsw_sample_psi(self._h, _ptr(out)), self._h)
+        return out
+
+    def misfit_forward(self, targets, steps_per_window: int, dt: float) -> float:
+        t = np.ascontiguousarray(targets, dtype=np.float64)
+        n_windows = t.shape[0]
+        J = ctypes.c_double()
+        _check(lib().dgsw_misfit_forward(self._h, n_windows, int(steps_per_window), float(dt),
+                                         _ptr(t), ctypes.byref(J)), self._h)
+        return J.value
+
+    def misfit_adjoint(self):
+        """dJ/du(t=0) of the last misfit_forward, as a device tensor."""
+        import torch
+        g = torch.empty(self.state_size, dtype=torch.float64, device="cuda:%d" % self.device)
+        _torch_ready(g)
+        _check(lib().dgsw_misfit_adjoint(self._h, _ptr(g)), self._h)
+        return g

@@ -847,3 +847,652 @@ int orc_evolve(int n_inst, const OrcBrick* br, const int32_t* elem_n, double gam
 }
 
 }  // extern "C"
+
+// ===================== CurvedScalarWave (configuration 5) =====================
+extern "C" {
+
+int orc_ks_background(int npts, double M, const double* xyz, double* bg) {
+  // Schwarzschild in Kerr-Schild coordinates (spin 0, centre 0): the closed
+  // forms of Test_KerrSchild.cpp:55-232.
+  if (npts < 0 || !xyz || !bg) return -1;
+  const int n = npts;
+  for (int p = 0; p < n; ++p) {
+    const double x[3] = {xyz[p], xyz[n + p], xyz[2 * n + p]};
+    const double r2 = x[0] * x[0] + x[1] * x[1] + x[2] * x[2];
+    const double r = std::sqrt(r2);
+    const double lapse = 1.0 / std::sqrt(1.0 + 2.0 * M / r);
+    const double l2 = lapse * lapse;
+    bg[p] = lapse;
+    for (int i = 0; i < 3; ++i) bg[(1 + i) * n + p] = 2.0 * M * x[i] / r2 * l2;
+    for (int i = 0; i < 3; ++i) bg[(4 + i) * n + p] = M * x[i] / (r2 * r) * l2 * lapse;
+    for (int i = 0; i < 3; ++i)
+      for (int j = 0; j < 3; ++j) {
+        // d_i shift^j
+        double v = (i == j) ? 2.0 * M / r2 * l2 : 0.0;
+        v -= 4.0 * M * x[i] * x[j] / (r2 * r2) * l2 * (1.0 - M / r * l2);
+        bg[(7 + 3 * i + j) * n + p] = v;
+      }
+    const int pairs[6][2] = {{0, 0}, {0, 1}, {0, 2}, {1, 1}, {1, 2}, {2, 2}};
+    for (int q = 0; q < 6; ++q) {
+      const int i = pairs[q][0], j = pairs[q][1];
+      bg[(16 + q) * n + p] = (i == j ? 1.0 : 0.0) - 2.0 * M * x[i] * x[j] / (r2 * (r + 2.0 * M));
+    }
+    const double f = M * (8.0 * M + 3.0 * r) / ((2.0 * M + r) * (2.0 * M + r) * r2);
+    for (int i = 0; i < 3; ++i) bg[(22 + i) * n + p] = f * x[i];
+    bg[25 * n + p] = 2.0 * M * (3.0 * M + r) * std::pow((2.0 * M + r) * r, -1.5);
+  }
+  return 0;
+}
+
+static inline double inv_metric(const double* bg, int n, int p, int i, int j) {
+  static const int idx[3][3] = {{0, 1, 2}, {1, 3, 4}, {2, 4, 5}};
+  return bg[(16 + idx[i][j]) * n + p];
+}
+
+int orc_csw_time_derivative(int npts, const double* d_psi, const double* d_pi,
+                            const double* d_phi, const double* pi, const double* phi,
+                            const double* bg, double gamma1, double gamma2, double* dt) {
+  // CurvedScalarWave::TimeDerivative<3>::apply, TimeDerivative.cpp:47-68
+  if (npts < 0 || !d_psi || !d_pi || !d_phi || !pi || !phi || !bg || !dt) return -1;
+  const int n = npts;
+  for (int p = 0; p < n; ++p) {
+    const double lapse = bg[p];
+    const double* shift = bg + n;  // shift^i at (1+i)*n + p
+    auto sh = [&](int i) { return shift[i * n + p]; };
+    auto dl = [&](int i) { return bg[(4 + i) * n + p]; };
+    auto ds = [&](int i, int j) { return bg[(7 + 3 * i + j) * n + p]; };
+    auto gam = [&](int i) { return bg[(22 + i) * n + p]; };
+    const double K = bg[25 * n + p];
+    auto dps = [&](int i) { return d_psi[i * n + p]; };
+    auto dpi = [&](int i) { return d_pi[i * n + p]; };
+    auto dph = [&](int i, int j) { return d_phi[(3 * i + j) * n + p]; };
+    auto ph = [&](int i) { return phi[i * n + p]; };
+    double s = -lapse * pi[p];
+    for (int i = 0; i < 3; ++i) s += sh(i) * dps(i);
+    for (int j = 0; j < 3; ++j) s += gamma1 * sh(j) * (dps(j) - ph(j));
+    dt[p] = s;
+    s = lapse * pi[p] * K;
+    for (int i = 0; i < 3; ++i) s += sh(i) * dpi(i);
+    for (int i = 0; i < 3; ++i) s += lapse * gam(i) * ph(i);
+    for (int i = 0; i < 3; ++i) s += gamma1 * gamma2 * sh(i) * (dps(i) - ph(i));
+    for (int i = 0; i < 3; ++i)
+      for (int j = 0; j < 3; ++j) s -= lapse * inv_metric(bg, n, p, i, j) * dph(i, j);
+    for (int i = 0; i < 3; ++i)
+      for (int j = 0; j < 3; ++j) s -= inv_metric(bg, n, p, i, j) * ph(i) * dl(j);
+    dt[n + p] = s;
+    for (int i = 0; i < 3; ++i) {
+      double v = -lapse * dpi(i);
+      for (int j = 0; j < 3; ++j) v += sh(j) * dph(j, i);
+      v += gamma2 * lapse * (dps(i) - ph(i));
+      v -= pi[p] * dl(i);
+      for (int j = 0; j < 3; ++j) v += ph(j) * ds(i, j);
+      dt[(2 + i) * n + p] = v;
+    }
+  }
+  return 0;
+}
+
+int orc_csw_package(int npts, const double* psi, const double* pi, const double* phi,
+                    const double* lapse, const double* shift, const double* gamma1,
+                    const double* gamma2, const double* nrm, const double* nvec,
+                    const double* ndotv, double* pkg, double* max_speed) {
+  // CurvedScalarWave UpwindPenalty::dg_package_data, UpwindPenalty.cpp:35-75,
+  // with characteristic_fields / characteristic_speeds, Characteristics.cpp
+  if (npts < 0 || !psi || !pi || !phi || !lapse || !shift || !gamma1 || !gamma2 || !nrm ||
+      !nvec || !pkg)
+    return -1;
+  const int n = npts;
+  double mx = -std::numeric_limits<double>::infinity();
+  for (int p = 0; p < n; ++p) {
+    double ndp = 0.0;  // n^i Phi_i
+    for (int i = 0; i < 3; ++i) ndp += nvec[i * n + p] * phi[i * n + p];
+    pkg[p] = psi[p];
+    for (int i = 0; i < 3; ++i) pkg[(1 + i) * n + p] = phi[i * n + p] - nrm[i * n + p] * ndp;
+    pkg[4 * n + p] = pi[p] + ndp - gamma2[p] * psi[p];
+    pkg[5 * n + p] = pi[p] - ndp - gamma2[p] * psi[p];
+    pkg[6 * n + p] = gamma2[p];
+    for (int i = 0; i < 3; ++i) pkg[(7 + i) * n + p] = nrm[i * n + p];
+    double bn = 0.0;  // shift^i n_i
+    for (int i = 0; i < 3; ++i) bn += shift[i * n + p] * nrm[i * n + p];
+    double c0 = -(1.0 + gamma1[p]) * bn, c1 = -bn, c2 = -bn + lapse[p], c3 = -bn - lapse[p];
+    if (ndotv) {
+      c0 -= ndotv[p];
+      c1 -= ndotv[p];
+      c2 -= ndotv[p];
+      c3 -= ndotv[p];
+    }
+    pkg[10 * n + p] = c0;
+    pkg[11 * n + p] = c1;
+    pkg[12 * n + p] = c2;
+    pkg[13 * n + p] = c3;
+    mx = std::max(mx, std::max(c0, std::max(c1, c2)));
+  }
+  if (max_speed) *max_speed = mx;
+  return 0;
+}
+
+int orc_csw_boundary_terms(int npts, const double* pi_, const double* pe, double* out) {
+  // CurvedScalarWave UpwindPenalty::dg_boundary_terms, UpwindPenalty.cpp:77-127
+  if (npts < 0 || !pi_ || !pe || !out) return -1;
+  const int n = npts;
+  auto step = [](double x) { return x >= 0.0 ? 1.0 : 0.0; };
+  for (int p = 0; p < n; ++p) {
+    const double* si = pi_ + 10 * n;
+    const double* se = pe + 10 * n;
+    const double psi_bc = -step(se[p]) * se[p] * pe[p] - step(-si[p]) * si[p] * pi_[p];
+    const double t1 = -step(se[2 * n + p]) * se[2 * n + p] * pe[4 * n + p] -
+                      step(-si[3 * n + p]) * si[3 * n + p] * pi_[5 * n + p];
+    const double t2 = step(-si[2 * n + p]) * si[2 * n + p] * pi_[4 * n + p] +
+                      step(se[3 * n + p]) * se[3 * n + p] * pe[5 * n + p];
+    out[p] = psi_bc;
+    out[n + p] = 0.5 * (t1 - t2) + pi_[6 * n + p] * psi_bc;
+    const double t1b = -0.5 * (t1 + t2);
+    for (int i = 0; i < 3; ++i)
+      out[(2 + i) * n + p] = t1b * pi_[(7 + i) * n + p] -
+                             step(se[n + p]) * se[n + p] * pe[(1 + i) * n + p] -
+                             step(-si[n + p]) * si[n + p] * pi_[(1 + i) * n + p];
+  }
+  return 0;
+}
+
+int orc_csw_cpsr(int npts, const double* psi, const double* pi, const double* phi,
+                 const double* lapse, const double* shift, const double* gamma1,
+                 const double* gamma2, const double* nrm, const double* nvec,
+                 const double* xyz, const double* d_psi, const double* d_pi,
+                 const double* d_phi, const double* dt_psi, const double* dt_pi,
+                 const double* dt_phi, double* out) {
+  // ConstraintPreservingSphericalRadiation::dg_time_derivative,
+  // ConstraintPreservingSphericalRadiation.cpp:40-156 (static mesh)
+  if (npts < 0 || !psi || !pi || !phi || !lapse || !shift || !gamma1 || !gamma2 || !nrm ||
+      !nvec || !xyz || !d_psi || !d_pi || !d_phi || !dt_psi || !dt_pi || !dt_phi || !out)
+    return -1;
+  (void)d_pi;
+  const int n = npts;
+  for (int p = 0; p < n; ++p) {
+    const double r = std::sqrt(xyz[p] * xyz[p] + xyz[n + p] * xyz[n + p] +
+                               xyz[2 * n + p] * xyz[2 * n + p]);
+    const double inv_r = 1.0 / r;
+    double bn = 0.0;
+    for (int i = 0; i < 3; ++i) bn += shift[i * n + p] * nrm[i * n + p];
+    const double c0 = -(1.0 + gamma1[p]) * bn, c1 = -bn;
+    double dpsi_c = nvec[p] * (d_psi[p] - phi[p]);
+    for (int i = 1; i < 3; ++i) dpsi_c += nvec[i * n + p] * (d_psi[i * n + p] - phi[i * n + p]);
+    dpsi_c *= std::min(0.0, c0);
+    out[p] = dpsi_c;
+    for (int i = 0; i < 3; ++i) {
+      double v = nvec[p] * (d_phi[(3 * 0 + i) * n + p] - d_phi[(3 * i + 0) * n + p]);
+      for (int j = 1; j < 3; ++j)
+        v += nvec[j * n + p] * (d_phi[(3 * j + i) * n + p] - d_phi[(3 * i + j) * n + p]);
+      out[(2 + i) * n + p] = v * std::min(0.0, c1);
+    }
+    double dpi_c = (2.0 * inv_r * psi[p] + 4.0 * dt_psi[p]) * inv_r;
+    for (int i = 0; i < 3; ++i) {
+      dpi_c += nvec[i * n + p] * (2.0 * dt_phi[i * n + p] + 4.0 * inv_r * phi[i * n + p]) +
+               shift[i * n + p] * dt_phi[i * n + p];
+      for (int j = 0; j < 3; ++j)
+        dpi_c += nvec[i * n + p] * nvec[j * n + p] * d_phi[(3 * i + j) * n + p];
+    }
+    dpi_c /= lapse[p];
+    dpi_c += gamma2[p] * dpsi_c - dt_pi[p];
+    out[n + p] = dpi_c;
+  }
+  return 0;
+}
+
+}  // extern "C"
+
+// ======================= spherical shell (configuration 5) =======================
+namespace {
+
+// global[i] = sign[b][i] * wedge_frame[perm[b][i]]: discrete_rotation of the
+// six orientations of DomainHelpers.cpp:553-578 (+z, -z, +y, -y, +x, -x)
+const int kShellPerm[6][3] = {{0, 1, 2}, {0, 1, 2}, {0, 2, 1}, {0, 2, 1}, {2, 0, 1}, {2, 0, 1}};
+const double kShellSign[6][3] = {{1, 1, 1}, {1, -1, -1}, {1, 1, -1},
+                                 {1, -1, 1}, {1, 1, 1},  {-1, -1, 1}};
+
+struct ShellLayout {
+  int per_axis[3];  // elements per block along xi, eta, zeta
+  int L[3];
+  int64_t per_block;
+};
+
+ShellLayout shell_layout(const OrcShell& s) {
+  ShellLayout l;
+  l.L[0] = l.L[1] = s.ref_ang;
+  l.L[2] = s.ref_rad;
+  for (int d = 0; d < 3; ++d) l.per_axis[d] = 1 << l.L[d];
+  l.per_block = (int64_t)l.per_axis[0] * l.per_axis[1] * l.per_axis[2];
+  return l;
+}
+
+// block and segments of element e (x-outer, z-inner inside a block)
+void shell_element(const ShellLayout& l, int64_t e, int* block, int seg[3]) {
+  *block = (int)(e / l.per_block);
+  int64_t w = e % l.per_block;
+  seg[2] = (int)(w % l.per_axis[2]);
+  w /= l.per_axis[2];
+  seg[1] = (int)(w % l.per_axis[1]);
+  seg[0] = (int)(w / l.per_axis[1]);
+}
+
+// Wedge<3> (Wedge.cpp:476-536) composed with the element map: coordinates
+// and the Jacobian dx^i/dxi_e^a (jac[3*i + a]) at element logical xi_e.
+void shell_map(const OrcShell& s, const ShellLayout& l, int block, const int seg[3],
+               const double xe[3], double x[3], double jac[9]) {
+  double xb[3], scale[3];
+  for (int d = 0; d < 3; ++d) {
+    scale[d] = 1.0 / l.per_axis[d];
+    xb[d] = -1.0 + (2.0 * seg[d] + 1.0 + xe[d]) * scale[d];
+  }
+  const double a = std::tan(M_PI_4 * xb[0]), b = std::tan(M_PI_4 * xb[1]);
+  const double rho2 = 1.0 + a * a + b * b, rho = std::sqrt(rho2), rho3 = rho2 * rho;
+  const double z0 = 0.5 * std::log(s.r_outer * s.r_inner);
+  const double k = 0.5 * std::log(s.r_outer / s.r_inner);
+  const double r = std::exp(z0 + k * xb[2]);
+  const double wf[3] = {r * a / rho, r * b / rho, r / rho};
+  const double da = M_PI_4 * (1.0 + a * a), db = M_PI_4 * (1.0 + b * b);
+  const double dxi[3] = {r * da * (1.0 + b * b) / rho3, -r * da * a * b / rho3, -r * da * a / rho3};
+  const double deta[3] = {-r * db * a * b / rho3, r * db * (1.0 + a * a) / rho3, -r * db * b / rho3};
+  const double dzeta[3] = {k * wf[0], k * wf[1], k * wf[2]};
+  for (int i = 0; i < 3; ++i) {
+    const int p = kShellPerm[block][i];
+    const double sg = kShellSign[block][i];
+    x[i] = sg * wf[p];
+    jac[3 * i + 0] = sg * dxi[p] * scale[0];
+    jac[3 * i + 1] = sg * deta[p] * scale[1];
+    jac[3 * i + 2] = sg * dzeta[p] * scale[2];
+  }
+}
+
+void invert3(const double m[9], double out[9]) {
+  const double c00 = m[4] * m[8] - m[5] * m[7], c01 = m[5] * m[6] - m[3] * m[8],
+               c02 = m[3] * m[7] - m[4] * m[6];
+  const double det = m[0] * c00 + m[1] * c01 + m[2] * c02;
+  const double id = 1.0 / det;
+  out[0] = c00 * id;
+  out[1] = (m[2] * m[7] - m[1] * m[8]) * id;
+  out[2] = (m[1] * m[5] - m[2] * m[4]) * id;
+  out[3] = c01 * id;
+  out[4] = (m[0] * m[8] - m[2] * m[6]) * id;
+  out[5] = (m[2] * m[3] - m[0] * m[5]) * id;
+  out[6] = c02 * id;
+  out[7] = (m[1] * m[6] - m[0] * m[7]) * id;
+  out[8] = (m[0] * m[4] - m[1] * m[3]) * id;
+}
+
+// face-point coordinates of element e, direction dir (points a + n*b)
+void shell_face_points(const OrcShell& s, const ShellLayout& l, int64_t e, int dir,
+                       std::vector<double>* pts) {
+  const int n = s.n;
+  const Spectral1d& sp = spectral(n);
+  int block, seg[3];
+  shell_element(l, e, &block, seg);
+  const int d = dir / 2;
+  const double side = (dir % 2) ? 1.0 : -1.0;
+  pts->resize(3 * n * n);
+  for (int bb = 0; bb < n; ++bb)
+    for (int aa = 0; aa < n; ++aa) {
+      double xe[3];
+      int fi[2] = {aa, bb}, c = 0;
+      for (int q = 0; q < 3; ++q) xe[q] = (q == d) ? side : sp.x[fi[c++]];
+      double x[3], jac[9];
+      shell_map(s, l, block, seg, xe, x, jac);
+      for (int q = 0; q < 3; ++q) (*pts)[3 * (aa + n * bb) + q] = x[q];
+    }
+}
+
+struct ShellMesh {
+  OrcShell s;
+  ShellLayout l;
+  int64_t E;
+  std::vector<double> xyz, ij;     // per element 3*NP, 9*NP
+  std::vector<int32_t> nbr, perm;  // 6 per element, 6*N^2 per element
+};
+
+void build_shell(const OrcShell& s, ShellMesh* m) {
+  m->s = s;
+  m->l = shell_layout(s);
+  m->E = 6 * m->l.per_block;
+  const int n = s.n;
+  const int64_t np = (int64_t)n * n * n;
+  const Spectral1d& sp = spectral(n);
+  m->xyz.assign(3 * np * m->E, 0.0);
+  m->ij.assign(9 * np * m->E, 0.0);
+  for (int64_t e = 0; e < m->E; ++e) {
+    int block, seg[3];
+    shell_element(m->l, e, &block, seg);
+    for (int k = 0; k < n; ++k)
+      for (int j = 0; j < n; ++j)
+        for (int i = 0; i < n; ++i) {
+          const int64_t p = i + n * (j + (int64_t)n * k);
+          const double xe[3] = {sp.x[i], sp.x[j], sp.x[k]};
+          double x[3], jac[9], inv[9];
+          shell_map(s, m->l, block, seg, xe, x, jac);
+          invert3(jac, inv);  // inv[3*a + i] = d xi^a / d x^i
+          for (int q = 0; q < 3; ++q) m->xyz[e * 3 * np + q * np + p] = x[q];
+          for (int q = 0; q < 9; ++q) m->ij[e * 9 * np + q * np + p] = inv[q];
+        }
+  }
+  // connectivity: inside a block by segments; across blocks by face centres
+  m->nbr.assign(6 * m->E, 0);
+  m->perm.assign(6 * (size_t)n * n * m->E, 0);
+  std::vector<double> centre(18 * m->E);
+  for (int64_t e = 0; e < m->E; ++e) {
+    int block, seg[3];
+    shell_element(m->l, e, &block, seg);
+    for (int dir = 0; dir < 6; ++dir) {
+      const int d = dir / 2;
+      double xe[3] = {0, 0, 0};
+      xe[d] = (dir % 2) ? 1.0 : -1.0;
+      double x[3], jac[9];
+      shell_map(s, m->l, block, seg, xe, x, jac);
+      for (int q = 0; q < 3; ++q) centre[18 * e + 3 * dir + q] = x[q];
+    }
+  }
+  const double tol = 1e-9 * s.r_outer;
+  for (int64_t e = 0; e < m->E; ++e) {
+    int block, seg[3];
+    shell_element(m->l, e, &block, seg);
+    for (int dir = 0; dir < 6; ++dir) {
+      const int d = dir / 2;
+      const bool upper = dir % 2;
+      int64_t nb = -1;
+      int ndir = -1;
+      if (d == 2 && !upper && seg[2] == 0) {
+        m->nbr[6 * e + dir] = -1;
+        continue;
+      }
+      if (d == 2 && upper && seg[2] == m->l.per_axis[2] - 1) {
+        m->nbr[6 * e + dir] = -2;
+        continue;
+      }
+      const double* c = &centre[18 * e + 3 * dir];
+      for (int64_t f = 0; f < m->E && nb < 0; ++f) {
+        if (f == e) continue;
+        for (int fd = 0; fd < 6; ++fd) {
+          const double* cf = &centre[18 * f + 3 * fd];
+          if (std::abs(cf[0] - c[0]) < tol && std::abs(cf[1] - c[1]) < tol &&
+              std::abs(cf[2] - c[2]) < tol) {
+            nb = f;
+            ndir = fd;
+            break;
+          }
+        }
+      }
+      m->nbr[6 * e + dir] = (int32_t)nb;
+      std::vector<double> mine, theirs;
+      shell_face_points(s, m->l, e, dir, &mine);
+      shell_face_points(s, m->l, nb, ndir, &theirs);
+      for (int q = 0; q < n * n; ++q) {
+        int hit = -1;
+        for (int r = 0; r < n * n; ++r) {
+          if (std::abs(mine[3 * q] - theirs[3 * r]) < tol &&
+              std::abs(mine[3 * q + 1] - theirs[3 * r + 1]) < tol &&
+              std::abs(mine[3 * q + 2] - theirs[3 * r + 2]) < tol) {
+            hit = r;
+            break;
+          }
+        }
+        m->perm[(6 * e + dir) * (size_t)n * n + q] = hit;
+      }
+    }
+  }
+}
+
+// the face direction of neighbour nb that touches element e
+int shell_back_dir(const ShellMesh& m, int64_t e, int64_t nb) {
+  for (int fd = 0; fd < 6; ++fd)
+    if (m.nbr[6 * nb + fd] == e) return fd;
+  return -1;
+}
+
+// curved normal on a face point: unnormalised n_i = sign * invjac(d, i),
+// NormalCovectorAndMagnitude.hpp:57-84 with the inverse spatial metric
+void curved_normal(const double* ij9, double sign, const double* gi6, double nco[3],
+                   double nvec[3], double* mag) {
+  static const int idx[3][3] = {{0, 1, 2}, {1, 3, 4}, {2, 4, 5}};
+  double un[3];
+  for (int i = 0; i < 3; ++i) un[i] = sign * ij9[i];
+  double v[3];
+  for (int i = 0; i < 3; ++i) {
+    v[i] = gi6[idx[i][0]] * un[0];
+    for (int j = 1; j < 3; ++j) v[i] += gi6[idx[i][j]] * un[j];
+  }
+  double m2 = v[0] * un[0] + v[1] * un[1] + v[2] * un[2];
+  *mag = std::sqrt(m2);
+  const double inv = 1.0 / *mag;
+  for (int i = 0; i < 3; ++i) {
+    nco[i] = un[i] * inv;
+    nvec[i] = v[i] * inv;
+  }
+}
+
+int shell_rhs_impl(const ShellMesh& m, const double* u, double* dudt) {
+  const OrcShell& s = m.s;
+  const int n = s.n;
+  const int64_t np = (int64_t)n * n * n;
+  const int nf = n * n;
+  const Spectral1d& sp = spectral(n);
+  int excision_violation = 0;
+#pragma omp parallel for schedule(dynamic, 2) reduction(| : excision_violation)
+  for (int64_t e = 0; e < m.E; ++e) {
+    const double* ue = u + e * 5 * np;
+    double* dt = dudt + e * 5 * np;
+    const double* X = &m.xyz[e * 3 * np];
+    const double* IJ = &m.ij[e * 9 * np];
+    std::vector<double> dl(15 * np), du(15 * np), bg(26 * np);
+    // logical derivatives (PartialDerivatives.tpp:315-363)
+    for (int v = 0; v < 5; ++v)
+      for (int a = 0; a < 3; ++a)
+        for (int k = 0; k < n; ++k)
+          for (int j = 0; j < n; ++j)
+            for (int i = 0; i < n; ++i) {
+              const int idx[3] = {i, j, k};
+              double acc = 0.0;
+              for (int q = 0; q < n; ++q) {
+                int id2[3] = {i, j, k};
+                id2[a] = q;
+                acc += sp.D[idx[a] * n + q] * ue[v * np + id2[0] + n * (id2[1] + n * id2[2])];
+              }
+              dl[(3 * v + a) * np + i + n * (j + (int64_t)n * k)] = acc;
+            }
+    // partial derivatives: du[(3v+i)] = sum_a invjac(a,i) d_a u_v, a = 0 first
+    for (int v = 0; v < 5; ++v)
+      for (int i = 0; i < 3; ++i)
+        for (int64_t p = 0; p < np; ++p) {
+          double acc = IJ[(3 * 0 + i) * np + p] * dl[(3 * v + 0) * np + p];
+          acc += IJ[(3 * 1 + i) * np + p] * dl[(3 * v + 1) * np + p];
+          acc += IJ[(3 * 2 + i) * np + p] * dl[(3 * v + 2) * np + p];
+          du[(3 * v + i) * np + p] = acc;
+        }
+    orc_ks_background((int)np, s.mass, X, bg.data());
+    // d_phi(i, j) = d_i Phi_j = du[(3*(2+j)+i)]
+    std::vector<double> dphi(9 * np);
+    for (int i = 0; i < 3; ++i)
+      for (int j = 0; j < 3; ++j)
+        for (int64_t p = 0; p < np; ++p) dphi[(3 * i + j) * np + p] = du[(3 * (2 + j) + i) * np + p];
+    orc_csw_time_derivative((int)np, du.data(), du.data() + 3 * np, dphi.data(), ue + np,
+                            ue + 2 * np, bg.data(), s.gamma1, s.gamma2, dt);
+    // external faces first (they use the volume time derivative), then mortars
+    for (int pass = 0; pass < 2; ++pass)
+      for (int dir = 0; dir < 6; ++dir) {
+        const int64_t nb = m.nbr[6 * e + dir];
+        if ((pass == 0) != (nb < 0)) continue;
+        const int d = dir / 2;
+        const bool upper = dir % 2;
+        const int slice = upper ? n - 1 : 0;
+        const double sign = upper ? 1.0 : -1.0;
+        for (int bb = 0; bb < n; ++bb)
+          for (int aa = 0; aa < n; ++aa) {
+            const int q = aa + n * bb;
+            const int64_t vp = volume_index(n, d, slice, aa, bb);
+            double ij9[3], gi6[6], nco[3], nvec[3], mag;
+            for (int i = 0; i < 3; ++i) ij9[i] = IJ[(3 * d + i) * np + vp];
+            for (int t = 0; t < 6; ++t) gi6[t] = bg[(16 + t) * np + vp];
+            curved_normal(ij9, sign, gi6, nco, nvec, &mag);
+            const double lapse = bg[vp];
+            double shift[3];
+            for (int i = 0; i < 3; ++i) shift[i] = bg[(1 + i) * np + vp];
+            const double g1 = s.gamma1, g2 = s.gamma2;
+            const double psi = ue[vp], pi = ue[np + vp];
+            double phi[3];
+            for (int i = 0; i < 3; ++i) phi[i] = ue[(2 + i) * np + vp];
+            if (nb == -1) {
+              // DemandOutgoingCharSpeeds (DemandOutgoingCharSpeeds.cpp:40-77)
+              double bn = shift[0] * nco[0] + shift[1] * nco[1] + shift[2] * nco[2];
+              const double sp4[4] = {-(1.0 + g1) * bn, -bn, -bn + lapse, -bn - lapse};
+              for (double c : sp4)
+                if (c < 0.0) excision_violation = 1;
+              continue;
+            }
+            if (nb == -2) {
+              // ConstraintPreservingSphericalRadiation::dg_time_derivative
+              double dps[3], dpi[3], dph[9], dtphi[3], xyz3[3], out[5];
+              for (int i = 0; i < 3; ++i) {
+                dps[i] = du[(3 * 0 + i) * np + vp];
+                dpi[i] = du[(3 * 1 + i) * np + vp];
+                dtphi[i] = dt[(2 + i) * np + vp];
+                xyz3[i] = X[i * np + vp];
+              }
+              for (int t = 0; t < 9; ++t) dph[t] = dphi[t * np + vp];
+              double dtpsi = dt[vp], dtpi = dt[np + vp];
+              orc_csw_cpsr(1, &psi, &pi, phi, &lapse, shift, &g1, &g2, nco, nvec, xyz3, dps, dpi,
+                           dph, &dtpsi, &dtpi, dtphi, out);
+              for (int v = 0; v < 5; ++v) dt[v * np + vp] += out[v];
+              continue;
+            }
+            // interior mortar: UpwindPenalty on both sides, lift_flux
+            double pk_i[14], pk_e[14], ms;
+            orc_csw_package(1, &psi, &pi, phi, &lapse, shift, &g1, &g2, nco, nvec, nullptr, pk_i,
+                            &ms);
+            const int nd = shell_back_dir(m, e, nb);
+            const int nd_d = nd / 2;
+            const int nq = m.perm[(6 * e + dir) * (size_t)nf + q];
+            const int na = nq % n, nbq = nq / n;
+            const int nslice = (nd % 2) ? n - 1 : 0;
+            const int64_t nvp = volume_index(n, nd_d, nslice, na, nbq);
+            const double* un = u + nb * 5 * np;
+            const double* IJn = &m.ij[nb * 9 * np];
+            double nX[3];
+            for (int i = 0; i < 3; ++i) nX[i] = m.xyz[nb * 3 * np + i * np + nvp];
+            double nbg[26];
+            orc_ks_background(1, s.mass, nX, nbg);
+            double nij9[3], ngi6[6], nnco[3], nnvec[3], nmag;
+            for (int i = 0; i < 3; ++i) nij9[i] = IJn[(3 * nd_d + i) * np + nvp];
+            for (int t = 0; t < 6; ++t) ngi6[t] = nbg[16 + t];
+            curved_normal(nij9, (nd % 2) ? 1.0 : -1.0, ngi6, nnco, nnvec, &nmag);
+            const double npsi = un[nvp], npi = un[np + nvp];
+            double nphi[3], nshift[3];
+            for (int i = 0; i < 3; ++i) {
+              nphi[i] = un[(2 + i) * np + nvp];
+              nshift[i] = nbg[1 + i];
+            }
+            orc_csw_package(1, &npsi, &npi, nphi, &nbg[0], nshift, &g1, &g2, nnco, nnvec, nullptr,
+                            pk_e, &ms);
+            double bc[5];
+            orc_csw_boundary_terms(1, pk_i, pk_e, bc);
+            const double fac = -0.5 * static_cast<double>(n * (n - 1)) * mag;
+            for (int v = 0; v < 5; ++v) dt[v * np + vp] += bc[v] * fac;
+          }
+      }
+  }
+  return excision_violation;
+}
+
+}  // namespace
+
+extern "C" {
+
+int64_t orc_shell_num_elements(const OrcShell* s) {
+  if (!s) return -1;
+  return 6 * shell_layout(*s).per_block;
+}
+
+static int check_shell(const OrcShell* s) {
+  if (!s || s->n < 2 || s->n > kMaxN || s->ref_ang < 0 || s->ref_rad < 0 || s->ref_ang > 6 ||
+      s->ref_rad > 6 || !(s->r_outer > s->r_inner) || !(s->r_inner > 0))
+    return -1;
+  return 0;
+}
+
+int orc_shell_geometry(const OrcShell* s, double* xyz, double* inv_jac) {
+  if (check_shell(s) || !xyz || !inv_jac) return -1;
+  ShellMesh m;
+  build_shell(*s, &m);
+  std::memcpy(xyz, m.xyz.data(), m.xyz.size() * sizeof(double));
+  std::memcpy(inv_jac, m.ij.data(), m.ij.size() * sizeof(double));
+  return 0;
+}
+
+int orc_shell_connectivity(const OrcShell* s, int32_t* nbr, int32_t* perm, uint64_t* ids) {
+  if (check_shell(s)) return -1;
+  ShellMesh m;
+  build_shell(*s, &m);
+  if (nbr) std::memcpy(nbr, m.nbr.data(), m.nbr.size() * sizeof(int32_t));
+  if (perm) std::memcpy(perm, m.perm.data(), m.perm.size() * sizeof(int32_t));
+  if (ids)
+    for (int64_t e = 0; e < m.E; ++e) {
+      int block, seg[3];
+      shell_element(m.l, e, &block, seg);
+      ids[e] = (uint64_t)block | ((uint64_t)seg[0] << 16) | ((uint64_t)m.l.L[0] << 28) |
+               ((uint64_t)seg[1] << 32) | ((uint64_t)m.l.L[1] << 44) |
+               ((uint64_t)seg[2] << 48) | ((uint64_t)m.l.L[2] << 60);
+    }
+  return 0;
+}
+
+int orc_shell_initial_data(const OrcShell* s, double r0, double w, double* u) {
+  if (check_shell(s) || !u) return -1;
+  ShellMesh m;
+  build_shell(*s, &m);
+  const int64_t np = (int64_t)s->n * s->n * s->n;
+  for (int64_t e = 0; e < m.E; ++e)
+    for (int64_t p = 0; p < np; ++p) {
+      double x[3];
+      for (int i = 0; i < 3; ++i) x[i] = m.xyz[e * 3 * np + i * np + p];
+      const double r = std::sqrt(x[0] * x[0] + x[1] * x[1] + x[2] * x[2]);
+      const double psi = std::exp(-(r - r0) * (r - r0) / (w * w));
+      double* ue = u + e * 5 * np;
+      ue[p] = psi;
+      ue[np + p] = 0.0;
+      for (int i = 0; i < 3; ++i) ue[(2 + i) * np + p] = -2.0 * (r - r0) / (w * w) * psi * x[i] / r;
+    }
+  return 0;
+}
+
+int orc_shell_rhs(const OrcShell* s, const double* u, double* dudt, int n_threads) {
+  if (check_shell(s) || !u || !dudt) return -1;
+#ifdef _OPENMP
+  if (n_threads > 0) omp_set_num_threads(n_threads);
+#endif
+  (void)n_threads;
+  ShellMesh m;
+  build_shell(*s, &m);
+  return shell_rhs_impl(m, u, dudt);
+}
+
+int orc_shell_evolve(const OrcShell* s, double dt, int n_steps, double* u, int n_threads) {
+  if (check_shell(s) || !u || n_steps < 0) return -1;
+#ifdef _OPENMP
+  if (n_threads > 0) omp_set_num_threads(n_threads);
+#endif
+  (void)n_threads;
+  ShellMesh m;
+  build_shell(*s, &m);
+  const int64_t n = m.E * 5 * (int64_t)s->n * s->n * s->n;
+  std::vector<double> u0(n), u1(n), du(n);
+  int rc = 0;
+  for (int st = 0; st < n_steps; ++st) {
+    std::memcpy(u0.data(), u, n * sizeof(double));
+    rc |= shell_rhs_impl(m, u0.data(), du.data());
+    orc_rk3_substep(n, 0, dt, u0.data(), u0.data(), du.data(), u1.data());
+    rc |= shell_rhs_impl(m, u1.data(), du.data());
+    orc_rk3_substep(n, 1, dt, u0.data(), u1.data(), du.data(), u);
+    std::memcpy(u1.data(), u, n * sizeof(double));
+    rc |= shell_rhs_impl(m, u1.data(), du.data());
+    orc_rk3_substep(n, 2, dt, u0.data(), u1.data(), du.data(), u);
+  }
+  return rc;
+}
+
+}  // extern "C"

@@ -111,6 +111,77 @@ int orc_rk3_substep(int64_t n, int k, double dt, const double* u0,
 int orc_evolve(int n_inst, const OrcBrick* bricks, const int32_t* elem_n,
                double gamma2, double dt, int n_steps, double* u, int n_threads);
 
+
+/* ---------------- CurvedScalarWave (configuration 5) ----------------
+ * Follows (paths relative to the SpECTRE tree):
+ *   TimeDerivative       src/Evolution/Systems/CurvedScalarWave/TimeDerivative.cpp:19-69
+ *   characteristics      src/Evolution/Systems/CurvedScalarWave/Characteristics.cpp:20-137
+ *   UpwindPenalty        src/Evolution/Systems/CurvedScalarWave/BoundaryCorrections/UpwindPenalty.cpp:35-146
+ *   CPSR boundary        src/Evolution/Systems/CurvedScalarWave/BoundaryConditions/
+ *                        ConstraintPreservingSphericalRadiation.cpp:40-156
+ *   Schwarzschild in Kerr-Schild coordinates: the closed forms checked by
+ *   tests/Unit/PointwiseFunctions/AnalyticSolutions/GeneralRelativity/Test_KerrSchild.cpp:55-232
+ * Per point, component-major arrays of npts each. */
+
+/* background out (26 per point): lapse, shift[3], d_lapse[3],
+ * d_shift[9] (d_i shift^j at 3*i+j), inv_metric[6] (xx xy xz yy yz zz),
+ * trace_christoffel[3], trace_K */
+int orc_ks_background(int npts, double mass, const double* xyz, double* bg);
+/* dt (5*npts) from d_psi[3], d_pi[3], d_phi[9] (d_i Phi_j at 3*i+j), pi,
+ * phi[3], background (26*npts), gamma1, gamma2 */
+int orc_csw_time_derivative(int npts, const double* d_psi, const double* d_pi,
+                            const double* d_phi, const double* pi,
+                            const double* phi, const double* bg, double gamma1,
+                            double gamma2, double* dt);
+/* packaged 14*npts: v_psi, v_zero[3], v_plus, v_minus, gamma2, normal[3],
+ * char_speeds[4]; returns the max char speed. ndotv may be NULL. */
+int orc_csw_package(int npts, const double* psi, const double* pi,
+                    const double* phi, const double* lapse, const double* shift,
+                    const double* gamma1, const double* gamma2,
+                    const double* normal, const double* normal_vector,
+                    const double* ndotv, double* packaged, double* max_speed);
+int orc_csw_boundary_terms(int npts, const double* pkg_int, const double* pkg_ext,
+                           double* out);
+/* CPSR dt corrections (5*npts) */
+int orc_csw_cpsr(int npts, const double* psi, const double* pi,
+                 const double* phi, const double* lapse, const double* shift,
+                 const double* gamma1, const double* gamma2, const double* normal,
+                 const double* normal_vector, const double* xyz,
+                 const double* d_psi, const double* d_pi, const double* d_phi,
+                 const double* dt_psi, const double* dt_pi, const double* dt_phi,
+                 double* out);
+
+/* ---------------- spherical shell of 6 wedges (configuration 5) ----------------
+ * Domain/Creators/Sphere.cpp (shell, no interior), Domain/CoordinateMaps/Wedge.cpp:476-536
+ * (sphericity 1 inside and out, equiangular, logarithmic radial distribution),
+ * block orientations DomainHelpers.cpp:553-578 (+z, -z, +y, -y, +x, -x),
+ * refinement (ref_ang, ref_ang, ref_rad) per block, elements in
+ * initial_element_ids order.  Neighbours across blocks are found by matching
+ * face centres; face points are matched by their coordinates (the role of
+ * orient_variables_on_slice, OrientationMapHelpers.hpp:63-120). */
+typedef struct {
+  double r_inner, r_outer;
+  int32_t ref_ang, ref_rad;
+  int32_t n;        /* LGL points per dimension */
+  double mass;      /* Kerr-Schild mass (spin 0) */
+  double gamma1, gamma2;
+} OrcShell;
+int64_t orc_shell_num_elements(const OrcShell* s);
+/* coordinates (3*N^3) and inverse Jacobian (9*N^3, d xi^a / d x^i at 3a+i)
+ * per element, component-major within the element */
+int orc_shell_geometry(const OrcShell* s, double* xyz, double* inv_jac);
+/* nbr: 6 per element, -1 inner boundary, -2 outer boundary; perm: 6*N^2 per
+ * element, the neighbour's face-point index of each of this face's points;
+ * element_ids: packed ElementId bits */
+int orc_shell_connectivity(const OrcShell* s, int32_t* nbr, int32_t* perm,
+                           uint64_t* element_ids);
+/* Gaussian shell psi = exp(-(r - r0)^2 / w^2), Pi = 0, Phi = grad psi */
+int orc_shell_initial_data(const OrcShell* s, double r0, double w, double* u);
+/* curved DG time derivative with UpwindPenalty, excision check at the inner
+ * sphere (returns 1 if a char speed is incoming) and CPSR at the outer one */
+int orc_shell_rhs(const OrcShell* s, const double* u, double* dudt, int n_threads);
+int orc_shell_evolve(const OrcShell* s, double dt, int n_steps, double* u, int n_threads);
+
 #ifdef __cplusplus
 }
 #endif

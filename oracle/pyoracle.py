@@ -19,6 +19,13 @@ class OrcBrick(ctypes.Structure):
                 ("n", ctypes.c_int32 * 3)]
 
 
+class OrcShell(ctypes.Structure):
+    _fields_ = [("r_inner", ctypes.c_double), ("r_outer", ctypes.c_double),
+                ("ref_ang", ctypes.c_int32), ("ref_rad", ctypes.c_int32),
+                ("n", ctypes.c_int32), ("mass", ctypes.c_double),
+                ("gamma1", ctypes.c_double), ("gamma2", ctypes.c_double)]
+
+
 def build():
     subprocess.run(["make", "-s", "-C", HERE], check=True)
     return LIB
@@ -45,6 +52,14 @@ def lib():
             "orc_package": [I, P, P, P, P, P, P, P, P], "orc_boundary_terms": [I, P, P, P],
             "orc_rhs": [I, P, P, D, P, P, I], "orc_volume_rhs": [I, P, P, D, P, P, I],
             "orc_rk3_substep": [I64, I, D, P, P, P, P], "orc_evolve": [I, P, P, D, D, I, P, I],
+            "orc_ks_background": [I, D, P, P],
+            "orc_csw_time_derivative": [I, P, P, P, P, P, P, D, D, P],
+            "orc_csw_package": [I, P, P, P, P, P, P, P, P, P, P, P, P],
+            "orc_csw_boundary_terms": [I, P, P, P],
+            "orc_csw_cpsr": [I] + [P] * 17,
+            "orc_shell_geometry": [P, P, P], "orc_shell_connectivity": [P, P, P, P],
+            "orc_shell_initial_data": [P, D, D, P], "orc_shell_rhs": [P, P, P, I],
+            "orc_shell_evolve": [P, D, I, P, I],
         }
         for name, args in sig.items():
             fn = getattr(L, name)
@@ -52,6 +67,8 @@ def lib():
             fn.restype = I
         L.orc_num_elements.argtypes = [I, P]
         L.orc_num_elements.restype = I64
+        L.orc_shell_num_elements.argtypes = [P]
+        L.orc_shell_num_elements.restype = I64
         _lib = L
     return _lib
 
@@ -210,3 +227,105 @@ def evolve(bricks, points, u, dt, steps, gamma2=0.0, threads=0):
 
 def gaussian_params(n_inst, amp=1.0, width=0.5, center=(math.pi, math.pi, math.pi)):
     return np.tile(np.array([amp, width, *center], dtype=np.float64), (n_inst, 1))
+
+
+def _c(a):
+    return np.ascontiguousarray(a, dtype=np.float64)
+
+
+def ks_background(xyz, mass=1.0):
+    """26 x npts: lapse, shift[3], d_lapse[3], d_shift[9] (d_i shift^j),
+    inverse metric[6], trace Christoffel[3], trace K."""
+    xyz = _c(xyz)
+    n = xyz.shape[1]
+    bg = np.zeros((26, n))
+    _check(lib().orc_ks_background(n, mass, _p(xyz), _p(bg)))
+    return bg
+
+
+def csw_time_derivative(d_psi, d_pi, d_phi, pi, phi, bg, gamma1, gamma2):
+    d_psi, d_pi, d_phi, pi, phi, bg = map(_c, (d_psi, d_pi, d_phi, pi, phi, bg))
+    n = pi.shape[0]
+    dt = np.zeros((5, n))
+    _check(lib().orc_csw_time_derivative(n, _p(d_psi), _p(d_pi), _p(d_phi), _p(pi), _p(phi),
+                                         _p(bg), gamma1, gamma2, _p(dt)))
+    return dt
+
+
+def csw_package(psi, pi, phi, lapse, shift, gamma1, gamma2, normal, normal_vector, ndotv=None):
+    a = [_c(x) for x in (psi, pi, phi, lapse, shift, gamma1, gamma2, normal, normal_vector)]
+    n = a[0].shape[0]
+    out = np.zeros((14, n))
+    ms = ctypes.c_double()
+    nd = None if ndotv is None else _c(ndotv)
+    _check(lib().orc_csw_package(n, *[_p(x) for x in a], _p(nd), _p(out), ctypes.addressof(ms)))
+    return out, ms.value
+
+
+def csw_boundary_terms(pkg_int, pkg_ext):
+    a, b = _c(pkg_int), _c(pkg_ext)
+    out = np.zeros((5, a.shape[1]))
+    _check(lib().orc_csw_boundary_terms(a.shape[1], _p(a), _p(b), _p(out)))
+    return out
+
+
+def csw_cpsr(psi, pi, phi, lapse, shift, gamma1, gamma2, normal, normal_vector, xyz, d_psi,
+             d_pi, d_phi, dt_psi, dt_pi, dt_phi):
+    a = [_c(x) for x in (psi, pi, phi, lapse, shift, gamma1, gamma2, normal, normal_vector, xyz,
+                         d_psi, d_pi, d_phi, dt_psi, dt_pi, dt_phi)]
+    n = a[0].shape[0]
+    out = np.zeros((5, n))
+    _check(lib().orc_csw_cpsr(n, *[_p(x) for x in a], _p(out)))
+    return out
+
+
+def shell(r_inner=1.9, r_outer=20.0, ref_ang=2, ref_rad=3, n=10, mass=1.0, gamma1=0.0,
+          gamma2=0.0):
+    """Six-wedge spherical shell, (ref_ang, ref_ang, ref_rad) per wedge."""
+    return OrcShell(r_inner, r_outer, ref_ang, ref_rad, n, mass, gamma1, gamma2)
+
+
+def shell_num_elements(s):
+    return int(lib().orc_shell_num_elements(ctypes.byref(s)))
+
+
+def shell_geometry(s):
+    """(xyz [E,3,N^3], inv_jac [E,9,N^3]) with inv_jac[3a+i] = d xi^a / d x^i."""
+    E, np3 = shell_num_elements(s), s.n ** 3
+    xyz = np.zeros((E, 3, np3))
+    ij = np.zeros((E, 9, np3))
+    _check(lib().orc_shell_geometry(ctypes.byref(s), _p(xyz), _p(ij)))
+    return xyz, ij
+
+
+def shell_connectivity(s):
+    E = shell_num_elements(s)
+    nbr = np.zeros((E, 6), dtype=np.int32)
+    perm = np.zeros((E, 6, s.n * s.n), dtype=np.int32)
+    ids = np.zeros(E, dtype=np.uint64)
+    _check(lib().orc_shell_connectivity(ctypes.byref(s), _p(nbr), _p(perm), _p(ids)))
+    return nbr, perm, ids
+
+
+def shell_initial_data(s, r0=8.0, width=1.5):
+    u = np.zeros((shell_num_elements(s), 5, s.n ** 3))
+    _check(lib().orc_shell_initial_data(ctypes.byref(s), r0, width, _p(u)))
+    return u
+
+
+def shell_rhs(s, u, threads=0):
+    """Returns (dudt, excision_ok)."""
+    u = _c(u)
+    du = np.zeros_like(u)
+    rc = lib().orc_shell_rhs(ctypes.byref(s), _p(u), _p(du), threads)
+    if rc < 0:
+        _check(rc)
+    return du, rc == 0
+
+
+def shell_evolve(s, u, dt, steps, threads=0):
+    u = _c(u).copy()
+    rc = lib().orc_shell_evolve(ctypes.byref(s), dt, steps, _p(u), threads)
+    if rc < 0:
+        _check(rc)
+    return u, rc == 0

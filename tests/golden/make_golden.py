@@ -8,6 +8,10 @@ Fixtures:
   lgl_golden.json      LGL points/weights, D-matrices and Vandermonde matrices
                        read as text from
                        tests/Unit/NumericalAlgorithms/Spectral/Test_LegendreGaussLobatto.cpp
+  curved_golden.json   seeded inputs and outputs of the CurvedScalarWave pypp
+                       golden functions: BoundaryCorrections/UpwindPenalty.py
+                       and BoundaryConditions/ConstraintPreservingSphericalRadiation.py
+                       under tests/Unit/Evolution/Systems/CurvedScalarWave
   upwind_golden.json   seeded inputs and the outputs of the reference's pypp
                        golden functions
                        tests/Unit/Evolution/Systems/ScalarWave/BoundaryCorrections/UpwindPenalty.py
@@ -168,11 +172,96 @@ def upwind_golden(seed=20241204, npts=40):
     }
 
 
+def curved_golden(seed=20241205, npts=30):
+    unit = os.path.join(ROOT, "tests/Unit")
+    if unit not in sys.path:
+        sys.path.insert(0, unit)
+    base = os.path.join(ROOT, "tests/Unit/Evolution/Systems/CurvedScalarWave")
+
+    def load(rel, name):
+        spec = importlib.util.spec_from_file_location(name, os.path.join(base, rel))
+        mod = importlib.util.module_from_spec(spec)
+        spec.loader.exec_module(mod)
+        return mod
+
+    up = load("BoundaryCorrections/UpwindPenalty.py", "ref_csw_upwind")
+    cp = load("BoundaryConditions/ConstraintPreservingSphericalRadiation.py", "ref_csw_cpsr")
+    rng = np.random.default_rng(seed)
+
+    def side():
+        d = {
+            "psi": rng.uniform(-1, 1, npts), "pi": rng.uniform(-1, 1, npts),
+            "phi": rng.uniform(-1, 1, (3, npts)), "lapse": rng.uniform(0.3, 1.0, npts),
+            "shift": rng.uniform(-0.6, 0.6, (3, npts)), "gamma1": rng.uniform(-1, 1, npts),
+            "gamma2": rng.uniform(0, 2, npts),
+        }
+        nrm = rng.normal(size=(3, npts))
+        nrm /= np.linalg.norm(nrm, axis=0)
+        # a normal vector raised with a random symmetric positive matrix
+        nvec = np.zeros((3, npts))
+        for p in range(npts):
+            A = rng.normal(size=(3, 3)) * 0.2
+            g = np.eye(3) + A @ A.T
+            v = g @ nrm[:, p]
+            nvec[:, p] = v / np.sqrt(v @ nrm[:, p])
+        d["normal"] = nrm
+        d["normal_vector"] = nvec
+        return d
+
+    sides = [side(), side()]
+    pk = []
+    for d in sides:
+        out = np.zeros((14, npts))
+        for p in range(npts):
+            r = up.dg_package_data(d["psi"][p], d["pi"][p], d["phi"][:, p], d["lapse"][p],
+                                   d["shift"][:, p], d["gamma1"][p], d["gamma2"][p],
+                                   d["normal"][:, p], d["normal_vector"][:, p], None, None)
+            out[:, p] = np.concatenate([np.atleast_1d(np.asarray(f, dtype=float)) for f in r])
+        pk.append(out)
+    bt = np.zeros((5, npts))
+    for p in range(npts):
+        def f(pkx):
+            return (pkx[0, p], pkx[1:4, p].copy(), pkx[4, p], pkx[5, p], pkx[6, p], pkx[7:10, p],
+                    pkx[10:14, p])
+        r = up.dg_boundary_terms(*f(pk[0]), *f(pk[1]), True)
+        bt[:, p] = np.concatenate([np.atleast_1d(np.asarray(x, dtype=float)) for x in r])
+    # CPSR dt corrections on side 0 with extra volume data
+    d = sides[0]
+    xyz = rng.uniform(5, 20, (3, npts)) * rng.choice([-1, 1], (3, npts))
+    dpsi = rng.uniform(-1, 1, (3, npts))
+    dpi = rng.uniform(-1, 1, (3, npts))
+    dphi = rng.uniform(-1, 1, (3, 3, npts))
+    dtpsi = rng.uniform(-1, 1, npts)
+    dtpi = rng.uniform(-1, 1, npts)
+    dtphi = rng.uniform(-1, 1, (3, npts))
+    cps = np.zeros((5, npts))
+    for p in range(npts):
+        args = (None, d["normal"][:, p], d["normal_vector"][:, p], d["psi"][p], d["phi"][:, p],
+                xyz[:, p], d["gamma1"][p], d["gamma2"][p], d["lapse"][p], d["shift"][:, p],
+                dtpsi[p], dtpi[p], dtphi[:, p], dpsi[:, p], dpi[:, p], dphi[:, :, p])
+        cps[0, p] = cp.dt_psi_constraint_preserving_spherical_radiation(*args)
+        cps[1, p] = cp.dt_pi_constraint_preserving_spherical_radiation(*args)
+        cps[2:5, p] = cp.dt_phi_constraint_preserving_spherical_radiation(*args)
+    tolist = lambda a: np.asarray(a).tolist()
+    return {
+        "source": "tests/Unit/Evolution/Systems/CurvedScalarWave/{BoundaryCorrections/UpwindPenalty.py,"
+                  "BoundaryConditions/ConstraintPreservingSphericalRadiation.py}",
+        "seed": seed, "npts": npts,
+        "sides": [{k: tolist(v) for k, v in d.items()} for d in sides],
+        "packaged": [tolist(x) for x in pk], "boundary_terms": tolist(bt),
+        "cpsr": {"xyz": tolist(xyz), "d_psi": tolist(dpsi), "d_pi": tolist(dpi),
+                 "d_phi": tolist(dphi), "dt_psi": tolist(dtpsi), "dt_pi": tolist(dtpi),
+                 "dt_phi": tolist(dtphi), "out": tolist(cps)},
+    }
+
+
 def main():
     with open(os.path.join(HERE, "lgl_golden.json"), "w") as f:
         json.dump(lgl_golden(), f, indent=1)
     with open(os.path.join(HERE, "upwind_golden.json"), "w") as f:
         json.dump(upwind_golden(), f)
+    with open(os.path.join(HERE, "curved_golden.json"), "w") as f:
+        json.dump(curved_golden(), f)
     print("wrote fixtures to", HERE)
 
 

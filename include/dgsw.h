@@ -39,7 +39,7 @@
 extern "C" {
 #endif
 
-#define DGSW_ABI_VERSION 1
+#define DGSW_ABI_VERSION 2
 
 typedef enum {
   DGSW_OK = 0,
@@ -51,8 +51,12 @@ typedef enum {
   DGSW_ERR_DEVICE_TIMEOUT = -6 /* a bounded device-side wait gave up */
 } DgswStatus;
 
-/* System::variables_tag, ScalarWave/System.hpp:39-57 */
-typedef enum { DGSW_SYSTEM_SCALAR_WAVE_3D = 0 } DgswSystem;
+/* System::variables_tag, ScalarWave/System.hpp:39-57 and
+ * CurvedScalarWave/System.hpp:24-62 (same Psi, Pi, Phi variables). */
+typedef enum {
+  DGSW_SYSTEM_SCALAR_WAVE_3D = 0,
+  DGSW_SYSTEM_CURVED_SCALAR_WAVE_3D = 1
+} DgswSystem;
 /* BoundaryCorrection creatable classes, ScalarWave/BoundaryCorrections/Factory.hpp */
 typedef enum { DGSW_CORRECTION_UPWIND_PENALTY = 0 } DgswBoundaryCorrection;
 /* TimeStepper creatable classes, Time/TimeSteppers/Factory.hpp */
@@ -72,6 +76,32 @@ typedef struct {
   int32_t elements[3];
 } DgswBrick;
 
+/* CurvedScalarWave domain: a spherical shell of six cubed-sphere wedges
+ * (Domain/Creators/Sphere.cpp, shell without interior cube; Wedge<3>,
+ * Domain/CoordinateMaps/Wedge.cpp:476-536, equiangular, sphericity 1 inside
+ * and out; blocks +z, -z, +y, -y, +x, -x, Domain/DomainHelpers.cpp:553-578),
+ * initial refinement (ang, ang, rad) per wedge, on the analytic Schwarzschild
+ * background in Kerr-Schild coordinates (gr::Solutions::KerrSchild with zero
+ * spin and centre, PointwiseFunctions/AnalyticSolutions/GeneralRelativity/
+ * KerrSchild.cpp).  Inner sphere: DemandOutgoingCharSpeeds (excision,
+ * CurvedScalarWave/BoundaryConditions/DemandOutgoingCharSpeeds.cpp:40-77);
+ * outer sphere: ConstraintPreservingSphericalRadiation
+ * (.../ConstraintPreservingSphericalRadiation.cpp:40-156). */
+typedef enum {
+  DGSW_RADIAL_LINEAR = 0,      /* Domain::CoordinateMaps::Distribution::Linear */
+  DGSW_RADIAL_LOGARITHMIC = 1  /* Distribution::Logarithmic */
+} DgswRadialDistribution;
+
+typedef struct {
+  double inner_radius;
+  double outer_radius;
+  int32_t refinement_angular;  /* elements per wedge along xi and eta: 2^ang */
+  int32_t refinement_radial;   /* elements per wedge along zeta: 2^rad */
+  int32_t radial_distribution; /* DgswRadialDistribution */
+  double mass;                 /* Kerr-Schild mass */
+  double gamma1;               /* CurvedScalarWave constraint damping gamma1 */
+} DgswShell;
+
 typedef struct {
   int32_t system;              /* DgswSystem */
   int32_t boundary_correction; /* DgswBoundaryCorrection */
@@ -85,6 +115,9 @@ typedef struct {
   int32_t uniform_points;
   double gamma2;               /* constraint damping, ScalarWave/Initialize.hpp:33-56 */
   int32_t device;              /* CUDA device ordinal */
+  /* DGSW_SYSTEM_CURVED_SCALAR_WAVE_3D: the shell domain (n_instances = 1,
+   * bricks ignored, uniform_points per element); NULL for the flat system. */
+  const DgswShell* shell;
 } DgswConfig;
 
 typedef struct DgswHandle_* DgswHandle;
@@ -111,7 +144,9 @@ int dgsw_get_state_device(DgswHandle h, double* dev_u);
  * kind 0: PlaneWave (PointwiseFunctions/AnalyticSolutions/WaveEquation/
  *         PlaneWave.cpp:56-80) psi = sin(k.x - |k| t), params = {kx, ky, kz}.
  * kind 1: Gaussian pulse psi = A exp(-|x-c|^2 / w^2), Pi = 0, Phi = grad psi;
- *         params = {A, w, cx, cy, cz} per instance (5 * n_instances values). */
+ *         params = {A, w, cx, cy, cz} per instance (5 * n_instances values).
+ * kind 2: spherical Gaussian shell psi = A exp(-(r - r0)^2 / w^2), Pi = 0,
+ *         Phi = grad psi; params = {A, r0, w} (curved system). */
 int dgsw_set_initial_data(DgswHandle h, int kind, const double* params,
                           double t);
 
@@ -192,12 +227,25 @@ int dgsw_mortar_projections(int ne, int nm, double* face_to_mortar,
  * neighbors: 6 per element in Direction<3>::all_directions() order
  *            (Direction.hpp:186-193), global element index;
  * mortar_points: 6 per element, mortar_mesh extent (MortarHelpers.cpp:21-47);
+ * Curved shell: neighbours -1 on the inner sphere and -2 on the outer one,
+ * where mortar_points is 0 (external boundaries carry no mortar).
  * Any output may be NULL.  Returns DGSW_ERR_UNSUPPORTED when a block id does
  * not fit the reference's 8 block-id bits (the other outputs are still set). */
 int dgsw_index_maps(const DgswConfig* config, uint64_t* element_ids,
                     int32_t* neighbors, int32_t* mortar_points);
 int dgsw_count_elements(const DgswConfig* config, int64_t* n_elements,
                         int64_t* state_doubles);
+/* Shell geometry of a curved configuration (host, FP64): per element the
+ * inertial coordinates (3*N^3, component-major), the inverse Jacobian
+ * d xi^a / d x^i (9*N^3, component 3a+i; ElementMap::inv_jacobian of the
+ * element's affine map composed with Wedge<3>), and for each of the 6 faces
+ * and each face point (a + N*b over the two remaining axes, ascending) the
+ * neighbour's face-point index of the same physical point: the permutation
+ * that orient_variables_on_slice (Domain/Structure/OrientationMapHelpers.cpp)
+ * applies between wedges (6*N^2 per element; -1 on the shell's boundary).
+ * Any output may be NULL. */
+int dgsw_shell_geometry(const DgswConfig* config, double* xyz, double* inverse_jacobian,
+                        int32_t* face_permutation);
 
 /* ---- stepping without any allocation ---------------------------------------
  * No counterpart in the reference.  For callers that cannot allocate device

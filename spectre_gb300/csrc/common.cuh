@@ -24,6 +24,20 @@ struct EoTable {
   double M[kMaxN / 2 + 1];
 };
 
+// CurvedScalarWave static per-point data.
+// Background (26 per point): lapse, shift[3], d_i lapse[3], d_i shift^j[9] at
+// 7 + 3i + j, inverse spatial metric[6] (xx xy xz yy yz zz), Gamma^i[3], K.
+constexpr int kBgFields = 26;
+// Operator coefficient table (41 per point), see csw_fp64.cu:
+//   B^a[3], A_ai[9] (3a+i), G^aj[9] (3a+j), alpha K, C^i[3], d_i alpha[3],
+//   d_i beta^j[9] (3i+j), alpha, beta^i[3]
+enum : int {
+  kTB = 0, kTA = 3, kTG = 12, kTK = 21, kTC = 22, kTDl = 25, kTDs = 28, kTLapse = 37,
+  kTBeta = 38, kCswT = 41
+};
+// Face table (10 per face point): n_i[3], n^i[3], lifted upwind weights[4].
+enum : int { kFn = 0, kFv = 3, kFm = 6, kCswF = 10 };
+
 // Per-stage update u_next = a * u0 + b * ucur + c * L(ucur).
 struct StageCoef {
   double a, b, c;

@@ -69,6 +69,16 @@ struct DgswHandle_ {
   cudaGraphExec_t graph_adj = nullptr;
   int graph_adj_steps = 0;
   double graph_adj_dt = std::nan("");
+  // CurvedScalarWave on the shell: static tables (csw_fp64.cu)
+  bool curved = false;
+  DgswShell shell{};
+  double* c_xyz = nullptr;
+  double* c_ij = nullptr;
+  double* c_T = nullptr;
+  double* c_F = nullptr;
+  float* c_T32 = nullptr;
+  float* c_F32 = nullptr;
+  int32_t* c_X = nullptr;
   // graphs of whole steps
   cudaGraphExec_t graph_one = nullptr;
   cudaGraphExec_t graph_many = nullptr;
@@ -195,6 +205,129 @@ cudaError_t general_f64(DgswHandle h, const double* x, const double* y, double* 
   return launch_general_classes(h, G);
 }
 
+// ---- CurvedScalarWave ------------------------------------------------------
+
+CswLaunch base_csw(DgswHandle h) {
+  CswLaunch L;
+  L.n = h->dom.elem_n.empty() ? 0 : h->dom.elem_n[0];
+  L.n_elem = h->dom.n_elem;
+  L.T = h->c_T;
+  L.F = h->c_F;
+  L.X = h->c_X;
+  L.ij = h->c_ij;
+  L.xyz = h->c_xyz;
+  L.nbr = h->nbr;
+  L.gamma1 = h->shell.gamma1;
+  L.gamma2 = h->cfg.gamma2;
+  L.eo = h->eo;
+  return L;
+}
+
+// FP64 curved stage: out = a u0 + b x + c L(x)
+cudaError_t csw_f64(DgswHandle h, const double* x, const double* u0, double* out, double a,
+                    double b, double c, int boundary = 1) {
+  CswLaunch L = base_csw(h);
+  L.ucur = x;
+  L.u0 = u0;
+  L.unext = out;
+  L.a = a;
+  L.b = b;
+  L.c = c;
+  L.boundary = boundary;
+  return launch_csw_fp64(L, h->stream);
+}
+
+CswMixedLaunch base_csw_mixed(DgswHandle h) {
+  CswMixedLaunch L;
+  L.n = h->dom.elem_n.empty() ? 0 : h->dom.elem_n[0];
+  L.n_elem = h->dom.n_elem;
+  L.T = h->c_T32;
+  L.F = h->c_F32;
+  L.X = h->c_X;
+  L.ij = h->c_ij;
+  L.xyz = h->c_xyz;
+  L.nbr = h->nbr;
+  L.gamma1 = (float)h->shell.gamma1;
+  L.gamma2 = (float)h->cfg.gamma2;
+  L.eo = h->eo;
+  return L;
+}
+
+// The neighbour's value offset of every face point (element * 5 N^3 + its
+// volume point) from the shell's face permutations; -1 / -2 on the inner /
+// outer sphere.
+std::vector<int32_t> shell_face_offsets(const Domain& dom, const ShellGeometry& geo) {
+  const int n = geo.n, nn = n * n, np = nn * n;
+  std::vector<int32_t> X(6 * (size_t)nn * dom.n_elem);
+  for (int64_t e = 0; e < dom.n_elem; ++e)
+    for (int dir = 0; dir < 6; ++dir) {
+      const int32_t nb = dom.neighbor[6 * e + dir];
+      int32_t* out = &X[(6 * e + dir) * (size_t)nn];
+      if (nb < 0) {
+        for (int q = 0; q < nn; ++q) out[q] = nb;
+        continue;
+      }
+      const int nd = geo.back_dir[6 * e + dir];
+      const int d = nd >> 1, sl = (nd & 1) ? n - 1 : 0;
+      for (int q = 0; q < nn; ++q) {
+        const int t = geo.face_perm[(6 * e + dir) * (size_t)nn + q];
+        const int a = t % n, b = t / n;
+        const int p = d == 0 ? sl + n * (a + n * b) : (d == 1 ? a + n * (sl + n * b) : a + n * (b + n * sl));
+        out[q] = nb * kVars * np + p;
+      }
+    }
+  return X;
+}
+
+// Uploads the shell geometry and forms the background, the operator tables
+// and the face geometry on the device (FP64).  Fails if a characteristic
+// speed on the inner (excision) sphere is incoming.
+int csw_init(DgswHandle h, const ShellGeometry& geo) {
+  const int64_t E = h->dom.n_elem;
+  const int n = geo.n;
+  const int64_t np = (int64_t)n * n * n, nn = (int64_t)n * n;
+  cudaError_t e;
+  if ((e = upload(&h->c_xyz, geo.xyz)) != cudaSuccess) return cuda_fail(h, e, "upload coordinates");
+  if ((e = upload(&h->c_ij, geo.inv_jac)) != cudaSuccess)
+    return cuda_fail(h, e, "upload inverse Jacobian");
+  if ((e = upload(&h->c_X, shell_face_offsets(h->dom, geo))) != cudaSuccess)
+    return cuda_fail(h, e, "upload face offsets");
+  DGSW_CUDA(h, cudaMalloc(&h->c_T, (size_t)E * kCswT * np * sizeof(double)));
+  DGSW_CUDA(h, cudaMalloc(&h->c_F, (size_t)E * 6 * kCswF * nn * sizeof(double)));
+  if (mixed(h)) {
+    DGSW_CUDA(h, cudaMalloc(&h->c_T32, (size_t)E * kCswT * np * sizeof(float)));
+    DGSW_CUDA(h, cudaMalloc(&h->c_F32, (size_t)E * 6 * kCswF * nn * sizeof(float)));
+  }
+  double* bg = nullptr;
+  DGSW_CUDA(h, cudaMalloc(&bg, (size_t)E * kBgFields * np * sizeof(double)));
+  CswSetup S;
+  S.n = n;
+  S.n_elem = E;
+  S.xyz = h->c_xyz;
+  S.ij = h->c_ij;
+  S.nbr = h->nbr;
+  S.mass = h->shell.mass;
+  S.gamma1 = h->shell.gamma1;
+  S.bg = bg;
+  S.T = h->c_T;
+  S.T32 = h->c_T32;
+  S.F = h->c_F;
+  S.F32 = h->c_F32;
+  S.excision = h->dev_err;
+  e = launch_csw_setup(S, h->stream);
+  if (e == cudaSuccess) e = cudaStreamSynchronize(h->stream);
+  cudaFree(bg);
+  if (e != cudaSuccess) return cuda_fail(h, e, "shell set-up kernels");
+  int flag = 0;
+  DGSW_CUDA(h, cudaMemcpy(&flag, h->dev_err, sizeof(int), cudaMemcpyDeviceToHost));
+  DGSW_CUDA(h, cudaMemset(h->dev_err, 0, sizeof(int)));
+  if (flag)
+    return fail(h, DGSW_ERR_ARGUMENT,
+                "DemandOutgoingCharSpeeds: a characteristic speed on the inner sphere is "
+                "incoming; the excision surface must lie inside the horizon");
+  return DGSW_OK;
+}
+
 // Reads and clears the device error word; DGSW_ERR_DEVICE_TIMEOUT when set.
 int check_device_error(DgswHandle h) {
   if (!h->dev_err) return DGSW_OK;
@@ -214,6 +347,30 @@ int check_device_error(DgswHandle h) {
 //   B: w2 = w1/2 + dt/4 L(w1)                [u0 + w2]
 //   C: u  = u0 + 2/3 (w2 + w1) + 2dt/3 L(w2)
 cudaError_t enqueue_mixed_stage(DgswHandle h, int k, double dt, const double* u0, double* out) {
+  if (h->curved) {
+    CswMixedLaunch L = base_csw_mixed(h);
+    if (k == 0) {
+      L.x64 = u0;
+      L.c = dt;
+      L.w32 = h->w1;
+    } else if (k == 1) {
+      L.x32 = h->w1;
+      L.alpha = 0.5;
+      L.c = 0.25 * dt;
+      L.w32 = h->w2;
+    } else {
+      L.x32 = h->w2;
+      L.y32 = h->w1;
+      L.alpha = 2.0 / 3.0;
+      L.beta = 2.0 / 3.0;
+      L.c = (2.0 / 3.0) * dt;
+    }
+    if (out) {
+      L.out64 = out;
+      L.base64 = u0;
+    }
+    return launch_csw_mixed(L, h->stream);
+  }
   if (h->general) {
     GeneralLaunch G = base_general(h);
     if (k == 0) {
@@ -276,6 +433,13 @@ cudaError_t enqueue_step(DgswHandle h, double dt) {
     e = enqueue_mixed_stage(h, 1, dt, h->state, nullptr);
     if (e != cudaSuccess) return e;
     return enqueue_mixed_stage(h, 2, dt, h->state, h->state);
+  }
+  if (h->curved) {
+    cudaError_t e = csw_f64(h, h->state, nullptr, h->t1, 0.0, 1.0, dt);
+    if (e != cudaSuccess) return e;
+    e = csw_f64(h, h->t1, h->state, h->t2, 0.75, 0.25, 0.25 * dt);
+    if (e != cudaSuccess) return e;
+    return csw_f64(h, h->t2, h->state, h->state, 1.0 / 3.0, 2.0 / 3.0, (2.0 / 3.0) * dt);
   }
   if (h->general) {
     cudaError_t e = general_f64(h, h->state, nullptr, h->t1, 1.0, 0.0, dt);
@@ -395,11 +559,18 @@ const char* dgsw_last_error(DgswHandle h) {
   return g_last_error.c_str();
 }
 
+// Builds the host maps of either system.
+bool any_domain(const DgswConfig& cfg, Domain* dom, ShellGeometry* geo, std::string* err) {
+  if (cfg.system == DGSW_SYSTEM_CURVED_SCALAR_WAVE_3D) return build_shell_domain(cfg, dom, geo, err);
+  return build_domain(cfg, dom, err);
+}
+
 int dgsw_count_elements(const DgswConfig* cfg, int64_t* n_elements, int64_t* state_doubles) {
   if (!cfg) return fail(nullptr, DGSW_ERR_ARGUMENT, "null config");
   Domain dom;
+  ShellGeometry geo;
   std::string err;
-  if (!build_domain(*cfg, &dom, &err)) return fail(nullptr, DGSW_ERR_ARGUMENT, err);
+  if (!any_domain(*cfg, &dom, &geo, &err)) return fail(nullptr, DGSW_ERR_ARGUMENT, err);
   if (n_elements) *n_elements = dom.n_elem;
   if (state_doubles) *state_doubles = dom.offset.back();
   return DGSW_OK;
@@ -408,18 +579,38 @@ int dgsw_count_elements(const DgswConfig* cfg, int64_t* n_elements, int64_t* sta
 int dgsw_index_maps(const DgswConfig* cfg, uint64_t* ids, int32_t* nbr, int32_t* mortar) {
   if (!cfg) return fail(nullptr, DGSW_ERR_ARGUMENT, "null config");
   Domain dom;
+  ShellGeometry geo;
   std::string err;
-  if (!build_domain(*cfg, &dom, &err)) return fail(nullptr, DGSW_ERR_ARGUMENT, err);
+  if (!any_domain(*cfg, &dom, &geo, &err)) return fail(nullptr, DGSW_ERR_ARGUMENT, err);
   if (ids) std::memcpy(ids, dom.element_id.data(), dom.n_elem * sizeof(uint64_t));
   if (nbr) std::memcpy(nbr, dom.neighbor.data(), 6 * dom.n_elem * sizeof(int32_t));
   if (mortar)
     for (int64_t e = 0; e < dom.n_elem; ++e)
       for (int dir = 0; dir < 6; ++dir) {
-        const int a = dom.elem_n[e], b = dom.elem_n[dom.neighbor[6 * e + dir]];
+        const int32_t nb = dom.neighbor[6 * e + dir];
+        if (nb < 0) {
+          mortar[6 * e + dir] = 0;
+          continue;
+        }
+        const int a = dom.elem_n[e], b = dom.elem_n[nb];
         mortar[6 * e + dir] = a > b ? a : b;
       }
   if (!dom.block_ids_fit)
     return fail(nullptr, DGSW_ERR_UNSUPPORTED, "a block id does not fit in 8 bits");
+  return DGSW_OK;
+}
+
+int dgsw_shell_geometry(const DgswConfig* cfg, double* xyz, double* inv_jac, int32_t* perm) {
+  if (!cfg) return fail(nullptr, DGSW_ERR_ARGUMENT, "null config");
+  if (cfg->system != DGSW_SYSTEM_CURVED_SCALAR_WAVE_3D)
+    return fail(nullptr, DGSW_ERR_ARGUMENT, "not a curved (shell) configuration");
+  Domain dom;
+  ShellGeometry geo;
+  std::string err;
+  if (!build_shell_domain(*cfg, &dom, &geo, &err)) return fail(nullptr, DGSW_ERR_ARGUMENT, err);
+  if (xyz) std::memcpy(xyz, geo.xyz.data(), geo.xyz.size() * sizeof(double));
+  if (inv_jac) std::memcpy(inv_jac, geo.inv_jac.data(), geo.inv_jac.size() * sizeof(double));
+  if (perm) std::memcpy(perm, geo.face_perm.data(), geo.face_perm.size() * sizeof(int32_t));
   return DGSW_OK;
 }
 
@@ -446,13 +637,17 @@ int dgsw_create(const DgswConfig* cfg, DgswHandle* out) {
   if (!h) return fail(nullptr, DGSW_ERR_ARGUMENT, "out of host memory");
   h->cfg = *cfg;
   std::string err;
-  if (!build_domain(*cfg, &h->dom, &err)) {
+  ShellGeometry geo;
+  h->curved = cfg->system == DGSW_SYSTEM_CURVED_SCALAR_WAVE_3D;
+  if (!any_domain(*cfg, &h->dom, &geo, &err)) {
     delete h;
     return fail(nullptr, DGSW_ERR_ARGUMENT, err);
   }
   h->cfg.bricks = nullptr;  // copies live in h->dom
   h->cfg.points_per_element = nullptr;
-  if (cfg->precision == DGSW_PRECISION_MIXED && cfg->gamma2 != 0.0) {
+  if (h->curved) h->shell = *cfg->shell;
+  h->cfg.shell = h->curved ? &h->shell : nullptr;
+  if (!h->curved && cfg->precision == DGSW_PRECISION_MIXED && cfg->gamma2 != 0.0) {
     delete h;
     return fail(nullptr, DGSW_ERR_UNSUPPORTED, "mixed precision needs gamma2 = 0");
   }
@@ -491,8 +686,9 @@ int dgsw_create(const DgswConfig* cfg, DgswHandle* out) {
     if ((e = cudaMalloc(&h->w1, bytes / 2 + 16)) != cudaSuccess) return bail(e, "cudaMalloc w1");
     if ((e = cudaMalloc(&h->w2, bytes / 2 + 16)) != cudaSuccess) return bail(e, "cudaMalloc w2");
   }
-  std::vector<double> jac(3 * h->dom.n_elem);
-  for (int64_t i = 0; i < 3 * h->dom.n_elem; ++i) jac[i] = 2.0 / h->dom.width[i];
+  std::vector<double> jac(3 * h->dom.n_elem, 0.0);
+  if (!h->curved)
+    for (int64_t i = 0; i < 3 * h->dom.n_elem; ++i) jac[i] = 2.0 / h->dom.width[i];
   if ((e = upload(&h->nbr, h->dom.neighbor)) != cudaSuccess) return bail(e, "upload neighbors");
   if ((e = upload(&h->jac, jac)) != cudaSuccess) return bail(e, "upload jacobian");
   if ((e = upload(&h->lower, h->dom.lower)) != cudaSuccess) return bail(e, "upload lower");
@@ -508,6 +704,14 @@ int dgsw_create(const DgswConfig* cfg, DgswHandle* out) {
   if ((e = upload(&h->lgl_x, nodes)) != cudaSuccess) return bail(e, "upload nodes");
   lgl_eo_table(h->dom.elem_n[0], &h->eo);
   lgl_eo_table_transposed(h->dom.elem_n[0], &h->eoT);
+  if (h->curved) {
+    int rc = csw_init(h, geo);
+    if (rc) {
+      const std::string msg = h->err;
+      dgsw_destroy(h);
+      return fail(nullptr, rc, msg);
+    }
+  }
   if (!h->dom.uniform) {
     h->general = true;
     std::vector<int32_t> lists[kMaxN + 1];
@@ -559,6 +763,12 @@ int dgsw_destroy(DgswHandle h) {
   for (double* p : adjbufs)
     if (p) cudaFree(p);
   if (h->samp_off) cudaFree(h->samp_off);
+  double* cdbl[] = {h->c_xyz, h->c_ij, h->c_T, h->c_F};
+  for (double* p : cdbl)
+    if (p) cudaFree(p);
+  if (h->c_T32) cudaFree(h->c_T32);
+  if (h->c_F32) cudaFree(h->c_F32);
+  if (h->c_X) cudaFree(h->c_X);
   if (h->dev_err) cudaFree(h->dev_err);
   for (int n = 0; n <= kMaxN; ++n)
     if (h->class_tasks[n]) cudaFree(h->class_tasks[n]);
@@ -629,6 +839,17 @@ int dgsw_get_state_device(DgswHandle h, double* dev_u) {
 
 int dgsw_set_initial_data(DgswHandle h, int kind, const double* params, double t) {
   if (!h || !params) return fail(h, DGSW_ERR_ARGUMENT, "null argument");
+  if (h->curved) {
+    if (kind != 2) return fail(h, DGSW_ERR_ARGUMENT, "the shell takes initial data kind 2");
+    if (!std::isfinite(params[0]) || !std::isfinite(params[1]) || !(params[2] > 0.0) ||
+        !std::isfinite(params[2]))
+      return fail(h, DGSW_ERR_ARGUMENT, "need finite A, r0 and a positive width");
+    if (int rc = select_device(h)) return rc;
+    DGSW_CUDA(h, launch_csw_initial(h->c_xyz, h->dom.elem_n[0], h->dom.n_elem, params[0],
+                                    params[1], params[2], h->state, h->stream));
+    DGSW_CUDA(h, cudaStreamSynchronize(h->stream));
+    return DGSW_OK;
+  }
   if (kind != 0 && kind != 1) return fail(h, DGSW_ERR_ARGUMENT, "unknown initial data kind");
   if (int rc = select_device(h)) return rc;
   const size_t count = kind == 0 ? 3 : 5 * (size_t)h->dom.bricks.size();
@@ -667,6 +888,18 @@ int dgsw_rhs_device(DgswHandle h, const double* dev_u, double* dev_dudt) {
   if (!h || !dev_u || !dev_dudt) return fail(h, DGSW_ERR_ARGUMENT, "null argument");
   if (dev_u == dev_dudt) return fail(h, DGSW_ERR_ARGUMENT, "input and output must differ");
   if (int rc = select_device(h)) return rc;
+  if (h->curved) {
+    if (mixed(h)) {
+      CswMixedLaunch M = base_csw_mixed(h);
+      M.x64 = dev_u;
+      M.c = 1.0;
+      M.out64 = dev_dudt;
+      DGSW_CUDA(h, launch_csw_mixed(M, h->stream));
+      return DGSW_OK;
+    }
+    DGSW_CUDA(h, csw_f64(h, dev_u, nullptr, dev_dudt, 0.0, 0.0, 1.0));
+    return DGSW_OK;
+  }
   if (mixed(h)) {
     if (h->general) {
       GeneralLaunch G = base_general(h);
@@ -702,6 +935,10 @@ int dgsw_volume_rhs_device(DgswHandle h, const double* dev_u, double* dev_dudt) 
   if (!h || !dev_u || !dev_dudt) return fail(h, DGSW_ERR_ARGUMENT, "null argument");
   if (dev_u == dev_dudt) return fail(h, DGSW_ERR_ARGUMENT, "input and output must differ");
   if (int rc = select_device(h)) return rc;
+  if (h->curved) {
+    DGSW_CUDA(h, csw_f64(h, dev_u, nullptr, dev_dudt, 0.0, 0.0, 1.0, 0));
+    return DGSW_OK;
+  }
   if (h->general) {
     DGSW_CUDA(h, general_f64(h, dev_u, nullptr, dev_dudt, 0.0, 0.0, 1.0, 0));
     return DGSW_OK;
@@ -758,6 +995,19 @@ int dgsw_substep(DgswHandle h, int k, double dt) {
     if (k == 0)
       DGSW_CUDA(h, cudaMemcpyAsync(h->u0s, h->state, bytes, cudaMemcpyDeviceToDevice, h->stream));
     DGSW_CUDA(h, enqueue_mixed_stage(h, k, dt, h->u0s, h->state));
+    return DGSW_OK;
+  }
+  if (h->curved) {
+    if (k == 0) {
+      DGSW_CUDA(h, cudaMemcpyAsync(h->u0s, h->state, bytes, cudaMemcpyDeviceToDevice, h->stream));
+      DGSW_CUDA(h, csw_f64(h, h->u0s, nullptr, h->state, 0.0, 1.0, dt));
+    } else {
+      DGSW_CUDA(h, cudaMemcpyAsync(h->t1, h->state, bytes, cudaMemcpyDeviceToDevice, h->stream));
+      if (k == 1)
+        DGSW_CUDA(h, csw_f64(h, h->t1, h->u0s, h->state, 0.75, 0.25, 0.25 * dt));
+      else
+        DGSW_CUDA(h, csw_f64(h, h->t1, h->u0s, h->state, 1.0 / 3.0, 2.0 / 3.0, (2.0 / 3.0) * dt));
+    }
     return DGSW_OK;
   }
   if (h->general) {
@@ -822,8 +1072,9 @@ int dgsw_step(DgswHandle h, int n_steps, double dt) {
 int dgsw_adjoint_rhs_device(DgswHandle h, const double* dev_lambda, double* dev_out) {
   if (!h || !dev_lambda || !dev_out) return fail(h, DGSW_ERR_ARGUMENT, "null argument");
   if (dev_lambda == dev_out) return fail(h, DGSW_ERR_ARGUMENT, "input and output must differ");
-  if (h->general || h->cfg.gamma2 != 0.0)
-    return fail(h, DGSW_ERR_UNSUPPORTED, "the adjoint needs uniform extents and gamma2 = 0");
+  if (h->general || h->curved || h->cfg.gamma2 != 0.0)
+    return fail(h, DGSW_ERR_UNSUPPORTED,
+                "the adjoint needs the flat system, uniform extents and gamma2 = 0");
   if (int rc = select_device(h)) return rc;
   AdjointLaunch A = base_adjoint(h);
   A.x = dev_lambda;
@@ -845,6 +1096,12 @@ int dgsw_set_samples(DgswHandle h, int n_samples, const double* xyz) {
     return fail(h, DGSW_ERR_ARGUMENT, "a sample point lies outside the brick");
   DGSW_CUDA(h, cudaStreamSynchronize(h->stream));
   if (h->samp_off) cudaFree(h->samp_off);
+  double* cdbl[] = {h->c_xyz, h->c_ij, h->c_T, h->c_F};
+  for (double* p : cdbl)
+    if (p) cudaFree(p);
+  if (h->c_T32) cudaFree(h->c_T32);
+  if (h->c_F32) cudaFree(h->c_F32);
+  if (h->c_X) cudaFree(h->c_X);
   if (h->samp_w) cudaFree(h->samp_w);
   h->samp_off = nullptr;
   h->samp_w = nullptr;

@@ -61,6 +61,23 @@ struct Domain {
 bool sample_weights(const Domain& dom, int n, int n_samples, const double* xyz,
                     int64_t* elem_off, double* weights);
 
+// Geometry of the curved shell (shell_setup.cpp), per element: coordinates
+// 3*N^3, inverse Jacobian 9*N^3 (component 3a+i = d xi^a / d x^i), and per
+// face (6) the neighbour's face direction and, per face point, the
+// neighbour's face-point index of the same physical point.
+struct ShellGeometry {
+  int n = 0;
+  std::vector<double> xyz;
+  std::vector<double> inv_jac;
+  std::vector<int32_t> face_perm;
+  std::vector<int32_t> back_dir;
+};
+
+// Builds the shell's element maps (Domain fields: element ids, neighbours
+// with -1 / -2 on the inner / outer sphere, offsets) and its geometry.
+bool build_shell_domain(const DgswConfig& cfg, Domain* dom, ShellGeometry* geo,
+                        std::string* err);
+
 // Validates a configuration and builds every host-side map.  On failure
 // returns false with a message in *err.
 bool build_domain(const DgswConfig& cfg, Domain* dom, std::string* err);

@@ -104,6 +104,72 @@ cudaError_t launch_sample_scatter(double* lam, int n_samples, int n, const int64
                                   const double* w, const double* r, double scale,
                                   cudaStream_t s);
 
+// CurvedScalarWave on the shell (csw_fp64.cu, csw_mixed.cu).
+// Static data, per element: T [kCswT][N^3] coefficients, F [6][kCswF][N^2]
+// face geometry, X [6][N^2] the neighbour's value offset of each face point
+// (element * 5 N^3 + point; -1 inner sphere, -2 outer sphere), ij [9][N^3]
+// inverse Jacobian, xyz [3][N^3] coordinates.
+struct CswLaunch {
+  int n = 0;
+  int64_t n_elem = 0;
+  int boundary = 1;  // 0: volume terms only
+  const double* ucur = nullptr;
+  const double* u0 = nullptr;
+  double* unext = nullptr;  // unext = a u0 + b ucur + c L(ucur)
+  double a = 0.0, b = 0.0, c = 1.0;
+  const double* T = nullptr;
+  const double* F = nullptr;
+  const int32_t* X = nullptr;
+  const double* ij = nullptr;
+  const double* xyz = nullptr;
+  const int32_t* nbr = nullptr;
+  double gamma1 = 0.0, gamma2 = 0.0;
+  EoTable eo{};
+};
+cudaError_t launch_csw_fp64(const CswLaunch& L, cudaStream_t s);
+
+// Mixed-precision stage on the shell: W = alpha X + beta Y + c L(X) in FP32
+// arithmetic, with X either FP64 (compensated double-float derivatives) or
+// an FP32 increment; out64 = base64 + W when set.
+struct CswMixedLaunch {
+  int n = 0;
+  int64_t n_elem = 0;
+  const double* x64 = nullptr;
+  const float* x32 = nullptr;
+  const float* y32 = nullptr;
+  float* w32 = nullptr;
+  double* out64 = nullptr;
+  const double* base64 = nullptr;
+  double alpha = 0.0, beta = 0.0, c = 1.0;
+  const float* T = nullptr;   // FP32 copies of the tables
+  const float* F = nullptr;
+  const int32_t* X = nullptr;
+  const double* ij = nullptr;
+  const double* xyz = nullptr;
+  const int32_t* nbr = nullptr;
+  float gamma1 = 0.0f, gamma2 = 0.0f;
+  EoTable eo{};
+};
+cudaError_t launch_csw_mixed(const CswMixedLaunch& L, cudaStream_t s);
+
+struct CswSetup {
+  int n = 0;
+  int64_t n_elem = 0;
+  const double* xyz = nullptr;
+  const double* ij = nullptr;
+  const int32_t* nbr = nullptr;
+  double mass = 1.0, gamma1 = 0.0;
+  double* bg = nullptr;   // [kBgFields][N^3] per element
+  double* T = nullptr;
+  float* T32 = nullptr;   // optional
+  double* F = nullptr;
+  float* F32 = nullptr;   // optional
+  int* excision = nullptr;  // set to 1 if a speed on the inner sphere is incoming
+};
+cudaError_t launch_csw_setup(const CswSetup& S, cudaStream_t s);
+cudaError_t launch_csw_initial(const double* xyz, int n, int64_t n_elem, double A, double r0,
+                               double w, double* u, cudaStream_t s);
+
 // UpwindPenalty pointwise kernels (face_kernels.cu).
 cudaError_t launch_package_data(int64_t npts, const double* psi, const double* pi,
                                 const double* phi, const double* gamma2,

@@ -53,13 +53,25 @@ class DgswBrick(ctypes.Structure):
                 ("elements", ctypes.c_int32 * 3)]
 
 
+class DgswShell(ctypes.Structure):
+    _fields_ = [("inner_radius", ctypes.c_double), ("outer_radius", ctypes.c_double),
+                ("refinement_angular", ctypes.c_int32), ("refinement_radial", ctypes.c_int32),
+                ("radial_distribution", ctypes.c_int32), ("mass", ctypes.c_double),
+                ("gamma1", ctypes.c_double)]
+
+
 class DgswConfig(ctypes.Structure):
     _fields_ = [("system", ctypes.c_int32), ("boundary_correction", ctypes.c_int32),
                 ("time_stepper", ctypes.c_int32), ("precision", ctypes.c_int32),
                 ("n_instances", ctypes.c_int32), ("bricks", ctypes.POINTER(DgswBrick)),
                 ("points_per_element", ctypes.POINTER(ctypes.c_int32)),
                 ("uniform_points", ctypes.c_int32), ("gamma2", ctypes.c_double),
-                ("device", ctypes.c_int32)]
+                ("device", ctypes.c_int32), ("shell", ctypes.POINTER(DgswShell))]
+
+
+SYSTEM_SCALAR_WAVE = 0
+SYSTEM_CURVED_SCALAR_WAVE = 1
+RADIAL_DISTRIBUTIONS = {"linear": 0, "logarithmic": 1}
 
 
 _P = ctypes.c_void_p
@@ -92,6 +104,7 @@ _SIGNATURES = {
     "dgsw_index_maps": (_I, [ctypes.POINTER(DgswConfig), _P, _P, _P]),
     "dgsw_count_elements": (_I, [ctypes.POINTER(DgswConfig), ctypes.POINTER(_I64),
                                  ctypes.POINTER(_I64)]),
+    "dgsw_shell_geometry": (_I, [ctypes.POINTER(DgswConfig), _P, _P, _P]),
     "dgsw_adjoint_rhs_device": (_I, [_P, _P, _P]),
     "dgsw_set_samples": (_I, [_P, _I, _P]),
     "dgsw_sample_psi": (_I, [_P, _P]),
@@ -191,11 +204,34 @@ class Brick:
     upper: Sequence[float] = (2 * math.pi, 2 * math.pi, 2 * math.pi)
 
 
+@dataclass
+class Shell:
+    """Spherical shell of six cubed-sphere wedges (Domain::Creators::Sphere
+    without its interior) on a Schwarzschild background in Kerr-Schild
+    coordinates; each wedge has 2^refinement_angular x 2^refinement_angular x
+    2^refinement_radial elements."""
+    inner_radius: float = 1.9
+    outer_radius: float = 20.0
+    refinement_angular: int = 2
+    refinement_radial: int = 3
+    radial_distribution: str = "logarithmic"
+    mass: float = 1.0
+    gamma1: float = 0.0
+
+
 class _ConfigHolder:
     """Keeps the ctypes arrays a DgswConfig points to alive."""
 
     def __init__(self, bricks, points, precision=PRECISION_FP64, gamma2=0.0, device=0):
-        self.bricks = (DgswBrick * len(bricks))()
+        self.shell = None
+        if isinstance(bricks, Shell):
+            sh = bricks
+            self.shell = DgswShell(float(sh.inner_radius), float(sh.outer_radius),
+                                   int(sh.refinement_angular), int(sh.refinement_radial),
+                                   RADIAL_DISTRIBUTIONS[sh.radial_distribution],
+                                   float(sh.mass), float(sh.gamma1))
+            bricks = []
+        self.bricks = (DgswBrick * max(1, len(bricks)))()
         for i, b in enumerate(bricks):
             self.bricks[i].lower[:] = [float(v) for v in b.lower]
             self.bricks[i].upper[:] = [float(v) for v in b.upper]
@@ -207,11 +243,11 @@ class _ConfigHolder:
         else:
             self.points = np.ascontiguousarray(points, dtype=np.int32)
         self.cfg = DgswConfig()
-        self.cfg.system = 0
+        self.cfg.system = SYSTEM_CURVED_SCALAR_WAVE if self.shell else SYSTEM_SCALAR_WAVE
         self.cfg.boundary_correction = 0
         self.cfg.time_stepper = 0
         self.cfg.precision = precision
-        self.cfg.n_instances = len(bricks)
+        self.cfg.n_instances = 1 if self.shell else len(bricks)
         self.cfg.bricks = ctypes.cast(self.bricks, ctypes.POINTER(DgswBrick))
         self.cfg.points_per_element = (
             self.points.ctypes.data_as(ctypes.POINTER(ctypes.c_int32))
@@ -219,6 +255,21 @@ class _ConfigHolder:
         self.cfg.uniform_points = uniform
         self.cfg.gamma2 = float(gamma2)
         self.cfg.device = device
+        self.cfg.shell = ctypes.pointer(self.shell) if self.shell else None
+
+
+def shell_geometry(shell: "Shell", points: int):
+    """(xyz [E,3,N^3], inverse Jacobian [E,9,N^3] with component 3a+i =
+    d xi^a / d x^i, face permutations [E,6,N^2]) of a shell (host, FP64)."""
+    h = _ConfigHolder(shell, points)
+    ne, nd = _I64(), _I64()
+    _check(lib().dgsw_count_elements(ctypes.byref(h.cfg), ctypes.byref(ne), ctypes.byref(nd)))
+    E, np3 = ne.value, points ** 3
+    xyz = np.zeros((E, 3, np3))
+    ij = np.zeros((E, 9, np3))
+    perm = np.zeros((E, 6, points * points), dtype=np.int32)
+    _check(lib().dgsw_shell_geometry(ctypes.byref(h.cfg), _ptr(xyz), _ptr(ij), _ptr(perm)))
+    return xyz, ij, perm
 
 
 def index_maps(bricks, points):
@@ -246,6 +297,14 @@ class ScalarWaveSystem:
     variables = ("Psi", "Pi", "Phi")
     number_of_components = N_VARS
     has_primitive_and_conservative_vars = False
+
+
+class CurvedScalarWaveSystem(ScalarWaveSystem):
+    """CurvedScalarWave::System<3> (CurvedScalarWave/System.hpp:24-62): the
+    same variables on a fixed background spacetime (lapse, shift, inverse
+    spatial metric and their derivatives), constraint damping gamma1, gamma2."""
+    spacetime_variables = ("Lapse", "Shift", "InverseSpatialMetric", "DerivLapse",
+                           "DerivShift", "TraceSpatialChristoffel", "TraceExtrinsicCurvature")
 
 
 class UpwindPenalty:
@@ -306,7 +365,8 @@ class Rk3HesthavenSsp:
 
 
 class DgEvolution:
-    """All elements of one or more periodic bricks on one GPU (one handle)."""
+    """All elements of one or more periodic bricks on one GPU (one handle), or
+    of one spherical shell (pass a Shell: the CurvedScalarWave system)."""
 
     def __init__(self, bricks, points, precision=PRECISION_FP64, gamma2=0.0, device=0):
         if isinstance(bricks, Brick):
@@ -320,7 +380,7 @@ class DgEvolution:
         self.n_elements = ne.value
         self.state_size = nd.value
         self.grid_points = npt.value
-        self.bricks = list(bricks)
+        self.bricks = [] if isinstance(bricks, Shell) else list(bricks)
         self.points = points
         self.precision = precision
         self.gamma2 = gamma2
@@ -378,7 +438,7 @@ class DgEvolution:
         return a
 
     def set_initial_data(self, kind: str, params, t: float = 0.0):
-        k = {"plane_wave": 0, "gaussian": 1}[kind]
+        k = {"plane_wave": 0, "gaussian": 1, "gaussian_shell": 2}[kind]
         p = np.ascontiguousarray(params, dtype=np.float64).ravel()
         _check(lib().dgsw_set_initial_data(self._h, k, _ptr(p), float(t)), self._h)
 
@@ -450,3 +510,17 @@ class DgEvolution:
         _torch_ready(g)
         _check(lib().dgsw_misfit_adjoint(self._h, _ptr(g)), self._h)
         return g
+
+
+class CurvedDgEvolution(DgEvolution):
+    """The CurvedScalarWave DG step (EvolveCurvedScalarWave's ComputeTimeDerivative
+    + ApplyBoundaryCorrections + UpdateU) on a Shell, one handle on one GPU.
+    gamma2 is CurvedScalarWave's constraint damping gamma2."""
+
+    def __init__(self, shell: Shell, points: int, precision=PRECISION_FP64, gamma2=1.0,
+                 device=0):
+        super().__init__(shell, points, precision, gamma2, device)
+        self.shell = shell
+
+    def set_gaussian_shell(self, amplitude=1.0, radius=8.0, width=1.0):
+        self.set_initial_data("gaussian_shell", [amplitude, radius, width])

@@ -30,7 +30,7 @@ def test_library_exports_every_header_symbol(dgsw_lib):
         assert hasattr(L, n), n
     # the Python binding declares a signature for every exported function
     assert set(names) <= set(dgsw.exported_symbols()) | {"dgsw_stream"}
-    assert L.dgsw_abi_version() == 1
+    assert L.dgsw_abi_version() == 2
 
 
 @pytest.mark.parametrize("n", sorted(int(k) for k in LGL["points_weights"]))
@@ -132,3 +132,45 @@ def test_null_handle_is_an_error_not_a_crash(dgsw_lib):
     assert L.dgsw_rhs(None, None, None) == -1
     assert L.dgsw_destroy(None) == 0
     assert L.dgsw_create(None, None) == -1
+
+
+# ---------------- curved shell: maps and geometry against the oracle ----------------
+
+SHELLS = [dict(ref_ang=0, ref_rad=0, n=4), dict(ref_ang=1, ref_rad=2, n=5),
+          dict(ref_ang=2, ref_rad=3, n=10)]
+
+
+@pytest.mark.parametrize("case", range(len(SHELLS)))
+def test_shell_maps_bit_exact(dgsw_lib, oracle, case):
+    c = SHELLS[case]
+    shell = dgsw.Shell(1.9, 20.0, c["ref_ang"], c["ref_rad"])
+    s = oracle.shell(1.9, 20.0, c["ref_ang"], c["ref_rad"], c["n"])
+    ids, nbr, mort, fits = dgsw.index_maps(shell, c["n"])
+    onbr, operm, oids = oracle.shell_connectivity(s)
+    assert fits
+    assert ids.tolist() == oids.tolist()
+    assert (nbr == onbr).all()
+    assert ((mort == 0) == (nbr < 0)).all() and (mort[nbr >= 0] == c["n"]).all()
+    xyz, ij, perm = dgsw.shell_geometry(shell, c["n"])
+    assert (perm[nbr >= 0] == operm[nbr >= 0]).all()
+    oxyz, oij = oracle.shell_geometry(s)
+    np.testing.assert_allclose(xyz, oxyz, rtol=0, atol=1e-13 * 20)
+    scale = np.abs(oij).max()
+    np.testing.assert_allclose(ij, oij, rtol=0, atol=1e-13 * scale)
+    # element counts of the reference's Sphere (shell) domain
+    assert len(ids) == 6 * 4 ** c["ref_ang"] * 2 ** c["ref_rad"]
+
+
+@pytest.mark.parametrize("bad", [
+    dict(inner_radius=0.0), dict(inner_radius=5.0, outer_radius=4.0),
+    dict(refinement_angular=-1), dict(radial_distribution="cubic"), dict(mass=-1.0),
+])
+def test_bad_shells_rejected(dgsw_lib, bad):
+    args = dict(inner_radius=1.9, outer_radius=20.0, refinement_angular=0, refinement_radial=0,
+                radial_distribution="logarithmic", mass=1.0)
+    if bad.get("radial_distribution") == "cubic":
+        with pytest.raises(KeyError):
+            dgsw.index_maps(dgsw.Shell(**{**args, **bad}), 4)
+        return
+    with pytest.raises(dgsw.DgswError):
+        dgsw.index_maps(dgsw.Shell(**{**args, **bad}), 4)

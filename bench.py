@@ -321,6 +321,82 @@ def time_adjoint(dev):
         p.close()
 
 
+def time_curved(args, dev, with_cpu):
+    """Config 5: CurvedScalarWave on Schwarzschild in Kerr-Schild coordinates
+    (M = 1, gamma1 = 0, gamma2 = 1), six-wedge shell r in [1.9, 20], 4 x 4
+    angular x 8 radial elements per wedge (768), logarithmic radial map, 10^3
+    LGL points per element, Gaussian shell Psi = exp(-(r-8)^2), excision
+    inside the horizon and the constraint-preserving radiation condition
+    outside; SSP-RK3 dt = 1e-3 for 1000 steps, plain FP64 and mixed."""
+    import torch
+    from oracle import pyoracle
+    from spectre_gb300.dgsw import (CurvedDgEvolution, PRECISION_FP64, PRECISION_MIXED,
+                                    Shell)
+    shell = Shell(1.9, 20.0, 2, 3, "logarithmic", 1.0, 0.0)
+    n, dt = 10, 1e-3
+    steps = 1000 if not args.curved_steps else args.curved_steps
+    res, states = {}, {}
+    for name, prec in (("fp64", PRECISION_FP64), ("mixed", PRECISION_MIXED)):
+        ev = CurvedDgEvolution(shell, n, precision=prec, gamma2=1.0, device=dev)
+        ev.set_gaussian_shell(1.0, 8.0, 1.0)
+        u0 = ev.get_state()
+        # warm-up: graphs captured, then the state reset to t = 0
+        ev.step(16, dt)
+        ev.step(1, dt)
+        ev.set_state(u0)
+        stream = torch.cuda.ExternalStream(ev.stream_ptr(), device=dev)
+        e0 = torch.cuda.Event(enable_timing=True)
+        e1 = torch.cuda.Event(enable_timing=True)
+        torch.cuda.synchronize()
+        e0.record(stream)
+        ev.step(steps, dt, sync=False)
+        e1.record(stream)
+        e1.synchronize()
+        ms = e0.elapsed_time(e1)
+        states[name] = ev.get_state()
+        res[name] = {"value": ev.grid_points * 3 * steps / (ms * 1e-3), "unit": UNIT,
+                     "ms_per_step": ms / steps}
+        points = ev.grid_points
+        if name == "fp64":
+            # FP64 against the oracle over the first steps
+            k = 3
+            ev.set_state(u0)
+            ev.step(k, dt)
+            s_orc = pyoracle.shell(1.9, 20.0, 2, 3, n, 1.0, 0.0, 1.0)
+            ref, _ = pyoracle.shell_evolve(s_orc, u0.reshape(-1, 5, n ** 3), dt, k,
+                                           threads=cpu_threads())
+            got = ev.get_state().reshape(ref.shape)
+            res["fp64"]["max_rel_err_vs_oracle_%d_steps" % k] = float(
+                max(np.abs(got[:, v] - ref[:, v]).max() / np.abs(ref[:, v]).max()
+                    for v in range(5)))
+        ev.close()
+    a, m = states["fp64"], states["mixed"]
+    out = {"workload": "CurvedScalarWave, Kerr-Schild M=1 (gamma1=0, gamma2=1), 6-wedge shell "
+                       "r in [1.9,20], 4x4x8 elements per wedge (768), log radial map, 10^3 "
+                       "LGL points, Gaussian shell Psi=exp(-(r-8)^2), excision + CPSR, "
+                       "SSP-RK3 dt=1e-3",
+           "grid_points": points, "steps": steps, "fp64": res["fp64"], "mixed": res["mixed"],
+           "mixed_speedup_vs_fp64": res["fp64"]["ms_per_step"] / res["mixed"]["ms_per_step"],
+           "rel_l2_mixed_vs_fp64_after_steps": float(np.linalg.norm(m - a) / np.linalg.norm(a)),
+           "max_abs_mixed_vs_fp64": float(np.abs(m - a).max())}
+    if with_cpu:
+        s_orc = pyoracle.shell(1.9, 20.0, 2, 3, n, 1.0, 0.0, 1.0)
+        u = pyoracle.shell_initial_data(s_orc, 8.0, 1.0)
+        threads = cpu_threads()
+        pyoracle.shell_rhs(s_orc, u, threads=threads)
+        t0 = time.perf_counter()
+        reps = 2
+        for _ in range(reps):
+            pyoracle.shell_rhs(s_orc, u, threads=threads)
+        el = (time.perf_counter() - t0) / reps
+        out["cpu_baseline"] = {"value": points / el, "unit": UNIT, "cores": threads,
+                               "kind": "port",
+                               "sample": "oracle curved RHS of the full shell, %d evaluations, "
+                                         "%.2f s each (includes its geometry set-up)"
+                                         % (reps, el)}
+    return out
+
+
 def run_ours(args):
     import torch
     from spectre_gb300 import PRECISION_FP64, PRECISION_MIXED
@@ -385,6 +461,9 @@ def run_ours(args):
     adjoint = None
     if not args.no_adjoint:
         adjoint = time_adjoint(dev)
+    curved = None
+    if not args.no_curved:
+        curved = time_curved(args, dev, rank == 0 and not args.no_cpu_baseline)
 
     cpu = None
     if rank == 0 and not args.no_cpu_baseline:
@@ -412,7 +491,8 @@ def run_ours(args):
                           "inst_per_point_stage": FP64_INST_PER_POINT_STAGE,
                           "note": "FP64 pipe binds the plain path on GB300; peak from a "
                                   "DFMA/DADD throughput probe on this pool's GB300"},
-            "mixed": mixed, "batched": batched, "adjoint": adjoint, "cpu_baseline": cpu, "e2e": e2e, "clocks": clocks,
+            "mixed": mixed, "batched": batched, "adjoint": adjoint, "curved": curved,
+            "cpu_baseline": cpu, "e2e": e2e, "clocks": clocks,
             "gpu_launches": 3 * args.steps,
             "gpu_launches_note": "stage kernels of the timed FP64 region (one launch per stage)",
         }
@@ -432,6 +512,9 @@ def main():
     ap.add_argument("--no-mixed", action="store_true")
     ap.add_argument("--no-batched", action="store_true")
     ap.add_argument("--no-adjoint", action="store_true")
+    ap.add_argument("--no-curved", action="store_true")
+    ap.add_argument("--curved-steps", type=int, default=0,
+                    help="SSP-RK3 steps of the curved shell run (default 1000)")
     ap.add_argument("--elements", type=int, default=ELEMS,
                     help="elements per axis (default 32: the benchmark workload; smaller "
                          "values only for profiling captures)")

@@ -69,15 +69,41 @@ __global__ void __launch_bounds__(kThreads, 2) csw_stage_mixed_kernel(CswMixedLa
   const int tid = threadIdx.x;
   const int64_t off = e * (int64_t)(kVars * NP);
   const bool outer = L.nbr[6 * e + 5] == -2;
+  // state of the element: vector loads when every element block starts on a
+  // 16-byte boundary (even N and an aligned base pointer), else scalar loads
   if (COMP) {
-    for (int q = tid; q < 5 * NP; q += kThreads) {
-      float hi, lo;
-      dev::split_df(L.x64[off + q], hi, lo);
-      Uh[q] = hi;
-      Ul[q] = lo;
+    if (NP % 2 == 0 && (reinterpret_cast<uintptr_t>(L.x64) & 15u) == 0) {
+      const double2* src = reinterpret_cast<const double2*>(L.x64 + off);
+      constexpr int Q = 5 * NP / 2;
+#pragma unroll 4
+      for (int q = tid; q < Q; q += kThreads) {
+        const double2 v = __ldg(src + q);
+        float h0, l0, h1, l1;
+        dev::split_df(v.x, h0, l0);
+        dev::split_df(v.y, h1, l1);
+        Uh[2 * q] = h0;
+        Ul[2 * q] = l0;
+        Uh[2 * q + 1] = h1;
+        Ul[2 * q + 1] = l1;
+      }
+    } else {
+      for (int q = tid; q < 5 * NP; q += kThreads) {
+        float hi, lo;
+        dev::split_df(L.x64[off + q], hi, lo);
+        Uh[q] = hi;
+        Ul[q] = lo;
+      }
     }
   } else {
-    for (int q = tid; q < 5 * NP; q += kThreads) Uh[q] = L.x32[off + q];
+    if (NP % 4 == 0 && (reinterpret_cast<uintptr_t>(L.x32) & 15u) == 0) {
+      const float4* src = reinterpret_cast<const float4*>(L.x32 + off);
+      float4* dst = reinterpret_cast<float4*>(Uh);
+      constexpr int Q = 5 * NP / 4;
+#pragma unroll 4
+      for (int q = tid; q < Q; q += kThreads) dst[q] = __ldg(src + q);
+    } else {
+      for (int q = tid; q < 5 * NP; q += kThreads) Uh[q] = L.x32[off + q];
+    }
   }
   for (int q = tid; q < TAB; q += kThreads) {
     constexpr int h = dev::Eo<N>::h, H = dev::Eo<N>::H;
@@ -103,6 +129,21 @@ __global__ void __launch_bounds__(kThreads, 2) csw_stage_mixed_kernel(CswMixedLa
 
 #pragma unroll 1
   for (int a = 0; a < 3; ++a) {
+    // this round's coefficients (B^a, G^a., A_a.) for the owned points are
+    // loaded before the derivative work, which then hides their latency
+    float cf[PTS][7];
+#pragma unroll
+    for (int r = 0; r < PTS; ++r) {
+      const int p = tid + r * kThreads;
+      if (p < NP) {
+        cf[r][0] = __ldg(T + (kTB + a) * NP + p);
+#pragma unroll
+        for (int j = 0; j < 3; ++j) {
+          cf[r][1 + j] = __ldg(T + (kTG + 3 * a + j) * NP + p);
+          cf[r][4 + j] = __ldg(T + (kTA + 3 * a + j) * NP + p);
+        }
+      }
+    }
     __syncthreads();
     for (int task = tid; task < 5 * NN; task += kThreads) {
       const int v = task / NN, line = task - v * NN;
@@ -129,16 +170,16 @@ __global__ void __launch_bounds__(kThreads, 2) csw_stage_mixed_kernel(CswMixedLa
       if (p < NP) {
         const float gpsi = Ga[p], gpi = Ga[NP + p];
         const float gf[3] = {Ga[2 * NP + p], Ga[3 * NP + p], Ga[4 * NP + p]};
-        const float B = T[(kTB + a) * NP + p];
+        const float B = cf[r][0];
         acc[r][0] = fmaf(B, gpsi, acc[r][0]);
         float s = B * fmaf(g1 * g2, gpsi, gpi);
 #pragma unroll
-        for (int j = 0; j < 3; ++j) s = fmaf(-T[(kTG + 3 * a + j) * NP + p], gf[j], s);
+        for (int j = 0; j < 3; ++j) s = fmaf(-cf[r][1 + j], gf[j], s);
         acc[r][1] += s;
         const float hh = fmaf(g2, gpsi, -gpi);
 #pragma unroll
         for (int i = 0; i < 3; ++i)
-          acc[r][2 + i] = fmaf(T[(kTA + 3 * a + i) * NP + p], hh, fmaf(B, gf[i], acc[r][2 + i]));
+          acc[r][2 + i] = fmaf(cf[r][4 + i], hh, fmaf(B, gf[i], acc[r][2 + i]));
         if (outer && p >= NP - NN) {
           const int q = p - (NP - NN);
           Go[(4 * a + 0) * NN + q] = gpsi;

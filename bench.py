@@ -515,12 +515,20 @@ def main():
     ap.add_argument("--no-curved", action="store_true")
     ap.add_argument("--curved-steps", type=int, default=0,
                     help="SSP-RK3 steps of the curved shell run (default 1000)")
+    ap.add_argument("--curved-only", action="store_true",
+                    help="run only the curved shell workload and print its numbers (for "
+                         "profiling captures)")
     ap.add_argument("--elements", type=int, default=ELEMS,
                     help="elements per axis (default 32: the benchmark workload; smaller "
                          "values only for profiling captures)")
     args = ap.parse_args()
     if args.impl == "reference":
         return run_reference(args)
+    if args.curved_only:
+        import torch
+        torch.cuda.set_device(0)
+        print(json.dumps(time_curved(args, 0, not args.no_cpu_baseline)), flush=True)
+        return 0
     return run_ours(args)
 
 

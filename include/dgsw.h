@@ -186,6 +186,19 @@ int dgsw_boundary_terms_device(int64_t npts, const double* packaged_int,
 int dgsw_step(DgswHandle h, int n_steps, double dt);
 int dgsw_substep(DgswHandle h, int k, double dt);
 
+/* ---- exponential filter ----------------------------------------------------
+ * Filters::Exponential (NumericalAlgorithms/LinearOperators/
+ * ExponentialFilter.cpp:23-80) applied by dg::Actions::Filter
+ * (ParallelAlgorithms/Actions/FilterAction.hpp:109-180) to Psi, Pi and Phi
+ * after every substep's update, as the curved executable's step actions do
+ * (Evolution/Executables/CurvedScalarWave/EvolveCurvedScalarWave.hpp:237-266):
+ * per axis F = V diag(exp(-alpha (k/(N-1))^(2 half_power))) V^-1
+ * (Spectral/Filtering.cpp:18-31).  enable = 0 switches it off.  FP64
+ * precision only (DGSW_ERR_UNSUPPORTED for mixed handles).
+ * dgsw_exponential_filter_matrix: the 1D matrix, row-major (host only). */
+int dgsw_set_exponential_filter(DgswHandle h, double alpha, int half_power, int enable);
+int dgsw_exponential_filter_matrix(int n, double alpha, int half_power, double* F);
+
 /* ---- discrete adjoint and the misfit objective -----------------------------
  * FP64, one brick of uniform extent, gamma2 = 0.  The step map of this path
  * is linear (fixed normals and char speeds), so the reverse sweep needs only

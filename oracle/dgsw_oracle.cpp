@@ -1041,6 +1041,69 @@ int orc_csw_cpsr(int npts, const double* psi, const double* pi, const double* ph
 
 }  // extern "C"
 
+// ======================= exponential filter =======================
+extern "C" {
+
+int orc_exponential_filter(int n, double alpha, int half_power, double* F) {
+  // exponential_filter, Filtering.cpp:18-31: modal_to_nodal * diag * nodal_to_modal
+  if (n < 2 || n > kMaxN || !F || half_power < 0) return -1;
+  double V[kMaxN * kMaxN], Vi[kMaxN * kMaxN];
+  orc_vandermonde(n, V);
+  orc_inv_vandermonde(n, Vi);
+  const double order = n - 1.0;
+  double d[kMaxN];
+  for (int k = 0; k < n; ++k) d[k] = std::exp(-alpha * std::pow(k / order, 2.0 * half_power));
+  for (int i = 0; i < n; ++i)
+    for (int j = 0; j < n; ++j) {
+      double acc = 0.0;
+      for (int k = 0; k < n; ++k) acc += V[i * n + k] * d[k] * Vi[k * n + j];
+      F[i * n + j] = acc;
+    }
+  return 0;
+}
+
+int orc_filter_elements(int64_t n_elem, const int32_t* elem_n, double alpha, int half_power,
+                        double* u) {
+  // dg::Actions::Filter, FilterAction.hpp:109-180: apply_matrices with the
+  // filter matrix of each dimension on every evolved variable
+  if (n_elem < 0 || !elem_n || !u) return -1;
+  std::vector<int64_t> off(n_elem + 1, 0);
+  for (int64_t e = 0; e < n_elem; ++e) {
+    const int64_t n = elem_n[e];
+    if (n < 2 || n > kMaxN) return -1;
+    off[e + 1] = off[e] + 5 * n * n * n;
+  }
+#pragma omp parallel for schedule(static)
+  for (int64_t e = 0; e < n_elem; ++e) {
+    const int n = elem_n[e];
+    const int64_t np = (int64_t)n * n * n;
+    double F[kMaxN * kMaxN];
+    orc_exponential_filter(n, alpha, half_power, F);
+    std::vector<double> tmp(np);
+    for (int v = 0; v < 5; ++v) {
+      double* f = u + off[e] + v * np;
+      for (int d = 0; d < 3; ++d) {
+        for (int k = 0; k < n; ++k)
+          for (int j = 0; j < n; ++j)
+            for (int i = 0; i < n; ++i) {
+              const int idx[3] = {i, j, k};
+              double acc = 0.0;
+              for (int q = 0; q < n; ++q) {
+                int id2[3] = {i, j, k};
+                id2[d] = q;
+                acc += F[idx[d] * n + q] * f[id2[0] + n * (id2[1] + (int64_t)n * id2[2])];
+              }
+              tmp[i + n * (j + (int64_t)n * k)] = acc;
+            }
+        std::memcpy(f, tmp.data(), np * sizeof(double));
+      }
+    }
+  }
+  return 0;
+}
+
+}  // extern "C"
+
 // ======================= spherical shell (configuration 5) =======================
 namespace {
 

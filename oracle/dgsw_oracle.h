@@ -112,6 +112,17 @@ int orc_evolve(int n_inst, const OrcBrick* bricks, const int32_t* elem_n,
                double gamma2, double dt, int n_steps, double* u, int n_threads);
 
 
+/* ---------------- exponential filter ----------------
+ * Spectral::filtering::exponential_filter (NumericalAlgorithms/Spectral/
+ * Filtering.cpp:18-31): F = V diag(exp(-alpha (k/(n-1))^(2 half_power))) V^-1
+ * with V the Legendre Vandermonde on the LGL nodes; F[i*n + j] row-major. */
+int orc_exponential_filter(int n, double alpha, int half_power, double* F);
+/* dg::Actions::Filter (ParallelAlgorithms/Actions/FilterAction.hpp:109-180):
+ * every element's five variables filtered along each axis (apply_matrices
+ * with F in every dimension), in place.  elem_n: extent per element. */
+int orc_filter_elements(int64_t n_elem, const int32_t* elem_n, double alpha,
+                        int half_power, double* u);
+
 /* ---------------- CurvedScalarWave (configuration 5) ----------------
  * Follows (paths relative to the SpECTRE tree):
  *   TimeDerivative       src/Evolution/Systems/CurvedScalarWave/TimeDerivative.cpp:19-69

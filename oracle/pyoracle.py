@@ -60,6 +60,7 @@ def lib():
             "orc_shell_geometry": [P, P, P], "orc_shell_connectivity": [P, P, P, P],
             "orc_shell_initial_data": [P, D, D, P], "orc_shell_rhs": [P, P, P, I],
             "orc_shell_evolve": [P, D, I, P, I],
+            "orc_exponential_filter": [I, D, I, P], "orc_filter_elements": [I64, P, D, I, P],
         }
         for name, args in sig.items():
             fn = getattr(L, name)
@@ -329,3 +330,17 @@ def shell_evolve(s, u, dt, steps, threads=0):
     if rc < 0:
         _check(rc)
     return u, rc == 0
+
+
+def exponential_filter(n, alpha, half_power):
+    F = np.zeros((n, n))
+    _check(lib().orc_exponential_filter(n, alpha, half_power, _p(F)))
+    return F
+
+
+def filter_elements(elem_n, u, alpha, half_power):
+    """Filtered copy of a state whose elements have extents elem_n."""
+    en = np.ascontiguousarray(elem_n, dtype=np.int32)
+    out = _c(u).copy()
+    _check(lib().orc_filter_elements(len(en), _p(en), alpha, half_power, _p(out)))
+    return out

@@ -79,6 +79,11 @@ struct DgswHandle_ {
   float* c_T32 = nullptr;
   float* c_F32 = nullptr;
   int32_t* c_X = nullptr;
+  // exponential filter after every substep (dg::Actions::Filter)
+  bool filter_on = false;
+  double filter_alpha = 0.0;
+  int filter_half_power = 0;
+  double* filt = nullptr;  // [kMaxN + 1][kMaxN * kMaxN], matrix of extent n at n
   // graphs of whole steps
   cudaGraphExec_t graph_one = nullptr;
   cudaGraphExec_t graph_many = nullptr;
@@ -328,6 +333,30 @@ int csw_init(DgswHandle h, const ShellGeometry& geo) {
   return DGSW_OK;
 }
 
+// The exponential filter on a state of this handle's layout (no-op when off).
+cudaError_t apply_filter(DgswHandle h, double* u) {
+  if (!h->filter_on) return cudaSuccess;
+  FilterLaunch F;
+  F.u = u;
+  if (h->general) {
+    F.offset = h->offset;
+    for (int n = kMinN; n <= kMaxN; ++n) {
+      if (h->class_count[n] == 0) continue;
+      F.n = n;
+      F.tasks = h->class_tasks[n];
+      F.n_tasks = h->class_count[n];
+      F.F = h->filt + (size_t)n * kMaxN * kMaxN;
+      cudaError_t e = launch_filter(F, h->stream);
+      if (e != cudaSuccess) return e;
+    }
+    return cudaSuccess;
+  }
+  F.n = h->dom.elem_n[0];
+  F.n_tasks = h->dom.n_elem;
+  F.F = h->filt + (size_t)F.n * kMaxN * kMaxN;
+  return launch_filter(F, h->stream);
+}
+
 // Reads and clears the device error word; DGSW_ERR_DEVICE_TIMEOUT when set.
 int check_device_error(DgswHandle h) {
   if (!h->dev_err) return DGSW_OK;
@@ -434,19 +463,27 @@ cudaError_t enqueue_step(DgswHandle h, double dt) {
     if (e != cudaSuccess) return e;
     return enqueue_mixed_stage(h, 2, dt, h->state, h->state);
   }
+  // each substep's result is filtered when the filter is on, as
+  // dg::Actions::Filter follows UpdateU in the reference's step actions
   if (h->curved) {
     cudaError_t e = csw_f64(h, h->state, nullptr, h->t1, 0.0, 1.0, dt);
-    if (e != cudaSuccess) return e;
-    e = csw_f64(h, h->t1, h->state, h->t2, 0.75, 0.25, 0.25 * dt);
-    if (e != cudaSuccess) return e;
-    return csw_f64(h, h->t2, h->state, h->state, 1.0 / 3.0, 2.0 / 3.0, (2.0 / 3.0) * dt);
+    if (e == cudaSuccess) e = apply_filter(h, h->t1);
+    if (e == cudaSuccess) e = csw_f64(h, h->t1, h->state, h->t2, 0.75, 0.25, 0.25 * dt);
+    if (e == cudaSuccess) e = apply_filter(h, h->t2);
+    if (e == cudaSuccess)
+      e = csw_f64(h, h->t2, h->state, h->state, 1.0 / 3.0, 2.0 / 3.0, (2.0 / 3.0) * dt);
+    if (e == cudaSuccess) e = apply_filter(h, h->state);
+    return e;
   }
   if (h->general) {
     cudaError_t e = general_f64(h, h->state, nullptr, h->t1, 1.0, 0.0, dt);
-    if (e != cudaSuccess) return e;
-    e = general_f64(h, h->t1, h->state, h->t2, 0.25, 0.75, 0.25 * dt);
-    if (e != cudaSuccess) return e;
-    return general_f64(h, h->t2, h->state, h->state, 2.0 / 3.0, 1.0 / 3.0, (2.0 / 3.0) * dt);
+    if (e == cudaSuccess) e = apply_filter(h, h->t1);
+    if (e == cudaSuccess) e = general_f64(h, h->t1, h->state, h->t2, 0.25, 0.75, 0.25 * dt);
+    if (e == cudaSuccess) e = apply_filter(h, h->t2);
+    if (e == cudaSuccess)
+      e = general_f64(h, h->t2, h->state, h->state, 2.0 / 3.0, 1.0 / 3.0, (2.0 / 3.0) * dt);
+    if (e == cudaSuccess) e = apply_filter(h, h->state);
+    return e;
   }
   StageLaunch L = base_launch(h);
   L.mode = kModeStageFirst;
@@ -455,6 +492,7 @@ cudaError_t enqueue_step(DgswHandle h, double dt) {
   L.unext = h->t1;
   L.coef = {0.0, 1.0, dt};
   cudaError_t e = launch_stage(h, L);
+  if (e == cudaSuccess) e = apply_filter(h, h->t1);
   if (e != cudaSuccess) return e;
   L.mode = kModeStage;
   L.ucur = h->t1;
@@ -462,12 +500,15 @@ cudaError_t enqueue_step(DgswHandle h, double dt) {
   L.unext = h->t2;
   L.coef = {0.75, 0.25, 0.25 * dt};
   e = launch_stage(h, L);
+  if (e == cudaSuccess) e = apply_filter(h, h->t2);
   if (e != cudaSuccess) return e;
   L.ucur = h->t2;
   L.u0 = h->state;
   L.unext = h->state;
   L.coef = {1.0 / 3.0, 2.0 / 3.0, (2.0 / 3.0) * dt};
-  return launch_stage(h, L);
+  e = launch_stage(h, L);
+  if (e == cudaSuccess) e = apply_filter(h, h->state);
+  return e;
 }
 
 AdjointLaunch base_adjoint(DgswHandle h) {
@@ -769,6 +810,7 @@ int dgsw_destroy(DgswHandle h) {
   if (h->c_T32) cudaFree(h->c_T32);
   if (h->c_F32) cudaFree(h->c_F32);
   if (h->c_X) cudaFree(h->c_X);
+  if (h->filt) cudaFree(h->filt);
   if (h->dev_err) cudaFree(h->dev_err);
   for (int n = 0; n <= kMaxN; ++n)
     if (h->class_tasks[n]) cudaFree(h->class_tasks[n]);
@@ -1008,6 +1050,7 @@ int dgsw_substep(DgswHandle h, int k, double dt) {
       else
         DGSW_CUDA(h, csw_f64(h, h->t1, h->u0s, h->state, 1.0 / 3.0, 2.0 / 3.0, (2.0 / 3.0) * dt));
     }
+    DGSW_CUDA(h, apply_filter(h, h->state));
     return DGSW_OK;
   }
   if (h->general) {
@@ -1021,6 +1064,7 @@ int dgsw_substep(DgswHandle h, int k, double dt) {
       else
         DGSW_CUDA(h, general_f64(h, h->t1, h->u0s, h->state, 2.0 / 3.0, 1.0 / 3.0, (2.0 / 3.0) * dt));
     }
+    DGSW_CUDA(h, apply_filter(h, h->state));
     return DGSW_OK;
   }
   StageLaunch L = base_launch(h);
@@ -1041,6 +1085,40 @@ int dgsw_substep(DgswHandle h, int k, double dt) {
                     : StageCoef{1.0 / 3.0, 2.0 / 3.0, (2.0 / 3.0) * dt};
   }
   DGSW_CUDA(h, launch_stage(h, L));
+  DGSW_CUDA(h, apply_filter(h, h->state));
+  return DGSW_OK;
+}
+
+int dgsw_set_exponential_filter(DgswHandle h, double alpha, int half_power, int enable) {
+  if (!h) return fail(nullptr, DGSW_ERR_ARGUMENT, "null handle");
+  if (!enable) {
+    if (h->filter_on) destroy_graphs(h);
+    h->filter_on = false;
+    return DGSW_OK;
+  }
+  if (!std::isfinite(alpha) || alpha < 0.0 || half_power < 0 || half_power > 64)
+    return fail(h, DGSW_ERR_ARGUMENT, "need a finite alpha >= 0 and half_power in [0, 64]");
+  if (mixed(h))
+    return fail(h, DGSW_ERR_UNSUPPORTED,
+                "the filter acts on FP64 substep states; use FP64 precision");
+  if (int rc = select_device(h)) return rc;
+  std::vector<double> mats((size_t)(kMaxN + 1) * kMaxN * kMaxN, 0.0);
+  for (int n = kMinN; n <= kMaxN; ++n)
+    lgl_exponential_filter(n, alpha, half_power, &mats[(size_t)n * kMaxN * kMaxN]);
+  DGSW_CUDA(h, cudaStreamSynchronize(h->stream));
+  if (!h->filt) DGSW_CUDA(h, cudaMalloc(&h->filt, mats.size() * sizeof(double)));
+  DGSW_CUDA(h, cudaMemcpy(h->filt, mats.data(), mats.size() * sizeof(double),
+                          cudaMemcpyHostToDevice));
+  destroy_graphs(h);
+  h->filter_on = true;
+  h->filter_alpha = alpha;
+  h->filter_half_power = half_power;
+  return DGSW_OK;
+}
+
+int dgsw_exponential_filter_matrix(int n, double alpha, int half_power, double* F) {
+  if (!lgl_exponential_filter(n, alpha, half_power, F))
+    return fail(nullptr, DGSW_ERR_ARGUMENT, "need 2 <= n <= 20, finite alpha, half_power >= 0");
   return DGSW_OK;
 }
 
@@ -1102,6 +1180,7 @@ int dgsw_set_samples(DgswHandle h, int n_samples, const double* xyz) {
   if (h->c_T32) cudaFree(h->c_T32);
   if (h->c_F32) cudaFree(h->c_F32);
   if (h->c_X) cudaFree(h->c_X);
+  if (h->filt) cudaFree(h->filt);
   if (h->samp_w) cudaFree(h->samp_w);
   h->samp_off = nullptr;
   h->samp_w = nullptr;

@@ -176,6 +176,32 @@ static bool eo_from_matrix(int n, const double* D, EoTable* t) {
   return true;
 }
 
+bool lgl_exponential_filter(int n, double alpha, int half_power, double* F) {
+  if (n < 2 || n > 20 || !F || half_power < 0 || !std::isfinite(alpha)) return false;
+  double x[20], w[20];
+  lgl_nodes_weights(n, x, w);
+  // nodal -> modal through the discrete Legendre norms of the LGL rule:
+  // V^T W V = diag(g) exactly (P_{n-1}^2 is the only product above the rule's
+  // degree, and it sits on the diagonal), so V^-1 = diag(1/g) V^T W
+  double V[20 * 20], g[20], d[20];
+  for (int i = 0; i < n; ++i)
+    for (int k = 0; k < n; ++k) V[i * n + k] = legendre(k, x[i]);
+  const double order = n - 1.0;
+  for (int k = 0; k < n; ++k) {
+    double s = 0.0;
+    for (int i = 0; i < n; ++i) s += w[i] * V[i * n + k] * V[i * n + k];
+    g[k] = s;
+    d[k] = std::exp(-alpha * std::pow(k / order, 2.0 * half_power));
+  }
+  for (int i = 0; i < n; ++i)
+    for (int j = 0; j < n; ++j) {
+      double s = 0.0;
+      for (int k = 0; k < n; ++k) s += V[i * n + k] * (d[k] / g[k]) * V[j * n + k];
+      F[i * n + j] = s * w[j];
+    }
+  return true;
+}
+
 bool lgl_eo_table(int n, EoTable* t) {
   if (n < kMinN || n > kMaxN || !t) return false;
   double D[kMaxN * kMaxN];

@@ -26,6 +26,10 @@ bool lgl_interp_matrix(int n, int m, const double* targets, double* M);
 // Face -> mortar (nm x ne, interpolation) and mortar -> face (ne x nm,
 // Legendre modal truncation), Projection.cpp:56-375, ChildSize::Full.
 bool lgl_mortar_projections(int ne, int nm, double* to_mortar, double* from_mortar);
+// Exponential filter V diag(exp(-alpha (k/(n-1))^(2 half_power))) V^-1 on n
+// LGL points (Spectral::filtering::exponential_filter, Filtering.cpp:18-31),
+// row-major.
+bool lgl_exponential_filter(int n, double alpha, int half_power, double* F);
 // Even/odd split tables of the differentiation matrix (see EoTable), and of
 // its transpose (also centro-antisymmetric), used by the adjoint.
 bool lgl_eo_table(int n, EoTable* t);

@@ -170,6 +170,19 @@ cudaError_t launch_csw_setup(const CswSetup& S, cudaStream_t s);
 cudaError_t launch_csw_initial(const double* xyz, int n, int64_t n_elem, double A, double r0,
                                double w, double* u, cudaStream_t s);
 
+// Exponential filter of every element's variables, in place (filter.cu).
+// tasks / offset null: elements 0..n_tasks-1 of extent n, packed; else the
+// listed elements at their value offsets.  F: n x n row-major, device.
+struct FilterLaunch {
+  int n = 0;
+  int64_t n_tasks = 0;
+  const int32_t* tasks = nullptr;
+  const int64_t* offset = nullptr;
+  double* u = nullptr;
+  const double* F = nullptr;
+};
+cudaError_t launch_filter(const FilterLaunch& L, cudaStream_t s);
+
 // UpwindPenalty pointwise kernels (face_kernels.cu).
 cudaError_t launch_package_data(int64_t npts, const double* psi, const double* pi,
                                 const double* phi, const double* gamma2,

@@ -97,6 +97,8 @@ _SIGNATURES = {
     "dgsw_package_data_device": (_I, [_I64, _P, _P, _P, _P, _P, _P, _P, _P]),
     "dgsw_boundary_terms_device": (_I, [_I64, _P, _P, _P, _P]),
     "dgsw_step": (_I, [_P, _I, _D]),
+    "dgsw_set_exponential_filter": (_I, [_P, _D, _I, _I]),
+    "dgsw_exponential_filter_matrix": (_I, [_I, _D, _I, _P]),
     "dgsw_substep": (_I, [_P, _I, _D]),
     "dgsw_lgl_points_weights": (_I, [_I, _P, _P]),
     "dgsw_differentiation_matrix": (_I, [_I, _P]),
@@ -183,6 +185,13 @@ def differentiation_matrix(n: int) -> np.ndarray:
     D = np.zeros((n, n))
     _check(lib().dgsw_differentiation_matrix(n, _ptr(D)))
     return D
+
+
+def exponential_filter_matrix(n: int, alpha: float, half_power: int) -> np.ndarray:
+    """Spectral::filtering::exponential_filter on n LGL points (row-major)."""
+    F = np.zeros((n, n))
+    _check(lib().dgsw_exponential_filter_matrix(n, float(alpha), int(half_power), _ptr(F)))
+    return F
 
 
 def mortar_projections(n_face: int, n_mortar: int):
@@ -474,6 +483,11 @@ class DgEvolution:
     def substep(self, k: int, dt: float):
         _check(lib().dgsw_substep(self._h, int(k), float(dt)), self._h)
         self.synchronize()
+
+    def set_exponential_filter(self, alpha: float, half_power: int, enable: bool = True):
+        """Filters::Exponential after every substep (dg::Actions::Filter)."""
+        _check(lib().dgsw_set_exponential_filter(self._h, float(alpha), int(half_power),
+                                                 1 if enable else 0), self._h)
 
     # discrete adjoint -----------------------------------------------------
     def adjoint_rhs(self, lam_dev):

@@ -1,0 +1,130 @@
+"""Exponential filter (Filters::Exponential applied by dg::Actions::Filter
+after every substep).
+
+CPU: the oracle's 1D filter matrix against the reference's known answer
+(Test_Filtering.cpp: each Legendre mode k is damped by
+exp(-alpha (k/(N-1))^(2 half_power)), 2e-12), and the product's host matrix
+against the oracle's (1e-13).  GPU: filtered SSP-RK3 steps of the flat,
+the mixed-extent and the curved paths against the oracle stepped substep by
+substep with the filter (<= 1e-11 relative per variable).
+"""
+import numpy as np
+import pytest
+
+from spectre_gb300 import dgsw
+from spectre_gb300.dgsw import Brick, CurvedDgEvolution, DgEvolution, Shell
+
+ALPHA, HALF_POWER = 36.0, 8
+
+
+@pytest.mark.parametrize("alpha", [10.0, 20.0, 30.0, 40.0])
+@pytest.mark.parametrize("half_power", [2, 4, 8, 16])
+def test_oracle_filter_damps_legendre_modes(oracle, alpha, half_power):
+    for n in range(2, 21):
+        F = oracle.exponential_filter(n, alpha, half_power)
+        V = oracle.vandermonde(n)
+        Vi = oracle.inv_vandermonde(n)
+        for modal in (np.full(n, float(n)), np.arange(1.0, n + 1.0)):
+            got = Vi @ (F @ (V @ modal))
+            want = modal * np.exp(-alpha * (np.arange(n) / (n - 1.0)) ** (2 * half_power))
+            assert np.all(np.abs(got - want) <= 2e-12 * (1.0 + np.abs(want))), n
+
+
+@pytest.mark.parametrize("n", range(2, 13))
+def test_product_filter_matrix_matches_oracle(dgsw_lib, oracle, n):
+    for alpha, hp in ((12.0, 32), (36.0, 8), (0.0, 4)):
+        np.testing.assert_allclose(dgsw.exponential_filter_matrix(n, alpha, hp),
+                                   oracle.exponential_filter(n, alpha, hp), rtol=0, atol=1e-13)
+
+
+def _rel(a, b, elem_n):
+    a = np.asarray(a).ravel()
+    b = np.asarray(b).ravel()
+    num = np.zeros(5)
+    den = np.zeros(5)
+    off = 0
+    for n in elem_n:
+        npt = int(n) ** 3
+        for v in range(5):
+            sl = slice(off + v * npt, off + (v + 1) * npt)
+            num[v] = max(num[v], np.abs(a[sl] - b[sl]).max())
+            den[v] = max(den[v], np.abs(b[sl]).max())
+        off += 5 * npt
+    return float(max(num[v] / den[v] if den[v] > 0 else num[v] for v in range(5)))
+
+
+def _oracle_filtered(oracle, rhs, u, dt, steps, elem_n):
+    u0 = np.array(u, dtype=np.float64).ravel()
+    for _ in range(steps):
+        cur = u0
+        for k in range(3):
+            cur = oracle.rk3_substep(k, dt, u0, cur, rhs(cur))
+            cur = oracle.filter_elements(elem_n, cur, ALPHA, HALF_POWER)
+        u0 = cur
+    return u0
+
+
+@pytest.mark.gpu
+def test_flat_filtered_steps_match_oracle(oracle):
+    bricks = [Brick((3, 2, 4))]
+    n, dt = 7, 2e-3
+    rng = np.random.default_rng(3)
+    en = oracle.elem_points(bricks, n)
+    u = rng.uniform(-1, 1, int(oracle.offsets(en)[-1]))
+    ref = _oracle_filtered(oracle, lambda x: oracle.rhs(bricks, n, x), u, dt, 4, en)
+    with DgEvolution(bricks, n) as ev:
+        ev.set_exponential_filter(ALPHA, HALF_POWER)
+        ev.set_state(u)
+        ev.step(4, dt)
+        assert _rel(ev.get_state(), ref, en) <= 1e-11
+        # one substep at a time gives the same states
+        ev.set_state(u)
+        for _ in range(4):
+            for k in range(3):
+                ev.substep(k, dt)
+        assert _rel(ev.get_state(), ref, en) <= 1e-11
+        # switched off again: plain steps
+        ev.set_exponential_filter(ALPHA, HALF_POWER, enable=False)
+        ev.set_state(u)
+        ev.step(1, dt)
+        plain = oracle.evolve(bricks, n, u, dt, 1)
+        assert _rel(ev.get_state(), plain, en) <= 1e-12
+
+
+@pytest.mark.gpu
+def test_mixed_extent_filtered_steps_match_oracle(oracle):
+    bricks = [Brick((2, 3, 2))]
+    rng = np.random.default_rng(5)
+    pts = rng.integers(4, 11, size=12).astype(np.int32)
+    dt = 1e-3
+    en = oracle.elem_points(bricks, pts)
+    u = rng.uniform(-1, 1, int(oracle.offsets(en)[-1]))
+    ref = _oracle_filtered(oracle, lambda x: oracle.rhs(bricks, pts, x), u, dt, 3, en)
+    with DgEvolution(bricks, pts) as ev:
+        ev.set_exponential_filter(ALPHA, HALF_POWER)
+        ev.set_state(u)
+        ev.step(3, dt)
+        assert _rel(ev.get_state(), ref, en) <= 1e-11
+
+
+@pytest.mark.gpu
+def test_curved_filtered_steps_match_oracle(oracle):
+    n, dt = 6, 1e-2
+    s = oracle.shell(1.9, 20.0, 1, 1, n, 1.0, 0.0, 1.0)
+    u = oracle.shell_initial_data(s, 8.0, 1.0)
+    E = u.shape[0]
+    en = np.full(E, n, dtype=np.int32)
+    rhs = lambda x: oracle.shell_rhs(s, x.reshape(u.shape))[0].ravel()  # noqa: E731
+    ref = _oracle_filtered(oracle, rhs, u, dt, 5, en)
+    with CurvedDgEvolution(Shell(1.9, 20.0, 1, 1), n, gamma2=1.0) as ev:
+        ev.set_exponential_filter(ALPHA, HALF_POWER)
+        ev.set_state(u.ravel())
+        ev.step(5, dt)
+        assert _rel(ev.get_state(), ref, en) <= 1e-11
+
+
+@pytest.mark.gpu
+def test_filter_refused_for_mixed_precision():
+    with DgEvolution([Brick((2, 2, 2))], 6, precision=dgsw.PRECISION_MIXED) as ev:
+        with pytest.raises(dgsw.DgswError, match="FP64"):
+            ev.set_exponential_filter(ALPHA, HALF_POWER)

@@ -127,3 +127,17 @@ def test_curved_mixed_evolution_error(oracle):
     assert err < 1e-6
     ev64.close()
     evm.close()
+
+
+def test_curved_mixed_n12(oracle):
+    # N = 12 on the 768-element shell (the largest extent compiled); two
+    # steps against FP64
+    n = 12
+    ev64, _ = make(oracle, 2, 3, n)
+    evm, _ = make(oracle, 2, 3, n, precision=dgsw.PRECISION_MIXED)
+    for ev in (ev64, evm):
+        ev.set_gaussian_shell(1.0, 8.0, 1.0)
+        ev.step(2, 1e-3)
+    assert rel_l2(evm.get_state(), ev64.get_state()) < 1e-7
+    ev64.close()
+    evm.close()

@@ -128,6 +128,27 @@ def dist_env():
     return ws, rank, local
 
 
+def max_over_ranks(x, ws):
+    """The largest of each rank's x (seconds or ms): the job's time is set by
+    the slowest replica.  All-reduce on the process group's own device type
+    (CUDA tensors under NCCL, CPU tensors under gloo)."""
+    if ws <= 1:
+        return float(x)
+    import torch
+    import torch.distributed as dist
+    device = "cuda" if dist.get_backend() == "nccl" else "cpu"
+    t = torch.tensor([float(x)], dtype=torch.float64, device=device)
+    dist.all_reduce(t, op=dist.ReduceOp.MAX)
+    return float(t.item())
+
+
+def replica_throughput(points_per_rank, rhs_per_step, steps, seconds_per_rank, ws):
+    """Whole-job grid-point RHS/s of ws independent replicas (weak scaling):
+    all ranks' point-RHS over the slowest rank's time."""
+    slowest = max_over_ranks(seconds_per_rank, ws)
+    return points_per_rank * rhs_per_step * steps * ws / slowest, slowest
+
+
 def cpu_threads():
     try:
         return len(os.sched_getaffinity(0))
@@ -219,9 +240,7 @@ def time_path(args, precision, dev, rank, ws, sample_clocks):
     torch.cuda.synchronize()
     ms = e0.elapsed_time(e1)
     if ws > 1:
-        t = torch.tensor([ms], device="cuda")
-        torch.distributed.all_reduce(t, op=torch.distributed.ReduceOp.MAX)
-        ms = float(t.item())
+        ms = max_over_ranks(ms, ws)
         torch.distributed.barrier()
     clocks = sampler.stop() if sampler else None
     state = ev.get_state()
@@ -429,11 +448,8 @@ def run_ours(args):
         ev.step(1, DT, sync=False)
         ev.get_state(hnp)
     el = time.perf_counter() - t0
-    if ws > 1:
-        t = torch.tensor([el], device="cuda")
-        torch.distributed.all_reduce(t, op=torch.distributed.ReduceOp.MAX)
-        el = float(t.item())
-    e2e = {"value": points * 3 * k2 * ws / el, "unit": UNIT,
+    e2e_value, el = replica_throughput(points, 3, k2, el, ws)
+    e2e = {"value": e2e_value, "unit": UNIT,
            "h2d_bytes_per_step": ev.state_size * 8, "d2h_bytes_per_step": ev.state_size * 8,
            "steps": k2}
     ev.close()

@@ -186,6 +186,22 @@ int dgsw_boundary_terms_device(int64_t npts, const double* packaged_int,
 int dgsw_step(DgswHandle h, int n_steps, double dt);
 int dgsw_substep(DgswHandle h, int k, double dt);
 
+/* ---- observation ------------------------------------------------------------
+ * Events::ObserveNorms (ParallelAlgorithms/Events/ObserveNorms.cpp:33-105,
+ * ObserveNorms.hpp:47-80,145-171) of Psi, Pi, Phi_x, Phi_y, Phi_z, each
+ * "Individual", over every element of the handle, on the device in FP64:
+ * out[5*v + m], m = 0 Max, 1 Min, 2 L2Norm = sqrt(sum u^2 / points),
+ * 3 L2IntegralNorm = sqrt(int u^2 dV / V), 4 VolumeIntegral = int u dV;
+ * out[25] = points, out[26] = V (definite_integral on the LGL mesh times
+ * det(Jacobian)).  dev_u: device state (NULL: the handle's state);
+ * dev_subtract (may be NULL) is subtracted first.
+ * dgsw_observe_plane_wave_errors: the same norms of the state minus
+ * PlaneWave(k, t) (PointwiseFunctions/AnalyticSolutions/WaveEquation/
+ * PlaneWave.cpp:56-80), the Error(...) norms of ObserveNorms; flat system. */
+int dgsw_observe_norms(DgswHandle h, const double* dev_u, const double* dev_subtract,
+                       double* out);
+int dgsw_observe_plane_wave_errors(DgswHandle h, const double* k, double t, double* out);
+
 /* ---- exponential filter ----------------------------------------------------
  * Filters::Exponential (NumericalAlgorithms/LinearOperators/
  * ExponentialFilter.cpp:23-80) applied by dg::Actions::Filter

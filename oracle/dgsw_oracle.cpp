@@ -1104,6 +1104,102 @@ int orc_filter_elements(int64_t n_elem, const int32_t* elem_n, double alpha, int
 
 }  // extern "C"
 
+// ======================= ObserveNorms =======================
+extern "C" {
+
+// norms over elements of one extent n, det_jac: one value per point
+int orc_shell_observe_norms_impl(int64_t n_elem, int n, const double* det_jac, const double* u,
+                                 const double* subtract, double* out) {
+  if (n_elem < 0 || n < 2 || n > kMaxN || !det_jac || !u || !out) return -1;
+  const Spectral1d& sp = spectral(n);
+  const int64_t np = (int64_t)n * n * n;
+  double mx[5], mn[5], sq[5], isq[5], iv[5], vol = 0.0;
+  for (int v = 0; v < 5; ++v) {
+    mx[v] = -std::numeric_limits<double>::infinity();
+    mn[v] = std::numeric_limits<double>::infinity();
+    sq[v] = isq[v] = iv[v] = 0.0;
+  }
+  for (int64_t e = 0; e < n_elem; ++e)
+    for (int k = 0; k < n; ++k)
+      for (int j = 0; j < n; ++j)
+        for (int i = 0; i < n; ++i) {
+          const int64_t p = i + n * (j + (int64_t)n * k);
+          const double w = sp.w[i] * sp.w[j] * sp.w[k] * det_jac[e * np + p];
+          vol += w;
+          for (int v = 0; v < 5; ++v) {
+            double x = u[e * 5 * np + v * np + p];
+            if (subtract) x -= subtract[e * 5 * np + v * np + p];
+            mx[v] = std::max(mx[v], x);
+            mn[v] = std::min(mn[v], x);
+            sq[v] += x * x;
+            isq[v] += w * x * x;
+            iv[v] += w * x;
+          }
+        }
+  const double pts = (double)(n_elem * np);
+  for (int v = 0; v < 5; ++v) {
+    out[5 * v + 0] = mx[v];
+    out[5 * v + 1] = mn[v];
+    out[5 * v + 2] = std::sqrt(sq[v] / pts);
+    out[5 * v + 3] = std::sqrt(isq[v] / vol);
+    out[5 * v + 4] = iv[v];
+  }
+  out[25] = pts;
+  out[26] = vol;
+  return 0;
+}
+
+int orc_observe_norms(int n_inst, const OrcBrick* br, const int32_t* elem_n, const double* u,
+                      const double* subtract, double* out) {
+  if (n_inst < 1 || !br || !elem_n || !u || !out) return -1;
+  Mesh m;
+  build_mesh(&m, n_inst, br, elem_n);
+  double mx[5], mn[5], sq[5], isq[5], iv[5], vol = 0.0, pts = 0.0;
+  for (int v = 0; v < 5; ++v) {
+    mx[v] = -std::numeric_limits<double>::infinity();
+    mn[v] = std::numeric_limits<double>::infinity();
+    sq[v] = isq[v] = iv[v] = 0.0;
+  }
+  int64_t pos = 0;
+  for (int64_t e = 0; e < m.n_elem; ++e) {
+    const int n = elem_n[e];
+    const int64_t np = (int64_t)n * n * n;
+    const Spectral1d& sp = spectral(n);
+    const ElemGeom& g = m.geom[e];
+    const double dj = 0.125 * g.h[0] * g.h[1] * g.h[2];
+    for (int k = 0; k < n; ++k)
+      for (int j = 0; j < n; ++j)
+        for (int i = 0; i < n; ++i) {
+          const int64_t p = i + n * (j + (int64_t)n * k);
+          const double w = sp.w[i] * sp.w[j] * sp.w[k] * dj;
+          vol += w;
+          for (int v = 0; v < 5; ++v) {
+            double x = u[pos + v * np + p];
+            if (subtract) x -= subtract[pos + v * np + p];
+            mx[v] = std::max(mx[v], x);
+            mn[v] = std::min(mn[v], x);
+            sq[v] += x * x;
+            isq[v] += w * x * x;
+            iv[v] += w * x;
+          }
+        }
+    pts += (double)np;
+    pos += 5 * np;
+  }
+  for (int v = 0; v < 5; ++v) {
+    out[5 * v + 0] = mx[v];
+    out[5 * v + 1] = mn[v];
+    out[5 * v + 2] = std::sqrt(sq[v] / pts);
+    out[5 * v + 3] = std::sqrt(isq[v] / vol);
+    out[5 * v + 4] = iv[v];
+  }
+  out[25] = pts;
+  out[26] = vol;
+  return 0;
+}
+
+}  // extern "C"
+
 // ======================= spherical shell (configuration 5) =======================
 namespace {
 
@@ -1532,6 +1628,24 @@ int orc_shell_rhs(const OrcShell* s, const double* u, double* dudt, int n_thread
   ShellMesh m;
   build_shell(*s, &m);
   return shell_rhs_impl(m, u, dudt);
+}
+
+int orc_shell_observe_norms(const OrcShell* s, const double* u, double* out) {
+  if (check_shell(s) || !u || !out) return -1;
+  ShellMesh m;
+  build_shell(*s, &m);
+  const int64_t np = (int64_t)s->n * s->n * s->n;
+  std::vector<double> dj(m.E * np);
+  for (int64_t e = 0; e < m.E; ++e)
+    for (int64_t p = 0; p < np; ++p) {
+      double inv[9];
+      for (int c = 0; c < 9; ++c) inv[c] = m.ij[e * 9 * np + c * np + p];
+      const double det = inv[0] * (inv[4] * inv[8] - inv[5] * inv[7]) -
+                         inv[1] * (inv[3] * inv[8] - inv[5] * inv[6]) +
+                         inv[2] * (inv[3] * inv[7] - inv[4] * inv[6]);
+      dj[e * np + p] = 1.0 / det;
+    }
+  return orc_shell_observe_norms_impl(m.E, s->n, dj.data(), u, nullptr, out);
 }
 
 int orc_shell_evolve(const OrcShell* s, double dt, int n_steps, double* u, int n_threads) {

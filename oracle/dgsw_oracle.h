@@ -123,6 +123,20 @@ int orc_exponential_filter(int n, double alpha, int half_power, double* F);
 int orc_filter_elements(int64_t n_elem, const int32_t* elem_n, double alpha,
                         int half_power, double* u);
 
+/* ---------------- ObserveNorms ----------------
+ * Events::ObserveNorms (ParallelAlgorithms/Events/ObserveNorms.cpp:33-105,
+ * ObserveNorms.hpp:47-80,145-171) of the five evolved components, each
+ * "Individual", reduced over all elements.  out[5*v + m] for variable v and
+ * m = Max, Min, L2Norm = sqrt(sum u^2 / points), L2IntegralNorm =
+ * sqrt(int u^2 dV / V), VolumeIntegral = int u dV; out[25] = points,
+ * out[26] = V.  The integrals are definite_integral on the LGL mesh times
+ * det(Jacobian).  subtract (may be NULL): a state-sized array subtracted
+ * first (errors against an analytic solution). */
+int orc_observe_norms(int n_inst, const OrcBrick* bricks, const int32_t* elem_n,
+                      const double* u, const double* subtract, double* out);
+int orc_shell_observe_norms_impl(int64_t n_elem, int n, const double* det_jac,
+                                 const double* u, const double* subtract, double* out);
+
 /* ---------------- CurvedScalarWave (configuration 5) ----------------
  * Follows (paths relative to the SpECTRE tree):
  *   TimeDerivative       src/Evolution/Systems/CurvedScalarWave/TimeDerivative.cpp:19-69
@@ -192,6 +206,8 @@ int orc_shell_initial_data(const OrcShell* s, double r0, double w, double* u);
  * sphere (returns 1 if a char speed is incoming) and CPSR at the outer one */
 int orc_shell_rhs(const OrcShell* s, const double* u, double* dudt, int n_threads);
 int orc_shell_evolve(const OrcShell* s, double dt, int n_steps, double* u, int n_threads);
+/* ObserveNorms (as orc_observe_norms) of a shell state */
+int orc_shell_observe_norms(const OrcShell* s, const double* u, double* out);
 
 #ifdef __cplusplus
 }

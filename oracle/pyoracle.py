@@ -61,6 +61,7 @@ def lib():
             "orc_shell_initial_data": [P, D, D, P], "orc_shell_rhs": [P, P, P, I],
             "orc_shell_evolve": [P, D, I, P, I],
             "orc_exponential_filter": [I, D, I, P], "orc_filter_elements": [I64, P, D, I, P],
+            "orc_observe_norms": [I, P, P, P, P, P], "orc_shell_observe_norms": [P, P, P],
         }
         for name, args in sig.items():
             fn = getattr(L, name)
@@ -343,4 +344,25 @@ def filter_elements(elem_n, u, alpha, half_power):
     en = np.ascontiguousarray(elem_n, dtype=np.int32)
     out = _c(u).copy()
     _check(lib().orc_filter_elements(len(en), _p(en), alpha, half_power, _p(out)))
+    return out
+
+
+NORM_NAMES = ("Max", "Min", "L2Norm", "L2IntegralNorm", "VolumeIntegral")
+
+
+def observe_norms(bricks, points, u, subtract=None):
+    """27 values: [5 * var + norm] for NORM_NAMES, then points, volume."""
+    en = elem_points(bricks, points)
+    arr = _bricks(bricks)
+    out = np.zeros(27)
+    u = _c(u)
+    sub = None if subtract is None else _c(subtract)
+    _check(lib().orc_observe_norms(len(bricks), ctypes.addressof(arr), _p(en), _p(u), _p(sub),
+                                   _p(out)))
+    return out
+
+
+def shell_observe_norms(s, u):
+    out = np.zeros(27)
+    _check(lib().orc_shell_observe_norms(ctypes.byref(s), _p(_c(u)), _p(out)))
     return out

@@ -79,6 +79,9 @@ struct DgswHandle_ {
   float* c_T32 = nullptr;
   float* c_F32 = nullptr;
   int32_t* c_X = nullptr;
+  // ObserveNorms scratch
+  double* lgl_w = nullptr;
+  double* norm_partial = nullptr;
   // exponential filter after every substep (dg::Actions::Filter)
   bool filter_on = false;
   double filter_alpha = 0.0;
@@ -811,6 +814,8 @@ int dgsw_destroy(DgswHandle h) {
   if (h->c_F32) cudaFree(h->c_F32);
   if (h->c_X) cudaFree(h->c_X);
   if (h->filt) cudaFree(h->filt);
+  if (h->lgl_w) cudaFree(h->lgl_w);
+  if (h->norm_partial) cudaFree(h->norm_partial);
   if (h->dev_err) cudaFree(h->dev_err);
   for (int n = 0; n <= kMaxN; ++n)
     if (h->class_tasks[n]) cudaFree(h->class_tasks[n]);
@@ -1089,6 +1094,89 @@ int dgsw_substep(DgswHandle h, int k, double dt) {
   return DGSW_OK;
 }
 
+// ObserveNorms of u (or u - subtract) into out[27] (see dgsw.h).
+static int observe_norms(DgswHandle h, const double* dev_u, const double* dev_sub, double* out) {
+  const int64_t E = h->dom.n_elem;
+  if (!h->norm_partial) {
+    std::vector<double> w((kMaxN + 1) * kMaxN, 0.0);
+    for (int n = kMinN; n <= kMaxN; ++n) {
+      double x[kMaxN];
+      lgl_nodes_weights(n, x, &w[n * kMaxN]);
+    }
+    DGSW_CUDA(h, upload(&h->lgl_w, w));
+    DGSW_CUDA(h, cudaMalloc(&h->norm_partial, ((size_t)E * 26 + 32) * sizeof(double)));
+  }
+  NormsLaunch L;
+  L.n_elem = E;
+  L.uniform_n = h->dom.uniform ? h->dom.elem_n[0] : 0;
+  L.elem_n = h->elem_n;
+  L.offset = h->dom.uniform ? nullptr : h->offset;
+  if (h->curved)
+    L.ij = h->c_ij;
+  else
+    L.width = h->width;
+  L.lgl_w = h->lgl_w;
+  L.u = dev_u ? dev_u : h->state;
+  L.subtract = dev_sub;
+  L.partial = h->norm_partial;
+  L.result = h->norm_partial + (size_t)E * 26;
+  DGSW_CUDA(h, launch_norms(L, h->stream));
+  double r[26];
+  DGSW_CUDA(h, cudaMemcpyAsync(r, L.result, sizeof(r), cudaMemcpyDeviceToHost, h->stream));
+  DGSW_CUDA(h, cudaStreamSynchronize(h->stream));
+  const double pts = (double)h->dom.n_points, vol = r[25];
+  for (int v = 0; v < 5; ++v) {
+    out[5 * v + 0] = r[5 * v + 0];
+    out[5 * v + 1] = r[5 * v + 1];
+    out[5 * v + 2] = std::sqrt(r[5 * v + 2] / pts);
+    out[5 * v + 3] = std::sqrt(r[5 * v + 3] / vol);
+    out[5 * v + 4] = r[5 * v + 4];
+  }
+  out[25] = pts;
+  out[26] = vol;
+  return DGSW_OK;
+}
+
+int dgsw_observe_norms(DgswHandle h, const double* dev_u, const double* dev_subtract,
+                       double* out) {
+  if (!h || !out) return fail(h, DGSW_ERR_ARGUMENT, "null argument");
+  if (int rc = select_device(h)) return rc;
+  return observe_norms(h, dev_u, dev_subtract, out);
+}
+
+int dgsw_observe_plane_wave_errors(DgswHandle h, const double* k, double t, double* out) {
+  if (!h || !k || !out) return fail(h, DGSW_ERR_ARGUMENT, "null argument");
+  if (h->curved) return fail(h, DGSW_ERR_UNSUPPORTED, "the plane wave is a flat-space solution");
+  for (int i = 0; i < 3; ++i)
+    if (!std::isfinite(k[i])) return fail(h, DGSW_ERR_ARGUMENT, "non-finite wave vector");
+  if (!std::isfinite(t)) return fail(h, DGSW_ERR_ARGUMENT, "non-finite time");
+  if (int rc = select_device(h)) return rc;
+  // the analytic solution at t goes to the stage buffer t1 (free between steps)
+  if (3 > h->params_cap) {
+    DGSW_CUDA(h, cudaStreamSynchronize(h->stream));
+    if (h->params) cudaFree(h->params);
+    h->params = nullptr;
+    DGSW_CUDA(h, cudaMalloc(&h->params, 3 * sizeof(double)));
+    h->params_cap = 3;
+  }
+  DGSW_CUDA(h, cudaMemcpyAsync(h->params, k, 3 * sizeof(double), cudaMemcpyHostToDevice,
+                               h->stream));
+  InitLaunch L;
+  L.kind = 0;
+  L.n_elem = h->dom.n_elem;
+  L.elem_n = h->elem_n;
+  L.offset = h->offset;
+  L.instance = h->instance;
+  L.lower = h->lower;
+  L.width = h->width;
+  L.params = h->params;
+  L.lgl_x = h->lgl_x;
+  L.t = t;
+  L.u = h->t1;
+  DGSW_CUDA(h, launch_initial_data(L, h->stream));
+  return observe_norms(h, h->state, h->t1, out);
+}
+
 int dgsw_set_exponential_filter(DgswHandle h, double alpha, int half_power, int enable) {
   if (!h) return fail(nullptr, DGSW_ERR_ARGUMENT, "null handle");
   if (!enable) {
@@ -1181,6 +1269,8 @@ int dgsw_set_samples(DgswHandle h, int n_samples, const double* xyz) {
   if (h->c_F32) cudaFree(h->c_F32);
   if (h->c_X) cudaFree(h->c_X);
   if (h->filt) cudaFree(h->filt);
+  if (h->lgl_w) cudaFree(h->lgl_w);
+  if (h->norm_partial) cudaFree(h->norm_partial);
   if (h->samp_w) cudaFree(h->samp_w);
   h->samp_off = nullptr;
   h->samp_w = nullptr;

@@ -183,6 +183,24 @@ struct FilterLaunch {
 };
 cudaError_t launch_filter(const FilterLaunch& L, cudaStream_t s);
 
+// ObserveNorms partial sums per element and their fixed-order total
+// (norms.cu).  Flat elements: width (3 per element) gives det J; curved:
+// ij (9 x N^3 per element) gives det J = 1 / det(inverse Jacobian).
+struct NormsLaunch {
+  int64_t n_elem = 0;
+  int uniform_n = 0;                // extent of every element, or 0: elem_n
+  const int32_t* elem_n = nullptr;
+  const int64_t* offset = nullptr;  // null: uniform packing
+  const double* width = nullptr;
+  const double* ij = nullptr;
+  const double* lgl_w = nullptr;    // [kMaxN + 1][kMaxN] LGL weights
+  const double* u = nullptr;
+  const double* subtract = nullptr;
+  double* partial = nullptr;        // n_elem x 26
+  double* result = nullptr;         // 26
+};
+cudaError_t launch_norms(const NormsLaunch& L, cudaStream_t s);
+
 // UpwindPenalty pointwise kernels (face_kernels.cu).
 cudaError_t launch_package_data(int64_t npts, const double* psi, const double* pi,
                                 const double* phi, const double* gamma2,

@@ -98,6 +98,8 @@ _SIGNATURES = {
     "dgsw_boundary_terms_device": (_I, [_I64, _P, _P, _P, _P]),
     "dgsw_step": (_I, [_P, _I, _D]),
     "dgsw_set_exponential_filter": (_I, [_P, _D, _I, _I]),
+    "dgsw_observe_norms": (_I, [_P, _P, _P, _P]),
+    "dgsw_observe_plane_wave_errors": (_I, [_P, _P, _D, _P]),
     "dgsw_exponential_filter_matrix": (_I, [_I, _D, _I, _P]),
     "dgsw_substep": (_I, [_P, _I, _D]),
     "dgsw_lgl_points_weights": (_I, [_I, _P, _P]),
@@ -483,6 +485,37 @@ class DgEvolution:
     def substep(self, k: int, dt: float):
         _check(lib().dgsw_substep(self._h, int(k), float(dt)), self._h)
         self.synchronize()
+
+    NORM_NAMES = ("Max", "Min", "L2Norm", "L2IntegralNorm", "VolumeIntegral")
+    VARIABLE_NAMES = ("Psi", "Pi", "Phi_x", "Phi_y", "Phi_z")
+
+    def observe_norms(self, u_dev=None, subtract_dev=None):
+        """Events::ObserveNorms of the state (or of a device tensor): a dict
+        {"Max(Psi)": ..., ..., "NumberOfPoints": ..., "Volume": ...}."""
+        out = np.zeros(27)
+        _torch_ready(u_dev, subtract_dev)
+        _check(lib().dgsw_observe_norms(self._h, _ptr(u_dev), _ptr(subtract_dev), _ptr(out)),
+               self._h)
+        return self._norm_dict(out)
+
+    def observe_plane_wave_errors(self, k, t: float):
+        """ObserveNorms of Psi - PlaneWave(k, t) etc. (the Error(...) norms)."""
+        kk = np.ascontiguousarray(k, dtype=np.float64)
+        out = np.zeros(27)
+        _check(lib().dgsw_observe_plane_wave_errors(self._h, _ptr(kk), float(t), _ptr(out)),
+               self._h)
+        return self._norm_dict(out, prefix="Error")
+
+    def _norm_dict(self, out, prefix=""):
+        d = {}
+        for v, vn in enumerate(self.VARIABLE_NAMES):
+            name = "%s(%s)" % (prefix, vn) if prefix else vn
+            for m, mn in enumerate(self.NORM_NAMES):
+                d["%s(%s)" % (mn, name)] = float(out[5 * v + m])
+        d["NumberOfPoints"] = int(out[25])
+        d["Volume"] = float(out[26])
+        d["raw"] = out
+        return d
 
     def set_exponential_filter(self, alpha: float, half_power: int, enable: bool = True):
         """Filters::Exponential after every substep (dg::Actions::Filter)."""

@@ -39,7 +39,7 @@
 extern "C" {
 #endif
 
-#define DGSW_ABI_VERSION 2
+#define DGSW_ABI_VERSION 3
 
 typedef enum {
   DGSW_OK = 0,
@@ -65,6 +65,13 @@ typedef enum { DGSW_STEPPER_RK3_HESTHAVEN_SSP = 0 } DgswTimeStepper;
  * MIXED: FP32 contractions with the D-matrix split into hi+lo FP32 parts,
  * FP64 state and FP64 accumulation of each time step. */
 typedef enum { DGSW_PRECISION_FP64 = 0, DGSW_PRECISION_MIXED = 1 } DgswPrecision;
+/* Spectral::Quadrature of the element meshes.  GAUSS_LOBATTO: faces are
+ * volume points and corrections are lifted onto them (lift_flux).  GAUSS:
+ * faces are interpolated (boundary_interpolation_matrices) and corrections
+ * lifted into the whole element (lift_boundary_terms_gauss_points,
+ * NumericalAlgorithms/DiscontinuousGalerkin/LiftFromBoundary.cpp:20-140);
+ * flat system, one extent for every element, FP64 precision. */
+typedef enum { DGSW_QUADRATURE_GAUSS_LOBATTO = 0, DGSW_QUADRATURE_GAUSS = 1 } DgswQuadrature;
 
 /* One periodic rectilinear evolution domain [lower, upper]^3 with
  * elements[d] elements along axis d.  A count n = b * 2^L (b odd) is laid out
@@ -118,6 +125,7 @@ typedef struct {
   /* DGSW_SYSTEM_CURVED_SCALAR_WAVE_3D: the shell domain (n_instances = 1,
    * bricks ignored, uniform_points per element); NULL for the flat system. */
   const DgswShell* shell;
+  int32_t quadrature;          /* DgswQuadrature (0 = Gauss-Lobatto) */
 } DgswConfig;
 
 typedef struct DgswHandle_* DgswHandle;
@@ -243,6 +251,13 @@ int dgsw_misfit_adjoint(DgswHandle h, double* dev_grad);
  * Spectral::collocation_points / quadrature_weights <Legendre, GaussLobatto>
  * (NumericalAlgorithms/Spectral/Legendre.cpp:186-239) */
 int dgsw_lgl_points_weights(int n, double* x, double* w);
+/* Legendre-Gauss tables (Spectral.cpp, Quadrature::Gauss): nodes x and
+ * weights w (Legendre.cpp:106-149), D row-major, the interpolation rows to
+ * xi = -1 and +1 (boundary_interpolation_matrices, Spectral.cpp:676-697) and
+ * the boundary_lifting_term rows (Spectral.cpp:753-781).  Any output may be
+ * NULL; each holds n (D: n*n) doubles. */
+int dgsw_gauss_spectral(int n, double* x, double* w, double* D, double* interp_lower,
+                        double* interp_upper, double* lift_lower, double* lift_upper);
 /* Spectral::differentiation_matrix, row-major D[i*n+j]
  * (NumericalAlgorithms/Spectral/Spectral.cpp:113-447) */
 int dgsw_differentiation_matrix(int n, double* D);

@@ -286,10 +286,11 @@ void package_face(const Mesh& m, const double* u, double gamma2, int64_t e, int 
   orc_package(nf, psi.data(), pi.data(), phi.data(), g2.data(), nrm.data(), nullptr, pkg, &ms);
 }
 
-void volume_terms(const Mesh& m, const double* u, double gamma2, int64_t e, double* dt) {
+void volume_terms(const Mesh& m, const double* u, double gamma2, int64_t e, double* dt,
+                  const double* Dmat = nullptr) {
   const int n = m.elem_n[e];
   const int64_t np = (int64_t)n * n * n;
-  const Spectral1d& sp = spectral(n);
+  const double* Dm = Dmat ? Dmat : spectral(n).D;
   const double* ue = u + m.off[e];
   // logical derivatives of all 5 vars (PartialDerivatives.tpp:315-363)
   std::vector<double> dl((size_t)3 * kVars * np);
@@ -305,7 +306,7 @@ void volume_terms(const Mesh& m, const double* u, double gamma2, int64_t e, doub
             for (int q = 0; q < n; ++q) {
               int id2[3] = {i, j, k};
               id2[a] = q;
-              s += sp.D[idx[a] * n + q] * f[id2[0] + n * (id2[1] + n * id2[2])];
+              s += Dm[idx[a] * n + q] * f[id2[0] + n * (id2[1] + n * id2[2])];
             }
             out[i + n * (j + n * k)] = s;
           }
@@ -1035,6 +1036,284 @@ int orc_csw_cpsr(int npts, const double* psi, const double* pi, const double* ph
     dpi_c /= lapse[p];
     dpi_c += gamma2[p] * dpsi_c - dt_pi[p];
     out[n + p] = dpi_c;
+  }
+  return 0;
+}
+
+}  // extern "C"
+
+// ======================= Legendre-Gauss quadrature =======================
+namespace {
+
+// P_n(x) and P_n'(x) by the three-term recurrence (Kopriva algorithm 22)
+void legendre_and_derivative(int n, double x, double* L, double* dL) {
+  double lm2 = 1.0, lm1 = x, dm2 = 0.0, dm1 = 1.0;
+  if (n == 0) {
+    *L = 1.0;
+    *dL = 0.0;
+    return;
+  }
+  for (int k = 2; k <= n; ++k) {
+    const double l = ((2.0 * k - 1.0) * x * lm1 - (k - 1.0) * lm2) / k;
+    const double d = dm2 + (2.0 * k - 1.0) * lm1;
+    lm2 = lm1;
+    lm1 = l;
+    dm2 = dm1;
+    dm1 = d;
+  }
+  *L = lm1;
+  *dL = dm1;
+}
+
+// root of P_n on a sign-changing bracket, bisected to adjacent doubles (the
+// reference runs TOMS748 to 6e-16 on the same brackets, Legendre.cpp:128-134)
+double lg_root(int n, double a, double b) {
+  double fa, fb, d;
+  legendre_and_derivative(n, a, &fa, &d);
+  legendre_and_derivative(n, b, &fb, &d);
+  if (fa == 0.0) return a;
+  if (fb == 0.0) return b;
+  for (int it = 0; it < 200; ++it) {
+    const double m = 0.5 * (a + b);
+    if (m <= std::min(a, b) || m >= std::max(a, b)) break;
+    double fm;
+    legendre_and_derivative(n, m, &fm, &d);
+    if (fm == 0.0) return m;
+    if ((fm < 0) == (fa < 0)) {
+      a = m;
+      fa = fm;
+    } else {
+      b = m;
+    }
+  }
+  return 0.5 * (a + b);
+}
+
+struct Gauss1d {
+  int n = 0;
+  double x[kMaxN], w[kMaxN], bw[kMaxN];
+  double D[kMaxN * kMaxN];
+  double lo[kMaxN], hi[kMaxN];            // interpolation to xi = -1, +1
+  double lift_lo[kMaxN], lift_hi[kMaxN];  // boundary_lifting_term
+};
+
+const Gauss1d& gauss(int n) {
+  static Gauss1d table[kMaxN + 1];
+  static bool init = [] {
+    for (int m = 2; m <= kMaxN; ++m) {
+      Gauss1d& g = table[m];
+      g.n = m;
+      orc_lg(m, g.x, g.w);
+      for (int j = 0; j < m; ++j) g.bw[j] = 1.0;
+      for (int j = 1; j < m; ++j)
+        for (int k = 0; k < j; ++k) {
+          g.bw[k] *= g.x[k] - g.x[j];
+          g.bw[j] *= g.x[j] - g.x[k];
+        }
+      for (int j = 0; j < m; ++j) g.bw[j] = 1.0 / g.bw[j];
+      for (int i = 0; i < m; ++i) {
+        double diag = 0.0;
+        for (int j = 0; j < m; ++j)
+          if (i != j) {
+            g.D[i * m + j] = g.bw[j] / (g.bw[i] * (g.x[i] - g.x[j]));
+            diag -= g.D[i * m + j];
+          }
+        g.D[i * m + i] = diag;
+      }
+      // barycentric interpolation to the end points (no node sits there)
+      for (int side = 0; side < 2; ++side) {
+        const double t = side ? 1.0 : -1.0;
+        double* row = side ? g.hi : g.lo;
+        double sum = 0.0;
+        for (int j = 0; j < m; ++j) {
+          row[j] = g.bw[j] / (t - g.x[j]);
+          sum += row[j];
+        }
+        for (int j = 0; j < m; ++j) row[j] /= sum;
+      }
+      for (int j = 0; j < m; ++j) {
+        g.lift_lo[j] = g.lo[j] / g.w[j];
+        g.lift_hi[j] = g.hi[j] / g.w[j];
+      }
+    }
+    return true;
+  }();
+  (void)init;
+  return table[n];
+}
+
+}  // namespace
+
+extern "C" {
+
+int orc_lg(int n, double* x, double* w) {
+  // compute_collocation_points_and_weights<Legendre, Gauss>, Legendre.cpp:106-149
+  // (Kopriva algorithm 23): roots of P_n, w = 2 / ((1 - x^2) P_n'(x)^2)
+  if (n < 2 || n > kMaxN || !x || !w) return -1;
+  const int p = n - 1;  // polynomial degree
+  if (p == 1) {
+    x[0] = -std::sqrt(1.0 / 3.0);
+    x[1] = -x[0];
+    w[0] = w[1] = 1.0;
+    return 0;
+  }
+  for (int j = 0; j <= (p + 1) / 2 - 1; ++j) {
+    const double r = lg_root(n, -std::cos((2.0 * j) * M_PI / (2.0 * p + 2.0)),
+                             -std::cos((2.0 * j + 2.0) * M_PI / (2.0 * p + 2.0)));
+    double L, dL;
+    legendre_and_derivative(n, r, &L, &dL);
+    x[j] = r;
+    x[p - j] = -r;
+    w[j] = w[p - j] = 2.0 / (1.0 - r * r) / (dL * dL);
+  }
+  if (p % 2 == 0) {
+    double L, dL;
+    legendre_and_derivative(n, 0.0, &L, &dL);
+    x[p / 2] = 0.0;
+    w[p / 2] = 2.0 / (dL * dL);
+  }
+  return 0;
+}
+
+int orc_lg_diff_matrix(int n, double* D) {
+  // differentiation_matrix<Legendre, Gauss>: the barycentric formula of
+  // Spectral.cpp:431-444 on the Gauss nodes
+  if (n < 2 || n > kMaxN || !D) return -1;
+  std::memcpy(D, gauss(n).D, sizeof(double) * n * n);
+  return 0;
+}
+
+int orc_lg_boundary(int n, double* lo, double* hi, double* lift_lo, double* lift_hi) {
+  // boundary_interpolation_matrices and boundary_lifting_term,
+  // Spectral.cpp:676-790
+  if (n < 2 || n > kMaxN) return -1;
+  const Gauss1d& g = gauss(n);
+  for (int j = 0; j < n; ++j) {
+    if (lo) lo[j] = g.lo[j];
+    if (hi) hi[j] = g.hi[j];
+    if (lift_lo) lift_lo[j] = g.lift_lo[j];
+    if (lift_hi) lift_hi[j] = g.lift_hi[j];
+  }
+  return 0;
+}
+
+}  // extern "C"
+
+// Gauss-point boundary corrections of element e (uniform extent n):
+// ApplyBoundaryCorrections.hpp:938-987 with lift_boundary_terms_gauss_points,
+// LiftFromBoundary.cpp:20-140.  Each side interpolates its own volume data to
+// the shared face (boundary_interpolation_matrices); on an affine element
+// det(inverse Jacobian) x det(Jacobian on the face) = 1, so
+//   dt(line point i) -= |n| lift_i(side) correction(face point).
+namespace {
+void boundary_terms_gauss(const Mesh& m, const double* u, double gamma2, int64_t e,
+                          double* dt) {
+  const int n = m.elem_n[e];
+  const int64_t np = (int64_t)n * n * n;
+  const int nf = n * n;
+  const Gauss1d& g = gauss(n);
+  for (int dir = 0; dir < 6; ++dir) {
+    const int d = dir / 2;
+    const bool upper = dir % 2;
+    const int64_t nb = m.nbr[6 * e + dir];
+    auto face_package = [&](int64_t el, bool up, double sign, double* pkg, double* mag) {
+      const double* ue = u + m.off[el];
+      const double* I = up ? g.hi : g.lo;
+      std::vector<double> psi(nf), pi(nf), phi(3 * nf), g2(nf, gamma2), nrm(3 * nf, 0.0);
+      for (int b = 0; b < n; ++b)
+        for (int a = 0; a < n; ++a) {
+          const int f = a + n * b;
+          double acc[kVars] = {0, 0, 0, 0, 0};
+          for (int i = 0; i < n; ++i) {
+            const int64_t vi = volume_index(n, d, i, a, b);
+            for (int v = 0; v < kVars; ++v) acc[v] += I[i] * ue[v * np + vi];
+          }
+          psi[f] = acc[0];
+          pi[f] = acc[1];
+          for (int c = 0; c < 3; ++c) phi[c * nf + f] = acc[2 + c];
+          nrm[d * nf + f] = sign;  // sign * invjac / |invjac|
+          mag[f] = m.geom[el].invjac[d];
+        }
+      double ms;
+      orc_package(nf, psi.data(), pi.data(), phi.data(), g2.data(), nrm.data(), nullptr, pkg,
+                  &ms);
+    };
+    std::vector<double> pi_((size_t)kPkg * nf), pe((size_t)kPkg * nf), mi(nf), me(nf);
+    face_package(e, upper, upper ? 1.0 : -1.0, pi_.data(), mi.data());
+    face_package(nb, !upper, upper ? -1.0 : 1.0, pe.data(), me.data());
+    std::vector<double> bc((size_t)kVars * nf);
+    orc_boundary_terms(nf, pi_.data(), pe.data(), bc.data());
+    const double* lift = upper ? g.lift_hi : g.lift_lo;
+    for (int b = 0; b < n; ++b)
+      for (int a = 0; a < n; ++a) {
+        const int f = a + n * b;
+        for (int i = 0; i < n; ++i) {
+          const int64_t vi = volume_index(n, d, i, a, b);
+          const double fac = mi[f] * lift[i];
+          for (int v = 0; v < kVars; ++v) dt[v * np + vi] -= fac * bc[(size_t)v * nf + f];
+        }
+      }
+  }
+}
+}  // namespace
+
+extern "C" {
+
+int orc_coords_gauss(int n_inst, const OrcBrick* br, int n, double* xyz) {
+  if (n_inst < 1 || !br || n < 2 || n > kMaxN || !xyz) return -1;
+  const int64_t E = orc_num_elements(n_inst, br);
+  std::vector<int32_t> en(E, n);
+  Mesh m;
+  build_mesh(&m, n_inst, br, en.data());
+  const Gauss1d& g = gauss(n);
+  const int64_t np = (int64_t)n * n * n;
+  for (int64_t e = 0; e < E; ++e)
+    for (int k = 0; k < n; ++k)
+      for (int j = 0; j < n; ++j)
+        for (int i = 0; i < n; ++i) {
+          const int64_t p = i + n * (j + (int64_t)n * k);
+          const int id[3] = {i, j, k};
+          for (int c = 0; c < 3; ++c)
+            xyz[e * 3 * np + c * np + p] =
+                m.geom[e].lo[c] + (g.x[id[c]] + 1.0) * (0.5 * m.geom[e].h[c]);
+        }
+  return 0;
+}
+
+int orc_rhs_gauss(int n_inst, const OrcBrick* br, int n, double gamma2, const double* u,
+                  double* dudt, int n_threads) {
+  if (n_inst < 1 || !br || n < 2 || n > kMaxN || !u || !dudt) return -1;
+  const int64_t E = orc_num_elements(n_inst, br);
+  std::vector<int32_t> en(E, n);
+  Mesh m;
+  build_mesh(&m, n_inst, br, en.data());
+  const Gauss1d& g = gauss(n);
+#ifdef _OPENMP
+  if (n_threads > 0) omp_set_num_threads(n_threads);
+#pragma omp parallel for schedule(dynamic, 4)
+#endif
+  for (int64_t e = 0; e < E; ++e) {
+    volume_terms(m, u, gamma2, e, dudt + m.off[e], g.D);
+    boundary_terms_gauss(m, u, gamma2, e, dudt + m.off[e]);
+  }
+  (void)n_threads;
+  return 0;
+}
+
+int orc_evolve_gauss(int n_inst, const OrcBrick* br, int n, double gamma2, double dt,
+                     int n_steps, double* u, int n_threads) {
+  if (n_inst < 1 || !br || n < 2 || n > kMaxN || !u || n_steps < 0) return -1;
+  const int64_t size = orc_num_elements(n_inst, br) * 5 * (int64_t)n * n * n;
+  std::vector<double> u0(size), u1(size), du(size);
+  for (int st = 0; st < n_steps; ++st) {
+    std::memcpy(u0.data(), u, size * sizeof(double));
+    orc_rhs_gauss(n_inst, br, n, gamma2, u0.data(), du.data(), n_threads);
+    orc_rk3_substep(size, 0, dt, u0.data(), u0.data(), du.data(), u1.data());
+    orc_rhs_gauss(n_inst, br, n, gamma2, u1.data(), du.data(), n_threads);
+    orc_rk3_substep(size, 1, dt, u0.data(), u1.data(), du.data(), u);
+    std::memcpy(u1.data(), u, size * sizeof(double));
+    orc_rhs_gauss(n_inst, br, n, gamma2, u1.data(), du.data(), n_threads);
+    orc_rk3_substep(size, 2, dt, u0.data(), u1.data(), du.data(), u);
   }
   return 0;
 }

@@ -112,6 +112,25 @@ int orc_evolve(int n_inst, const OrcBrick* bricks, const int32_t* elem_n,
                double gamma2, double dt, int n_steps, double* u, int n_threads);
 
 
+/* ---------------- Legendre-Gauss quadrature ----------------
+ * collocation points/weights <Legendre, Gauss> (Legendre.cpp:106-149),
+ * differentiation_matrix on those nodes, boundary_interpolation_matrices
+ * (rows to xi = -1, +1) and boundary_lifting_term (rows / weights),
+ * Spectral.cpp:676-790. */
+int orc_lg(int n, double* x, double* w);
+int orc_lg_diff_matrix(int n, double* D);
+int orc_lg_boundary(int n, double* lo, double* hi, double* lift_lo, double* lift_hi);
+/* Flat ScalarWave on Gauss points, uniform extent n, periodic bricks:
+ * volume terms with the Gauss D; faces interpolated to the boundary, packaged
+ * and corrected by UpwindPenalty; the correction lifted into the whole
+ * element by lift_boundary_terms_gauss_points (LiftFromBoundary.cpp:20-140,
+ * called from ApplyBoundaryCorrections.hpp:938-987). */
+int orc_coords_gauss(int n_inst, const OrcBrick* bricks, int n, double* xyz);
+int orc_rhs_gauss(int n_inst, const OrcBrick* bricks, int n, double gamma2, const double* u,
+                  double* dudt, int n_threads);
+int orc_evolve_gauss(int n_inst, const OrcBrick* bricks, int n, double gamma2, double dt,
+                     int n_steps, double* u, int n_threads);
+
 /* ---------------- exponential filter ----------------
  * Spectral::filtering::exponential_filter (NumericalAlgorithms/Spectral/
  * Filtering.cpp:18-31): F = V diag(exp(-alpha (k/(n-1))^(2 half_power))) V^-1

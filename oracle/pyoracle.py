@@ -62,6 +62,9 @@ def lib():
             "orc_shell_evolve": [P, D, I, P, I],
             "orc_exponential_filter": [I, D, I, P], "orc_filter_elements": [I64, P, D, I, P],
             "orc_observe_norms": [I, P, P, P, P, P], "orc_shell_observe_norms": [P, P, P],
+            "orc_lg": [I, P, P], "orc_lg_diff_matrix": [I, P], "orc_lg_boundary": [I, P, P, P, P],
+            "orc_coords_gauss": [I, P, I, P], "orc_rhs_gauss": [I, P, I, D, P, P, I],
+            "orc_evolve_gauss": [I, P, I, D, D, I, P, I],
         }
         for name, args in sig.items():
             fn = getattr(L, name)
@@ -366,3 +369,62 @@ def shell_observe_norms(s, u):
     out = np.zeros(27)
     _check(lib().orc_shell_observe_norms(ctypes.byref(s), _p(_c(u)), _p(out)))
     return out
+
+
+def lg(n):
+    """Legendre-Gauss nodes and weights."""
+    x, w = np.zeros(n), np.zeros(n)
+    _check(lib().orc_lg(n, _p(x), _p(w)))
+    return x, w
+
+
+def lg_diff_matrix(n):
+    D = np.zeros((n, n))
+    _check(lib().orc_lg_diff_matrix(n, _p(D)))
+    return D
+
+
+def lg_boundary(n):
+    """(interp to -1, interp to +1, lifting term -1, lifting term +1)."""
+    a = [np.zeros(n) for _ in range(4)]
+    _check(lib().orc_lg_boundary(n, *[_p(x) for x in a]))
+    return tuple(a)
+
+
+def coords_gauss(bricks, n):
+    E = num_elements(bricks)
+    xyz = np.zeros((E, 3, n ** 3))
+    arr = _bricks(bricks)
+    _check(lib().orc_coords_gauss(len(bricks), ctypes.addressof(arr), n, _p(xyz)))
+    return xyz
+
+
+def plane_wave_gauss(bricks, n, k, t=0.0):
+    """PlaneWave initial data on the Gauss nodes, [E, 5, n^3]."""
+    xyz = coords_gauss(bricks, n)
+    k = np.asarray(k, dtype=np.float64)
+    om = float(np.sqrt((k * k).sum()))
+    ph = np.einsum("i,eip->ep", k, xyz) - om * t
+    u = np.zeros((xyz.shape[0], 5, n ** 3))
+    u[:, 0] = np.sin(ph)
+    u[:, 1] = om * np.cos(ph)
+    for d in range(3):
+        u[:, 2 + d] = k[d] * np.cos(ph)
+    return u
+
+
+def rhs_gauss(bricks, n, u, gamma2=0.0, threads=0):
+    u = _c(u)
+    out = np.zeros_like(u)
+    arr = _bricks(bricks)
+    _check(lib().orc_rhs_gauss(len(bricks), ctypes.addressof(arr), n, gamma2, _p(u), _p(out),
+                               threads))
+    return out
+
+
+def evolve_gauss(bricks, n, u, dt, steps, gamma2=0.0, threads=0):
+    u = _c(u).copy()
+    arr = _bricks(bricks)
+    _check(lib().orc_evolve_gauss(len(bricks), ctypes.addressof(arr), n, gamma2, dt, steps,
+                                  _p(u), threads))
+    return u

@@ -79,6 +79,9 @@ struct DgswHandle_ {
   float* c_T32 = nullptr;
   float* c_F32 = nullptr;
   int32_t* c_X = nullptr;
+  // Legendre-Gauss quadrature (flat, uniform, FP64)
+  bool gauss = false;
+  GaussTables gt{};
   // ObserveNorms scratch
   double* lgl_w = nullptr;
   double* norm_partial = nullptr;
@@ -211,6 +214,32 @@ cudaError_t general_f64(DgswHandle h, const double* x, const double* y, double* 
   G.c = c;
   G.boundary = boundary;
   return launch_general_classes(h, G);
+}
+
+// FP64 stage on Gauss points: out = a u0 + b x + c L(x)
+cudaError_t gauss_f64(DgswHandle h, const double* x, const double* u0, double* out, double a,
+                      double b, double c, int boundary = 1) {
+  GaussLaunch G;
+  G.n = h->dom.elem_n[0];
+  G.n_elem = h->dom.n_elem;
+  G.boundary = boundary;
+  G.ucur = x;
+  G.u0 = u0;
+  G.unext = out;
+  G.a = a;
+  G.b = b;
+  G.c = c;
+  G.nbr = h->nbr;
+  G.jac = h->jac;
+  G.gamma2 = h->cfg.gamma2;
+  G.eo = h->eo;
+  for (int i = 0; i < G.n; ++i) {
+    G.lo[i] = h->gt.lo[i];
+    G.hi[i] = h->gt.hi[i];
+    G.lift_lo[i] = h->gt.lift_lo[i];
+    G.lift_hi[i] = h->gt.lift_hi[i];
+  }
+  return launch_stage_gauss(G, h->stream);
 }
 
 // ---- CurvedScalarWave ------------------------------------------------------
@@ -468,6 +497,13 @@ cudaError_t enqueue_step(DgswHandle h, double dt) {
   }
   // each substep's result is filtered when the filter is on, as
   // dg::Actions::Filter follows UpdateU in the reference's step actions
+  if (h->gauss) {
+    cudaError_t e = gauss_f64(h, h->state, nullptr, h->t1, 0.0, 1.0, dt);
+    if (e == cudaSuccess) e = gauss_f64(h, h->t1, h->state, h->t2, 0.75, 0.25, 0.25 * dt);
+    if (e == cudaSuccess)
+      e = gauss_f64(h, h->t2, h->state, h->state, 1.0 / 3.0, 2.0 / 3.0, (2.0 / 3.0) * dt);
+    return e;
+  }
   if (h->curved) {
     cudaError_t e = csw_f64(h, h->state, nullptr, h->t1, 0.0, 1.0, dt);
     if (e == cudaSuccess) e = apply_filter(h, h->t1);
@@ -658,6 +694,22 @@ int dgsw_shell_geometry(const DgswConfig* cfg, double* xyz, double* inv_jac, int
   return DGSW_OK;
 }
 
+int dgsw_gauss_spectral(int n, double* x, double* w, double* D, double* ilo, double* ihi,
+                        double* llo, double* lhi) {
+  GaussTables g;
+  if (!lg_spectral(n, &g)) return fail(nullptr, DGSW_ERR_ARGUMENT, "n must be in [2, 20]");
+  for (int i = 0; i < n; ++i) {
+    if (x) x[i] = g.x[i];
+    if (w) w[i] = g.w[i];
+    if (ilo) ilo[i] = g.lo[i];
+    if (ihi) ihi[i] = g.hi[i];
+    if (llo) llo[i] = g.lift_lo[i];
+    if (lhi) lhi[i] = g.lift_hi[i];
+  }
+  if (D) std::memcpy(D, g.D, sizeof(double) * n * n);
+  return DGSW_OK;
+}
+
 int dgsw_lgl_points_weights(int n, double* x, double* w) {
   if (!lgl_nodes_weights(n, x, w)) return fail(nullptr, DGSW_ERR_ARGUMENT, "n must be in [2, 20]");
   return DGSW_OK;
@@ -691,6 +743,16 @@ int dgsw_create(const DgswConfig* cfg, DgswHandle* out) {
   h->cfg.points_per_element = nullptr;
   if (h->curved) h->shell = *cfg->shell;
   h->cfg.shell = h->curved ? &h->shell : nullptr;
+  h->gauss = cfg->quadrature == DGSW_QUADRATURE_GAUSS;
+  if (cfg->quadrature != DGSW_QUADRATURE_GAUSS_LOBATTO && !h->gauss) {
+    delete h;
+    return fail(nullptr, DGSW_ERR_ARGUMENT, "unknown quadrature");
+  }
+  if (h->gauss && (h->curved || !h->dom.uniform || cfg->precision != DGSW_PRECISION_FP64)) {
+    delete h;
+    return fail(nullptr, DGSW_ERR_UNSUPPORTED,
+                "Gauss quadrature: flat system, one extent for every element, FP64 precision");
+  }
   if (!h->curved && cfg->precision == DGSW_PRECISION_MIXED && cfg->gamma2 != 0.0) {
     delete h;
     return fail(nullptr, DGSW_ERR_UNSUPPORTED, "mixed precision needs gamma2 = 0");
@@ -743,11 +805,21 @@ int dgsw_create(const DgswConfig* cfg, DgswHandle* out) {
   std::vector<double> nodes((kMaxN + 1) * kMaxN, 0.0);
   for (int n = kMinN; n <= kMaxN; ++n) {
     double w[kMaxN];
-    lgl_nodes_weights(n, &nodes[n * kMaxN], w);
+    if (h->gauss) {
+      GaussTables g;
+      lg_spectral(n, &g);
+      for (int i = 0; i < n; ++i) nodes[n * kMaxN + i] = g.x[i];
+    } else {
+      lgl_nodes_weights(n, &nodes[n * kMaxN], w);
+    }
   }
   if ((e = upload(&h->lgl_x, nodes)) != cudaSuccess) return bail(e, "upload nodes");
   lgl_eo_table(h->dom.elem_n[0], &h->eo);
   lgl_eo_table_transposed(h->dom.elem_n[0], &h->eoT);
+  if (h->gauss) {
+    lg_spectral(h->dom.elem_n[0], &h->gt);
+    lg_eo_table(h->dom.elem_n[0], &h->eo);
+  }
   if (h->curved) {
     int rc = csw_init(h, geo);
     if (rc) {
@@ -947,6 +1019,10 @@ int dgsw_rhs_device(DgswHandle h, const double* dev_u, double* dev_dudt) {
     DGSW_CUDA(h, csw_f64(h, dev_u, nullptr, dev_dudt, 0.0, 0.0, 1.0));
     return DGSW_OK;
   }
+  if (h->gauss) {
+    DGSW_CUDA(h, gauss_f64(h, dev_u, nullptr, dev_dudt, 0.0, 0.0, 1.0));
+    return DGSW_OK;
+  }
   if (mixed(h)) {
     if (h->general) {
       GeneralLaunch G = base_general(h);
@@ -984,6 +1060,10 @@ int dgsw_volume_rhs_device(DgswHandle h, const double* dev_u, double* dev_dudt) 
   if (int rc = select_device(h)) return rc;
   if (h->curved) {
     DGSW_CUDA(h, csw_f64(h, dev_u, nullptr, dev_dudt, 0.0, 0.0, 1.0, 0));
+    return DGSW_OK;
+  }
+  if (h->gauss) {
+    DGSW_CUDA(h, gauss_f64(h, dev_u, nullptr, dev_dudt, 0.0, 0.0, 1.0, 0));
     return DGSW_OK;
   }
   if (h->general) {
@@ -1044,6 +1124,19 @@ int dgsw_substep(DgswHandle h, int k, double dt) {
     DGSW_CUDA(h, enqueue_mixed_stage(h, k, dt, h->u0s, h->state));
     return DGSW_OK;
   }
+  if (h->gauss) {
+    if (k == 0) {
+      DGSW_CUDA(h, cudaMemcpyAsync(h->u0s, h->state, bytes, cudaMemcpyDeviceToDevice, h->stream));
+      DGSW_CUDA(h, gauss_f64(h, h->u0s, nullptr, h->state, 0.0, 1.0, dt));
+    } else {
+      DGSW_CUDA(h, cudaMemcpyAsync(h->t1, h->state, bytes, cudaMemcpyDeviceToDevice, h->stream));
+      if (k == 1)
+        DGSW_CUDA(h, gauss_f64(h, h->t1, h->u0s, h->state, 0.75, 0.25, 0.25 * dt));
+      else
+        DGSW_CUDA(h, gauss_f64(h, h->t1, h->u0s, h->state, 1.0 / 3.0, 2.0 / 3.0, (2.0 / 3.0) * dt));
+    }
+    return DGSW_OK;
+  }
   if (h->curved) {
     if (k == 0) {
       DGSW_CUDA(h, cudaMemcpyAsync(h->u0s, h->state, bytes, cudaMemcpyDeviceToDevice, h->stream));
@@ -1101,7 +1194,13 @@ static int observe_norms(DgswHandle h, const double* dev_u, const double* dev_su
     std::vector<double> w((kMaxN + 1) * kMaxN, 0.0);
     for (int n = kMinN; n <= kMaxN; ++n) {
       double x[kMaxN];
-      lgl_nodes_weights(n, x, &w[n * kMaxN]);
+      if (h->gauss) {
+        GaussTables g;
+        lg_spectral(n, &g);
+        for (int i = 0; i < n; ++i) w[n * kMaxN + i] = g.w[i];
+      } else {
+        lgl_nodes_weights(n, x, &w[n * kMaxN]);
+      }
     }
     DGSW_CUDA(h, upload(&h->lgl_w, w));
     DGSW_CUDA(h, cudaMalloc(&h->norm_partial, ((size_t)E * 26 + 32) * sizeof(double)));
@@ -1189,6 +1288,8 @@ int dgsw_set_exponential_filter(DgswHandle h, double alpha, int half_power, int 
   if (mixed(h))
     return fail(h, DGSW_ERR_UNSUPPORTED,
                 "the filter acts on FP64 substep states; use FP64 precision");
+  if (h->gauss)
+    return fail(h, DGSW_ERR_UNSUPPORTED, "the filter is built for Gauss-Lobatto meshes");
   if (int rc = select_device(h)) return rc;
   std::vector<double> mats((size_t)(kMaxN + 1) * kMaxN * kMaxN, 0.0);
   for (int n = kMinN; n <= kMaxN; ++n)
@@ -1238,7 +1339,7 @@ int dgsw_step(DgswHandle h, int n_steps, double dt) {
 int dgsw_adjoint_rhs_device(DgswHandle h, const double* dev_lambda, double* dev_out) {
   if (!h || !dev_lambda || !dev_out) return fail(h, DGSW_ERR_ARGUMENT, "null argument");
   if (dev_lambda == dev_out) return fail(h, DGSW_ERR_ARGUMENT, "input and output must differ");
-  if (h->general || h->curved || h->cfg.gamma2 != 0.0)
+  if (h->general || h->curved || h->gauss || h->cfg.gamma2 != 0.0)
     return fail(h, DGSW_ERR_UNSUPPORTED,
                 "the adjoint needs the flat system, uniform extents and gamma2 = 0");
   if (int rc = select_device(h)) return rc;
@@ -1251,7 +1352,7 @@ int dgsw_adjoint_rhs_device(DgswHandle h, const double* dev_lambda, double* dev_
 
 int dgsw_set_samples(DgswHandle h, int n_samples, const double* xyz) {
   if (!h || n_samples < 1 || !xyz) return fail(h, DGSW_ERR_ARGUMENT, "need sample points");
-  if (h->general || h->dom.bricks.size() != 1 || h->cfg.gamma2 != 0.0)
+  if (h->general || h->gauss || h->dom.bricks.size() != 1 || h->cfg.gamma2 != 0.0)
     return fail(h, DGSW_ERR_UNSUPPORTED,
                 "samples and the adjoint need one brick of uniform extent and gamma2 = 0");
   if (int rc = select_device(h)) return rc;

@@ -176,6 +176,65 @@ static bool eo_from_matrix(int n, const double* D, EoTable* t) {
   return true;
 }
 
+bool lg_spectral(int n, GaussTables* g) {
+  if (n < 2 || n > 20 || !g) return false;
+  g->n = n;
+  // nodes: roots of P_n by Newton from the Chebyshev-Gauss guess, weights
+  // 2 / ((1 - x^2) P_n'(x)^2) (Legendre.cpp:106-149, Kopriva algorithm 23)
+  for (int j = 0; j < (n + 1) / 2; ++j) {
+    double r = -std::cos((2.0 * j + 1.0) * M_PI / (2.0 * n));
+    if (2 * j + 1 == n) r = 0.0;
+    double dP = 0.0;
+    for (int it = 0; it < 100; ++it) {
+      double pm1, p, pp1;
+      legendre_triple(n - 1, r, &pm1, &p, &pp1);  // P_{n-2}, P_{n-1}, P_n
+      dP = n * (r * pp1 - p) / (r * r - 1.0);
+      const double dr = pp1 / dP;
+      r -= dr;
+      if (std::abs(dr) <= 1e-17) break;
+    }
+    if (2 * j + 1 == n) r = 0.0;
+    double pm1, p, pp1;
+    legendre_triple(n - 1, r, &pm1, &p, &pp1);
+    dP = n * (r * pp1 - p) / (r * r - 1.0);
+    g->x[j] = r;
+    g->x[n - 1 - j] = -r;
+    g->w[j] = g->w[n - 1 - j] = 2.0 / ((1.0 - r * r) * dP * dP);
+  }
+  double bw[20];
+  barycentric(n, g->x, bw);
+  for (int i = 0; i < n; ++i) {
+    double diag = 0.0;
+    for (int j = 0; j < n; ++j)
+      if (j != i) {
+        g->D[i * n + j] = bw[j] / (bw[i] * (g->x[i] - g->x[j]));
+        diag -= g->D[i * n + j];
+      }
+    g->D[i * n + i] = diag;
+  }
+  for (int side = 0; side < 2; ++side) {
+    const double t = side ? 1.0 : -1.0;
+    double* row = side ? g->hi : g->lo;
+    double sum = 0.0;
+    for (int j = 0; j < n; ++j) {
+      row[j] = bw[j] / (t - g->x[j]);
+      sum += row[j];
+    }
+    for (int j = 0; j < n; ++j) row[j] /= sum;
+  }
+  for (int j = 0; j < n; ++j) {
+    g->lift_lo[j] = g->lo[j] / g->w[j];
+    g->lift_hi[j] = g->hi[j] / g->w[j];
+  }
+  return true;
+}
+
+bool lg_eo_table(int n, EoTable* t) {
+  GaussTables g;
+  if (n < kMinN || n > kMaxN || !lg_spectral(n, &g)) return false;
+  return eo_from_matrix(n, g.D, t);
+}
+
 bool lgl_exponential_filter(int n, double alpha, int half_power, double* F) {
   if (n < 2 || n > 20 || !F || half_power < 0 || !std::isfinite(alpha)) return false;
   double x[20], w[20];

@@ -26,6 +26,17 @@ bool lgl_interp_matrix(int n, int m, const double* targets, double* M);
 // Face -> mortar (nm x ne, interpolation) and mortar -> face (ne x nm,
 // Legendre modal truncation), Projection.cpp:56-375, ChildSize::Full.
 bool lgl_mortar_projections(int ne, int nm, double* to_mortar, double* from_mortar);
+// Legendre-Gauss spectral tables on n points: nodes, weights, the
+// barycentric differentiation matrix, interpolation rows to xi = -1 / +1
+// (boundary_interpolation_matrices) and those rows over the weights
+// (boundary_lifting_term), Spectral.cpp:676-790.
+struct GaussTables {
+  int n = 0;
+  double x[20], w[20], D[400], lo[20], hi[20], lift_lo[20], lift_hi[20];
+};
+bool lg_spectral(int n, GaussTables* g);
+bool lg_eo_table(int n, EoTable* t);
+
 // Exponential filter V diag(exp(-alpha (k/(n-1))^(2 half_power))) V^-1 on n
 // LGL points (Spectral::filtering::exponential_filter, Filtering.cpp:18-31),
 // row-major.

@@ -170,6 +170,25 @@ cudaError_t launch_csw_setup(const CswSetup& S, cudaStream_t s);
 cudaError_t launch_csw_initial(const double* xyz, int n, int64_t n_elem, double A, double r0,
                                double w, double* u, cudaStream_t s);
 
+// Flat ScalarWave on Legendre-Gauss points (stage_gauss.cu): uniform extent
+// n, conforming periodic bricks, FP64.  unext = a u0 + b ucur + c L(ucur).
+struct GaussLaunch {
+  int n = 0;
+  int64_t n_elem = 0;
+  int boundary = 1;  // 0: volume terms only
+  const double* ucur = nullptr;
+  const double* u0 = nullptr;
+  double* unext = nullptr;
+  double a = 0.0, b = 0.0, c = 1.0;
+  const int32_t* nbr = nullptr;
+  const double* jac = nullptr;  // 3 per element
+  double gamma2 = 0.0;
+  EoTable eo{};                 // split of the Gauss D
+  double lo[kMaxN] = {}, hi[kMaxN] = {};            // interpolation to -1, +1
+  double lift_lo[kMaxN] = {}, lift_hi[kMaxN] = {};  // boundary lifting terms
+};
+cudaError_t launch_stage_gauss(const GaussLaunch& L, cudaStream_t s);
+
 // Exponential filter of every element's variables, in place (filter.cu).
 // tasks / offset null: elements 0..n_tasks-1 of extent n, packed; else the
 // listed elements at their value offsets.  F: n x n row-major, device.

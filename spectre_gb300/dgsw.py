@@ -66,12 +66,14 @@ class DgswConfig(ctypes.Structure):
                 ("n_instances", ctypes.c_int32), ("bricks", ctypes.POINTER(DgswBrick)),
                 ("points_per_element", ctypes.POINTER(ctypes.c_int32)),
                 ("uniform_points", ctypes.c_int32), ("gamma2", ctypes.c_double),
-                ("device", ctypes.c_int32), ("shell", ctypes.POINTER(DgswShell))]
+                ("device", ctypes.c_int32), ("shell", ctypes.POINTER(DgswShell)),
+                ("quadrature", ctypes.c_int32)]
 
 
 SYSTEM_SCALAR_WAVE = 0
 SYSTEM_CURVED_SCALAR_WAVE = 1
 RADIAL_DISTRIBUTIONS = {"linear": 0, "logarithmic": 1}
+QUADRATURES = {"gauss_lobatto": 0, "gauss": 1}
 
 
 _P = ctypes.c_void_p
@@ -109,6 +111,7 @@ _SIGNATURES = {
     "dgsw_count_elements": (_I, [ctypes.POINTER(DgswConfig), ctypes.POINTER(_I64),
                                  ctypes.POINTER(_I64)]),
     "dgsw_shell_geometry": (_I, [ctypes.POINTER(DgswConfig), _P, _P, _P]),
+    "dgsw_gauss_spectral": (_I, [_I, _P, _P, _P, _P, _P, _P, _P]),
     "dgsw_adjoint_rhs_device": (_I, [_P, _P, _P]),
     "dgsw_set_samples": (_I, [_P, _I, _P]),
     "dgsw_sample_psi": (_I, [_P, _P]),
@@ -196,6 +199,18 @@ def exponential_filter_matrix(n: int, alpha: float, half_power: int) -> np.ndarr
     return F
 
 
+def gauss_spectral(n: int):
+    """Legendre-Gauss tables: dict of x, w, D, interp_lower, interp_upper,
+    lift_lower, lift_upper (Spectral::Quadrature::Gauss)."""
+    out = {k: np.zeros(n) for k in ("x", "w", "interp_lower", "interp_upper", "lift_lower",
+                                     "lift_upper")}
+    out["D"] = np.zeros((n, n))
+    _check(lib().dgsw_gauss_spectral(n, _ptr(out["x"]), _ptr(out["w"]), _ptr(out["D"]),
+                                     _ptr(out["interp_lower"]), _ptr(out["interp_upper"]),
+                                     _ptr(out["lift_lower"]), _ptr(out["lift_upper"])))
+    return out
+
+
 def mortar_projections(n_face: int, n_mortar: int):
     """(face->mortar [nm x ne], mortar->face [ne x nm]) for ChildSize::Full."""
     a = np.zeros((n_mortar, n_face))
@@ -233,7 +248,8 @@ class Shell:
 class _ConfigHolder:
     """Keeps the ctypes arrays a DgswConfig points to alive."""
 
-    def __init__(self, bricks, points, precision=PRECISION_FP64, gamma2=0.0, device=0):
+    def __init__(self, bricks, points, precision=PRECISION_FP64, gamma2=0.0, device=0,
+                 quadrature="gauss_lobatto"):
         self.shell = None
         if isinstance(bricks, Shell):
             sh = bricks
@@ -267,6 +283,7 @@ class _ConfigHolder:
         self.cfg.gamma2 = float(gamma2)
         self.cfg.device = device
         self.cfg.shell = ctypes.pointer(self.shell) if self.shell else None
+        self.cfg.quadrature = QUADRATURES[quadrature]
 
 
 def shell_geometry(shell: "Shell", points: int):
@@ -379,10 +396,12 @@ class DgEvolution:
     """All elements of one or more periodic bricks on one GPU (one handle), or
     of one spherical shell (pass a Shell: the CurvedScalarWave system)."""
 
-    def __init__(self, bricks, points, precision=PRECISION_FP64, gamma2=0.0, device=0):
+    def __init__(self, bricks, points, precision=PRECISION_FP64, gamma2=0.0, device=0,
+                 quadrature="gauss_lobatto"):
         if isinstance(bricks, Brick):
             bricks = [bricks]
-        self._cfg = _ConfigHolder(bricks, points, precision, gamma2, device)
+        self._cfg = _ConfigHolder(bricks, points, precision, gamma2, device, quadrature)
+        self.quadrature = quadrature
         h = _P()
         _check(lib().dgsw_create(ctypes.byref(self._cfg.cfg), ctypes.byref(h)))
         self._h = h

@@ -8,6 +8,9 @@ Fixtures:
   lgl_golden.json      LGL points/weights, D-matrices and Vandermonde matrices
                        read as text from
                        tests/Unit/NumericalAlgorithms/Spectral/Test_LegendreGaussLobatto.cpp
+  gauss_golden.json    Legendre-Gauss points/weights, D-matrices and
+                       Vandermonde matrices read as text from
+                       tests/Unit/NumericalAlgorithms/Spectral/Test_LegendreGauss.cpp
   curved_golden.json   seeded inputs and outputs of the CurvedScalarWave pypp
                        golden functions: BoundaryCorrections/UpwindPenalty.py
                        and BoundaryConditions/ConstraintPreservingSphericalRadiation.py
@@ -88,25 +91,29 @@ def _calls(src, fname):
 
 
 def lgl_golden():
-    path = os.path.join(
-        ROOT, "tests/Unit/NumericalAlgorithms/Spectral/Test_LegendreGaussLobatto.cpp")
+    return spectral_golden("tests/Unit/NumericalAlgorithms/Spectral/Test_LegendreGaussLobatto.cpp")
+
+
+def spectral_golden(rel):
+    path = os.path.join(ROOT, rel)
     src = open(path).read()
     src = re.sub(r"//[^\n]*", "", src)
-    res = {"source": "tests/Unit/NumericalAlgorithms/Spectral/Test_LegendreGaussLobatto.cpp",
+    res = {"source": rel,
            "points_weights": {}, "diff_matrix": {}, "modal_to_nodal": {},
            "nodal_to_modal": {}}
     for args in _calls(src, "test_points_and_weights"):
-        if len(args) != 3 or not args[0].isdigit():
+        if len(args) != 3 or not args[0].isdigit() or int(args[0]) < 2:
             continue
         n = int(args[0])
         x = eval(_cpp_expr_to_py(args[1]), {"np": np})
         w = eval(_cpp_expr_to_py(args[2]), {"np": np})
-        res["points_weights"][n] = {"x": list(map(float, x)), "w": list(map(float, w))}
+        res["points_weights"][n] = {"x": list(map(float, np.ravel(x))),
+                                   "w": list(map(float, np.ravel(w)))}
     for key, fname in (("diff_matrix", "test_diff_matrix"),
                        ("modal_to_nodal", "test_modal_to_nodal_matrix"),
                        ("nodal_to_modal", "test_nodal_to_modal_matrix")):
         for args in _calls(src, fname):
-            if len(args) != 2 or not args[0].isdigit():
+            if len(args) != 2 or not args[0].isdigit() or int(args[0]) < 2:
                 continue
             n = int(args[0])
             M = eval(_cpp_expr_to_py(args[1]), {"np": np})
@@ -262,6 +269,9 @@ def main():
         json.dump(upwind_golden(), f)
     with open(os.path.join(HERE, "curved_golden.json"), "w") as f:
         json.dump(curved_golden(), f)
+    with open(os.path.join(HERE, "gauss_golden.json"), "w") as f:
+        json.dump(spectral_golden(
+            "tests/Unit/NumericalAlgorithms/Spectral/Test_LegendreGauss.cpp"), f, indent=1)
     print("wrote fixtures to", HERE)
 
 

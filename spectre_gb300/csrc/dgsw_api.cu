@@ -475,6 +475,15 @@ cudaError_t enqueue_mixed_stage(DgswHandle h, int k, double dt, const double* u0
     L.alpha = 2.0 / 3.0;
     L.beta = 2.0 / 3.0;
     L.c = (2.0 / 3.0) * dt;
+    if (out) {
+      // W lands in d1 (each point's d1 is read only by the thread that
+      // overwrites it), then one stream forms u0 + W in FP64: the stage then
+      // stages no FP64 data and keeps twice the blocks per SM
+      L.w32 = h->w1;
+      cudaError_t e = launch_mixed(h, L);
+      if (e != cudaSuccess) return e;
+      return launch_accumulate(out, u0, h->w1, h->dom.offset.back(), h->stream);
+    }
   }
   if (out) {
     L.out64 = out;

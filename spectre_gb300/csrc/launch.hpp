@@ -46,6 +46,9 @@ struct MixedLaunch {
 };
 
 cudaError_t launch_stage_mixed(const MixedLaunch& L, cudaStream_t s);
+// out = base + (double)w elementwise (n values; out may alias base).
+cudaError_t launch_accumulate(double* out, const double* base, const float* w, int64_t n,
+                              cudaStream_t s);
 // Persistent TMA-pipelined variant for even extents (stage_mixed_pipe.cu).
 bool mixed_pipe_supported(int n);
 cudaError_t launch_stage_mixed_pipe(const MixedLaunch& L, cudaStream_t s);

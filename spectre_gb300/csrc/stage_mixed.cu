@@ -312,4 +312,38 @@ cudaError_t launch_stage_mixed(const MixedLaunch& L, cudaStream_t s) {
   }
 }
 
+// out[i] = base[i] + (double)w[i]: the FP64 update of the last incremental
+// stage, as its own stream (pairs of values per thread when both arrays
+// allow 16- and 8-byte vector access).
+__global__ void accumulate_kernel(double* out, const double* base, const float* w, int64_t n) {
+  const int64_t stride = (int64_t)gridDim.x * blockDim.x;
+  const int64_t i0 = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  const bool vec = ((reinterpret_cast<uintptr_t>(out) | reinterpret_cast<uintptr_t>(base)) & 15u) == 0 &&
+                   (reinterpret_cast<uintptr_t>(w) & 7u) == 0;
+  if (vec) {
+    const int64_t n2 = n / 2;
+    for (int64_t i = i0; i < n2; i += stride) {
+      const double2 b = reinterpret_cast<const double2*>(base)[i];
+      const float2 x = reinterpret_cast<const float2*>(w)[i];
+      reinterpret_cast<double2*>(out)[i] = make_double2(b.x + dev::widen(x.x), b.y + dev::widen(x.y));
+    }
+    if (i0 == 0 && (n & 1)) out[n - 1] = base[n - 1] + dev::widen(w[n - 1]);
+  } else {
+    for (int64_t i = i0; i < n; i += stride) out[i] = base[i] + dev::widen(w[i]);
+  }
+}
+
+cudaError_t launch_accumulate(double* out, const double* base, const float* w, int64_t n,
+                              cudaStream_t s) {
+  if (n <= 0) return cudaSuccess;
+  int dev = 0, sms = 0;
+  cudaError_t e = cudaGetDevice(&dev);
+  if (e == cudaSuccess) e = cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
+  if (e != cudaSuccess) return e;
+  const int64_t want = (n / 2 + 255) / 256;
+  const int64_t grid = want < (int64_t)sms * 8 ? (want > 0 ? want : 1) : (int64_t)sms * 8;
+  accumulate_kernel<<<(unsigned)grid, 256, 0, s>>>(out, base, w, n);
+  return cudaGetLastError();
+}
+
 }  // namespace dgsw

@@ -194,6 +194,15 @@ int dgsw_boundary_terms_device(int64_t npts, const double* packaged_int,
 int dgsw_step(DgswHandle h, int n_steps, double dt);
 int dgsw_substep(DgswHandle h, int k, double dt);
 
+/* ---- diagnostics -------------------------------------------------------------
+ * dgsw_check_device_timeout: runs the mixed-precision pipeline's bounded
+ * device-side wait on an mbarrier that no copy ever completes, with the given
+ * limit (at most 10 s).  The kernel gives up, records the handle's error word
+ * and returns; the call then reports DGSW_ERR_DEVICE_TIMEOUT exactly as a
+ * stage whose staged copy never landed would, and the handle stays usable.
+ * No counterpart in the reference (its runtime has no device-side waits). */
+int dgsw_check_device_timeout(DgswHandle h, double limit_seconds);
+
 /* ---- observation ------------------------------------------------------------
  * Events::ObserveNorms (ParallelAlgorithms/Events/ObserveNorms.cpp:33-105,
  * ObserveNorms.hpp:47-80,145-171) of Psi, Pi, Phi_x, Phi_y, Phi_z, each

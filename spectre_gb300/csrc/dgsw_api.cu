@@ -1285,6 +1285,17 @@ int dgsw_observe_plane_wave_errors(DgswHandle h, const double* k, double t, doub
   return observe_norms(h, h->state, h->t1, out);
 }
 
+int dgsw_check_device_timeout(DgswHandle h, double limit_seconds) {
+  if (!h) return fail(nullptr, DGSW_ERR_ARGUMENT, "null handle");
+  if (!(limit_seconds > 0.0) || limit_seconds > 10.0)
+    return fail(h, DGSW_ERR_ARGUMENT, "the wait limit must be in (0, 10] s");
+  if (int rc = select_device(h)) return rc;
+  DGSW_CUDA(h, launch_bounded_wait_check(h->dev_err, (uint64_t)(limit_seconds * 1e9),
+                                         h->stream));
+  DGSW_CUDA(h, cudaStreamSynchronize(h->stream));
+  return check_device_error(h);
+}
+
 int dgsw_set_exponential_filter(DgswHandle h, double alpha, int half_power, int enable) {
   if (!h) return fail(nullptr, DGSW_ERR_ARGUMENT, "null handle");
   if (!enable) {

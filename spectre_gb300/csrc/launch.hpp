@@ -51,6 +51,9 @@ cudaError_t launch_accumulate(double* out, const double* base, const float* w, i
                               cudaStream_t s);
 // Persistent TMA-pipelined variant for even extents (stage_mixed_pipe.cu).
 bool mixed_pipe_supported(int n);
+// Exercises the pipeline's bounded mbarrier wait on a barrier nothing
+// completes: sets *err after limit_ns and returns (stage_mixed_pipe.cu).
+cudaError_t launch_bounded_wait_check(int* err, uint64_t limit_ns, cudaStream_t s);
 cudaError_t launch_stage_mixed_pipe(const MixedLaunch& L, cudaStream_t s);
 
 // One class of elements of extent n with neighbours of any extent

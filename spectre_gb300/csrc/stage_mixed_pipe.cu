@@ -515,6 +515,30 @@ cudaError_t launch_pipe_n(const MixedLaunch& L, cudaStream_t s) {
 
 }  // namespace
 
+namespace {
+// The bounded wait of the pipeline on an mbarrier whose transaction never
+// arrives: the wait gives up after limit_ns, the kernel records the error
+// word and returns, exactly as the stage kernel does when a copy does not
+// land.  Nothing faults and nothing spins without a bound.
+__global__ void bounded_wait_check_kernel(int* err, uint64_t limit_ns) {
+  __shared__ uint64_t bar;
+  if (threadIdx.x == 0) {
+    mbar_init(&bar, 1);
+    fence_mbar_init();
+  }
+  __syncthreads();
+  const bool landed = mbar_wait(&bar, 0u, limit_ns);
+  if (__syncthreads_or(!landed)) {
+    if (threadIdx.x == 0) atomicExch(err, 1);
+  }
+}
+}  // namespace
+
+cudaError_t launch_bounded_wait_check(int* err, uint64_t limit_ns, cudaStream_t s) {
+  bounded_wait_check_kernel<<<1, 64, 0, s>>>(err, limit_ns);
+  return cudaGetLastError();
+}
+
 bool mixed_pipe_supported(int n) { return n % 2 == 0 && n >= 2 && n <= kMaxN; }
 
 cudaError_t launch_stage_mixed_pipe(const MixedLaunch& L, cudaStream_t s) {

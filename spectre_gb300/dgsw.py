@@ -101,6 +101,7 @@ _SIGNATURES = {
     "dgsw_step": (_I, [_P, _I, _D]),
     "dgsw_set_exponential_filter": (_I, [_P, _D, _I, _I]),
     "dgsw_observe_norms": (_I, [_P, _P, _P, _P]),
+    "dgsw_check_device_timeout": (_I, [_P, _D]),
     "dgsw_observe_plane_wave_errors": (_I, [_P, _P, _D, _P]),
     "dgsw_exponential_filter_matrix": (_I, [_I, _D, _I, _P]),
     "dgsw_substep": (_I, [_P, _I, _D]),
@@ -504,6 +505,11 @@ class DgEvolution:
     def substep(self, k: int, dt: float):
         _check(lib().dgsw_substep(self._h, int(k), float(dt)), self._h)
         self.synchronize()
+
+    def check_device_timeout(self, limit_seconds: float = 0.05) -> int:
+        """Runs the bounded device wait on a barrier nothing completes; returns
+        the status (DGSW_ERR_DEVICE_TIMEOUT when the wait gave up)."""
+        return lib().dgsw_check_device_timeout(self._h, float(limit_seconds))
 
     NORM_NAMES = ("Max", "Min", "L2Norm", "L2IntegralNorm", "VolumeIntegral")
     VARIABLE_NAMES = ("Psi", "Pi", "Phi_x", "Phi_y", "Phi_z")

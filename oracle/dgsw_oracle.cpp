@@ -1320,6 +1320,362 @@ int orc_evolve_gauss(int n_inst, const OrcBrick* br, int n, double gamma2, doubl
 
 }  // extern "C"
 
+// ======================= h-nonconforming refined bricks =======================
+namespace {
+
+struct RElem {
+  int block, level, seg[3];
+  double lo[3], h[3];
+};
+
+struct RMesh {
+  int n = 0;
+  std::vector<RElem> el;
+  std::vector<int32_t> nbr;    // 4 per face
+  std::vector<int32_t> msize;  // 2 per slot
+  std::vector<uint64_t> ids;
+};
+
+// ChildSize codes: 0 Full, 1 LowerHalf, 2 UpperHalf
+int build_refined(const OrcRefinedBrick& b, RMesh* m) {
+  const int nb = b.blocks[0] * b.blocks[1] * b.blocks[2];
+  std::vector<int64_t> first(nb + 1, 0);
+  for (int k = 0; k < nb; ++k) {
+    const int L = b.level[k];
+    if (L < 0 || L > 8) return -1;
+    first[k + 1] = first[k] + ((int64_t)1 << (3 * L));
+  }
+  const int64_t E = first[nb];
+  m->el.resize(E);
+  m->ids.resize(E);
+  auto block_xyz = [&](int k, int q[3]) {
+    q[0] = k % b.blocks[0];
+    q[1] = (k / b.blocks[0]) % b.blocks[1];
+    q[2] = k / (b.blocks[0] * b.blocks[1]);
+  };
+  auto block_of = [&](const int q[3]) { return q[0] + b.blocks[0] * (q[1] + b.blocks[1] * q[2]); };
+  auto elem_of = [&](int k, const int seg[3]) {
+    const int L = b.level[k];
+    return first[k] + (((int64_t)seg[0] << (2 * L)) | ((int64_t)seg[1] << L) | seg[2]);
+  };
+  for (int k = 0; k < nb; ++k) {
+    const int L = b.level[k];
+    int q[3];
+    block_xyz(k, q);
+    for (int64_t w = 0; w < ((int64_t)1 << (3 * L)); ++w) {
+      RElem& r = m->el[first[k] + w];
+      r.block = k;
+      r.level = L;
+      r.seg[2] = (int)(w & ((1 << L) - 1));
+      r.seg[1] = (int)((w >> L) & ((1 << L) - 1));
+      r.seg[0] = (int)(w >> (2 * L));
+      for (int d = 0; d < 3; ++d) {
+        const double W = (b.hi[d] - b.lo[d]) / b.blocks[d];
+        r.h[d] = W / (1 << L);
+        r.lo[d] = b.lo[d] + W * q[d] + r.h[d] * r.seg[d];
+      }
+      m->ids[first[k] + w] = (uint64_t)(k & 0xff) | ((uint64_t)r.seg[0] << 16) |
+                             ((uint64_t)L << 28) | ((uint64_t)r.seg[1] << 32) |
+                             ((uint64_t)L << 44) | ((uint64_t)r.seg[2] << 48) |
+                             ((uint64_t)L << 60);
+    }
+  }
+  m->nbr.assign(E * 24, -1);
+  m->msize.assign(E * 48, 0);
+  for (int64_t e = 0; e < E; ++e) {
+    const RElem& r = m->el[e];
+    const int L = r.level;
+    for (int dir = 0; dir < 6; ++dir) {
+      const int d = dir / 2;
+      const bool up = dir % 2;
+      int32_t* nbr = &m->nbr[(6 * e + dir) * 4];
+      int32_t* ms = &m->msize[(6 * e + dir) * 8];
+      const int t0 = d == 0 ? 1 : 0, t1 = d == 2 ? 1 : 2;  // transverse dims, ascending
+      const int last = (1 << L) - 1;
+      if ((up && r.seg[d] < last) || (!up && r.seg[d] > 0)) {
+        int sg[3] = {r.seg[0], r.seg[1], r.seg[2]};
+        sg[d] += up ? 1 : -1;
+        nbr[0] = (int32_t)elem_of(r.block, sg);
+        continue;
+      }
+      int q[3];
+      block_xyz(r.block, q);
+      q[d] = (q[d] + (up ? 1 : b.blocks[d] - 1)) % b.blocks[d];
+      const int k2 = block_of(q);
+      const int L2 = b.level[k2];
+      if (L2 == L) {
+        int sg[3] = {r.seg[0], r.seg[1], r.seg[2]};
+        sg[d] = up ? 0 : last;
+        nbr[0] = (int32_t)elem_of(k2, sg);
+      } else if (L2 == L + 1) {
+        for (int c = 0; c < 4; ++c) {
+          int sg[3] = {0, 0, 0};
+          sg[d] = up ? 0 : (1 << L2) - 1;
+          sg[t0] = 2 * r.seg[t0] + (c & 1);
+          sg[t1] = 2 * r.seg[t1] + (c >> 1);
+          nbr[c] = (int32_t)elem_of(k2, sg);
+          ms[2 * c] = 1 + (c & 1);
+          ms[2 * c + 1] = 1 + (c >> 1);
+        }
+      } else if (L2 == L - 1) {
+        int sg[3] = {0, 0, 0};
+        sg[d] = up ? 0 : (1 << L2) - 1;
+        sg[t0] = r.seg[t0] >> 1;
+        sg[t1] = r.seg[t1] >> 1;
+        nbr[0] = (int32_t)elem_of(k2, sg);
+      } else {
+        return -2;
+      }
+    }
+  }
+  return 0;
+}
+
+// Legendre-Gauss nodes/weights of a high-order rule for exact projections
+void gauss_rule(int m, double* x, double* w) { orc_lg(m, x, w); }
+
+}  // namespace
+
+extern "C" {
+
+int orc_proj_half(int n, int upper, double* P, double* R) {
+  // parent -> child: interpolation to x = (xi -+ 1) / 2 (Projection.cpp:341-372);
+  // child -> parent: L2 projection of the half-supported child polynomial
+  // onto the parent's Legendre modes, c_k = (2k+1)/4 int P_k(x(xi)) f(xi) dxi,
+  // the integral of Projection.cpp:140-220 evaluated with a Gauss rule exact
+  // for its degree
+  if (n < 2 || n > kMaxN) return -1;
+  const Spectral1d& sp = spectral(n);
+  const double shift = upper ? 1.0 : -1.0;
+  if (P) {
+    double t[kMaxN];
+    for (int i = 0; i < n; ++i) t[i] = 0.5 * (sp.x[i] + shift);
+    orc_interp_matrix(n, n, t, P);
+  }
+  if (R) {
+    double V[kMaxN * kMaxN], Vi[kMaxN * kMaxN];
+    orc_vandermonde(n, V);
+    orc_inv_vandermonde(n, Vi);
+    const int m = n + 1;  // degree 2n - 2 integrands
+    double gx[kMaxN + 1], gw[kMaxN + 1];
+    gauss_rule(m, gx, gw);
+    double S[kMaxN * kMaxN];  // S[k][j]
+    for (int k = 0; k < n; ++k)
+      for (int j = 0; j < n; ++j) {
+        double acc = 0.0;
+        for (int q = 0; q < m; ++q)
+          acc += gw[q] * legendre_p(k, 0.5 * (gx[q] + shift)) * legendre_p(j, gx[q]);
+        S[k * n + j] = (2.0 * k + 1.0) / 4.0 * acc;
+      }
+    for (int i = 0; i < n; ++i)
+      for (int j = 0; j < n; ++j) {
+        double acc = 0.0;
+        for (int k = 0; k < n; ++k) {
+          double vs = 0.0;
+          for (int l = 0; l < n; ++l) vs += S[k * n + l] * Vi[l * n + j];
+          acc += V[i * n + k] * vs;
+        }
+        R[i * n + j] = acc;
+      }
+  }
+  return 0;
+}
+
+int64_t orc_refined_num_elements(const OrcRefinedBrick* b) {
+  if (!b || !b->level) return -1;
+  int64_t c = 0;
+  for (int k = 0; k < b->blocks[0] * b->blocks[1] * b->blocks[2]; ++k)
+    c += (int64_t)1 << (3 * b->level[k]);
+  return c;
+}
+
+int orc_refined_index_maps(const OrcRefinedBrick* b, uint64_t* ids, int32_t* nbr,
+                           int32_t* msize) {
+  if (!b || !b->level) return -1;
+  RMesh m;
+  const int rc = build_refined(*b, &m);
+  if (rc) return rc;
+  if (ids) std::memcpy(ids, m.ids.data(), m.ids.size() * sizeof(uint64_t));
+  if (nbr) std::memcpy(nbr, m.nbr.data(), m.nbr.size() * sizeof(int32_t));
+  if (msize) std::memcpy(msize, m.msize.data(), m.msize.size() * sizeof(int32_t));
+  return 0;
+}
+
+int orc_refined_coords(const OrcRefinedBrick* b, int n, double* xyz) {
+  if (!b || !b->level || n < 2 || n > kMaxN || !xyz) return -1;
+  RMesh m;
+  if (build_refined(*b, &m)) return -1;
+  const Spectral1d& sp = spectral(n);
+  const int64_t np = (int64_t)n * n * n;
+  for (size_t e = 0; e < m.el.size(); ++e)
+    for (int k = 0; k < n; ++k)
+      for (int j = 0; j < n; ++j)
+        for (int i = 0; i < n; ++i) {
+          const int id[3] = {i, j, k};
+          for (int c = 0; c < 3; ++c)
+            xyz[e * 3 * np + c * np + i + n * (j + (int64_t)n * k)] =
+                m.el[e].lo[c] + (sp.x[id[c]] + 1.0) * 0.5 * m.el[e].h[c];
+        }
+  return 0;
+}
+
+}  // extern "C"
+
+namespace {
+
+// out(a', b') = sum_a sum_b M0(a', a) M1(b', b) in(a, b), a fastest; a null
+// matrix is the identity
+void apply_face_2d(int n, const double* M0, const double* M1, int nfields, const double* in,
+                   double* out) {
+  std::vector<double> tmp((size_t)n * n);
+  for (int f = 0; f < nfields; ++f) {
+    const double* src = in + (size_t)f * n * n;
+    double* dst = out + (size_t)f * n * n;
+    for (int b = 0; b < n; ++b)
+      for (int ap = 0; ap < n; ++ap) {
+        double acc = 0.0;
+        if (M0)
+          for (int a = 0; a < n; ++a) acc += M0[ap * n + a] * src[a + n * b];
+        else
+          acc = src[ap + n * b];
+        tmp[ap + n * b] = acc;
+      }
+    for (int bp = 0; bp < n; ++bp)
+      for (int ap = 0; ap < n; ++ap) {
+        double acc = 0.0;
+        if (M1)
+          for (int b = 0; b < n; ++b) acc += M1[bp * n + b] * tmp[ap + n * b];
+        else
+          acc = tmp[ap + n * bp];
+        dst[ap + n * bp] = acc;
+      }
+  }
+}
+
+void make_mesh_view(const RMesh& rm, int n, const OrcRefinedBrick& b, Mesh* m,
+                    std::vector<int32_t>* elem_n) {
+  const int64_t E = (int64_t)rm.el.size();
+  elem_n->assign(E, n);
+  m->n_inst = 1;
+  m->br = nullptr;
+  m->n_elem = E;
+  m->elem_n = elem_n->data();
+  m->geom.resize(E);
+  m->off.resize(E + 1);
+  orc_offsets(E, elem_n->data(), m->off.data());
+  for (int64_t e = 0; e < E; ++e) {
+    ElemGeom& g = m->geom[e];
+    g.inst = 0;
+    for (int d = 0; d < 3; ++d) {
+      g.ijk[d] = rm.el[e].seg[d];
+      g.lo[d] = rm.el[e].lo[d];
+      g.h[d] = rm.el[e].h[d];
+      g.invjac[d] = 2.0 / g.h[d];
+    }
+  }
+  (void)b;
+}
+
+// ApplyBoundaryCorrections.hpp:723-1050 with h-nonconforming mortars: per
+// mortar, both packages projected face -> mortar (identity where the mortar
+// is the face), dg_boundary_terms, mortar -> face (identity, or the
+// half-interval restriction), lift_flux on the GLL face.
+void boundary_terms_refined(const Mesh& m, const RMesh& rm, const double* u, double gamma2,
+                            int64_t e, double* dt) {
+  const int n = m.elem_n[e];
+  const int64_t np = (int64_t)n * n * n;
+  const int nf = n * n;
+  double P[2][kMaxN * kMaxN], R[2][kMaxN * kMaxN];
+  orc_proj_half(n, 0, P[0], R[0]);
+  orc_proj_half(n, 1, P[1], R[1]);
+  for (int dir = 0; dir < 6; ++dir) {
+    const int d = dir / 2;
+    const bool upper = dir % 2;
+    const int t0 = d == 0 ? 1 : 0, t1 = d == 2 ? 1 : 2;
+    std::vector<double> pki((size_t)kPkg * nf), mag(nf), pke((size_t)kPkg * nf), mage(nf);
+    package_face(m, u, gamma2, e, dir, pki.data(), mag.data());
+    std::vector<double> bc_face((size_t)kVars * nf, 0.0);
+    for (int k = 0; k < 4; ++k) {
+      const int32_t nb = rm.nbr[(6 * e + dir) * 4 + k];
+      if (nb < 0) continue;
+      const int32_t* ms = &rm.msize[((6 * e + dir) * 4 + k) * 2];
+      package_face(m, u, gamma2, nb, dir ^ 1, pke.data(), mage.data());
+      // mortar_size(neighbour, self): halves where this element is the
+      // neighbour's child (the neighbour is one level coarser)
+      int mse[2] = {0, 0};
+      if (rm.el[nb].level == rm.el[e].level - 1) {
+        mse[0] = 1 + (rm.el[e].seg[t0] & 1);
+        mse[1] = 1 + (rm.el[e].seg[t1] & 1);
+      }
+      std::vector<double> mi((size_t)kPkg * nf), me((size_t)kPkg * nf);
+      apply_face_2d(n, ms[0] ? P[ms[0] - 1] : nullptr, ms[1] ? P[ms[1] - 1] : nullptr, kPkg,
+                    pki.data(), mi.data());
+      apply_face_2d(n, mse[0] ? P[mse[0] - 1] : nullptr, mse[1] ? P[mse[1] - 1] : nullptr,
+                    kPkg, pke.data(), me.data());
+      std::vector<double> bcm((size_t)kVars * nf), bcf((size_t)kVars * nf);
+      orc_boundary_terms(nf, mi.data(), me.data(), bcm.data());
+      apply_face_2d(n, ms[0] ? R[ms[0] - 1] : nullptr, ms[1] ? R[ms[1] - 1] : nullptr, kVars,
+                    bcm.data(), bcf.data());
+      // lift this mortar's correction (LiftFlux.hpp:57-61)
+      const double slice_factor = -0.5 * static_cast<double>(n * (n - 1));
+      const int slice = upper ? n - 1 : 0;
+      for (int b = 0; b < n; ++b)
+        for (int a = 0; a < n; ++a) {
+          const int f = a + n * b;
+          const int64_t vi = volume_index(n, d, slice, a, b);
+          const double fac = slice_factor * mag[f];
+          for (int v = 0; v < kVars; ++v) dt[v * np + vi] += bcf[(size_t)v * nf + f] * fac;
+        }
+    }
+  }
+}
+
+}  // namespace
+
+extern "C" {
+
+int orc_refined_rhs(const OrcRefinedBrick* b, int n, double gamma2, const double* u,
+                    double* dudt, int n_threads) {
+  if (!b || !b->level || n < 2 || n > kMaxN || !u || !dudt) return -1;
+  RMesh rm;
+  if (build_refined(*b, &rm)) return -2;
+  Mesh m;
+  std::vector<int32_t> en;
+  make_mesh_view(rm, n, *b, &m, &en);
+#ifdef _OPENMP
+  if (n_threads > 0) omp_set_num_threads(n_threads);
+#pragma omp parallel for schedule(dynamic, 4)
+#endif
+  for (int64_t e = 0; e < m.n_elem; ++e) {
+    volume_terms(m, u, gamma2, e, dudt + m.off[e]);
+    boundary_terms_refined(m, rm, u, gamma2, e, dudt + m.off[e]);
+  }
+  (void)n_threads;
+  return 0;
+}
+
+int orc_refined_evolve(const OrcRefinedBrick* b, int n, double gamma2, double dt, int n_steps,
+                       double* u, int n_threads) {
+  const int64_t E = orc_refined_num_elements(b);
+  if (E < 0 || n < 2 || n > kMaxN || !u || n_steps < 0) return -1;
+  const int64_t size = E * 5 * (int64_t)n * n * n;
+  std::vector<double> u0(size), u1(size), du(size);
+  for (int st = 0; st < n_steps; ++st) {
+    std::memcpy(u0.data(), u, size * sizeof(double));
+    int rc = orc_refined_rhs(b, n, gamma2, u0.data(), du.data(), n_threads);
+    if (rc) return rc;
+    orc_rk3_substep(size, 0, dt, u0.data(), u0.data(), du.data(), u1.data());
+    orc_refined_rhs(b, n, gamma2, u1.data(), du.data(), n_threads);
+    orc_rk3_substep(size, 1, dt, u0.data(), u1.data(), du.data(), u);
+    std::memcpy(u1.data(), u, size * sizeof(double));
+    orc_refined_rhs(b, n, gamma2, u1.data(), du.data(), n_threads);
+    orc_rk3_substep(size, 2, dt, u0.data(), u1.data(), du.data(), u);
+  }
+  return 0;
+}
+
+}  // extern "C"
+
 // ======================= exponential filter =======================
 extern "C" {
 

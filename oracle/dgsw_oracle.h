@@ -131,6 +131,37 @@ int orc_rhs_gauss(int n_inst, const OrcBrick* bricks, int n, double gamma2, cons
 int orc_evolve_gauss(int n_inst, const OrcBrick* bricks, int n, double gamma2, double dt,
                      int n_steps, double* u, int n_threads);
 
+/* ---------------- h-nonconforming refined bricks ----------------
+ * A periodic lattice of blocks on [lo, hi]^3 (blocks x fastest), each block
+ * with its own isotropic refinement level (2^level elements per axis);
+ * neighbouring blocks differ by at most one level (2:1).  Faces between a
+ * coarse and a fine block carry one mortar per fine element, of
+ * Spectral::MortarSize LowerHalf / UpperHalf in each transverse dimension
+ * on the coarse side (MortarHelpers.cpp:49-75); data go face -> mortar by
+ * projection_matrix_parent_to_child and back by projection_matrix_child_to_parent
+ * (Projection.cpp:56-375). */
+typedef struct {
+  double lo[3], hi[3];
+  int32_t blocks[3];
+  const int32_t* level;  /* blocks[0]*blocks[1]*blocks[2] levels */
+} OrcRefinedBrick;
+int64_t orc_refined_num_elements(const OrcRefinedBrick* b);
+/* ids: packed ElementId; nbr: 4 slots per element face ((6e + dir) * 4 + k,
+ * -1 unused); msize: 2 per slot (transverse dims ascending), 0 Full,
+ * 1 LowerHalf, 2 UpperHalf, as mortar_size(self, neighbour).  Returns -2 if
+ * two neighbouring blocks differ by more than one level. */
+int orc_refined_index_maps(const OrcRefinedBrick* b, uint64_t* ids, int32_t* nbr,
+                           int32_t* msize);
+int orc_refined_coords(const OrcRefinedBrick* b, int n, double* xyz);
+int orc_refined_rhs(const OrcRefinedBrick* b, int n, double gamma2, const double* u,
+                    double* dudt, int n_threads);
+int orc_refined_evolve(const OrcRefinedBrick* b, int n, double gamma2, double dt, int n_steps,
+                       double* u, int n_threads);
+/* n x n matrices, row-major: parent (element face) -> child half (mortar)
+ * interpolation and child half -> parent L2 restriction; upper = 1 for
+ * UpperHalf, 0 for LowerHalf */
+int orc_proj_half(int n, int upper, double* parent_to_child, double* child_to_parent);
+
 /* ---------------- exponential filter ----------------
  * Spectral::filtering::exponential_filter (NumericalAlgorithms/Spectral/
  * Filtering.cpp:18-31): F = V diag(exp(-alpha (k/(n-1))^(2 half_power))) V^-1

@@ -19,6 +19,11 @@ class OrcBrick(ctypes.Structure):
                 ("n", ctypes.c_int32 * 3)]
 
 
+class OrcRefinedBrick(ctypes.Structure):
+    _fields_ = [("lo", ctypes.c_double * 3), ("hi", ctypes.c_double * 3),
+                ("blocks", ctypes.c_int32 * 3), ("level", ctypes.c_void_p)]
+
+
 class OrcShell(ctypes.Structure):
     _fields_ = [("r_inner", ctypes.c_double), ("r_outer", ctypes.c_double),
                 ("ref_ang", ctypes.c_int32), ("ref_rad", ctypes.c_int32),
@@ -65,6 +70,9 @@ def lib():
             "orc_lg": [I, P, P], "orc_lg_diff_matrix": [I, P], "orc_lg_boundary": [I, P, P, P, P],
             "orc_coords_gauss": [I, P, I, P], "orc_rhs_gauss": [I, P, I, D, P, P, I],
             "orc_evolve_gauss": [I, P, I, D, D, I, P, I],
+            "orc_refined_index_maps": [P, P, P, P], "orc_refined_coords": [P, I, P],
+            "orc_refined_rhs": [P, I, D, P, P, I], "orc_refined_evolve": [P, I, D, D, I, P, I],
+            "orc_proj_half": [I, I, P, P],
         }
         for name, args in sig.items():
             fn = getattr(L, name)
@@ -72,6 +80,8 @@ def lib():
             fn.restype = I
         L.orc_num_elements.argtypes = [I, P]
         L.orc_num_elements.restype = I64
+        L.orc_refined_num_elements.argtypes = [P]
+        L.orc_refined_num_elements.restype = I64
         L.orc_shell_num_elements.argtypes = [P]
         L.orc_shell_num_elements.restype = I64
         _lib = L
@@ -428,3 +438,63 @@ def evolve_gauss(bricks, n, u, dt, steps, gamma2=0.0, threads=0):
     _check(lib().orc_evolve_gauss(len(bricks), ctypes.addressof(arr), n, gamma2, dt, steps,
                                   _p(u), threads))
     return u
+
+
+class refined:
+    """A periodic block lattice with one refinement level per block (kept
+    alive with its level array for the ctypes calls)."""
+
+    def __init__(self, blocks, levels, lo=(0.0, 0.0, 0.0), hi=(2 * math.pi,) * 3):
+        self.levels = np.ascontiguousarray(levels, dtype=np.int32).ravel()
+        self.s = OrcRefinedBrick()
+        self.s.lo[:] = [float(v) for v in lo]
+        self.s.hi[:] = [float(v) for v in hi]
+        self.s.blocks[:] = [int(v) for v in blocks]
+        self.s.level = self.levels.ctypes.data
+
+    def num_elements(self):
+        return int(lib().orc_refined_num_elements(ctypes.byref(self.s)))
+
+    def index_maps(self):
+        E = self.num_elements()
+        ids = np.zeros(E, dtype=np.uint64)
+        nbr = np.zeros((E, 6, 4), dtype=np.int32)
+        ms = np.zeros((E, 6, 4, 2), dtype=np.int32)
+        rc = lib().orc_refined_index_maps(ctypes.byref(self.s), _p(ids), _p(nbr), _p(ms))
+        _check(rc)
+        return ids, nbr, ms
+
+    def coords(self, n):
+        xyz = np.zeros((self.num_elements(), 3, n ** 3))
+        _check(lib().orc_refined_coords(ctypes.byref(self.s), n, _p(xyz)))
+        return xyz
+
+    def plane_wave(self, n, k, t=0.0):
+        xyz = self.coords(n)
+        k = np.asarray(k, dtype=np.float64)
+        om = float(np.sqrt((k * k).sum()))
+        ph = np.einsum("i,eip->ep", k, xyz) - om * t
+        u = np.zeros((xyz.shape[0], 5, n ** 3))
+        u[:, 0] = np.sin(ph)
+        u[:, 1] = om * np.cos(ph)
+        for d in range(3):
+            u[:, 2 + d] = k[d] * np.cos(ph)
+        return u
+
+    def rhs(self, n, u, gamma2=0.0, threads=0):
+        u = _c(u)
+        out = np.zeros_like(u)
+        _check(lib().orc_refined_rhs(ctypes.byref(self.s), n, gamma2, _p(u), _p(out), threads))
+        return out
+
+    def evolve(self, n, u, dt, steps, gamma2=0.0, threads=0):
+        u = _c(u).copy()
+        _check(lib().orc_refined_evolve(ctypes.byref(self.s), n, gamma2, dt, steps, _p(u),
+                                        threads))
+        return u
+
+
+def proj_half(n, upper):
+    P, R = np.zeros((n, n)), np.zeros((n, n))
+    _check(lib().orc_proj_half(n, int(upper), _p(P), _p(R)))
+    return P, R

@@ -1383,15 +1383,6 @@ int dgsw_set_samples(DgswHandle h, int n_samples, const double* xyz) {
     return fail(h, DGSW_ERR_ARGUMENT, "a sample point lies outside the brick");
   DGSW_CUDA(h, cudaStreamSynchronize(h->stream));
   if (h->samp_off) cudaFree(h->samp_off);
-  double* cdbl[] = {h->c_xyz, h->c_ij, h->c_T, h->c_F};
-  for (double* p : cdbl)
-    if (p) cudaFree(p);
-  if (h->c_T32) cudaFree(h->c_T32);
-  if (h->c_F32) cudaFree(h->c_F32);
-  if (h->c_X) cudaFree(h->c_X);
-  if (h->filt) cudaFree(h->filt);
-  if (h->lgl_w) cudaFree(h->lgl_w);
-  if (h->norm_partial) cudaFree(h->norm_partial);
   if (h->samp_w) cudaFree(h->samp_w);
   h->samp_off = nullptr;
   h->samp_w = nullptr;

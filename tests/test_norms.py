@@ -59,3 +59,18 @@ def test_plane_wave_error_norms(oracle):
     _check(got["raw"], oracle.observe_norms(bricks, n, state, subtract=exact))
     # discretisation error of the 4^3 x 6^3 plane wave after 50 steps
     assert got["L2Norm(Error(Psi))"] < 5e-3
+
+
+def test_norms_survive_sample_setup(oracle):
+    # setting sample points must not release the handle's other device tables
+    bricks = [Brick((2, 2, 2))]
+    with DgEvolution(bricks, 8) as ev:
+        ev.set_initial_data("plane_wave", [1.0, 1.0, 1.0])
+        a = ev.observe_norms()["raw"].copy()
+        ev.set_samples(np.array([[1.0, 2.0, 3.0], [4.0, 5.0, 1.5]]))
+        ev.set_exponential_filter(36.0, 8)
+        b = ev.observe_norms()["raw"]
+        ev.set_samples(np.array([[0.5, 0.5, 0.5]]))
+        c = ev.observe_norms()["raw"]
+        ev.step(2, 1e-3)
+    assert np.array_equal(a, b) and np.array_equal(a, c)

@@ -39,7 +39,7 @@
 extern "C" {
 #endif
 
-#define DGSW_ABI_VERSION 3
+#define DGSW_ABI_VERSION 4
 
 typedef enum {
   DGSW_OK = 0,
@@ -82,6 +82,21 @@ typedef struct {
   double upper[3];
   int32_t elements[3];
 } DgswBrick;
+
+/* A periodic lattice of blocks[0] x blocks[1] x blocks[2] equal blocks on
+ * [lower, upper]^3 (blocks x fastest), block k split into 2^levels[k]
+ * elements per axis (isotropic initial refinement per block, as
+ * Domain/Creators/AlignedLattice's refined regions give).  Blocks that share
+ * a face differ by at most one level: the 2:1 faces carry h-nonconforming
+ * mortars (Spectral::MortarSize LowerHalf / UpperHalf,
+ * NumericalAlgorithms/DiscontinuousGalerkin/MortarHelpers.cpp:49-75).  Flat
+ * system, Gauss-Lobatto, one extent for every element, FP64. */
+typedef struct {
+  double lower[3];
+  double upper[3];
+  int32_t blocks[3];
+  const int32_t* levels;
+} DgswRefinedBrick;
 
 /* CurvedScalarWave domain: a spherical shell of six cubed-sphere wedges
  * (Domain/Creators/Sphere.cpp, shell without interior cube; Wedge<3>,
@@ -126,6 +141,9 @@ typedef struct {
    * bricks ignored, uniform_points per element); NULL for the flat system. */
   const DgswShell* shell;
   int32_t quadrature;          /* DgswQuadrature (0 = Gauss-Lobatto) */
+  /* non-NULL: the domain is this refined block lattice (n_instances = 1,
+   * bricks ignored) */
+  const DgswRefinedBrick* refined;
 } DgswConfig;
 
 typedef struct DgswHandle_* DgswHandle;
@@ -288,6 +306,20 @@ int dgsw_index_maps(const DgswConfig* config, uint64_t* element_ids,
                     int32_t* neighbors, int32_t* mortar_points);
 int dgsw_count_elements(const DgswConfig* config, int64_t* n_elements,
                         int64_t* state_doubles);
+/* Mortars of a refined block lattice: 4 neighbour slots per element face
+ * (slot (6e + dir) * 4 + k; -1 unused) and, per slot, the mortar size in the
+ * face's two transverse dimensions (ascending): 0 Full, 1 LowerHalf,
+ * 2 UpperHalf, as mortar_size(self, neighbour) (MortarHelpers.cpp:49-75).
+ * DGSW_ERR_ARGUMENT when neighbouring blocks differ by more than one level. */
+int dgsw_refined_mortars(const DgswConfig* config, int32_t* neighbor_slots,
+                         int32_t* mortar_sizes);
+/* Half-interval projections on n LGL points, n x n row-major:
+ * projection_matrix_parent_to_child (interpolation to the half) and
+ * projection_matrix_child_to_parent (L2 restriction from the half),
+ * ChildSize LowerHalf (upper = 0) or UpperHalf (upper = 1),
+ * NumericalAlgorithms/Spectral/Projection.cpp:56-375. */
+int dgsw_half_projections(int n, int upper, double* parent_to_child,
+                          double* child_to_parent);
 /* Shell geometry of a curved configuration (host, FP64): per element the
  * inertial coordinates (3*N^3, component-major), the inverse Jacobian
  * d xi^a / d x^i (9*N^3, component 3a+i; ElementMap::inv_jacobian of the

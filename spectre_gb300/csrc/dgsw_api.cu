@@ -79,6 +79,15 @@ struct DgswHandle_ {
   float* c_T32 = nullptr;
   float* c_F32 = nullptr;
   int32_t* c_X = nullptr;
+  // refined block lattice (h-nonconforming 2:1 faces)
+  bool refined = false;
+  DgswRefinedBrick rbrick{};
+  std::vector<int32_t> rlevels;
+  int64_t r_nfaces = 0;
+  int32_t* r_faces = nullptr;     // 9 per 2:1 face record
+  int32_t* r_face_idx = nullptr;  // per element face
+  double* r_PR = nullptr;         // [P lower, P upper, R lower, R upper], n*n each
+  double* r_wext = nullptr;       // n*n per record
   // Legendre-Gauss quadrature (flat, uniform, FP64)
   bool gauss = false;
   GaussTables gt{};
@@ -148,10 +157,30 @@ StageLaunch base_launch(DgswHandle h) {
   L.n_elem = h->dom.n_elem;
   L.gamma2 = h->cfg.gamma2;
   L.eo = h->eo;
+  if (h->refined && h->r_nfaces > 0) {
+    L.face_idx = h->r_face_idx;
+    L.wext = h->r_wext;
+  }
   return L;
 }
 
+// On a refined lattice the exterior w of every 2:1 face is assembled from
+// the stage input first (refined_faces.cu).
 cudaError_t launch_stage(DgswHandle h, const StageLaunch& L) {
+  if (h->refined && h->r_nfaces > 0 && L.mode != kModeVolume) {
+    const int n = L.n;
+    RefinedFaceLaunch R;
+    R.n = n;
+    R.n_faces = h->r_nfaces;
+    R.faces = h->r_faces;
+    R.P = h->r_PR;
+    R.R = h->r_PR + 2 * n * n;
+    R.u = L.ucur;
+    R.gamma2 = h->cfg.gamma2;
+    R.wext = h->r_wext;
+    cudaError_t e = launch_refined_faces(R, h->stream);
+    if (e != cudaSuccess) return e;
+  }
   return launch_stage_fp64(L, h->stream);
 }
 
@@ -649,7 +678,12 @@ const char* dgsw_last_error(DgswHandle h) {
 }
 
 // Builds the host maps of either system.
-bool any_domain(const DgswConfig& cfg, Domain* dom, ShellGeometry* geo, std::string* err) {
+bool any_domain(const DgswConfig& cfg, Domain* dom, ShellGeometry* geo, std::string* err,
+                RefinedMaps* rmaps = nullptr) {
+  if (cfg.refined) {
+    RefinedMaps local;
+    return build_refined_domain(cfg, dom, rmaps ? rmaps : &local, err);
+  }
   if (cfg.system == DGSW_SYSTEM_CURVED_SCALAR_WAVE_3D) return build_shell_domain(cfg, dom, geo, err);
   return build_domain(cfg, dom, err);
 }
@@ -703,6 +737,23 @@ int dgsw_shell_geometry(const DgswConfig* cfg, double* xyz, double* inv_jac, int
   return DGSW_OK;
 }
 
+int dgsw_refined_mortars(const DgswConfig* cfg, int32_t* slots, int32_t* sizes) {
+  if (!cfg || !cfg->refined) return fail(nullptr, DGSW_ERR_ARGUMENT, "not a refined lattice");
+  Domain dom;
+  RefinedMaps rm;
+  std::string err;
+  if (!build_refined_domain(*cfg, &dom, &rm, &err)) return fail(nullptr, DGSW_ERR_ARGUMENT, err);
+  if (slots) std::memcpy(slots, rm.slots.data(), rm.slots.size() * sizeof(int32_t));
+  if (sizes) std::memcpy(sizes, rm.sizes.data(), rm.sizes.size() * sizeof(int32_t));
+  return DGSW_OK;
+}
+
+int dgsw_half_projections(int n, int upper, double* P, double* R) {
+  if (!half_projections(n, upper, P, R))
+    return fail(nullptr, DGSW_ERR_ARGUMENT, "n must be in [2, 12]");
+  return DGSW_OK;
+}
+
 int dgsw_gauss_spectral(int n, double* x, double* w, double* D, double* ilo, double* ihi,
                         double* llo, double* lhi) {
   GaussTables g;
@@ -744,13 +795,22 @@ int dgsw_create(const DgswConfig* cfg, DgswHandle* out) {
   std::string err;
   ShellGeometry geo;
   h->curved = cfg->system == DGSW_SYSTEM_CURVED_SCALAR_WAVE_3D;
-  if (!any_domain(*cfg, &h->dom, &geo, &err)) {
+  h->refined = cfg->refined != nullptr;
+  RefinedMaps rmaps;
+  if (!any_domain(*cfg, &h->dom, &geo, &err, &rmaps)) {
     delete h;
     return fail(nullptr, DGSW_ERR_ARGUMENT, err);
   }
   h->cfg.bricks = nullptr;  // copies live in h->dom
   h->cfg.points_per_element = nullptr;
   if (h->curved) h->shell = *cfg->shell;
+  if (h->refined) {
+    h->rbrick = *cfg->refined;
+    const int nb = cfg->refined->blocks[0] * cfg->refined->blocks[1] * cfg->refined->blocks[2];
+    h->rlevels.assign(cfg->refined->levels, cfg->refined->levels + nb);
+    h->rbrick.levels = h->rlevels.data();
+  }
+  h->cfg.refined = h->refined ? &h->rbrick : nullptr;
   h->cfg.shell = h->curved ? &h->shell : nullptr;
   h->gauss = cfg->quadrature == DGSW_QUADRATURE_GAUSS;
   if (cfg->quadrature != DGSW_QUADRATURE_GAUSS_LOBATTO && !h->gauss) {
@@ -811,6 +871,26 @@ int dgsw_create(const DgswConfig* cfg, DgswHandle* out) {
   if ((e = upload(&h->elem_n, h->dom.elem_n)) != cudaSuccess) return bail(e, "upload extents");
   if ((e = upload(&h->offset, h->dom.offset)) != cudaSuccess) return bail(e, "upload offsets");
   if ((e = upload(&h->instance, h->dom.instance)) != cudaSuccess) return bail(e, "upload instance");
+  if (h->refined && !rmaps.faces.empty()) {
+    const int n = h->dom.elem_n[0];
+    h->r_nfaces = (int64_t)rmaps.faces.size();
+    std::vector<int32_t> rec;
+    rec.reserve(9 * rmaps.faces.size());
+    for (const RefinedFace& f : rmaps.faces) {
+      const int32_t r9[9] = {f.element, f.dir, f.coarse, f.nb[0], f.nb[1],
+                             f.nb[2], f.nb[3], f.child[0], f.child[1]};
+      rec.insert(rec.end(), r9, r9 + 9);
+    }
+    std::vector<double> PR(4 * (size_t)n * n);
+    half_projections(n, 0, &PR[0], &PR[2 * (size_t)n * n]);
+    half_projections(n, 1, &PR[(size_t)n * n], &PR[3 * (size_t)n * n]);
+    if ((e = upload(&h->r_faces, rec)) != cudaSuccess) return bail(e, "upload 2:1 faces");
+    if ((e = upload(&h->r_face_idx, rmaps.face_index)) != cudaSuccess)
+      return bail(e, "upload 2:1 face index");
+    if ((e = upload(&h->r_PR, PR)) != cudaSuccess) return bail(e, "upload half projections");
+    if ((e = cudaMalloc(&h->r_wext, (size_t)h->r_nfaces * n * n * sizeof(double))) != cudaSuccess)
+      return bail(e, "cudaMalloc 2:1 exterior values");
+  }
   std::vector<double> nodes((kMaxN + 1) * kMaxN, 0.0);
   for (int n = kMinN; n <= kMaxN; ++n) {
     double w[kMaxN];
@@ -897,6 +977,10 @@ int dgsw_destroy(DgswHandle h) {
   if (h->filt) cudaFree(h->filt);
   if (h->lgl_w) cudaFree(h->lgl_w);
   if (h->norm_partial) cudaFree(h->norm_partial);
+  if (h->r_faces) cudaFree(h->r_faces);
+  if (h->r_face_idx) cudaFree(h->r_face_idx);
+  if (h->r_PR) cudaFree(h->r_PR);
+  if (h->r_wext) cudaFree(h->r_wext);
   if (h->dev_err) cudaFree(h->dev_err);
   for (int n = 0; n <= kMaxN; ++n)
     if (h->class_tasks[n]) cudaFree(h->class_tasks[n]);
@@ -1359,7 +1443,7 @@ int dgsw_step(DgswHandle h, int n_steps, double dt) {
 int dgsw_adjoint_rhs_device(DgswHandle h, const double* dev_lambda, double* dev_out) {
   if (!h || !dev_lambda || !dev_out) return fail(h, DGSW_ERR_ARGUMENT, "null argument");
   if (dev_lambda == dev_out) return fail(h, DGSW_ERR_ARGUMENT, "input and output must differ");
-  if (h->general || h->curved || h->gauss || h->cfg.gamma2 != 0.0)
+  if (h->general || h->curved || h->gauss || h->refined || h->cfg.gamma2 != 0.0)
     return fail(h, DGSW_ERR_UNSUPPORTED,
                 "the adjoint needs the flat system, uniform extents and gamma2 = 0");
   if (int rc = select_device(h)) return rc;

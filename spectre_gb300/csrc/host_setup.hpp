@@ -93,6 +93,28 @@ struct ShellGeometry {
 bool build_shell_domain(const DgswConfig& cfg, Domain* dom, ShellGeometry* geo,
                         std::string* err);
 
+// h-nonconforming refined lattice (refined_setup.cpp).  One record per
+// 2:1 face: coarse = 1 for the coarse side (four fine neighbours nb[c],
+// c = c0 + 2 c1 the half in each transverse dimension), coarse = 0 for a fine
+// side (nb[0] the coarse neighbour, child[t] which half of its face).
+struct RefinedFace {
+  int32_t element, dir, coarse;
+  int32_t nb[4];
+  int32_t child[2];
+};
+struct RefinedMaps {
+  std::vector<int32_t> level;       // per element
+  std::vector<int32_t> slots;       // 4 per element face
+  std::vector<int32_t> sizes;       // 2 per slot: 0 Full, 1 LowerHalf, 2 UpperHalf
+  std::vector<int32_t> face_index;  // per element face: record index or -1
+  std::vector<RefinedFace> faces;
+};
+bool build_refined_domain(const DgswConfig& cfg, Domain* dom, RefinedMaps* rm,
+                          std::string* err);
+// Half-interval projections on n LGL points (n x n, row-major), parent ->
+// child interpolation and child -> parent L2 restriction, Projection.cpp.
+bool half_projections(int n, int upper, double* parent_to_child, double* child_to_parent);
+
 // Validates a configuration and builds every host-side map.  On failure
 // returns false with a message in *err.
 bool build_domain(const DgswConfig& cfg, Domain* dom, std::string* err);

@@ -22,9 +22,30 @@ struct StageLaunch {
   StageCoef coef{0.0, 0.0, 1.0};
   double gamma2 = 0.0;
   EoTable eo{};
+  // refined lattices: per element face the index of its 2:1 record (-1
+  // conforming) and the exterior w assembled for each record
+  const int32_t* face_idx = nullptr;
+  const double* wext = nullptr;
 };
 
 cudaError_t launch_stage_fp64(const StageLaunch& L, cudaStream_t s);
+
+// Exterior w = Pi - s Phi_d - gamma2 Psi of every 2:1 face of a refined
+// lattice (refined_faces.cu): the coarse neighbour's face interpolated to this
+// fine face, or the four fine faces restricted to this coarse face.
+// faces: 9 int32 per record (element, dir, coarse, nb[4], child[2]);
+// P, R: [2][n*n] half-interval prolongation and restriction.
+struct RefinedFaceLaunch {
+  int n = 0;
+  int64_t n_faces = 0;
+  const int32_t* faces = nullptr;
+  const double* P = nullptr;
+  const double* R = nullptr;
+  const double* u = nullptr;
+  double gamma2 = 0.0;
+  double* wext = nullptr;
+};
+cudaError_t launch_refined_faces(const RefinedFaceLaunch& L, cudaStream_t s);
 
 // One mixed-precision stage: W = alpha X + beta Y + c L(X) (stage_mixed.cu).
 // Exactly one of x64 (FP64 input, compensated double-float arithmetic) and

@@ -57,7 +57,8 @@ template <int N, int EPB, int MINB, int MODE>
 __global__ void __launch_bounds__(N * N * EPB, MINB)
     stage_fp64_kernel(const double* ucur, const double* u0, double* unext,
                       const int32_t* __restrict__ nbr, const double* __restrict__ jac,
-                      int64_t n_elem, StageCoef coef, double gamma2, EoTable eo) {
+                      int64_t n_elem, StageCoef coef, double gamma2, EoTable eo,
+                      const int32_t* __restrict__ face_idx, const double* __restrict__ wext) {
   using S = Shape<N>;
   constexpr int NN = S::NN, NP = S::NP, TAB = S::TAB, h = S::h, H = S::H;
   constexpr bool kBoundary = MODE != kModeVolume;
@@ -138,6 +139,13 @@ __global__ void __launch_bounds__(N * N * EPB, MINB)
           we_lo = fma(-gamma2, ucur[nlo + lo_pt], we_lo);
           wi_hi = fma(-gamma2, ucur[off + base + (N - 1) * stride], wi_hi);
           we_hi = fma(-gamma2, ucur[nhi + hi_pt], we_hi);
+        }
+        if (face_idx) {
+          // 2:1 faces: the exterior w on this face, assembled from the
+          // mortars by refined_faces.cu (face point index = line index t)
+          const int32_t flo = face_idx[6 * e + 2 * d], fhi = face_idx[6 * e + 2 * d + 1];
+          if (flo >= 0) we_lo = wext[(int64_t)flo * NN + t];
+          if (fhi >= 0) we_hi = wext[(int64_t)fhi * NN + t];
         }
         const double dw_lo = wi_lo - we_lo;
         const double dw_hi = wi_hi - we_hi;
@@ -232,7 +240,7 @@ cudaError_t launch_n(const StageLaunch& L, cudaStream_t s) {
   const int64_t blocks = (L.n_elem + EPB - 1) / EPB;
   if (blocks <= 0) return cudaSuccess;
   k<<<(unsigned)blocks, N * N * EPB, smem, s>>>(L.ucur, L.u0, L.unext, L.nbr, L.jac, L.n_elem,
-                                                 L.coef, L.gamma2, L.eo);
+                                                 L.coef, L.gamma2, L.eo, L.face_idx, L.wext);
   return cudaGetLastError();
 }
 

@@ -53,6 +53,11 @@ class DgswBrick(ctypes.Structure):
                 ("elements", ctypes.c_int32 * 3)]
 
 
+class DgswRefinedBrick(ctypes.Structure):
+    _fields_ = [("lower", ctypes.c_double * 3), ("upper", ctypes.c_double * 3),
+                ("blocks", ctypes.c_int32 * 3), ("levels", ctypes.POINTER(ctypes.c_int32))]
+
+
 class DgswShell(ctypes.Structure):
     _fields_ = [("inner_radius", ctypes.c_double), ("outer_radius", ctypes.c_double),
                 ("refinement_angular", ctypes.c_int32), ("refinement_radial", ctypes.c_int32),
@@ -67,7 +72,8 @@ class DgswConfig(ctypes.Structure):
                 ("points_per_element", ctypes.POINTER(ctypes.c_int32)),
                 ("uniform_points", ctypes.c_int32), ("gamma2", ctypes.c_double),
                 ("device", ctypes.c_int32), ("shell", ctypes.POINTER(DgswShell)),
-                ("quadrature", ctypes.c_int32)]
+                ("quadrature", ctypes.c_int32),
+                ("refined", ctypes.POINTER(DgswRefinedBrick))]
 
 
 SYSTEM_SCALAR_WAVE = 0
@@ -113,6 +119,8 @@ _SIGNATURES = {
                                  ctypes.POINTER(_I64)]),
     "dgsw_shell_geometry": (_I, [ctypes.POINTER(DgswConfig), _P, _P, _P]),
     "dgsw_gauss_spectral": (_I, [_I, _P, _P, _P, _P, _P, _P, _P]),
+    "dgsw_refined_mortars": (_I, [ctypes.POINTER(DgswConfig), _P, _P]),
+    "dgsw_half_projections": (_I, [_I, _I, _P, _P]),
     "dgsw_adjoint_rhs_device": (_I, [_P, _P, _P]),
     "dgsw_set_samples": (_I, [_P, _I, _P]),
     "dgsw_sample_psi": (_I, [_P, _P]),
@@ -232,6 +240,17 @@ class Brick:
 
 
 @dataclass
+class RefinedBrick:
+    """Periodic lattice of blocks on [lower, upper]^3 (blocks x fastest); block
+    k has 2^levels[k] elements per axis; face-sharing blocks differ by at most
+    one level (h-nonconforming 2:1 mortars)."""
+    blocks: Sequence[int]
+    levels: Sequence[int]
+    lower: Sequence[float] = (0.0, 0.0, 0.0)
+    upper: Sequence[float] = (2 * math.pi, 2 * math.pi, 2 * math.pi)
+
+
+@dataclass
 class Shell:
     """Spherical shell of six cubed-sphere wedges (Domain::Creators::Sphere
     without its interior) on a Schwarzschild background in Kerr-Schild
@@ -252,6 +271,16 @@ class _ConfigHolder:
     def __init__(self, bricks, points, precision=PRECISION_FP64, gamma2=0.0, device=0,
                  quadrature="gauss_lobatto"):
         self.shell = None
+        self.refined = None
+        if isinstance(bricks, RefinedBrick):
+            rb = bricks
+            self.levels = np.ascontiguousarray(rb.levels, dtype=np.int32).ravel()
+            self.refined = DgswRefinedBrick()
+            self.refined.lower[:] = [float(v) for v in rb.lower]
+            self.refined.upper[:] = [float(v) for v in rb.upper]
+            self.refined.blocks[:] = [int(v) for v in rb.blocks]
+            self.refined.levels = self.levels.ctypes.data_as(ctypes.POINTER(ctypes.c_int32))
+            bricks = []
         if isinstance(bricks, Shell):
             sh = bricks
             self.shell = DgswShell(float(sh.inner_radius), float(sh.outer_radius),
@@ -275,7 +304,7 @@ class _ConfigHolder:
         self.cfg.boundary_correction = 0
         self.cfg.time_stepper = 0
         self.cfg.precision = precision
-        self.cfg.n_instances = 1 if self.shell else len(bricks)
+        self.cfg.n_instances = 1 if (self.shell or self.refined) else len(bricks)
         self.cfg.bricks = ctypes.cast(self.bricks, ctypes.POINTER(DgswBrick))
         self.cfg.points_per_element = (
             self.points.ctypes.data_as(ctypes.POINTER(ctypes.c_int32))
@@ -285,6 +314,27 @@ class _ConfigHolder:
         self.cfg.device = device
         self.cfg.shell = ctypes.pointer(self.shell) if self.shell else None
         self.cfg.quadrature = QUADRATURES[quadrature]
+        self.cfg.refined = ctypes.pointer(self.refined) if self.refined else None
+
+
+def refined_mortars(refined: "RefinedBrick", points: int):
+    """(neighbour slots [E, 6, 4], mortar sizes [E, 6, 4, 2]: 0 Full,
+    1 LowerHalf, 2 UpperHalf) of a refined lattice."""
+    h = _ConfigHolder(refined, points)
+    ne, nd = _I64(), _I64()
+    _check(lib().dgsw_count_elements(ctypes.byref(h.cfg), ctypes.byref(ne), ctypes.byref(nd)))
+    E = ne.value
+    slots = np.zeros((E, 6, 4), dtype=np.int32)
+    sizes = np.zeros((E, 6, 4, 2), dtype=np.int32)
+    _check(lib().dgsw_refined_mortars(ctypes.byref(h.cfg), _ptr(slots), _ptr(sizes)))
+    return slots, sizes
+
+
+def half_projections(n: int, upper: bool):
+    """(parent -> child interpolation, child -> parent restriction), n x n."""
+    P, R = np.zeros((n, n)), np.zeros((n, n))
+    _check(lib().dgsw_half_projections(n, int(upper), _ptr(P), _ptr(R)))
+    return P, R
 
 
 def shell_geometry(shell: "Shell", points: int):
@@ -411,7 +461,7 @@ class DgEvolution:
         self.n_elements = ne.value
         self.state_size = nd.value
         self.grid_points = npt.value
-        self.bricks = [] if isinstance(bricks, Shell) else list(bricks)
+        self.bricks = [] if isinstance(bricks, (Shell, RefinedBrick)) else list(bricks)
         self.points = points
         self.precision = precision
         self.gamma2 = gamma2

@@ -45,6 +45,14 @@ BYTES_PER_POINT_LAUNCH = (80.0 + 120.0 + 120.0) / 3.0
 # d1 and writes s2 (20 + 20 B); stage 3 reads s2, d1 (FP32) and u0, and
 # writes u (20 + 20 + 40 + 40 B).
 MIXED_BYTES_PER_POINT_LAUNCH = (60.0 + 40.0 + 120.0) / 3.0
+# DRAM traffic (read + write) per grid point per stage launch measured by ncu
+# on the 20^3 x 8^3 case (profiles/stage_fp64_N8_20cube.md: 287.4, 467.5 and
+# 452.1 MB for the three stages of 4,096,000 points; and
+# profiles/stage_mixed_pipe_N8_20cube.md: 180.5 + 120.3 + 204.1 + 355.4 MB for
+# the three mixed stages and the FP64 accumulate, per three stage launches).
+# Traffic grows with the points, so the 32^3 figure is this times its points.
+FP64_TRAFFIC_PER_POINT_LAUNCH = 1207.0e6 / 3 / 4096000
+MIXED_TRAFFIC_PER_POINT_LAUNCH = 860.3e6 / 3 / 4096000
 # FP64 pipe instructions per point per stage of the plain kernel at N = 8
 # (even/odd contraction 6 per derivative x 6, dt Pi sum 2, RK update 5-11,
 # face corrections ~3.75); the ncu capture of the 20^3 case measured
@@ -467,7 +475,10 @@ def run_ours(args):
                  "rel_l2_vs_fp64_after_steps": err, "steps_compared": warm + args.steps,
                  "dtype": "f32 split-product contractions, f64 state and step accumulation",
                  "roofline": {"bound": "hbm", "achieved": gbs_m, "peak": hbm, "unit": "GB/s",
-                              "frac": gbs_m / hbm, "traffic": None,
+                              "frac": gbs_m / hbm,
+                              "traffic": MIXED_TRAFFIC_PER_POINT_LAUNCH * points,
+                              "traffic_note": "ncu DRAM bytes per stage launch, 20^3 capture "
+                                              "scaled by points",
                               "bytes_per_point_launch": MIXED_BYTES_PER_POINT_LAUNCH,
                               "avg_launch_ms": launch_m}}
 
@@ -498,7 +509,10 @@ def run_ours(args):
             "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f64",
             "data": "synthetic", "config": workload_config(args.elements),
             "roofline": {"bound": "hbm", "achieved": achieved_gbs, "peak": hbm, "unit": "GB/s",
-                         "frac": achieved_gbs / hbm, "traffic": None,
+                         "frac": achieved_gbs / hbm,
+                         "traffic": FP64_TRAFFIC_PER_POINT_LAUNCH * points,
+                         "traffic_note": "ncu DRAM bytes per launch, 20^3 capture scaled by "
+                                         "points",
                          "peak_source": peak_kind,
                          "bytes_per_point_launch": BYTES_PER_POINT_LAUNCH,
                          "avg_launch_ms": launch_ms},

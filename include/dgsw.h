@@ -212,6 +212,18 @@ int dgsw_boundary_terms_device(int64_t npts, const double* packaged_int,
 int dgsw_step(DgswHandle h, int n_steps, double dt);
 int dgsw_substep(DgswHandle h, int k, double dt);
 
+/* ---- launch autotuner -------------------------------------------------------
+ * The plain FP64 stage kernel exists in two launch configurations per N
+ * (elements per block, resident blocks per SM).  The first dgsw_step of a
+ * handle times both on the handle's own data (without touching its state),
+ * keeps the faster and reuses the choice for handles of the same shape.
+ * dgsw_autotune re-runs the timing now and returns the chosen variant and
+ * the measured ms per stage launch of each (zeros where nothing is tuned:
+ * mixed, curved, Gauss and mixed-extent handles use fixed configurations);
+ * force_variant 0 or 1 then imposes that variant (-1 keeps the faster).
+ * No counterpart in the reference. */
+int dgsw_autotune(DgswHandle h, int force_variant, int* variant, double* ms_per_launch);
+
 /* ---- diagnostics -------------------------------------------------------------
  * dgsw_check_device_timeout: runs the mixed-precision pipeline's bounded
  * device-side wait on an mbarrier that no copy ever completes, with the given

@@ -9,6 +9,8 @@
 #include <cmath>
 #include <cstdio>
 #include <cstring>
+#include <map>
+#include <mutex>
 #include <new>
 #include <string>
 #include <vector>
@@ -79,6 +81,10 @@ struct DgswHandle_ {
   float* c_T32 = nullptr;
   float* c_F32 = nullptr;
   int32_t* c_X = nullptr;
+  // launch autotuner: the FP64 stage's launch-configuration variant
+  bool tuned = false;
+  int stage_variant = 0;
+  double tune_ms[2] = {0.0, 0.0};
   // refined block lattice (h-nonconforming 2:1 faces)
   bool refined = false;
   DgswRefinedBrick rbrick{};
@@ -161,6 +167,7 @@ StageLaunch base_launch(DgswHandle h) {
     L.face_idx = h->r_face_idx;
     L.wext = h->r_wext;
   }
+  L.variant = h->stage_variant;
   return L;
 }
 
@@ -416,6 +423,68 @@ cudaError_t apply_filter(DgswHandle h, double* u) {
   F.n_tasks = h->dom.n_elem;
   F.F = h->filt + (size_t)F.n * kMaxN * kMaxN;
   return launch_filter(F, h->stream);
+}
+
+// ---- launch autotuner ------------------------------------------------------
+// The FP64 stage kernel is compiled in two launch configurations per N
+// (elements per block and resident blocks asked of the register allocator).
+// Before the first step the handle times both on its own data (the stage
+// input copied to t1, output to t2: the state is untouched) and keeps the
+// faster; the choice is cached per (N, elements) for later handles.
+bool tunable(DgswHandle h) { return !mixed(h) && !h->curved && !h->gauss && !h->general; }
+
+std::mutex g_tune_mu;
+std::map<std::pair<int, int64_t>, int> g_tuned;
+
+int autotune(DgswHandle h, bool force) {
+  if (!tunable(h) || (h->tuned && !force)) return DGSW_OK;
+  const std::pair<int, int64_t> key(h->dom.elem_n[0], h->dom.n_elem);
+  if (!force) {
+    std::lock_guard<std::mutex> lk(g_tune_mu);
+    auto it = g_tuned.find(key);
+    if (it != g_tuned.end()) {
+      h->stage_variant = it->second;
+      h->tuned = true;
+      return DGSW_OK;
+    }
+  }
+  const size_t bytes = h->dom.offset.back() * sizeof(double);
+  DGSW_CUDA(h, cudaMemcpyAsync(h->t1, h->state, bytes, cudaMemcpyDeviceToDevice, h->stream));
+  cudaEvent_t e0, e1;
+  DGSW_CUDA(h, cudaEventCreate(&e0));
+  DGSW_CUDA(h, cudaEventCreate(&e1));
+  float best = -1.0f;
+  int choice = 0;
+  cudaError_t err = cudaSuccess;
+  for (int v = 0; v < 2 && err == cudaSuccess; ++v) {
+    StageLaunch L = base_launch(h);
+    L.variant = v;
+    L.mode = kModeStage;
+    L.ucur = h->t1;
+    L.u0 = h->state;
+    L.unext = h->t2;
+    L.coef = {0.75, 0.25, 1e-4};
+    err = launch_stage(h, L);  // warm-up (attributes, caches)
+    if (err == cudaSuccess) err = cudaEventRecord(e0, h->stream);
+    for (int r = 0; r < 3 && err == cudaSuccess; ++r) err = launch_stage(h, L);
+    if (err == cudaSuccess) err = cudaEventRecord(e1, h->stream);
+    if (err == cudaSuccess) err = cudaEventSynchronize(e1);
+    float ms = 0.0f;
+    if (err == cudaSuccess) err = cudaEventElapsedTime(&ms, e0, e1);
+    h->tune_ms[v] = ms / 3.0;
+    if (err == cudaSuccess && (best < 0.0f || ms < best)) {
+      best = ms;
+      choice = v;
+    }
+  }
+  cudaEventDestroy(e0);
+  cudaEventDestroy(e1);
+  if (err != cudaSuccess) return cuda_fail(h, err, "autotune");
+  h->stage_variant = choice;
+  h->tuned = true;
+  std::lock_guard<std::mutex> lk(g_tune_mu);
+  g_tuned[key] = choice;
+  return DGSW_OK;
 }
 
 // Reads and clears the device error word; DGSW_ERR_DEVICE_TIMEOUT when set.
@@ -1369,6 +1438,24 @@ int dgsw_observe_plane_wave_errors(DgswHandle h, const double* k, double t, doub
   return observe_norms(h, h->state, h->t1, out);
 }
 
+int dgsw_autotune(DgswHandle h, int force_variant, int* variant, double* ms_per_launch) {
+  if (!h) return fail(nullptr, DGSW_ERR_ARGUMENT, "null handle");
+  if (force_variant < -1 || force_variant > 1)
+    return fail(h, DGSW_ERR_ARGUMENT, "force_variant must be -1, 0 or 1");
+  if (int rc = select_device(h)) return rc;
+  if (tunable(h)) {
+    destroy_graphs(h);
+    if (int rc = autotune(h, true)) return rc;
+    if (force_variant >= 0) h->stage_variant = force_variant;
+  }
+  if (variant) *variant = h->stage_variant;
+  if (ms_per_launch) {
+    ms_per_launch[0] = h->tune_ms[0];
+    ms_per_launch[1] = h->tune_ms[1];
+  }
+  return DGSW_OK;
+}
+
 int dgsw_check_device_timeout(DgswHandle h, double limit_seconds) {
   if (!h) return fail(nullptr, DGSW_ERR_ARGUMENT, "null handle");
   if (!(limit_seconds > 0.0) || limit_seconds > 10.0)
@@ -1420,6 +1507,10 @@ int dgsw_step(DgswHandle h, int n_steps, double dt) {
   if (n_steps < 0 || !std::isfinite(dt)) return fail(h, DGSW_ERR_ARGUMENT, "bad step arguments");
   if (n_steps == 0) return DGSW_OK;
   if (int rc = select_device(h)) return rc;
+  if (!h->tuned && tunable(h)) {
+    destroy_graphs(h);
+    if (int rc = autotune(h, false)) return rc;
+  }
   if (!(h->graph_dt == dt)) {
     destroy_graphs(h);
     DGSW_CUDA(h, capture_steps(h, dt, 1, &h->graph_one));

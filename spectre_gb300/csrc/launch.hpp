@@ -26,6 +26,7 @@ struct StageLaunch {
   // conforming) and the exterior w assembled for each record
   const int32_t* face_idx = nullptr;
   const double* wext = nullptr;
+  int variant = 0;  // launch-configuration candidate of the stage modes (0 or 1)
 };
 
 cudaError_t launch_stage_fp64(const StageLaunch& L, cudaStream_t s);

@@ -216,20 +216,26 @@ __global__ void __launch_bounds__(N * N * EPB, MINB)
 // register allocator: chosen per N so that no variant spills and several
 // blocks share an SM (one block's global loads and barriers overlap another
 // block's FP64 work).
-template <int N>
+//
+// Variant 1, a candidate of the launch autotuner (StageLaunch::variant, timed
+// on the handle's own data by dgsw_autotune), halves the elements per block
+// and doubles the resident blocks asked for.
+template <int N, int V>
 constexpr int elems_per_block() {
-  return N <= 4 ? 16 : (N <= 6 ? 8 : (N == 7 ? 4 : (N <= 11 ? 2 : 1)));
+  constexpr int e = N <= 4 ? 16 : (N <= 6 ? 8 : (N == 7 ? 4 : (N <= 11 ? 2 : 1)));
+  return V == 0 ? e : (e > 1 ? e / 2 : 1);
 }
-template <int N>
+template <int N, int V>
 constexpr int min_blocks() {
-  return N <= 5 ? 2 : (N == 8 ? 3 : 1);
+  constexpr int m = N <= 5 ? 2 : (N == 8 ? 3 : 1);
+  return V == 0 ? m : (2 * m > 8 ? 8 : 2 * m);
 }
 
-template <int N, int MODE>
+template <int N, int MODE, int V = 0>
 cudaError_t launch_n(const StageLaunch& L, cudaStream_t s) {
-  constexpr int EPB = elems_per_block<N>();
+  constexpr int EPB = elems_per_block<N, V>();
   const size_t smem = (size_t)EPB * Shape<N>::SLOT * sizeof(double);
-  auto k = stage_fp64_kernel<N, EPB, min_blocks<N>(), MODE>;
+  auto k = stage_fp64_kernel<N, EPB, min_blocks<N, V>(), MODE>;
   cudaError_t err = cudaFuncSetAttribute(k, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
   if (err != cudaSuccess) return err;
   // two resident blocks per SM overlap one block's loads and barriers with
@@ -249,8 +255,10 @@ cudaError_t launch_mode(const StageLaunch& L, cudaStream_t s) {
   switch (L.mode) {
     case kModeRhs: return launch_n<N, kModeRhs>(L, s);
     case kModeVolume: return launch_n<N, kModeVolume>(L, s);
-    case kModeStageFirst: return launch_n<N, kModeStageFirst>(L, s);
-    case kModeStage: return launch_n<N, kModeStage>(L, s);
+    case kModeStageFirst:
+      return L.variant ? launch_n<N, kModeStageFirst, 1>(L, s) : launch_n<N, kModeStageFirst>(L, s);
+    case kModeStage:
+      return L.variant ? launch_n<N, kModeStage, 1>(L, s) : launch_n<N, kModeStage>(L, s);
     default: return cudaErrorInvalidValue;
   }
 }

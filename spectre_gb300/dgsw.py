@@ -108,6 +108,7 @@ _SIGNATURES = {
     "dgsw_set_exponential_filter": (_I, [_P, _D, _I, _I]),
     "dgsw_observe_norms": (_I, [_P, _P, _P, _P]),
     "dgsw_check_device_timeout": (_I, [_P, _D]),
+    "dgsw_autotune": (_I, [_P, _I, ctypes.POINTER(_I), _P]),
     "dgsw_observe_plane_wave_errors": (_I, [_P, _P, _D, _P]),
     "dgsw_exponential_filter_matrix": (_I, [_I, _D, _I, _P]),
     "dgsw_substep": (_I, [_P, _I, _D]),
@@ -555,6 +556,16 @@ class DgEvolution:
     def substep(self, k: int, dt: float):
         _check(lib().dgsw_substep(self._h, int(k), float(dt)), self._h)
         self.synchronize()
+
+    def autotune(self, force_variant: int = -1):
+        """Re-times the FP64 stage's launch variants on this handle; returns
+        (chosen variant, [ms per launch of each]).  force_variant 0 / 1
+        imposes a variant afterwards."""
+        v = _I()
+        ms = np.zeros(2)
+        _check(lib().dgsw_autotune(self._h, int(force_variant), ctypes.byref(v), _ptr(ms)),
+               self._h)
+        return v.value, ms
 
     def check_device_timeout(self, limit_seconds: float = 0.05) -> int:
         """Runs the bounded device wait on a barrier nothing completes; returns

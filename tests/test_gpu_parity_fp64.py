@@ -244,3 +244,19 @@ def test_errors_are_reported_not_fatal():
         with pytest.raises(dgsw.DgswError):
             ev.set_initial_data("gaussian", [1.0, -1.0, 0, 0, 0])
         ev.step(1, 1e-3)  # the handle stays usable
+
+
+def test_autotuned_variants_agree(oracle):
+    # both launch configurations of the FP64 stage match the oracle
+    bricks = [Brick((3, 2, 4))]
+    for n in (4, 8, 11):
+        u = random_state(np.random.default_rng(n), bricks, n, oracle)
+        ref = oracle.evolve(bricks, n, u, 1e-3, 2)
+        for force in (0, 1):
+            with DgEvolution(bricks, n) as ev:
+                ev.set_state(u)
+                v, ms = ev.autotune(force)
+                assert v == force and (ms > 0).all()
+                ev.step(2, 1e-3)
+                got = ev.get_state()
+            assert rel_err_per_var(got, ref, oracle.elem_points(bricks, n)) <= 1e-12

@@ -1,7 +1,7 @@
 """h-nonconforming refined block lattices through the C ABI.
 
 CPU: element ids, neighbour slots and mortar sizes bit-exact with the oracle;
-half-interval projections within 2e-15 of the oracle's.  GPU: FP64
+half-interval projections within 1e-14 of the oracle's.  GPU: FP64
 right-hand side on random states (2:1 faces in every direction, with and
 without gamma2) and steps against the oracle (<= 1e-12 / 1e-11 relative per
 variable); a smooth plane wave converges across the 2:1 faces."""
@@ -40,8 +40,10 @@ def test_half_projections_match_oracle(dgsw_lib, oracle, n):
     for up in (0, 1):
         P, R = dgsw.half_projections(n, up)
         oP, oR = oracle.proj_half(n, up)
-        np.testing.assert_allclose(P, oP, rtol=0, atol=2e-15)
-        np.testing.assert_allclose(R, oR, rtol=0, atol=2e-15)
+        # different FMA contraction on different hosts: a few ulps of the
+        # largest entry
+        np.testing.assert_allclose(P, oP, rtol=0, atol=1e-14)
+        np.testing.assert_allclose(R, oR, rtol=0, atol=1e-14)
 
 
 def _rel(a, b, n):

@@ -1,0 +1,547 @@
+// adams_oracle.cpp -- CPU FP64 restatement of SpECTRE's Adams-Bashforth time
+// stepper with local time stepping (test infrastructure only; part of the
+// oracle library, never linked by the product).
+//
+// Follows (file:line relative to the SpECTRE source tree):
+//   constant AB coefficients     src/Time/TimeSteppers/AdamsCoefficients.cpp:20-47
+//   variable_coefficients        src/Time/TimeSteppers/AdamsCoefficients.cpp:73-117
+//   coefficients (dispatcher)    src/Time/TimeSteppers/AdamsCoefficients.hpp:29-67
+//   find_relevant_ids            src/Time/TimeSteppers/AdamsLts.cpp:178-210
+//   merge_to_small_steps         src/Time/TimeSteppers/AdamsLts.cpp:212-272 (explicit)
+//   interpolation_coefficients   src/Time/TimeSteppers/AdamsLts.cpp:274-299
+//   lts_coefficients(_for_gts)   src/Time/TimeSteppers/AdamsLts.cpp:301-415
+//   AB update / clean / boundary src/Time/TimeSteppers/AdamsBashforth.cpp:131-330
+//   self-start procedure         src/Time/Actions/SelfStartActions.hpp:136-482,
+//                                src/Time/SelfStart.cpp:9-17
+//   LTS DG step                  src/Evolution/DiscontinuousGalerkin/Actions/
+//                                ComputeTimeDerivative.hpp:642-645,776-840 (record +
+//                                volume update), ApplyBoundaryCorrections.hpp:
+//                                816-1011 (coupling, add_boundary_delta,
+//                                add_slice_to_data), src/Time/TakeStep.hpp:36-61,
+//                                src/Time/Actions/CleanHistory.hpp:63-130
+//
+// Times are exact: an integer tick count, a slab being ticks_per_slab ticks,
+// converted to double the way the reference's Time/TimeDelta do
+// (src/Time/Time.cpp:96-118: slab duration times the reduced fraction).
+#include <algorithm>
+#include <cmath>
+#include <cstdint>
+#include <cstring>
+#include <deque>
+#include <vector>
+
+#include "dgsw_oracle.h"
+
+namespace {
+
+constexpr int kMaxOrder = 8;
+
+// Adams-Bashforth coefficients for constant steps, oldest first, as exact
+// rationals over a common denominator (the standard table; equal to the
+// reference's values, AdamsCoefficients.cpp:20-47).
+const double kAbNum[kMaxOrder][kMaxOrder] = {
+    {1},
+    {-1, 3},
+    {5, -16, 23},
+    {-9, 37, -59, 55},
+    {251, -1274, 2616, -2774, 1901},
+    {-475, 2877, -7298, 9982, -7923, 4277},
+    {19087, -134472, 407139, -688256, 705549, -447288, 198721},
+    {-36799, 295767, -1041723, 2102243, -2664477, 2183877, -1152169, 434241}};
+const double kAbDen[kMaxOrder] = {1, 2, 12, 24, 720, 1440, 60480, 120960};
+
+struct Clock {
+  double slab;     // slab duration
+  int64_t ticks;   // ticks per slab
+  double t0;       // initial time
+  double delta(int64_t d) const { return slab * ((double)d / (double)ticks); }
+  double value(int64_t t) const {
+    // Time::compute_value on the slab containing t
+    const int64_t m = t >= 0 ? t / ticks : -((-t + ticks - 1) / ticks);
+    const int64_t r = t - m * ticks;
+    const double start = t0 + slab * (double)m, end = t0 + slab * (double)(m + 1);
+    return ((double)(ticks - r) / (double)ticks) * start + ((double)r / (double)ticks) * end;
+  }
+};
+
+std::vector<double> variable_coefficients(std::vector<double> ct, double start, double end) {
+  for (double& t : ct) t -= start;
+  const size_t order = ct.size();
+  std::vector<double> out;
+  for (size_t j = 0; j < order; ++j) {
+    // Lagrange polynomial l_j in monomial form, built one factor at a time
+    std::vector<double> poly(order, 0.0);
+    poly[0] = 1.0;
+    for (size_t m = 0; m < order; ++m) {
+      if (m == j) continue;
+      const double denom = 1.0 / (ct[j] - ct[m]);
+      for (size_t i = m < j ? m + 1 : m; i > 0; --i) poly[i] = (poly[i - 1] - poly[i] * ct[m]) * denom;
+      poly[0] *= -ct[m] * denom;
+    }
+    // integral from 0 (the step start) to end - start, Horner from the top
+    for (size_t m = 0; m < order; ++m) poly[m] /= (double)(m + 1);
+    const double x = end - start;
+    double acc = 0.0;
+    for (size_t m = order; m-- > 0;) acc = acc * x + poly[m];
+    out.push_back(x * acc);
+  }
+  return out;
+}
+
+std::vector<double> coefficients(const std::vector<int64_t>& times, int64_t start, int64_t end,
+                                 const Clock& clk) {
+  if (times.empty()) return {};
+  const double step = clk.delta(end - start);
+  bool constant = true;
+  std::vector<double> ct{0.0};
+  int64_t prev = times[0];
+  for (size_t i = 1; i < times.size(); ++i) {
+    ct.push_back(ct.back() + clk.delta(times[i] - prev));
+    if (times[i] - prev != end - start) constant = false;
+    prev = times[i];
+  }
+  if (constant && start == prev) {
+    const size_t k = times.size();
+    std::vector<double> out(k);
+    for (size_t i = 0; i < k; ++i) out[i] = (kAbNum[k - 1][i] / kAbDen[k - 1]) * step;
+    return out;
+  }
+  return variable_coefficients(ct, ct.back() + clk.delta(start - prev),
+                               ct.back() + clk.delta(end - prev));
+}
+
+struct Id {
+  int64_t slab;
+  int64_t tick;
+  bool operator<(const Id& o) const { return slab < o.slab || (slab == o.slab && tick < o.tick); }
+  bool operator==(const Id& o) const { return slab == o.slab && tick == o.tick; }
+};
+
+struct Term {
+  int32_t local, remote;  // indices into the local / remote histories
+  double coef;
+};
+
+int find_relevant(const std::vector<Id>& ids, int64_t end, int order, int* first) {
+  int used_end = (int)ids.size();
+  while (used_end > 0) {
+    if (ids[used_end - 1].tick < end) break;
+    --used_end;
+  }
+  if (used_end < order) return -1;  // "Insufficient past data"
+  *first = used_end - order;
+  return 0;
+}
+
+std::vector<double> interpolation_coefficients(const std::vector<int64_t>& ct, int64_t t,
+                                               const Clock& clk) {
+  std::vector<double> out(ct.size(), 0.0);
+  for (size_t i = 0; i < ct.size(); ++i)
+    if (ct[i] == t) {
+      out[i] = 1.0;
+      return out;
+    }
+  const double x = clk.value(t);
+  for (size_t i = 0; i < ct.size(); ++i) {
+    const double xi = clk.value(ct[i]);
+    double r = 1.0;
+    for (size_t m = 0; m < ct.size(); ++m) {
+      if (m == i) continue;
+      const double xm = clk.value(ct[m]);
+      r *= (xm - x) / (xm - xi);
+    }
+    out[i] = r;
+  }
+  return out;
+}
+
+// lts_coefficients for explicit schemes of orders lo (local side), ro
+// (remote side) and so (small steps); AdamsBashforth::add_boundary_delta_impl
+// (AdamsBashforth.cpp:264-281) uses one order for all three.
+int lts_coefficients(const std::vector<Id>& local, const std::vector<Id>& remote, int64_t start,
+                     int64_t end, int lo, int ro, int so, const Clock& clk,
+                     std::vector<Term>* out) {
+  out->clear();
+  if (start == end) return 0;
+  std::vector<Term> terms;
+  int64_t small_end = end;
+  for (;;) {
+    int lf, rf;
+    if (find_relevant(local, small_end, lo, &lf) || find_relevant(remote, small_end, ro, &rf))
+      return -1;
+    bool same = terms.empty() && lo == ro && lo == so;
+    for (int i = 0; same && i < lo; ++i) same = local[lf + i] == remote[rf + i];
+    if (same) {
+      std::vector<int64_t> t(lo);
+      for (int i = 0; i < lo; ++i) t[i] = local[lf + i].tick;
+      const std::vector<double> c = coefficients(t, start, end, clk);
+      for (int i = 0; i < lo; ++i) out->push_back({lf + i, rf + i, c[i]});
+      return 0;
+    }
+    std::vector<int64_t> lt(lo), rt(ro);
+    for (int i = 0; i < lo; ++i) lt[i] = local[lf + i].tick;
+    for (int i = 0; i < ro; ++i) rt[i] = remote[rf + i].tick;
+    // merge_to_small_steps: newest first, the later of the two sides each time
+    std::vector<int64_t> small(so);
+    int li = lo - 1, ri = ro - 1;
+    for (int o = so - 1; o >= 0; --o) {
+      if (li < 0 && ri < 0) return -1;  // "Ran out of data"
+      if (li < 0) {
+        small[o] = rt[ri--];
+      } else if (ri < 0) {
+        small[o] = lt[li--];
+      } else {
+        const int64_t m = std::max(lt[li], rt[ri]);
+        small[o] = m;
+        if (lt[li] == m) --li;
+        if (rt[ri] == m) --ri;
+      }
+    }
+    const int64_t current = small[so - 1];
+    if (current < start) return -2;
+    const std::vector<double> sc = coefficients(small, current, small_end, clk);
+    for (int s = 0; s < so; ++s) {
+      const std::vector<double> lic = interpolation_coefficients(lt, small[s], clk);
+      const std::vector<double> ric = interpolation_coefficients(rt, small[s], clk);
+      for (int a = 0; a < lo; ++a) {
+        if (lic[a] == 0.0) continue;
+        for (int b = 0; b < ro; ++b) {
+          if (ric[b] == 0.0) continue;
+          terms.push_back({lf + a, rf + b, sc[s] * lic[a] * ric[b]});
+        }
+      }
+    }
+    if (current == start) break;
+    small_end = current;
+  }
+  // sort by (local id, remote id, value) and combine duplicates in order
+  std::sort(terms.begin(), terms.end(), [&](const Term& x, const Term& y) {
+    if (!(local[x.local] == local[y.local])) return local[x.local] < local[y.local];
+    if (!(remote[x.remote] == remote[y.remote])) return remote[x.remote] < remote[y.remote];
+    return x.coef < y.coef;
+  });
+  for (const Term& t : terms) {
+    if (!out->empty() && local[out->back().local] == local[t.local] &&
+        remote[out->back().remote] == remote[t.remote])
+      out->back().coef += t.coef;
+    else
+      out->push_back(t);
+  }
+  return 0;
+}
+
+}  // namespace
+
+// ---------------------------------------------------------------------------
+// Flat scalar wave on conforming periodic bricks, uniform extent n, stepped by
+// AdamsBashforth with local time stepping.  Every element keeps the
+// reference's three histories: the volume history of dt u (no boundary
+// terms), and per mortar the local and remote boundary histories of packaged
+// face data (dg_package_data).  A step records dt u and the face data,
+// updates u with the volume part at once, adds the boundary delta when the
+// step ends, then cleans the histories.
+namespace {
+
+constexpr int kPkgA = 16;  // packaged doubles per face point
+constexpr int kVarsA = 5;
+
+struct LocalEntry {
+  Id id;
+  int order;
+  std::vector<double> pkg, mag;
+};
+struct RemoteEntry {
+  Id id;
+  std::vector<double> pkg;
+};
+struct VolEntry {
+  Id id;
+  int order;
+  std::vector<double> dt;
+};
+struct Mortar {
+  std::deque<LocalEntry> local;
+  std::deque<RemoteEntry> remote;
+};
+struct Elem {
+  std::deque<VolEntry> vol;
+  Mortar mortar[6];
+  int64_t start = 0, end = 0;
+};
+
+int64_t face_volume_index(int n, int d, int slice, int a, int b) {
+  switch (d) {
+    case 0: return slice + (int64_t)n * (a + (int64_t)n * b);
+    case 1: return a + (int64_t)n * (slice + (int64_t)n * b);
+    default: return a + (int64_t)n * (b + (int64_t)n * slice);
+  }
+}
+
+struct LtsRun {
+  int n_inst;
+  const OrcBrick* br;
+  int n;
+  int64_t E, np;
+  double gamma2;
+  int threads;
+  std::vector<int32_t> elem_n, nbr, inst;
+  std::vector<double> invjac;  // 3 per element
+  std::vector<Elem> el;
+  Clock clk;
+
+  // the face package of element e in direction dir (outward normal)
+  void package(const double* u, int64_t e, int dir, std::vector<double>* pkg,
+               std::vector<double>* mag) const {
+    const int d = dir / 2, nf = n * n;
+    const bool upper = dir % 2;
+    const int slice = upper ? n - 1 : 0;
+    const double* ue = u + e * kVarsA * np;
+    std::vector<double> psi(nf), pi(nf), phi(3 * nf), g2(nf, gamma2), nrm(3 * nf, 0.0);
+    mag->assign(nf, invjac[3 * e + d]);
+    for (int b = 0; b < n; ++b)
+      for (int a = 0; a < n; ++a) {
+        const int f = a + n * b;
+        const int64_t v = face_volume_index(n, d, slice, a, b);
+        psi[f] = ue[v];
+        pi[f] = ue[np + v];
+        for (int i = 0; i < 3; ++i) phi[i * nf + f] = ue[(2 + i) * np + v];
+        nrm[d * nf + f] = upper ? 1.0 : -1.0;
+      }
+    pkg->assign((size_t)kPkgA * nf, 0.0);
+    double ms;
+    orc_package(nf, psi.data(), pi.data(), phi.data(), g2.data(), nrm.data(), nullptr, pkg->data(),
+                &ms);
+  }
+
+  // ComputeTimeDerivative for the listed elements: dt u (volume terms only)
+  // into the volume history, face packages into the own local and the
+  // neighbours' remote boundary histories.
+  void record(const double* u, const std::vector<int64_t>& who, Id id, int order) {
+    std::vector<double> dudt((size_t)E * kVarsA * np);
+    orc_volume_rhs(n_inst, br, elem_n.data(), gamma2, u, dudt.data(), threads);
+    for (int64_t e : who) {
+      VolEntry v{id, order, std::vector<double>(dudt.begin() + e * kVarsA * np,
+                                                 dudt.begin() + (e + 1) * kVarsA * np)};
+      el[e].vol.push_back(std::move(v));
+      for (int dir = 0; dir < 6; ++dir) {
+        LocalEntry le{id, order, {}, {}};
+        package(u, e, dir, &le.pkg, &le.mag);
+        el[nbr[6 * e + dir]].mortar[dir ^ 1].remote.push_back({id, le.pkg});
+        el[e].mortar[dir].local.push_back(std::move(le));
+      }
+    }
+  }
+
+  // AdamsBashforth::update_u_impl with the element's volume history
+  int volume_update(double* u, int64_t e, int64_t start, int64_t end) const {
+    const std::deque<VolEntry>& h = el[e].vol;
+    const int order = h.back().order;
+    if ((int)h.size() != order) return -3;
+    std::vector<int64_t> t;
+    for (const VolEntry& v : h) t.push_back(v.id.tick);
+    const std::vector<double> c = coefficients(t, start, end, clk);
+    double* ue = u + e * kVarsA * np;
+    for (int j = 0; j < order; ++j)
+      for (int64_t p = 0; p < kVarsA * np; ++p) ue[p] += c[j] * h[j].dt[p];
+    return 0;
+  }
+
+  // AdamsBashforth::add_boundary_delta_impl on every mortar, the coupling
+  // being the UpwindPenalty correction lifted onto the GLL face; then
+  // add_slice_to_data.
+  int boundary_delta(double* u, int64_t e, int64_t start, int64_t end) const {
+    const int nf = n * n;
+    double* ue = u + e * kVarsA * np;
+    for (int dir = 0; dir < 6; ++dir) {
+      const Mortar& m = el[e].mortar[dir];
+      std::vector<Id> lid, rid;
+      for (const LocalEntry& x : m.local) lid.push_back(x.id);
+      for (const RemoteEntry& x : m.remote) rid.push_back(x.id);
+      std::vector<Term> terms;
+      const int ord = m.local.back().order;
+      const int rc = lts_coefficients(lid, rid, start, end, ord, ord, ord, clk, &terms);
+      if (rc) return rc;
+      std::vector<double> lifted((size_t)kVarsA * nf, 0.0), bc((size_t)kVarsA * nf);
+      const double slice_factor = -0.5 * (double)(n * (n - 1));
+      for (const Term& t : terms) {
+        const LocalEntry& L = m.local[t.local];
+        orc_boundary_terms(nf, L.pkg.data(), m.remote[t.remote].pkg.data(), bc.data());
+        for (int v = 0; v < kVarsA; ++v)
+          for (int f = 0; f < nf; ++f)
+            lifted[(size_t)v * nf + f] += t.coef * (bc[(size_t)v * nf + f] * (slice_factor * L.mag[f]));
+      }
+      const int d = dir / 2, slice = (dir % 2) ? n - 1 : 0;
+      for (int b = 0; b < n; ++b)
+        for (int a = 0; a < n; ++a) {
+          const int64_t vi = face_volume_index(n, d, slice, a, b);
+          for (int v = 0; v < kVarsA; ++v) ue[v * np + vi] += lifted[(size_t)v * nf + a + n * b];
+        }
+    }
+    return 0;
+  }
+
+  // AdamsBashforth::clean_history_impl and clean_boundary_history_impl
+  void clean(int64_t e) {
+    std::deque<VolEntry>& h = el[e].vol;
+    const size_t order = (size_t)h.back().order;
+    while (h.size() >= order) h.pop_front();
+    for (int dir = 0; dir < 6; ++dir) {
+      Mortar& m = el[e].mortar[dir];
+      const size_t ob = (size_t)m.local.back().order;
+      while (m.local.size() >= ob) m.local.pop_front();
+      while (m.remote.size() > ob) m.remote.pop_front();
+    }
+  }
+};
+
+}  // namespace
+
+extern "C" {
+
+int orc_variable_coefficients(int n, const double* control_times, double step_start,
+                              double step_end, double* out) {
+  if (n < 0 || n > kMaxOrder || (n > 0 && (!control_times || !out))) return -1;
+  const std::vector<double> c =
+      variable_coefficients(std::vector<double>(control_times, control_times + n), step_start,
+                            step_end);
+  std::copy(c.begin(), c.end(), out);
+  return 0;
+}
+
+int orc_adams_coefficients(int n, const int64_t* control_ticks, int64_t step_start,
+                           int64_t step_end, double slab, int64_t ticks_per_slab, double* out) {
+  if (n < 0 || n > kMaxOrder || ticks_per_slab < 1 || (n > 0 && (!control_ticks || !out)))
+    return -1;
+  const Clock clk{slab, ticks_per_slab, 0.0};
+  const std::vector<double> c =
+      coefficients(std::vector<int64_t>(control_ticks, control_ticks + n), step_start, step_end,
+                   clk);
+  std::copy(c.begin(), c.end(), out);
+  return 0;
+}
+
+int orc_lts_coefficients(int n_local, const int64_t* local_slab, const int64_t* local_tick,
+                         int n_remote, const int64_t* remote_slab, const int64_t* remote_tick,
+                         int64_t step_start, int64_t step_end, double slab, int64_t ticks_per_slab,
+                         int local_order, int remote_order, int small_order, int max_out,
+                         int32_t* out_local, int32_t* out_remote, double* out_coef) {
+  for (int o : {local_order, remote_order, small_order})
+    if (o < 1 || o > kMaxOrder) return -1;
+  if (n_local < 0 || n_remote < 0 || ticks_per_slab < 1 || max_out < 0) return -1;
+  std::vector<Id> l(n_local), r(n_remote);
+  for (int i = 0; i < n_local; ++i) l[i] = {local_slab[i], local_tick[i]};
+  for (int i = 0; i < n_remote; ++i) r[i] = {remote_slab[i], remote_tick[i]};
+  std::vector<Term> terms;
+  const int rc = lts_coefficients(l, r, step_start, step_end, local_order, remote_order,
+                                  small_order, Clock{slab, ticks_per_slab, 0.0}, &terms);
+  if (rc) return -2;
+  if ((int)terms.size() > max_out) return -3;
+  for (size_t i = 0; i < terms.size(); ++i) {
+    out_local[i] = terms[i].local;
+    out_remote[i] = terms[i].remote;
+    out_coef[i] = terms[i].coef;
+  }
+  return (int)terms.size();
+}
+
+int orc_evolve_adams(int n_inst, const OrcBrick* br, int n, double gamma2, int order,
+                     const int32_t* levels, double slab, int n_slabs, double* u, int n_threads) {
+  if (n_inst < 1 || !br || n < 2 || n > 20 || order < 1 || order > kMaxOrder || !(slab > 0.0) ||
+      n_slabs < 0 || !u)
+    return -1;
+  LtsRun R;
+  R.n_inst = n_inst;
+  R.br = br;
+  R.n = n;
+  R.E = orc_num_elements(n_inst, br);
+  R.np = (int64_t)n * n * n;
+  R.gamma2 = gamma2;
+  R.threads = n_threads;
+  R.elem_n.assign(R.E, n);
+  R.nbr.resize(6 * R.E);
+  R.inst.resize(R.E);
+  std::vector<uint64_t> ids(R.E);
+  std::vector<int32_t> ijk(3 * R.E);
+  const int mrc = orc_index_maps(n_inst, br, ids.data(), R.nbr.data(), ijk.data(), R.inst.data());
+  if (mrc != 0 && mrc != -2) return -1;
+  R.invjac.resize(3 * R.E);
+  for (int64_t e = 0; e < R.E; ++e)
+    for (int d = 0; d < 3; ++d) {
+      const OrcBrick& b = br[R.inst[e]];
+      R.invjac[3 * e + d] = 2.0 / ((b.hi[d] - b.lo[d]) / b.n[d]);
+    }
+  int L = 0;
+  for (int64_t e = 0; e < R.E; ++e) {
+    const int l = levels ? levels[e] : 0;
+    if (l < 0 || l > 6) return -1;
+    L = std::max(L, l);
+  }
+  // ticks: a slab of order * 2^L ticks; the first real steps are
+  // slab / 2^L = order ticks, the self-start steps one tick
+  // (SelfStartActions.hpp:196-216: initial step / (values_needed + 1))
+  const int64_t S = (int64_t)order << L;
+  const int64_t first_step = S >> L;
+  // levels keep the first step until the slab boundary after which no
+  // self-start value is left in any history; there they take slab / 2^level
+  const int64_t switch_tick = (((int64_t)order - 1 + ((int64_t)1 << L) - 1) >> L) * S;
+  auto step_of = [&](int64_t e, int64_t t) -> int64_t {
+    return t < switch_tick ? first_step : (S >> (levels ? levels[e] : 0));
+  };
+  R.clk = Clock{slab, S, 0.0};
+  R.el.assign(R.E, Elem{});
+  const int64_t total = (int64_t)kVarsA * R.np * R.E;
+  std::vector<double> u0(u, u + total);
+  std::vector<int64_t> all(R.E);
+  for (int64_t e = 0; e < R.E; ++e) all[e] = e;
+  int rc = 0;
+  // self-start (SelfStartActions.hpp:471-482): for each order o < k, reset to
+  // the initial values, take o steps of one tick at order o from the slab
+  // start, and record one more (unused) value at tick o with order o + 1
+  for (int o = 1; o < order; ++o) {
+    const int64_t sn = -(int64_t)(order - o);
+    for (int j = 0; j <= o; ++j) {
+      if (j >= 1)
+        for (int64_t e : all) {
+          if ((rc = R.boundary_delta(u, e, j - 1, j))) return rc;
+          R.clean(e);
+        }
+      if (j == 0) std::copy(u0.begin(), u0.end(), u);
+      R.record(u, all, Id{sn, j}, j < o ? o : o + 1);
+      for (int64_t e : all) {
+        if (j < o) {
+          if ((rc = R.volume_update(u, e, j, j + 1))) return rc;
+        } else {
+          R.clean(e);  // the step is unused (SelfStart::step_unused)
+        }
+      }
+    }
+  }
+  if (order > 1) std::copy(u0.begin(), u0.end(), u);
+  R.record(u, all, Id{0, 0}, order);
+  for (int64_t e : all) {
+    R.el[e].start = 0;
+    R.el[e].end = step_of(e, 0);
+    if ((rc = R.volume_update(u, e, 0, R.el[e].end))) return rc;
+  }
+  const int64_t final_tick = (int64_t)n_slabs * S;
+  for (int64_t P = 1; P <= final_tick; ++P) {
+    std::vector<int64_t> fin;
+    for (int64_t e : all)
+      if (R.el[e].end == P) fin.push_back(e);
+    if (fin.empty()) continue;
+    for (int64_t e : fin) {
+      if ((rc = R.boundary_delta(u, e, R.el[e].start, P))) return rc;
+      R.clean(e);
+    }
+    if (P == final_tick) break;
+    R.record(u, fin, Id{P / S, P}, order);
+    for (int64_t e : fin) {
+      R.el[e].start = P;
+      R.el[e].end = P + step_of(e, P);
+      if ((rc = R.volume_update(u, e, P, R.el[e].end))) return rc;
+    }
+  }
+  return 0;
+}
+
+}  // extern "C"

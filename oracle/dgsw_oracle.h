@@ -259,6 +259,31 @@ int orc_shell_evolve(const OrcShell* s, double dt, int n_steps, double* u, int n
 /* ObserveNorms (as orc_observe_norms) of a shell state */
 int orc_shell_observe_norms(const OrcShell* s, const double* u, double* out);
 
+/* ---------------- Adams-Bashforth, local time stepping (f5) ---------------- */
+/* adams_oracle.cpp.  Times are integer ticks, ticks_per_slab to a slab of
+ * duration `slab` (exact, as the reference's Time).
+ * variable_coefficients: AdamsCoefficients.cpp:73-117 (n <= 8) */
+int orc_variable_coefficients(int n, const double* control_times, double step_start,
+                              double step_end, double* out);
+/* adams_coefficients::coefficients, AdamsCoefficients.hpp:29-67 */
+int orc_adams_coefficients(int n, const int64_t* control_ticks, int64_t step_start,
+                           int64_t step_end, double slab, int64_t ticks_per_slab, double* out);
+/* adams_lts::lts_coefficients for explicit schemes (AdamsLts.cpp:301-415) of
+ * orders local_order, remote_order and small_order.  Histories are (slab
+ * number, tick) ids in insertion order; the output terms index them.
+ * Returns the number of terms, or < 0. */
+int orc_lts_coefficients(int n_local, const int64_t* local_slab, const int64_t* local_tick,
+                         int n_remote, const int64_t* remote_slab, const int64_t* remote_tick,
+                         int64_t step_start, int64_t step_end, double slab, int64_t ticks_per_slab,
+                         int local_order, int remote_order, int small_order, int max_out,
+                         int32_t* out_local, int32_t* out_remote, double* out_coef);
+/* Self-start, then n_slabs slabs of AdamsBashforth(order) with local time
+ * stepping on conforming bricks of uniform extent n: element e steps
+ * slab / 2^levels[e] (levels may be NULL: global stepping), after the first
+ * steps at the finest step.  u in place. */
+int orc_evolve_adams(int n_inst, const OrcBrick* bricks, int n, double gamma2, int order,
+                     const int32_t* levels, double slab, int n_slabs, double* u, int n_threads);
+
 #ifdef __cplusplus
 }
 #endif

@@ -42,8 +42,9 @@ _lib = None
 def lib():
     global _lib
     if _lib is None:
-        if not os.path.exists(LIB) or os.path.getmtime(LIB) < os.path.getmtime(
-                os.path.join(HERE, "dgsw_oracle.cpp")):
+        srcs = ("dgsw_oracle.cpp", "adams_oracle.cpp", "dgsw_oracle.h")
+        if not os.path.exists(LIB) or os.path.getmtime(LIB) < max(
+                os.path.getmtime(os.path.join(HERE, f)) for f in srcs):
             build()
         L = ctypes.CDLL(LIB)
         P, D, I, I64 = ctypes.c_void_p, ctypes.c_double, ctypes.c_int, ctypes.c_int64
@@ -73,6 +74,10 @@ def lib():
             "orc_refined_index_maps": [P, P, P, P], "orc_refined_coords": [P, I, P],
             "orc_refined_rhs": [P, I, D, P, P, I], "orc_refined_evolve": [P, I, D, D, I, P, I],
             "orc_proj_half": [I, I, P, P],
+            "orc_variable_coefficients": [I, P, D, D, P],
+            "orc_adams_coefficients": [I, P, I64, I64, D, I64, P],
+            "orc_lts_coefficients": [I, P, P, I, P, P, I64, I64, D, I64, I, I, I, I, P, P, P],
+            "orc_evolve_adams": [I, P, I, D, I, P, D, I, P, I],
         }
         for name, args in sig.items():
             fn = getattr(L, name)
@@ -498,3 +503,50 @@ def proj_half(n, upper):
     P, R = np.zeros((n, n)), np.zeros((n, n))
     _check(lib().orc_proj_half(n, int(upper), _p(P), _p(R)))
     return P, R
+
+
+# ---------------- Adams-Bashforth and local time stepping ----------------
+
+def variable_coefficients(control_times, step_start, step_end):
+    ct = np.ascontiguousarray(control_times, dtype=np.float64)
+    out = np.zeros(len(ct))
+    _check(lib().orc_variable_coefficients(len(ct), _p(ct), step_start, step_end, _p(out)))
+    return out
+
+
+def adams_coefficients(control_ticks, step_start, step_end, slab=1.0, ticks_per_slab=1):
+    t = np.ascontiguousarray(control_ticks, dtype=np.int64)
+    out = np.zeros(len(t))
+    _check(lib().orc_adams_coefficients(len(t), _p(t), step_start, step_end, slab,
+                                        ticks_per_slab, _p(out)))
+    return out
+
+
+def lts_coefficients(local_ids, remote_ids, step_start, step_end, order, slab=1.0,
+                     ticks_per_slab=1):
+    """local_ids / remote_ids: lists of (slab number, tick); order an int or
+    (local, remote, small step) orders.  Returns a dict
+    {(local id, remote id): coefficient}."""
+    lo, ro, so = (order,) * 3 if np.ndim(order) == 0 else order
+    ls = np.array([i[0] for i in local_ids], dtype=np.int64)
+    lt = np.array([i[1] for i in local_ids], dtype=np.int64)
+    rs = np.array([i[0] for i in remote_ids], dtype=np.int64)
+    rt = np.array([i[1] for i in remote_ids], dtype=np.int64)
+    m = 256
+    ol = np.zeros(m, dtype=np.int32)
+    orr = np.zeros(m, dtype=np.int32)
+    oc = np.zeros(m)
+    cnt = lib().orc_lts_coefficients(len(ls), _p(ls), _p(lt), len(rs), _p(rs), _p(rt),
+                                      step_start, step_end, slab, ticks_per_slab, lo, ro, so, m,
+                                      _p(ol), _p(orr), _p(oc))
+    _check(min(cnt, 0))
+    return {(tuple(local_ids[ol[i]]), tuple(remote_ids[orr[i]])): oc[i] for i in range(cnt)}
+
+
+def evolve_adams(bricks, n, u, slab, n_slabs, order, levels=None, gamma2=0.0, threads=0):
+    u = np.array(u, dtype=np.float64, copy=True)
+    arr = _bricks(bricks)
+    lv = None if levels is None else np.ascontiguousarray(levels, dtype=np.int32)
+    _check(lib().orc_evolve_adams(len(bricks), ctypes.addressof(arr), n, gamma2, order, _p(lv),
+                                  slab, n_slabs, _p(u), threads))
+    return u

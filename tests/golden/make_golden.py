@@ -15,6 +15,12 @@ Fixtures:
                        golden functions: BoundaryCorrections/UpwindPenalty.py
                        and BoundaryConditions/ConstraintPreservingSphericalRadiation.py
                        under tests/Unit/Evolution/Systems/CurvedScalarWave
+  adams_golden.json    Adams-Bashforth known answers read as text from
+                       tests/Unit/Time/TimeSteppers/Test_AdamsCoefficients.cpp
+                       (exact variable_coefficients cases) and
+                       tests/Unit/Time/TimeSteppers/Test_AdamsLts.cpp (every
+                       explicit "AB ..." lts_coefficients step case; the
+                       Adams-Moulton cases and dense output are not taken)
   upwind_golden.json   seeded inputs and the outputs of the reference's pypp
                        golden functions
                        tests/Unit/Evolution/Systems/ScalarWave/BoundaryCorrections/UpwindPenalty.py
@@ -262,7 +268,113 @@ def curved_golden(seed=20241205, npts=30):
     }
 
 
+def _rational(text):
+    """'{-5, 2}' -> -2.5, '3' -> 3.0"""
+    text = text.strip()
+    m = re.fullmatch(r"\{\s*(-?\d+)\s*,\s*(-?\d+)\s*\}", text)
+    if m:
+        return int(m.group(1)) / int(m.group(2))
+    return float(int(text))
+
+
+def _rational_list(text):
+    """'{{5, 12}, {-4, 3}, 2}' -> [5/12, -4/3, 2]"""
+    body = text.strip()[1:-1]
+    items, depth, cur = [], 0, ""
+    for c in body:
+        if c == "{":
+            depth += 1
+        elif c == "}":
+            depth -= 1
+        if c == "," and depth == 0:
+            items.append(cur)
+            cur = ""
+        else:
+            cur += c
+    if cur.strip():
+        items.append(cur)
+    return [_rational(i) for i in items]
+
+
+def _fake_id(text):
+    """FakeId text -> [slab, time]; None for a substep id (Adams-Moulton)."""
+    parts = [p.strip() for p in _split_args(text.strip()[1:-1])]
+    if len(parts) == 1:
+        return [0, int(parts[0])]
+    if len(parts) == 3 and parts[1] == "{}":
+        return [int(parts[2]), int(parts[0])]
+    return None
+
+
+def _brace_items(body):
+    items, depth, start = [], 0, None
+    for i, c in enumerate(body):
+        if c == "{":
+            if depth == 0:
+                start = i
+            depth += 1
+        elif c == "}":
+            depth -= 1
+            if depth == 0:
+                items.append(body[start:i + 1])
+    return items
+
+
+def adams_golden():
+    out = {"source": ["tests/Unit/Time/TimeSteppers/Test_AdamsCoefficients.cpp",
+                      "tests/Unit/Time/TimeSteppers/Test_AdamsLts.cpp"],
+           "variable": [], "lts": []}
+    src = open(os.path.join(ROOT, out["source"][0])).read()
+    for m in re.finditer(r"ac::variable_coefficients<Rational>\((.*?)\)\s*==\s*"
+                         r"ac::OrderVector<Rational>(\{.*?\})\);", src, re.S):
+        args = _split_args(m.group(1))
+        out["variable"].append({"control_times": _rational_list(args[0]),
+                                "step_start": _rational(args[1]),
+                                "step_end": _rational(args[2]),
+                                "expected": _rational_list(m.group(2))})
+    src = open(os.path.join(ROOT, out["source"][1])).read()
+    body = src[src.index("void test_lts_coefficients()"):]
+    body = body[:body.index("SPECTRE_TEST_CASE")]
+    arrays = {}
+    for m in re.finditer(r"const std::array (\w+)\{(.*?)\};", body, re.S):
+        arrays[m.group(1)] = [eval(v) for v in _split_args(m.group(2))]
+    infos = [(m.start(), m.group(1)) for m in re.finditer(r'INFO\("([^"]+)"\)', body)]
+    for i, (pos, name) in enumerate(infos):
+        if not name.startswith("AB "):
+            continue
+        block = body[pos:infos[i + 1][0] if i + 1 < len(infos) else len(body)]
+        orders = {m.group(1): int(m.group(3)) for m in re.finditer(
+            r"adams_lts::AdamsScheme (\w+)\{adams_lts::SchemeType::(\w+), (\d+)\}", block)
+            if m.group(2) == "Explicit"}
+        steps = {}
+        for m in re.finditer(r"const std::vector<FakeId> (\w+)\{(.*?)\};", block, re.S):
+            steps[m.group(1)] = [_fake_id(t) for t in _brace_items(m.group(2))]
+        expected = {}
+        for m in re.finditer(r"const ExpectedCoefficients (\w+)\{(.*?)\};", block, re.S):
+            entries = []
+            for item in _brace_items(m.group(2)):
+                inner = item[1:-1]
+                ids_text = _brace_items(inner)[0]
+                value = inner[len(ids_text):].strip().lstrip(",").strip()
+                value = re.sub(r"(\w+)\[(\d+)\]", lambda a: repr(arrays[a.group(1)][int(a.group(2))]),
+                               value)
+                pair = [_fake_id(t) for t in _brace_items(ids_text[1:-1])]
+                entries.append({"local": pair[0], "remote": pair[1], "coef": eval(value)})
+            expected[m.group(1)] = entries
+        for m in re.finditer(r"step_coefficients\(\s*(\w+),\s*(\w+),\s*(\w+),\s*(\w+),"
+                             r"\s*(\w+),\s*(-?\d+),\s*(-?\d+)(?:,\s*false)?\),\s*(\w+)\);",
+                             block):
+            loc, rem, sl, sr, ss, t0, t1, exp = m.groups()
+            out["lts"].append({
+                "case": name, "local": steps[loc], "remote": steps[rem],
+                "orders": [orders[sl], orders[sr], orders[ss]],
+                "step_start": int(t0), "step_end": int(t1), "expected": expected[exp]})
+    return out
+
+
 def main():
+    with open(os.path.join(HERE, "adams_golden.json"), "w") as f:
+        json.dump(adams_golden(), f, indent=1)
     with open(os.path.join(HERE, "lgl_golden.json"), "w") as f:
         json.dump(lgl_golden(), f, indent=1)
     with open(os.path.join(HERE, "upwind_golden.json"), "w") as f:

@@ -39,7 +39,7 @@
 extern "C" {
 #endif
 
-#define DGSW_ABI_VERSION 4
+#define DGSW_ABI_VERSION 5
 
 typedef enum {
   DGSW_OK = 0,
@@ -60,7 +60,12 @@ typedef enum {
 /* BoundaryCorrection creatable classes, ScalarWave/BoundaryCorrections/Factory.hpp */
 typedef enum { DGSW_CORRECTION_UPWIND_PENALTY = 0 } DgswBoundaryCorrection;
 /* TimeStepper creatable classes, Time/TimeSteppers/Factory.hpp */
-typedef enum { DGSW_STEPPER_RK3_HESTHAVEN_SSP = 0 } DgswTimeStepper;
+typedef enum {
+  DGSW_STEPPER_RK3_HESTHAVEN_SSP = 0,
+  /* TimeSteppers::AdamsBashforth (AdamsBashforth.cpp:51-339) with local time
+   * stepping (AdamsLts.cpp:301-415); see dgsw_step */
+  DGSW_STEPPER_ADAMS_BASHFORTH = 1
+} DgswTimeStepper;
 /* Arithmetic of the derivative/flux/lift work.  FP64: everything in FP64.
  * MIXED: FP32 contractions with the D-matrix split into hi+lo FP32 parts,
  * FP64 state and FP64 accumulation of each time step. */
@@ -144,6 +149,11 @@ typedef struct {
   /* non-NULL: the domain is this refined block lattice (n_instances = 1,
    * bricks ignored) */
   const DgswRefinedBrick* refined;
+  /* DGSW_STEPPER_ADAMS_BASHFORTH: order 1..8 (0 means 3) and, per element,
+   * its step level 0..3 (the element steps slab / 2^level; NULL: all 0,
+   * global time stepping). */
+  int32_t stepper_order;
+  const int32_t* step_levels;
 } DgswConfig;
 
 typedef struct DgswHandle_* DgswHandle;
@@ -211,6 +221,68 @@ int dgsw_boundary_terms_device(int64_t npts, const double* packaged_int,
  * TimeStepper::update_u one substep at a time. */
 int dgsw_step(DgswHandle h, int n_steps, double dt);
 int dgsw_substep(DgswHandle h, int k, double dt);
+
+/* ---- TimeStepper (AdamsBashforth, local time stepping) -------------------
+ * Handles with time_stepper DGSW_STEPPER_ADAMS_BASHFORTH: flat system,
+ * Gauss-Lobatto, one uniform extent, conforming bricks, FP64.  dgsw_step
+ * advances n_steps slabs of duration dt (the same dt on every call); within a
+ * slab an element of step level l takes 2^l steps, and the UpwindPenalty
+ * coupling across faces between levels is integrated by
+ * AdamsBashforth::add_boundary_delta.  The first call (and the first after
+ * dgsw_set_state or dgsw_set_initial_data) runs the reference's self-start
+ * procedure (SelfStartActions.hpp:136-482) at steps of slab / (order 2^L),
+ * L the finest level; every element then steps slab / 2^L until the first
+ * slab boundary after which no self-start value remains in any history,
+ * and from there slab / 2^level.  dgsw_substep returns
+ * DGSW_ERR_UNSUPPORTED. */
+/* Device history of AdamsBashforth handles: ring slots per element, ticks
+ * per slab, grid-point time derivatives evaluated per slab after the
+ * start-up, and device launches per slab. */
+int dgsw_adams_info(DgswHandle h, int* ring_slots, int64_t* ticks_per_slab,
+                    int64_t* rhs_points_per_slab, int* launches_per_slab);
+
+/* Host-only restatements used by the schedule (no GPU needed).  Times are
+ * integer ticks, ticks_per_slab to a slab of duration `slab`.
+ * adams_coefficients::coefficients (AdamsCoefficients.hpp:29-67), n <= 8: */
+int dgsw_adams_coefficients(int n, const int64_t* control_ticks, int64_t step_start,
+                            int64_t step_end, double slab, int64_t ticks_per_slab,
+                            double* out);
+/* adams_lts::lts_coefficients for explicit schemes (AdamsLts.cpp:301-415) of
+ * orders local_order, remote_order, small_order.  Histories are (slab
+ * number, tick) time ids in insertion order; output terms index them, one
+ * per (local id, remote id), sorted by ids.  Returns the number of terms
+ * (<= max_out) or a negative status. */
+int dgsw_lts_coefficients(int n_local, const int64_t* local_slab, const int64_t* local_tick,
+                          int n_remote, const int64_t* remote_slab, const int64_t* remote_tick,
+                          int64_t step_start, int64_t step_end, double slab,
+                          int64_t ticks_per_slab, int local_order, int remote_order,
+                          int small_order, int max_out, int32_t* out_local,
+                          int32_t* out_remote, double* out_coef);
+/* One level's work in one device launch of the schedule (the coefficient
+ * tables the kernel applies; marginals of the lts_coefficients terms). */
+typedef struct {
+  int32_t launch;   /* index of the device launch */
+  int32_t level;
+  int32_t update;   /* finish the step: volume update and boundary delta */
+  int32_t reset;    /* restore the initial values (self-start) */
+  int32_t rec_slot; /* ring slot of the record of the new state */
+  int32_t n_vol;
+  int32_t vol_slot[8];
+  double vol_c[8];
+  int32_t n_loc[4]; /* per neighbour level */
+  int32_t loc_slot[4][8];
+  double loc_c[4][8];
+  int32_t n_rem[4];
+  int32_t rem_slot[4][16];
+  double rem_c[4][16];
+} DgswAdamsJob;
+/* The schedule of n_slabs slabs (the first includes the self-start) for
+ * level_counts[l] elements of level l and adjacency[4*l + m] != 0 when a
+ * level-l element has a level-m face neighbour.  Writes up to max_jobs jobs
+ * and their number, the ticks per slab and the ring slots needed. */
+int dgsw_adams_schedule(int order, const int64_t* level_counts, const int32_t* adjacency,
+                        double slab, int n_slabs, int max_jobs, DgswAdamsJob* jobs,
+                        int* n_jobs, int64_t* ticks_per_slab, int* ring_slots);
 
 /* ---- launch autotuner -------------------------------------------------------
  * The plain FP64 stage kernel exists in two launch configurations per N

@@ -1,0 +1,253 @@
+// adams_step.cu -- one tick position of AdamsBashforth with local time
+// stepping for the flat scalar wave (uniform LGL extent N, conforming
+// periodic bricks, FP64).
+//
+// A launch runs the jobs of the levels whose step ends at this position
+// (AdamsSchedule, adams_schedule.cpp).  Per element of such a level:
+//  1. finish the step (job.update):
+//       u += sum_j c_j F_j                      AdamsBashforth::update_u
+//                                               (AdamsBashforth.cpp:131-200)
+//     with F_j the element's recorded volume time derivatives, then on every
+//     face the boundary delta (add_boundary_delta, AdamsBashforth.cpp:264-281;
+//     lifted and added to the face slice, ApplyBoundaryCorrections.hpp:
+//     990-1011).  The flat UpwindPenalty correction is linear: with
+//     w = Pi - s Phi_d - gamma2 Psi (s the face's outward sign), D_Pi =
+//     (w_int - w_ext) / 2, D_Phi_d = -s D_Pi, D_Psi = 0, lifted by
+//     -N(N-1)/2 |n| (LiftFlux.hpp:57-61).  The pairwise LTS sum therefore
+//     collapses to marginal weights: W_int = sum_l a_l w_int(l),
+//     W_ext = sum_r b_r w_ext(r), and
+//       Pi_face += g (W_int - W_ext),  Phi_d,face += -s g (W_int - W_ext),
+//     g = -N(N-1) J_d / 4 (J_d = d xi / d x).
+//  2. optionally restore the initial values (self-start resets),
+//  3. record the new state: its volume time derivative
+//     (TimeDerivative.cpp:37-44, no boundary terms) into ring slot rec_slot
+//     of F, and per face point (P, Q) = (Pi - gamma2 Psi, Phi_d) into the
+//     same slot of B, from which any later step forms w = P - s Q.
+// The new record's slot is never one this launch reads (the schedule keeps
+// it out), so elements of one launch do not race.
+//
+// Work split as stage_fp64.cu: N*N threads per element, one line per thread
+// in each of the three axis passes; the element's state is staged in shared
+// memory.
+#include "common.cuh"
+#include "dg_device.cuh"
+#include "launch.hpp"
+
+namespace dgsw {
+namespace {
+
+template <int N>
+struct AbShape {
+  static constexpr int h = N / 2;
+  static constexpr int H = h + N % 2;
+  static constexpr int NN = N * N;
+  static constexpr int NP = N * N * N;
+  static constexpr int TAB = 2 * H * h + H;
+  static constexpr int SLOT = 6 * NP + 3 * TAB;  // state (5 NP), dt Pi sum, tables
+};
+
+template <int N>
+constexpr int ab_epb() {
+  return N <= 4 ? 8 : (N <= 6 ? 4 : (N <= 10 ? 2 : 1));
+}
+
+// w = P - s Q of face record `slot` of element e, face dir, point t
+__device__ __forceinline__ double face_w(const double* __restrict__ B, int64_t rec, int dir, int t,
+                                         int NN, double s) {
+  const double* p = B + (rec * 6 + dir) * 2 * (int64_t)NN + t;
+  return fma(-s, p[NN], p[0]);
+}
+
+template <int N, int EPB>
+__global__ void __launch_bounds__(N * N * EPB) ab_step_kernel(const __grid_constant__ AbArgs A) {
+  using S = AbShape<N>;
+  constexpr int NN = S::NN, NP = S::NP, TAB = S::TAB, h = S::h, H = S::H;
+  extern __shared__ double smem[];
+  const int slot = threadIdx.x / NN;
+  const int t = threadIdx.x - slot * NN;
+  int64_t g = (int64_t)blockIdx.x * EPB + slot;
+  int j = -1;
+  for (int q = 0; q < A.L.n_jobs; ++q) {
+    if (g < A.L.job[q].count) {
+      j = q;
+      break;
+    }
+    g -= A.L.job[q].count;
+  }
+  const bool active = j >= 0;
+  const AbLevelJob& J = A.L.job[active ? j : 0];
+  const int64_t e = active ? (int64_t)A.list[J.begin + g] : 0;
+  const bool update = active && J.update;
+  double* U = smem + slot * S::SLOT;  // Psi, Pi, Phi_x, Phi_y, Phi_z
+  double* Sacc = U + 5 * NP;          // running dt Pi
+  double* T = Sacc + NP;              // three scaled split tables
+  const int64_t off = e * (int64_t)(kVars * NP);
+  const int64_t E = A.n_elem;
+  const double g2 = A.gamma2;
+
+  double jd[3] = {0.0, 0.0, 0.0};
+  if (active) {
+    for (int d = 0; d < 3; ++d) jd[d] = A.jac[3 * e + d];
+    const double* src = (J.reset ? A.u0 : A.u) + off;
+    for (int q = t; q < 5 * NP; q += NN) U[q] = src[q];
+    for (int q = t; q < 3 * TAB; q += NN) {
+      const int d = q / TAB, r = q - d * TAB;
+      double v;
+      if (r < H * h)
+        v = A.eo.A[r / h][r % h];
+      else if (r < 2 * H * h)
+        v = A.eo.B[(r - H * h) / h][(r - H * h) % h];
+      else
+        v = A.eo.M[r - 2 * H * h];
+      T[q] = -jd[d] * v;
+    }
+  }
+  __syncthreads();
+
+  // 1. volume part of the step
+  if (update && !J.reset) {
+    for (int q = t; q < 5 * NP; q += NN) {
+      double acc = U[q];
+      for (int i = 0; i < J.n_vol; ++i)
+        acc = fma(J.vol_c[i], A.F[((int64_t)J.vol_slot[i] * E + e) * (kVars * NP) + q], acc);
+      U[q] = acc;
+    }
+  }
+  __syncthreads();
+
+  const int ta = t % N, tb = t / N;
+  auto line = [&](int d, int& base, int& stride) {
+    if (d == 0) {
+      base = N * ta + NN * tb;
+      stride = 1;
+    } else if (d == 1) {
+      base = ta + NN * tb;
+      stride = N;
+    } else {
+      base = ta + N * tb;
+      stride = NN;
+    }
+  };
+
+  // 1b. boundary delta, one axis at a time (edge points belong to faces of
+  // two axes)
+#pragma unroll 1
+  for (int d = 0; d < 3; ++d) {
+    if (update && !J.reset) {
+      int base, stride;
+      line(d, base, stride);
+      const double gf = -0.25 * (double)(N * (N - 1)) * jd[d];
+      for (int up = 0; up < 2; ++up) {
+        const int dir = 2 * d + up;
+        const double s = up ? 1.0 : -1.0;
+        const int64_t nb = A.nbr[6 * e + dir];
+        const AbFaceTable& f = J.face[A.level[nb]];
+        double wi = 0.0, we = 0.0;
+        for (int i = 0; i < f.n_loc; ++i)
+          wi = fma(f.loc_c[i], face_w(A.B, (int64_t)f.loc_slot[i] * E + e, dir, t, NN, s), wi);
+        for (int i = 0; i < f.n_rem; ++i)
+          we = fma(f.rem_c[i], face_w(A.B, (int64_t)f.rem_slot[i] * E + nb, dir ^ 1, t, NN, s), we);
+        const double dw = gf * (wi - we);
+        const int p = base + (up ? (N - 1) * stride : 0);
+        U[NP + p] += dw;
+        U[(2 + d) * NP + p] = fma(-s, dw, U[(2 + d) * NP + p]);
+      }
+    }
+    __syncthreads();
+  }
+
+  if (active && (update || J.reset))
+    for (int q = t; q < 5 * NP; q += NN) A.u[off + q] = U[q];
+
+  // 3. record: volume time derivative and face data of the new state
+  double* Fo = A.F + ((int64_t)(active ? J.rec_slot : 0) * E + e) * (kVars * NP);
+  double* Bo = A.B + ((int64_t)(active ? J.rec_slot : 0) * E + e) * 12 * (int64_t)NN;
+#pragma unroll 1
+  for (int d = 0; d < 3; ++d) {
+    if (active) {
+      int base, stride;
+      line(d, base, stride);
+      double up[N], uf[N], dF[N], dP[N];
+#pragma unroll
+      for (int i = 0; i < N; ++i) {
+        up[i] = U[NP + base + i * stride];
+        uf[i] = U[(2 + d) * NP + base + i * stride];
+      }
+      const double* tab = T + d * TAB;
+      dev::eo_line<N, double>(uf, dF, tab);  // -J_d D Phi_d: part of dt Pi
+      dev::eo_line<N, double>(up, dP, tab);  // -J_d D Pi = dt Phi_d (gamma2 = 0)
+      const double psi_lo = U[base], psi_hi = U[base + (N - 1) * stride];
+      if (g2 != 0.0) {
+        // gamma2 (d_d Psi - Phi_d) of dt Phi_d (TimeDerivative.cpp:42-43)
+        double ps[N], dpsi[N];
+#pragma unroll
+        for (int i = 0; i < N; ++i) ps[i] = U[base + i * stride];
+        dev::eo_line<N, double>(ps, dpsi, tab);
+#pragma unroll
+        for (int i = 0; i < N; ++i) dP[i] = fma(-g2, dpsi[i] + uf[i], dP[i]);
+      }
+#pragma unroll
+      for (int i = 0; i < N; ++i) Fo[(2 + d) * NP + base + i * stride] = dP[i];
+      double* b_lo = Bo + (2 * d) * 2 * NN;
+      double* b_hi = Bo + (2 * d + 1) * 2 * NN;
+      b_lo[t] = fma(-g2, psi_lo, up[0]);
+      b_lo[NN + t] = uf[0];
+      b_hi[t] = fma(-g2, psi_hi, up[N - 1]);
+      b_hi[NN + t] = uf[N - 1];
+      if (d < 2) {
+#pragma unroll
+        for (int i = 0; i < N; ++i) {
+          if (d == 0)
+            Sacc[base + i * stride] = dF[i];
+          else
+            Sacc[base + i * stride] += dF[i];
+        }
+      } else {
+#pragma unroll
+        for (int i = 0; i < N; ++i) {
+          const int p = base + i * stride;
+          Fo[NP + p] = Sacc[p] + dF[i];
+          Fo[p] = -up[i];
+        }
+      }
+    }
+    // Sacc points of pass d are touched by other threads in pass d + 1
+    if (d < 2) __syncthreads();
+  }
+}
+
+template <int N>
+cudaError_t launch_n(const AbArgs& A, cudaStream_t s) {
+  constexpr int EPB = ab_epb<N>();
+  const size_t smem = (size_t)EPB * AbShape<N>::SLOT * sizeof(double);
+  auto k = ab_step_kernel<N, EPB>;
+  cudaError_t err = cudaFuncSetAttribute(k, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+  if (err != cudaSuccess) return err;
+  int64_t total = 0;
+  for (int q = 0; q < A.L.n_jobs; ++q) total += A.L.job[q].count;
+  const int64_t blocks = (total + EPB - 1) / EPB;
+  if (blocks <= 0) return cudaSuccess;
+  k<<<(unsigned)blocks, N * N * EPB, smem, s>>>(A);
+  return cudaGetLastError();
+}
+
+}  // namespace
+
+cudaError_t launch_adams_step(const AbArgs& A, int n, cudaStream_t s) {
+  switch (n) {
+    case 2: return launch_n<2>(A, s);
+    case 3: return launch_n<3>(A, s);
+    case 4: return launch_n<4>(A, s);
+    case 5: return launch_n<5>(A, s);
+    case 6: return launch_n<6>(A, s);
+    case 7: return launch_n<7>(A, s);
+    case 8: return launch_n<8>(A, s);
+    case 9: return launch_n<9>(A, s);
+    case 10: return launch_n<10>(A, s);
+    case 11: return launch_n<11>(A, s);
+    case 12: return launch_n<12>(A, s);
+    default: return cudaErrorInvalidValue;
+  }
+}
+
+}  // namespace dgsw

@@ -16,6 +16,7 @@
 #include <vector>
 
 #include "../../include/dgsw.h"
+#include "adams.hpp"
 #include "common.cuh"
 #include "host_setup.hpp"
 #include "launch.hpp"
@@ -94,6 +95,15 @@ struct DgswHandle_ {
   int32_t* r_face_idx = nullptr;  // per element face
   double* r_PR = nullptr;         // [P lower, P upper, R lower, R upper], n*n each
   double* r_wext = nullptr;       // n*n per record
+  // AdamsBashforth with local time stepping (adams_schedule.cpp, adams_step.cu)
+  bool adams = false;
+  AdamsSchedule ab;
+  int64_t ab_count[kAbMaxLevels] = {};
+  int32_t* ab_list = nullptr;   // element ids sorted by step level
+  int8_t* ab_level = nullptr;   // step level per element
+  double* ab_F = nullptr;       // ring of volume time derivatives
+  double* ab_B = nullptr;       // ring of face data
+  double ab_slab = std::nan("");
   // Legendre-Gauss quadrature (flat, uniform, FP64)
   bool gauss = false;
   GaussTables gt{};
@@ -735,9 +745,104 @@ cudaError_t capture_steps(DgswHandle h, double dt, int steps, cudaGraphExec_t* o
   return e;
 }
 
+// AdamsBashforth handle set-up: step levels, the level-sorted element list,
+// the schedule (whose dry run sizes the history rings) and the rings.
+int adams_init(DgswHandle h, const DgswConfig& cfg) {
+  if (h->curved || h->refined || h->gauss || !h->dom.uniform || mixed(h))
+    return fail(h, DGSW_ERR_UNSUPPORTED,
+                "AdamsBashforth: flat system, Gauss-Lobatto, one extent, conforming bricks, FP64");
+  const int64_t E = h->dom.n_elem;
+  std::vector<int8_t> level(E, 0);
+  for (int64_t e = 0; e < E; ++e) {
+    const int l = cfg.step_levels ? cfg.step_levels[e] : 0;
+    if (l < 0 || l >= kAbMaxLevels) return fail(h, DGSW_ERR_ARGUMENT, "step levels must be in [0, 3]");
+    level[e] = (int8_t)l;
+  }
+  bool adj[kAbMaxLevels][kAbMaxLevels] = {};
+  for (int64_t e = 0; e < E; ++e) {
+    ++h->ab_count[level[e]];
+    for (int f = 0; f < 6; ++f) adj[level[e]][level[h->dom.neighbor[6 * e + f]]] = true;
+  }
+  std::vector<int32_t> list;
+  list.reserve(E);
+  for (int l = 0; l < kAbMaxLevels; ++l)
+    for (int64_t e = 0; e < E; ++e)
+      if (level[e] == l) list.push_back((int32_t)e);
+  std::string err;
+  const int order = cfg.stepper_order ? cfg.stepper_order : 3;
+  if (!h->ab.init(order, adj, h->ab_count, &err)) return fail(h, DGSW_ERR_ARGUMENT, err);
+  cudaError_t e;
+  if ((e = upload(&h->ab_list, list)) != cudaSuccess) return cuda_fail(h, e, "upload level list");
+  if ((e = upload(&h->ab_level, level)) != cudaSuccess) return cuda_fail(h, e, "upload levels");
+  const int n = h->dom.elem_n[0];
+  const size_t slots = (size_t)h->ab.ring_slots();
+  if ((e = cudaMalloc(&h->ab_F, slots * E * kVars * n * n * n * sizeof(double))) != cudaSuccess)
+    return cuda_fail(h, e, "cudaMalloc time-derivative ring");
+  if ((e = cudaMalloc(&h->ab_B, slots * E * 12 * n * n * sizeof(double))) != cudaSuccess)
+    return cuda_fail(h, e, "cudaMalloc face-data ring");
+  h->adams = true;
+  return DGSW_OK;
+}
+
+// n_steps slabs of duration dt: the schedule's launches, one per tick
+// position (the first slab after a restart begins with the self-start).
+int adams_step(DgswHandle h, int n_steps, double dt) {
+  if (!(dt > 0.0)) return fail(h, DGSW_ERR_ARGUMENT, "the slab duration must be positive");
+  if (h->ab.started() && !(dt == h->ab_slab))
+    return fail(h, DGSW_ERR_ARGUMENT,
+                "AdamsBashforth steps slabs of one duration; set the state again to change it");
+  h->ab.set_slab(dt);
+  h->ab_slab = dt;
+  const size_t bytes = h->dom.offset.back() * sizeof(double);
+  AbArgs A;
+  A.u = h->state;
+  A.u0 = h->t1;
+  A.F = h->ab_F;
+  A.B = h->ab_B;
+  A.nbr = h->nbr;
+  A.jac = h->jac;
+  A.list = h->ab_list;
+  A.level = h->ab_level;
+  A.n_elem = h->dom.n_elem;
+  A.gamma2 = h->cfg.gamma2;
+  A.eo = h->eo;
+  const int n = h->dom.elem_n[0];
+  std::vector<AbLaunch> launches;
+  std::string err;
+  for (int s = 0; s < n_steps; ++s) {
+    if (!h->ab.started())  // initial values for the self-start resets
+      DGSW_CUDA(h, cudaMemcpyAsync(h->t1, h->state, bytes, cudaMemcpyDeviceToDevice, h->stream));
+    if (!h->ab.slab(&launches, &err)) return fail(h, DGSW_ERR_ARGUMENT, err);
+    for (const AbLaunch& L : launches) {
+      A.L = L;
+      DGSW_CUDA(h, launch_adams_step(A, n, h->stream));
+    }
+  }
+  return DGSW_OK;
+}
+
 }  // namespace
 
 extern "C" {
+
+int dgsw_adams_info(DgswHandle h, int* ring_slots, int64_t* ticks_per_slab,
+                    int64_t* rhs_points_per_slab, int* launches_per_slab) {
+  if (!h) return fail(nullptr, DGSW_ERR_ARGUMENT, "null handle");
+  if (!h->adams) return fail(h, DGSW_ERR_UNSUPPORTED, "not an AdamsBashforth handle");
+  const int64_t np = (int64_t)h->dom.elem_n[0] * h->dom.elem_n[0] * h->dom.elem_n[0];
+  int64_t pts = 0;
+  int finest = 0;
+  for (int l = 0; l < kAbMaxLevels; ++l)
+    if (h->ab_count[l]) {
+      pts += h->ab_count[l] * np * h->ab.steps_per_slab(l);
+      finest = l;
+    }
+  if (ring_slots) *ring_slots = h->ab.ring_slots();
+  if (ticks_per_slab) *ticks_per_slab = h->ab.ticks_per_slab();
+  if (rhs_points_per_slab) *rhs_points_per_slab = pts;
+  if (launches_per_slab) *launches_per_slab = 1 << finest;
+  return DGSW_OK;
+}
 
 int dgsw_abi_version(void) { return DGSW_ABI_VERSION; }
 
@@ -841,6 +946,97 @@ int dgsw_gauss_spectral(int n, double* x, double* w, double* D, double* ilo, dou
 
 int dgsw_lgl_points_weights(int n, double* x, double* w) {
   if (!lgl_nodes_weights(n, x, w)) return fail(nullptr, DGSW_ERR_ARGUMENT, "n must be in [2, 20]");
+  return DGSW_OK;
+}
+
+int dgsw_adams_coefficients(int n, const int64_t* ticks, int64_t start, int64_t end, double slab,
+                            int64_t ticks_per_slab, double* out) {
+  if (!adams_step_coefficients(n, ticks, start, end, slab, ticks_per_slab, out))
+    return fail(nullptr, DGSW_ERR_ARGUMENT, "need 0 <= n <= 8 and ticks_per_slab >= 1");
+  return DGSW_OK;
+}
+
+int dgsw_lts_coefficients(int n_local, const int64_t* local_slab, const int64_t* local_tick,
+                          int n_remote, const int64_t* remote_slab, const int64_t* remote_tick,
+                          int64_t start, int64_t end, double slab, int64_t ticks_per_slab,
+                          int local_order, int remote_order, int small_order, int max_out,
+                          int32_t* out_local, int32_t* out_remote, double* out_coef) {
+  if (n_local < 0 || n_remote < 0 || max_out < 0 || ticks_per_slab < 1 ||
+      (n_local && (!local_slab || !local_tick)) || (n_remote && (!remote_slab || !remote_tick)) ||
+      (max_out && (!out_local || !out_remote || !out_coef)))
+    return fail(nullptr, DGSW_ERR_ARGUMENT, "bad history or output arguments");
+  std::vector<AbId> l(n_local), r(n_remote);
+  for (int i = 0; i < n_local; ++i) l[i] = {local_slab[i], local_tick[i]};
+  for (int i = 0; i < n_remote; ++i) r[i] = {remote_slab[i], remote_tick[i]};
+  std::vector<AbTerm> terms;
+  if (adams_lts_terms(l, r, start, end, local_order, remote_order, small_order, slab,
+                      ticks_per_slab, &terms))
+    return fail(nullptr, DGSW_ERR_ARGUMENT, "the histories lack the data of the step");
+  if ((int)terms.size() > max_out) return fail(nullptr, DGSW_ERR_ARGUMENT, "max_out too small");
+  for (size_t i = 0; i < terms.size(); ++i) {
+    out_local[i] = terms[i].local;
+    out_remote[i] = terms[i].remote;
+    out_coef[i] = terms[i].coef;
+  }
+  return (int)terms.size();
+}
+
+int dgsw_adams_schedule(int order, const int64_t* level_counts, const int32_t* adjacency,
+                        double slab, int n_slabs, int max_jobs, DgswAdamsJob* jobs, int* n_jobs,
+                        int64_t* ticks_per_slab, int* ring_slots) {
+  if (!level_counts || !adjacency || n_slabs < 0 || max_jobs < 0 || (max_jobs && !jobs) ||
+      !(slab > 0.0))
+    return fail(nullptr, DGSW_ERR_ARGUMENT, "bad schedule arguments");
+  bool adj[kAbMaxLevels][kAbMaxLevels];
+  int64_t cnt[kAbMaxLevels];
+  for (int l = 0; l < kAbMaxLevels; ++l) {
+    cnt[l] = level_counts[l];
+    for (int m = 0; m < kAbMaxLevels; ++m) adj[l][m] = adjacency[kAbMaxLevels * l + m] != 0;
+  }
+  AdamsSchedule sched;
+  std::string err;
+  if (!sched.init(order, adj, cnt, &err)) return fail(nullptr, DGSW_ERR_ARGUMENT, err);
+  sched.set_slab(slab);
+  int count = 0, launch_index = 0;
+  for (int s = 0; s < n_slabs; ++s) {
+    std::vector<AbLaunch> launches;
+    if (!sched.slab(&launches, &err)) return fail(nullptr, DGSW_ERR_ARGUMENT, err);
+    for (const AbLaunch& L : launches) {
+      for (int j = 0; j < L.n_jobs; ++j) {
+        if (count >= max_jobs) return fail(nullptr, DGSW_ERR_ARGUMENT, "max_jobs too small");
+        const AbLevelJob& a = L.job[j];
+        DgswAdamsJob& o = jobs[count++];
+        std::memset(&o, 0, sizeof(o));
+        o.launch = launch_index;
+        o.level = a.level;
+        o.update = a.update;
+        o.reset = a.reset;
+        o.rec_slot = a.rec_slot;
+        o.n_vol = a.n_vol;
+        for (int i = 0; i < a.n_vol; ++i) {
+          o.vol_slot[i] = a.vol_slot[i];
+          o.vol_c[i] = a.vol_c[i];
+        }
+        for (int m = 0; m < kAbMaxLevels; ++m) {
+          const AbFaceTable& f = a.face[m];
+          o.n_loc[m] = f.n_loc;
+          o.n_rem[m] = f.n_rem;
+          for (int i = 0; i < f.n_loc; ++i) {
+            o.loc_slot[m][i] = f.loc_slot[i];
+            o.loc_c[m][i] = f.loc_c[i];
+          }
+          for (int i = 0; i < f.n_rem; ++i) {
+            o.rem_slot[m][i] = f.rem_slot[i];
+            o.rem_c[m][i] = f.rem_c[i];
+          }
+        }
+      }
+      ++launch_index;
+    }
+  }
+  if (n_jobs) *n_jobs = count;
+  if (ticks_per_slab) *ticks_per_slab = sched.ticks_per_slab();
+  if (ring_slots) *ring_slots = sched.ring_slots();
   return DGSW_OK;
 }
 
@@ -1020,6 +1216,14 @@ int dgsw_create(const DgswConfig* cfg, DgswHandle* out) {
     if ((e = upload(&h->op_lo, lo)) != cudaSuccess) return bail(e, "upload face operators");
     if ((e = upload(&h->op_off, op_off)) != cudaSuccess) return bail(e, "upload face operators");
   }
+  if (cfg->time_stepper == DGSW_STEPPER_ADAMS_BASHFORTH) {
+    int rc = adams_init(h, *cfg);
+    if (rc) {
+      const std::string msg = h->err;
+      dgsw_destroy(h);
+      return fail(nullptr, rc, msg);
+    }
+  }
   *out = h;
   return DGSW_OK;
 }
@@ -1051,6 +1255,10 @@ int dgsw_destroy(DgswHandle h) {
   if (h->r_PR) cudaFree(h->r_PR);
   if (h->r_wext) cudaFree(h->r_wext);
   if (h->dev_err) cudaFree(h->dev_err);
+  if (h->ab_list) cudaFree(h->ab_list);
+  if (h->ab_level) cudaFree(h->ab_level);
+  if (h->ab_F) cudaFree(h->ab_F);
+  if (h->ab_B) cudaFree(h->ab_B);
   for (int n = 0; n <= kMaxN; ++n)
     if (h->class_tasks[n]) cudaFree(h->class_tasks[n]);
   if (h->op64) cudaFree(h->op64);
@@ -1087,6 +1295,7 @@ int dgsw_synchronize(DgswHandle h) {
 
 int dgsw_set_state(DgswHandle h, const double* host_u) {
   if (!h || !host_u) return fail(h, DGSW_ERR_ARGUMENT, "null argument");
+  if (h->adams) h->ab.restart();  // new initial values: self-start again
   if (int rc = select_device(h)) return rc;
   DGSW_CUDA(h, cudaMemcpyAsync(h->state, host_u, h->dom.offset.back() * sizeof(double),
                                cudaMemcpyHostToDevice, h->stream));
@@ -1104,6 +1313,7 @@ int dgsw_get_state(DgswHandle h, double* host_u) {
 
 int dgsw_set_state_device(DgswHandle h, const double* dev_u) {
   if (!h || !dev_u) return fail(h, DGSW_ERR_ARGUMENT, "null argument");
+  if (h->adams) h->ab.restart();  // new initial values: self-start again
   if (int rc = select_device(h)) return rc;
   DGSW_CUDA(h, cudaMemcpyAsync(h->state, dev_u, h->dom.offset.back() * sizeof(double),
                                cudaMemcpyDeviceToDevice, h->stream));
@@ -1120,6 +1330,7 @@ int dgsw_get_state_device(DgswHandle h, double* dev_u) {
 
 int dgsw_set_initial_data(DgswHandle h, int kind, const double* params, double t) {
   if (!h || !params) return fail(h, DGSW_ERR_ARGUMENT, "null argument");
+  if (h->adams) h->ab.restart();  // new initial values: self-start again
   if (h->curved) {
     if (kind != 2) return fail(h, DGSW_ERR_ARGUMENT, "the shell takes initial data kind 2");
     if (!std::isfinite(params[0]) || !std::isfinite(params[1]) || !(params[2] > 0.0) ||
@@ -1277,6 +1488,8 @@ int dgsw_boundary_terms_device(int64_t npts, const double* pkg_int, const double
 
 int dgsw_substep(DgswHandle h, int k, double dt) {
   if (!h) return fail(nullptr, DGSW_ERR_ARGUMENT, "null handle");
+  if (h->adams)
+    return fail(h, DGSW_ERR_UNSUPPORTED, "AdamsBashforth has no substeps; use dgsw_step");
   if (k < 0 || k > 2 || !std::isfinite(dt)) return fail(h, DGSW_ERR_ARGUMENT, "bad substep");
   if (int rc = select_device(h)) return rc;
   const size_t bytes = h->dom.offset.back() * sizeof(double);
@@ -1507,6 +1720,7 @@ int dgsw_step(DgswHandle h, int n_steps, double dt) {
   if (n_steps < 0 || !std::isfinite(dt)) return fail(h, DGSW_ERR_ARGUMENT, "bad step arguments");
   if (n_steps == 0) return DGSW_OK;
   if (int rc = select_device(h)) return rc;
+  if (h->adams) return adams_step(h, n_steps, dt);
   if (!h->tuned && tunable(h)) {
     destroy_graphs(h);
     if (int rc = autotune(h, false)) return rc;

@@ -320,7 +320,8 @@ bool build_domain(const DgswConfig& cfg, Domain* dom, std::string* err) {
     *err = "unsupported boundary correction";
     return false;
   }
-  if (cfg.time_stepper != DGSW_STEPPER_RK3_HESTHAVEN_SSP) {
+  if (cfg.time_stepper != DGSW_STEPPER_RK3_HESTHAVEN_SSP &&
+      cfg.time_stepper != DGSW_STEPPER_ADAMS_BASHFORTH) {
     *err = "unsupported time stepper";
     return false;
   }

@@ -5,6 +5,7 @@
 #include <cstdint>
 #include <cuda_runtime.h>
 
+#include "adams.hpp"
 #include "common.cuh"
 
 namespace dgsw {
@@ -30,6 +31,25 @@ struct StageLaunch {
 };
 
 cudaError_t launch_stage_fp64(const StageLaunch& L, cudaStream_t s);
+
+// One tick position of AdamsBashforth with local time stepping
+// (adams_step.cu): the coefficient tables of the levels stepping there, by
+// value in the kernel's parameter space.
+struct AbArgs {
+  double* u = nullptr;         // state, updated in place
+  const double* u0 = nullptr;  // initial values (self-start resets)
+  double* F = nullptr;         // ring slots x elements x 5 N^3 volume time derivatives
+  double* B = nullptr;         // ring slots x elements x 6 faces x (P, Q) x N^2
+  const int32_t* nbr = nullptr;
+  const double* jac = nullptr;
+  const int32_t* list = nullptr;  // element ids sorted by level
+  const int8_t* level = nullptr;  // per element
+  int64_t n_elem = 0;
+  double gamma2 = 0.0;
+  EoTable eo{};
+  AbLaunch L{};
+};
+cudaError_t launch_adams_step(const AbArgs& A, int n, cudaStream_t s);
 
 // Exterior w = Pi - s Phi_d - gamma2 Psi of every 2:1 face of a refined
 // lattice (refined_faces.cu): the coarse neighbour's face interpolated to this

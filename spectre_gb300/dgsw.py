@@ -73,13 +73,26 @@ class DgswConfig(ctypes.Structure):
                 ("uniform_points", ctypes.c_int32), ("gamma2", ctypes.c_double),
                 ("device", ctypes.c_int32), ("shell", ctypes.POINTER(DgswShell)),
                 ("quadrature", ctypes.c_int32),
-                ("refined", ctypes.POINTER(DgswRefinedBrick))]
+                ("refined", ctypes.POINTER(DgswRefinedBrick)),
+                ("stepper_order", ctypes.c_int32),
+                ("step_levels", ctypes.POINTER(ctypes.c_int32))]
+
+
+class DgswAdamsJob(ctypes.Structure):
+    _fields_ = [("launch", ctypes.c_int32), ("level", ctypes.c_int32),
+                ("update", ctypes.c_int32), ("reset", ctypes.c_int32),
+                ("rec_slot", ctypes.c_int32), ("n_vol", ctypes.c_int32),
+                ("vol_slot", ctypes.c_int32 * 8), ("vol_c", ctypes.c_double * 8),
+                ("n_loc", ctypes.c_int32 * 4), ("loc_slot", (ctypes.c_int32 * 8) * 4),
+                ("loc_c", (ctypes.c_double * 8) * 4), ("n_rem", ctypes.c_int32 * 4),
+                ("rem_slot", (ctypes.c_int32 * 16) * 4), ("rem_c", (ctypes.c_double * 16) * 4)]
 
 
 SYSTEM_SCALAR_WAVE = 0
 SYSTEM_CURVED_SCALAR_WAVE = 1
 RADIAL_DISTRIBUTIONS = {"linear": 0, "logarithmic": 1}
 QUADRATURES = {"gauss_lobatto": 0, "gauss": 1}
+TIME_STEPPERS = {"rk3_hesthaven_ssp": 0, "adams_bashforth": 1}
 
 
 _P = ctypes.c_void_p
@@ -128,6 +141,11 @@ _SIGNATURES = {
     "dgsw_misfit_forward": (_I, [_P, _I, _I, _D, _P, ctypes.POINTER(_D)]),
     "dgsw_misfit_adjoint": (_I, [_P, _P]),
     "dgsw_step_noalloc": (_I, [ctypes.POINTER(DgswBrick), _I, _D, _P, _I, _D, _P]),
+    "dgsw_adams_info": (_I, [_P, _P, _P, _P, _P]),
+    "dgsw_adams_coefficients": (_I, [_I, _P, _I64, _I64, _D, _I64, _P]),
+    "dgsw_lts_coefficients": (_I, [_I, _P, _P, _I, _P, _P, _I64, _I64, _D, _I64, _I, _I, _I,
+                                   _I, _P, _P, _P]),
+    "dgsw_adams_schedule": (_I, [_I, _P, _P, _D, _I, _I, _P, _P, _P, _P]),
     "dgsw_noalloc_scratch_bytes": (ctypes.c_size_t, []),
     "dgsw_noalloc_last_error": (ctypes.c_char_p, []),
 }
@@ -270,7 +288,8 @@ class _ConfigHolder:
     """Keeps the ctypes arrays a DgswConfig points to alive."""
 
     def __init__(self, bricks, points, precision=PRECISION_FP64, gamma2=0.0, device=0,
-                 quadrature="gauss_lobatto"):
+                 quadrature="gauss_lobatto", time_stepper="rk3_hesthaven_ssp", order=0,
+                 step_levels=None):
         self.shell = None
         self.refined = None
         if isinstance(bricks, RefinedBrick):
@@ -316,6 +335,14 @@ class _ConfigHolder:
         self.cfg.shell = ctypes.pointer(self.shell) if self.shell else None
         self.cfg.quadrature = QUADRATURES[quadrature]
         self.cfg.refined = ctypes.pointer(self.refined) if self.refined else None
+        self.cfg.time_stepper = TIME_STEPPERS[time_stepper]
+        self.cfg.stepper_order = int(order)
+        self.step_levels = None
+        if step_levels is not None:
+            self.step_levels = np.ascontiguousarray(step_levels, dtype=np.int32).ravel()
+        self.cfg.step_levels = (
+            self.step_levels.ctypes.data_as(ctypes.POINTER(ctypes.c_int32))
+            if self.step_levels is not None else None)
 
 
 def refined_mortars(refined: "RefinedBrick", points: int):
@@ -336,6 +363,53 @@ def half_projections(n: int, upper: bool):
     P, R = np.zeros((n, n)), np.zeros((n, n))
     _check(lib().dgsw_half_projections(n, int(upper), _ptr(P), _ptr(R)))
     return P, R
+
+
+def adams_coefficients(control_ticks, step_start, step_end, slab=1.0, ticks_per_slab=1):
+    """adams_coefficients::coefficients for control times given in ticks."""
+    t = np.ascontiguousarray(control_ticks, dtype=np.int64)
+    out = np.zeros(len(t))
+    _check(lib().dgsw_adams_coefficients(len(t), _ptr(t), int(step_start), int(step_end),
+                                         float(slab), int(ticks_per_slab), _ptr(out)))
+    return out
+
+
+def lts_coefficients(local_ids, remote_ids, step_start, step_end, order, slab=1.0,
+                     ticks_per_slab=1):
+    """adams_lts::lts_coefficients; ids are (slab number, tick) pairs, order
+    an int or (local, remote, small step) orders.  Returns
+    {(local id, remote id): coefficient}."""
+    lo, ro, so = (order,) * 3 if np.ndim(order) == 0 else order
+    ls = np.array([i[0] for i in local_ids], dtype=np.int64)
+    lt = np.array([i[1] for i in local_ids], dtype=np.int64)
+    rs = np.array([i[0] for i in remote_ids], dtype=np.int64)
+    rt = np.array([i[1] for i in remote_ids], dtype=np.int64)
+    m = 256
+    ol, orr, oc = np.zeros(m, np.int32), np.zeros(m, np.int32), np.zeros(m)
+    cnt = lib().dgsw_lts_coefficients(len(ls), _ptr(ls), _ptr(lt), len(rs), _ptr(rs), _ptr(rt),
+                                      int(step_start), int(step_end), float(slab),
+                                      int(ticks_per_slab), lo, ro, so, m, _ptr(ol), _ptr(orr),
+                                      _ptr(oc))
+    if cnt < 0:
+        _check(cnt)
+    return {(tuple(local_ids[ol[i]]), tuple(remote_ids[orr[i]])): oc[i] for i in range(cnt)}
+
+
+def adams_schedule(order, level_counts, adjacency, slab, n_slabs, max_jobs=100000):
+    """The device schedule of n_slabs slabs: (jobs, ticks per slab, ring
+    slots); jobs is a list of DgswAdamsJob."""
+    cnt = np.zeros(4, np.int64)
+    cnt[:len(level_counts)] = level_counts
+    adj = np.zeros((4, 4), np.int32)
+    a = np.asarray(adjacency, dtype=np.int32)
+    adj[:a.shape[0], :a.shape[1]] = a
+    adj = np.ascontiguousarray(adj.ravel())
+    jobs = (DgswAdamsJob * max_jobs)()
+    nj, S, ring = ctypes.c_int(), ctypes.c_int64(), ctypes.c_int()
+    _check(lib().dgsw_adams_schedule(int(order), _ptr(cnt), _ptr(adj), float(slab), int(n_slabs),
+                                     max_jobs, ctypes.addressof(jobs), ctypes.byref(nj),
+                                     ctypes.byref(S), ctypes.byref(ring)))
+    return list(jobs[:nj.value]), S.value, ring.value
 
 
 def shell_geometry(shell: "Shell", points: int):
@@ -449,11 +523,18 @@ class DgEvolution:
     of one spherical shell (pass a Shell: the CurvedScalarWave system)."""
 
     def __init__(self, bricks, points, precision=PRECISION_FP64, gamma2=0.0, device=0,
-                 quadrature="gauss_lobatto"):
+                 quadrature="gauss_lobatto", time_stepper="rk3_hesthaven_ssp", order=3,
+                 step_levels=None):
+        """time_stepper "adams_bashforth": AdamsBashforth of the given order
+        with local time stepping; step_levels (one per element, 0..3, or
+        None) make element e step slab / 2^step_levels[e], and step(dt)
+        advances slabs of duration dt."""
         if isinstance(bricks, Brick):
             bricks = [bricks]
-        self._cfg = _ConfigHolder(bricks, points, precision, gamma2, device, quadrature)
+        self._cfg = _ConfigHolder(bricks, points, precision, gamma2, device, quadrature,
+                                  time_stepper, order, step_levels)
         self.quadrature = quadrature
+        self.time_stepper = time_stepper
         h = _P()
         _check(lib().dgsw_create(ctypes.byref(self._cfg.cfg), ctypes.byref(h)))
         self._h = h
@@ -491,6 +572,16 @@ class DgEvolution:
 
     def stream_ptr(self) -> int:
         return lib().dgsw_stream(self._h) or 0
+
+    def adams_info(self):
+        """AdamsBashforth handles: dict of ring_slots, ticks_per_slab,
+        rhs_points_per_slab (grid-point time derivatives per slab after the
+        start-up) and launches_per_slab."""
+        r, t, p, n = ctypes.c_int(), _I64(), _I64(), ctypes.c_int()
+        _check(lib().dgsw_adams_info(self._h, ctypes.byref(r), ctypes.byref(t), ctypes.byref(p),
+                                     ctypes.byref(n)), self._h)
+        return {"ring_slots": r.value, "ticks_per_slab": t.value,
+                "rhs_points_per_slab": p.value, "launches_per_slab": n.value}
 
     def synchronize(self):
         _check(lib().dgsw_synchronize(self._h), self._h)

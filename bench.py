@@ -423,6 +423,63 @@ def time_curved(args, dev, with_cpu):
     return out
 
 
+def ab_bytes_per_point(order, n):
+    """Compulsory HBM bytes per grid point of one AdamsBashforth launch of an
+    element (update + record, global stepping): read u and `order` recorded
+    time derivatives, write u and the new record (5 FP64 vars each); on the
+    faces read `order` own and `order` neighbour records of (P, Q) per face
+    point of the six faces and write the new ones."""
+    vol = (5 + 5 * order + 5 + 5) * 8.0
+    faces = (6 * 2 * order * 2 + 12) * n * n * 8.0 / n ** 3
+    return vol + faces
+
+
+def time_adams(args, dev):
+    """AdamsBashforth(3) on the FP64 config-2 mesh (32^3 elements at 8^3,
+    Gaussian pulse, slab = step = 2e-4): global stepping, and local time
+    stepping with half of the elements (seeded) on level 1 (two steps of
+    1e-4 per slab).  The start-up runs in the warm-up; the timed slabs are
+    steady-state AB3.  One launch per tick position."""
+    import torch
+    from spectre_gb300.dgsw import Brick, DgEvolution
+    e = args.elements
+    bricks = [Brick((e, e, e), (0.0, 0.0, 0.0), (2 * math.pi,) * 3)]
+    slabs = max(10, args.steps * 2)
+    out = {"workload": "AdamsBashforth(3), %d^3 elements x %d^3 LGL points, Gaussian pulse, "
+                       "slab %.0e" % (e, N_PTS, DT), "slabs": slabs}
+    rng = np.random.default_rng(7)
+    for name, levels in (("gts", None), ("lts_2to1", rng.integers(0, 2, size=e ** 3))):
+        ev = DgEvolution(bricks, N_PTS, device=dev, time_stepper="adams_bashforth", order=3,
+                         step_levels=levels)
+        ev.set_initial_data("gaussian", [1.0, 0.5, math.pi, math.pi, math.pi])
+        ev.step(4, DT)  # self-start + switch + steady slabs
+        info = ev.adams_info()
+        stream = torch.cuda.ExternalStream(ev.stream_ptr(), device=dev)
+        e0 = torch.cuda.Event(enable_timing=True)
+        e1 = torch.cuda.Event(enable_timing=True)
+        torch.cuda.synchronize()
+        e0.record(stream)
+        ev.step(slabs, DT, sync=False)
+        e1.record(stream)
+        e1.synchronize()
+        ms = e0.elapsed_time(e1)
+        pts = info["rhs_points_per_slab"]
+        launches = info["launches_per_slab"] * slabs
+        r = {"value": pts * slabs / (ms * 1e-3), "unit": UNIT, "ms_per_slab": ms / slabs,
+             "gpu_launches": launches, "ring_slots": info["ring_slots"],
+             "rhs_points_per_slab": pts}
+        if name == "gts":
+            bpp = ab_bytes_per_point(3, N_PTS)
+            gbs = bpp * pts * slabs / (ms * 1e-3) / 1e9
+            r["roofline"] = {"bound": "hbm", "achieved": gbs, "unit": "GB/s",
+                             "bytes_per_point_launch": bpp, "avg_launch_ms": ms / launches}
+        else:
+            r["elements_per_level"] = [int((levels == 0).sum()), int((levels == 1).sum())]
+        out[name] = r
+        ev.close()
+    return out
+
+
 def run_ours(args):
     import torch
     from spectre_gb300 import PRECISION_FP64, PRECISION_MIXED
@@ -492,6 +549,15 @@ def run_ours(args):
     adjoint = None
     if not args.no_adjoint:
         adjoint = time_adjoint(dev)
+    adams = None
+    if not args.no_adams:
+        adams = time_adams(args, dev)
+        peak = hbm or 1.0
+        adams["gts"]["roofline"]["peak"] = hbm
+        adams["gts"]["roofline"]["frac"] = adams["gts"]["roofline"]["achieved"] / peak
+        # per unit of simulated time at the same step: AB3 takes one launch
+        # per step where SSP-RK3 takes three
+        adams["time_to_solution_speedup_vs_rk3_fp64"] = (ms / args.steps) / adams["gts"]["ms_per_slab"]
     curved = None
     if not args.no_curved:
         curved = time_curved(args, dev, rank == 0 and not args.no_cpu_baseline)
@@ -527,6 +593,7 @@ def run_ours(args):
                                   "DFMA/DADD throughput probe on this pool's GB300"},
             "autotune": autotune,
             "mixed": mixed, "batched": batched, "adjoint": adjoint, "curved": curved,
+            "adams": adams,
             "cpu_baseline": cpu, "e2e": e2e, "clocks": clocks,
             "gpu_launches": 3 * args.steps,
             "gpu_launches_note": "stage kernels of the timed FP64 region (one launch per stage)",
@@ -548,6 +615,7 @@ def main():
     ap.add_argument("--no-batched", action="store_true")
     ap.add_argument("--no-adjoint", action="store_true")
     ap.add_argument("--no-curved", action="store_true")
+    ap.add_argument("--no-adams", action="store_true")
     ap.add_argument("--curved-steps", type=int, default=0,
                     help="SSP-RK3 steps of the curved shell run (default 1000)")
     ap.add_argument("--curved-only", action="store_true",

@@ -21,8 +21,10 @@
 //  2. optionally restore the initial values (self-start resets),
 //  3. record the new state: its volume time derivative
 //     (TimeDerivative.cpp:37-44, no boundary terms) into ring slot rec_slot
-//     of F, and per face point (P, Q) = (Pi - gamma2 Psi, Phi_d) into the
-//     same slot of B, from which any later step forms w = P - s Q.
+//     of F, and per face point, with P = Pi - gamma2 Psi, Q = Phi_d and s
+//     the face's sign, the pair (P - s Q, P + s Q) into the same slot of B:
+//     the first is this element's w on the face, the second the w the
+//     neighbour across the face forms with its own (opposite) sign.
 // The new record's slot is never one this launch reads (the schedule keeps
 // it out), so elements of one launch do not race.
 //
@@ -51,15 +53,25 @@ constexpr int ab_epb() {
   return N <= 4 ? 8 : (N <= 6 ? 4 : (N <= 10 ? 2 : 1));
 }
 
-// w = P - s Q of face record `slot` of element e, face dir, point t
+// face record of element rec's face dir at point t: side 0 is the element's
+// own w there, side 1 the w of the neighbour's sign
 __device__ __forceinline__ double face_w(const double* __restrict__ B, int64_t rec, int dir, int t,
-                                         int NN, double s) {
-  const double* p = B + (rec * 6 + dir) * 2 * (int64_t)NN + t;
-  return fma(-s, p[NN], p[0]);
+                                         int NN, int side) {
+  return __ldg(B + ((rec * 6 + dir) * 2 + side) * (int64_t)NN + t);
+}
+
+// resident blocks per SM asked of the register allocator: the FP64 pipe binds
+// this kernel, and more resident elements overlap one element's loads with
+// another's arithmetic (at N = 8, four blocks measured 1.14x faster than
+// three despite a few spilled registers)
+template <int N>
+constexpr int ab_min_blocks() {
+  return N == 8 ? 4 : 1;
 }
 
 template <int N, int EPB>
-__global__ void __launch_bounds__(N * N * EPB) ab_step_kernel(const __grid_constant__ AbArgs A) {
+__global__ void __launch_bounds__(N * N * EPB, ab_min_blocks<N>())
+    ab_step_kernel(const __grid_constant__ AbArgs A) {
   using S = AbShape<N>;
   constexpr int NN = S::NN, NP = S::NP, TAB = S::TAB, h = S::h, H = S::H;
   extern __shared__ double smem[];
@@ -77,7 +89,7 @@ __global__ void __launch_bounds__(N * N * EPB) ab_step_kernel(const __grid_const
   const bool active = j >= 0;
   const AbLevelJob& J = A.L.job[active ? j : 0];
   const int64_t e = active ? (int64_t)A.list[J.begin + g] : 0;
-  const bool update = active && J.update;
+  const bool update = active && J.update && !J.reset;
   double* U = smem + slot * S::SLOT;  // Psi, Pi, Phi_x, Phi_y, Phi_z
   double* Sacc = U + 5 * NP;          // running dt Pi
   double* T = Sacc + NP;              // three scaled split tables
@@ -86,34 +98,8 @@ __global__ void __launch_bounds__(N * N * EPB) ab_step_kernel(const __grid_const
   const double g2 = A.gamma2;
 
   double jd[3] = {0.0, 0.0, 0.0};
-  if (active) {
+  if (active)
     for (int d = 0; d < 3; ++d) jd[d] = A.jac[3 * e + d];
-    const double* src = (J.reset ? A.u0 : A.u) + off;
-    for (int q = t; q < 5 * NP; q += NN) U[q] = src[q];
-    for (int q = t; q < 3 * TAB; q += NN) {
-      const int d = q / TAB, r = q - d * TAB;
-      double v;
-      if (r < H * h)
-        v = A.eo.A[r / h][r % h];
-      else if (r < 2 * H * h)
-        v = A.eo.B[(r - H * h) / h][(r - H * h) % h];
-      else
-        v = A.eo.M[r - 2 * H * h];
-      T[q] = -jd[d] * v;
-    }
-  }
-  __syncthreads();
-
-  // 1. volume part of the step
-  if (update && !J.reset) {
-    for (int q = t; q < 5 * NP; q += NN) {
-      double acc = U[q];
-      for (int i = 0; i < J.n_vol; ++i)
-        acc = fma(J.vol_c[i], A.F[((int64_t)J.vol_slot[i] * E + e) * (kVars * NP) + q], acc);
-      U[q] = acc;
-    }
-  }
-  __syncthreads();
 
   const int ta = t % N, tb = t / N;
   auto line = [&](int d, int& base, int& stride) {
@@ -129,29 +115,62 @@ __global__ void __launch_bounds__(N * N * EPB) ab_step_kernel(const __grid_const
     }
   };
 
-  // 1b. boundary delta, one axis at a time (edge points belong to faces of
-  // two axes)
-#pragma unroll 1
+  // 1a. boundary delta of this thread's six face points (the ends of its
+  // line along each axis).  The loops run to the job's own term counts
+  // (uniform in a warp): no issue slots are spent on absent terms.
+  double dwf[6] = {0.0, 0.0, 0.0, 0.0, 0.0, 0.0};
+  if (update) {
+#pragma unroll
+    for (int dir = 0; dir < 6; ++dir) {
+      const int64_t nb = A.nbr[6 * e + dir];
+      const AbFaceTable& f = J.face[A.level[nb]];
+      double wi = 0.0, we = 0.0;
+      for (int i = 0; i < f.n_loc; ++i)
+        wi = fma(f.loc_c[i], face_w(A.B, (int64_t)f.loc_slot[i] * E + e, dir, t, NN, 0), wi);
+      for (int i = 0; i < f.n_rem; ++i)
+        we = fma(f.rem_c[i], face_w(A.B, (int64_t)f.rem_slot[i] * E + nb, dir ^ 1, t, NN, 1), we);
+      dwf[dir] = -0.25 * (double)(N * (N - 1)) * jd[dir >> 1] * (wi - we);
+    }
+  }
+
+  // 1b. state (the initial values on a reset) plus the volume part of the
+  // step, u + sum_j c_j F_j, accumulated in shared memory one record at a
+  // time (each thread updates only its own points: no barrier in between)
+  if (active) {
+    const double* src = (J.reset ? A.u0 : A.u) + off;
+    for (int q = t; q < 5 * NP; q += NN) U[q] = src[q];
+    if (update)
+      for (int i = 0; i < J.n_vol; ++i) {
+        const double c = J.vol_c[i];
+        const double* Fi = A.F + ((int64_t)J.vol_slot[i] * E + e) * (kVars * NP);
+        for (int q = t; q < 5 * NP; q += NN) U[q] = fma(c, __ldg(Fi + q), U[q]);
+      }
+    for (int q = t; q < 3 * TAB; q += NN) {
+      const int d = q / TAB, r = q - d * TAB;
+      double v;
+      if (r < H * h)
+        v = A.eo.A[r / h][r % h];
+      else if (r < 2 * H * h)
+        v = A.eo.B[(r - H * h) / h][(r - H * h) % h];
+      else
+        v = A.eo.M[r - 2 * H * h];
+      T[q] = -jd[d] * v;
+    }
+  }
+  __syncthreads();
+
+  // 1c. the boundary delta added to the face points, one axis at a time
+  // (edge points belong to faces of two axes)
+#pragma unroll
   for (int d = 0; d < 3; ++d) {
-    if (update && !J.reset) {
+    if (update) {
       int base, stride;
       line(d, base, stride);
-      const double gf = -0.25 * (double)(N * (N - 1)) * jd[d];
-      for (int up = 0; up < 2; ++up) {
-        const int dir = 2 * d + up;
-        const double s = up ? 1.0 : -1.0;
-        const int64_t nb = A.nbr[6 * e + dir];
-        const AbFaceTable& f = J.face[A.level[nb]];
-        double wi = 0.0, we = 0.0;
-        for (int i = 0; i < f.n_loc; ++i)
-          wi = fma(f.loc_c[i], face_w(A.B, (int64_t)f.loc_slot[i] * E + e, dir, t, NN, s), wi);
-        for (int i = 0; i < f.n_rem; ++i)
-          we = fma(f.rem_c[i], face_w(A.B, (int64_t)f.rem_slot[i] * E + nb, dir ^ 1, t, NN, s), we);
-        const double dw = gf * (wi - we);
-        const int p = base + (up ? (N - 1) * stride : 0);
-        U[NP + p] += dw;
-        U[(2 + d) * NP + p] = fma(-s, dw, U[(2 + d) * NP + p]);
-      }
+      const int p0 = base, p1 = base + (N - 1) * stride;
+      U[NP + p0] += dwf[2 * d];
+      U[(2 + d) * NP + p0] += dwf[2 * d];         // -s dw, s = -1
+      U[NP + p1] += dwf[2 * d + 1];
+      U[(2 + d) * NP + p1] -= dwf[2 * d + 1];     // -s dw, s = +1
     }
     __syncthreads();
   }
@@ -188,12 +207,15 @@ __global__ void __launch_bounds__(N * N * EPB) ab_step_kernel(const __grid_const
       }
 #pragma unroll
       for (int i = 0; i < N; ++i) Fo[(2 + d) * NP + base + i * stride] = dP[i];
+        // lower face (s = -1): own w = P + Q, the neighbour's P - Q; upper
+      // face (s = +1): own P - Q, the neighbour's P + Q
       double* b_lo = Bo + (2 * d) * 2 * NN;
       double* b_hi = Bo + (2 * d + 1) * 2 * NN;
-      b_lo[t] = fma(-g2, psi_lo, up[0]);
-      b_lo[NN + t] = uf[0];
-      b_hi[t] = fma(-g2, psi_hi, up[N - 1]);
-      b_hi[NN + t] = uf[N - 1];
+      const double p_lo = fma(-g2, psi_lo, up[0]), p_hi = fma(-g2, psi_hi, up[N - 1]);
+      b_lo[t] = p_lo + uf[0];
+      b_lo[NN + t] = p_lo - uf[0];
+      b_hi[t] = p_hi - uf[N - 1];
+      b_hi[NN + t] = p_hi + uf[N - 1];
       if (d < 2) {
 #pragma unroll
         for (int i = 0; i < N; ++i) {

@@ -39,7 +39,7 @@ struct AbArgs {
   double* u = nullptr;         // state, updated in place
   const double* u0 = nullptr;  // initial values (self-start resets)
   double* F = nullptr;         // ring slots x elements x 5 N^3 volume time derivatives
-  double* B = nullptr;         // ring slots x elements x 6 faces x (P, Q) x N^2
+  double* B = nullptr;         // ring slots x elements x 6 faces x (own w, neighbour w) x N^2
   const int32_t* nbr = nullptr;
   const double* jac = nullptr;
   const int32_t* list = nullptr;  // element ids sorted by level

@@ -426,12 +426,21 @@ def time_curved(args, dev, with_cpu):
 def ab_bytes_per_point(order, n):
     """Compulsory HBM bytes per grid point of one AdamsBashforth launch of an
     element (update + record, global stepping): read u and `order` recorded
-    time derivatives, write u and the new record (5 FP64 vars each); on the
-    faces read `order` own and `order` neighbour records of (P, Q) per face
-    point of the six faces and write the new ones."""
+    time derivatives, write u and the new record (5 FP64 vars each); of the
+    face records (12 n^2 values per element: both w's of six faces) read
+    `order` (each value once: its element reads one w, the neighbour the
+    other) and write one."""
     vol = (5 + 5 * order + 5 + 5) * 8.0
-    faces = (6 * 2 * order * 2 + 12) * n * n * 8.0 / n ** 3
+    faces = (12 * order + 12) * n * n * 8.0 / n ** 3
     return vol + faces
+
+
+# FP64 thread instructions per grid point of one AB3 launch at N = 8 (update
+# + record): DFMA 156.7M + DADD 76.8M + DMUL 30.0M per launch on the 20^3 x
+# 8^3 case (ncu sass op counters, 4,096,000 points)
+AB3_FP64_INST_PER_POINT = (156.672e6 + 76.8e6 + 30.048e6) / 4096000
+# DRAM read + write per launch of that capture, per point
+AB3_TRAFFIC_PER_POINT = (814.1e6 + 415.1e6) / 4096000
 
 
 def time_adams(args, dev):
@@ -472,7 +481,15 @@ def time_adams(args, dev):
             bpp = ab_bytes_per_point(3, N_PTS)
             gbs = bpp * pts * slabs / (ms * 1e-3) / 1e9
             r["roofline"] = {"bound": "hbm", "achieved": gbs, "unit": "GB/s",
-                             "bytes_per_point_launch": bpp, "avg_launch_ms": ms / launches}
+                             "bytes_per_point_launch": bpp, "avg_launch_ms": ms / launches,
+                             "traffic": AB3_TRAFFIC_PER_POINT * pts,
+                             "traffic_note": "ncu DRAM bytes per launch, 20^3 capture scaled "
+                                             "by points"}
+            inst = AB3_FP64_INST_PER_POINT * pts * slabs / (ms * 1e-3) / 1e12
+            r["fp64_pipe"] = {"achieved_tinst_s": inst, "peak_tinst_s": FP64_PEAK_TINST,
+                              "frac": inst / FP64_PEAK_TINST,
+                              "inst_per_point_launch": AB3_FP64_INST_PER_POINT,
+                              "note": "the FP64 pipe binds this kernel"}
         else:
             r["elements_per_level"] = [int((levels == 0).sum()), int((levels == 1).sum())]
         out[name] = r

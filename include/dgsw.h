@@ -221,6 +221,15 @@ int dgsw_boundary_terms_device(int64_t npts, const double* packaged_int,
  * TimeStepper::update_u one substep at a time. */
 int dgsw_step(DgswHandle h, int n_steps, double dt);
 int dgsw_substep(DgswHandle h, int k, double dt);
+/* n_steps of dgsw_step on a state that lives in host memory: host_u is read,
+ * stepped on the device and written back in place before the call returns
+ * (the handle's device state ends equal to it).  On the plain FP64 path of
+ * handles with at least 4096 elements the copies are cut into element chunks
+ * overlapped with the stages of the first and the last step (a stage of a
+ * chunk waits only for the chunks holding its face neighbours); otherwise
+ * the whole state is copied around the steps.  host_u should be pinned
+ * (cudaHostAlloc / cudaHostRegister) for full link bandwidth. */
+int dgsw_step_host(DgswHandle h, double* host_u, int n_steps, double dt);
 
 /* ---- TimeStepper (AdamsBashforth, local time stepping) -------------------
  * Handles with time_stepper DGSW_STEPPER_ADAMS_BASHFORTH: flat system,

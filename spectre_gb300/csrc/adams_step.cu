@@ -242,8 +242,8 @@ template <int N>
 cudaError_t launch_n(const AbArgs& A, cudaStream_t s) {
   constexpr int EPB = ab_epb<N>();
   const size_t smem = (size_t)EPB * AbShape<N>::SLOT * sizeof(double);
-  auto k = ab_step_kernel<N, EPB>;
-  cudaError_t err = cudaFuncSetAttribute(k, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+  constexpr auto k = ab_step_kernel<N, EPB>;
+  cudaError_t err = set_kernel_smem<k>((int)smem, false);
   if (err != cudaSuccess) return err;
   int64_t total = 0;
   for (int q = 0; q < A.L.n_jobs; ++q) total += A.L.job[q].count;

@@ -2,6 +2,7 @@
 // units and the C-ABI layer.
 #pragma once
 
+#include <atomic>
 #include <cstdint>
 #include <cuda_runtime.h>
 
@@ -9,6 +10,30 @@
 #include "common.cuh"
 
 namespace dgsw {
+
+// Dynamic shared memory size (and, optionally, the largest shared-memory
+// carveout) of a kernel, set once per device: the attributes persist for the
+// process, and setting them on every launch costs host time that a chain of
+// small launches notices.
+template <auto Kernel>
+cudaError_t set_kernel_smem(int smem, bool max_carveout) {
+  static std::atomic<uint64_t> done{0};
+  static std::atomic<int> done_smem[64];
+  int dev = 0;
+  cudaError_t e = cudaGetDevice(&dev);
+  if (e != cudaSuccess) return e;
+  const bool tracked = dev >= 0 && dev < 64;
+  if (tracked && ((done.load() >> dev) & 1) && done_smem[dev].load() >= smem) return cudaSuccess;
+  e = cudaFuncSetAttribute(Kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, smem);
+  if (e == cudaSuccess && max_carveout)
+    e = cudaFuncSetAttribute(Kernel, cudaFuncAttributePreferredSharedMemoryCarveout,
+                             cudaSharedmemCarveoutMaxShared);
+  if (e == cudaSuccess && tracked) {
+    done_smem[dev].store(smem);
+    done.fetch_or(uint64_t(1) << dev);
+  }
+  return e;
+}
 
 // One fused RHS / RK-substep launch over elements of a uniform extent n.
 struct StageLaunch {
@@ -28,6 +53,10 @@ struct StageLaunch {
   const int32_t* face_idx = nullptr;
   const double* wext = nullptr;
   int variant = 0;  // launch-configuration candidate of the stage modes (0 or 1)
+  // the elements [elem_begin, elem_begin + elem_count) only (count < 0: to
+  // the end); neighbours are read wherever they are
+  int64_t elem_begin = 0;
+  int64_t elem_count = -1;
 };
 
 cudaError_t launch_stage_fp64(const StageLaunch& L, cudaStream_t s);

@@ -58,15 +58,16 @@ __global__ void __launch_bounds__(N * N * EPB, MINB)
     stage_fp64_kernel(const double* ucur, const double* u0, double* unext,
                       const int32_t* __restrict__ nbr, const double* __restrict__ jac,
                       int64_t n_elem, StageCoef coef, double gamma2, EoTable eo,
-                      const int32_t* __restrict__ face_idx, const double* __restrict__ wext) {
+                      const int32_t* __restrict__ face_idx, const double* __restrict__ wext,
+                      int64_t elem_begin, int64_t elem_end) {
   using S = Shape<N>;
   constexpr int NN = S::NN, NP = S::NP, TAB = S::TAB, h = S::h, H = S::H;
   constexpr bool kBoundary = MODE != kModeVolume;
   extern __shared__ double smem[];
   const int slot = threadIdx.x / NN;
   const int t = threadIdx.x - slot * NN;
-  const int64_t e = (int64_t)blockIdx.x * EPB + slot;
-  const bool active = e < n_elem;
+  const int64_t e = elem_begin + (int64_t)blockIdx.x * EPB + slot;
+  const bool active = e < elem_end;
   double* F = smem + slot * S::SLOT;  // Pi, Phi_x, Phi_y, Phi_z of ucur
   double* Sacc = F + 4 * NP;         // running c * (dt Pi)
   double* T = Sacc + NP;             // three scaled split tables
@@ -235,18 +236,17 @@ template <int N, int MODE, int V = 0>
 cudaError_t launch_n(const StageLaunch& L, cudaStream_t s) {
   constexpr int EPB = elems_per_block<N, V>();
   const size_t smem = (size_t)EPB * Shape<N>::SLOT * sizeof(double);
-  auto k = stage_fp64_kernel<N, EPB, min_blocks<N, V>(), MODE>;
-  cudaError_t err = cudaFuncSetAttribute(k, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+  constexpr auto k = stage_fp64_kernel<N, EPB, min_blocks<N, V>(), MODE>;
+  // several resident blocks per SM overlap one block's loads and barriers
+  // with another's FP64 work: the largest carveout
+  cudaError_t err = set_kernel_smem<k>((int)smem, true);
   if (err != cudaSuccess) return err;
-  // two resident blocks per SM overlap one block's loads and barriers with
-  // the other's FP64 work
-  err = cudaFuncSetAttribute(k, cudaFuncAttributePreferredSharedMemoryCarveout,
-                             cudaSharedmemCarveoutMaxShared);
-  if (err != cudaSuccess) return err;
-  const int64_t blocks = (L.n_elem + EPB - 1) / EPB;
+  const int64_t count = L.elem_count < 0 ? L.n_elem - L.elem_begin : L.elem_count;
+  const int64_t blocks = (count + EPB - 1) / EPB;
   if (blocks <= 0) return cudaSuccess;
   k<<<(unsigned)blocks, N * N * EPB, smem, s>>>(L.ucur, L.u0, L.unext, L.nbr, L.jac, L.n_elem,
-                                                 L.coef, L.gamma2, L.eo, L.face_idx, L.wext);
+                                                 L.coef, L.gamma2, L.eo, L.face_idx, L.wext,
+                                                 L.elem_begin, L.elem_begin + count);
   return cudaGetLastError();
 }
 

@@ -118,6 +118,7 @@ _SIGNATURES = {
     "dgsw_package_data_device": (_I, [_I64, _P, _P, _P, _P, _P, _P, _P, _P]),
     "dgsw_boundary_terms_device": (_I, [_I64, _P, _P, _P, _P]),
     "dgsw_step": (_I, [_P, _I, _D]),
+    "dgsw_step_host": (_I, [_P, _P, _I, _D]),
     "dgsw_set_exponential_filter": (_I, [_P, _D, _I, _I]),
     "dgsw_observe_norms": (_I, [_P, _P, _P, _P]),
     "dgsw_check_device_timeout": (_I, [_P, _D]),
@@ -643,6 +644,15 @@ class DgEvolution:
         _check(lib().dgsw_step(self._h, int(n_steps), float(dt)), self._h)
         if sync:
             self.synchronize()
+
+    def step_host(self, u, n_steps: int, dt: float):
+        """n_steps on a host state (numpy float64, contiguous; pinned memory,
+        e.g. a torch pin_memory tensor's numpy view, for full bandwidth),
+        stepped in place: the copies overlap the first and last steps."""
+        a = u if isinstance(u, np.ndarray) else u.numpy()
+        assert a.dtype == np.float64 and a.flags["C_CONTIGUOUS"] and a.size == self.state_size
+        _check(lib().dgsw_step_host(self._h, _ptr(a), int(n_steps), float(dt)), self._h)
+        return a
 
     def substep(self, k: int, dt: float):
         _check(lib().dgsw_substep(self._h, int(k), float(dt)), self._h)

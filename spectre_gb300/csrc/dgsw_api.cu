@@ -1292,6 +1292,30 @@ int dgsw_create(const DgswConfig* cfg, DgswHandle* out) {
     delete h;
     return fail(nullptr, DGSW_ERR_UNSUPPORTED, "mixed precision needs gamma2 = 0");
   }
+  if (cfg->time_stepper == DGSW_STEPPER_ADAMS_BASHFORTH) {
+    // checked before any device work, so that a bad request fails the same
+    // way with or without a GPU
+    int code = DGSW_OK;
+    const char* why = nullptr;
+    if (h->curved || h->refined || h->gauss || !h->dom.uniform ||
+        cfg->precision != DGSW_PRECISION_FP64) {
+      code = DGSW_ERR_UNSUPPORTED;
+      why = "AdamsBashforth: flat system, Gauss-Lobatto, one extent, conforming bricks, FP64";
+    } else if (cfg->stepper_order < 0 || cfg->stepper_order > kAbMaxOrder) {
+      code = DGSW_ERR_ARGUMENT;
+      why = "AdamsBashforth order must be in [1, 8] (0: 3)";
+    } else if (cfg->step_levels) {
+      for (int64_t e = 0; e < h->dom.n_elem && !why; ++e)
+        if (cfg->step_levels[e] < 0 || cfg->step_levels[e] >= kAbMaxLevels) {
+          code = DGSW_ERR_ARGUMENT;
+          why = "step levels must be in [0, 3]";
+        }
+    }
+    if (why) {
+      delete h;
+      return fail(nullptr, code, why);
+    }
+  }
   int count = 0;
   if (cudaGetDeviceCount(&count) != cudaSuccess || count <= cfg->device || cfg->device < 0) {
     delete h;

@@ -134,6 +134,34 @@ def test_null_handle_is_an_error_not_a_crash(dgsw_lib):
     assert L.dgsw_create(None, None) == -1
 
 
+def test_adams_configs_rejected_before_any_device_work(dgsw_lib):
+    # bad AdamsBashforth requests fail with their own status, with or
+    # without a GPU (a valid request here reaches the device check)
+    import ctypes
+    L = dgsw_lib.lib()
+    E = 4 * 4 * 4
+
+    def create(levels=None, order=3, precision=dgsw.PRECISION_FP64, points=4):
+        holder = dgsw._ConfigHolder([dgsw.Brick((4, 4, 4))], points, precision=precision,
+                                    time_stepper="adams_bashforth", order=order,
+                                    step_levels=levels)
+        h = ctypes.c_void_p()
+        return L.dgsw_create(ctypes.byref(holder.cfg), ctypes.byref(h)), h
+
+    rc, _ = create(levels=np.full(E, 4, np.int32))
+    assert rc == -1 and b"step levels" in L.dgsw_last_error(None)
+    rc, _ = create(order=9)
+    assert rc == -1 and b"order" in L.dgsw_last_error(None)
+    rc, _ = create(precision=dgsw.PRECISION_MIXED)
+    assert rc == -3
+    rc, _ = create(points=np.full(E, 4, np.int32).tolist()[:-1] + [5])
+    assert rc == -3
+    rc, h = create(levels=np.zeros(E, np.int32))
+    assert rc in (0, -5)  # ok with a GPU, no device without one
+    if rc == 0:
+        L.dgsw_destroy(h)
+
+
 # ---------------- curved shell: maps and geometry against the oracle ----------------
 
 SHELLS = [dict(ref_ang=0, ref_rad=0, n=4), dict(ref_ang=1, ref_rad=2, n=5),

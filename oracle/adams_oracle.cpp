@@ -30,6 +30,7 @@
 #include <deque>
 #include <vector>
 
+#include "adams_oracle.hpp"
 #include "dgsw_oracle.h"
 
 namespace {
@@ -233,16 +234,15 @@ int lts_coefficients(const std::vector<Id>& local, const std::vector<Id>& remote
 }  // namespace
 
 // ---------------------------------------------------------------------------
-// Flat scalar wave on conforming periodic bricks, uniform extent n, stepped by
-// AdamsBashforth with local time stepping.  Every element keeps the
-// reference's three histories: the volume history of dt u (no boundary
-// terms), and per mortar the local and remote boundary histories of packaged
-// face data (dg_package_data).  A step records dt u and the face data,
-// updates u with the volume part at once, adds the boundary delta when the
-// step ends, then cleans the histories.
+// The evolution.  Every element keeps the reference's three histories: the
+// volume history of dt u (no internal mortar terms), and per internal mortar
+// the local and remote boundary histories of packaged face data
+// (dg_package_data).  A step records dt u and the face data, updates u with
+// the volume part at once, adds the boundary delta when the step ends, then
+// cleans the histories.
+namespace orc_adams {
 namespace {
 
-constexpr int kPkgA = 16;  // packaged doubles per face point
 constexpr int kVarsA = 5;
 
 struct LocalEntry {
@@ -277,21 +277,116 @@ int64_t face_volume_index(int n, int d, int slice, int a, int b) {
   }
 }
 
-struct LtsRun {
+struct Run {
+  System& sys;
+  std::vector<Elem> el;
+  Clock clk;
+  explicit Run(System& s) : sys(s), el(s.E) {}
+
+  // ComputeTimeDerivative for the listed elements: dt u into the volume
+  // history, face packages into the own local and the neighbours' remote
+  // boundary histories
+  void record(const double* u, const std::vector<int64_t>& who, Id id, int order) {
+    std::vector<double> dudt((size_t)sys.E * kVarsA * sys.np);
+    sys.volume_rhs(u, dudt.data());
+    const int64_t per = kVarsA * sys.np;
+    for (int64_t e : who) {
+      el[e].vol.push_back(
+          {id, order, std::vector<double>(dudt.begin() + e * per, dudt.begin() + (e + 1) * per)});
+      for (int dir = 0; dir < 6; ++dir) {
+        const int64_t nb = sys.neighbor(e, dir);
+        if (nb < 0) continue;
+        LocalEntry le{id, order, {}, {}};
+        sys.package(u, e, dir, &le.pkg, &le.mag);
+        el[e].mortar[dir].local.push_back(std::move(le));
+        const int bd = sys.back_dir(e, dir);
+        RemoteEntry re{id, {}};
+        sys.exterior_package(u, nb, bd, &re.pkg);
+        el[nb].mortar[bd].remote.push_back(std::move(re));
+      }
+    }
+  }
+
+  // AdamsBashforth::update_u_impl with the element's volume history
+  int volume_update(double* u, int64_t e, int64_t start, int64_t end) const {
+    const std::deque<VolEntry>& h = el[e].vol;
+    const int order = h.back().order;
+    if ((int)h.size() != order) return -3;
+    std::vector<int64_t> t;
+    for (const VolEntry& v : h) t.push_back(v.id.tick);
+    const std::vector<double> c = coefficients(t, start, end, clk);
+    double* ue = u + e * kVarsA * sys.np;
+    for (int j = 0; j < order; ++j)
+      for (int64_t p = 0; p < kVarsA * sys.np; ++p) ue[p] += c[j] * h[j].dt[p];
+    return 0;
+  }
+
+  // AdamsBashforth::add_boundary_delta_impl on every internal mortar, the
+  // coupling being dg_boundary_terms lifted onto the GLL face; then
+  // add_slice_to_data
+  int boundary_delta(double* u, int64_t e, int64_t start, int64_t end) const {
+    const int n = sys.n, nf = n * n;
+    double* ue = u + e * kVarsA * sys.np;
+    const double slice_factor = -0.5 * (double)(n * (n - 1));
+    for (int dir = 0; dir < 6; ++dir) {
+      if (sys.neighbor(e, dir) < 0) continue;
+      const Mortar& m = el[e].mortar[dir];
+      std::vector<Id> lid, rid;
+      for (const LocalEntry& x : m.local) lid.push_back(x.id);
+      for (const RemoteEntry& x : m.remote) rid.push_back(x.id);
+      std::vector<Term> terms;
+      const int ord = m.local.back().order;
+      const int rc = lts_coefficients(lid, rid, start, end, ord, ord, ord, clk, &terms);
+      if (rc) return rc;
+      std::vector<double> lifted((size_t)kVarsA * nf, 0.0), bc((size_t)kVarsA * nf);
+      for (const Term& t : terms) {
+        const LocalEntry& L = m.local[t.local];
+        sys.boundary_terms(L.pkg, m.remote[t.remote].pkg, bc.data());
+        for (int v = 0; v < kVarsA; ++v)
+          for (int f = 0; f < nf; ++f)
+            lifted[(size_t)v * nf + f] += t.coef * (bc[(size_t)v * nf + f] * (slice_factor * L.mag[f]));
+      }
+      const int d = dir / 2, slice = (dir % 2) ? n - 1 : 0;
+      for (int b = 0; b < n; ++b)
+        for (int a = 0; a < n; ++a) {
+          const int64_t vi = face_volume_index(n, d, slice, a, b);
+          for (int v = 0; v < kVarsA; ++v) ue[v * sys.np + vi] += lifted[(size_t)v * nf + a + n * b];
+        }
+    }
+    return 0;
+  }
+
+  // AdamsBashforth::clean_history_impl and clean_boundary_history_impl
+  void clean(int64_t e) {
+    std::deque<VolEntry>& h = el[e].vol;
+    const size_t order = (size_t)h.back().order;
+    while (h.size() >= order) h.pop_front();
+    for (int dir = 0; dir < 6; ++dir) {
+      Mortar& m = el[e].mortar[dir];
+      if (m.local.empty()) continue;
+      const size_t ob = (size_t)m.local.back().order;
+      while (m.local.size() >= ob) m.local.pop_front();
+      while (m.remote.size() > ob) m.remote.pop_front();
+    }
+  }
+};
+
+// Flat scalar wave on conforming periodic bricks of uniform extent n
+struct FlatSystem : System {
   int n_inst;
   const OrcBrick* br;
-  int n;
-  int64_t E, np;
   double gamma2;
   int threads;
   std::vector<int32_t> elem_n, nbr, inst;
   std::vector<double> invjac;  // 3 per element
-  std::vector<Elem> el;
-  Clock clk;
 
-  // the face package of element e in direction dir (outward normal)
+  int64_t neighbor(int64_t e, int dir) const override { return nbr[6 * e + dir]; }
+  int back_dir(int64_t, int dir) const override { return dir ^ 1; }
+  void volume_rhs(const double* u, double* dudt) override {
+    orc_volume_rhs(n_inst, br, elem_n.data(), gamma2, u, dudt, threads);
+  }
   void package(const double* u, int64_t e, int dir, std::vector<double>* pkg,
-               std::vector<double>* mag) const {
+               std::vector<double>* mag) const override {
     const int d = dir / 2, nf = n * n;
     const bool upper = dir % 2;
     const int slice = upper ? n - 1 : 0;
@@ -307,171 +402,29 @@ struct LtsRun {
         for (int i = 0; i < 3; ++i) phi[i * nf + f] = ue[(2 + i) * np + v];
         nrm[d * nf + f] = upper ? 1.0 : -1.0;
       }
-    pkg->assign((size_t)kPkgA * nf, 0.0);
+    pkg->assign((size_t)16 * nf, 0.0);
     double ms;
     orc_package(nf, psi.data(), pi.data(), phi.data(), g2.data(), nrm.data(), nullptr, pkg->data(),
                 &ms);
   }
-
-  // ComputeTimeDerivative for the listed elements: dt u (volume terms only)
-  // into the volume history, face packages into the own local and the
-  // neighbours' remote boundary histories.
-  void record(const double* u, const std::vector<int64_t>& who, Id id, int order) {
-    std::vector<double> dudt((size_t)E * kVarsA * np);
-    orc_volume_rhs(n_inst, br, elem_n.data(), gamma2, u, dudt.data(), threads);
-    for (int64_t e : who) {
-      VolEntry v{id, order, std::vector<double>(dudt.begin() + e * kVarsA * np,
-                                                 dudt.begin() + (e + 1) * kVarsA * np)};
-      el[e].vol.push_back(std::move(v));
-      for (int dir = 0; dir < 6; ++dir) {
-        LocalEntry le{id, order, {}, {}};
-        package(u, e, dir, &le.pkg, &le.mag);
-        el[nbr[6 * e + dir]].mortar[dir ^ 1].remote.push_back({id, le.pkg});
-        el[e].mortar[dir].local.push_back(std::move(le));
-      }
-    }
+  void exterior_package(const double* u, int64_t e, int dir,
+                        std::vector<double>* pkg) const override {
+    std::vector<double> mag;
+    package(u, nbr[6 * e + dir], dir ^ 1, pkg, &mag);  // aligned bricks: same point order
   }
-
-  // AdamsBashforth::update_u_impl with the element's volume history
-  int volume_update(double* u, int64_t e, int64_t start, int64_t end) const {
-    const std::deque<VolEntry>& h = el[e].vol;
-    const int order = h.back().order;
-    if ((int)h.size() != order) return -3;
-    std::vector<int64_t> t;
-    for (const VolEntry& v : h) t.push_back(v.id.tick);
-    const std::vector<double> c = coefficients(t, start, end, clk);
-    double* ue = u + e * kVarsA * np;
-    for (int j = 0; j < order; ++j)
-      for (int64_t p = 0; p < kVarsA * np; ++p) ue[p] += c[j] * h[j].dt[p];
-    return 0;
-  }
-
-  // AdamsBashforth::add_boundary_delta_impl on every mortar, the coupling
-  // being the UpwindPenalty correction lifted onto the GLL face; then
-  // add_slice_to_data.
-  int boundary_delta(double* u, int64_t e, int64_t start, int64_t end) const {
-    const int nf = n * n;
-    double* ue = u + e * kVarsA * np;
-    for (int dir = 0; dir < 6; ++dir) {
-      const Mortar& m = el[e].mortar[dir];
-      std::vector<Id> lid, rid;
-      for (const LocalEntry& x : m.local) lid.push_back(x.id);
-      for (const RemoteEntry& x : m.remote) rid.push_back(x.id);
-      std::vector<Term> terms;
-      const int ord = m.local.back().order;
-      const int rc = lts_coefficients(lid, rid, start, end, ord, ord, ord, clk, &terms);
-      if (rc) return rc;
-      std::vector<double> lifted((size_t)kVarsA * nf, 0.0), bc((size_t)kVarsA * nf);
-      const double slice_factor = -0.5 * (double)(n * (n - 1));
-      for (const Term& t : terms) {
-        const LocalEntry& L = m.local[t.local];
-        orc_boundary_terms(nf, L.pkg.data(), m.remote[t.remote].pkg.data(), bc.data());
-        for (int v = 0; v < kVarsA; ++v)
-          for (int f = 0; f < nf; ++f)
-            lifted[(size_t)v * nf + f] += t.coef * (bc[(size_t)v * nf + f] * (slice_factor * L.mag[f]));
-      }
-      const int d = dir / 2, slice = (dir % 2) ? n - 1 : 0;
-      for (int b = 0; b < n; ++b)
-        for (int a = 0; a < n; ++a) {
-          const int64_t vi = face_volume_index(n, d, slice, a, b);
-          for (int v = 0; v < kVarsA; ++v) ue[v * np + vi] += lifted[(size_t)v * nf + a + n * b];
-        }
-    }
-    return 0;
-  }
-
-  // AdamsBashforth::clean_history_impl and clean_boundary_history_impl
-  void clean(int64_t e) {
-    std::deque<VolEntry>& h = el[e].vol;
-    const size_t order = (size_t)h.back().order;
-    while (h.size() >= order) h.pop_front();
-    for (int dir = 0; dir < 6; ++dir) {
-      Mortar& m = el[e].mortar[dir];
-      const size_t ob = (size_t)m.local.back().order;
-      while (m.local.size() >= ob) m.local.pop_front();
-      while (m.remote.size() > ob) m.remote.pop_front();
-    }
+  void boundary_terms(const std::vector<double>& pi, const std::vector<double>& pe,
+                      double* out) const override {
+    orc_boundary_terms(n * n, pi.data(), pe.data(), out);
   }
 };
 
 }  // namespace
 
-extern "C" {
-
-int orc_variable_coefficients(int n, const double* control_times, double step_start,
-                              double step_end, double* out) {
-  if (n < 0 || n > kMaxOrder || (n > 0 && (!control_times || !out))) return -1;
-  const std::vector<double> c =
-      variable_coefficients(std::vector<double>(control_times, control_times + n), step_start,
-                            step_end);
-  std::copy(c.begin(), c.end(), out);
-  return 0;
-}
-
-int orc_adams_coefficients(int n, const int64_t* control_ticks, int64_t step_start,
-                           int64_t step_end, double slab, int64_t ticks_per_slab, double* out) {
-  if (n < 0 || n > kMaxOrder || ticks_per_slab < 1 || (n > 0 && (!control_ticks || !out)))
-    return -1;
-  const Clock clk{slab, ticks_per_slab, 0.0};
-  const std::vector<double> c =
-      coefficients(std::vector<int64_t>(control_ticks, control_ticks + n), step_start, step_end,
-                   clk);
-  std::copy(c.begin(), c.end(), out);
-  return 0;
-}
-
-int orc_lts_coefficients(int n_local, const int64_t* local_slab, const int64_t* local_tick,
-                         int n_remote, const int64_t* remote_slab, const int64_t* remote_tick,
-                         int64_t step_start, int64_t step_end, double slab, int64_t ticks_per_slab,
-                         int local_order, int remote_order, int small_order, int max_out,
-                         int32_t* out_local, int32_t* out_remote, double* out_coef) {
-  for (int o : {local_order, remote_order, small_order})
-    if (o < 1 || o > kMaxOrder) return -1;
-  if (n_local < 0 || n_remote < 0 || ticks_per_slab < 1 || max_out < 0) return -1;
-  std::vector<Id> l(n_local), r(n_remote);
-  for (int i = 0; i < n_local; ++i) l[i] = {local_slab[i], local_tick[i]};
-  for (int i = 0; i < n_remote; ++i) r[i] = {remote_slab[i], remote_tick[i]};
-  std::vector<Term> terms;
-  const int rc = lts_coefficients(l, r, step_start, step_end, local_order, remote_order,
-                                  small_order, Clock{slab, ticks_per_slab, 0.0}, &terms);
-  if (rc) return -2;
-  if ((int)terms.size() > max_out) return -3;
-  for (size_t i = 0; i < terms.size(); ++i) {
-    out_local[i] = terms[i].local;
-    out_remote[i] = terms[i].remote;
-    out_coef[i] = terms[i].coef;
-  }
-  return (int)terms.size();
-}
-
-int orc_evolve_adams(int n_inst, const OrcBrick* br, int n, double gamma2, int order,
-                     const int32_t* levels, double slab, int n_slabs, double* u, int n_threads) {
-  if (n_inst < 1 || !br || n < 2 || n > 20 || order < 1 || order > kMaxOrder || !(slab > 0.0) ||
-      n_slabs < 0 || !u)
-    return -1;
-  LtsRun R;
-  R.n_inst = n_inst;
-  R.br = br;
-  R.n = n;
-  R.E = orc_num_elements(n_inst, br);
-  R.np = (int64_t)n * n * n;
-  R.gamma2 = gamma2;
-  R.threads = n_threads;
-  R.elem_n.assign(R.E, n);
-  R.nbr.resize(6 * R.E);
-  R.inst.resize(R.E);
-  std::vector<uint64_t> ids(R.E);
-  std::vector<int32_t> ijk(3 * R.E);
-  const int mrc = orc_index_maps(n_inst, br, ids.data(), R.nbr.data(), ijk.data(), R.inst.data());
-  if (mrc != 0 && mrc != -2) return -1;
-  R.invjac.resize(3 * R.E);
-  for (int64_t e = 0; e < R.E; ++e)
-    for (int d = 0; d < 3; ++d) {
-      const OrcBrick& b = br[R.inst[e]];
-      R.invjac[3 * e + d] = 2.0 / ((b.hi[d] - b.lo[d]) / b.n[d]);
-    }
+int lts_evolve(System& sys, int order, const int32_t* levels, double slab, int n_slabs, double* u) {
+  if (order < 1 || order > kMaxOrder || !(slab > 0.0) || n_slabs < 0 || !u) return -1;
+  Run R(sys);
   int L = 0;
-  for (int64_t e = 0; e < R.E; ++e) {
+  for (int64_t e = 0; e < sys.E; ++e) {
     const int l = levels ? levels[e] : 0;
     if (l < 0 || l > 6) return -1;
     L = std::max(L, l);
@@ -488,11 +441,10 @@ int orc_evolve_adams(int n_inst, const OrcBrick* br, int n, double gamma2, int o
     return t < switch_tick ? first_step : (S >> (levels ? levels[e] : 0));
   };
   R.clk = Clock{slab, S, 0.0};
-  R.el.assign(R.E, Elem{});
-  const int64_t total = (int64_t)kVarsA * R.np * R.E;
+  const int64_t total = (int64_t)kVarsA * sys.np * sys.E;
   std::vector<double> u0(u, u + total);
-  std::vector<int64_t> all(R.E);
-  for (int64_t e = 0; e < R.E; ++e) all[e] = e;
+  std::vector<int64_t> all(sys.E);
+  for (int64_t e = 0; e < sys.E; ++e) all[e] = e;
   int rc = 0;
   // self-start (SelfStartActions.hpp:471-482): for each order o < k, reset to
   // the initial values, take o steps of one tick at order o from the slab
@@ -542,6 +494,84 @@ int orc_evolve_adams(int n_inst, const OrcBrick* br, int n, double gamma2, int o
     }
   }
   return 0;
+}
+
+}  // namespace orc_adams
+
+extern "C" {
+
+
+int orc_variable_coefficients(int n, const double* control_times, double step_start,
+                              double step_end, double* out) {
+  if (n < 0 || n > kMaxOrder || (n > 0 && (!control_times || !out))) return -1;
+  const std::vector<double> c =
+      variable_coefficients(std::vector<double>(control_times, control_times + n), step_start,
+                            step_end);
+  std::copy(c.begin(), c.end(), out);
+  return 0;
+}
+
+int orc_adams_coefficients(int n, const int64_t* control_ticks, int64_t step_start,
+                           int64_t step_end, double slab, int64_t ticks_per_slab, double* out) {
+  if (n < 0 || n > kMaxOrder || ticks_per_slab < 1 || (n > 0 && (!control_ticks || !out)))
+    return -1;
+  const Clock clk{slab, ticks_per_slab, 0.0};
+  const std::vector<double> c =
+      coefficients(std::vector<int64_t>(control_ticks, control_ticks + n), step_start, step_end,
+                   clk);
+  std::copy(c.begin(), c.end(), out);
+  return 0;
+}
+
+int orc_lts_coefficients(int n_local, const int64_t* local_slab, const int64_t* local_tick,
+                         int n_remote, const int64_t* remote_slab, const int64_t* remote_tick,
+                         int64_t step_start, int64_t step_end, double slab, int64_t ticks_per_slab,
+                         int local_order, int remote_order, int small_order, int max_out,
+                         int32_t* out_local, int32_t* out_remote, double* out_coef) {
+  for (int o : {local_order, remote_order, small_order})
+    if (o < 1 || o > kMaxOrder) return -1;
+  if (n_local < 0 || n_remote < 0 || ticks_per_slab < 1 || max_out < 0) return -1;
+  std::vector<Id> l(n_local), r(n_remote);
+  for (int i = 0; i < n_local; ++i) l[i] = {local_slab[i], local_tick[i]};
+  for (int i = 0; i < n_remote; ++i) r[i] = {remote_slab[i], remote_tick[i]};
+  std::vector<Term> terms;
+  const int rc = lts_coefficients(l, r, step_start, step_end, local_order, remote_order,
+                                  small_order, Clock{slab, ticks_per_slab, 0.0}, &terms);
+  if (rc) return -2;
+  if ((int)terms.size() > max_out) return -3;
+  for (size_t i = 0; i < terms.size(); ++i) {
+    out_local[i] = terms[i].local;
+    out_remote[i] = terms[i].remote;
+    out_coef[i] = terms[i].coef;
+  }
+  return (int)terms.size();
+}
+
+int orc_evolve_adams(int n_inst, const OrcBrick* br, int n, double gamma2, int order,
+                     const int32_t* levels, double slab, int n_slabs, double* u, int n_threads) {
+  if (n_inst < 1 || !br || n < 2 || n > 20) return -1;
+  orc_adams::FlatSystem sys;
+  sys.n_inst = n_inst;
+  sys.br = br;
+  sys.n = n;
+  sys.E = orc_num_elements(n_inst, br);
+  sys.np = (int64_t)n * n * n;
+  sys.gamma2 = gamma2;
+  sys.threads = n_threads;
+  sys.elem_n.assign(sys.E, n);
+  sys.nbr.resize(6 * sys.E);
+  sys.inst.resize(sys.E);
+  std::vector<uint64_t> ids(sys.E);
+  std::vector<int32_t> ijk(3 * sys.E);
+  const int mrc = orc_index_maps(n_inst, br, ids.data(), sys.nbr.data(), ijk.data(), sys.inst.data());
+  if (mrc != 0 && mrc != -2) return -1;
+  sys.invjac.resize(3 * sys.E);
+  for (int64_t e = 0; e < sys.E; ++e)
+    for (int d = 0; d < 3; ++d) {
+      const OrcBrick& b = br[sys.inst[e]];
+      sys.invjac[3 * e + d] = 2.0 / ((b.hi[d] - b.lo[d]) / b.n[d]);
+    }
+  return orc_adams::lts_evolve(sys, order, levels, slab, n_slabs, u);
 }
 
 }  // extern "C"

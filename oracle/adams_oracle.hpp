@@ -1,0 +1,44 @@
+// adams_oracle.hpp -- the system interface of the Adams-Bashforth / local
+// time-stepping oracle (test infrastructure only).  The time stepping
+// (adams_oracle.cpp) is written once against this interface; the flat brick
+// (adams_oracle.cpp) and the curved shell (dgsw_oracle.cpp) implement it.
+#pragma once
+
+#include <cstdint>
+#include <vector>
+
+namespace orc_adams {
+
+struct System {
+  int64_t E = 0;   // elements
+  int n = 0;       // GLL points per dimension
+  int64_t np = 0;  // points per element
+  virtual ~System() = default;
+  // neighbour across face dir of element e; < 0 for an external face
+  virtual int64_t neighbor(int64_t e, int dir) const = 0;
+  // the neighbour's face that touches e
+  virtual int back_dir(int64_t e, int dir) const = 0;
+  // every element's volume time derivative with the external boundary
+  // conditions of time-derivative type, no internal mortar terms
+  // (ComputeTimeDerivative in local time stepping)
+  virtual void volume_rhs(const double* u, double* dudt) = 0;
+  // dg_package_data of e's face dir, face points in e's order, and the
+  // normal magnitudes there
+  virtual void package(const double* u, int64_t e, int dir, std::vector<double>* pkg,
+                       std::vector<double>* magnitude) const = 0;
+  // the neighbour's own packaged data of the face it shares with e's face
+  // dir, in e's face-point order (the mortar data it sends)
+  virtual void exterior_package(const double* u, int64_t e, int dir,
+                                std::vector<double>* pkg) const = 0;
+  // dg_boundary_terms of interior and exterior packages: 5 * n^2 values,
+  // component-major
+  virtual void boundary_terms(const std::vector<double>& pkg_int,
+                              const std::vector<double>& pkg_ext, double* out) const = 0;
+};
+
+// Self-start and n_slabs slabs of AdamsBashforth(order) with local time
+// stepping; element e steps slab / 2^levels[e] after the start-up (levels
+// may be NULL).  Returns 0, or < 0 on bad input or missing history data.
+int lts_evolve(System& sys, int order, const int32_t* levels, double slab, int n_slabs, double* u);
+
+}  // namespace orc_adams

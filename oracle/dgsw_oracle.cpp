@@ -4,6 +4,7 @@
 // Each function names the reference file:line it restates (paths relative to
 // the SpECTRE source tree).  Compiled with -ffp-contract=off so that every
 // product and sum is rounded separately, as in the reference's scalar code.
+#include "adams_oracle.hpp"
 #include "dgsw_oracle.h"
 
 #include <algorithm>
@@ -2061,7 +2062,7 @@ void curved_normal(const double* ij9, double sign, const double* gi6, double nco
   }
 }
 
-int shell_rhs_impl(const ShellMesh& m, const double* u, double* dudt) {
+int shell_rhs_impl(const ShellMesh& m, const double* u, double* dudt, bool mortars = true) {
   const OrcShell& s = m.s;
   const int n = s.n;
   const int64_t np = (int64_t)n * n * n;
@@ -2112,6 +2113,7 @@ int shell_rhs_impl(const ShellMesh& m, const double* u, double* dudt) {
       for (int dir = 0; dir < 6; ++dir) {
         const int64_t nb = m.nbr[6 * e + dir];
         if ((pass == 0) != (nb < 0)) continue;
+        if (nb >= 0 && !mortars) continue;
         const int d = dir / 2;
         const bool upper = dir % 2;
         const int slice = upper ? n - 1 : 0;
@@ -2193,6 +2195,77 @@ int shell_rhs_impl(const ShellMesh& m, const double* u, double* dudt) {
   return excision_violation;
 }
 
+// The curved shell as a system of the Adams-Bashforth / LTS oracle: volume
+// terms with the radiation condition on the outer sphere (a time-derivative
+// condition, part of dt u), packaged data with each side's own normal and
+// background, and the curved UpwindPenalty boundary terms.
+struct ShellSystem : orc_adams::System {
+  ShellMesh m;
+  int64_t neighbor(int64_t e, int dir) const override { return m.nbr[6 * e + dir]; }
+  int back_dir(int64_t e, int dir) const override {
+    return shell_back_dir(m, e, m.nbr[6 * e + dir]);
+  }
+  void volume_rhs(const double* u, double* dudt) override { shell_rhs_impl(m, u, dudt, false); }
+  // package of face point vp of element e on its face dir (14 values)
+  void point_package(const double* u, int64_t e, int dir, int64_t vp, double* pk,
+                     double* mag) const {
+    const OrcShell& s = m.s;
+    const int d = dir / 2;
+    const double* ue = u + e * 5 * np;
+    const double* IJ = &m.ij[e * 9 * np];
+    double X[3], bg[26];
+    for (int i = 0; i < 3; ++i) X[i] = m.xyz[e * 3 * np + i * np + vp];
+    orc_ks_background(1, s.mass, X, bg);
+    double ij9[3], gi6[6], nco[3], nvec[3];
+    for (int i = 0; i < 3; ++i) ij9[i] = IJ[(3 * d + i) * np + vp];
+    for (int t = 0; t < 6; ++t) gi6[t] = bg[16 + t];
+    curved_normal(ij9, (dir % 2) ? 1.0 : -1.0, gi6, nco, nvec, mag);
+    const double psi = ue[vp], pi = ue[np + vp];
+    double phi[3], shift[3];
+    for (int i = 0; i < 3; ++i) {
+      phi[i] = ue[(2 + i) * np + vp];
+      shift[i] = bg[1 + i];
+    }
+    const double g1 = s.gamma1, g2 = s.gamma2;
+    double ms;
+    orc_csw_package(1, &psi, &pi, phi, &bg[0], shift, &g1, &g2, nco, nvec, nullptr, pk, &ms);
+  }
+  void package(const double* u, int64_t e, int dir, std::vector<double>* pkg,
+               std::vector<double>* mag) const override {
+    const int nf = n * n, d = dir / 2, slice = (dir % 2) ? n - 1 : 0;
+    pkg->assign((size_t)14 * nf, 0.0);
+    mag->assign(nf, 0.0);
+    for (int bb = 0; bb < n; ++bb)
+      for (int aa = 0; aa < n; ++aa) {
+        const int q = aa + n * bb;
+        point_package(u, e, dir, volume_index(n, d, slice, aa, bb), &(*pkg)[14 * q], &(*mag)[q]);
+      }
+  }
+  void exterior_package(const double* u, int64_t e, int dir,
+                        std::vector<double>* pkg) const override {
+    const int nf = n * n;
+    const int64_t nb = m.nbr[6 * e + dir];
+    const int nd = shell_back_dir(m, e, nb);
+    const int nslice = (nd % 2) ? n - 1 : 0;
+    pkg->assign((size_t)14 * nf, 0.0);
+    for (int q = 0; q < nf; ++q) {
+      const int nq = m.perm[(6 * e + dir) * (size_t)nf + q];
+      double mag;
+      point_package(u, nb, nd, volume_index(n, nd / 2, nslice, nq % n, nq / n), &(*pkg)[14 * q],
+                    &mag);
+    }
+  }
+  void boundary_terms(const std::vector<double>& pi, const std::vector<double>& pe,
+                      double* out) const override {
+    const int nf = n * n;
+    for (int q = 0; q < nf; ++q) {
+      double bc[5];
+      orc_csw_boundary_terms(1, &pi[14 * q], &pe[14 * q], bc);
+      for (int v = 0; v < 5; ++v) out[(size_t)v * nf + q] = bc[v];
+    }
+  }
+};
+
 }  // namespace
 
 extern "C" {
@@ -2263,6 +2336,21 @@ int orc_shell_rhs(const OrcShell* s, const double* u, double* dudt, int n_thread
   ShellMesh m;
   build_shell(*s, &m);
   return shell_rhs_impl(m, u, dudt);
+}
+
+int orc_shell_evolve_adams(const OrcShell* s, int order, const int32_t* levels, double slab,
+                           int n_slabs, double* u, int n_threads) {
+  if (check_shell(s) || !u) return -1;
+#ifdef _OPENMP
+  if (n_threads > 0) omp_set_num_threads(n_threads);
+#endif
+  (void)n_threads;
+  ShellSystem sys;
+  build_shell(*s, &sys.m);
+  sys.E = sys.m.E;
+  sys.n = s->n;
+  sys.np = (int64_t)s->n * s->n * s->n;
+  return orc_adams::lts_evolve(sys, order, levels, slab, n_slabs, u);
 }
 
 int orc_shell_observe_norms(const OrcShell* s, const double* u, double* out) {

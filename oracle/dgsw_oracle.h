@@ -256,6 +256,12 @@ int orc_shell_initial_data(const OrcShell* s, double r0, double w, double* u);
  * sphere (returns 1 if a char speed is incoming) and CPSR at the outer one */
 int orc_shell_rhs(const OrcShell* s, const double* u, double* dudt, int n_threads);
 int orc_shell_evolve(const OrcShell* s, double dt, int n_steps, double* u, int n_threads);
+/* AdamsBashforth(order) with local time stepping on the shell (self-start,
+ * then n_slabs slabs; element e steps slab / 2^levels[e], levels may be
+ * NULL), the outer radiation condition in dt u, UpwindPenalty across wedges
+ * through the boundary histories (adams_oracle.cpp) */
+int orc_shell_evolve_adams(const OrcShell* s, int order, const int32_t* levels, double slab,
+                           int n_slabs, double* u, int n_threads);
 /* ObserveNorms (as orc_observe_norms) of a shell state */
 int orc_shell_observe_norms(const OrcShell* s, const double* u, double* out);
 

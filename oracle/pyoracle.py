@@ -42,7 +42,7 @@ _lib = None
 def lib():
     global _lib
     if _lib is None:
-        srcs = ("dgsw_oracle.cpp", "adams_oracle.cpp", "dgsw_oracle.h")
+        srcs = ("dgsw_oracle.cpp", "adams_oracle.cpp", "dgsw_oracle.h", "adams_oracle.hpp")
         if not os.path.exists(LIB) or os.path.getmtime(LIB) < max(
                 os.path.getmtime(os.path.join(HERE, f)) for f in srcs):
             build()
@@ -78,6 +78,7 @@ def lib():
             "orc_adams_coefficients": [I, P, I64, I64, D, I64, P],
             "orc_lts_coefficients": [I, P, P, I, P, P, I64, I64, D, I64, I, I, I, I, P, P, P],
             "orc_evolve_adams": [I, P, I, D, I, P, D, I, P, I],
+            "orc_shell_evolve_adams": [P, I, P, D, I, P, I],
         }
         for name, args in sig.items():
             fn = getattr(L, name)
@@ -549,4 +550,13 @@ def evolve_adams(bricks, n, u, slab, n_slabs, order, levels=None, gamma2=0.0, th
     lv = None if levels is None else np.ascontiguousarray(levels, dtype=np.int32)
     _check(lib().orc_evolve_adams(len(bricks), ctypes.addressof(arr), n, gamma2, order, _p(lv),
                                   slab, n_slabs, _p(u), threads))
+    return u
+
+
+def shell_evolve_adams(s, u, slab, n_slabs, order, levels=None, threads=0):
+    """AdamsBashforth(order) with local time stepping on the shell."""
+    u = np.array(u, dtype=np.float64, copy=True)
+    lv = None if levels is None else np.ascontiguousarray(levels, dtype=np.int32)
+    _check(lib().orc_shell_evolve_adams(ctypes.addressof(s), order, _p(lv), slab, n_slabs, _p(u),
+                                        threads))
     return u

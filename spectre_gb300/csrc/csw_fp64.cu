@@ -289,7 +289,7 @@ __global__ void __launch_bounds__(kThreads, CswShape<N>::SMEM * 8 <= 113 * 1024 
   double* Ga = U + 5 * NP;   // 5 * NP: d_a of the five fields, one axis at a time
   double* Go = Ga + 5 * NP;  // 12 * NN: outer layer d_a Psi, d_a Phi_j ([a][4][NN])
   double* tab = Go + 12 * NN;
-  const int64_t e = blockIdx.x;
+  const int64_t e = L.list ? (int64_t)L.list[blockIdx.x] : (int64_t)blockIdx.x;
   const int tid = threadIdx.x;
   const int64_t off = e * (int64_t)(kVars * NP);
   const bool outer = kBoundary && L.nbr[6 * e + 5] == -2;
@@ -394,6 +394,7 @@ __global__ void __launch_bounds__(kThreads, CswShape<N>::SMEM * 8 <= 113 * 1024 
         const int32_t x = L.X[ef * NN + q];
         const double* f = L.F + ef * kCswF * NN + q;
         if (x >= 0) {
+          if (!L.internal) continue;
           double ue[5];
 #pragma unroll
           for (int v = 0; v < 5; ++v) ue[v] = L.ucur[x + (int64_t)v * NP];
@@ -464,7 +465,80 @@ __global__ void __launch_bounds__(kThreads, CswShape<N>::SMEM * 8 <= 113 * 1024 
       double o = fma(L.b, uc, L.c * dt[v]);
       if (L.a != 0.0) o = fma(L.a, L.u0[off + v * NP + p], o);
       L.unext[off + v * NP + p] = o;
+      if (L.ucopy) L.ucopy[off + v * NP + p] = uc;
     }
+  }
+}
+
+// AdamsBashforth on the shell, one element per block: u (or the initial
+// values on a self-start reset) plus sum_j c_j F_j, plus on every internal
+// face point the curved UpwindPenalty of the marginal-weighted records.
+// The correction is linear in the exterior-minus-interior jump with static
+// weights (csw_face_kernel), so sum_{l,r} c_lr C(L_l, R_r) =
+// C(sum_l a_l L_l, sum_r b_r R_r).  The exterior record point is the
+// neighbour's offset X of the face point in the same ring slot layout.
+template <int N>
+__global__ void __launch_bounds__(kThreads) csw_ab_update_kernel(const __grid_constant__ CswAbArgs A) {
+  constexpr int NN = N * N, NP = NN * N;
+  int64_t g = blockIdx.x;
+  int j = -1;
+  for (int q = 0; q < A.L.n_jobs; ++q) {
+    if (g < A.L.job[q].count) {
+      j = q;
+      break;
+    }
+    g -= A.L.job[q].count;
+  }
+  if (j < 0) return;  // no barrier in this kernel
+  const AbLevelJob& J = A.L.job[j];
+  const int64_t e = A.list[J.begin + g];
+  const int64_t per = (int64_t)kVars * NP, E = A.n_elem;
+  const int64_t off = e * per;
+  const bool update = J.update && !J.reset;
+  if (!update && !J.reset) return;
+  const double* src = J.reset ? A.u0 : A.u;
+  for (int p = threadIdx.x; p < NP; p += kThreads) {
+    double val[5];
+#pragma unroll
+    for (int v = 0; v < 5; ++v) val[v] = src[off + v * NP + p];
+    if (update) {
+      for (int i = 0; i < J.n_vol; ++i) {
+        const double* Fi = A.F + ((int64_t)J.vol_slot[i] * E + e) * per + p;
+#pragma unroll
+        for (int v = 0; v < 5; ++v) val[v] = fma(J.vol_c[i], Fi[v * NP], val[v]);
+      }
+      const int i0 = p % N, j0 = (p / N) % N, k0 = p / NN;
+      const int dirs[6] = {i0 == 0 ? 0 : -1, i0 == N - 1 ? 1 : -1, j0 == 0 ? 2 : -1,
+                           j0 == N - 1 ? 3 : -1, k0 == 0 ? 4 : -1, k0 == N - 1 ? 5 : -1};
+      const int fq[3] = {j0 + N * k0, i0 + N * k0, i0 + N * j0};
+      double corr[5] = {0.0, 0.0, 0.0, 0.0, 0.0};
+#pragma unroll
+      for (int s6 = 0; s6 < 6; ++s6) {
+        const int dir = dirs[s6];
+        if (dir < 0) continue;
+        const int q = fq[dir >> 1];
+        const int64_t ef = e * 6 + dir;
+        const int32_t x = A.X[ef * NN + q];
+        if (x < 0) continue;  // external: its condition is in the time derivative
+        const AbFaceTable& f = J.face[A.level[x / per]];
+        double ui[5] = {0.0, 0.0, 0.0, 0.0, 0.0}, ue[5] = {0.0, 0.0, 0.0, 0.0, 0.0};
+        for (int i = 0; i < f.n_loc; ++i) {
+          const double* Ul = A.U + ((int64_t)f.loc_slot[i] * E + e) * per + p;
+#pragma unroll
+          for (int v = 0; v < 5; ++v) ui[v] = fma(f.loc_c[i], Ul[v * NP], ui[v]);
+        }
+        for (int i = 0; i < f.n_rem; ++i) {
+          const double* Ur = A.U + (int64_t)f.rem_slot[i] * E * per + x;
+#pragma unroll
+          for (int v = 0; v < 5; ++v) ue[v] = fma(f.rem_c[i], Ur[v * NP], ue[v]);
+        }
+        upwind_face<double>(ui, ue, A.Fc + ef * kCswF * NN + q, NN, A.gamma2, corr);
+      }
+#pragma unroll
+      for (int v = 0; v < 5; ++v) val[v] += corr[v];
+    }
+#pragma unroll
+    for (int v = 0; v < 5; ++v) A.u[off + v * NP + p] = val[v];
   }
 }
 
@@ -478,8 +552,9 @@ cudaError_t launch_fp64_n(const CswLaunch& L, cudaStream_t s) {
   err = cudaFuncSetAttribute(k, cudaFuncAttributePreferredSharedMemoryCarveout,
                              cudaSharedmemCarveoutMaxShared);
   if (err != cudaSuccess) return err;
-  if (L.n_elem <= 0) return cudaSuccess;
-  k<<<(unsigned)L.n_elem, kThreads, smem, s>>>(L);
+  const int64_t blocks = L.list ? L.list_count : L.n_elem;
+  if (blocks <= 0) return cudaSuccess;
+  k<<<(unsigned)blocks, kThreads, smem, s>>>(L);
   return cudaGetLastError();
 }
 
@@ -507,6 +582,21 @@ cudaError_t launch_csw_fp64(const CswLaunch& L, cudaStream_t s) {
     case 12: return launch_fp64_mode<12>(L, s);
     default: return cudaErrorInvalidValue;
   }
+}
+
+cudaError_t launch_csw_ab_update(const CswAbArgs& A, cudaStream_t s) {
+  int64_t total = 0;
+  for (int q = 0; q < A.L.n_jobs; ++q) total += A.L.job[q].count;
+  if (total <= 0) return cudaSuccess;
+  switch (A.n) {
+#define DGSW_CSW_AB(NV) \
+  case NV: csw_ab_update_kernel<NV><<<(unsigned)total, kThreads, 0, s>>>(A); break;
+    DGSW_CSW_AB(2) DGSW_CSW_AB(3) DGSW_CSW_AB(4) DGSW_CSW_AB(5) DGSW_CSW_AB(6) DGSW_CSW_AB(7)
+    DGSW_CSW_AB(8) DGSW_CSW_AB(9) DGSW_CSW_AB(10) DGSW_CSW_AB(11) DGSW_CSW_AB(12)
+#undef DGSW_CSW_AB
+    default: return cudaErrorInvalidValue;
+  }
+  return cudaGetLastError();
 }
 
 cudaError_t launch_csw_setup(const CswSetup& S, cudaStream_t s) {

@@ -762,9 +762,9 @@ cudaError_t capture_steps(DgswHandle h, double dt, int steps, cudaGraphExec_t* o
 // AdamsBashforth handle set-up: step levels, the level-sorted element list,
 // the schedule (whose dry run sizes the history rings) and the rings.
 int adams_init(DgswHandle h, const DgswConfig& cfg) {
-  if (h->curved || h->refined || h->gauss || !h->dom.uniform || mixed(h))
+  if (h->refined || h->gauss || !h->dom.uniform || mixed(h))
     return fail(h, DGSW_ERR_UNSUPPORTED,
-                "AdamsBashforth: flat system, Gauss-Lobatto, one extent, conforming bricks, FP64");
+                "AdamsBashforth: Gauss-Lobatto, one extent, conforming elements, FP64");
   const int64_t E = h->dom.n_elem;
   std::vector<int8_t> level(E, 0);
   for (int64_t e = 0; e < E; ++e) {
@@ -775,7 +775,10 @@ int adams_init(DgswHandle h, const DgswConfig& cfg) {
   bool adj[kAbMaxLevels][kAbMaxLevels] = {};
   for (int64_t e = 0; e < E; ++e) {
     ++h->ab_count[level[e]];
-    for (int f = 0; f < 6; ++f) adj[level[e]][level[h->dom.neighbor[6 * e + f]]] = true;
+    for (int f = 0; f < 6; ++f) {
+      const int32_t nb = h->dom.neighbor[6 * e + f];
+      if (nb >= 0) adj[level[e]][level[nb]] = true;  // < 0: the shell's boundary spheres
+    }
   }
   std::vector<int32_t> list;
   list.reserve(E);
@@ -792,7 +795,10 @@ int adams_init(DgswHandle h, const DgswConfig& cfg) {
   const size_t slots = (size_t)h->ab.ring_slots();
   if ((e = cudaMalloc(&h->ab_F, slots * E * kVars * n * n * n * sizeof(double))) != cudaSuccess)
     return cuda_fail(h, e, "cudaMalloc time-derivative ring");
-  if ((e = cudaMalloc(&h->ab_B, slots * E * 12 * n * n * sizeof(double))) != cudaSuccess)
+  // the shell records the whole state (its exterior points are reached
+  // through the face offsets of the volume layout); bricks record the face w's
+  const size_t rec = h->curved ? (size_t)kVars * n * n * n : (size_t)12 * n * n;
+  if ((e = cudaMalloc(&h->ab_B, slots * E * rec * sizeof(double))) != cudaSuccess)
     return cuda_fail(h, e, "cudaMalloc face-data ring");
   h->adams = true;
   return DGSW_OK;
@@ -821,6 +827,9 @@ int adams_step(DgswHandle h, int n_steps, double dt) {
   A.gamma2 = h->cfg.gamma2;
   A.eo = h->eo;
   const int n = h->dom.elem_n[0];
+  const int64_t per = (int64_t)kVars * n * n * n;
+  if (h->filter_on)
+    return fail(h, DGSW_ERR_UNSUPPORTED, "the exponential filter is not applied with AdamsBashforth");
   std::vector<AbLaunch> launches;
   std::string err;
   for (int s = 0; s < n_steps; ++s) {
@@ -828,8 +837,41 @@ int adams_step(DgswHandle h, int n_steps, double dt) {
       DGSW_CUDA(h, cudaMemcpyAsync(h->t1, h->state, bytes, cudaMemcpyDeviceToDevice, h->stream));
     if (!h->ab.slab(&launches, &err)) return fail(h, DGSW_ERR_ARGUMENT, err);
     for (const AbLaunch& L : launches) {
-      A.L = L;
-      DGSW_CUDA(h, launch_adams_step(A, n, h->stream));
+      if (!h->curved) {
+        A.L = L;
+        DGSW_CUDA(h, launch_adams_step(A, n, h->stream));
+        continue;
+      }
+      // shell: update (volume part and boundary delta), then the records
+      // (time derivative with the radiation condition, and the state)
+      CswAbArgs C;
+      C.u = h->state;
+      C.u0 = h->t1;
+      C.F = h->ab_F;
+      C.U = h->ab_B;
+      C.Fc = h->c_F;
+      C.X = h->c_X;
+      C.list = h->ab_list;
+      C.level = h->ab_level;
+      C.n = n;
+      C.n_elem = h->dom.n_elem;
+      C.gamma2 = h->cfg.gamma2;
+      C.L = L;
+      DGSW_CUDA(h, launch_csw_ab_update(C, h->stream));
+      for (int j = 0; j < L.n_jobs; ++j) {
+        const AbLevelJob& J = L.job[j];
+        CswLaunch R = base_csw(h);
+        R.ucur = h->state;
+        R.unext = h->ab_F + (int64_t)J.rec_slot * h->dom.n_elem * per;
+        R.ucopy = h->ab_B + (int64_t)J.rec_slot * h->dom.n_elem * per;
+        R.a = 0.0;
+        R.b = 0.0;
+        R.c = 1.0;
+        R.internal = 0;
+        R.list = h->ab_list + J.begin;
+        R.list_count = J.count;
+        DGSW_CUDA(h, launch_csw_fp64(R, h->stream));
+      }
     }
   }
   return DGSW_OK;
@@ -1297,10 +1339,9 @@ int dgsw_create(const DgswConfig* cfg, DgswHandle* out) {
     // way with or without a GPU
     int code = DGSW_OK;
     const char* why = nullptr;
-    if (h->curved || h->refined || h->gauss || !h->dom.uniform ||
-        cfg->precision != DGSW_PRECISION_FP64) {
+    if (h->refined || h->gauss || !h->dom.uniform || cfg->precision != DGSW_PRECISION_FP64) {
       code = DGSW_ERR_UNSUPPORTED;
-      why = "AdamsBashforth: flat system, Gauss-Lobatto, one extent, conforming bricks, FP64";
+      why = "AdamsBashforth: Gauss-Lobatto, one extent, conforming elements, FP64";
     } else if (cfg->stepper_order < 0 || cfg->stepper_order > kAbMaxOrder) {
       code = DGSW_ERR_ARGUMENT;
       why = "AdamsBashforth order must be in [1, 8] (0: 3)";

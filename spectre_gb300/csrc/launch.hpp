@@ -202,8 +202,33 @@ struct CswLaunch {
   const int32_t* nbr = nullptr;
   double gamma1 = 0.0, gamma2 = 0.0;
   EoTable eo{};
+  // AdamsBashforth records: only the listed elements (list non-null), no
+  // internal mortar terms (internal = 0), and a copy of ucur written to ucopy
+  const int32_t* list = nullptr;
+  int64_t list_count = 0;
+  int internal = 1;
+  double* ucopy = nullptr;
 };
 cudaError_t launch_csw_fp64(const CswLaunch& L, cudaStream_t s);
+
+// One tick position of AdamsBashforth with local time stepping on the shell:
+// the volume update and the boundary delta of the listed levels' elements
+// (csw_fp64.cu); the records follow with launch_csw_fp64 in record mode.
+struct CswAbArgs {
+  double* u = nullptr;
+  const double* u0 = nullptr;
+  const double* F = nullptr;  // ring slots x elements x 5 N^3 time derivatives
+  const double* U = nullptr;  // ring slots x elements x 5 N^3 recorded states
+  const double* Fc = nullptr; // face table (kCswF per face point)
+  const int32_t* X = nullptr; // exterior point offsets
+  const int32_t* list = nullptr;
+  const int8_t* level = nullptr;
+  int n = 0;
+  int64_t n_elem = 0;
+  double gamma2 = 0.0;
+  AbLaunch L{};
+};
+cudaError_t launch_csw_ab_update(const CswAbArgs& A, cudaStream_t s);
 
 // Mixed-precision stage on the shell: W = alpha X + beta Y + c L(X) in FP32
 // arithmetic, with X either FP64 (compensated double-float derivatives) or

@@ -141,7 +141,8 @@ bool build_shell_domain(const DgswConfig& cfg, Domain* dom, ShellGeometry* geo,
     return false;
   }
   if (cfg.boundary_correction != DGSW_CORRECTION_UPWIND_PENALTY ||
-      cfg.time_stepper != DGSW_STEPPER_RK3_HESTHAVEN_SSP) {
+      (cfg.time_stepper != DGSW_STEPPER_RK3_HESTHAVEN_SSP &&
+       cfg.time_stepper != DGSW_STEPPER_ADAMS_BASHFORTH)) {
     *err = "unsupported boundary correction or time stepper";
     return false;
   }

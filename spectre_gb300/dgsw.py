@@ -752,8 +752,12 @@ class CurvedDgEvolution(DgEvolution):
     gamma2 is CurvedScalarWave's constraint damping gamma2."""
 
     def __init__(self, shell: Shell, points: int, precision=PRECISION_FP64, gamma2=1.0,
-                 device=0):
-        super().__init__(shell, points, precision, gamma2, device)
+                 device=0, time_stepper="rk3_hesthaven_ssp", order=3, step_levels=None):
+        """time_stepper "adams_bashforth": the stepper family the reference's
+        curved executable runs (AdamsBashforth with local time stepping);
+        FP64 only."""
+        super().__init__(shell, points, precision, gamma2, device, time_stepper=time_stepper,
+                         order=order, step_levels=step_levels)
         self.shell = shell
 
     def set_gaussian_shell(self, amplitude=1.0, radius=8.0, width=1.0):

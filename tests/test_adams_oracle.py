@@ -98,3 +98,19 @@ def test_uniform_levels_are_global_stepping(oracle):
     a = oracle.evolve_adams(bricks, n, u0, 0.05, 3, 3)
     b = oracle.evolve_adams(bricks, n, u0, 0.05, 3, 3, levels=[0] * 8)
     np.testing.assert_array_equal(a, b)
+
+
+@pytest.mark.parametrize("order,lts", [(2, False), (3, False), (3, True)])
+def test_curved_shell_order(oracle, order, lts):
+    # the shell (curved UpwindPenalty across wedges, radiation condition in
+    # dt u): AB(k), with or without 2:1 local stepping, converges at order k
+    # against a time-resolved SSP-RK3 run of the same semi-discrete system
+    s = oracle.shell(1.9, 20.0, 0, 1, 5, 1.0, 0.0, 1.0)
+    E = oracle.shell_num_elements(s)
+    u0 = oracle.shell_initial_data(s, 8.0, 1.5)
+    T = 0.4
+    ref, ok = oracle.shell_evolve(s, u0, T / 400, 400)
+    levels = np.array([i % 2 for i in range(E)], np.int32) if lts else None
+    errs = [np.abs(oracle.shell_evolve_adams(s, u0, T / k, k, order, levels=levels).ravel()
+                   - ref.ravel()).max() for k in (8, 16)]
+    assert math.log2(errs[0] / errs[1]) > order - 0.5

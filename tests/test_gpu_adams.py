@@ -160,3 +160,24 @@ def test_local_stepping_accuracy_large(oracle):
         rk.step(400, 0.0005)
         u_rk = rk.get_state()
     assert float(np.abs(u_lts - u_rk).max()) < 1e-6
+
+
+@pytest.mark.parametrize("order,L", [(1, 0), (3, 0), (4, 0), (2, 1), (3, 2)])
+def test_curved_shell_matches_oracle(oracle, order, L):
+    # the reference's curved executable steps with AdamsBashforth (LTS):
+    # Kerr-Schild shell, curved UpwindPenalty across wedges, radiation
+    # condition on the outer sphere, gamma2 = 1
+    from spectre_gb300.dgsw import CurvedDgEvolution, Shell
+    n = 6
+    s = oracle.shell(1.9, 20.0, 1, 1, n, 1.0, 0.0, 1.0)
+    E = oracle.shell_num_elements(s)
+    u0 = oracle.shell_initial_data(s, 8.0, 1.5)
+    levels = pattern(E, L, seed=order) if L else None
+    slab, slabs = 0.02, 3
+    with CurvedDgEvolution(Shell(1.9, 20.0, 1, 1), n, gamma2=1.0, time_stepper="adams_bashforth",
+                           order=order, step_levels=levels) as ev:
+        ev.set_state(u0.ravel())
+        ev.step(slabs, slab)
+        got = ev.get_state()
+    want = oracle.shell_evolve_adams(s, u0, slab, slabs, order, levels=levels).ravel()
+    assert per_var_rel(got, want, E, n) <= tol(order, slabs, L)

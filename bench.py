@@ -347,6 +347,48 @@ def time_adjoint(dev):
         p.close()
 
 
+def time_curved_adams(shell, n, dt, steps, dev):
+    """The shell stepped as the reference's curved executable steps it:
+    AdamsBashforth(3), global stepping at dt, and local time stepping with
+    the slab 4 dt and the radial layers on levels by element size (the
+    logarithmic radial map makes the inner layers smallest: layers 0-1 step
+    dt, 2-4 2 dt, 5-7 4 dt).  Both cover the same simulated time."""
+    import torch
+    from spectre_gb300.dgsw import CurvedDgEvolution
+    E = 768
+    layer = np.arange(E) % 8  # radial segment: the innermost index of a wedge's elements
+    levels = np.where(layer < 2, 2, np.where(layer < 5, 1, 0)).astype(np.int32)
+    res, states = {}, {}
+    for name, lv, slab, slabs in (("gts", None, dt, steps), ("lts", levels, 4 * dt, steps // 4)):
+        ev = CurvedDgEvolution(shell, n, gamma2=1.0, device=dev, time_stepper="adams_bashforth",
+                               order=3, step_levels=lv)
+        ev.set_gaussian_shell(1.0, 8.0, 1.0)
+        u0 = ev.get_state()
+        ev.step(2, slab)  # start-up and switch
+        ev.set_state(u0)  # time the whole run from t = 0, start-up included
+        stream = torch.cuda.ExternalStream(ev.stream_ptr(), device=dev)
+        e0 = torch.cuda.Event(enable_timing=True)
+        e1 = torch.cuda.Event(enable_timing=True)
+        torch.cuda.synchronize()
+        e0.record(stream)
+        ev.step(slabs, slab, sync=False)
+        e1.record(stream)
+        e1.synchronize()
+        ms = e0.elapsed_time(e1)
+        info = ev.adams_info()
+        states[name] = ev.get_state()
+        res[name] = {"value": info["rhs_points_per_slab"] * slabs / (ms * 1e-3), "unit": UNIT,
+                     "ms_per_unit_time": ms / (slabs * slab), "slab": slab, "slabs": slabs,
+                     "launches_per_slab": 2 * info["launches_per_slab"]}
+        ev.close()
+    res["lts_speedup_vs_gts"] = res["gts"]["ms_per_unit_time"] / res["lts"]["ms_per_unit_time"]
+    a, b = states["gts"], states["lts"]
+    res["max_abs_lts_vs_gts"] = float(np.abs(a - b).max())
+    res["note"] = ("AdamsBashforth(3); value counts each element's own steps; the start-up "
+                   "(self-start at dt/3 resp. the finest step / 3) is inside the timed run")
+    return res
+
+
 def time_curved(args, dev, with_cpu):
     """Config 5: CurvedScalarWave on Schwarzschild in Kerr-Schild coordinates
     (M = 1, gamma1 = 0, gamma2 = 1), six-wedge shell r in [1.9, 20], 4 x 4
@@ -405,6 +447,7 @@ def time_curved(args, dev, with_cpu):
            "mixed_speedup_vs_fp64": res["fp64"]["ms_per_step"] / res["mixed"]["ms_per_step"],
            "rel_l2_mixed_vs_fp64_after_steps": float(np.linalg.norm(m - a) / np.linalg.norm(a)),
            "max_abs_mixed_vs_fp64": float(np.abs(m - a).max())}
+    out["adams"] = time_curved_adams(shell, n, dt, steps, dev)
     if with_cpu:
         s_orc = pyoracle.shell(1.9, 20.0, 2, 3, n, 1.0, 0.0, 1.0)
         u = pyoracle.shell_initial_data(s_orc, 8.0, 1.0)

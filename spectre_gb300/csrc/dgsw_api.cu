@@ -892,11 +892,30 @@ bool pipelinable(DgswHandle h) {
 int pipe_init(DgswHandle h) {
   if (h->pipe_in) return DGSW_OK;
   const int64_t E = h->dom.n_elem;
-  // 16 chunks: at 32^3 x 8^3 this measured 7.50 ms per step against 7.84 ms
-  // with 32 (smaller launches leave more of each wave idle)
-  const int C = (int)std::min<int64_t>(16, E / 1024);
-  h->chunk_begin.resize(C + 1);
-  for (int c = 0; c <= C; ++c) h->chunk_begin[c] = E * c / C;
+  // Chunks of E/16 elements, except thin ones (E/32) at both ends of the
+  // element order: on a periodic brick the chunks are x-slabs on a ring, and
+  // the last chunk copied in holds back the three-stage chains of the chunks
+  // within three of it (the first and the last few), whose stages and
+  // copies-out then form the tail of the step.  Thin chunks there shorten
+  // the tail; thick ones elsewhere keep the launches efficient.
+  // Chunk sizes are whole waves of the stage kernel where the state allows,
+  // so that no chunk launch ends on a partly filled wave.
+  int64_t thin = std::max<int64_t>(256, E / 32), thick = std::max<int64_t>(512, E / 16);
+  const int64_t wave = stage_fp64_wave_elements(h->dom.elem_n[0], h->stage_variant);
+  if (wave > 0 && E >= 24 * wave) {
+    thin = wave;
+    thick = 2 * wave;
+  }
+  h->chunk_begin.assign(1, 0);
+  for (int k = 0; k < 3 && h->chunk_begin.back() + thin < E; ++k)
+    h->chunk_begin.push_back(h->chunk_begin.back() + thin);
+  const int64_t tail_start = std::max(h->chunk_begin.back(), E - 4 * thin);
+  while (h->chunk_begin.back() + thick <= tail_start)
+    h->chunk_begin.push_back(h->chunk_begin.back() + thick);
+  if (h->chunk_begin.back() < tail_start) h->chunk_begin.push_back(tail_start);
+  while (h->chunk_begin.back() + thin < E) h->chunk_begin.push_back(h->chunk_begin.back() + thin);
+  h->chunk_begin.push_back(E);
+  const int C = (int)h->chunk_begin.size() - 1;
   std::vector<int> chunk_of(E);
   for (int c = 0; c < C; ++c)
     for (int64_t e = h->chunk_begin[c]; e < h->chunk_begin[c + 1]; ++e) chunk_of[e] = c;

@@ -60,6 +60,9 @@ struct StageLaunch {
 };
 
 cudaError_t launch_stage_fp64(const StageLaunch& L, cudaStream_t s);
+// Elements that one full wave of the FP64 stage kernel (extent n, launch
+// variant) holds on the current device; 0 if unknown.
+int64_t stage_fp64_wave_elements(int n, int variant);
 
 // One tick position of AdamsBashforth with local time stepping
 // (adams_step.cu): the coefficient tables of the levels stepping there, by

@@ -263,7 +263,45 @@ cudaError_t launch_mode(const StageLaunch& L, cudaStream_t s) {
   }
 }
 
+// elements one full wave of the FP64 stage kernel (mode kModeStage) holds on
+// the current device
+template <int N, int V>
+int64_t wave_n() {
+  constexpr int EPB = elems_per_block<N, V>();
+  constexpr auto k = stage_fp64_kernel<N, EPB, min_blocks<N, V>(), kModeStage>;
+  const size_t smem = (size_t)EPB * Shape<N>::SLOT * sizeof(double);
+  if (set_kernel_smem<k>((int)smem, true) != cudaSuccess) return 0;
+  int dev = 0, sms = 0, per_sm = 0;
+  if (cudaGetDevice(&dev) != cudaSuccess ||
+      cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev) != cudaSuccess ||
+      cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k, N * N * EPB, smem) != cudaSuccess)
+    return 0;
+  return (int64_t)per_sm * sms * EPB;
+}
+
+template <int N>
+int64_t wave_v(int variant) {
+  return variant ? wave_n<N, 1>() : wave_n<N, 0>();
+}
+
 }  // namespace
+
+int64_t stage_fp64_wave_elements(int n, int variant) {
+  switch (n) {
+    case 2: return wave_v<2>(variant);
+    case 3: return wave_v<3>(variant);
+    case 4: return wave_v<4>(variant);
+    case 5: return wave_v<5>(variant);
+    case 6: return wave_v<6>(variant);
+    case 7: return wave_v<7>(variant);
+    case 8: return wave_v<8>(variant);
+    case 9: return wave_v<9>(variant);
+    case 10: return wave_v<10>(variant);
+    case 11: return wave_v<11>(variant);
+    case 12: return wave_v<12>(variant);
+    default: return 0;
+  }
+}
 
 cudaError_t launch_stage_fp64(const StageLaunch& L, cudaStream_t s) {
   switch (L.n) {

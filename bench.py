@@ -255,7 +255,7 @@ def time_path(args, precision, dev, rank, ws, sample_clocks):
 
 
 def time_batched(args, dev):
-    """Config 3: 256 independent evolutions, per-element LGL extents in
+    """The batched case: 256 independent evolutions, per-element LGL extents in
     {4..10}, p-nonconforming mortars, Gaussian pulses; FP64 and mixed, and
     the worst per-instance rel L2 of mixed against FP64 after the same steps."""
     import torch
@@ -308,7 +308,7 @@ def time_batched(args, dev):
 
 
 def time_adjoint(dev):
-    """Config 4: 8^3 elements x 8^3 points, dt 5e-4, 2000 SSP-RK3 steps, 64
+    """The adjoint case: 8^3 elements x 8^3 points, dt 5e-4, 2000 SSP-RK3 steps, 64
     samples every 10 steps; seconds per gradient (forward misfit run + the
     discrete adjoint sweep), with central-difference and tangent-linear checks
     along seeded directions."""
@@ -390,7 +390,7 @@ def time_curved_adams(shell, n, dt, steps, dev):
 
 
 def time_curved(args, dev, with_cpu):
-    """Config 5: CurvedScalarWave on Schwarzschild in Kerr-Schild coordinates
+    """The curved case: CurvedScalarWave on Schwarzschild in Kerr-Schild coordinates
     (M = 1, gamma1 = 0, gamma2 = 1), six-wedge shell r in [1.9, 20], 4 x 4
     angular x 8 radial elements per wedge (768), logarithmic radial map, 10^3
     LGL points per element, Gaussian shell Psi = exp(-(r-8)^2), excision
@@ -487,7 +487,7 @@ AB3_TRAFFIC_PER_POINT = (814.1e6 + 415.1e6) / 4096000
 
 
 def time_adams(args, dev):
-    """AdamsBashforth(3) on the FP64 config-2 mesh (32^3 elements at 8^3,
+    """AdamsBashforth(3) on the 32^3-element mesh (8^3 points,
     Gaussian pulse, slab = step = 2e-4): global stepping, and local time
     stepping with half of the elements (seeded) on level 1 (two steps of
     1e-4 per slab).  The start-up runs in the warm-up; the timed slabs are

@@ -110,7 +110,7 @@ def test_autograd_function():
 
 @pytest.mark.slow
 def test_config4_gradient_checks():
-    # Config 4 at full size: 8^3 elements x 8^3 points, dt 5e-4, 2000 steps,
+    # The adjoint case at full size: 8^3 elements x 8^3 points, dt 5e-4, 2000 steps,
     # 64 samples every 10 steps; 16 central-difference directions and one
     # tangent-linear direction
     import torch

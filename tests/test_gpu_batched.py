@@ -94,7 +94,7 @@ def test_general_substeps(oracle):
 
 
 def test_batched_evolution_matches_oracle(oracle):
-    # 12 instances drawn like config 3, 10 SSP-RK3 steps at dt = 1e-4
+    # 12 instances drawn like the 256-instance batch, 10 SSP-RK3 steps at dt = 1e-4
     bricks, pts, params = workloads.batched_instances(12, seed=5)
     dt, steps = 1e-4, 10
     u0 = oracle.initial_data(bricks, pts, "gaussian", params)
@@ -136,7 +136,7 @@ def test_batched_mixed_rhs(oracle):
 
 @pytest.mark.slow
 def test_config3_full_size(oracle):
-    # Config 3 at full size: 256 instances; one FP64 step against the oracle,
+    # The 256-instance batch at full size; one FP64 step against the oracle,
     # then 30 steps mixed vs FP64 on the device, rel L2 per instance
     bricks, pts, params = workloads.batched_instances(256, seed=2024)
     dt = 1e-4

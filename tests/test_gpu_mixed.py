@@ -58,7 +58,7 @@ def test_mixed_substeps_match_oracle(oracle):
 
 
 def test_mixed_config1_full_run(oracle):
-    # Config 1 for 200 steps: mixed vs the FP64 oracle (rel L2 <= 1e-6)
+    # The 4^3 x 6^3 plane-wave case for 200 steps: mixed vs the FP64 oracle (rel L2 <= 1e-6)
     bricks = [Brick((4, 4, 4))]
     n, dt, steps = 6, 1e-3, 200
     u0 = oracle.initial_data(bricks, n, "plane_wave", [1, 1, 1])
@@ -72,7 +72,7 @@ def test_mixed_config1_full_run(oracle):
 
 
 def test_mixed_vs_fp64_config2_size():
-    # Config 2 grid (32^3 x 8^3, Gaussian pulse, dt 2e-4), 50 steps: mixed vs
+    # The Gaussian-pulse grid (32^3 x 8^3, Gaussian pulse, dt 2e-4), 50 steps: mixed vs
     # the plain FP64 CUDA path (which matches the oracle to 1e-12 per step)
     bricks = [Brick((32, 32, 32))]
     n, dt, steps = 8, 2e-4, 50

@@ -120,7 +120,7 @@ def test_volume_rhs_matches_oracle(oracle):
 
 
 def test_config1_rhs_and_substeps(oracle):
-    # Config 1: 4^3 elements, N = 6, plane wave k = (1,1,1)
+    # The plane-wave case: 4^3 elements, N = 6, k = (1,1,1)
     bricks = [Brick((4, 4, 4))]
     n, dt = 6, 1e-3
     u0 = oracle.initial_data(bricks, n, "plane_wave", [1, 1, 1])
@@ -178,7 +178,7 @@ def test_graph_chunks_equal_single_steps(oracle):
 
 @pytest.mark.slow
 def test_config2_full_size_one_step(oracle):
-    # Config 2 at full size: 32^3 elements, N = 8, Gaussian pulse, one SSP-RK3
+    # The Gaussian-pulse case at full size: 32^3 elements, N = 8, Gaussian pulse, one SSP-RK3
     # step against the oracle (about 16.8M points; the oracle runs multi-threaded).
     bricks = [Brick((32, 32, 32))]
     n, dt = 8, 2e-4
@@ -194,7 +194,7 @@ def test_config2_full_size_one_step(oracle):
 
 
 def test_linearity_full_size():
-    # L(a u + b v) = a L(u) + b L(v) at config-2 size, on the device
+    # L(a u + b v) = a L(u) + b L(v) at 32^3 x 8^3, on the device
     import torch
     bricks = [Brick((32, 32, 32))]
     n = 8

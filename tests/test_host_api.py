@@ -62,9 +62,9 @@ def test_product_mortar_projections_match_oracle(dgsw_lib, oracle):
 
 
 CASES = [
-    [Brick((4, 4, 4))],                     # config 1 lattice
-    [Brick((32, 32, 32))],                  # config 2 lattice (32,768 elements)
-    [Brick((8, 8, 8))],                     # config 4 lattice
+    [Brick((4, 4, 4))],                     # the 4^3 plane-wave lattice
+    [Brick((32, 32, 32))],                  # the 32^3 lattice (32,768 elements)
+    [Brick((8, 8, 8))],                     # the 8^3 adjoint lattice
     [Brick((3, 6, 5)), Brick((2, 7, 8)), Brick((1, 1, 1))],
 ]
 
@@ -81,7 +81,7 @@ def test_index_maps_bit_exact(dgsw_lib, oracle, case):
 
 
 def test_index_maps_random_batched(dgsw_lib, oracle):
-    # config-3-like batches: per-axis counts in {2..8}, per-element N in {4..10}
+    # batches like the 256-instance one: per-axis counts in {2..8}, per-element N in {4..10}
     rng = np.random.default_rng(7)
     bricks = [Brick(tuple(int(v) for v in rng.integers(2, 9, 3))) for _ in range(24)]
     E = oracle.num_elements(bricks)

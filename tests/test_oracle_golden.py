@@ -181,7 +181,7 @@ def test_index_maps_known(oracle):
 
 
 def test_plane_wave_convergence(oracle):
-    # Scaled-down config 1 (plane wave on [0, 2pi]^3, k=(1,1,1)): the DG
+    # A scaled-down plane-wave case (plane wave on [0, 2pi]^3, k=(1,1,1)): the DG
     # solution converges to the analytic wave at the spectral rate.
     errs = []
     for n in (4, 5, 6):

@@ -228,7 +228,9 @@ int dgsw_substep(DgswHandle h, int k, double dt);
  * overlapped with the stages of the first and the last step (a stage of a
  * chunk waits only for the chunks holding its face neighbours); otherwise
  * the whole state is copied around the steps.  host_u should be pinned
- * (cudaHostAlloc / cudaHostRegister) for full link bandwidth. */
+ * (cudaHostAlloc / cudaHostRegister) for full link bandwidth.  As with
+ * dgsw_set_state, an AdamsBashforth handle takes the host values as new
+ * initial values (self-start). */
 int dgsw_step_host(DgswHandle h, double* host_u, int n_steps, double dt);
 
 /* ---- TimeStepper (AdamsBashforth, local time stepping) -------------------

@@ -574,6 +574,15 @@ cudaError_t enqueue_mixed_stage(DgswHandle h, int k, double dt, const double* u0
       G.alpha = 2.0 / 3.0;
       G.beta = 2.0 / 3.0;
       G.c = (2.0 / 3.0) * dt;
+      if (out) {
+        // as on the uniform path: W in place into d1 (each point's d1 is
+        // read only by the thread that overwrites it), then u0 + W in one
+        // FP64 stream; reading u0 pointwise inside the stage measured slower
+        G.w32 = h->w1;
+        cudaError_t e = launch_general_classes(h, G);
+        if (e != cudaSuccess) return e;
+        return launch_accumulate(out, u0, h->w1, h->dom.offset.back(), h->stream);
+      }
     }
     if (out) {
       G.out64 = out;

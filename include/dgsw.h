@@ -48,7 +48,8 @@ typedef enum {
   DGSW_ERR_UNSUPPORTED = -3,  /* valid request this build does not support */
   DGSW_ERR_NOT_FINITE = -4,   /* NaN or Inf detected in the state */
   DGSW_ERR_NO_DEVICE = -5,    /* no usable GB300-class device */
-  DGSW_ERR_DEVICE_TIMEOUT = -6 /* a bounded device-side wait gave up */
+  DGSW_ERR_DEVICE_TIMEOUT = -6, /* a bounded device-side wait gave up */
+  DGSW_ERR_CFL = -7             /* a step longer than the Cfl step (dgsw_set_guards) */
 } DgswStatus;
 
 /* System::variables_tag, ScalarWave/System.hpp:39-57 and
@@ -294,6 +295,27 @@ typedef struct {
 int dgsw_adams_schedule(int order, const int64_t* level_counts, const int32_t* adjacency,
                         double slab, int n_slabs, int max_jobs, DgswAdamsJob* jobs,
                         int* n_jobs, int64_t* ticks_per_slab, int* ring_slots);
+
+/* ---- step size and state guards ---------------------------------------------
+ * dgsw_cfl_steps: StepChoosers::Cfl (src/Time/StepChoosers/Cfl.hpp:55-67) for
+ * every element of a configuration: safety_factor * stable_step of the
+ * configured time stepper (Rk3HesthavenSsp.cpp:23-26, AdamsBashforth.cpp:
+ * 66-82) * the element's minimum grid spacing (src/Domain/
+ * MinimumGridSpacing.cpp) / (its largest characteristic speed * 3)
+ * (ScalarWave: 1; CurvedScalarWave: Characteristics.cpp:202-212).  Host-only;
+ * element_steps (one per element) and min_step may be NULL.
+ * dgsw_set_guards: with cfl_safety_factor > 0, dgsw_step refuses, before any
+ * work, a step longer than an element's Cfl step (for AdamsBashforth: the
+ * slab / 2^level of any element) with DGSW_ERR_CFL, as the Cfl chooser
+ * rejects it; with check_finite, dgsw_step checks the state afterwards and
+ * reports a NaN or Inf with DGSW_ERR_NOT_FINITE (the message names the first
+ * element).  Both off at creation.
+ * dgsw_check_finite: the first element whose values hold a NaN or an Inf,
+ * -1 when all are finite. */
+int dgsw_cfl_steps(const DgswConfig* config, double safety_factor, double* element_steps,
+                   double* min_step);
+int dgsw_set_guards(DgswHandle h, double cfl_safety_factor, int check_finite);
+int dgsw_check_finite(DgswHandle h, int64_t* first_element);
 
 /* ---- launch autotuner -------------------------------------------------------
  * The plain FP64 stage kernel exists in two launch configurations per N

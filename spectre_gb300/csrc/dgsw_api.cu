@@ -12,6 +12,7 @@
 #include <map>
 #include <mutex>
 #include <new>
+#include <algorithm>
 #include <string>
 #include <vector>
 
@@ -95,8 +96,14 @@ struct DgswHandle_ {
   int32_t* r_face_idx = nullptr;  // per element face
   double* r_PR = nullptr;         // [P lower, P upper, R lower, R upper], n*n each
   double* r_wext = nullptr;       // n*n per record
+  // guards of dgsw_step (dgsw_set_guards)
+  double guard_cfl = 0.0;
+  bool guard_finite = false;
+  std::vector<double> cfl_e;            // Cfl step per element
+  unsigned long long* dev_first = nullptr;
   // AdamsBashforth with local time stepping (adams_schedule.cpp, adams_step.cu)
   bool adams = false;
+  std::vector<int8_t> ab_level_host;
   AdamsSchedule ab;
   int64_t ab_count[kAbMaxLevels] = {};
   int32_t* ab_list = nullptr;   // element ids sorted by step level
@@ -800,6 +807,7 @@ int adams_init(DgswHandle h, const DgswConfig& cfg) {
   cudaError_t e;
   if ((e = upload(&h->ab_list, list)) != cudaSuccess) return cuda_fail(h, e, "upload level list");
   if ((e = upload(&h->ab_level, level)) != cudaSuccess) return cuda_fail(h, e, "upload levels");
+  h->ab_level_host = level;
   const int n = h->dom.elem_n[0];
   const size_t slots = (size_t)h->ab.ring_slots();
   if ((e = cudaMalloc(&h->ab_F, slots * E * kVars * n * n * n * sizeof(double))) != cudaSuccess)
@@ -1554,6 +1562,7 @@ int dgsw_destroy(DgswHandle h) {
   if (h->pipe_in) cudaStreamDestroy(h->pipe_in);
   if (h->pipe_out) cudaStreamDestroy(h->pipe_out);
   if (h->pipe_aux) cudaStreamDestroy(h->pipe_aux);
+  if (h->dev_first) cudaFree(h->dev_first);
   if (h->ab_list) cudaFree(h->ab_list);
   if (h->ab_level) cudaFree(h->ab_level);
   if (h->ab_F) cudaFree(h->ab_F);
@@ -2014,10 +2023,88 @@ int dgsw_exponential_filter_matrix(int n, double alpha, int half_power, double* 
   return DGSW_OK;
 }
 
+static int step_impl(DgswHandle h, int n_steps, double dt);
+
+// the first element whose block holds a NaN or an Inf, -1 if none
+static int first_non_finite(DgswHandle h, int64_t* first) {
+  if (!h->dev_first) DGSW_CUDA(h, cudaMalloc(&h->dev_first, sizeof(unsigned long long)));
+  DGSW_CUDA(h, cudaMemsetAsync(h->dev_first, 0xff, sizeof(unsigned long long), h->stream));
+  DGSW_CUDA(h, launch_finite_check(h->state, h->offset, h->dom.n_elem, h->dev_first, h->stream));
+  unsigned long long v = 0;
+  DGSW_CUDA(h, cudaMemcpyAsync(&v, h->dev_first, sizeof(v), cudaMemcpyDeviceToHost, h->stream));
+  DGSW_CUDA(h, cudaStreamSynchronize(h->stream));
+  *first = v == ~0ull ? -1 : (int64_t)v;
+  return DGSW_OK;
+}
+
 int dgsw_step(DgswHandle h, int n_steps, double dt) {
   if (!h) return fail(nullptr, DGSW_ERR_ARGUMENT, "null handle");
   if (n_steps < 0 || !std::isfinite(dt)) return fail(h, DGSW_ERR_ARGUMENT, "bad step arguments");
   if (n_steps == 0) return DGSW_OK;
+  if (h->guard_cfl > 0.0) {
+    // StepChoosers::Cfl rejects a step longer than the element's Cfl step
+    for (int64_t e = 0; e < h->dom.n_elem; ++e) {
+      const double step = h->adams ? std::ldexp(std::abs(dt), -(int)h->ab_level_host[e]) : std::abs(dt);
+      if (step > h->cfl_e[e])
+        return fail(h, DGSW_ERR_CFL,
+                    "the step " + std::to_string(step) + " of element " + std::to_string(e) +
+                        " exceeds its Cfl step " + std::to_string(h->cfl_e[e]));
+    }
+  }
+  const int rc = step_impl(h, n_steps, dt);
+  if (rc || !h->guard_finite) return rc;
+  int64_t first = -1;
+  if (int r = first_non_finite(h, &first)) return r;
+  if (first >= 0)
+    return fail(h, DGSW_ERR_NOT_FINITE,
+                "NaN or Inf in the state after the step, first in element " + std::to_string(first));
+  return DGSW_OK;
+}
+
+int dgsw_set_guards(DgswHandle h, double cfl_safety_factor, int check_finite) {
+  if (!h) return fail(nullptr, DGSW_ERR_ARGUMENT, "null handle");
+  if (!std::isfinite(cfl_safety_factor) || cfl_safety_factor < 0.0)
+    return fail(h, DGSW_ERR_ARGUMENT, "the Cfl safety factor must be >= 0 (0: off)");
+  if (cfl_safety_factor > 0.0) {
+    std::string err;
+    ShellGeometry geo;
+    Domain dom;
+    const Domain* d = &h->dom;
+    if (h->curved) {  // the shell's inertial coordinates, rebuilt on the host
+      if (!build_shell_domain(h->cfg, &dom, &geo, &err)) return fail(h, DGSW_ERR_ARGUMENT, err);
+      d = &dom;
+    }
+    if (!cfl_steps(h->cfg, *d, h->curved ? &geo : nullptr, cfl_safety_factor, &h->cfl_e, &err))
+      return fail(h, DGSW_ERR_ARGUMENT, err);
+  }
+  h->guard_cfl = cfl_safety_factor;
+  h->guard_finite = check_finite != 0;
+  return DGSW_OK;
+}
+
+int dgsw_check_finite(DgswHandle h, int64_t* first_element) {
+  if (!h || !first_element) return fail(h, DGSW_ERR_ARGUMENT, "null argument");
+  if (int rc = select_device(h)) return rc;
+  return first_non_finite(h, first_element);
+}
+
+int dgsw_cfl_steps(const DgswConfig* cfg, double safety_factor, double* element_steps,
+                   double* min_step) {
+  if (!cfg) return fail(nullptr, DGSW_ERR_ARGUMENT, "null config");
+  Domain dom;
+  ShellGeometry geo;
+  std::string err;
+  if (!any_domain(*cfg, &dom, &geo, &err)) return fail(nullptr, DGSW_ERR_ARGUMENT, err);
+  std::vector<double> steps;
+  const bool curved = cfg->system == DGSW_SYSTEM_CURVED_SCALAR_WAVE_3D;
+  if (!cfl_steps(*cfg, dom, curved ? &geo : nullptr, safety_factor, &steps, &err))
+    return fail(nullptr, DGSW_ERR_ARGUMENT, err);
+  if (element_steps) std::memcpy(element_steps, steps.data(), steps.size() * sizeof(double));
+  if (min_step) *min_step = steps.empty() ? 0.0 : *std::min_element(steps.begin(), steps.end());
+  return DGSW_OK;
+}
+
+static int step_impl(DgswHandle h, int n_steps, double dt) {
   if (int rc = select_device(h)) return rc;
   if (h->adams) return adams_step(h, n_steps, dt);
   if (!h->tuned && tunable(h)) {

@@ -88,6 +88,12 @@ struct ShellGeometry {
   std::vector<int32_t> back_dir;
 };
 
+// StepChoosers::Cfl per element (cfl.cpp): safety * stable_step * minimum
+// grid spacing / (largest characteristic speed * 3).
+double time_stepper_stable_step(const DgswConfig& cfg);
+bool cfl_steps(const DgswConfig& cfg, const Domain& dom, const struct ShellGeometry* geo,
+               double safety, std::vector<double>* steps, std::string* err);
+
 // Builds the shell's element maps (Domain fields: element ids, neighbours
 // with -1 / -2 on the inner / outer sphere, offsets) and its geometry.
 bool build_shell_domain(const DgswConfig& cfg, Domain* dom, ShellGeometry* geo,

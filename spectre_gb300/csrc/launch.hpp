@@ -60,6 +60,10 @@ struct StageLaunch {
 };
 
 cudaError_t launch_stage_fp64(const StageLaunch& L, cudaStream_t s);
+// Lowers *first to the smallest element index whose block of u holds a NaN
+// or an Inf (guards.cu).
+cudaError_t launch_finite_check(const double* u, const int64_t* offset, int64_t n_elem,
+                                unsigned long long* first, cudaStream_t s);
 // Elements that one full wave of the FP64 stage kernel (extent n, launch
 // variant) holds on the current device; 0 if unknown.
 int64_t stage_fp64_wave_elements(int n, int variant);

@@ -35,6 +35,7 @@ STATUS_NAMES = {
     -4: "DGSW_ERR_NOT_FINITE",
     -5: "DGSW_ERR_NO_DEVICE",
     -6: "DGSW_ERR_DEVICE_TIMEOUT",
+    -7: "DGSW_ERR_CFL",
 }
 PRECISION_FP64 = 0
 PRECISION_MIXED = 1
@@ -143,6 +144,9 @@ _SIGNATURES = {
     "dgsw_misfit_adjoint": (_I, [_P, _P]),
     "dgsw_step_noalloc": (_I, [ctypes.POINTER(DgswBrick), _I, _D, _P, _I, _D, _P]),
     "dgsw_adams_info": (_I, [_P, _P, _P, _P, _P]),
+    "dgsw_cfl_steps": (_I, [ctypes.POINTER(DgswConfig), _D, _P, _P]),
+    "dgsw_set_guards": (_I, [_P, _D, _I]),
+    "dgsw_check_finite": (_I, [_P, ctypes.POINTER(_I64)]),
     "dgsw_adams_coefficients": (_I, [_I, _P, _I64, _I64, _D, _I64, _P]),
     "dgsw_lts_coefficients": (_I, [_I, _P, _P, _I, _P, _P, _I64, _I64, _D, _I64, _I, _I, _I,
                                    _I, _P, _P, _P]),
@@ -366,6 +370,33 @@ def half_projections(n: int, upper: bool):
     return P, R
 
 
+def cfl_steps(bricks, points, safety_factor=1.0, time_stepper="rk3_hesthaven_ssp", order=3,
+              quadrature="gauss_lobatto", gamma2=0.0):
+    """StepChoosers::Cfl per element (host-only): returns the array of
+    element steps.  bricks: Brick list, Shell or RefinedBrick."""
+    if isinstance(bricks, Brick):
+        bricks = [bricks]
+    holder = _ConfigHolder(bricks, points, gamma2=gamma2, quadrature=quadrature,
+                           time_stepper=time_stepper, order=order)
+    ne, nd = _I64(), _I64()
+    _check(lib().dgsw_count_elements(ctypes.byref(holder.cfg), ctypes.byref(ne), ctypes.byref(nd)))
+    out = np.zeros(ne.value)
+    m = ctypes.c_double()
+    _check(lib().dgsw_cfl_steps(ctypes.byref(holder.cfg), float(safety_factor), _ptr(out),
+                                ctypes.byref(m)))
+    return out
+
+
+def levels_from_cfl(element_steps, slab):
+    """Step levels for AdamsBashforth local time stepping: the smallest l in
+    0..3 with slab / 2^l within each element's Cfl step."""
+    s = np.asarray(element_steps, dtype=np.float64)
+    lv = np.ceil(np.log2(np.maximum(slab / s, 1.0))).astype(np.int32)
+    if np.any(lv > 3):
+        raise ValueError("the slab needs more than 3 levels below it")
+    return lv
+
+
 def adams_coefficients(control_ticks, step_start, step_end, slab=1.0, ticks_per_slab=1):
     """adams_coefficients::coefficients for control times given in ticks."""
     t = np.ascontiguousarray(control_ticks, dtype=np.int64)
@@ -573,6 +604,18 @@ class DgEvolution:
 
     def stream_ptr(self) -> int:
         return lib().dgsw_stream(self._h) or 0
+
+    def set_guards(self, cfl_safety_factor: float = 0.0, check_finite: bool = False):
+        """dgsw_step refuses steps longer than the Cfl step (factor > 0) and
+        reports NaN / Inf in the state afterwards (check_finite)."""
+        _check(lib().dgsw_set_guards(self._h, float(cfl_safety_factor), int(bool(check_finite))),
+               self._h)
+
+    def first_non_finite_element(self) -> int:
+        """The first element holding a NaN or Inf, -1 if none."""
+        v = _I64()
+        _check(lib().dgsw_check_finite(self._h, ctypes.byref(v)), self._h)
+        return v.value
 
     def adams_info(self):
         """AdamsBashforth handles: dict of ring_slots, ticks_per_slab,

@@ -8,6 +8,7 @@
 // (dt, steps-per-graph) and replayed.
 #include <cmath>
 #include <cstdio>
+#include <cstdlib>
 #include <cstring>
 #include <map>
 #include <mutex>
@@ -112,10 +113,16 @@ struct DgswHandle_ {
   double* ab_B = nullptr;       // ring of face data
   double ab_slab = std::nan("");
   // steps of a host-resident state with the copies overlapped (dgsw_step_host)
-  cudaStream_t pipe_in = nullptr, pipe_out = nullptr, pipe_aux = nullptr;
+  cudaStream_t pipe_in = nullptr, pipe_out = nullptr;
+  std::vector<cudaStream_t> pipe_aux;          // compute streams besides the handle's
   std::vector<cudaEvent_t> pipe_ev;            // per chunk: in, stage 1, 2, 3; plus 2
   std::vector<int64_t> chunk_begin;            // chunks + 1 element offsets
   std::vector<std::vector<int>> chunk_deps;    // chunks holding a chunk's neighbours
+  std::vector<int> pipe_order[2];              // stage launches (3 c + stage) in issue
+                                               // order, without / with copies in
+  int pipe_streams = 4;                        // compute streams
+  int pipe_priority = 0;                       // PipePriority of the issue order
+  int pipe_edge_chunks = 3;                    // thin chunks at each end of the order
   // graphs of pipelined steps on pinned host buffers: copies in and out, in
   // only, out only; each for one host pointer and dt
   cudaGraphExec_t pipe_graph[3] = {nullptr, nullptr, nullptr};
@@ -898,35 +905,114 @@ int adams_step(DgswHandle h, int n_steps, double dt) {
 // The elements are cut into contiguous chunks.  Copy-in of chunk c, the
 // three stages of chunk c and the copy-out of chunk c are separate
 // operations; a stage of chunk c waits only for the previous stage (or the
-// copy-in) of the chunks holding c's face neighbours.  Issued in wavefront
-// order on two compute streams, the copies of one chunk overlap the stages
-// of others and each other (the host link carries both directions at once).
+// copy-in) of the chunks holding c's face neighbours.  The stage launches are
+// issued in the order of a list schedule (plan_pipe) over several compute
+// streams, so that launches that do not depend on each other fill each
+// other's tails, and the copies of some chunks overlap the stages of others
+// (the host link carries both directions at once).
 bool pipelinable(DgswHandle h) {
   return !mixed(h) && !h->curved && !h->gauss && !h->general && !h->refined && !h->adams &&
          !h->filter_on && h->dom.n_elem >= 4096;
 }
 
+// Priorities of the list schedule among the launches whose inputs are
+// complete in the model
+enum PipePriority {
+  kPipeLatestStage = 0,  // the latest stage first (its chunk's copy-out starts sooner)
+  kPipeFirstStage = 1,   // first stages first (they use the copied data), then the latest
+  kPipeEarliest = 2,     // the launch whose inputs completed first
+};
+
+// The issue order of the 3 C stage launches (3 c + stage).  The model: the
+// copies in land one after another in element order at the host link's rate
+// (copy_s per element; all at time 0 without copies in), and the GPU runs one
+// launch at a time, a stage of chunk c taking its elements times stage_s.
+// Whenever the modelled GPU is free it takes, among the launches whose
+// inputs are complete, the first by the priority; ties go to the lower chunk.
+std::vector<int> plan_pipe(const std::vector<int64_t>& begin,
+                           const std::vector<std::vector<int>>& deps, bool copy_in,
+                           double copy_s, double stage_s, int priority) {
+  const int C = (int)begin.size() - 1;
+  std::vector<double> t_in(C, 0.0), done(3 * C, 0.0);
+  double t = 0.0;
+  if (copy_in)
+    for (int c = 0; c < C; ++c) t_in[c] = (t += (begin[c + 1] - begin[c]) * copy_s);
+  std::vector<int> level(C, 0), order;
+  t = 0.0;
+  while ((int)order.size() < 3 * C) {
+    int best = -1;
+    double best_ready = 0.0, next_ready = INFINITY;
+    for (int c = 0; c < C; ++c) {
+      const int st = level[c];
+      if (st == 3) continue;
+      bool ok = true;
+      double ready = 0.0;
+      for (int d : deps[c]) {
+        if (st > 0 && level[d] < st) ok = false;
+        else ready = std::max(ready, st == 0 ? t_in[d] : done[3 * d + st - 1]);
+      }
+      if (!ok) continue;
+      if (ready > t) {
+        next_ready = std::min(next_ready, ready);
+        continue;
+      }
+      bool better = best < 0;
+      if (!better) {
+        const int bst = level[best];
+        switch (priority) {
+          case kPipeFirstStage:
+            better = (st == 0) != (bst == 0) ? st == 0 : st > bst;
+            break;
+          case kPipeEarliest:
+            better = ready < best_ready || (ready == best_ready && st > bst);
+            break;
+          default:
+            better = st > bst;
+        }
+      }
+      if (better) {
+        best = c;
+        best_ready = ready;
+      }
+    }
+    if (best < 0) {
+      if (!(next_ready < INFINITY)) break;  // a dependency cycle: cannot happen
+      t = next_ready;
+      continue;
+    }
+    const int st = level[best]++;
+    t += (begin[best + 1] - begin[best]) * stage_s;
+    done[3 * best + st] = t;
+    order.push_back(3 * best + st);
+  }
+  return order;
+}
+
 int pipe_init(DgswHandle h) {
   if (h->pipe_in) return DGSW_OK;
   const int64_t E = h->dom.n_elem;
-  // Chunks of E/16 elements, except thin ones (E/32) at both ends of the
-  // element order: on a periodic brick the chunks are x-slabs on a ring, and
-  // the last chunk copied in holds back the three-stage chains of the chunks
-  // within three of it (the first and the last few), whose stages and
-  // copies-out then form the tail of the step.  Thin chunks there shorten
-  // the tail; thick ones elsewhere keep the launches efficient.
-  // Chunk sizes are whole waves of the stage kernel where the state allows,
-  // so that no chunk launch ends on a partly filled wave.
-  int64_t thin = std::max<int64_t>(256, E / 32), thick = std::max<int64_t>(512, E / 16);
+  // Chunks of two waves of the stage kernel in the middle of the element
+  // order and thin ones at both ends.  On a periodic brick the chunks are
+  // slabs on a ring, and the last chunk copied in holds back the stage
+  // chains of the chunks around it (the last few and the first few), which
+  // then form the tail of the step.  The thin chunks are as wide as the
+  // neighbour reach (the largest distance around the ring of element indices
+  // between an element and a face neighbour), so that the work held back is
+  // whole neighbour layers.
+  int64_t reach = 1;
+  for (int64_t e = 0; e < E; ++e)
+    for (int f = 0; f < 6; ++f) {
+      const int64_t d = std::llabs(h->dom.neighbor[6 * e + f] - e);
+      reach = std::max(reach, std::min(d, E - d));
+    }
   const int64_t wave = stage_fp64_wave_elements(h->dom.elem_n[0], h->stage_variant);
-  if (wave > 0 && E >= 24 * wave) {
-    thin = wave;
-    thick = 2 * wave;
-  }
+  const int64_t thick = std::max<int64_t>(512, wave > 0 && E >= 24 * wave ? 2 * wave : E / 16);
+  const int64_t thin = std::min(thick, std::max<int64_t>(256, reach));
+  const int n_edge = std::max(1, h->pipe_edge_chunks);
   h->chunk_begin.assign(1, 0);
-  for (int k = 0; k < 3 && h->chunk_begin.back() + thin < E; ++k)
+  for (int k = 0; k < n_edge && h->chunk_begin.back() + thin < E; ++k)
     h->chunk_begin.push_back(h->chunk_begin.back() + thin);
-  const int64_t tail_start = std::max(h->chunk_begin.back(), E - 4 * thin);
+  const int64_t tail_start = std::max(h->chunk_begin.back(), E - n_edge * thin);
   while (h->chunk_begin.back() + thick <= tail_start)
     h->chunk_begin.push_back(h->chunk_begin.back() + thick);
   if (h->chunk_begin.back() < tail_start) h->chunk_begin.push_back(tail_start);
@@ -945,9 +1031,23 @@ int pipe_init(DgswHandle h) {
     for (int d = 0; d < C; ++d)
       if (need[d]) h->chunk_deps[c].push_back(d);
   }
+  // the model's rates: the host link at 200 GB/s; a stage at the launch time
+  // the autotuner measured on the whole state, else 0.1 ns per point
+  const int64_t pts = (int64_t)h->dom.elem_n[0] * h->dom.elem_n[0] * h->dom.elem_n[0];
+  const double copy_s = kVars * pts * sizeof(double) / 200e9;
+  const double tuned_ms = h->tuned ? h->tune_ms[h->stage_variant] : 0.0;
+  const double stage_s = tuned_ms > 0.0 ? tuned_ms * 1e-3 / E : pts * 1e-10;
+  for (int k = 0; k < 2; ++k) {
+    h->pipe_order[k] = plan_pipe(h->chunk_begin, h->chunk_deps, k == 1, copy_s, stage_s,
+                                 h->pipe_priority);
+    if ((int)h->pipe_order[k].size() != 3 * C)
+      return fail(h, DGSW_ERR_ARGUMENT, "chunk schedule did not complete");
+  }
   DGSW_CUDA(h, cudaStreamCreateWithFlags(&h->pipe_in, cudaStreamNonBlocking));
   DGSW_CUDA(h, cudaStreamCreateWithFlags(&h->pipe_out, cudaStreamNonBlocking));
-  DGSW_CUDA(h, cudaStreamCreateWithFlags(&h->pipe_aux, cudaStreamNonBlocking));
+  h->pipe_aux.assign(std::max(1, h->pipe_streams) - 1, nullptr);
+  for (cudaStream_t& s : h->pipe_aux)
+    DGSW_CUDA(h, cudaStreamCreateWithFlags(&s, cudaStreamNonBlocking));
   h->pipe_ev.assign(4 * C + 2, nullptr);
   for (cudaEvent_t& ev : h->pipe_ev)
     DGSW_CUDA(h, cudaEventCreateWithFlags(&ev, cudaEventDisableTiming));
@@ -961,10 +1061,12 @@ int pipelined_step(DgswHandle h, double* host_u, double dt, bool copy_in, bool c
   const int64_t per = kVars * (int64_t)h->dom.elem_n[0] * h->dom.elem_n[0] * h->dom.elem_n[0];
   auto ev = [&](int kind, int c) { return h->pipe_ev[4 * c + kind]; };  // 0 in, 1-3 stages
   cudaEvent_t start = h->pipe_ev[4 * C], done = h->pipe_ev[4 * C + 1];
-  cudaStream_t cs[2] = {h->stream, h->pipe_aux};
+  std::vector<cudaStream_t> cs(1, h->stream);
+  cs.insert(cs.end(), h->pipe_aux.begin(), h->pipe_aux.end());
+  const int S = (int)cs.size();
   // everything already queued on the handle's stream comes first
   DGSW_CUDA(h, cudaEventRecord(start, h->stream));
-  DGSW_CUDA(h, cudaStreamWaitEvent(h->pipe_aux, start, 0));
+  for (int s = 1; s < S; ++s) DGSW_CUDA(h, cudaStreamWaitEvent(cs[s], start, 0));
   if (copy_in) {
     DGSW_CUDA(h, cudaStreamWaitEvent(h->pipe_in, start, 0));
     for (int c = 0; c < C; ++c) {
@@ -975,61 +1077,51 @@ int pipelined_step(DgswHandle h, double* host_u, double dt, bool copy_in, bool c
     }
   }
   if (copy_out) DGSW_CUDA(h, cudaStreamWaitEvent(h->pipe_out, start, 0));
-  // wavefront order: after each chunk's copy-in, every stage whose inputs
-  // are then complete
-  std::vector<int> level(C, 0);  // stages issued per chunk
-  std::vector<char> loaded(C, copy_in ? 0 : 1);
   const StageCoef coef[3] = {{0.0, 1.0, dt}, {0.75, 0.25, 0.25 * dt},
                              {1.0 / 3.0, 2.0 / 3.0, (2.0 / 3.0) * dt}};
   const double* in[3] = {h->state, h->t1, h->t2};
   double* out[3] = {h->t1, h->t2, h->state};
-  for (int k = 0; k <= C; ++k) {
-    if (copy_in && k < C) loaded[k] = 1;
-    if (!copy_in && k > 0) break;
-    bool progress = true;
-    while (progress) {
-      progress = false;
-      for (int c = 0; c < C; ++c) {
-        const int st = level[c];
-        if (st == 3) continue;
-        bool ready = true;
-        for (int d : h->chunk_deps[c]) ready = ready && (st == 0 ? loaded[d] != 0 : level[d] >= st);
-        if (!ready) continue;
-        cudaStream_t q = cs[c & 1];
-        for (int d : h->chunk_deps[c]) {
-          if (st == 0) {
-            if (copy_in) DGSW_CUDA(h, cudaStreamWaitEvent(q, ev(0, d), 0));
-          } else if ((d & 1) != (c & 1)) {
-            DGSW_CUDA(h, cudaStreamWaitEvent(q, ev(st, d), 0));
-          }
-        }
-        StageLaunch L = base_launch(h);
-        L.mode = st == 0 ? kModeStageFirst : kModeStage;
-        L.ucur = in[st];
-        L.u0 = h->state;
-        L.unext = out[st];
-        L.coef = coef[st];
-        L.elem_begin = h->chunk_begin[c];
-        L.elem_count = h->chunk_begin[c + 1] - h->chunk_begin[c];
-        DGSW_CUDA(h, launch_stage_fp64(L, q));
-        DGSW_CUDA(h, cudaEventRecord(ev(st + 1, c), q));
-        level[c] = st + 1;
-        progress = true;
-        if (level[c] == 3 && copy_out) {
-          const int64_t off = h->chunk_begin[c] * per;
-          const int64_t n = (h->chunk_begin[c + 1] - h->chunk_begin[c]) * per;
-          DGSW_CUDA(h, cudaStreamWaitEvent(h->pipe_out, ev(3, c), 0));
-          DGSW_CUDA(h, cudaMemcpyAsync(host_u + off, h->state + off, n * sizeof(double),
-                                       cudaMemcpyDeviceToHost, h->pipe_out));
-        }
+  // the stream each launch went to; launches round-robin over the streams in
+  // issue order, waiting on the launches (or copies) they need that went
+  // elsewhere
+  std::vector<int> stream_of(3 * C, -1);
+  const std::vector<int>& order = h->pipe_order[copy_in ? 1 : 0];
+  for (size_t i = 0; i < order.size(); ++i) {
+    const int c = order[i] / 3, st = order[i] % 3, s = (int)(i % S);
+    cudaStream_t q = cs[s];
+    for (int d : h->chunk_deps[c]) {
+      if (st == 0) {
+        if (copy_in) DGSW_CUDA(h, cudaStreamWaitEvent(q, ev(0, d), 0));
+      } else {
+        const int src = stream_of[3 * d + st - 1];
+        if (src < 0) return fail(h, DGSW_ERR_ARGUMENT, "chunk schedule out of order");
+        if (src != s) DGSW_CUDA(h, cudaStreamWaitEvent(q, ev(st, d), 0));
       }
     }
+    StageLaunch L = base_launch(h);
+    L.mode = st == 0 ? kModeStageFirst : kModeStage;
+    L.ucur = in[st];
+    L.u0 = h->state;
+    L.unext = out[st];
+    L.coef = coef[st];
+    L.elem_begin = h->chunk_begin[c];
+    L.elem_count = h->chunk_begin[c + 1] - h->chunk_begin[c];
+    DGSW_CUDA(h, launch_stage_fp64(L, q));
+    DGSW_CUDA(h, cudaEventRecord(ev(st + 1, c), q));
+    stream_of[3 * c + st] = s;
+    if (st == 2 && copy_out) {
+      const int64_t off = h->chunk_begin[c] * per;
+      const int64_t n = (h->chunk_begin[c + 1] - h->chunk_begin[c]) * per;
+      DGSW_CUDA(h, cudaStreamWaitEvent(h->pipe_out, ev(3, c), 0));
+      DGSW_CUDA(h, cudaMemcpyAsync(host_u + off, h->state + off, n * sizeof(double),
+                                   cudaMemcpyDeviceToHost, h->pipe_out));
+    }
   }
-  for (int c = 0; c < C; ++c)
-    if (level[c] != 3) return fail(h, DGSW_ERR_ARGUMENT, "chunk schedule did not complete");
   // the handle's stream resumes after every chunk's last stage (and copy)
-  DGSW_CUDA(h, cudaEventRecord(done, h->pipe_aux));
-  DGSW_CUDA(h, cudaStreamWaitEvent(h->stream, done, 0));
+  for (int s = 1; s < S; ++s) {
+    DGSW_CUDA(h, cudaEventRecord(done, cs[s]));
+    DGSW_CUDA(h, cudaStreamWaitEvent(h->stream, done, 0));
+  }
   if (copy_out) {
     DGSW_CUDA(h, cudaEventRecord(done, h->pipe_out));
     DGSW_CUDA(h, cudaStreamWaitEvent(h->stream, done, 0));
@@ -1561,7 +1653,8 @@ int dgsw_destroy(DgswHandle h) {
     if (ev) cudaEventDestroy(ev);
   if (h->pipe_in) cudaStreamDestroy(h->pipe_in);
   if (h->pipe_out) cudaStreamDestroy(h->pipe_out);
-  if (h->pipe_aux) cudaStreamDestroy(h->pipe_aux);
+  for (cudaStream_t s : h->pipe_aux)
+    if (s) cudaStreamDestroy(s);
   if (h->dev_first) cudaFree(h->dev_first);
   if (h->ab_list) cudaFree(h->ab_list);
   if (h->ab_level) cudaFree(h->ab_level);

@@ -59,6 +59,13 @@ struct DgswHandle_ {
   float* op_hi = nullptr;
   float* op_lo = nullptr;
   int32_t* op_off = nullptr;
+  // FP64 path: per element face the index of its record within the
+  // element's class (-1: the neighbour has the same extent), and per class
+  // the records' faces (6 e + dir) and their exterior w (n^2 per record)
+  int32_t* pnc_face_idx = nullptr;
+  int32_t* pnc_rec[kMaxN + 1] = {};
+  int64_t pnc_count[kMaxN + 1] = {};
+  double* pnc_wext[kMaxN + 1] = {};
   // misfit objective and discrete adjoint (uniform FP64 path)
   EoTable eoT{};
   int n_samples = 0;
@@ -121,8 +128,10 @@ struct DgswHandle_ {
   std::vector<int> pipe_order[2];              // stage launches (3 c + stage) in issue
                                                // order, without / with copies in
   int pipe_streams = 4;                        // compute streams
-  int pipe_priority = 0;                       // PipePriority of the issue order
   int pipe_edge_chunks = 3;                    // thin chunks at each end of the order
+  double pipe_link_gbs = 160.0;                // host link rate of the model
+  double pipe_stage_ns = 0.0;                  // stage time per element of the model
+                                               // (0: the autotuner's, else per point)
   // graphs of pipelined steps on pinned host buffers: copies in and out, in
   // only, out only; each for one host pointer and dt
   cudaGraphExec_t pipe_graph[3] = {nullptr, nullptr, nullptr};
@@ -275,9 +284,56 @@ cudaError_t launch_general_classes(DgswHandle h, GeneralLaunch G) {
   return cudaSuccess;
 }
 
-// FP64 stage on the general path: out = alpha x + beta y + c L(x)
+// FP64 stage on the general path: out = alpha x + beta y + c L(x).  The
+// forms of the SSP-RK3 stages, the right-hand side and the volume terms run
+// the stage kernel of uniform meshes per extent class (stage_fp64.cu), after
+// the exterior w of the class's faces with neighbours of another extent is
+// mapped onto them (launch_pnc_faces); other forms run stage_general.cu.
 cudaError_t general_f64(DgswHandle h, const double* x, const double* y, double* out, double alpha,
                         double beta, double c, int boundary = 1) {
+  int mode = -1;
+  if (y) mode = boundary ? kModeStage : -1;
+  else if (alpha == 1.0 && beta == 0.0) mode = boundary ? kModeStageFirst : -1;
+  else if (alpha == 0.0 && beta == 0.0 && c == 1.0) mode = boundary ? kModeRhs : kModeVolume;
+  if (mode >= 0) {
+    for (int n = kMinN; n <= kMaxN; ++n) {
+      if (h->class_count[n] == 0) continue;
+      if (mode != kModeVolume && h->pnc_count[n] > 0) {
+        PncFaceLaunch P;
+        P.n = n;
+        P.n_rec = h->pnc_count[n];
+        P.rec_face = h->pnc_rec[n];
+        P.offset = h->offset;
+        P.elem_n = h->elem_n;
+        P.nbr = h->nbr;
+        P.op64 = h->op64;
+        P.op_off = h->op_off;
+        P.gamma2 = h->cfg.gamma2;
+        P.x = x;
+        P.wext = h->pnc_wext[n];
+        cudaError_t e = launch_pnc_faces(P, h->stream);
+        if (e != cudaSuccess) return e;
+      }
+      StageLaunch L = base_launch(h);
+      L.n = n;
+      L.mode = mode;
+      L.ucur = x;
+      L.u0 = y ? y : x;
+      L.unext = out;
+      L.coef = {beta, alpha, c};
+      L.eo = h->class_eo[n];
+      L.variant = 0;
+      L.face_idx = h->pnc_face_idx;
+      L.wext = h->pnc_wext[n];
+      L.tasks = h->class_tasks[n];
+      L.offset = h->offset;
+      L.elem_begin = 0;
+      L.elem_count = h->class_count[n];
+      cudaError_t e = launch_stage_fp64(L, h->stream);
+      if (e != cudaSuccess) return e;
+    }
+    return cudaSuccess;
+  }
   GeneralLaunch G = base_general(h);
   G.prec = kPrecF64;
   G.x64 = x;
@@ -915,23 +971,16 @@ bool pipelinable(DgswHandle h) {
          !h->filter_on && h->dom.n_elem >= 4096;
 }
 
-// Priorities of the list schedule among the launches whose inputs are
-// complete in the model
-enum PipePriority {
-  kPipeLatestStage = 0,  // the latest stage first (its chunk's copy-out starts sooner)
-  kPipeFirstStage = 1,   // first stages first (they use the copied data), then the latest
-  kPipeEarliest = 2,     // the launch whose inputs completed first
-};
-
 // The issue order of the 3 C stage launches (3 c + stage).  The model: the
 // copies in land one after another in element order at the host link's rate
 // (copy_s per element; all at time 0 without copies in), and the GPU runs one
 // launch at a time, a stage of chunk c taking its elements times stage_s.
 // Whenever the modelled GPU is free it takes, among the launches whose
-// inputs are complete, the first by the priority; ties go to the lower chunk.
+// inputs are complete, one of the latest stage (its chunk's copy-out can
+// start sooner); ties go to the lower chunk.
 std::vector<int> plan_pipe(const std::vector<int64_t>& begin,
                            const std::vector<std::vector<int>>& deps, bool copy_in,
-                           double copy_s, double stage_s, int priority) {
+                           double copy_s, double stage_s) {
   const int C = (int)begin.size() - 1;
   std::vector<double> t_in(C, 0.0), done(3 * C, 0.0);
   double t = 0.0;
@@ -941,7 +990,7 @@ std::vector<int> plan_pipe(const std::vector<int64_t>& begin,
   t = 0.0;
   while ((int)order.size() < 3 * C) {
     int best = -1;
-    double best_ready = 0.0, next_ready = INFINITY;
+    double next_ready = INFINITY;
     for (int c = 0; c < C; ++c) {
       const int st = level[c];
       if (st == 3) continue;
@@ -956,24 +1005,7 @@ std::vector<int> plan_pipe(const std::vector<int64_t>& begin,
         next_ready = std::min(next_ready, ready);
         continue;
       }
-      bool better = best < 0;
-      if (!better) {
-        const int bst = level[best];
-        switch (priority) {
-          case kPipeFirstStage:
-            better = (st == 0) != (bst == 0) ? st == 0 : st > bst;
-            break;
-          case kPipeEarliest:
-            better = ready < best_ready || (ready == best_ready && st > bst);
-            break;
-          default:
-            better = st > bst;
-        }
-      }
-      if (better) {
-        best = c;
-        best_ready = ready;
-      }
+      if (best < 0 || st > level[best]) best = c;
     }
     if (best < 0) {
       if (!(next_ready < INFINITY)) break;  // a dependency cycle: cannot happen
@@ -1031,21 +1063,26 @@ int pipe_init(DgswHandle h) {
     for (int d = 0; d < C; ++d)
       if (need[d]) h->chunk_deps[c].push_back(d);
   }
-  // the model's rates: the host link at 200 GB/s; a stage at the launch time
-  // the autotuner measured on the whole state, else 0.1 ns per point
+  // the model's rates: the host link at pipe_link_gbs (each direction's
+  // share with both busy; a faster link in the model issues launches that
+  // wait on copies too early, where they hold up their stream); a stage at
+  // pipe_stage_ns per element if set, else at the launch time the autotuner
+  // measured on the whole state, else at 0.1 ns per point
   const int64_t pts = (int64_t)h->dom.elem_n[0] * h->dom.elem_n[0] * h->dom.elem_n[0];
-  const double copy_s = kVars * pts * sizeof(double) / 200e9;
+  const double copy_s = kVars * pts * sizeof(double) / (h->pipe_link_gbs * 1e9);
   const double tuned_ms = h->tuned ? h->tune_ms[h->stage_variant] : 0.0;
-  const double stage_s = tuned_ms > 0.0 ? tuned_ms * 1e-3 / E : pts * 1e-10;
+  const double stage_s = h->pipe_stage_ns > 0.0 ? h->pipe_stage_ns * 1e-9
+                         : tuned_ms > 0.0       ? tuned_ms * 1e-3 / E
+                                                : pts * 1e-10;
+  const int n_streams = std::max(1, h->pipe_streams);
   for (int k = 0; k < 2; ++k) {
-    h->pipe_order[k] = plan_pipe(h->chunk_begin, h->chunk_deps, k == 1, copy_s, stage_s,
-                                 h->pipe_priority);
+    h->pipe_order[k] = plan_pipe(h->chunk_begin, h->chunk_deps, k == 1, copy_s, stage_s);
     if ((int)h->pipe_order[k].size() != 3 * C)
       return fail(h, DGSW_ERR_ARGUMENT, "chunk schedule did not complete");
   }
   DGSW_CUDA(h, cudaStreamCreateWithFlags(&h->pipe_in, cudaStreamNonBlocking));
   DGSW_CUDA(h, cudaStreamCreateWithFlags(&h->pipe_out, cudaStreamNonBlocking));
-  h->pipe_aux.assign(std::max(1, h->pipe_streams) - 1, nullptr);
+  h->pipe_aux.assign(n_streams - 1, nullptr);
   for (cudaStream_t& s : h->pipe_aux)
     DGSW_CUDA(h, cudaStreamCreateWithFlags(&s, cudaStreamNonBlocking));
   h->pipe_ev.assign(4 * C + 2, nullptr);
@@ -1081,9 +1118,8 @@ int pipelined_step(DgswHandle h, double* host_u, double dt, bool copy_in, bool c
                              {1.0 / 3.0, 2.0 / 3.0, (2.0 / 3.0) * dt}};
   const double* in[3] = {h->state, h->t1, h->t2};
   double* out[3] = {h->t1, h->t2, h->state};
-  // the stream each launch went to; launches round-robin over the streams in
-  // issue order, waiting on the launches (or copies) they need that went
-  // elsewhere
+  // the launches go round-robin to the streams in issue order; each waits on
+  // the launches (or copies) it needs that went to other streams
   std::vector<int> stream_of(3 * C, -1);
   const std::vector<int>& order = h->pipe_order[copy_in ? 1 : 0];
   for (size_t i = 0; i < order.size(); ++i) {
@@ -1609,6 +1645,24 @@ int dgsw_create(const DgswConfig* cfg, DgswHandle* out) {
     if ((e = upload(&h->op_hi, hi)) != cudaSuccess) return bail(e, "upload face operators");
     if ((e = upload(&h->op_lo, lo)) != cudaSuccess) return bail(e, "upload face operators");
     if ((e = upload(&h->op_off, op_off)) != cudaSuccess) return bail(e, "upload face operators");
+    // records of the faces whose neighbour has another extent
+    std::vector<int32_t> face_idx(6 * h->dom.n_elem, -1), recs[kMaxN + 1];
+    for (int64_t el = 0; el < h->dom.n_elem; ++el) {
+      const int n = h->dom.elem_n[el];
+      for (int dir = 0; dir < 6; ++dir)
+        if (h->dom.elem_n[h->dom.neighbor[6 * el + dir]] != n) {
+          face_idx[6 * el + dir] = (int32_t)recs[n].size();
+          recs[n].push_back((int32_t)(6 * el + dir));
+        }
+    }
+    if ((e = upload(&h->pnc_face_idx, face_idx)) != cudaSuccess) return bail(e, "upload face records");
+    for (int n = kMinN; n <= kMaxN; ++n) {
+      h->pnc_count[n] = (int64_t)recs[n].size();
+      if (recs[n].empty()) continue;
+      if ((e = upload(&h->pnc_rec[n], recs[n])) != cudaSuccess) return bail(e, "upload face records");
+      if ((e = cudaMalloc(&h->pnc_wext[n], recs[n].size() * n * n * sizeof(double))) != cudaSuccess)
+        return bail(e, "allocate face records");
+    }
   }
   if (cfg->time_stepper == DGSW_STEPPER_ADAMS_BASHFORTH) {
     int rc = adams_init(h, *cfg);
@@ -1660,8 +1714,12 @@ int dgsw_destroy(DgswHandle h) {
   if (h->ab_level) cudaFree(h->ab_level);
   if (h->ab_F) cudaFree(h->ab_F);
   if (h->ab_B) cudaFree(h->ab_B);
-  for (int n = 0; n <= kMaxN; ++n)
+  for (int n = 0; n <= kMaxN; ++n) {
     if (h->class_tasks[n]) cudaFree(h->class_tasks[n]);
+    if (h->pnc_rec[n]) cudaFree(h->pnc_rec[n]);
+    if (h->pnc_wext[n]) cudaFree(h->pnc_wext[n]);
+  }
+  if (h->pnc_face_idx) cudaFree(h->pnc_face_idx);
   if (h->op64) cudaFree(h->op64);
   if (h->op_hi) cudaFree(h->op_hi);
   if (h->op_lo) cudaFree(h->op_lo);

@@ -57,6 +57,11 @@ struct StageLaunch {
   // the end); neighbours are read wherever they are
   int64_t elem_begin = 0;
   int64_t elem_count = -1;
+  // elements of differing extents: the range runs over tasks (element
+  // indices of one extent class) and element e's values start at offset[e];
+  // faces whose neighbour has another extent have face_idx records
+  const int32_t* tasks = nullptr;
+  const int64_t* offset = nullptr;
 };
 
 cudaError_t launch_stage_fp64(const StageLaunch& L, cudaStream_t s);
@@ -164,6 +169,27 @@ struct GeneralLaunch {
 };
 
 cudaError_t launch_stage_general(const GeneralLaunch& L, cudaStream_t s);
+
+// Exterior w of the faces of one extent class n whose neighbour has another
+// extent (stage_general.cu): record r is face rec_face[r] = 6 e + dir of an
+// element e of the class; wext[r n^2 + a + n b] is the neighbour's
+// w = Pi - s Phi_d - gamma2 Psi mapped onto e's face points by
+// T = R_{mortar->face} P_{nbr->mortar} in both face dimensions.
+struct PncFaceLaunch {
+  int n = 0;
+  int64_t n_rec = 0;
+  const int32_t* rec_face = nullptr;
+  const int64_t* offset = nullptr;
+  const int32_t* elem_n = nullptr;
+  const int32_t* nbr = nullptr;
+  const double* op64 = nullptr;
+  const int32_t* op_off = nullptr;
+  double gamma2 = 0.0;
+  const double* x = nullptr;
+  double* wext = nullptr;
+};
+
+cudaError_t launch_pnc_faces(const PncFaceLaunch& L, cudaStream_t s);
 
 // Transposed operator (adjoint_fp64.cu): out = alpha X + beta Y + c L^T X,
 // out2 = alpha2 X + beta2 Y (optional, pointwise).

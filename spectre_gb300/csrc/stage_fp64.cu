@@ -59,19 +59,23 @@ __global__ void __launch_bounds__(N * N * EPB, MINB)
                       const int32_t* __restrict__ nbr, const double* __restrict__ jac,
                       int64_t n_elem, StageCoef coef, double gamma2, EoTable eo,
                       const int32_t* __restrict__ face_idx, const double* __restrict__ wext,
-                      int64_t elem_begin, int64_t elem_end) {
+                      int64_t elem_begin, int64_t elem_end, const int32_t* __restrict__ tasks,
+                      const int64_t* __restrict__ offset) {
   using S = Shape<N>;
   constexpr int NN = S::NN, NP = S::NP, TAB = S::TAB, h = S::h, H = S::H;
   constexpr bool kBoundary = MODE != kModeVolume;
   extern __shared__ double smem[];
   const int slot = threadIdx.x / NN;
   const int t = threadIdx.x - slot * NN;
-  const int64_t e = elem_begin + (int64_t)blockIdx.x * EPB + slot;
-  const bool active = e < elem_end;
+  // task i: element tasks[i] of a class list, or element i; its values at
+  // offset[e] (elements of differing extents) or e * 5 N^3
+  const int64_t i_task = elem_begin + (int64_t)blockIdx.x * EPB + slot;
+  const bool active = i_task < elem_end;
+  const int64_t e = tasks ? (active ? (int64_t)tasks[i_task] : 0) : i_task;
   double* F = smem + slot * S::SLOT;  // Pi, Phi_x, Phi_y, Phi_z of ucur
   double* Sacc = F + 4 * NP;         // running c * (dt Pi)
   double* T = Sacc + NP;             // three scaled split tables
-  const int64_t off = e * (int64_t)(kVars * NP);
+  const int64_t off = offset ? (active ? offset[e] : 0) : e * (int64_t)(kVars * NP);
   const double c = coef.c;
 
   double jd[3] = {0.0, 0.0, 0.0};
@@ -127,26 +131,36 @@ __global__ void __launch_bounds__(N * N * EPB, MINB)
         // neighbour's fields and this element's s).  Lifted with
         // -N(N-1)/2 |n| and scaled by c: G = -c N(N-1) J_d / 4.
         const double G = -0.25 * c * (double)(N * (N - 1)) * jd[d];
-        const int64_t nlo = (int64_t)nbr[6 * e + 2 * d] * (kVars * NP);
-        const int64_t nhi = (int64_t)nbr[6 * e + 2 * d + 1] * (kVars * NP);
-        const int64_t lo_pt = base + (N - 1) * stride;  // neighbour's upper face
-        const int64_t hi_pt = base;                     // neighbour's lower face
         double wi_lo = up[0] + uf[0];  // s = -1
-        double we_lo = ucur[nlo + NP + lo_pt] + ucur[nlo + (2 + d) * NP + lo_pt];
         double wi_hi = up[N - 1] - uf[N - 1];  // s = +1
-        double we_hi = ucur[nhi + NP + hi_pt] - ucur[nhi + (2 + d) * NP + hi_pt];
         if (gamma2 != 0.0) {
           wi_lo = fma(-gamma2, ucur[off + base], wi_lo);
-          we_lo = fma(-gamma2, ucur[nlo + lo_pt], we_lo);
           wi_hi = fma(-gamma2, ucur[off + base + (N - 1) * stride], wi_hi);
-          we_hi = fma(-gamma2, ucur[nhi + hi_pt], we_hi);
         }
-        if (face_idx) {
-          // 2:1 faces: the exterior w on this face, assembled from the
-          // mortars by refined_faces.cu (face point index = line index t)
-          const int32_t flo = face_idx[6 * e + 2 * d], fhi = face_idx[6 * e + 2 * d + 1];
-          if (flo >= 0) we_lo = wext[(int64_t)flo * NN + t];
-          if (fhi >= 0) we_hi = wext[(int64_t)fhi * NN + t];
+        // Faces with a record (2:1 faces of refined lattices, faces whose
+        // neighbour has another extent) take the exterior w on this face's
+        // points from it (face point index = line index t); the others read
+        // the neighbour's volume, which then has this element's extent.
+        const int32_t flo = face_idx ? face_idx[6 * e + 2 * d] : -1;
+        const int32_t fhi = face_idx ? face_idx[6 * e + 2 * d + 1] : -1;
+        double we_lo, we_hi;
+        if (flo >= 0) {
+          we_lo = wext[(int64_t)flo * NN + t];
+        } else {
+          const int32_t nb = nbr[6 * e + 2 * d];
+          const int64_t nlo = offset ? offset[nb] : (int64_t)nb * (kVars * NP);
+          const int64_t lo_pt = base + (N - 1) * stride;  // neighbour's upper face
+          we_lo = ucur[nlo + NP + lo_pt] + ucur[nlo + (2 + d) * NP + lo_pt];
+          if (gamma2 != 0.0) we_lo = fma(-gamma2, ucur[nlo + lo_pt], we_lo);
+        }
+        if (fhi >= 0) {
+          we_hi = wext[(int64_t)fhi * NN + t];
+        } else {
+          const int32_t nb = nbr[6 * e + 2 * d + 1];
+          const int64_t nhi = offset ? offset[nb] : (int64_t)nb * (kVars * NP);
+          const int64_t hi_pt = base;  // neighbour's lower face
+          we_hi = ucur[nhi + NP + hi_pt] - ucur[nhi + (2 + d) * NP + hi_pt];
+          if (gamma2 != 0.0) we_hi = fma(-gamma2, ucur[nhi + hi_pt], we_hi);
         }
         const double dw_lo = wi_lo - we_lo;
         const double dw_hi = wi_hi - we_hi;
@@ -246,7 +260,8 @@ cudaError_t launch_n(const StageLaunch& L, cudaStream_t s) {
   if (blocks <= 0) return cudaSuccess;
   k<<<(unsigned)blocks, N * N * EPB, smem, s>>>(L.ucur, L.u0, L.unext, L.nbr, L.jac, L.n_elem,
                                                  L.coef, L.gamma2, L.eo, L.face_idx, L.wext,
-                                                 L.elem_begin, L.elem_begin + count);
+                                                 L.elem_begin, L.elem_begin + count, L.tasks,
+                                                 L.offset);
   return cudaGetLastError();
 }
 

@@ -474,7 +474,85 @@ cudaError_t launch_general_n(const GeneralLaunch& L, cudaStream_t s) {
   }
 }
 
+
+// ---- exterior w of the faces whose neighbour has another extent ------------
+// For the FP64 path the stage kernel of uniform meshes (stage_fp64.cu) runs
+// each extent class over its task list and reads, on these faces, the
+// exterior w mapped onto its own face points from a record written here
+// before the stage: ext = (T x T) w_nbr, T = R_{mortar->face} P_{nbr->mortar}
+// (N x nn), w = Pi - s Phi_d - gamma2 Psi of the neighbour's face points with
+// this face's sign s.  One warp per record; w_nbr and the first sweep sit in
+// the warp's shared memory.
+constexpr int kPncWarps = 4;
+
+template <int N>
+__global__ void __launch_bounds__(32 * kPncWarps) pnc_faces_kernel(PncFaceLaunch L) {
+  constexpr int NN = N * N;
+  __shared__ double sw[kPncWarps][kNmax * kNmax];
+  __shared__ double s2[kPncWarps][kNmax * N];
+  const int warp = threadIdx.x / 32, lane = threadIdx.x % 32;
+  const int64_t r = (int64_t)blockIdx.x * kPncWarps + warp;
+  if (r >= L.n_rec) return;  // whole warps leave; only warp barriers follow
+  const int64_t face = L.rec_face[r];
+  const int64_t e = face / 6;
+  const int dir = (int)(face - 6 * e), d = dir >> 1;
+  const bool upper = dir & 1;
+  const int64_t nb = L.nbr[face];
+  const int nn = L.elem_n[nb];
+  const int64_t noff = L.offset[nb], np_n = (int64_t)nn * nn * nn;
+  const int nslice = upper ? 0 : nn - 1;
+  const double sgn = upper ? 1.0 : -1.0;
+  double* w = sw[warp];
+  double* t2 = s2[warp];
+  for (int q = lane; q < nn * nn; q += 32) {
+    const int v = face_point(nn, d, nslice, q % nn, q / nn);
+    double x = L.x[noff + np_n + v] - sgn * L.x[noff + (2 + d) * np_n + v];
+    if (L.gamma2 != 0.0) x = fma(-L.gamma2, L.x[noff + v], x);
+    w[q] = x;
+  }
+  __syncwarp();
+  const double* T = L.op64 + L.op_off[N * (kNmax + 1) + nn];  // N x nn, row-major
+  for (int q = lane; q < nn * N; q += 32) {
+    const int pp = q % nn, b = q / nn;
+    double acc = 0.0;
+    for (int k = 0; k < nn; ++k) acc = fma(T[b * nn + k], w[pp + nn * k], acc);
+    t2[q] = acc;
+  }
+  __syncwarp();
+  for (int q = lane; q < NN; q += 32) {
+    const int a = q % N, b = q / N;
+    double acc = 0.0;
+    for (int k = 0; k < nn; ++k) acc = fma(T[a * nn + k], t2[k + nn * b], acc);
+    L.wext[r * NN + q] = acc;
+  }
+}
+
+template <int N>
+cudaError_t launch_pnc_n(const PncFaceLaunch& L, cudaStream_t s) {
+  const int64_t blocks = (L.n_rec + kPncWarps - 1) / kPncWarps;
+  if (blocks <= 0) return cudaSuccess;
+  pnc_faces_kernel<N><<<(unsigned)blocks, 32 * kPncWarps, 0, s>>>(L);
+  return cudaGetLastError();
+}
+
 }  // namespace
+
+cudaError_t launch_pnc_faces(const PncFaceLaunch& L, cudaStream_t s) {
+  switch (L.n) {
+    case 2: return launch_pnc_n<2>(L, s);
+    case 3: return launch_pnc_n<3>(L, s);
+    case 4: return launch_pnc_n<4>(L, s);
+    case 5: return launch_pnc_n<5>(L, s);
+    case 6: return launch_pnc_n<6>(L, s);
+    case 7: return launch_pnc_n<7>(L, s);
+    case 8: return launch_pnc_n<8>(L, s);
+    case 9: return launch_pnc_n<9>(L, s);
+    case 10: return launch_pnc_n<10>(L, s);
+    case 11: return launch_pnc_n<11>(L, s);
+    case 12: return launch_pnc_n<12>(L, s);
+    default: return cudaErrorInvalidValue;
+  }
+}
 
 cudaError_t launch_stage_general(const GeneralLaunch& L, cudaStream_t s) {
   switch (L.n) {

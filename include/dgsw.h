@@ -39,7 +39,7 @@
 extern "C" {
 #endif
 
-#define DGSW_ABI_VERSION 5
+#define DGSW_ABI_VERSION 6
 
 typedef enum {
   DGSW_OK = 0,
@@ -366,6 +366,31 @@ int dgsw_observe_plane_wave_errors(DgswHandle h, const double* k, double t, doub
  * dgsw_exponential_filter_matrix: the 1D matrix, row-major (host only). */
 int dgsw_set_exponential_filter(DgswHandle h, double alpha, int half_power, int enable);
 int dgsw_exponential_filter_matrix(int n, double alpha, int half_power, double* F);
+
+/* ---- AMR projection of element data ----------------------------------------
+ * amr::projectors::ProjectVariables (ParallelAlgorithms/Amr/Projectors/
+ * Variables.hpp:25-99) on the device.  Per dimension d of target block k,
+ * child[3k + d] selects the 1D matrix from source extent src_extents[3k + d]
+ * to target extent dst_extents[3k + d]:
+ *   0  p-refinement (ChildSize::Full, Spectral::p_projection_matrices,
+ *      Projection.cpp:401-421): identity for equal extents, interpolation to
+ *      a finer extent, Legendre modal truncation to a coarser one;
+ *   1, 2  h-refinement to the lower / upper half
+ *      (projection_matrix_parent_to_child, Projection.cpp:291-372):
+ *      interpolation to the child's points mapped into that half; the target
+ *      needs at least as many points as the source.
+ * dgsw_amr_matrix: that matrix, dst x src row-major (host only).
+ * dgsw_amr_project_device: target block k (n_vars components, x fastest, as
+ * in Variables) is written at dev_out + out_offset[k] from source block
+ * src[k] at dev_in + in_offset[src[k]] (offsets in doubles, host arrays;
+ * device pointers for the data; dev_in != dev_out).  Uses h's device and
+ * stream and returns when the projection is done.  h-coarsening is not
+ * provided (the reference ERRORs on it too). */
+int dgsw_amr_matrix(int src_extent, int dst_extent, int child, double* M);
+int dgsw_amr_project_device(DgswHandle h, int n_vars, int64_t n_in, const int64_t* in_offset,
+                            const double* dev_in, int64_t n_out, const int32_t* src,
+                            const int32_t* src_extents, const int32_t* dst_extents,
+                            const int8_t* child, const int64_t* out_offset, double* dev_out);
 
 /* ---- discrete adjoint and the misfit objective -----------------------------
  * FP64, one brick of uniform extent, gamma2 = 0.  The step map of this path

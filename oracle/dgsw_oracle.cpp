@@ -2395,4 +2395,64 @@ int orc_shell_evolve(const OrcShell* s, double dt, int n_steps, double* u, int n
   return rc;
 }
 
+
+// The 1D matrix (dst x src) of amr::projectors::ProjectVariables along one
+// dimension (ParallelAlgorithms/Amr/Projectors/Variables.hpp:25-99):
+// child 0 is p_projection_matrices (Projection.cpp:401-421: identity, the
+// parent-to-child interpolation when the target is at least as fine, else
+// the child-to-parent modal truncation); child 1 / 2 is
+// projection_matrix_parent_to_child LowerHalf / UpperHalf
+// (Projection.cpp:291-372), interpolation to 0.5 (x -/+ 1), target at least
+// as fine as the source.
+int orc_amr_matrix(int src, int dst, int child, double* M) {
+  if (src < 2 || dst < 2 || src > kMaxN || dst > kMaxN || child < 0 || child > 2 || !M)
+    return -1;
+  if (child == 0) {
+    if (src == dst) {
+      for (int i = 0; i < dst; ++i)
+        for (int j = 0; j < src; ++j) M[i * src + j] = i == j ? 1.0 : 0.0;
+      return 0;
+    }
+    return dst > src ? orc_proj_face_to_mortar(src, dst, M) : orc_proj_mortar_to_face(dst, src, M);
+  }
+  if (dst < src) return -1;
+  const Spectral1d& sd = spectral(dst);
+  std::vector<double> t(dst);
+  for (int i = 0; i < dst; ++i) t[i] = 0.5 * (sd.x[i] + (child == 2 ? 1.0 : -1.0));
+  return orc_interp_matrix(src, dst, t.data(), M);
+}
+
+// Target block k = the source block src[k] with the three 1D matrices
+// applied as apply_matrices does (x fastest), n_vars components per block.
+int orc_amr_project(int n_vars, int64_t n_out, const int32_t* src, const int32_t* src_ext,
+                    const int32_t* dst_ext, const int8_t* child, const double* in,
+                    const int64_t* in_off, double* out, const int64_t* out_off) {
+  for (int64_t k = 0; k < n_out; ++k) {
+    const int* se = src_ext + 3 * k;
+    const int* de = dst_ext + 3 * k;
+    std::vector<double> Mx(de[0] * se[0]), My(de[1] * se[1]), Mz(de[2] * se[2]);
+    if (orc_amr_matrix(se[0], de[0], child[3 * k], Mx.data()) ||
+        orc_amr_matrix(se[1], de[1], child[3 * k + 1], My.data()) ||
+        orc_amr_matrix(se[2], de[2], child[3 * k + 2], Mz.data()))
+      return -1;
+    const int64_t s_np = (int64_t)se[0] * se[1] * se[2], d_np = (int64_t)de[0] * de[1] * de[2];
+    for (int v = 0; v < n_vars; ++v) {
+      const double* u = in + in_off[src[k]] + v * s_np;
+      double* w = out + out_off[k] + v * d_np;
+      for (int c = 0; c < de[2]; ++c)
+        for (int b = 0; b < de[1]; ++b)
+          for (int a = 0; a < de[0]; ++a) {
+            double acc = 0.0;
+            for (int r = 0; r < se[2]; ++r)
+              for (int q = 0; q < se[1]; ++q)
+                for (int p = 0; p < se[0]; ++p)
+                  acc += Mz[c * se[2] + r] * My[b * se[1] + q] * Mx[a * se[0] + p] *
+                         u[p + se[0] * (q + se[1] * r)];
+            w[a + de[0] * (b + de[1] * c)] = acc;
+          }
+    }
+  }
+  return 0;
+}
+
 }  // extern "C"

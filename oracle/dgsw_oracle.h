@@ -51,6 +51,13 @@ int orc_interp_matrix(int n, int m, const double* targets, double* M);
 int orc_proj_face_to_mortar(int ne, int nm, double* P);
 /* mortar (nm pts) -> face (ne <= nm pts): P[i*nm + j], i < ne (modal truncation) */
 int orc_proj_mortar_to_face(int ne, int nm, double* P);
+/* amr::projectors::ProjectVariables: the 1D matrix (dst x src) for child 0
+ * (p-projection), 1 (LowerHalf) or 2 (UpperHalf), and the projection of
+ * n_out target blocks from source blocks src[k] (extents 3 per block) */
+int orc_amr_matrix(int src, int dst, int child, double* M);
+int orc_amr_project(int n_vars, int64_t n_out, const int32_t* src, const int32_t* src_ext,
+                    const int32_t* dst_ext, const int8_t* child, const double* in,
+                    const int64_t* in_off, double* out, const int64_t* out_off);
 
 /* ---------------- domain (a13, a14) ---------------- */
 /* One periodic brick evolution: [lo, hi]^3 with n[d] elements along axis d.

@@ -74,6 +74,7 @@ def lib():
             "orc_refined_index_maps": [P, P, P, P], "orc_refined_coords": [P, I, P],
             "orc_refined_rhs": [P, I, D, P, P, I], "orc_refined_evolve": [P, I, D, D, I, P, I],
             "orc_proj_half": [I, I, P, P],
+            "orc_amr_matrix": [I, I, I, P], "orc_amr_project": [I, I64, P, P, P, P, P, P, P, P],
             "orc_variable_coefficients": [I, P, D, D, P],
             "orc_adams_coefficients": [I, P, I64, I64, D, I64, P],
             "orc_lts_coefficients": [I, P, P, I, P, P, I64, I64, D, I64, I, I, I, I, P, P, P],
@@ -504,6 +505,30 @@ def proj_half(n, upper):
     P, R = np.zeros((n, n)), np.zeros((n, n))
     _check(lib().orc_proj_half(n, int(upper), _p(P), _p(R)))
     return P, R
+
+
+def amr_matrix(src, dst, child):
+    """The dst x src 1D matrix of ProjectVariables: child 0 (p-projection),
+    1 (LowerHalf) or 2 (UpperHalf)."""
+    M = np.zeros((dst, src))
+    _check(lib().orc_amr_matrix(int(src), int(dst), int(child), _p(M)))
+    return M
+
+
+def amr_project(n_vars, src, src_ext, dst_ext, child, u_in, in_off):
+    """Target blocks from source blocks (ProjectVariables); returns the
+    concatenated targets and their offsets."""
+    src = np.ascontiguousarray(src, dtype=np.int32)
+    src_ext = np.ascontiguousarray(src_ext, dtype=np.int32).reshape(-1, 3)
+    dst_ext = np.ascontiguousarray(dst_ext, dtype=np.int32).reshape(-1, 3)
+    child = np.ascontiguousarray(child, dtype=np.int8).reshape(-1, 3)
+    sizes = n_vars * np.prod(dst_ext.astype(np.int64), axis=1)
+    out_off = np.concatenate([[0], np.cumsum(sizes)[:-1]]).astype(np.int64)
+    out = np.zeros(int(sizes.sum()))
+    _check(lib().orc_amr_project(int(n_vars), len(src), _p(src), _p(src_ext), _p(dst_ext),
+                                 _p(child), _p(_c(u_in)), _p(np.ascontiguousarray(in_off, dtype=np.int64)),
+                                 _p(out), _p(out_off)))
+    return out, out_off
 
 
 # ---------------- Adams-Bashforth and local time stepping ----------------

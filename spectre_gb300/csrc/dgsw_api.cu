@@ -11,6 +11,8 @@
 #include <cstdlib>
 #include <cstring>
 #include <map>
+#include <tuple>
+#include <type_traits>
 #include <mutex>
 #include <new>
 #include <algorithm>
@@ -1326,6 +1328,84 @@ int dgsw_refined_mortars(const DgswConfig* cfg, int32_t* slots, int32_t* sizes) 
   if (!build_refined_domain(*cfg, &dom, &rm, &err)) return fail(nullptr, DGSW_ERR_ARGUMENT, err);
   if (slots) std::memcpy(slots, rm.slots.data(), rm.slots.size() * sizeof(int32_t));
   if (sizes) std::memcpy(sizes, rm.sizes.data(), rm.sizes.size() * sizeof(int32_t));
+  return DGSW_OK;
+}
+
+int dgsw_amr_matrix(int src_extent, int dst_extent, int child, double* M) {
+  if (!M) return fail(nullptr, DGSW_ERR_ARGUMENT, "null argument");
+  if (!amr_matrix(src_extent, dst_extent, child, M))
+    return fail(nullptr, DGSW_ERR_ARGUMENT,
+                "need extents in [2, 12], child 0 (Full), 1 (LowerHalf) or 2 (UpperHalf), and "
+                "a half-interval target at least as fine as its source");
+  return DGSW_OK;
+}
+
+int dgsw_amr_project_device(DgswHandle h, int n_vars, int64_t n_in, const int64_t* in_offset,
+                            const double* dev_in, int64_t n_out, const int32_t* src,
+                            const int32_t* src_extents, const int32_t* dst_extents,
+                            const int8_t* child, const int64_t* out_offset, double* dev_out) {
+  if (!h) return fail(nullptr, DGSW_ERR_ARGUMENT, "null handle");
+  if (n_out < 0 || n_vars < 1 || n_in < 1) return fail(h, DGSW_ERR_ARGUMENT, "bad sizes");
+  if (n_out == 0) return DGSW_OK;
+  if (!in_offset || !dev_in || !src || !src_extents || !dst_extents || !child || !out_offset ||
+      !dev_out)
+    return fail(h, DGSW_ERR_ARGUMENT, "null argument");
+  if (dev_in == dev_out) return fail(h, DGSW_ERR_ARGUMENT, "input and output must differ");
+  if (n_out > INT32_MAX) return fail(h, DGSW_ERR_ARGUMENT, "too many target blocks");
+  // one matrix per distinct (source extent, target extent, child size)
+  std::map<std::tuple<int, int, int>, int64_t> mat_at;
+  std::vector<double> mats;
+  std::vector<int64_t> mat_off(3 * n_out);
+  double M[kMaxN * kMaxN];
+  for (int64_t k = 0; k < n_out; ++k) {
+    if (src[k] < 0 || src[k] >= n_in)
+      return fail(h, DGSW_ERR_ARGUMENT, "source block index out of range");
+    for (int d = 0; d < 3; ++d) {
+      const int se = src_extents[3 * k + d], de = dst_extents[3 * k + d], c = child[3 * k + d];
+      const auto key = std::make_tuple(se, de, c);
+      auto it = mat_at.find(key);
+      if (it == mat_at.end()) {
+        if (!amr_matrix(se, de, c, M))
+          return fail(h, DGSW_ERR_ARGUMENT,
+                      "bad projection: extents in [2, 12], child 0, 1 or 2, and a half-interval "
+                      "target at least as fine as its source");
+        it = mat_at.emplace(key, (int64_t)mats.size()).first;
+        mats.insert(mats.end(), M, M + de * se);
+      }
+      mat_off[3 * k + d] = it->second;
+    }
+  }
+  if (int rc = select_device(h)) return rc;
+  // the tables live for this call only
+  struct Temp {
+    std::vector<void*> p;
+    ~Temp() {
+      for (void* q : p) cudaFree(q);
+    }
+  } tmp;
+  AmrLaunch L;
+  L.n_vars = n_vars;
+  L.n_out = n_out;
+  auto up = [&](auto** dst, const auto* host, size_t n) {
+    using T = typename std::remove_const<typename std::remove_pointer<decltype(host)>::type>::type;
+    std::vector<T> v(host, host + n);
+    T* d = nullptr;
+    const cudaError_t e = upload(&d, v);
+    if (d) tmp.p.push_back(d);
+    *dst = d;
+    return e;
+  };
+  DGSW_CUDA(h, up(&L.src, src, n_out));
+  DGSW_CUDA(h, up(&L.src_ext, src_extents, 3 * n_out));
+  DGSW_CUDA(h, up(&L.dst_ext, dst_extents, 3 * n_out));
+  DGSW_CUDA(h, up(&L.mat_off, mat_off.data(), mat_off.size()));
+  DGSW_CUDA(h, up(&L.mats, mats.data(), mats.size()));
+  DGSW_CUDA(h, up(&L.in_off, in_offset, n_in));
+  DGSW_CUDA(h, up(&L.out_off, out_offset, n_out));
+  L.in = dev_in;
+  L.out = dev_out;
+  DGSW_CUDA(h, launch_amr_project(L, h->stream));
+  DGSW_CUDA(h, cudaStreamSynchronize(h->stream));
   return DGSW_OK;
 }
 

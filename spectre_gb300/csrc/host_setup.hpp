@@ -120,6 +120,11 @@ bool build_refined_domain(const DgswConfig& cfg, Domain* dom, RefinedMaps* rm,
 // Half-interval projections on n LGL points (n x n, row-major), parent ->
 // child interpolation and child -> parent L2 restriction, Projection.cpp.
 bool half_projections(int n, int upper, double* parent_to_child, double* child_to_parent);
+// The 1D matrix (dst x src, row-major) of amr::projectors::ProjectVariables
+// along one dimension: child 0 (ChildSize::Full) is p-projection (identity,
+// interpolation to a finer or truncation to a coarser extent), child 1 / 2
+// (LowerHalf / UpperHalf) interpolation into that half, dst >= src (amr.cu).
+bool amr_matrix(int src, int dst, int child, double* M);
 
 // Validates a configuration and builds every host-side map.  On failure
 // returns false with a message in *err.

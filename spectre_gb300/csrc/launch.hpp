@@ -191,6 +191,26 @@ struct PncFaceLaunch {
 
 cudaError_t launch_pnc_faces(const PncFaceLaunch& L, cudaStream_t s);
 
+// AMR projection of element data (amr.cu): target block k (n_vars
+// components, x fastest, at out + out_off[k]) from source block src[k] (at
+// in + in_off[src[k]]) with extents src_ext[3k..] -> dst_ext[3k..] by the
+// dst x src matrices at mats + mat_off[3k + d].
+struct AmrLaunch {
+  int n_vars = 0;
+  int64_t n_out = 0;
+  const int32_t* src = nullptr;
+  const int32_t* src_ext = nullptr;
+  const int32_t* dst_ext = nullptr;
+  const int64_t* mat_off = nullptr;
+  const double* mats = nullptr;
+  const double* in = nullptr;
+  const int64_t* in_off = nullptr;
+  double* out = nullptr;
+  const int64_t* out_off = nullptr;
+};
+
+cudaError_t launch_amr_project(const AmrLaunch& L, cudaStream_t s);
+
 // Transposed operator (adjoint_fp64.cu): out = alpha X + beta Y + c L^T X,
 // out2 = alpha2 X + beta2 Y (optional, pointwise).
 struct AdjointLaunch {

@@ -137,6 +137,8 @@ _SIGNATURES = {
     "dgsw_gauss_spectral": (_I, [_I, _P, _P, _P, _P, _P, _P, _P]),
     "dgsw_refined_mortars": (_I, [ctypes.POINTER(DgswConfig), _P, _P]),
     "dgsw_half_projections": (_I, [_I, _I, _P, _P]),
+    "dgsw_amr_matrix": (_I, [_I, _I, _I, _P]),
+    "dgsw_amr_project_device": (_I, [_P, _I, _I64, _P, _P, _I64, _P, _P, _P, _P, _P, _P]),
     "dgsw_adjoint_rhs_device": (_I, [_P, _P, _P]),
     "dgsw_set_samples": (_I, [_P, _I, _P]),
     "dgsw_sample_psi": (_I, [_P, _P]),
@@ -368,6 +370,45 @@ def half_projections(n: int, upper: bool):
     P, R = np.zeros((n, n)), np.zeros((n, n))
     _check(lib().dgsw_half_projections(n, int(upper), _ptr(P), _ptr(R)))
     return P, R
+
+
+AMR_FULL, AMR_LOWER_HALF, AMR_UPPER_HALF = 0, 1, 2
+
+
+def amr_matrix(src_extent: int, dst_extent: int, child: int = AMR_FULL):
+    """The dst x src 1D matrix of amr::projectors::ProjectVariables along one
+    dimension (host only): AMR_FULL p-projection, AMR_LOWER_HALF /
+    AMR_UPPER_HALF h-refinement into that half."""
+    M = np.zeros((int(dst_extent), int(src_extent)))
+    _check(lib().dgsw_amr_matrix(int(src_extent), int(dst_extent), int(child), _ptr(M)))
+    return M
+
+
+def amr_project(owner, n_vars, u_in, in_offset, src, src_extents, dst_extents, child):
+    """ProjectVariables on the device through dgsw_amr_project_device.
+
+    owner: any open DgEvolution (its device and stream are used).  u_in: a
+    CUDA tensor of float64 holding the source blocks at in_offset (doubles).
+    src: source block of each target; src_extents / dst_extents / child:
+    3 per target.  Returns (CUDA float64 tensor of the targets, concatenated
+    in order, and their offsets)."""
+    import torch
+    src = np.ascontiguousarray(src, dtype=np.int32)
+    se = np.ascontiguousarray(src_extents, dtype=np.int32).reshape(-1, 3)
+    de = np.ascontiguousarray(dst_extents, dtype=np.int32).reshape(-1, 3)
+    ch = np.ascontiguousarray(child, dtype=np.int8).reshape(-1, 3)
+    ino = np.ascontiguousarray(in_offset, dtype=np.int64)
+    if not (len(src) == len(se) == len(de) == len(ch)):
+        raise ValueError("one source index and three extents / child sizes per target")
+    sizes = int(n_vars) * np.prod(de.astype(np.int64), axis=1)
+    out_off = np.concatenate([[0], np.cumsum(sizes)[:-1]]).astype(np.int64)
+    assert u_in.is_cuda and u_in.dtype == torch.float64 and u_in.is_contiguous()
+    out = torch.empty(int(sizes.sum()), dtype=torch.float64, device=u_in.device)
+    _check(lib().dgsw_amr_project_device(owner.handle, int(n_vars), len(ino), _ptr(ino),
+                                          u_in.data_ptr(), len(src), _ptr(src), _ptr(se),
+                                          _ptr(de), _ptr(ch), _ptr(out_off), out.data_ptr()),
+           owner.handle)
+    return out, out_off
 
 
 def cfl_steps(bricks, points, safety_factor=1.0, time_stepper="rk3_hesthaven_ssp", order=3,

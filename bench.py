@@ -72,7 +72,11 @@ def load_peaks():
 
 
 class ClockSampler:
-    """nvidia-smi clocks and throttle reasons sampled during the timed region."""
+    """nvidia-smi clocks and throttle reasons sampled during the timed region.
+
+    Every line is stamped when it arrives; with begin() / end() marking the
+    timed region, only the lines stamped inside it count (all lines when
+    none is)."""
 
     FIELDS = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
               "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
@@ -83,12 +87,13 @@ class ClockSampler:
         self.proc = None
         self.lines = []
         self.thread = None
+        self.window = [None, None]
 
     def start(self):
         try:
             self.proc = subprocess.Popen(
                 ["nvidia-smi", "-i", str(self.device_index), "--query-gpu=" + self.FIELDS,
-                 "--format=csv,noheader,nounits", "-lms", "200"],
+                 "--format=csv,noheader,nounits", "-lms", "100"],
                 stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
         except Exception:
             self.proc = None
@@ -98,7 +103,13 @@ class ClockSampler:
 
     def _read(self):
         for line in self.proc.stdout:
-            self.lines.append(line.strip())
+            self.lines.append((time.perf_counter(), line.strip()))
+
+    def begin(self):
+        self.window[0] = time.perf_counter()
+
+    def end(self):
+        self.window[1] = time.perf_counter()
 
     def stop(self):
         if self.proc is None:
@@ -112,7 +123,13 @@ class ClockSampler:
             self.thread.join(timeout=2)
         sm, smax, reasons = [], None, set()
         names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
-        for ln in self.lines:
+        lo, hi = self.window
+        lines = [ln for t, ln in self.lines
+                 if lo is not None and hi is not None and lo <= t <= hi]
+        in_window = bool(lines)
+        if not lines:
+            lines = [ln for _, ln in self.lines]
+        for ln in lines:
             parts = [p.strip() for p in ln.split(",")]
             if len(parts) < 9:
                 continue
@@ -127,7 +144,8 @@ class ClockSampler:
         if not sm:
             return None
         return {"sm_mhz": float(np.median(sm)), "sm_max_mhz": smax,
-                "reasons": sorted(reasons), "samples": len(sm)}
+                "reasons": sorted(reasons), "samples": len(sm),
+                "window": "timed region" if in_window else "whole sampler run"}
 
 
 def dist_env():
@@ -243,11 +261,15 @@ def time_path(args, precision, dev, rank, ws, sample_clocks):
     torch.cuda.synchronize()
     e0 = torch.cuda.Event(enable_timing=True)
     e1 = torch.cuda.Event(enable_timing=True)
+    if sampler:
+        sampler.begin()
     e0.record(stream)
     ev.step(args.steps, DT, sync=False)
     e1.record(stream)
     e1.synchronize()
     torch.cuda.synchronize()
+    if sampler:
+        sampler.end()
     ms = e0.elapsed_time(e1)
     if ws > 1:
         ms = max_over_ranks(ms, ws)
@@ -672,7 +694,7 @@ def run_ours(args):
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
-    ap.add_argument("--steps", type=int, default=30)
+    ap.add_argument("--steps", type=int, default=200)
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
     ap.add_argument("--no-cpu-baseline", action="store_true")

@@ -5,6 +5,7 @@
 #pragma once
 
 #include <cstdint>
+#include <type_traits>
 
 #include "common.cuh"
 
@@ -21,12 +22,17 @@ struct Eo {
 
 // (scaled D) u along one line with the even/odd split, FP64.  tab holds the
 // scaled A (H x h), B (H x h) and M (H) tables of an EoTable.
-template <int N, typename T>
+// kReload reads every table entry from shared memory where it is used
+// (volatile loads), instead of letting the compiler keep the table in
+// registers across calls: fewer registers per thread for a few more shared
+// loads, which the FP64 pipe's rate hides.
+template <int N, typename T, bool kReload = false>
 __device__ __forceinline__ void eo_line(const T (&u)[N], T (&out)[N], const T* __restrict__ tab) {
   constexpr int h = Eo<N>::h, H = Eo<N>::H, odd = Eo<N>::odd;
-  const T* A = tab;
-  const T* B = tab + H * h;
-  const T* M = tab + 2 * H * h;
+  using Tab = typename std::conditional<kReload, const volatile T*, const T*>::type;
+  const Tab A = tab;
+  const Tab B = tab + H * h;
+  const Tab M = tab + 2 * H * h;
   T e[h], o[h];
 #pragma unroll
   for (int j = 0; j < h; ++j) {

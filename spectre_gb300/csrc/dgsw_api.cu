@@ -1028,7 +1028,7 @@ std::vector<int> plan_pipe(const std::vector<int64_t>& begin,
 int pipe_init(DgswHandle h) {
   if (h->pipe_in) return DGSW_OK;
   const int64_t E = h->dom.n_elem;
-  // Chunks of two waves of the stage kernel in the middle of the element
+  // Chunks of whole waves of the stage kernel in the middle of the element
   // order and thin ones at both ends.  On a periodic brick the chunks are
   // slabs on a ring, and the last chunk copied in holds back the stage
   // chains of the chunks around it (the last few and the first few), which
@@ -1042,8 +1042,12 @@ int pipe_init(DgswHandle h) {
       const int64_t d = std::llabs(h->dom.neighbor[6 * e + f] - e);
       reach = std::max(reach, std::min(d, E - d));
     }
+  // The middle chunks are the fewest whole waves that span the neighbour
+  // reach (at 32^3 x 8^3: 2 x 912 elements with 6 resident blocks per SM,
+  // 1 x 1216 with 8).
   const int64_t wave = stage_fp64_wave_elements(h->dom.elem_n[0], h->stage_variant);
-  const int64_t thick = std::max<int64_t>(512, wave > 0 && E >= 24 * wave ? 2 * wave : E / 16);
+  const int64_t thick = std::max<int64_t>(
+      512, wave > 0 && E >= 24 * wave ? wave * ((reach + wave - 1) / wave) : E / 16);
   const int64_t thin = std::min(thick, std::max<int64_t>(256, reach));
   const int n_edge = std::max(1, h->pipe_edge_chunks);
   h->chunk_begin.assign(1, 0);

@@ -50,7 +50,7 @@ struct Shape {
 template <int N>
 __device__ __forceinline__ void eo_line(const double (&u)[N], double (&out)[N],
                                         const double* __restrict__ tab) {
-  dev::eo_line<N, double>(u, out, tab);
+  dev::eo_line<N, double, true>(u, out, tab);  // table reloaded: registers for occupancy
 }
 
 template <int N, int EPB, int MINB, int MODE>
@@ -242,7 +242,7 @@ constexpr int elems_per_block() {
 }
 template <int N, int V>
 constexpr int min_blocks() {
-  constexpr int m = N <= 5 ? 2 : (N == 8 ? 3 : 1);
+  constexpr int m = N <= 5 ? 2 : (N == 8 ? 3 : (N == 9 || N == 10 ? 2 : 1));
   return V == 0 ? m : (2 * m > 8 ? 8 : 2 * m);
 }
 

@@ -176,6 +176,34 @@ def replica_throughput(points_per_rank, rhs_per_step, steps, seconds_per_rank, w
     return points_per_rank * rhs_per_step * steps * ws / slowest, slowest
 
 
+def host_link_rates(host, dev):
+    """GB/s of whole-state copies between the pinned host buffer and the
+    device, measured beside the e2e run: host->device alone, device->host
+    alone, and both at once on two streams (each the mean of 3 copies).  The
+    host link is shared with whatever else the host runs, so the e2e figure
+    moves with it."""
+    import torch
+    d = torch.empty(host.numel(), dtype=host.dtype, device=dev)
+    nbytes = host.numel() * host.element_size()
+    s1, s2 = torch.cuda.Stream(dev), torch.cuda.Stream(dev)
+    out = {}
+    for name in ("h2d", "d2h", "both"):
+        torch.cuda.synchronize(dev)
+        t0 = time.perf_counter()
+        for _ in range(3):
+            if name in ("h2d", "both"):
+                with torch.cuda.stream(s1):
+                    d.copy_(host, non_blocking=True)
+            if name in ("d2h", "both"):
+                with torch.cuda.stream(s2):
+                    host.copy_(d, non_blocking=True)
+        torch.cuda.synchronize(dev)
+        moved = 3 * nbytes * (2 if name == "both" else 1)
+        out[name] = moved / (time.perf_counter() - t0) / 1e9
+    del d
+    return out
+
+
 def cpu_threads():
     try:
         return len(os.sched_getaffinity(0))
@@ -606,7 +634,8 @@ def run_ours(args):
     e2e = {"value": e2e_value, "unit": UNIT,
            "h2d_bytes_per_step": ev.state_size * 8, "d2h_bytes_per_step": ev.state_size * 8,
            "steps": k2, "call": "dgsw_step_host(h, pinned host state, 1, dt) per step",
-           "ms_per_step": el / k2 * 1e3}
+           "ms_per_step": el / k2 * 1e3,
+           "host_link_gbs": host_link_rates(host, dev)}
     ev.close()
 
     mixed = None

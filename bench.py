@@ -48,11 +48,11 @@ BYTES_PER_POINT_LAUNCH = (80.0 + 120.0 + 120.0) / 3.0
 # writes u (20 + 20 + 40 + 40 B).
 MIXED_BYTES_PER_POINT_LAUNCH = (60.0 + 40.0 + 120.0) / 3.0
 # DRAM traffic (read + write) per grid point per stage launch measured by ncu
-# on the 20^3 x 8^3 case (4,096,000 points): 287.4, 467.5 and 452.1 MB for the
+# on the 20^3 x 8^3 case (4,096,000 points): 287.7, 470.1 and 452.9 MB for the
 # three FP64 stages; 180.5 + 120.3 + 204.1 + 355.4 MB for the three mixed
 # stages and the FP64 accumulate, per three stage launches.
 # Traffic grows with the points, so the 32^3 figure is this times its points.
-FP64_TRAFFIC_PER_POINT_LAUNCH = 1207.0e6 / 3 / 4096000
+FP64_TRAFFIC_PER_POINT_LAUNCH = 1210.7e6 / 3 / 4096000
 MIXED_TRAFFIC_PER_POINT_LAUNCH = 860.3e6 / 3 / 4096000
 # FP64 pipe instructions per point per stage of the plain kernel at N = 8
 # (even/odd contraction 6 per derivative x 6, dt Pi sum 2, RK update 5-11,

@@ -40,6 +40,8 @@ N_PTS = 8
 DT = 2e-4
 # timed steps of the CPU baseline on the workload itself (about 10 s on 16 cores)
 CPU_SAMPLE_STEPS = 10
+# timed steps of the reference arm at most (the rest of --steps is not run)
+REFERENCE_MAX_STEPS = 20
 # Compulsory HBM bytes per grid point per stage launch.  Plain FP64: read
 # ucur (40 B) + write unext (40 B) + read u0 on stages 2 and 3 (40 B).
 BYTES_PER_POINT_LAUNCH = (80.0 + 120.0 + 120.0) / 3.0
@@ -238,7 +240,9 @@ def run_reference(args):
     if rank != 0:
         return 0
     threads = cpu_threads()
-    steps = max(1, args.steps)
+    # a bounded sample: one SSP-RK3 step of the workload takes about 1 s on 16
+    # host cores, so at most REFERENCE_MAX_STEPS of the requested steps run
+    steps = max(1, min(args.steps, REFERENCE_MAX_STEPS))
     value, el, points = cpu_reference_run(steps, min(args.warmup, 1), threads)
     sample = ("FP64 C++ restatement of the reference (oracle/) on the workload itself, "
               "32^3 elements x 8^3 LGL points (%d points), %d SSP-RK3 steps, %d threads, %.1f s"

@@ -124,6 +124,8 @@ struct DgswHandle_ {
   // steps of a host-resident state with the copies overlapped (dgsw_step_host)
   cudaStream_t pipe_in = nullptr, pipe_out = nullptr;
   std::vector<cudaStream_t> pipe_aux;          // compute streams besides the handle's
+  cudaStream_t pipe_seam = nullptr;            // the launches the last copy-in holds back
+  std::vector<char> pipe_seam_set;             // per stage launch (3 c + stage)
   std::vector<cudaEvent_t> pipe_ev;            // per chunk: in, stage 1, 2, 3; plus 2
   std::vector<int64_t> chunk_begin;            // chunks + 1 element offsets
   std::vector<std::vector<int>> chunk_deps;    // chunks holding a chunk's neighbours
@@ -1089,6 +1091,19 @@ int pipe_init(DgswHandle h) {
     if ((int)h->pipe_order[k].size() != 3 * C)
       return fail(h, DGSW_ERR_ARGUMENT, "chunk schedule did not complete");
   }
+  // The launches that need the last chunk copied in, directly or through an
+  // earlier stage (the ring's seam), go to a stream of their own with the
+  // highest priority: they wait there for the copy without holding up other
+  // launches, and no other launch needs them.  They start as soon as the
+  // copy lands.
+  h->pipe_seam_set.assign(3 * C, 0);
+  for (int st = 0; st < 3; ++st)
+    for (int c = 0; c < C; ++c)
+      for (int d : h->chunk_deps[c])
+        if (st == 0 ? d == C - 1 : h->pipe_seam_set[3 * d + st - 1] != 0) h->pipe_seam_set[3 * c + st] = 1;
+  int least = 0, greatest = 0;
+  DGSW_CUDA(h, cudaDeviceGetStreamPriorityRange(&least, &greatest));
+  DGSW_CUDA(h, cudaStreamCreateWithPriority(&h->pipe_seam, cudaStreamNonBlocking, greatest));
   DGSW_CUDA(h, cudaStreamCreateWithFlags(&h->pipe_in, cudaStreamNonBlocking));
   DGSW_CUDA(h, cudaStreamCreateWithFlags(&h->pipe_out, cudaStreamNonBlocking));
   h->pipe_aux.assign(n_streams - 1, nullptr);
@@ -1110,9 +1125,10 @@ int pipelined_step(DgswHandle h, double* host_u, double dt, bool copy_in, bool c
   std::vector<cudaStream_t> cs(1, h->stream);
   cs.insert(cs.end(), h->pipe_aux.begin(), h->pipe_aux.end());
   const int S = (int)cs.size();
+  cs.push_back(h->pipe_seam);  // index S: the seam's launches when copying in
   // everything already queued on the handle's stream comes first
   DGSW_CUDA(h, cudaEventRecord(start, h->stream));
-  for (int s = 1; s < S; ++s) DGSW_CUDA(h, cudaStreamWaitEvent(cs[s], start, 0));
+  for (int s = 1; s <= S; ++s) DGSW_CUDA(h, cudaStreamWaitEvent(cs[s], start, 0));
   if (copy_in) {
     DGSW_CUDA(h, cudaStreamWaitEvent(h->pipe_in, start, 0));
     for (int c = 0; c < C; ++c) {
@@ -1127,12 +1143,15 @@ int pipelined_step(DgswHandle h, double* host_u, double dt, bool copy_in, bool c
                              {1.0 / 3.0, 2.0 / 3.0, (2.0 / 3.0) * dt}};
   const double* in[3] = {h->state, h->t1, h->t2};
   double* out[3] = {h->t1, h->t2, h->state};
-  // the launches go round-robin to the streams in issue order; each waits on
-  // the launches (or copies) it needs that went to other streams
+  // the launches go round-robin to the streams in issue order (the seam's to
+  // its own stream); each waits on the launches (or copies) it needs that
+  // went to other streams
   std::vector<int> stream_of(3 * C, -1);
   const std::vector<int>& order = h->pipe_order[copy_in ? 1 : 0];
+  int rr = 0;
   for (size_t i = 0; i < order.size(); ++i) {
-    const int c = order[i] / 3, st = order[i] % 3, s = (int)(i % S);
+    const int c = order[i] / 3, st = order[i] % 3;
+    const int s = copy_in && h->pipe_seam_set[order[i]] ? S : (rr++ % S);
     cudaStream_t q = cs[s];
     for (int d : h->chunk_deps[c]) {
       if (st == 0) {
@@ -1163,7 +1182,7 @@ int pipelined_step(DgswHandle h, double* host_u, double dt, bool copy_in, bool c
     }
   }
   // the handle's stream resumes after every chunk's last stage (and copy)
-  for (int s = 1; s < S; ++s) {
+  for (int s = 1; s <= S; ++s) {
     DGSW_CUDA(h, cudaEventRecord(done, cs[s]));
     DGSW_CUDA(h, cudaStreamWaitEvent(h->stream, done, 0));
   }
@@ -1796,6 +1815,7 @@ int dgsw_destroy(DgswHandle h) {
   if (h->pipe_out) cudaStreamDestroy(h->pipe_out);
   for (cudaStream_t s : h->pipe_aux)
     if (s) cudaStreamDestroy(s);
+  if (h->pipe_seam) cudaStreamDestroy(h->pipe_seam);
   if (h->dev_first) cudaFree(h->dev_first);
   if (h->ab_list) cudaFree(h->ab_list);
   if (h->ab_level) cudaFree(h->ab_level);

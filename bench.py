@@ -181,27 +181,31 @@ def replica_throughput(points_per_rank, rhs_per_step, steps, seconds_per_rank, w
 def host_link_rates(host, dev):
     """GB/s of whole-state copies between the pinned host buffer and the
     device, measured beside the e2e run: host->device alone, device->host
-    alone, and both at once on two streams (each the mean of 3 copies).  The
+    alone, and both at once on two streams (half the state each way; each
+    the mean of 3 rounds).  The
     host link is shared with whatever else the host runs, so the e2e figure
     moves with it."""
     import torch
     d = torch.empty(host.numel(), dtype=host.dtype, device=dev)
     nbytes = host.numel() * host.element_size()
+    half = host.numel() // 2
     s1, s2 = torch.cuda.Stream(dev), torch.cuda.Stream(dev)
     out = {}
     for name in ("h2d", "d2h", "both"):
         torch.cuda.synchronize(dev)
         t0 = time.perf_counter()
         for _ in range(3):
-            if name in ("h2d", "both"):
+            if name == "h2d":
+                d.copy_(host, non_blocking=True)
+            elif name == "d2h":
+                host.copy_(d, non_blocking=True)
+            else:  # one half in, the other half out, at once
                 with torch.cuda.stream(s1):
-                    d.copy_(host, non_blocking=True)
-            if name in ("d2h", "both"):
+                    d[:half].copy_(host[:half], non_blocking=True)
                 with torch.cuda.stream(s2):
-                    host.copy_(d, non_blocking=True)
+                    host[half:].copy_(d[half:], non_blocking=True)
         torch.cuda.synchronize(dev)
-        moved = 3 * nbytes * (2 if name == "both" else 1)
-        out[name] = moved / (time.perf_counter() - t0) / 1e9
+        out[name] = 3 * nbytes / (time.perf_counter() - t0) / 1e9
     del d
     return out
 

@@ -182,9 +182,8 @@ def host_link_rates(host, dev):
     """GB/s of whole-state copies between the pinned host buffer and the
     device, measured beside the e2e run: host->device alone, device->host
     alone, and both at once on two streams (half the state each way; each
-    the mean of 3 rounds).  The
-    host link is shared with whatever else the host runs, so the e2e figure
-    moves with it."""
+    the mean of 3 rounds).  The host link is shared with whatever else the
+    host runs, so the e2e figure moves with it."""
     import torch
     d = torch.empty(host.numel(), dtype=host.dtype, device=dev)
     nbytes = host.numel() * host.element_size()

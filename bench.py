@@ -633,15 +633,28 @@ def run_ours(args):
     k2 = max(1, min(args.steps, 10))
     ev.step_host(hnp, 1, DT)  # chunk schedule and streams set up
     torch.cuda.synchronize()
+    stream = torch.cuda.ExternalStream(ev.stream_ptr(), device=dev)
+    marks = [torch.cuda.Event(enable_timing=True) for _ in range(k2 + 1)]
+    walls = []
     t0 = time.perf_counter()
-    for _ in range(k2):
+    marks[0].record(stream)
+    for i in range(k2):
+        a = time.perf_counter()
         ev.step_host(hnp, 1, DT)
+        walls.append(time.perf_counter() - a)
+        marks[i + 1].record(stream)
     el = time.perf_counter() - t0
+    torch.cuda.synchronize()
+    device_ms = [marks[i].elapsed_time(marks[i + 1]) for i in range(k2)]
     e2e_value, el = replica_throughput(points, 3, k2, el, ws)
     e2e = {"value": e2e_value, "unit": UNIT,
            "h2d_bytes_per_step": ev.state_size * 8, "d2h_bytes_per_step": ev.state_size * 8,
            "steps": k2, "call": "dgsw_step_host(h, pinned host state, 1, dt) per step",
            "ms_per_step": el / k2 * 1e3,
+           "ms_per_call_min_median_max": [float(np.min(walls) * 1e3), float(np.median(walls) * 1e3),
+                                          float(np.max(walls) * 1e3)],
+           "device_ms_per_call_median": float(np.median(device_ms)),
+           "host_pinned": bool(host.is_pinned()),
            "host_link_gbs": host_link_rates(host, dev)}
     ev.close()
 

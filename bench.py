@@ -757,6 +757,9 @@ def main():
     ap.add_argument("--curved-only", action="store_true",
                     help="run only the curved shell workload and print its numbers (for "
                          "profiling captures)")
+    ap.add_argument("--batched-only", action="store_true",
+                    help="run only the 256-instance mixed-extent workload and print its "
+                         "numbers (for profiling captures)")
     ap.add_argument("--elements", type=int, default=ELEMS,
                     help="elements per axis (default 32: the benchmark workload; smaller "
                          "values only for profiling captures)")
@@ -767,6 +770,11 @@ def main():
         import torch
         torch.cuda.set_device(0)
         print(json.dumps(time_curved(args, 0, not args.no_cpu_baseline)), flush=True)
+        return 0
+    if args.batched_only:
+        import torch
+        torch.cuda.set_device(0)
+        print(json.dumps(time_batched(args, 0)), flush=True)
         return 0
     return run_ours(args)
 

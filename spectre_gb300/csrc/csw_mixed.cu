@@ -54,8 +54,11 @@ __device__ __forceinline__ void line_geometry(int a, int line, int& base, int& s
   }
 }
 
+// Resident blocks per SM asked of the register allocator: three for the
+// plain FP32 stages, whose split tables are read from shared memory where
+// used (fewer registers); two for the compensated stage.
 template <int N, bool COMP>
-__global__ void __launch_bounds__(kThreads, 2) csw_stage_mixed_kernel(CswMixedLaunch L) {
+__global__ void __launch_bounds__(kThreads, COMP ? 2 : 3) csw_stage_mixed_kernel(CswMixedLaunch L) {
   using S = CmShape<N, COMP>;
   constexpr int NN = S::NN, NP = S::NP, PTS = S::PTS, TAB = S::TAB;
   extern __shared__ float fsm[];
@@ -158,7 +161,7 @@ __global__ void __launch_bounds__(kThreads, 2) csw_stage_mixed_kernel(CswMixedLa
         for (int i = 0; i < N; ++i) ul[i] = Ul[v * NP + base + i * stride];
         dev::eo_line_df<N>(uh, ul, du, th, tl);
       } else {
-        dev::eo_line<N, float>(uh, du, th);
+        dev::eo_line<N, float, true>(uh, du, th);
       }
 #pragma unroll
       for (int i = 0; i < N; ++i) Ga[v * NP + base + i * stride] = du[i];

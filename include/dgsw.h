@@ -39,7 +39,7 @@
 extern "C" {
 #endif
 
-#define DGSW_ABI_VERSION 6
+#define DGSW_ABI_VERSION 7
 
 typedef enum {
   DGSW_OK = 0,
@@ -296,6 +296,40 @@ int dgsw_adams_schedule(int order, const int64_t* level_counts, const int32_t* a
                         double slab, int n_slabs, int max_jobs, DgswAdamsJob* jobs,
                         int* n_jobs, int64_t* ticks_per_slab, int* ring_slots);
 
+/* ---- time bookkeeping: TimeStepId and next_time_id --------------------------
+ * TimeStepId (src/Time/TimeStepId.hpp:26-70, TimeStepId.cpp:19-98) with the
+ * step start as an exact fraction of its slab (Time, src/Time/Time.cpp:96-98:
+ * value = (1 - f) start + f end; Slab::advance / retreat, Slab.cpp:31-33),
+ * and the time steppers' next_time_id: Rk3HesthavenSsp
+ * (src/Time/TimeSteppers/Rk3HesthavenSsp.cpp:36-48: substep 0 -> 1 at
+ * fraction 1 of the step, 1 -> 2 at 1/2, 2 -> the next step) and
+ * AdamsBashforth (one substep: the next step).  Host-only.  The substeps of
+ * dgsw_step evaluate the right-hand side at these times; nothing on this
+ * path depends on time explicitly, so they are bookkeeping for callers. */
+typedef struct DgswTimeStepId {
+  int64_t slab_number;
+  double slab_start, slab_end; /* the slab of the step's start */
+  int32_t step_num, step_den;  /* step start = step_num/step_den of the slab (reduced) */
+  int32_t substep;
+  int32_t size_num, size_den;  /* step size as a slab fraction; +-1/1 (time's
+                                  direction) at substep 0 */
+  double substep_time;         /* time of this substep */
+} DgswTimeStepId;
+/* The id at the start of a step at fraction num/den of the slab
+ * [slab_start, slab_end] (the TimeStepId(bool, int64_t, const Time&)
+ * constructor: a time at the slab's end moves into the next slab). */
+int dgsw_time_step_id(int time_runs_forward, int64_t slab_number, double slab_start,
+                      double slab_end, int32_t num, int32_t den, DgswTimeStepId* out);
+/* TimeStepper::next_time_id for time_stepper (DgswTimeStepper) with the step
+ * size size_num/size_den of the slab.  DGSW_ERR_ARGUMENT where the reference
+ * ERRORs or ASSERTs (bad substep, a step leaving its slab, a step size that
+ * changes within a step, 32-bit fraction overflow). */
+int dgsw_next_time_id(int time_stepper, const DgswTimeStepId* current, int32_t size_num,
+                      int32_t size_den, DgswTimeStepId* next);
+/* The fraction of the step at which substep k evaluates the right-hand side
+ * (Rk3HesthavenSsp: 0, 1, 1/2; AdamsBashforth: 0). */
+int dgsw_substep_time_fraction(int time_stepper, int substep, double* fraction);
+
 /* ---- step size and state guards ---------------------------------------------
  * dgsw_cfl_steps: StepChoosers::Cfl (src/Time/StepChoosers/Cfl.hpp:55-67) for
  * every element of a configuration: safety_factor * stable_step of the
@@ -486,10 +520,12 @@ int dgsw_shell_geometry(const DgswConfig* config, double* xyz, double* inverse_j
  * loads it until the process exits.  The limit is
  *   2 * elements * 5 * points^3 + 6 * elements <= 4,194,304 doubles
  * (e.g. 8^3 elements at 8 points, 12^3 elements at 5 points); larger bricks
- * return DGSW_ERR_ARGUMENT.  The first call on a device looks up the array's
- * device address (with that device current); make it before any stream
- * capture.  Calls share the array: calls that overlap on the GPU race.
- * Errors: dgsw_noalloc_last_error(). */
+ * return DGSW_ERR_ARGUMENT, and so does a dev_u that is not memory of the
+ * current device.  Every call looks up the array's address on the current
+ * device; the first call on a device may load the library's device code
+ * there, so make it before any stream capture.  Calls share the array and
+ * it keeps the last call's contents: calls that overlap on the GPU race, and
+ * the caller must serialise them.  Errors: dgsw_noalloc_last_error(). */
 int dgsw_step_noalloc(const DgswBrick* brick, int points, double gamma2,
                       double* dev_u, int n_steps, double dt, void* stream);
 size_t dgsw_noalloc_scratch_bytes(void);

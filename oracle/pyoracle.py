@@ -585,3 +585,84 @@ def shell_evolve_adams(s, u, slab, n_slabs, order, levels=None, threads=0):
     _check(lib().orc_shell_evolve_adams(ctypes.addressof(s), order, _p(lv), slab, n_slabs, _p(u),
                                         threads))
     return u
+
+
+# ---------------- time bookkeeping (pure Python, exact fractions) ----------------
+
+class TimeStepIdOracle:
+    """TimeStepId restated with exact fractions (test infrastructure).
+
+    Time: a slab [start, end] and a fraction f of it, value (1 - f) start +
+    f end with each fraction converted to double (Time.cpp:96-98,
+    Rational.cpp:41-43).  next_step / next_substep / canonicalize follow
+    TimeStepId.cpp:65-97; Slab::advance / retreat follow Slab.cpp:31-33."""
+
+    def __init__(self, forward, slab_number, slab_start, slab_end, frac):
+        from fractions import Fraction
+        self.slab_number = slab_number
+        self.slab = (slab_start, slab_end)
+        self.frac = Fraction(frac)
+        self.substep = 0
+        self.size = Fraction(1 if forward else -1)
+        self.substep_time = self._value(self.frac)
+        self._canonicalize()
+
+    def _value(self, f):
+        start, end = self.slab
+        return float(1 - f) * start + float(f) * end
+
+    def _canonicalize(self):
+        forward = self.size > 0
+        if (self.frac == 1) if forward else (self.frac == 0):
+            assert self.substep == 0
+            start, end = self.slab
+            if forward:
+                self.slab = (end, end + (end - start))
+                self.frac = self.frac - 1
+            else:
+                self.slab = (start - (end - start), start)
+                self.frac = self.frac + 1
+            self.slab_number += 1
+
+    def _copy(self):
+        import copy
+        return copy.copy(self)
+
+    def next_step(self, size):
+        from fractions import Fraction
+        out = self._copy()
+        out.frac = self.frac + Fraction(size)
+        assert 0 <= out.frac <= 1
+        out.substep = 0
+        out.size = Fraction(1 if size > 0 else -1)
+        out.substep_time = out._value(out.frac)
+        out._canonicalize()
+        return out
+
+    def next_substep(self, size, step_fraction):
+        from fractions import Fraction
+        end = self.frac + Fraction(size)
+        assert 0 <= end <= 1
+        out = self._copy()
+        out.substep = self.substep + 1
+        out.size = Fraction(size)
+        out.substep_time = ((1.0 - step_fraction) * self._value(self.frac)
+                            + step_fraction * self._value(end))
+        return out
+
+    def key(self):
+        size = self.size
+        return (self.slab_number, self.slab[0], self.slab[1], self.frac.numerator,
+                self.frac.denominator, self.substep, size.numerator, size.denominator,
+                self.substep_time)
+
+
+def rk3_next_time_id(current, size):
+    """Rk3HesthavenSsp::next_time_id, Rk3HesthavenSsp.cpp:36-48."""
+    if current.substep == 0:
+        return current.next_substep(size, 1.0)
+    if current.substep == 1:
+        return current.next_substep(size, 0.5)
+    if current.substep == 2:
+        return current.next_step(size)
+    raise ValueError("Bad id")

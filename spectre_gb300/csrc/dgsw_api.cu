@@ -2362,6 +2362,32 @@ int dgsw_cfl_steps(const DgswConfig* cfg, double safety_factor, double* element_
   return DGSW_OK;
 }
 
+int dgsw_time_step_id(int time_runs_forward, int64_t slab_number, double slab_start,
+                      double slab_end, int32_t num, int32_t den, DgswTimeStepId* out) {
+  if (!out) return fail(nullptr, DGSW_ERR_ARGUMENT, "null output");
+  std::string err;
+  if (!make_time_step_id(time_runs_forward, slab_number, slab_start, slab_end, num, den, out, &err))
+    return fail(nullptr, DGSW_ERR_ARGUMENT, err);
+  return DGSW_OK;
+}
+
+int dgsw_next_time_id(int time_stepper, const DgswTimeStepId* current, int32_t size_num,
+                      int32_t size_den, DgswTimeStepId* next) {
+  if (!current || !next) return fail(nullptr, DGSW_ERR_ARGUMENT, "null argument");
+  std::string err;
+  if (!next_time_id(time_stepper, *current, size_num, size_den, next, &err))
+    return fail(nullptr, DGSW_ERR_ARGUMENT, err);
+  return DGSW_OK;
+}
+
+int dgsw_substep_time_fraction(int time_stepper, int substep, double* fraction) {
+  if (!fraction) return fail(nullptr, DGSW_ERR_ARGUMENT, "null output");
+  std::string err;
+  if (!substep_fraction(time_stepper, substep, fraction, &err))
+    return fail(nullptr, DGSW_ERR_ARGUMENT, err);
+  return DGSW_OK;
+}
+
 static int step_impl(DgswHandle h, int n_steps, double dt) {
   if (int rc = select_device(h)) return rc;
   if (h->adams) return adams_step(h, n_steps, dt);

@@ -91,6 +91,12 @@ struct ShellGeometry {
 // StepChoosers::Cfl per element (cfl.cpp): safety * stable_step * minimum
 // grid spacing / (largest characteristic speed * 3).
 double time_stepper_stable_step(const DgswConfig& cfg);
+// TimeStepId and the time steppers' next_time_id (time_step_id.cpp).
+bool make_time_step_id(int forward, int64_t slab_number, double slab_start, double slab_end,
+                       int32_t num, int32_t den, DgswTimeStepId* out, std::string* err);
+bool substep_fraction(int time_stepper, int substep, double* fraction, std::string* err);
+bool next_time_id(int time_stepper, const DgswTimeStepId& cur, int32_t size_num, int32_t size_den,
+                  DgswTimeStepId* next, std::string* err);
 bool cfl_steps(const DgswConfig& cfg, const Domain& dom, const struct ShellGeometry* geo,
                double safety, std::vector<double>* steps, std::string* err);
 

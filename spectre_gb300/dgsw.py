@@ -79,6 +79,18 @@ class DgswConfig(ctypes.Structure):
                 ("step_levels", ctypes.POINTER(ctypes.c_int32))]
 
 
+class DgswTimeStepId(ctypes.Structure):
+    _fields_ = [("slab_number", ctypes.c_int64), ("slab_start", ctypes.c_double),
+                ("slab_end", ctypes.c_double), ("step_num", ctypes.c_int32),
+                ("step_den", ctypes.c_int32), ("substep", ctypes.c_int32),
+                ("size_num", ctypes.c_int32), ("size_den", ctypes.c_int32),
+                ("substep_time", ctypes.c_double)]
+
+    def key(self):
+        return (self.slab_number, self.slab_start, self.slab_end, self.step_num,
+                self.step_den, self.substep, self.size_num, self.size_den, self.substep_time)
+
+
 class DgswAdamsJob(ctypes.Structure):
     _fields_ = [("launch", ctypes.c_int32), ("level", ctypes.c_int32),
                 ("update", ctypes.c_int32), ("reset", ctypes.c_int32),
@@ -153,6 +165,11 @@ _SIGNATURES = {
     "dgsw_lts_coefficients": (_I, [_I, _P, _P, _I, _P, _P, _I64, _I64, _D, _I64, _I, _I, _I,
                                    _I, _P, _P, _P]),
     "dgsw_adams_schedule": (_I, [_I, _P, _P, _D, _I, _I, _P, _P, _P, _P]),
+    "dgsw_time_step_id": (_I, [_I, _I64, _D, _D, ctypes.c_int32, ctypes.c_int32,
+                               ctypes.POINTER(DgswTimeStepId)]),
+    "dgsw_next_time_id": (_I, [_I, ctypes.POINTER(DgswTimeStepId), ctypes.c_int32,
+                               ctypes.c_int32, ctypes.POINTER(DgswTimeStepId)]),
+    "dgsw_substep_time_fraction": (_I, [_I, _I, ctypes.POINTER(_D)]),
     "dgsw_noalloc_scratch_bytes": (ctypes.c_size_t, []),
     "dgsw_noalloc_last_error": (ctypes.c_char_p, []),
 }
@@ -587,8 +604,36 @@ class Rk3HesthavenSsp:
         return 0.5 * (1.0 + c - 1.0 / c)
 
     def substep_time_fractions(self):
-        """Fractions of dt at which substeps 0, 1, 2 evaluate the RHS."""
-        return (0.0, 1.0, 0.5)
+        """Fractions of dt at which substeps 0, 1, 2 evaluate the RHS
+        (dgsw_substep_time_fraction)."""
+        out = []
+        for k in range(self.number_of_substeps()):
+            f = ctypes.c_double()
+            _check(lib().dgsw_substep_time_fraction(TIME_STEPPERS["rk3_hesthaven_ssp"], k,
+                                                    ctypes.byref(f)))
+            out.append(f.value)
+        return tuple(out)
+
+    def next_time_id(self, current, step_num, step_den):
+        """Rk3HesthavenSsp::next_time_id (Rk3HesthavenSsp.cpp:36-48) with a step
+        of step_num/step_den of the slab."""
+        return next_time_id("rk3_hesthaven_ssp", current, step_num, step_den)
+
+
+def time_step_id(slab_number, slab_start, slab_end, num, den, time_runs_forward=True):
+    """TimeStepId at the start of a step at fraction num/den of the slab."""
+    out = DgswTimeStepId()
+    _check(lib().dgsw_time_step_id(int(bool(time_runs_forward)), slab_number, slab_start,
+                                   slab_end, num, den, ctypes.byref(out)))
+    return out
+
+
+def next_time_id(time_stepper, current, step_num, step_den):
+    """TimeStepper::next_time_id of a DgswTimeStepId (dgsw_next_time_id)."""
+    out = DgswTimeStepId()
+    _check(lib().dgsw_next_time_id(TIME_STEPPERS[time_stepper], ctypes.byref(current),
+                                   step_num, step_den, ctypes.byref(out)))
+    return out
 
 
 class DgEvolution:

@@ -13,16 +13,17 @@
 // caller passes the state (input and output) and the domain; no cudaMalloc,
 // cudaFree or other allocating routine is called, on the host or the device.
 //
-// Set-up: the first call on a device (with that device current) looks up the
-// device address of the array with cudaGetSymbolAddress and caches it; make
-// that first call before any stream capture.  All calls share the array and
+// Set-up: every call looks up the device address of the array on the current
+// device with cudaGetSymbolAddress (no allocation; a cached address could go
+// stale after cudaDeviceReset reloads the module).  The first call on a device
+// may load the library's device code there, so make that first call before
+// any stream capture.  All calls share the array and
 // it keeps the last call's contents; every word a call reads is written by
 // the same call first (tables, then stage 1 before stage 2 reads it, ...), so
 // nothing needs clearing.  Calls that overlap on the GPU (different streams,
 // or other host threads) race on the array and must be serialised by the
 // caller.
 #include <cmath>
-#include <mutex>
 
 #include "../../include/dgsw.h"
 #include "common.cuh"
@@ -34,10 +35,6 @@ namespace {
 
 constexpr size_t kScratchDoubles = (size_t)4 * 1024 * 1024;  // 32 MiB
 static __device__ __align__(256) double g_noalloc_scratch[kScratchDoubles];
-
-constexpr int kMaxDevices = 64;
-std::mutex g_scratch_mutex;
-double* g_scratch_ptr[kMaxDevices] = {};
 
 struct BrickTables {
   int32_t elements[3];
@@ -89,20 +86,14 @@ int noalloc_fail(int code, const char* msg) {
   return code;
 }
 
-// Device address of g_noalloc_scratch on the current device, looked up once.
+// Device address of g_noalloc_scratch on the current device.  Looked up on
+// every call: the lookup allocates nothing, and an address cached across calls
+// would be stale after cudaDeviceReset reloads the module.
 cudaError_t scratch_address(double** out) {
-  int dev = 0;
-  cudaError_t e = cudaGetDevice(&dev);
+  void* p = nullptr;
+  const cudaError_t e = cudaGetSymbolAddress(&p, g_noalloc_scratch);
   if (e != cudaSuccess) return e;
-  if (dev < 0 || dev >= kMaxDevices) return cudaErrorInvalidDevice;
-  std::lock_guard<std::mutex> lock(g_scratch_mutex);
-  if (!g_scratch_ptr[dev]) {
-    void* p = nullptr;
-    e = cudaGetSymbolAddress(&p, g_noalloc_scratch);
-    if (e != cudaSuccess) return e;
-    g_scratch_ptr[dev] = static_cast<double*>(p);
-  }
-  *out = g_scratch_ptr[dev];
+  *out = static_cast<double*>(p);
   return cudaSuccess;
 }
 
@@ -158,6 +149,12 @@ int dgsw_step_noalloc(const DgswBrick* brick, int points, double gamma2, double*
   cudaError_t e = cudaPointerGetAttributes(&attr, dev_u);
   if (e != cudaSuccess || (attr.type != cudaMemoryTypeDevice && attr.type != cudaMemoryTypeManaged))
     return noalloc_fail(DGSW_ERR_ARGUMENT, "dev_u must be device memory");
+  // the scratch array used is the current device's: device memory of another
+  // GPU would mix two devices' pointers in one launch
+  int cur = 0;
+  if ((e = cudaGetDevice(&cur)) != cudaSuccess) return noalloc_fail(DGSW_ERR_CUDA, cudaGetErrorString(e));
+  if (attr.type == cudaMemoryTypeDevice && attr.device != cur)
+    return noalloc_fail(DGSW_ERR_ARGUMENT, "dev_u is not on the current device");
   double* scratch = nullptr;
   e = scratch_address(&scratch);
   if (e != cudaSuccess) return noalloc_fail(DGSW_ERR_CUDA, cudaGetErrorString(e));

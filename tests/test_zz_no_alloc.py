@@ -4,11 +4,16 @@ Some callers cannot call cudaMalloc while they step -- a host framework that
 owns a fixed device-memory budget and only lends plug-ins the buffers it has
 placed, or a caller that must not trigger cudaMalloc's device-wide
 synchronisation.  dgsw_step_noalloc keeps all of its scratch in one fixed
-device array inside the library.  This test calls it through the C ABI and
-checks its result against the handle-based dgsw_step on the same state, for
-two calls in a row (the second call reuses the array the first one left
-behind).  The file sorts last so that a run stopping at the first failure has
-already run every other test.
+device array inside the library.  These tests call it through the C ABI and
+check it, for two calls in a row (the second call reuses the array the first
+one left behind):
+  - against the handle-based dgsw_step on the same state,
+  - against the CPU oracle's SSP-RK3 evolution directly,
+  - with gamma2 != 0 and on a non-default CUDA stream,
+  - and that the device's free memory is the same before and after calls once
+    the library's device code is loaded (nothing is allocated per call).
+The file sorts last so that a run stopping at the first failure has already
+run every other test.
 """
 import ctypes
 import math
@@ -35,6 +40,12 @@ def _rel(a, b):
     return float(np.max(np.abs(a - b)) / np.max(np.abs(b)))
 
 
+def _call(L, brick, n, gamma2, u, steps, dt, stream_ptr=None):
+    rc = L.dgsw_step_noalloc(ctypes.byref(brick), n, gamma2, u.data_ptr(), steps, dt,
+                             stream_ptr)
+    assert rc == 0, L.dgsw_noalloc_last_error()
+
+
 @pytest.mark.parametrize("elements,points", [((4, 4, 4), 6), ((3, 2, 4), 5)])
 def test_noalloc_matches_handle_step_two_calls(elements, points):
     import torch
@@ -51,16 +62,50 @@ def test_noalloc_matches_handle_step_two_calls(elements, points):
     brick = _brick(elements)
     u = torch.tensor(u0, dtype=torch.float64, device="cuda")
     torch.cuda.synchronize()
-    rc = L.dgsw_step_noalloc(ctypes.byref(brick), n, 0.0, u.data_ptr(), steps, dt, None)
-    assert rc == 0, L.dgsw_noalloc_last_error()
+    _call(L, brick, n, 0.0, u, steps, dt)
     torch.cuda.synchronize()
     got1 = u.cpu().numpy()
-    rc = L.dgsw_step_noalloc(ctypes.byref(brick), n, 0.0, u.data_ptr(), steps, dt, None)
-    assert rc == 0, L.dgsw_noalloc_last_error()
+    _call(L, brick, n, 0.0, u, steps, dt)
     torch.cuda.synchronize()
     got2 = u.cpu().numpy()
     assert _rel(got1, ref1) <= RTOL
     assert _rel(got2, ref2) <= RTOL
+
+
+@pytest.mark.parametrize("gamma2", [0.0, 1.5])
+def test_noalloc_matches_oracle_on_a_side_stream(oracle, gamma2):
+    """Two calls in a row on a non-default stream against the oracle's own
+    SSP-RK3 evolution (Rk3HesthavenSsp.cpp:63-80 restated on the CPU), and the
+    device's free memory unchanged across the calls."""
+    import torch
+    L = dgsw.lib()
+    elements, n, dt, steps = (3, 4, 2), 6, 2e-3, 2
+    bricks = [Brick(elements)]
+    u0 = oracle.initial_data(bricks, n, "plane_wave", [1.0, 1.0, 1.0])
+    ref1 = oracle.evolve(bricks, n, u0, dt, steps, gamma2=gamma2)
+    ref2 = oracle.evolve(bricks, n, ref1, dt, steps, gamma2=gamma2)
+    brick = _brick(elements)
+    side = torch.cuda.Stream()
+    with torch.cuda.stream(side):
+        u = torch.tensor(u0, dtype=torch.float64, device="cuda")
+    side.synchronize()
+    # load the library's device code (and its fixed array) before measuring
+    warm = u.clone()
+    torch.cuda.synchronize()
+    _call(L, brick, n, gamma2, warm, 1, dt, side.cuda_stream)
+    side.synchronize()
+    free0, _ = torch.cuda.mem_get_info()
+    _call(L, brick, n, gamma2, u, steps, dt, side.cuda_stream)
+    side.synchronize()
+    got1 = u.cpu().numpy()
+    free1, _ = torch.cuda.mem_get_info()
+    _call(L, brick, n, gamma2, u, steps, dt, side.cuda_stream)
+    side.synchronize()
+    got2 = u.cpu().numpy()
+    free2, _ = torch.cuda.mem_get_info()
+    assert _rel(got1, ref1) <= RTOL
+    assert _rel(got2, ref2) <= RTOL
+    assert free0 == free1 == free2, (free0, free1, free2)
 
 
 def test_noalloc_rejects_bricks_beyond_the_fixed_scratch():
@@ -72,7 +117,9 @@ def test_noalloc_rejects_bricks_beyond_the_fixed_scratch():
     rc = L.dgsw_step_noalloc(ctypes.byref(too_big), 8, 0.0, u.data_ptr(), 1, 1e-3, None)
     assert rc == -1
     assert b"32 MiB" in L.dgsw_noalloc_last_error()
-    host = np.zeros(16)
+    # host memory is refused before anything is launched
+    host = np.zeros(5 * 8 * 8)
     rc = L.dgsw_step_noalloc(ctypes.byref(_brick((2, 2, 2))), 2, 0.0, host.ctypes.data, 1,
                              1e-3, None)
     assert rc == -1
+    assert b"device memory" in L.dgsw_noalloc_last_error()

@@ -216,6 +216,14 @@ def cpu_threads():
         return os.cpu_count() or 1
 
 
+def cpu_flags():
+    from oracle import pyoracle
+    try:
+        return pyoracle.fast_build_flags()
+    except Exception:
+        return "unknown flags"
+
+
 def cpu_reference_run(steps, warmup, threads, elems=None):
     """Times the FP64 oracle (C++ restatement of the reference) on host cores.
 
@@ -231,9 +239,9 @@ def cpu_reference_run(steps, warmup, threads, elems=None):
     u = pyoracle.initial_data(bricks, N_PTS, "gaussian", params)
     points = elems ** 3 * N_PTS ** 3
     if warmup:
-        u = pyoracle.evolve(bricks, N_PTS, u, DT, warmup, threads=threads)
+        u = pyoracle.evolve(bricks, N_PTS, u, DT, warmup, threads=threads, fast=True)
     t0 = time.perf_counter()
-    u = pyoracle.evolve(bricks, N_PTS, u, DT, steps, threads=threads)
+    u = pyoracle.evolve(bricks, N_PTS, u, DT, steps, threads=threads, fast=True)
     el = time.perf_counter() - t0
     return points * 3 * steps / el, el, points
 
@@ -247,9 +255,9 @@ def run_reference(args):
     # host cores, so at most REFERENCE_MAX_STEPS of the requested steps run
     steps = max(1, min(args.steps, REFERENCE_MAX_STEPS))
     value, el, points = cpu_reference_run(steps, min(args.warmup, 1), threads)
-    sample = ("FP64 C++ restatement of the reference (oracle/) on the workload itself, "
-              "32^3 elements x 8^3 LGL points (%d points), %d SSP-RK3 steps, %d threads, %.1f s"
-              % (points, steps, threads, el))
+    sample = ("FP64 C++ restatement of the reference (oracle/, built with %s) on the "
+              "workload itself, 32^3 elements x 8^3 LGL points (%d points), %d SSP-RK3 steps, "
+              "%d threads, %.1f s" % (cpu_flags(), points, steps, threads, el))
     line = {
         "impl": "reference", "metric": METRIC, "value": value, "unit": UNIT,
         "n_gpus": args.gpus, "steps": steps, "warmup": args.warmup,
@@ -520,17 +528,17 @@ def time_curved(args, dev, with_cpu):
         s_orc = pyoracle.shell(1.9, 20.0, 2, 3, n, 1.0, 0.0, 1.0)
         u = pyoracle.shell_initial_data(s_orc, 8.0, 1.0)
         threads = cpu_threads()
-        pyoracle.shell_rhs(s_orc, u, threads=threads)
+        pyoracle.shell_rhs(s_orc, u, threads=threads, fast=True)
         t0 = time.perf_counter()
         reps = 2
         for _ in range(reps):
-            pyoracle.shell_rhs(s_orc, u, threads=threads)
+            pyoracle.shell_rhs(s_orc, u, threads=threads, fast=True)
         el = (time.perf_counter() - t0) / reps
         out["cpu_baseline"] = {"value": points / el, "unit": UNIT, "cores": threads,
                                "kind": "port",
-                               "sample": "oracle curved RHS of the full shell, %d evaluations, "
-                                         "%.2f s each (includes its geometry set-up)"
-                                         % (reps, el)}
+                               "sample": "oracle curved RHS of the full shell (built with %s), "
+                                         "%d evaluations, %.2f s each (includes its geometry "
+                                         "set-up)" % (cpu_flags(), reps, el)}
     return out
 
 

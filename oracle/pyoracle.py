@@ -12,6 +12,9 @@ import numpy as np
 
 HERE = os.path.dirname(os.path.abspath(__file__))
 LIB = os.path.join(HERE, "_build", "liboracle.so")
+# the same sources built for speed (FMA contraction, the host CPU's vector
+# ISA): used only as the timed CPU baseline, never as the checker
+LIB_FAST = os.path.join(HERE, "_build", "liboracle_fast.so")
 
 
 class OrcBrick(ctypes.Structure):
@@ -37,62 +40,80 @@ def build():
 
 
 _lib = None
+_lib_fast = None
 
 
-def lib():
-    global _lib
+def fast_build_flags():
+    """The compiler flags of liboracle_fast.so on this host."""
+    r = subprocess.run(["make", "-s", "-C", HERE, "flags"], check=True, capture_output=True,
+                       text=True)
+    return r.stdout.strip()
+
+
+def lib(fast=False):
+    """The checker library, or with fast=True the speed build of the same
+    sources (the timed CPU baseline)."""
+    global _lib, _lib_fast
+    if fast:
+        if _lib_fast is None:
+            _lib_fast = _load(LIB_FAST)
+        return _lib_fast
     if _lib is None:
-        srcs = ("dgsw_oracle.cpp", "adams_oracle.cpp", "dgsw_oracle.h", "adams_oracle.hpp")
-        if not os.path.exists(LIB) or os.path.getmtime(LIB) < max(
-                os.path.getmtime(os.path.join(HERE, f)) for f in srcs):
-            build()
-        L = ctypes.CDLL(LIB)
-        P, D, I, I64 = ctypes.c_void_p, ctypes.c_double, ctypes.c_int, ctypes.c_int64
-        sig = {
-            "orc_lgl": [I, P, P], "orc_barycentric_weights": [I, P],
-            "orc_diff_matrix": [I, P], "orc_vandermonde": [I, P],
-            "orc_inv_vandermonde": [I, P], "orc_interp_matrix": [I, I, P, P],
-            "orc_proj_face_to_mortar": [I, I, P], "orc_proj_mortar_to_face": [I, I, P],
-            "orc_index_maps": [I, P, P, P, P, P], "orc_offsets": [I64, P, P],
-            "orc_coords": [I, P, P, P], "orc_initial_data": [I, P, P, I, P, D, P],
-            "orc_package": [I, P, P, P, P, P, P, P, P], "orc_boundary_terms": [I, P, P, P],
-            "orc_rhs": [I, P, P, D, P, P, I], "orc_volume_rhs": [I, P, P, D, P, P, I],
-            "orc_rk3_substep": [I64, I, D, P, P, P, P], "orc_evolve": [I, P, P, D, D, I, P, I],
-            "orc_ks_background": [I, D, P, P],
-            "orc_csw_time_derivative": [I, P, P, P, P, P, P, D, D, P],
-            "orc_csw_package": [I, P, P, P, P, P, P, P, P, P, P, P, P],
-            "orc_csw_boundary_terms": [I, P, P, P],
-            "orc_csw_cpsr": [I] + [P] * 17,
-            "orc_shell_geometry": [P, P, P], "orc_shell_connectivity": [P, P, P, P],
-            "orc_shell_initial_data": [P, D, D, P], "orc_shell_rhs": [P, P, P, I],
-            "orc_shell_evolve": [P, D, I, P, I],
-            "orc_exponential_filter": [I, D, I, P], "orc_filter_elements": [I64, P, D, I, P],
-            "orc_observe_norms": [I, P, P, P, P, P], "orc_shell_observe_norms": [P, P, P],
-            "orc_lg": [I, P, P], "orc_lg_diff_matrix": [I, P], "orc_lg_boundary": [I, P, P, P, P],
-            "orc_coords_gauss": [I, P, I, P], "orc_rhs_gauss": [I, P, I, D, P, P, I],
-            "orc_evolve_gauss": [I, P, I, D, D, I, P, I],
-            "orc_refined_index_maps": [P, P, P, P], "orc_refined_coords": [P, I, P],
-            "orc_refined_rhs": [P, I, D, P, P, I], "orc_refined_evolve": [P, I, D, D, I, P, I],
-            "orc_proj_half": [I, I, P, P],
-            "orc_amr_matrix": [I, I, I, P], "orc_amr_project": [I, I64, P, P, P, P, P, P, P, P],
-            "orc_variable_coefficients": [I, P, D, D, P],
-            "orc_adams_coefficients": [I, P, I64, I64, D, I64, P],
-            "orc_lts_coefficients": [I, P, P, I, P, P, I64, I64, D, I64, I, I, I, I, P, P, P],
-            "orc_evolve_adams": [I, P, I, D, I, P, D, I, P, I],
-            "orc_shell_evolve_adams": [P, I, P, D, I, P, I],
-        }
-        for name, args in sig.items():
-            fn = getattr(L, name)
-            fn.argtypes = args
-            fn.restype = I
-        L.orc_num_elements.argtypes = [I, P]
-        L.orc_num_elements.restype = I64
-        L.orc_refined_num_elements.argtypes = [P]
-        L.orc_refined_num_elements.restype = I64
-        L.orc_shell_num_elements.argtypes = [P]
-        L.orc_shell_num_elements.restype = I64
-        _lib = L
+        _lib = _load(LIB)
     return _lib
+
+
+def _load(path):
+    srcs = ("dgsw_oracle.cpp", "adams_oracle.cpp", "dgsw_oracle.h", "adams_oracle.hpp")
+    if not os.path.exists(path) or os.path.getmtime(path) < max(
+            os.path.getmtime(os.path.join(HERE, f)) for f in srcs):
+        build()
+    L = ctypes.CDLL(path)
+    P, D, I, I64 = ctypes.c_void_p, ctypes.c_double, ctypes.c_int, ctypes.c_int64
+    sig = {
+        "orc_lgl": [I, P, P], "orc_barycentric_weights": [I, P],
+        "orc_diff_matrix": [I, P], "orc_vandermonde": [I, P],
+        "orc_inv_vandermonde": [I, P], "orc_interp_matrix": [I, I, P, P],
+        "orc_proj_face_to_mortar": [I, I, P], "orc_proj_mortar_to_face": [I, I, P],
+        "orc_index_maps": [I, P, P, P, P, P], "orc_offsets": [I64, P, P],
+        "orc_coords": [I, P, P, P], "orc_initial_data": [I, P, P, I, P, D, P],
+        "orc_package": [I, P, P, P, P, P, P, P, P], "orc_boundary_terms": [I, P, P, P],
+        "orc_rhs": [I, P, P, D, P, P, I], "orc_volume_rhs": [I, P, P, D, P, P, I],
+        "orc_rk3_substep": [I64, I, D, P, P, P, P], "orc_evolve": [I, P, P, D, D, I, P, I],
+        "orc_ks_background": [I, D, P, P],
+        "orc_csw_time_derivative": [I, P, P, P, P, P, P, D, D, P],
+        "orc_csw_package": [I, P, P, P, P, P, P, P, P, P, P, P, P],
+        "orc_csw_boundary_terms": [I, P, P, P],
+        "orc_csw_cpsr": [I] + [P] * 17,
+        "orc_shell_geometry": [P, P, P], "orc_shell_connectivity": [P, P, P, P],
+        "orc_shell_initial_data": [P, D, D, P], "orc_shell_rhs": [P, P, P, I],
+        "orc_shell_evolve": [P, D, I, P, I],
+        "orc_exponential_filter": [I, D, I, P], "orc_filter_elements": [I64, P, D, I, P],
+        "orc_observe_norms": [I, P, P, P, P, P], "orc_shell_observe_norms": [P, P, P],
+        "orc_lg": [I, P, P], "orc_lg_diff_matrix": [I, P], "orc_lg_boundary": [I, P, P, P, P],
+        "orc_coords_gauss": [I, P, I, P], "orc_rhs_gauss": [I, P, I, D, P, P, I],
+        "orc_evolve_gauss": [I, P, I, D, D, I, P, I],
+        "orc_refined_index_maps": [P, P, P, P], "orc_refined_coords": [P, I, P],
+        "orc_refined_rhs": [P, I, D, P, P, I], "orc_refined_evolve": [P, I, D, D, I, P, I],
+        "orc_proj_half": [I, I, P, P],
+        "orc_amr_matrix": [I, I, I, P], "orc_amr_project": [I, I64, P, P, P, P, P, P, P, P],
+        "orc_variable_coefficients": [I, P, D, D, P],
+        "orc_adams_coefficients": [I, P, I64, I64, D, I64, P],
+        "orc_lts_coefficients": [I, P, P, I, P, P, I64, I64, D, I64, I, I, I, I, P, P, P],
+        "orc_evolve_adams": [I, P, I, D, I, P, D, I, P, I],
+        "orc_shell_evolve_adams": [P, I, P, D, I, P, I],
+    }
+    for name, args in sig.items():
+        fn = getattr(L, name)
+        fn.argtypes = args
+        fn.restype = I
+    L.orc_num_elements.argtypes = [I, P]
+    L.orc_num_elements.restype = I64
+    L.orc_refined_num_elements.argtypes = [P]
+    L.orc_refined_num_elements.restype = I64
+    L.orc_shell_num_elements.argtypes = [P]
+    L.orc_shell_num_elements.restype = I64
+    return L
 
 
 def _p(a):
@@ -238,11 +259,11 @@ def rk3_substep(k, dt, u0, ucur, dudt):
     return out
 
 
-def evolve(bricks, points, u, dt, steps, gamma2=0.0, threads=0):
+def evolve(bricks, points, u, dt, steps, gamma2=0.0, threads=0, fast=False):
     en = elem_points(bricks, points)
     u = np.array(u, dtype=np.float64, copy=True)
     arr = _bricks(bricks)
-    _check(lib().orc_evolve(len(bricks), ctypes.addressof(arr), _p(en), gamma2, dt, steps,
+    _check(lib(fast).orc_evolve(len(bricks), ctypes.addressof(arr), _p(en), gamma2, dt, steps,
                             _p(u), threads))
     return u
 
@@ -335,11 +356,11 @@ def shell_initial_data(s, r0=8.0, width=1.5):
     return u
 
 
-def shell_rhs(s, u, threads=0):
+def shell_rhs(s, u, threads=0, fast=False):
     """Returns (dudt, excision_ok)."""
     u = _c(u)
     du = np.zeros_like(u)
-    rc = lib().orc_shell_rhs(ctypes.byref(s), _p(u), _p(du), threads)
+    rc = lib(fast).orc_shell_rhs(ctypes.byref(s), _p(u), _p(du), threads)
     if rc < 0:
         _check(rc)
     return du, rc == 0

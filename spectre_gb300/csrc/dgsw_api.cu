@@ -68,6 +68,29 @@ struct DgswHandle_ {
   int32_t* pnc_rec[kMaxN + 1] = {};
   int64_t pnc_count[kMaxN + 1] = {};
   double* pnc_wext[kMaxN + 1] = {};
+  // mixed precision in one persistent launch per stage over every extent
+  // (stage_batch.cu): the task list, the compact face buffers of the state
+  // (double-float) and of the two increments, and the launch shapes
+  bool batch = false;
+  int bt_variant = 0;               // launch shape in use
+  int2* bt_tasks[2] = {};           // task lists for 128 and 256 threads per CTA
+  int64_t bt_ntasks[2] = {};
+  int32_t* bt_elems[2] = {};
+  int bt_nmax = 0;                  // largest extent of the domain
+  int64_t* bt_foff = nullptr;
+  int64_t bt_fsize = 0;
+  float2* bt_fu = nullptr;
+  float* bt_fw1 = nullptr;
+  float* bt_fw2 = nullptr;
+  float* bt_fw3 = nullptr;
+  EoTable* bt_eo = nullptr;
+  // per variant and precision (0: FP64 input, 1: FP32): shared-memory regions
+  // and resident grid
+  static constexpr int kBtVariants = 8;
+  int bt_buf[kBtVariants][2] = {}, bt_s[kBtVariants][2] = {}, bt_tab[kBtVariants][2] = {},
+      bt_grid[kBtVariants][2] = {};
+  double bt_tune_ms[kBtVariants] = {};
+  int bt_fu_age = 0;  // steps since the state's face values were formed from it
   // misfit objective and discrete adjoint (uniform FP64 path)
   EoTable eoT{};
   int n_samples = 0;
@@ -272,6 +295,83 @@ GeneralLaunch base_general(DgswHandle h) {
   G.op_off = h->op_off;
   G.gamma2 = h->cfg.gamma2;
   return G;
+}
+
+BatchLaunch base_batch(DgswHandle h, bool comp) {
+  BatchLaunch B;
+  const int v = h->bt_variant, lst = batch_threads(v) == 256 ? 1 : 0;
+  B.variant = v;
+  B.prec = comp ? kPrecComp : kPrecF32;
+  B.tasks = h->bt_tasks[lst];
+  B.n_tasks = h->bt_ntasks[lst];
+  B.task_elems = h->bt_elems[lst];
+  B.offset = h->offset;
+  B.foff = h->bt_foff;
+  B.elem_n = h->elem_n;
+  B.nbr = h->nbr;
+  B.jac = h->jac;
+  B.eo = h->bt_eo;
+  B.op_hi = h->op_hi;
+  B.op_off = h->op_off;
+  B.err = h->dev_err;
+  const int i = comp ? 0 : 1;
+  B.buf_bytes = h->bt_buf[v][i];
+  B.s_bytes = h->bt_s[v][i];
+  B.tab_bytes = h->bt_tab[v][i];
+  B.grid = h->bt_grid[v][i];
+  return B;
+}
+
+// The double-float face values of the state, formed from it.
+cudaError_t batch_state_faces(DgswHandle h) {
+  BatchFaceLaunch F;
+  F.n_elem = h->dom.n_elem;
+  F.elem_n = h->elem_n;
+  F.offset = h->offset;
+  F.foff = h->bt_foff;
+  F.nbr = h->nbr;
+  F.op_hi = h->op_hi;
+  F.op_lo = h->op_lo;
+  F.op_off = h->op_off;
+  F.x64 = h->state;
+  F.fu2 = h->bt_fu;
+  return launch_batch_faces(F, h->stream);
+}
+
+// One mixed-precision SSP-RK3 step in three persistent launches (incremental
+// form of Rk3HesthavenSsp, see enqueue_mixed_stage); the last stage updates
+// the state in place and adds the faces of its increment to the state's.
+cudaError_t enqueue_batch_step(DgswHandle h, double dt) {
+  BatchLaunch A = base_batch(h, true);
+  A.x64 = h->state;
+  A.fx2 = h->bt_fu;
+  A.w32 = h->w1;
+  A.fw32 = h->bt_fw1;
+  A.c = dt;
+  cudaError_t e = launch_stage_batch(A, h->stream);
+  if (e != cudaSuccess) return e;
+  BatchLaunch B = base_batch(h, false);
+  B.x32 = h->w1;
+  B.fx32 = h->bt_fw1;
+  B.w32 = h->w2;
+  B.fw32 = h->bt_fw2;
+  B.alpha = 0.5;
+  B.c = 0.25 * dt;
+  if ((e = launch_stage_batch(B, h->stream)) != cudaSuccess) return e;
+  // W3 = 2/3 W2 + 2dt/3 L(W2) in place of W2 (each element's block is read
+  // only by the CTA that overwrites it) with its face values, then in one
+  // stream u = u0 + W3 + 2/3 W1 and the state's face values += those of
+  // W3 + 2/3 W1 (T linear)
+  BatchLaunch C = base_batch(h, false);
+  C.x32 = h->w2;
+  C.fx32 = h->bt_fw2;
+  C.w32 = h->w2;
+  C.fw32 = h->bt_fw3;
+  C.alpha = 2.0 / 3.0;
+  C.c = (2.0 / 3.0) * dt;
+  if ((e = launch_stage_batch(C, h->stream)) != cudaSuccess) return e;
+  return launch_accumulate_step(h->state, h->w2, h->w1, 2.0 / 3.0, h->dom.offset.back(), h->bt_fu,
+                                h->bt_fw3, h->bt_fw1, h->bt_fsize, h->stream);
 }
 
 // One launch per extent class present in the domain.
@@ -705,6 +805,7 @@ cudaError_t enqueue_mixed_stage(DgswHandle h, int k, double dt, const double* u0
 //   u  = 1/3 u + 2/3 t2 + 2dt/3 L(t2)   (in place: each element reads only
 //   its own u, neighbours' faces come from t2).
 cudaError_t enqueue_step(DgswHandle h, double dt) {
+  if (h->batch) return enqueue_batch_step(h, dt);
   if (mixed(h)) {
     cudaError_t e = enqueue_mixed_stage(h, 0, dt, h->state, nullptr);
     if (e != cudaSuccess) return e;
@@ -1564,6 +1665,102 @@ int dgsw_mortar_projections(int ne, int nm, double* to_m, double* from_m) {
   return DGSW_OK;
 }
 
+// Set-up of the mixed-precision batch path (stage_batch.cu): per element
+// face-buffer offsets (6 N^2 values, rounded up to 4 so that every element's
+// block starts 16-byte aligned), the three face buffers, the split tables of
+// every extent, the task list and the launch shapes.  Tasks: the elements in
+// windows of 256 consecutive elements, grouped by extent within a window
+// (largest first) into tasks of at most batch_task_elements(n).
+int batch_init(DgswHandle h) {
+  const int64_t E = h->dom.n_elem;
+  std::vector<int64_t> foff(E + 1, 0);
+  for (int64_t e = 0; e < E; ++e) {
+    const int64_t n = h->dom.elem_n[e];
+    foff[e + 1] = foff[e] + (6 * n * n + 3) / 4 * 4;
+  }
+  h->bt_fsize = foff[E];
+  cudaError_t e = upload(&h->bt_foff, foff);
+  if (e != cudaSuccess) return cuda_fail(h, e, "upload face offsets");
+  const size_t pad = 64;
+  if ((e = cudaMalloc(&h->bt_fu, h->bt_fsize * sizeof(float2) + pad)) != cudaSuccess ||
+      (e = cudaMalloc(&h->bt_fw1, h->bt_fsize * sizeof(float) + pad)) != cudaSuccess ||
+      (e = cudaMalloc(&h->bt_fw2, h->bt_fsize * sizeof(float) + pad)) != cudaSuccess ||
+      (e = cudaMalloc(&h->bt_fw3, h->bt_fsize * sizeof(float) + pad)) != cudaSuccess)
+    return cuda_fail(h, e, "allocate face buffers");
+  // the rounding pads are read by the copies: keep them finite
+  if ((e = cudaMemset(h->bt_fu, 0, h->bt_fsize * sizeof(float2) + pad)) != cudaSuccess ||
+      (e = cudaMemset(h->bt_fw1, 0, h->bt_fsize * sizeof(float) + pad)) != cudaSuccess ||
+      (e = cudaMemset(h->bt_fw2, 0, h->bt_fsize * sizeof(float) + pad)) != cudaSuccess ||
+      (e = cudaMemset(h->bt_fw3, 0, h->bt_fsize * sizeof(float) + pad)) != cudaSuccess)
+    return cuda_fail(h, e, "clear face buffers");
+  std::vector<EoTable> eo(kMaxN + 1);
+  for (int n = kMinN; n <= kMaxN; ++n) lgl_eo_table(n, &eo[n]);
+  if ((e = upload(&h->bt_eo, eo)) != cudaSuccess) return cuda_fail(h, e, "upload split tables");
+  constexpr int64_t kWindow = 256;
+  bool present[kMaxN + 1] = {};
+  for (int64_t el = 0; el < E; ++el) present[h->dom.elem_n[el]] = true;
+  for (int n = kMinN; n <= kMaxN; ++n)
+    if (present[n]) h->bt_nmax = n;
+  for (int lst = 0; lst < 2; ++lst) {
+    const int variant = lst == 0 ? 0 : 1;  // 128 / 256 threads per CTA
+    if (h->bt_nmax > batch_max_extent(variant)) continue;
+    std::vector<int2> tasks;
+    std::vector<int32_t> elems;
+    elems.reserve(E);
+    for (int64_t w0 = 0; w0 < E; w0 += kWindow) {
+      std::vector<int32_t> bucket[kMaxN + 1];
+      for (int64_t el = w0; el < std::min(E, w0 + kWindow); ++el)
+        bucket[h->dom.elem_n[el]].push_back((int32_t)el);
+      for (int n = kMaxN; n >= kMinN; --n) {
+        if (bucket[n].empty()) continue;
+        const int gmax = batch_task_elements(n, variant);  // >= 1: n <= batch_max_extent
+        for (size_t i = 0; i < bucket[n].size(); i += gmax) {
+          const int g = (int)std::min<size_t>(gmax, bucket[n].size() - i);
+          tasks.push_back(make_int2(n | (g << 8), (int)elems.size()));
+          elems.insert(elems.end(), bucket[n].begin() + i, bucket[n].begin() + i + g);
+        }
+      }
+    }
+    h->bt_ntasks[lst] = (int64_t)tasks.size();
+    if ((e = upload(&h->bt_tasks[lst], tasks)) != cudaSuccess) return cuda_fail(h, e, "upload tasks");
+    if ((e = upload(&h->bt_elems[lst], elems)) != cudaSuccess) return cuda_fail(h, e, "upload tasks");
+  }
+  if (batch_variants() > DgswHandle_::kBtVariants)
+    return fail(h, DGSW_ERR_UNSUPPORTED, "batch stage: more launch shapes than the handle holds");
+  for (int v = 0; v < batch_variants(); ++v) {
+    if (h->bt_nmax > batch_max_extent(v)) continue;
+    for (int i = 0; i < 2; ++i) {
+      size_t buf = 0, sb = 0, tb = 0;
+      for (int n = kMinN; n <= kMaxN; ++n) {
+        if (!present[n]) continue;
+        size_t b1, s1, t1;
+        batch_smem_bytes(n, i == 0, v, &b1, &s1, &t1);
+        buf = std::max(buf, b1);
+        sb = std::max(sb, s1);
+        tb = std::max(tb, t1);
+      }
+      const size_t total = batch_smem_total(v, buf, sb, tb);
+      if (total > 227 * 1024)
+        return fail(h, DGSW_ERR_UNSUPPORTED, "batch stage: shared memory of a task exceeds 227 KB");
+      h->bt_buf[v][i] = (int)buf;
+      h->bt_s[v][i] = (int)sb;
+      h->bt_tab[v][i] = (int)tb;
+      if ((e = batch_grid(i == 0, v, total, &h->bt_grid[v][i])) != cudaSuccess)
+        return cuda_fail(h, e, "batch stage occupancy");
+    }
+  }
+  // the shape compiled for the domain's largest extent, 128 threads per CTA
+  // where an element fits, single-buffered where extents are at most 10
+  h->bt_variant = h->bt_nmax <= batch_max_extent(3) ? 3 : (h->bt_nmax <= batch_max_extent(0) ? 0 : 1);
+  const char* env = std::getenv("DGSW_BATCH_VARIANT");
+  if (env) {
+    const int v = std::atoi(env);
+    if (v >= 0 && v < batch_variants() && h->bt_nmax <= batch_max_extent(v)) h->bt_variant = v;
+  }
+  h->batch = true;
+  return DGSW_OK;
+}
+
 int dgsw_create(const DgswConfig* cfg, DgswHandle* out) {
   if (!cfg || !out) return fail(nullptr, DGSW_ERR_ARGUMENT, "null argument");
   *out = nullptr;
@@ -1651,16 +1848,21 @@ int dgsw_create(const DgswConfig* cfg, DgswHandle* out) {
   cudaError_t e = cudaStreamCreateWithFlags(&h->stream, cudaStreamNonBlocking);
   if (e != cudaSuccess) return bail(e, "cudaStreamCreate");
   const size_t bytes = (size_t)h->dom.offset.back() * sizeof(double);
-  if ((e = cudaMalloc(&h->state, bytes)) != cudaSuccess) return bail(e, "cudaMalloc state");
-  if ((e = cudaMalloc(&h->t1, bytes)) != cudaSuccess) return bail(e, "cudaMalloc stage 1");
-  if ((e = cudaMalloc(&h->t2, bytes)) != cudaSuccess) return bail(e, "cudaMalloc stage 2");
-  if ((e = cudaMalloc(&h->u0s, bytes)) != cudaSuccess) return bail(e, "cudaMalloc step start");
-  if ((e = cudaMemset(h->state, 0, bytes)) != cudaSuccess) return bail(e, "cudaMemset");
+  // 64 bytes of padding past each state-sized buffer: the batch stage's bulk
+  // copies of odd-extent blocks round their end up to 16 bytes
+  const size_t pad = 64;
+  if ((e = cudaMalloc(&h->state, bytes + pad)) != cudaSuccess) return bail(e, "cudaMalloc state");
+  if ((e = cudaMalloc(&h->t1, bytes + pad)) != cudaSuccess) return bail(e, "cudaMalloc stage 1");
+  if ((e = cudaMalloc(&h->t2, bytes + pad)) != cudaSuccess) return bail(e, "cudaMalloc stage 2");
+  if ((e = cudaMalloc(&h->u0s, bytes + pad)) != cudaSuccess) return bail(e, "cudaMalloc step start");
+  if ((e = cudaMemset(h->state, 0, bytes + pad)) != cudaSuccess) return bail(e, "cudaMemset");
   if ((e = cudaMalloc(&h->dev_err, sizeof(int))) != cudaSuccess) return bail(e, "cudaMalloc err");
   if ((e = cudaMemset(h->dev_err, 0, sizeof(int))) != cudaSuccess) return bail(e, "cudaMemset err");
   if (cfg->precision == DGSW_PRECISION_MIXED) {
-    if ((e = cudaMalloc(&h->w1, bytes / 2 + 16)) != cudaSuccess) return bail(e, "cudaMalloc w1");
-    if ((e = cudaMalloc(&h->w2, bytes / 2 + 16)) != cudaSuccess) return bail(e, "cudaMalloc w2");
+    if ((e = cudaMalloc(&h->w1, bytes / 2 + pad)) != cudaSuccess) return bail(e, "cudaMalloc w1");
+    if ((e = cudaMalloc(&h->w2, bytes / 2 + pad)) != cudaSuccess) return bail(e, "cudaMalloc w2");
+    if ((e = cudaMemset(h->w1, 0, bytes / 2 + pad)) != cudaSuccess) return bail(e, "cudaMemset w1");
+    if ((e = cudaMemset(h->w2, 0, bytes / 2 + pad)) != cudaSuccess) return bail(e, "cudaMemset w2");
   }
   std::vector<double> jac(3 * h->dom.n_elem, 0.0);
   if (!h->curved)
@@ -1770,6 +1972,22 @@ int dgsw_create(const DgswConfig* cfg, DgswHandle* out) {
         return bail(e, "allocate face records");
     }
   }
+  if (mixed(h) && !h->curved && !h->gauss && !h->refined) {
+    // the batch kernels take every mixed-extent mixed-precision handle; on
+    // uniform meshes DGSW_MIXED_KERNEL=batch selects them in place of the
+    // even-extent pipeline kernel
+    const char* env = std::getenv("DGSW_MIXED_KERNEL");
+    const bool want = h->general ? !(env && std::string(env) == "general")
+                                 : (env && std::string(env) == "batch");
+    if (want) {
+      int rc = batch_init(h);
+      if (rc) {
+        const std::string msg = h->err;
+        dgsw_destroy(h);
+        return fail(nullptr, rc, msg);
+      }
+    }
+  }
   if (cfg->time_stepper == DGSW_STEPPER_ADAMS_BASHFORTH) {
     int rc = adams_init(h, *cfg);
     if (rc) {
@@ -1827,6 +2045,10 @@ int dgsw_destroy(DgswHandle h) {
     if (h->pnc_wext[n]) cudaFree(h->pnc_wext[n]);
   }
   if (h->pnc_face_idx) cudaFree(h->pnc_face_idx);
+  void* bt[] = {h->bt_tasks[0], h->bt_tasks[1], h->bt_elems[0], h->bt_elems[1], h->bt_foff,
+                h->bt_fu, h->bt_fw1, h->bt_fw2, h->bt_fw3, h->bt_eo};
+  for (void* p : bt)
+    if (p) cudaFree(p);
   if (h->op64) cudaFree(h->op64);
   if (h->op_hi) cudaFree(h->op_hi);
   if (h->op_lo) cudaFree(h->op_lo);
@@ -2406,12 +2628,30 @@ static int step_impl(DgswHandle h, int n_steps, double dt) {
     DGSW_CUDA(h, capture_steps(h, dt, kChunk, &h->graph_many));
     h->graph_many_steps = kChunk;
   }
+  // batch handles: the state's face values are formed from the state at the
+  // start of every call (whatever changed it since) and again every kChunk
+  // steps; in between each step's last stage keeps them current
+  if (h->batch) {
+    DGSW_CUDA(h, batch_state_faces(h));
+    h->bt_fu_age = 0;
+  }
+  auto resync = [&]() -> cudaError_t {
+    if (!h->batch || h->bt_fu_age < kChunk) return cudaSuccess;
+    h->bt_fu_age = 0;
+    return batch_state_faces(h);
+  };
   int left = n_steps;
   while (h->graph_many && left >= h->graph_many_steps) {
+    DGSW_CUDA(h, resync());
     DGSW_CUDA(h, cudaGraphLaunch(h->graph_many, h->stream));
     left -= h->graph_many_steps;
+    h->bt_fu_age += h->graph_many_steps;
   }
-  for (; left > 0; --left) DGSW_CUDA(h, cudaGraphLaunch(h->graph_one, h->stream));
+  for (; left > 0; --left) {
+    DGSW_CUDA(h, resync());
+    DGSW_CUDA(h, cudaGraphLaunch(h->graph_one, h->stream));
+    ++h->bt_fu_age;
+  }
   return DGSW_OK;
 }
 

@@ -139,6 +139,69 @@ bool mixed_pipe_supported(int n);
 cudaError_t launch_bounded_wait_check(int* err, uint64_t limit_ns, cudaStream_t s);
 cudaError_t launch_stage_mixed_pipe(const MixedLaunch& L, cudaStream_t s);
 
+// One mixed-precision stage over every element of a batch of any extents in
+// one persistent launch (stage_batch.cu): W = alpha X + c L(X) with the
+// exterior face values of X read from a compact face buffer, and the face
+// values of W written for the next stage.
+struct BatchLaunch {
+  int variant = 0;                  // compiled launch shape (batch_threads, ...)
+  int prec = kPrecComp;             // kPrecComp (FP64 X) or kPrecF32
+  const int2* tasks = nullptr;      // (n | g << 8, first index into task_elems)
+  int64_t n_tasks = 0;
+  const int32_t* task_elems = nullptr;
+  const int64_t* offset = nullptr;  // per element, values of the state layout
+  const int64_t* foff = nullptr;    // per element, values of the face buffers
+  const int32_t* elem_n = nullptr;
+  const int32_t* nbr = nullptr;
+  const double* jac = nullptr;
+  const EoTable* eo = nullptr;      // device, [kMaxN + 1]
+  const float* op_hi = nullptr;     // face operators T (n x nn) at op_off[n (kMaxN+1) + nn]
+  const int32_t* op_off = nullptr;
+  const double* x64 = nullptr;      // X (kPrecComp): FP64 state
+  const float* x32 = nullptr;       // X (kPrecF32): FP32 increment
+  const float2* fx2 = nullptr;      // exterior face values of X (kPrecComp, double-float)
+  const float* fx32 = nullptr;      // exterior face values of X (kPrecF32)
+  float* w32 = nullptr;             // FP32 output W (may be X's own buffer)
+  float* fw32 = nullptr;            // optional: face values of W for the next stage
+  double alpha = 0.0, c = 1.0;
+  int* err = nullptr;               // device error word (bounded waits that timed out)
+  int buf_bytes = 0, s_bytes = 0, tab_bytes = 0;  // shared-memory regions
+  int grid = 0;
+};
+cudaError_t launch_stage_batch(const BatchLaunch& L, cudaStream_t s);
+// The compiled launch shapes (variants): threads per CTA and largest extent;
+// elements per task of extent n; shared-memory bytes of a launch whose tasks
+// have extent n (its regions in *buf, *s, *tab).
+int batch_variants();
+int batch_threads(int variant);
+int batch_max_extent(int variant);
+int batch_task_elements(int n, int variant);
+void batch_smem_bytes(int n, bool comp, int variant, size_t* buf, size_t* s, size_t* tab);
+// the launch's shared memory for the given region sizes (pipeline buffers,
+// accumulator, tables and the face maps' scratch)
+size_t batch_smem_total(int variant, size_t buf, size_t s, size_t tab);
+// resident grid of the batch kernel with smem bytes of shared memory
+cudaError_t batch_grid(bool comp, int variant, size_t smem, int* grid);
+// The step's update of the FP64 state u (n values) by (double)(w + beta y),
+// and of its double-float face values fu (nf values) by fw + beta fy.
+cudaError_t launch_accumulate_step(double* u, const float* w, const float* y, double beta,
+                                   int64_t n, float2* fu, const float* fw, const float* fy,
+                                   int64_t nf, cudaStream_t s);
+// Double-float exterior face values of an FP64 state for the first stage.
+struct BatchFaceLaunch {
+  int64_t n_elem = 0;
+  const int32_t* elem_n = nullptr;
+  const int64_t* offset = nullptr;
+  const int64_t* foff = nullptr;
+  const int32_t* nbr = nullptr;
+  const float* op_hi = nullptr;
+  const float* op_lo = nullptr;
+  const int32_t* op_off = nullptr;
+  const double* x64 = nullptr;
+  float2* fu2 = nullptr;
+};
+cudaError_t launch_batch_faces(const BatchFaceLaunch& L, cudaStream_t s);
+
 // One class of elements of extent n with neighbours of any extent
 // (stage_general.cu): W = alpha X + beta Y + c L(X).
 struct GeneralLaunch {

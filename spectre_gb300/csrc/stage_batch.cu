@@ -1,0 +1,806 @@
+// stage_batch.cu -- one persistent, TMA-pipelined launch per mixed-precision
+// SSP-RK3 stage over elements of any LGL extents (many independent
+// evolutions with p-nonconforming mortars in one launch).
+//
+// The operator is the same as in stage_general.cu: the ScalarWave time
+// derivative (ScalarWave/TimeDerivative.cpp:37-44) with the UpwindPenalty
+// correction (UpwindPenalty.cpp:35-205) lifted onto GLL faces
+// (LiftFlux.hpp:41-62).  With char speeds (0, +1, -1) the reference's mortar
+// round trip (project both sides to the mortar, dg_boundary_terms, project
+// back: ApplyBoundaryCorrections.hpp:880-937, Projection.cpp:56-375) equals
+//   D_Pi = (w_int - T w_ext)/2,  D_Phi = -n D_Pi,  w = Pi - n.Phi,
+// with T = R_{mortar->face} P_{nbr face->mortar} applied along both face
+// dimensions.
+//
+// Work and data flow (mixed precision, incremental SSP-RK3 of
+// stage_mixed.cu: W1 = dt L(u0), W2 = W1/2 + dt/4 L(W1),
+// u = u0 + 2/3 (W2 + W1) + 2dt/3 L(W2)):
+//  - Tasks: a host-built list of (extent N, g elements of that extent), at
+//    most (threads per CTA) / N^2 elements so that one thread owns one grid
+//    line of one element in each axis pass.  The launch is persistent: CTA b
+//    takes tasks b, b + grid, ...; every extent class runs in the same launch.
+//  - Exterior face values are not gathered from the neighbours' volume data.
+//    Each stage writes, for every face of every element, the w of its output
+//    already mapped by T onto the neighbour's face points, into the
+//    neighbour's slot of a compact face buffer ([element][6][N^2], each
+//    element's block contiguous).  The next stage then reads an element's six
+//    exterior faces as one contiguous block.  For the FP64 state u the face
+//    buffer holds double-float (hi, lo) values: it is formed from u by
+//    batch_faces_kernel and then kept current by the last stage of every step
+//    (faces of u + W = faces of u + T w(W), T linear).
+//  - Each task's element blocks (X and the face block) are staged into
+//    shared memory by TMA bulk copies completing on an mbarrier; with two
+//    pipeline buffers the next task's copies land while the current task
+//    computes, with one the other resident CTAs cover the wait.  Element
+//    blocks of odd extent start on 8- or 4-byte boundaries; the copy starts at
+//    the 16-byte boundary below and reads up to 15 bytes past the block
+//    (every buffer the kernel reads is allocated with padding).
+//  - The three axis passes write the stage's output W to the FP32 output
+//    and in place over X in shared memory (each value is read and
+//    overwritten by the one thread that owns its line in that pass); the
+//    warps then form the next stage's face values from it.  The FP64 state
+//    is updated once per step by a streaming kernel (u0 + W3 + 2/3 W1, FP64
+//    add), which also adds the last stage's face values to the state's.
+//  - Arithmetic: FP32 with the even/odd split of D in the two lanes of packed
+//    FFMA2; the first stage differentiates the FP64 state as double-float
+//    (hi + lo FP32 pairs formed once per value in shared memory, compensated
+//    products and sums).
+// Every mbarrier wait is bounded (2 s of wall clock); a wait that gives up
+// sets the device error word and the CTA returns.
+#include <cstdint>
+#include <type_traits>
+
+#include "common.cuh"
+#include "dg_device.cuh"
+#include "launch.hpp"
+#include "pipe.cuh"
+
+namespace dgsw {
+namespace {
+
+using namespace pipe;
+using dev::dot2_first;
+using dev::dot2_term;
+using dev::split_df;
+using dev::two_sum;
+using dev::widen;
+
+constexpr uint64_t kLimitNs = 2000000000ull;  // 2 s per bounded wait
+
+// ------------------------------------------------------------ split tables
+// Per direction, the scaled even/odd split of D (h = N/2):
+//   pairs (A_ij, B_ij), i, j < h, as float2 [h*h], then for odd N the
+//   middle-point column M_i (i < h) and the middle row B_hj (j < h).
+__host__ __device__ constexpr int tab_stride(int n) {
+  return 2 * (n / 2) * (n / 2) + ((n & 1) ? 2 * (n / 2) : 0);
+}
+
+// packed plain contraction (lanes: x = even part P, y = odd part Q)
+template <int N>
+__device__ __forceinline__ void eo_line_pg(const float (&x)[N], float (&out)[N],
+                                           const float* __restrict__ tab) {
+  constexpr int h = N / 2, odd = N & 1;
+  const float2* pr = reinterpret_cast<const float2*>(tab);
+  float2 eo[h];
+#pragma unroll
+  for (int j = 0; j < h; ++j) eo[j] = make_float2(x[j] + x[N - 1 - j], x[j] - x[N - 1 - j]);
+#pragma unroll
+  for (int i = 0; i < h; ++i) {
+    float2 acc = mul2(pr[i * h], eo[0]);
+#pragma unroll
+    for (int j = 1; j < h; ++j) acc = fma2(pr[i * h + j], eo[j], acc);
+    float P = acc.x;
+    if (odd) P = fmaf(tab[2 * h * h + i], x[h], P);
+    out[i] = P + acc.y;
+    out[N - 1 - i] = acc.y - P;
+  }
+  if (odd) {
+    const float* bm = tab + 2 * h * h + h;
+    float Q = bm[0] * eo[0].y;
+#pragma unroll
+    for (int j = 1; j < h; ++j) Q = fmaf(bm[j], eo[j].y, Q);
+    out[h] = Q;
+  }
+}
+
+// packed compensated contraction of a double-float line (hi + lo tables)
+template <int N>
+__device__ __forceinline__ void eo_line_pdfg(const float (&xh)[N], const float (&xl)[N],
+                                             float (&out)[N], const float* __restrict__ th,
+                                             const float* __restrict__ tl) {
+  constexpr int h = N / 2, odd = N & 1;
+  const float2* ph = reinterpret_cast<const float2*>(th);
+  const float2* pl = reinterpret_cast<const float2*>(tl);
+  float2 eoh[h], eol[h];
+#pragma unroll
+  for (int j = 0; j < h; ++j) {
+    float2 s, t;
+    two_sum2(make_float2(xh[j], xh[j]), make_float2(xh[N - 1 - j], -xh[N - 1 - j]), s, t);
+    eoh[j] = s;
+    eol[j] = add2(t, make_float2(xl[j] + xl[N - 1 - j], xl[j] - xl[N - 1 - j]));
+  }
+#pragma unroll
+  for (int i = 0; i < h; ++i) {
+    // s: the running sum of the products' high parts; the corrections are
+    // three independent sums (rounding errors of s and of the products; the
+    // table's low parts; the data's low parts), added at the end
+    float2 s = mul2(ph[i * h], eoh[0]);
+    float2 c1 = fma2(ph[i * h], eoh[0], neg2(s));
+    float2 c2 = mul2(pl[i * h], eoh[0]);
+    float2 c3 = mul2(ph[i * h], eol[0]);
+#pragma unroll
+    for (int j = 1; j < h; ++j) {
+      const float2 a = ph[i * h + j];
+      const float2 p = mul2(a, eoh[j]);
+      const float2 pe = fma2(a, eoh[j], neg2(p));
+      float2 t;
+      two_sum2(s, p, s, t);
+      c1 = add2(c1, add2(t, pe));
+      c2 = fma2(pl[i * h + j], eoh[j], c2);
+      c3 = fma2(a, eol[j], c3);
+    }
+    float2 c = add2(c1, add2(c2, c3));
+    if (odd) dot2_term(th[2 * h * h + i], tl[2 * h * h + i], xh[h], xl[h], s.x, c.x);
+    out[i] = (s.x + s.y) + (c.x + c.y);
+    out[N - 1 - i] = (s.y - s.x) + (c.y - c.x);
+  }
+  if (odd) {
+    const float* bh = th + 2 * h * h + h;
+    const float* bl = tl + 2 * h * h + h;
+    float qs, qc;
+    dot2_first(bh[0], bl[0], eoh[0].y, eol[0].y, qs, qc);
+#pragma unroll
+    for (int j = 1; j < h; ++j) dot2_term(bh[j], bl[j], eoh[j].y, eol[j].y, qs, qc);
+    out[h] = qs + qc;
+  }
+}
+
+// --------------------------------------------------------- buffer layout
+// Bytes of one element's X block, its face block, and their shared-memory
+// slots (room for the 16-byte alignment shift of the copy).
+__host__ __device__ constexpr int x_bytes(int n, bool comp) {
+  return comp ? 4 * 8 * n * n * n : 5 * 4 * n * n * n;
+}
+__host__ __device__ constexpr int f_bytes(int n, bool comp) {
+  return comp ? 6 * 8 * n * n : (6 * 4 * n * n + 15) / 16 * 16;
+}
+__host__ __device__ constexpr int round128(int b) { return (b + 127) / 128 * 128; }
+__host__ __device__ constexpr int x_slot(int n, bool comp) { return round128(x_bytes(n, comp) + 32); }
+__host__ __device__ constexpr int f_slot(int n, bool comp) { return round128(f_bytes(n, comp) + 32); }
+// elements per task of extent n with bt threads per CTA (one per grid line)
+__host__ __device__ constexpr int task_g(int n, int bt) { return bt / (n * n); }
+// per-warp scratch of the face maps: T (m x n), w and the first sweep
+constexpr int kScratchFloats = 3 * kMaxN * kMaxN;
+
+// face coordinates (a, b) of face direction dir -> volume index of extent n
+__device__ __forceinline__ int face_point(int n, int d, int slice, int a, int b) {
+  return d == 0 ? slice + n * (a + n * b) : (d == 1 ? a + n * (slice + n * b) : a + n * (b + n * slice));
+}
+
+// copy source of element e's X block
+template <bool COMP>
+__device__ __forceinline__ const unsigned char* x_src(const BatchLaunch& L, int64_t off, int np) {
+  return COMP ? reinterpret_cast<const unsigned char*>(L.x64 + off + np)
+              : reinterpret_cast<const unsigned char*>(L.x32 + off);
+}
+
+// issue the TMA copies of task tk into buffer buf (one thread)
+template <bool COMP>
+__device__ void issue_task(const BatchLaunch& L, int2 tk, unsigned char* buf, uint64_t* bar) {
+  const int n = tk.x & 0xff, g = tk.x >> 8;
+  const int np = n * n * n;
+  const int xs = x_slot(n, COMP), fb = f_bytes(n, COMP);
+  uint32_t total = 0;
+  for (int s = 0; s < g; ++s) {
+    const int64_t e = L.task_elems[tk.y + s];
+    const uintptr_t src = reinterpret_cast<uintptr_t>(x_src<COMP>(L, L.offset[e], np));
+    const uintptr_t a0 = src & ~(uintptr_t)15;
+    const uintptr_t a1 = (src + (uintptr_t)x_bytes(n, COMP) + 15) & ~(uintptr_t)15;
+    total += (uint32_t)(a1 - a0) + (uint32_t)fb;
+  }
+  mbar_arrive_expect_tx(bar, total);
+  for (int s = 0; s < g; ++s) {
+    const int64_t e = L.task_elems[tk.y + s];
+    const uintptr_t src = reinterpret_cast<uintptr_t>(x_src<COMP>(L, L.offset[e], np));
+    const uintptr_t a0 = src & ~(uintptr_t)15;
+    const uintptr_t a1 = (src + (uintptr_t)x_bytes(n, COMP) + 15) & ~(uintptr_t)15;
+    bulk_g2s(buf + s * xs, reinterpret_cast<const void*>(a0), (uint32_t)(a1 - a0), bar);
+    const unsigned char* fsrc = COMP ? reinterpret_cast<const unsigned char*>(L.fx2 + L.foff[e])
+                                     : reinterpret_cast<const unsigned char*>(L.fx32 + L.foff[e]);
+    bulk_g2s(buf + g * xs + s * f_slot(n, COMP), fsrc, (uint32_t)fb, bar);
+  }
+}
+
+// Where the element in slot s of the current task sits in shared memory.
+template <bool COMP>
+struct TaskView {
+  unsigned char* buf;   // the task's pipeline buffer
+  const int64_t* offs;  // value offset of each slot's element (shared memory)
+  const BatchLaunch* L;
+  int n, g;
+  __device__ __forceinline__ unsigned char* x(int s) const {
+    const uintptr_t src = reinterpret_cast<uintptr_t>(x_src<COMP>(*L, offs[s], n * n * n));
+    return buf + s * x_slot(n, COMP) + (int)(src & 15);
+  }
+  __device__ __forceinline__ const unsigned char* f(int s) const {
+    return buf + g * x_slot(n, COMP) + s * f_slot(n, COMP);
+  }
+};
+
+// ------------------------------------------------------------- one task
+// W of slot s, field f (Psi, Pi, Phi_x, Phi_y, Phi_z), point p: where the
+// passes leave it inside the X block.  F32: in place of X.  COMP (X holds
+// Pi, Phi_x, Phi_y, Phi_z as (hi, lo) FP32 pairs): Phi_d in the first word of
+// X's Phi_d pair, Pi in the first and Psi in the second word of X's Pi pair.
+template <bool COMP>
+__device__ __forceinline__ int w_index(int f, int p, int np) {
+  if (!COMP) return f * np + p;
+  return f <= 1 ? 2 * p + (f == 0 ? 1 : 0) : 2 * ((f - 1) * np + p);
+}
+
+template <int N, bool COMP>
+__device__ __forceinline__ void task_passes(const BatchLaunch& L, const TaskView<COMP>& V,
+                                            float* S, const float* tabs, const int g,
+                                            const float cf, const float* G) {
+  constexpr int NN = N * N, NP = NN * N, TS = tab_stride(N);
+  const int slot = threadIdx.x / NN;
+  const int t = threadIdx.x - slot * NN;
+  const bool active = slot < g;
+  const int ta = t % N, tb = t / N;
+  const float alpha = (float)L.alpha;
+  unsigned char* xb = active ? V.x(slot) : nullptr;
+  const unsigned char* fbk = active ? V.f(slot) : nullptr;
+  float* Sl = S + slot * NP;
+  const float* th_all = tabs + slot * (COMP ? 2 : 1) * 3 * TS;
+  const int64_t off = active ? V.offs[slot] : 0;
+#pragma unroll 1
+  for (int d = 0; d < 3; ++d) {
+    if (active) {
+      int base, stride;
+      if (d == 0) {
+        base = N * ta + NN * tb;
+        stride = 1;
+      } else if (d == 1) {
+        base = ta + NN * tb;
+        stride = N;
+      } else {
+        base = ta + N * tb;
+        stride = NN;
+      }
+      const int fidx = ta + N * tb;
+      const float* th = th_all + d * TS;
+      const float* tl = th_all + 3 * TS + d * TS;
+      const float Gd = G[slot * 3 + d];
+      // the two lines one after the other (fewer live registers): Phi_d,
+      // keeping its end values, then Pi
+      float dF[N], dP[N], pih[N], pil[N];
+      float dw_lo, dw_hi;
+      if (COMP) {
+        // X holds each FP64 value as its (hi, lo) FP32 pair (split_x)
+        const float2* X = reinterpret_cast<const float2*>(xb);
+        float f0h, f0l, f1h, f1l;
+        {
+          float fh[N], fl[N];
+#pragma unroll
+          for (int i = 0; i < N; ++i) {
+            const float2 v = X[(1 + d) * NP + base + i * stride];
+            fh[i] = v.x;
+            fl[i] = v.y;
+          }
+          eo_line_pdfg<N>(fh, fl, dF, th, tl);
+          f0h = fh[0];
+          f0l = fl[0];
+          f1h = fh[N - 1];
+          f1l = fl[N - 1];
+        }
+#pragma unroll
+        for (int i = 0; i < N; ++i) {
+          const float2 v = X[base + i * stride];
+          pih[i] = v.x;
+          pil[i] = v.y;
+        }
+        eo_line_pdfg<N>(pih, pil, dP, th, tl);
+        const float2* ext = reinterpret_cast<const float2*>(fbk);
+        const float2 elo = ext[(2 * d) * NN + fidx], ehi = ext[(2 * d + 1) * NN + fidx];
+        float wh, wl, t0, dh;
+        two_sum(pih[0], f0h, wh, t0);
+        wl = t0 + (pil[0] + f0l);
+        two_sum(wh, -elo.x, dh, t0);
+        dw_lo = dh + (t0 + (wl - elo.y));
+        two_sum(pih[N - 1], -f1h, wh, t0);
+        wl = t0 + (pil[N - 1] - f1l);
+        two_sum(wh, -ehi.x, dh, t0);
+        dw_hi = dh + (t0 + (wl - ehi.y));
+      } else {
+        const float* X = reinterpret_cast<const float*>(xb);
+        float f0h, f1h;
+        {
+          float fh[N];
+#pragma unroll
+          for (int i = 0; i < N; ++i) fh[i] = X[(2 + d) * NP + base + i * stride];
+          eo_line_pg<N>(fh, dF, th);
+          f0h = fh[0];
+          f1h = fh[N - 1];
+          // alpha X_Phi_d enters the Phi_d output
+#pragma unroll
+          for (int i = 0; i < N; ++i) dP[i] = alpha * fh[i];
+        }
+#pragma unroll
+        for (int i = 0; i < N; ++i) {
+          pih[i] = X[NP + base + i * stride];
+          pil[i] = 0.0f;
+        }
+        {
+          float dd[N];
+          eo_line_pg<N>(pih, dd, th);
+#pragma unroll
+          for (int i = 0; i < N; ++i) dP[i] += dd[i];
+        }
+        const float* ext = reinterpret_cast<const float*>(fbk);
+        dw_lo = (pih[0] + f0h) - ext[(2 * d) * NN + fidx];
+        dw_hi = (pih[N - 1] - f1h) - ext[(2 * d + 1) * NN + fidx];
+      }
+      dF[0] = fmaf(Gd, dw_lo, dF[0]);
+      dP[0] = fmaf(Gd, dw_lo, dP[0]);
+      dF[N - 1] = fmaf(Gd, dw_hi, dF[N - 1]);
+      dP[N - 1] = fmaf(-Gd, dw_hi, dP[N - 1]);
+      float* W = reinterpret_cast<float*>(xb);
+      float* Wg = L.w32 + off;  // this element's block of the FP32 output
+      // Phi_d output: to the output and, in place, for the face maps
+#pragma unroll
+      for (int i = 0; i < N; ++i) {
+        W[w_index<COMP>(2 + d, base + i * stride, NP)] = dP[i];
+        Wg[(2 + d) * NP + base + i * stride] = dP[i];
+      }
+      if (d < 2) {
+#pragma unroll
+        for (int i = 0; i < N; ++i) {
+          if (d == 0)
+            Sl[base + i * stride] = dF[i];
+          else
+            Sl[base + i * stride] += dF[i];
+        }
+      } else {
+#pragma unroll
+        for (int i = 0; i < N; ++i) {
+          const int p = base + i * stride;
+          float wpi = Sl[p] + dF[i];
+          float wpsi = COMP ? fmaf(-cf, pih[i], -cf * pil[i]) : -cf * pih[i];
+          if (!COMP) {
+            wpi = fmaf(alpha, pih[i], wpi);
+            wpsi = fmaf(alpha, reinterpret_cast<const float*>(xb)[p], wpsi);
+          }
+          W[w_index<COMP>(1, p, NP)] = wpi;
+          W[w_index<COMP>(0, p, NP)] = wpsi;
+          Wg[NP + p] = wpi;
+          Wg[p] = wpsi;
+        }
+      }
+    }
+    if (d < 2) __syncthreads();
+  }
+}
+
+// COMP: each FP64 value of the staged X becomes its (hi, lo) FP32 pair in
+// place (the same 8 bytes), so that the passes split each value once.
+template <int N>
+__device__ __forceinline__ void split_x(const TaskView<true>& V, int g, int bt) {
+  constexpr int NP4 = 4 * N * N * N;
+  for (int s = 0; s < g; ++s) {
+    double* X = reinterpret_cast<double*>(V.x(s));
+    for (int q = threadIdx.x; q < NP4; q += bt) {
+      float hi, lo;
+      split_df(X[q], hi, lo);
+      reinterpret_cast<float2*>(X)[q] = make_float2(hi, lo);
+    }
+  }
+}
+
+// The next stage's exterior values from the faces of W: for face dir of the
+// element in slot s, w = Pi + s_e Phi_d (s_e = +1 upper, -1 lower) mapped by
+// T (m x n, m the neighbour's extent) onto the neighbour's face points and
+// stored into the neighbour's slot opposite dir.  One warp per face; T, w and
+// the first sweep sit in the warp's scratch.
+template <bool COMP, int BT>
+__device__ void task_faces(const BatchLaunch& L, const TaskView<COMP>& V, const int32_t* elems,
+                           float* scratch) {
+  constexpr int kWarps = BT / 32;
+  const int n = V.n, g = V.g;
+  const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+  const int nn = n * n, np = nn * n;
+  float* Ts = scratch + warp * kScratchFloats;
+  float* wv = Ts + kMaxN * kMaxN;
+  float* tv = wv + kMaxN * kMaxN;
+  for (int fc = warp; fc < 6 * g; fc += kWarps) {
+    const int s = fc / 6, dir = fc - 6 * s, d = dir >> 1;
+    const bool upper = dir & 1;
+    const int slice = upper ? n - 1 : 0;
+    const float* W = reinterpret_cast<const float*>(V.x(s));
+    const int64_t e = elems[s];
+    const int64_t nb = L.nbr[6 * e + dir];
+    const int m = L.elem_n[nb];
+    const int64_t dst = L.foff[nb] + (int64_t)(dir ^ 1) * m * m;
+    if (m != n) {
+      const float* T = L.op_hi + L.op_off[m * (kMaxN + 1) + n];  // m x n, row-major
+      for (int q = lane; q < m * n; q += 32) Ts[q] = __ldg(T + q);
+    }
+    for (int q = lane; q < nn; q += 32) {
+      const int p = face_point(n, d, slice, q % n, q / n);
+      const float pi = W[w_index<COMP>(1, p, np)], ph = W[w_index<COMP>(2 + d, p, np)];
+      wv[q] = upper ? pi + ph : pi - ph;
+    }
+    __syncwarp();
+    if (m != n) {
+      // tv[pp + n b] = sum_k T(b, k) wv[pp + n k], b < m
+      for (int q = lane; q < n * m; q += 32) {
+        const int pp = q % n, b = q / n;
+        float acc = 0.0f;
+        for (int k = 0; k < n; ++k) acc = fmaf(Ts[b * n + k], wv[pp + n * k], acc);
+        tv[q] = acc;
+      }
+      __syncwarp();
+      // wv[a + m b] = sum_k T(a, k) tv[k + n b]
+      for (int q = lane; q < m * m; q += 32) {
+        const int a = q % m, b = q / m;
+        float acc = 0.0f;
+        for (int k = 0; k < n; ++k) acc = fmaf(Ts[a * n + k], tv[k + n * b], acc);
+        wv[q] = acc;
+      }
+      __syncwarp();
+    }
+    for (int q = lane; q < m * m; q += 32) L.fw32[dst + q] = wv[q];
+    __syncwarp();
+  }
+}
+
+template <int N, bool COMP, int BT>
+__device__ __forceinline__ void run_task(const BatchLaunch& L, const TaskView<COMP>& V, float* S,
+                                         const float* tabs, const float* G) {
+  if constexpr (COMP) {
+    split_x<N>(V, V.g, BT);
+    __syncthreads();
+  }
+  task_passes<N, COMP>(L, V, S, tabs, V.g, (float)L.c, G);
+}
+
+template <bool COMP, int BT, int NMAX>
+__device__ __forceinline__ void dispatch_task(const BatchLaunch& L, const TaskView<COMP>& V,
+                                              float* S, const float* tabs, const float* G) {
+  switch (V.n) {
+    case 2: run_task<2, COMP, BT>(L, V, S, tabs, G); break;
+    case 3: run_task<3, COMP, BT>(L, V, S, tabs, G); break;
+    case 4: run_task<4, COMP, BT>(L, V, S, tabs, G); break;
+    case 5: run_task<5, COMP, BT>(L, V, S, tabs, G); break;
+    case 6: run_task<6, COMP, BT>(L, V, S, tabs, G); break;
+    case 7: run_task<7, COMP, BT>(L, V, S, tabs, G); break;
+    case 8: run_task<8, COMP, BT>(L, V, S, tabs, G); break;
+    case 9: if (NMAX >= 9) run_task<(NMAX >= 9 ? 9 : 2), COMP, BT>(L, V, S, tabs, G); break;
+    case 10: if (NMAX >= 10) run_task<(NMAX >= 10 ? 10 : 2), COMP, BT>(L, V, S, tabs, G); break;
+    case 11: if (NMAX >= 11) run_task<(NMAX >= 11 ? 11 : 2), COMP, BT>(L, V, S, tabs, G); break;
+    case 12: if (NMAX >= 12) run_task<(NMAX >= 12 ? 12 : 2), COMP, BT>(L, V, S, tabs, G); break;
+    default: break;
+  }
+}
+
+// One stage over every task.  BT threads per CTA (one per grid line of the
+// task's elements), MINB resident CTAs per SM asked of the register
+// allocator, extents up to NMAX compiled in, STAGES pipeline buffers (2:
+// the next task's copies land while this one computes; 1: they are issued
+// when this one is done, and other resident CTAs cover the wait).
+template <bool COMP, int BT, int MINB, int NMAX, int STAGES>
+__global__ void __launch_bounds__(BT, MINB) stage_batch_kernel(BatchLaunch L) {
+  constexpr int kMaxG = BT / (kMinN * kMinN);  // elements per task at most (N = 2)
+  extern __shared__ __align__(128) unsigned char smem[];
+  __shared__ uint64_t bars[2];
+  __shared__ int32_t s_elems[kMaxG];
+  __shared__ int64_t s_offs[kMaxG];
+  __shared__ float s_G[3 * kMaxG];
+  unsigned char* bufs[2] = {smem, smem + (STAGES - 1) * L.buf_bytes};
+  unsigned char* rest = smem + STAGES * L.buf_bytes;
+  float* S = reinterpret_cast<float*>(rest);
+  float* tabs = reinterpret_cast<float*>(rest + L.s_bytes);
+  float* scratch = reinterpret_cast<float*>(rest + L.s_bytes + L.tab_bytes);
+
+  if (threadIdx.x == 0) {
+    mbar_init(&bars[0], 1);
+    mbar_init(&bars[1], 1);
+    fence_mbar_init();
+  }
+  __syncthreads();
+  const int64_t Gd = gridDim.x;
+  int64_t task = blockIdx.x;
+  if (task < L.n_tasks && threadIdx.x == 0) issue_task<COMP>(L, L.tasks[task], bufs[0], &bars[0]);
+  const double c = L.c;
+  for (int k = 0; task < L.n_tasks; ++k, task += Gd) {
+    const int b = STAGES == 2 ? (k & 1) : 0;
+    const uint32_t parity = STAGES == 2 ? (uint32_t)((k >> 1) & 1) : (uint32_t)(k & 1);
+    const int64_t next = task + Gd;
+    if (STAGES == 2 && threadIdx.x == 0 && next < L.n_tasks)
+      issue_task<COMP>(L, L.tasks[next], bufs[b ^ 1], &bars[b ^ 1]);
+    const int2 tk = L.tasks[task];
+    const int n = tk.x & 0xff, g = tk.x >> 8;
+    const int ts = tab_stride(n);
+    // per-element data and the scaled split tables (overlap the copies)
+    if (threadIdx.x < g) {
+      const int32_t e = L.task_elems[tk.y + threadIdx.x];
+      s_elems[threadIdx.x] = e;
+      s_offs[threadIdx.x] = L.offset[e];
+      for (int d = 0; d < 3; ++d)
+        s_G[3 * threadIdx.x + d] = (float)(-0.25 * c * (double)(n * (n - 1)) * L.jac[3 * (int64_t)e + d]);
+    }
+    {
+      const EoTable& eo = L.eo[n];
+      const int h = n / 2, odd = n & 1;
+      const int per = 3 * ts;
+      for (int q = threadIdx.x; q < g * per; q += BT) {
+        const int s = q / per, r = q - s * per, d = r / ts, rr = r - d * ts;
+        const int32_t e = L.task_elems[tk.y + s];
+        double v;
+        if (rr < 2 * h * h) {
+          const int pi = rr >> 1, i = pi / h, j = pi - i * h;
+          v = (rr & 1) ? eo.B[i][j] : eo.A[i][j];
+        } else if (odd && rr < 2 * h * h + h) {
+          v = eo.M[rr - 2 * h * h];
+        } else {
+          v = eo.B[h][rr - 2 * h * h - h];
+        }
+        const double sv = (-c * L.jac[3 * (int64_t)e + d]) * v;
+        const float hi = __double2float_rn(sv);
+        float* base = tabs + s * (COMP ? 2 : 1) * per;
+        base[r] = hi;
+        if (COMP) base[per + r] = __double2float_rn(sv - (double)hi);
+      }
+    }
+    const bool landed = mbar_wait(&bars[b], parity, kLimitNs);
+    if (__syncthreads_or(!landed)) {
+      // a copy did not land in time: record it, give the copies still in
+      // flight one more bounded wait, and leave together
+      if (threadIdx.x == 0 && L.err) atomicExch(L.err, 1);
+      if (!landed) mbar_wait(&bars[b], parity, kLimitNs);
+      if (STAGES == 2 && threadIdx.x == 0 && next < L.n_tasks)
+        mbar_wait(&bars[b ^ 1], (uint32_t)(((k + 1) >> 1) & 1), kLimitNs);
+      return;
+    }
+    TaskView<COMP> V;
+    V.buf = bufs[b];
+    V.offs = s_offs;
+    V.L = &L;
+    V.n = n;
+    V.g = g;
+    dispatch_task<COMP, BT, NMAX>(L, V, S, tabs, s_G);
+    if (L.fw32 != nullptr) {
+      __syncthreads();
+      task_faces<COMP, BT>(L, V, s_elems, scratch);
+    }
+    // generic-proxy accesses of this buffer before the next TMA writes into it
+    fence_proxy_async_smem();
+    __syncthreads();
+    if (STAGES == 1 && threadIdx.x == 0 && next < L.n_tasks)
+      issue_task<COMP>(L, L.tasks[next], bufs[0], &bars[0]);
+  }
+}
+
+// The step's update of the FP64 state and of its face values, as streams:
+// u = u + (W + beta Y) for every value (FP64 add), and every face value
+// fu += fw + beta fy in double-float.
+__global__ void accumulate_step_kernel(double* u, const float* w, const float* y, float beta,
+                                       int64_t n, float2* fu, const float* fw, const float* fy,
+                                       int64_t nf) {
+  const int64_t stride = (int64_t)gridDim.x * blockDim.x;
+  const int64_t i0 = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  const int64_t n2 = n / 2;
+  for (int64_t i = i0; i < n2; i += stride) {
+    const double2 b = reinterpret_cast<const double2*>(u)[i];
+    const float2 x = reinterpret_cast<const float2*>(w)[i];
+    const float2 v = reinterpret_cast<const float2*>(y)[i];
+    reinterpret_cast<double2*>(u)[i] =
+        make_double2(b.x + widen(fmaf(beta, v.x, x.x)), b.y + widen(fmaf(beta, v.y, x.y)));
+  }
+  if (i0 == 0 && (n & 1)) u[n - 1] = u[n - 1] + widen(fmaf(beta, y[n - 1], w[n - 1]));
+  for (int64_t i = i0; i < nf; i += stride) {
+    const float v = fmaf(beta, fy[i], fw[i]);
+    const float2 o = fu[i];
+    float sh, st;
+    two_sum(o.x, v, sh, st);
+    st += o.y;
+    const float hi = sh + st;
+    fu[i] = make_float2(hi, st - (hi - sh));
+  }
+}
+
+// ---------------------------------------------------------------- faces of u
+// Double-float exterior values of an FP64 state: one warp per (element,
+// face): w = Pi + s_e Phi_d split into hi + lo, mapped by T (compensated
+// products and sums, hi + lo tables) onto the neighbour's face points.
+constexpr int kFaceWarps = 4;
+
+__global__ void __launch_bounds__(32 * kFaceWarps) batch_faces_kernel(BatchFaceLaunch L) {
+  __shared__ float2 sw[kFaceWarps][kMaxN * kMaxN];
+  __shared__ float2 st[kFaceWarps][kMaxN * kMaxN];
+  __shared__ float2 sT[kFaceWarps][kMaxN * kMaxN];
+  const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+  const int64_t fc = (int64_t)blockIdx.x * kFaceWarps + warp;
+  if (fc >= 6 * L.n_elem) return;  // whole warps leave; only warp barriers follow
+  const int64_t e = fc / 6;
+  const int dir = (int)(fc - 6 * e), d = dir >> 1;
+  const bool upper = dir & 1;
+  const int n = L.elem_n[e], nn = n * n, np = nn * n;
+  const int slice = upper ? n - 1 : 0;
+  const int64_t off = L.offset[e];
+  const int64_t nb = L.nbr[fc];
+  const int m = L.elem_n[nb];
+  const int64_t dst = L.foff[nb] + (int64_t)(dir ^ 1) * m * m;
+  float2* wv = sw[warp];
+  float2* tv = st[warp];
+  float2* T = sT[warp];
+  if (m != n) {
+    const int oo = L.op_off[m * (kMaxN + 1) + n];
+    for (int q = lane; q < m * n; q += 32) T[q] = make_float2(L.op_hi[oo + q], L.op_lo[oo + q]);
+  }
+  for (int q = lane; q < nn; q += 32) {
+    const int p = face_point(n, d, slice, q % n, q / n);
+    float ph, pl, qh, ql, wh, t0;
+    split_df(L.x64[off + np + p], ph, pl);
+    split_df(L.x64[off + (2 + d) * np + p], qh, ql);
+    if (upper) {
+      two_sum(ph, qh, wh, t0);
+      t0 += pl + ql;
+    } else {
+      two_sum(ph, -qh, wh, t0);
+      t0 += pl - ql;
+    }
+    float hi, lo;
+    two_sum(wh, t0, hi, lo);
+    wv[q] = make_float2(hi, lo);
+  }
+  __syncwarp();
+  if (m == n) {
+    for (int q = lane; q < nn; q += 32) L.fu2[dst + q] = wv[q];
+    return;
+  }
+  for (int q = lane; q < n * m; q += 32) {
+    const int pp = q % n, b = q / n;
+    float sh, sc;
+    dot2_first(T[b * n].x, T[b * n].y, wv[pp].x, wv[pp].y, sh, sc);
+    for (int k = 1; k < n; ++k)
+      dot2_term(T[b * n + k].x, T[b * n + k].y, wv[pp + n * k].x, wv[pp + n * k].y, sh, sc);
+    float r, rt;
+    two_sum(sh, sc, r, rt);
+    tv[q] = make_float2(r, rt);
+  }
+  __syncwarp();
+  for (int q = lane; q < m * m; q += 32) {
+    const int a = q % m, b = q / m;
+    float sh, sc;
+    dot2_first(T[a * n].x, T[a * n].y, tv[n * b].x, tv[n * b].y, sh, sc);
+    for (int k = 1; k < n; ++k)
+      dot2_term(T[a * n + k].x, T[a * n + k].y, tv[k + n * b].x, tv[k + n * b].y, sh, sc);
+    float r, rt;
+    two_sum(sh, sc, r, rt);
+    L.fu2[dst + q] = make_float2(r, rt);
+  }
+}
+
+// The compiled launch shapes (variants): threads per CTA, resident CTAs
+// asked of the register allocator for the FP64-input and the FP32 stages,
+// largest extent, pipeline buffers.
+struct ShapeSpec {
+  int bt, minb_comp, minb_f32, nmax, stages;
+};
+constexpr ShapeSpec kShapes[] = {
+    {128, 2, 3, 11, 2},  // 0
+    {256, 1, 2, 12, 2},  // 1
+    {128, 2, 4, 10, 2},  // 2
+    {128, 4, 6, 10, 1},  // 3
+    {128, 3, 5, 10, 1},  // 4
+};
+constexpr int kNumShapes = sizeof(kShapes) / sizeof(kShapes[0]);
+
+template <bool COMP, int V>
+constexpr auto kernel_of() {
+  constexpr ShapeSpec S = kShapes[V];
+  return stage_batch_kernel<COMP, S.bt, COMP ? S.minb_comp : S.minb_f32, S.nmax, S.stages>;
+}
+
+template <bool COMP, int V>
+cudaError_t launch_v(const BatchLaunch& L, size_t smem, cudaStream_t s) {
+  constexpr auto k = kernel_of<COMP, V>();
+  cudaError_t e = set_kernel_smem<k>((int)smem, true);
+  if (e != cudaSuccess) return e;
+  k<<<(unsigned)L.grid, kShapes[V].bt, smem, s>>>(L);
+  return cudaGetLastError();
+}
+
+template <bool COMP, int V>
+cudaError_t grid_v(size_t smem, int* per_sm) {
+  constexpr auto k = kernel_of<COMP, V>();
+  cudaError_t e = set_kernel_smem<k>((int)smem, true);
+  if (e != cudaSuccess) return e;
+  return cudaOccupancyMaxActiveBlocksPerMultiprocessor(per_sm, k, kShapes[V].bt, smem);
+}
+
+template <int V>
+cudaError_t launch_any(bool comp, const BatchLaunch& L, size_t smem, cudaStream_t s) {
+  if (L.variant == V) return comp ? launch_v<true, V>(L, smem, s) : launch_v<false, V>(L, smem, s);
+  if constexpr (V + 1 < kNumShapes) return launch_any<V + 1>(comp, L, smem, s);
+  return cudaErrorInvalidValue;
+}
+
+template <int V>
+cudaError_t grid_any(bool comp, int variant, size_t smem, int* per_sm) {
+  if (variant == V) return comp ? grid_v<true, V>(smem, per_sm) : grid_v<false, V>(smem, per_sm);
+  if constexpr (V + 1 < kNumShapes) return grid_any<V + 1>(comp, variant, smem, per_sm);
+  return cudaErrorInvalidValue;
+}
+
+}  // namespace
+
+int batch_variants() { return kNumShapes; }
+
+int batch_threads(int variant) { return kShapes[variant].bt; }
+
+int batch_max_extent(int variant) { return kShapes[variant].nmax; }
+
+int batch_task_elements(int n, int variant) { return task_g(n, batch_threads(variant)); }
+
+void batch_smem_bytes(int n, bool comp, int variant, size_t* buf, size_t* s, size_t* tab) {
+  const int g = task_g(n, batch_threads(variant));
+  *buf = (size_t)g * (x_slot(n, comp) + f_slot(n, comp));
+  *s = (size_t)round128(g * n * n * n * 4);
+  *tab = (size_t)round128(g * (comp ? 2 : 1) * 3 * tab_stride(n) * 4);
+}
+
+size_t batch_smem_total(int variant, size_t buf, size_t s, size_t tab) {
+  return (size_t)kShapes[variant].stages * buf + s + tab +
+         (size_t)(batch_threads(variant) / 32) * kScratchFloats * 4;
+}
+
+cudaError_t launch_stage_batch(const BatchLaunch& L, cudaStream_t s) {
+  if (L.n_tasks <= 0) return cudaSuccess;
+  const bool comp = L.prec == kPrecComp;
+  if (comp ? (L.x64 == nullptr || L.fx2 == nullptr) : (L.x32 == nullptr || L.fx32 == nullptr))
+    return cudaErrorInvalidValue;
+  if (L.w32 == nullptr) return cudaErrorInvalidValue;
+  if (L.variant < 0 || L.variant >= kNumShapes) return cudaErrorInvalidValue;
+  const size_t smem = batch_smem_total(L.variant, L.buf_bytes, L.s_bytes, L.tab_bytes);
+  return launch_any<0>(comp, L, smem, s);
+}
+
+cudaError_t batch_grid(bool comp, int variant, size_t smem, int* grid) {
+  int dev = 0, sms = 0, per_sm = 0;
+  cudaError_t e;
+  if ((e = cudaGetDevice(&dev)) != cudaSuccess) return e;
+  if ((e = cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev)) != cudaSuccess) return e;
+  if (variant < 0 || variant >= kNumShapes) return cudaErrorInvalidValue;
+  if ((e = grid_any<0>(comp, variant, smem, &per_sm)) != cudaSuccess) return e;
+  if (per_sm < 1) return cudaErrorInvalidConfiguration;
+  *grid = sms * per_sm;
+  return cudaSuccess;
+}
+
+cudaError_t launch_batch_faces(const BatchFaceLaunch& L, cudaStream_t s) {
+  const int64_t faces = 6 * L.n_elem;
+  if (faces <= 0) return cudaSuccess;
+  const int64_t blocks = (faces + kFaceWarps - 1) / kFaceWarps;
+  batch_faces_kernel<<<(unsigned)blocks, 32 * kFaceWarps, 0, s>>>(L);
+  return cudaGetLastError();
+}
+
+cudaError_t launch_accumulate_step(double* u, const float* w, const float* y, double beta,
+                                   int64_t n, float2* fu, const float* fw, const float* fy,
+                                   int64_t nf, cudaStream_t s) {
+  if (n <= 0) return cudaSuccess;
+  if ((reinterpret_cast<uintptr_t>(u) & 15u) != 0 ||
+      ((reinterpret_cast<uintptr_t>(w) | reinterpret_cast<uintptr_t>(y)) & 7u) != 0)
+    return cudaErrorInvalidValue;
+  int dev = 0, sms = 0;
+  cudaError_t e = cudaGetDevice(&dev);
+  if (e == cudaSuccess) e = cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
+  if (e != cudaSuccess) return e;
+  const int64_t want = (n / 2 + 255) / 256;
+  const int64_t grid = want < (int64_t)sms * 8 ? (want > 0 ? want : 1) : (int64_t)sms * 8;
+  accumulate_step_kernel<<<(unsigned)grid, 256, 0, s>>>(u, w, y, (float)beta, n, fu, fw, fy, nf);
+  return cudaGetLastError();
+}
+
+}  // namespace dgsw

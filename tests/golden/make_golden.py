@@ -1,8 +1,9 @@
 """Generate the golden fixtures in this directory from the reference's tests.
 
-Run in a container that has the SpECTRE source tree (release 2024.09.29) at
-SPECTRE_ROOT (default /root/reference).  The generated JSON files are
-committed; nothing at test time reads the reference tree.
+Run with the environment variable SPECTRE_ROOT set to a checkout of the
+SpECTRE source tree (release 2024.09.29); the script stops with a message if
+it is unset.  The generated JSON files are committed; nothing at test time
+reads the reference tree.
 
 Fixtures:
   lgl_golden.json      LGL points/weights, D-matrices and Vandermonde matrices
@@ -35,7 +36,7 @@ import sys
 
 import numpy as np
 
-ROOT = os.environ.get("SPECTRE_ROOT", "/root/reference")
+ROOT = os.environ.get("SPECTRE_ROOT")
 HERE = os.path.dirname(os.path.abspath(__file__))
 
 
@@ -373,6 +374,10 @@ def adams_golden():
 
 
 def main():
+    if not ROOT or not os.path.isdir(ROOT):
+        sys.stderr.write("set SPECTRE_ROOT to a checkout of the SpECTRE source tree "
+                         "(release 2024.09.29)\n")
+        return 2
     with open(os.path.join(HERE, "adams_golden.json"), "w") as f:
         json.dump(adams_golden(), f, indent=1)
     with open(os.path.join(HERE, "lgl_golden.json"), "w") as f:

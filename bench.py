@@ -216,8 +216,29 @@ def cpu_threads():
         return os.cpu_count() or 1
 
 
+_FAST_OK = None
+
+
+def cpu_fast_ok():
+    """Whether the speed build of the oracle runs on this host: a small
+    evolution in a child process (a CPU that lacks an instruction the build
+    uses ends that process, not the bench)."""
+    global _FAST_OK
+    if _FAST_OK is None:
+        import subprocess
+        code = ("import sys; sys.path.insert(0, %r); from oracle import pyoracle; "
+                "from spectre_gb300.dgsw import Brick; b = [Brick((2, 2, 2))]; "
+                "u = pyoracle.initial_data(b, 4, 'plane_wave', [1.0, 1.0, 1.0]); "
+                "pyoracle.evolve(b, 4, u, 1e-3, 2, fast=True)" % ROOT)
+        r = subprocess.run([sys.executable, "-c", code], capture_output=True, timeout=300)
+        _FAST_OK = r.returncode == 0
+    return _FAST_OK
+
+
 def cpu_flags():
     from oracle import pyoracle
+    if not cpu_fast_ok():
+        return "the portable checker flags (the speed build does not run on this host)"
     try:
         return pyoracle.fast_build_flags()
     except Exception:
@@ -239,9 +260,9 @@ def cpu_reference_run(steps, warmup, threads, elems=None):
     u = pyoracle.initial_data(bricks, N_PTS, "gaussian", params)
     points = elems ** 3 * N_PTS ** 3
     if warmup:
-        u = pyoracle.evolve(bricks, N_PTS, u, DT, warmup, threads=threads, fast=True)
+        u = pyoracle.evolve(bricks, N_PTS, u, DT, warmup, threads=threads, fast=cpu_fast_ok())
     t0 = time.perf_counter()
-    u = pyoracle.evolve(bricks, N_PTS, u, DT, steps, threads=threads, fast=True)
+    u = pyoracle.evolve(bricks, N_PTS, u, DT, steps, threads=threads, fast=cpu_fast_ok())
     el = time.perf_counter() - t0
     return points * 3 * steps / el, el, points
 
@@ -357,6 +378,16 @@ def time_batched(args, dev):
                      "ms_per_step": ms / steps}
         points = ev.grid_points
         n_elem = ev.n_elements
+        if name == "mixed":
+            # launch shape the autotuner chose, re-timed after the timed region
+            res[name]["tune"] = ev.tune()
+            hbm = load_peaks()[0].get("hbm_gbs")
+            gbs = MIXED_BYTES_PER_POINT_LAUNCH * points / (ms / (3 * steps) * 1e-3) / 1e9
+            res[name]["roofline"] = {"bound": "hbm", "achieved": gbs, "peak": hbm, "unit": "GB/s",
+                                     "frac": gbs / hbm if hbm else None,
+                                     "bytes_per_point_launch": MIXED_BYTES_PER_POINT_LAUNCH,
+                                     "note": "algorithmic bytes per grid point and stage "
+                                             "launch ÷ the step's mean time per stage"}
         ev.close()
     out = {"workload": "256 periodic ScalarWave evolutions on [0,2pi]^3, elements per axis "
                        "U{2..8}, LGL points per element U{4..10} (p-nonconforming mortars), "
@@ -380,7 +411,55 @@ def time_batched(args, dev):
     out.update({"mixed_speedup_vs_fp64": res["fp64"]["ms_per_step"] / res["mixed"]["ms_per_step"],
                 "max_instance_rel_l2_mixed_vs_fp64": worst,
                 "steps_compared": max(1, args.warmup) + steps})
+    if not getattr(args, "no_full_length", False):
+        out["full_length"] = batched_full_length(bricks, pts, params, dev)
     return out
+
+
+def instance_rel_l2(bricks, pts, a, b):
+    """Per-instance relative L2 of b against a."""
+    errs = []
+    off = 0
+    e = 0
+    for br in bricks:
+        ne = br.elements[0] * br.elements[1] * br.elements[2]
+        size = int(5 * np.sum(np.asarray(pts[e:e + ne], dtype=np.int64) ** 3))
+        errs.append(float(np.linalg.norm(b[off:off + size] - a[off:off + size])
+                          / np.linalg.norm(a[off:off + size])))
+        off += size
+        e += ne
+    return errs
+
+
+def batched_full_length(bricks, pts, params, dev, steps=300, dt=1e-4):
+    """The 256-instance case over its configured 300 steps from the initial
+    data: per-instance relative L2 of the mixed path against the FP64 path."""
+    from spectre_gb300 import DgEvolution, PRECISION_FP64, PRECISION_MIXED
+    states = {}
+    for name, prec in (("fp64", PRECISION_FP64), ("mixed", PRECISION_MIXED)):
+        with DgEvolution(bricks, pts, precision=prec, device=dev) as ev:
+            ev.set_initial_data("gaussian", params)
+            ev.step(steps, dt)
+            states[name] = ev.get_state()
+    errs = instance_rel_l2(bricks, pts, states["fp64"], states["mixed"])
+    return {"steps": steps, "dt": dt, "max_instance_rel_l2_mixed_vs_fp64": max(errs),
+            "median_instance_rel_l2_mixed_vs_fp64": float(np.median(errs))}
+
+
+def config2_full_length(dev, steps=500):
+    """The 32^3 x 8^3 Gaussian case over its configured 500 steps: relative L2
+    of the mixed path against the FP64 path."""
+    from spectre_gb300 import Brick, DgEvolution, PRECISION_FP64, PRECISION_MIXED
+    params = np.array([[1.0, 0.5, np.pi, np.pi, np.pi]])
+    states = {}
+    for name, prec in (("fp64", PRECISION_FP64), ("mixed", PRECISION_MIXED)):
+        with DgEvolution([Brick((ELEMS, ELEMS, ELEMS))], N_PTS, precision=prec, device=dev) as ev:
+            ev.set_initial_data("gaussian", params)
+            ev.step(steps, DT)
+            states[name] = ev.get_state()
+    a, m = states["fp64"], states["mixed"]
+    return {"steps": steps, "dt": DT,
+            "rel_l2_mixed_vs_fp64": float(np.linalg.norm(m - a) / np.linalg.norm(a))}
 
 
 def time_adjoint(dev):
@@ -528,11 +607,11 @@ def time_curved(args, dev, with_cpu):
         s_orc = pyoracle.shell(1.9, 20.0, 2, 3, n, 1.0, 0.0, 1.0)
         u = pyoracle.shell_initial_data(s_orc, 8.0, 1.0)
         threads = cpu_threads()
-        pyoracle.shell_rhs(s_orc, u, threads=threads, fast=True)
+        pyoracle.shell_rhs(s_orc, u, threads=threads, fast=cpu_fast_ok())
         t0 = time.perf_counter()
         reps = 2
         for _ in range(reps):
-            pyoracle.shell_rhs(s_orc, u, threads=threads, fast=True)
+            pyoracle.shell_rhs(s_orc, u, threads=threads, fast=cpu_fast_ok())
         el = (time.perf_counter() - t0) / reps
         out["cpu_baseline"] = {"value": points / el, "unit": UNIT, "cores": threads,
                                "kind": "port",
@@ -694,6 +773,9 @@ def run_ours(args):
                               "bytes_per_point_launch": MIXED_BYTES_PER_POINT_LAUNCH,
                               "avg_launch_ms": launch_m}}
 
+    if mixed is not None and not args.no_full_length and args.elements == ELEMS:
+        mixed["full_length"] = config2_full_length(dev)
+
     batched = None
     if not args.no_batched:
         batched = time_batched(args, dev)
@@ -718,9 +800,9 @@ def run_ours(args):
         threads = cpu_threads()
         v, elc, pts = cpu_reference_run(CPU_SAMPLE_STEPS, 0, threads, args.elements)
         cpu = {"value": v, "unit": UNIT, "cores": threads, "kind": "port",
-               "sample": "FP64 C++ restatement (oracle/) on the workload itself, %d^3 elements "
-                         "x 8^3 points, %d SSP-RK3 steps, %.1f s"
-                         % (args.elements, CPU_SAMPLE_STEPS, elc)}
+               "sample": "FP64 C++ restatement (oracle/, built with %s) on the workload "
+                         "itself, %d^3 elements x 8^3 points, %d SSP-RK3 steps, %.1f s"
+                         % (cpu_flags(), args.elements, CPU_SAMPLE_STEPS, elc)}
     if ws > 1:
         torch.distributed.barrier()
     if rank == 0:
@@ -776,6 +858,9 @@ def main():
     ap.add_argument("--batched-only", action="store_true",
                     help="run only the 256-instance mixed-extent workload and print its "
                          "numbers (for profiling captures)")
+    ap.add_argument("--no-full-length", action="store_true",
+                    help="skip the accuracy runs over the configured step counts (500 steps "
+                         "of the 32^3 case, 300 of the 256-instance case)")
     ap.add_argument("--batched-precision", default="both", choices=["both", "fp64", "mixed"],
                     help="which precision paths the 256-instance workload times (both by "
                          "default; one alone only for profiling captures)")

@@ -39,7 +39,7 @@
 extern "C" {
 #endif
 
-#define DGSW_ABI_VERSION 7
+#define DGSW_ABI_VERSION 8
 
 typedef enum {
   DGSW_OK = 0,
@@ -362,6 +362,24 @@ int dgsw_check_finite(DgswHandle h, int64_t* first_element);
  * force_variant 0 or 1 then imposes that variant (-1 keeps the faster).
  * No counterpart in the reference. */
 int dgsw_autotune(DgswHandle h, int force_variant, int* variant, double* ms_per_launch);
+
+/* The launch autotuner of whichever step kernels the handle runs.
+ * family: DGSW_TUNE_FP64_STAGE (the plain FP64 stage kernel's two
+ * configurations, as dgsw_autotune), DGSW_TUNE_MIXED_BATCH (mixed precision
+ * on elements of differing extents: the persistent batch kernels' compiled
+ * launch shapes -- threads per CTA, resident CTAs per SM, pipeline buffers,
+ * largest extent), or DGSW_TUNE_NONE (fixed configurations).  Re-times every
+ * candidate now on the handle's own state (saved and restored), keeps the
+ * fastest (force_variant >= 0 imposes one instead) and returns the number of
+ * candidates, the choice and ms per step of each (ms_per_step holds
+ * DGSW_TUNE_MAX_VARIANTS values; 0 for candidates that cannot hold the
+ * domain).  The first dgsw_step of a handle runs the same timing when its
+ * shape has not been tuned in this process.  No counterpart in the
+ * reference. */
+enum { DGSW_TUNE_NONE = 0, DGSW_TUNE_FP64_STAGE = 1, DGSW_TUNE_MIXED_BATCH = 2 };
+#define DGSW_TUNE_MAX_VARIANTS 8
+int dgsw_tune(DgswHandle h, int force_variant, int* family, int* n_variants, int* variant,
+              double* ms_per_step);
 
 /* ---- diagnostics -------------------------------------------------------------
  * dgsw_check_device_timeout: runs the mixed-precision pipeline's bounded

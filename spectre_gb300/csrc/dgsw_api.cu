@@ -90,6 +90,7 @@ struct DgswHandle_ {
   int bt_buf[kBtVariants][2] = {}, bt_s[kBtVariants][2] = {}, bt_tab[kBtVariants][2] = {},
       bt_grid[kBtVariants][2] = {};
   double bt_tune_ms[kBtVariants] = {};
+  bool bt_tuned = false;
   int bt_fu_age = 0;  // steps since the state's face values were formed from it
   // misfit objective and discrete adjoint (uniform FP64 path)
   EoTable eoT{};
@@ -685,6 +686,72 @@ int autotune(DgswHandle h, bool force) {
   h->tuned = true;
   std::lock_guard<std::mutex> lk(g_tune_mu);
   g_tuned[key] = choice;
+  return DGSW_OK;
+}
+
+// Launch autotuner of the mixed-precision batch path: every compiled launch
+// shape valid for the domain (threads per CTA, resident CTAs, pipeline
+// buffers, largest extent) is timed over whole steps on the handle's own
+// state, which is saved first and restored after; the fastest is kept for
+// the handle and for handles of the same shape in this process.
+std::map<std::tuple<int64_t, int64_t, int>, int> g_batch_tuned;
+
+int batch_autotune(DgswHandle h, bool force) {
+  if (!h->batch || (h->bt_tuned && !force)) return DGSW_OK;
+  const std::tuple<int64_t, int64_t, int> key(h->dom.n_elem, h->dom.offset.back(), h->bt_nmax);
+  if (!force) {
+    std::lock_guard<std::mutex> lk(g_tune_mu);
+    auto it = g_batch_tuned.find(key);
+    if (it != g_batch_tuned.end()) {
+      h->bt_variant = it->second;
+      h->bt_tuned = true;
+      return DGSW_OK;
+    }
+  }
+  const size_t bytes = h->dom.offset.back() * sizeof(double);
+  DGSW_CUDA(h, cudaMemcpyAsync(h->u0s, h->state, bytes, cudaMemcpyDeviceToDevice, h->stream));
+  cudaEvent_t e0, e1;
+  DGSW_CUDA(h, cudaEventCreate(&e0));
+  DGSW_CUDA(h, cudaEventCreate(&e1));
+  const double dt = 1e-9;  // the state is restored: any step will do
+  const int keep = h->bt_variant;
+  int choice = -1;
+  double best = 0.0;
+  cudaError_t err = cudaSuccess;
+  for (int v = 0; v < batch_variants() && err == cudaSuccess; ++v) {
+    h->bt_tune_ms[v] = 0.0;
+    if (h->bt_nmax > batch_max_extent(v) || h->bt_grid[v][0] <= 0 || h->bt_grid[v][1] <= 0) continue;
+    h->bt_variant = v;
+    err = batch_state_faces(h);  // warm-up step (attributes, caches)
+    if (err == cudaSuccess) err = enqueue_batch_step(h, dt);
+    if (err == cudaSuccess)
+      err = cudaMemcpyAsync(h->state, h->u0s, bytes, cudaMemcpyDeviceToDevice, h->stream);
+    if (err == cudaSuccess) err = batch_state_faces(h);
+    if (err == cudaSuccess) err = cudaEventRecord(e0, h->stream);
+    for (int r = 0; r < 2 && err == cudaSuccess; ++r) err = enqueue_batch_step(h, dt);
+    if (err == cudaSuccess) err = cudaEventRecord(e1, h->stream);
+    if (err == cudaSuccess) err = cudaEventSynchronize(e1);
+    float ms = 0.0f;
+    if (err == cudaSuccess) err = cudaEventElapsedTime(&ms, e0, e1);
+    if (err == cudaSuccess)
+      err = cudaMemcpyAsync(h->state, h->u0s, bytes, cudaMemcpyDeviceToDevice, h->stream);
+    h->bt_tune_ms[v] = ms / 2.0;
+    if (err == cudaSuccess && (choice < 0 || ms / 2.0 < best)) {
+      best = ms / 2.0;
+      choice = v;
+    }
+  }
+  cudaEventDestroy(e0);
+  cudaEventDestroy(e1);
+  if (err == cudaSuccess) err = cudaStreamSynchronize(h->stream);
+  if (err != cudaSuccess) {
+    h->bt_variant = keep;
+    return cuda_fail(h, err, "batch autotune");
+  }
+  if (choice >= 0) h->bt_variant = choice;
+  h->bt_tuned = true;
+  std::lock_guard<std::mutex> lk(g_tune_mu);
+  g_batch_tuned[key] = h->bt_variant;
   return DGSW_OK;
 }
 
@@ -2457,6 +2524,44 @@ int dgsw_autotune(DgswHandle h, int force_variant, int* variant, double* ms_per_
   return DGSW_OK;
 }
 
+int dgsw_tune(DgswHandle h, int force_variant, int* family, int* n_variants, int* variant,
+              double* ms_per_step) {
+  if (!h) return fail(nullptr, DGSW_ERR_ARGUMENT, "null handle");
+  if (int rc = select_device(h)) return rc;
+  int fam = DGSW_TUNE_NONE, nv = 0, v = 0;
+  double ms[DGSW_TUNE_MAX_VARIANTS] = {};
+  if (h->batch) {
+    fam = DGSW_TUNE_MIXED_BATCH;
+    nv = batch_variants();
+    if (force_variant >= nv || force_variant < -1)
+      return fail(h, DGSW_ERR_ARGUMENT, "force_variant out of range");
+    if (force_variant >= 0 && h->bt_nmax > batch_max_extent(force_variant))
+      return fail(h, DGSW_ERR_ARGUMENT, "that launch shape does not hold the domain's extents");
+    destroy_graphs(h);
+    if (int rc = batch_autotune(h, true)) return rc;
+    if (force_variant >= 0) h->bt_variant = force_variant;
+    v = h->bt_variant;
+    for (int i = 0; i < nv && i < DGSW_TUNE_MAX_VARIANTS; ++i) ms[i] = h->bt_tune_ms[i];
+  } else if (tunable(h)) {
+    fam = DGSW_TUNE_FP64_STAGE;
+    nv = 2;
+    if (force_variant >= nv || force_variant < -1)
+      return fail(h, DGSW_ERR_ARGUMENT, "force_variant out of range");
+    destroy_graphs(h);
+    if (int rc = autotune(h, true)) return rc;
+    if (force_variant >= 0) h->stage_variant = force_variant;
+    v = h->stage_variant;
+    ms[0] = 3.0 * h->tune_ms[0];
+    ms[1] = 3.0 * h->tune_ms[1];
+  }
+  if (family) *family = fam;
+  if (n_variants) *n_variants = nv;
+  if (variant) *variant = v;
+  if (ms_per_step)
+    for (int i = 0; i < DGSW_TUNE_MAX_VARIANTS; ++i) ms_per_step[i] = ms[i];
+  return DGSW_OK;
+}
+
 int dgsw_check_device_timeout(DgswHandle h, double limit_seconds) {
   if (!h) return fail(nullptr, DGSW_ERR_ARGUMENT, "null handle");
   if (!(limit_seconds > 0.0) || limit_seconds > 10.0)
@@ -2616,6 +2721,10 @@ static int step_impl(DgswHandle h, int n_steps, double dt) {
   if (!h->tuned && tunable(h)) {
     destroy_graphs(h);
     if (int rc = autotune(h, false)) return rc;
+  }
+  if (h->batch && !h->bt_tuned) {
+    destroy_graphs(h);
+    if (int rc = batch_autotune(h, false)) return rc;
   }
   if (!(h->graph_dt == dt)) {
     destroy_graphs(h);

@@ -136,6 +136,7 @@ _SIGNATURES = {
     "dgsw_observe_norms": (_I, [_P, _P, _P, _P]),
     "dgsw_check_device_timeout": (_I, [_P, _D]),
     "dgsw_autotune": (_I, [_P, _I, ctypes.POINTER(_I), _P]),
+    "dgsw_tune": (_I, [_P, _I, ctypes.POINTER(_I), ctypes.POINTER(_I), ctypes.POINTER(_I), _P]),
     "dgsw_observe_plane_wave_errors": (_I, [_P, _P, _D, _P]),
     "dgsw_exponential_filter_matrix": (_I, [_I, _D, _I, _P]),
     "dgsw_substep": (_I, [_P, _I, _D]),
@@ -796,6 +797,19 @@ class DgEvolution:
         _check(lib().dgsw_autotune(self._h, int(force_variant), ctypes.byref(v), _ptr(ms)),
                self._h)
         return v.value, ms
+
+    TUNE_FAMILIES = {0: "none", 1: "fp64_stage", 2: "mixed_batch"}
+
+    def tune(self, force_variant: int = -1):
+        """Re-times the launch shapes of the handle's step kernels on its own
+        state (dgsw_tune); returns {"family", "variant", "ms_per_step": [...]}
+        with one time per candidate.  force_variant >= 0 imposes a shape."""
+        fam, nv, v = _I(), _I(), _I()
+        ms = np.zeros(8)
+        _check(lib().dgsw_tune(self._h, int(force_variant), ctypes.byref(fam), ctypes.byref(nv),
+                               ctypes.byref(v), _ptr(ms)), self._h)
+        return {"family": self.TUNE_FAMILIES.get(fam.value, str(fam.value)),
+                "variant": v.value, "ms_per_step": [float(x) for x in ms[:nv.value]]}
 
     def check_device_timeout(self, limit_seconds: float = 0.05) -> int:
         """Runs the bounded device wait on a barrier nothing completes; returns

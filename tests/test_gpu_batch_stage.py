@@ -93,3 +93,28 @@ def test_batch_uniform_extent_vs_oracle(oracle, n):
     got = _evolve(bricks, n, u0, dt, steps, kernel="batch")
     ref = oracle.evolve(bricks, n, u0, dt, steps)
     assert worst_rel_l2(got, ref, bricks, [n] * 48) <= RTOL_MIXED
+
+
+def test_batch_tuner_keeps_state_and_every_shape_agrees(oracle):
+    bricks, pts, params = workloads.batched_instances(6, seed=8)
+    u0 = oracle.initial_data(bricks, pts, "gaussian", params)
+    dt, steps = 1e-4, 10
+    ref = oracle.evolve(bricks, pts, u0, dt, steps)
+    results = []
+    with DgEvolution(bricks, pts, precision=PRECISION_MIXED) as ev:
+        ev.set_state(u0)
+        info = ev.tune()
+        assert info["family"] == "mixed_batch"
+        assert np.array_equal(ev.get_state(), u0)  # the timing restores the state
+        timed = [v for v, ms in enumerate(info["ms_per_step"]) if ms > 0]
+        assert info["variant"] in timed and len(timed) >= 2
+        for v in timed:
+            assert ev.tune(force_variant=v)["variant"] == v
+            ev.set_state(u0)
+            ev.step(steps, dt)
+            got = ev.get_state()
+            assert worst_rel_l2(got, ref, bricks, pts) <= RTOL_MIXED
+            results.append(got)
+    # every launch shape does the same arithmetic per element
+    for r in results[1:]:
+        np.testing.assert_array_equal(r, results[0])

@@ -72,10 +72,10 @@ def test_mixed_config1_full_run(oracle):
 
 
 def test_mixed_vs_fp64_config2_size():
-    # The Gaussian-pulse grid (32^3 x 8^3, Gaussian pulse, dt 2e-4), 50 steps: mixed vs
-    # the plain FP64 CUDA path (which matches the oracle to 1e-12 per step)
+    # The Gaussian-pulse grid (32^3 x 8^3, Gaussian pulse, dt 2e-4) over its full 500 steps:
+    # mixed vs the plain FP64 CUDA path (which matches the oracle to 1e-12 per step)
     bricks = [Brick((32, 32, 32))]
-    n, dt, steps = 8, 2e-4, 50
+    n, dt, steps = 8, 2e-4, 500
     params = np.array([[1.0, 0.5, np.pi, np.pi, np.pi]])
     with DgEvolution(bricks, n, precision=PRECISION_FP64) as a:
         a.set_initial_data("gaussian", params)

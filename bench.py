@@ -756,6 +756,8 @@ def run_ours(args):
     mixed = None
     if not args.no_mixed:
         evm, msm, _, statem, _ = time_path(args, PRECISION_MIXED, dev, rank, ws, False)
+        # the launch shape the autotuner chose, re-timed after the timed region
+        mixed_tune = evm.tune()
         evm.close()
         err = float(np.linalg.norm(statem - state64) / np.linalg.norm(state64))
         launch_m = msm / (3 * args.steps)
@@ -764,6 +766,7 @@ def run_ours(args):
                  "ms_per_step": msm / args.steps,
                  "speedup_vs_fp64": ms / msm,
                  "rel_l2_vs_fp64_after_steps": err, "steps_compared": warm + args.steps,
+                 "tune": mixed_tune,
                  "dtype": "f32 split-product contractions, f64 state and step accumulation",
                  "roofline": {"bound": "hbm", "achieved": gbs_m, "peak": hbm, "unit": "GB/s",
                               "frac": gbs_m / hbm,

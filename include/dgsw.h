@@ -368,7 +368,9 @@ int dgsw_autotune(DgswHandle h, int force_variant, int* variant, double* ms_per_
  * configurations, as dgsw_autotune), DGSW_TUNE_MIXED_BATCH (mixed precision
  * on elements of differing extents: the persistent batch kernels' compiled
  * launch shapes -- threads per CTA, resident CTAs per SM, pipeline buffers,
- * largest extent), or DGSW_TUNE_NONE (fixed configurations).  Re-times every
+ * largest extent), DGSW_TUNE_MIXED_PIPE (mixed precision on one even extent:
+ * the pipelined kernel with two pipeline buffers, or one buffer and more
+ * resident CTAs), or DGSW_TUNE_NONE (fixed configurations).  Re-times every
  * candidate now on the handle's own state (saved and restored), keeps the
  * fastest (force_variant >= 0 imposes one instead) and returns the number of
  * candidates, the choice and ms per step of each (ms_per_step holds
@@ -376,7 +378,12 @@ int dgsw_autotune(DgswHandle h, int force_variant, int* variant, double* ms_per_
  * domain).  The first dgsw_step of a handle runs the same timing when its
  * shape has not been tuned in this process.  No counterpart in the
  * reference. */
-enum { DGSW_TUNE_NONE = 0, DGSW_TUNE_FP64_STAGE = 1, DGSW_TUNE_MIXED_BATCH = 2 };
+enum {
+  DGSW_TUNE_NONE = 0,
+  DGSW_TUNE_FP64_STAGE = 1,
+  DGSW_TUNE_MIXED_BATCH = 2,
+  DGSW_TUNE_MIXED_PIPE = 3
+};
 #define DGSW_TUNE_MAX_VARIANTS 8
 int dgsw_tune(DgswHandle h, int force_variant, int* family, int* n_variants, int* variant,
               double* ms_per_step);

@@ -91,6 +91,10 @@ struct DgswHandle_ {
       bt_grid[kBtVariants][2] = {};
   double bt_tune_ms[kBtVariants] = {};
   bool bt_tuned = false;
+  // launch shape of the uniform-extent pipelined mixed kernel (stage_mixed_pipe.cu)
+  int pipe_variant = 0;
+  bool pipe_tuned = false;
+  double pipe_tune_ms[2] = {0.0, 0.0};
   int bt_fu_age = 0;  // steps since the state's face values were formed from it
   // misfit objective and discrete adjoint (uniform FP64 path)
   EoTable eoT{};
@@ -276,6 +280,7 @@ MixedLaunch base_mixed(DgswHandle h) {
   L.jac = h->jac;
   L.eo = h->eo;
   L.err = h->dev_err;
+  L.variant = h->pipe_variant;
   return L;
 }
 
@@ -689,11 +694,59 @@ int autotune(DgswHandle h, bool force) {
   return DGSW_OK;
 }
 
+cudaError_t enqueue_step(DgswHandle h, double dt);
+
+// Times whole steps of each launch shape v < nv for which select(v) (which
+// also puts the shape in place) is true, on the handle's own state: the
+// state is saved first and restored after each candidate.  ms[v] is 0 for
+// shapes not timed; *best is the fastest (-1 if none).
+template <typename Select>
+cudaError_t time_step_shapes(DgswHandle h, int nv, Select select, double* ms, int* best) {
+  const size_t bytes = h->dom.offset.back() * sizeof(double);
+  cudaError_t err = cudaMemcpyAsync(h->u0s, h->state, bytes, cudaMemcpyDeviceToDevice, h->stream);
+  if (err != cudaSuccess) return err;
+  cudaEvent_t e0, e1;
+  if ((err = cudaEventCreate(&e0)) != cudaSuccess) return err;
+  if ((err = cudaEventCreate(&e1)) != cudaSuccess) {
+    cudaEventDestroy(e0);
+    return err;
+  }
+  const double dt = 1e-9;  // the state is restored: any step will do
+  double fastest = 0.0;
+  *best = -1;
+  for (int v = 0; v < nv && err == cudaSuccess; ++v) {
+    ms[v] = 0.0;
+    if (!select(v)) continue;
+    if (h->batch) err = batch_state_faces(h);  // warm-up step (attributes, caches)
+    if (err == cudaSuccess) err = enqueue_step(h, dt);
+    if (err == cudaSuccess)
+      err = cudaMemcpyAsync(h->state, h->u0s, bytes, cudaMemcpyDeviceToDevice, h->stream);
+    if (err == cudaSuccess && h->batch) err = batch_state_faces(h);
+    if (err == cudaSuccess) err = cudaEventRecord(e0, h->stream);
+    for (int r = 0; r < 2 && err == cudaSuccess; ++r) err = enqueue_step(h, dt);
+    if (err == cudaSuccess) err = cudaEventRecord(e1, h->stream);
+    if (err == cudaSuccess) err = cudaEventSynchronize(e1);
+    float t = 0.0f;
+    if (err == cudaSuccess) err = cudaEventElapsedTime(&t, e0, e1);
+    if (err == cudaSuccess)
+      err = cudaMemcpyAsync(h->state, h->u0s, bytes, cudaMemcpyDeviceToDevice, h->stream);
+    ms[v] = t / 2.0;
+    if (err == cudaSuccess && (*best < 0 || ms[v] < fastest)) {
+      fastest = ms[v];
+      *best = v;
+    }
+  }
+  cudaEventDestroy(e0);
+  cudaEventDestroy(e1);
+  if (err == cudaSuccess) err = cudaStreamSynchronize(h->stream);
+  return err;
+}
+
 // Launch autotuner of the mixed-precision batch path: every compiled launch
 // shape valid for the domain (threads per CTA, resident CTAs, pipeline
 // buffers, largest extent) is timed over whole steps on the handle's own
-// state, which is saved first and restored after; the fastest is kept for
-// the handle and for handles of the same shape in this process.
+// state; the fastest is kept for the handle and for handles of the same
+// shape in this process.
 std::map<std::tuple<int64_t, int64_t, int>, int> g_batch_tuned;
 
 int batch_autotune(DgswHandle h, bool force) {
@@ -708,50 +761,67 @@ int batch_autotune(DgswHandle h, bool force) {
       return DGSW_OK;
     }
   }
-  const size_t bytes = h->dom.offset.back() * sizeof(double);
-  DGSW_CUDA(h, cudaMemcpyAsync(h->u0s, h->state, bytes, cudaMemcpyDeviceToDevice, h->stream));
-  cudaEvent_t e0, e1;
-  DGSW_CUDA(h, cudaEventCreate(&e0));
-  DGSW_CUDA(h, cudaEventCreate(&e1));
-  const double dt = 1e-9;  // the state is restored: any step will do
   const int keep = h->bt_variant;
-  int choice = -1;
-  double best = 0.0;
-  cudaError_t err = cudaSuccess;
-  for (int v = 0; v < batch_variants() && err == cudaSuccess; ++v) {
-    h->bt_tune_ms[v] = 0.0;
-    if (h->bt_nmax > batch_max_extent(v) || h->bt_grid[v][0] <= 0 || h->bt_grid[v][1] <= 0) continue;
-    h->bt_variant = v;
-    err = batch_state_faces(h);  // warm-up step (attributes, caches)
-    if (err == cudaSuccess) err = enqueue_batch_step(h, dt);
-    if (err == cudaSuccess)
-      err = cudaMemcpyAsync(h->state, h->u0s, bytes, cudaMemcpyDeviceToDevice, h->stream);
-    if (err == cudaSuccess) err = batch_state_faces(h);
-    if (err == cudaSuccess) err = cudaEventRecord(e0, h->stream);
-    for (int r = 0; r < 2 && err == cudaSuccess; ++r) err = enqueue_batch_step(h, dt);
-    if (err == cudaSuccess) err = cudaEventRecord(e1, h->stream);
-    if (err == cudaSuccess) err = cudaEventSynchronize(e1);
-    float ms = 0.0f;
-    if (err == cudaSuccess) err = cudaEventElapsedTime(&ms, e0, e1);
-    if (err == cudaSuccess)
-      err = cudaMemcpyAsync(h->state, h->u0s, bytes, cudaMemcpyDeviceToDevice, h->stream);
-    h->bt_tune_ms[v] = ms / 2.0;
-    if (err == cudaSuccess && (choice < 0 || ms / 2.0 < best)) {
-      best = ms / 2.0;
-      choice = v;
-    }
-  }
-  cudaEventDestroy(e0);
-  cudaEventDestroy(e1);
-  if (err == cudaSuccess) err = cudaStreamSynchronize(h->stream);
+  int best = -1;
+  cudaError_t err = time_step_shapes(
+      h, batch_variants(),
+      [&](int v) {
+        if (h->bt_nmax > batch_max_extent(v) || h->bt_grid[v][0] <= 0 || h->bt_grid[v][1] <= 0)
+          return false;
+        h->bt_variant = v;
+        return true;
+      },
+      h->bt_tune_ms, &best);
   if (err != cudaSuccess) {
     h->bt_variant = keep;
     return cuda_fail(h, err, "batch autotune");
   }
-  if (choice >= 0) h->bt_variant = choice;
+  h->bt_variant = best >= 0 ? best : keep;
   h->bt_tuned = true;
   std::lock_guard<std::mutex> lk(g_tune_mu);
   g_batch_tuned[key] = h->bt_variant;
+  return DGSW_OK;
+}
+
+// The uniform-extent mixed path on the pipelined kernel (even extents): its
+// two launch shapes (two pipeline buffers, or one with more resident CTAs)
+// timed the same way, cached per (extent, elements).
+bool pipe_tunable(DgswHandle h) {
+  return mixed(h) && !h->batch && !h->curved && !h->general && !h->gauss && !h->refined &&
+         !h->adams && mixed_pipe_supported(h->dom.elem_n[0]);
+}
+
+std::map<std::pair<int, int64_t>, int> g_pipe_tuned;
+
+int pipe_autotune(DgswHandle h, bool force) {
+  if (!pipe_tunable(h) || (h->pipe_tuned && !force)) return DGSW_OK;
+  const std::pair<int, int64_t> key(h->dom.elem_n[0], h->dom.n_elem);
+  if (!force) {
+    std::lock_guard<std::mutex> lk(g_tune_mu);
+    auto it = g_pipe_tuned.find(key);
+    if (it != g_pipe_tuned.end()) {
+      h->pipe_variant = it->second;
+      h->pipe_tuned = true;
+      return DGSW_OK;
+    }
+  }
+  const int keep = h->pipe_variant;
+  int best = -1;
+  cudaError_t err = time_step_shapes(
+      h, 2,
+      [&](int v) {
+        h->pipe_variant = v;
+        return true;
+      },
+      h->pipe_tune_ms, &best);
+  if (err != cudaSuccess) {
+    h->pipe_variant = keep;
+    return cuda_fail(h, err, "pipeline autotune");
+  }
+  h->pipe_variant = best >= 0 ? best : keep;
+  h->pipe_tuned = true;
+  std::lock_guard<std::mutex> lk(g_tune_mu);
+  g_pipe_tuned[key] = h->pipe_variant;
   return DGSW_OK;
 }
 
@@ -2542,6 +2612,17 @@ int dgsw_tune(DgswHandle h, int force_variant, int* family, int* n_variants, int
     if (force_variant >= 0) h->bt_variant = force_variant;
     v = h->bt_variant;
     for (int i = 0; i < nv && i < DGSW_TUNE_MAX_VARIANTS; ++i) ms[i] = h->bt_tune_ms[i];
+  } else if (pipe_tunable(h)) {
+    fam = DGSW_TUNE_MIXED_PIPE;
+    nv = 2;
+    if (force_variant >= nv || force_variant < -1)
+      return fail(h, DGSW_ERR_ARGUMENT, "force_variant out of range");
+    destroy_graphs(h);
+    if (int rc = pipe_autotune(h, true)) return rc;
+    if (force_variant >= 0) h->pipe_variant = force_variant;
+    v = h->pipe_variant;
+    ms[0] = h->pipe_tune_ms[0];
+    ms[1] = h->pipe_tune_ms[1];
   } else if (tunable(h)) {
     fam = DGSW_TUNE_FP64_STAGE;
     nv = 2;
@@ -2725,6 +2806,10 @@ static int step_impl(DgswHandle h, int n_steps, double dt) {
   if (h->batch && !h->bt_tuned) {
     destroy_graphs(h);
     if (int rc = batch_autotune(h, false)) return rc;
+  }
+  if (pipe_tunable(h) && !h->pipe_tuned) {
+    destroy_graphs(h);
+    if (int rc = pipe_autotune(h, false)) return rc;
   }
   if (!(h->graph_dt == dt)) {
     destroy_graphs(h);

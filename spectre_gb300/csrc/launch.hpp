@@ -126,6 +126,7 @@ struct MixedLaunch {
   double alpha = 0.0, beta = 0.0, c = 1.0;
   EoTable eo{};
   int* err = nullptr;  // device error word (bounded waits that timed out)
+  int variant = 0;     // launch shape of the pipelined kernel (0 or 1)
 };
 
 cudaError_t launch_stage_mixed(const MixedLaunch& L, cudaStream_t s);

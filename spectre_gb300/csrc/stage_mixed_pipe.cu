@@ -56,7 +56,8 @@ struct Lay {
   static constexpr int kHiLo = 0;  // the double-float split is done as values are read
   static constexpr int kS = round128(S::NP * 4);
   static constexpr int kTab = round128((COMP ? 2 : 1) * 3 * S::TAB2 * 8);
-  static constexpr int kSlot = 2 * kBuf + kHiLo + kS + kTab;
+  static constexpr int kSlot = 2 * kBuf + kHiLo + kS + kTab;  // two pipeline buffers
+  static constexpr int kSlot1 = kBuf + kHiLo + kS + kTab;     // one
   // bytes the TMA copies of one element move (unpadded)
   static constexpr uint32_t kXBytes = COMP ? 4 * S::NP * 8 : 5 * S::NP * 4;
   static constexpr uint32_t kYBytes = HAS_Y ? 5 * S::NP * 4 : 0;
@@ -97,10 +98,13 @@ __device__ __forceinline__ void eo_line_pdf(const float (&xh)[N], const float (&
   }
 #pragma unroll
   for (int i = 0; i < h; ++i) {
+    // s: running sum of the products' high parts; the corrections are three
+    // independent sums (rounding errors of s and of the products; the
+    // table's low parts; the data's low parts), added at the end
     float2 s = mul2(th[i * h], eoh[0]);
-    float2 c = fma2(th[i * h], eoh[0], neg2(s));
-    c = fma2(tl[i * h], eoh[0], c);
-    c = fma2(th[i * h], eol[0], c);
+    float2 c1 = fma2(th[i * h], eoh[0], neg2(s));
+    float2 c2 = mul2(tl[i * h], eoh[0]);
+    float2 c3 = mul2(th[i * h], eol[0]);
 #pragma unroll
     for (int j = 1; j < h; ++j) {
       const float2 a = th[i * h + j];
@@ -108,18 +112,23 @@ __device__ __forceinline__ void eo_line_pdf(const float (&xh)[N], const float (&
       const float2 pe = fma2(a, eoh[j], neg2(p));
       float2 t;
       two_sum2(s, p, s, t);
-      c = add2(c, add2(t, pe));
-      c = fma2(tl[i * h + j], eoh[j], c);
-      c = fma2(a, eol[j], c);
+      c1 = add2(c1, add2(t, pe));
+      c2 = fma2(tl[i * h + j], eoh[j], c2);
+      c3 = fma2(a, eol[j], c3);
     }
+    const float2 c = add2(c1, add2(c2, c3));
     // lanes: x = P_i (even part), y = Q_i (odd part)
     out[i] = (s.x + s.y) + (c.x + c.y);
     out[N - 1 - i] = (s.y - s.x) + (c.y - c.x);
   }
 }
 
-template <int N, int EPB, bool COMP, bool HAS_Y, bool HAS_B>
-__global__ void __launch_bounds__(N * N * EPB)
+// STAGES pipeline buffers per element slot (2: the next group's copies land
+// while this one computes; 1: they are issued when this one is done, and the
+// other resident CTAs -- MINB asked of the register allocator -- cover the
+// wait).
+template <int N, int EPB, bool COMP, bool HAS_Y, bool HAS_B, int STAGES, int MINB>
+__global__ void __launch_bounds__(N * N * EPB, MINB)
     stage_mixed_pipe_kernel(MixedLaunch L, int64_t n_groups) {
   using S = P<N>;
   using Y = Lay<N, COMP, HAS_Y, HAS_B>;
@@ -131,10 +140,11 @@ __global__ void __launch_bounds__(N * N * EPB)
   __shared__ uint64_t bars[2];
   const int slot = threadIdx.x / NN;
   const int t = threadIdx.x - slot * NN;
-  unsigned char* slot_base = smem_raw + (size_t)slot * Y::kSlot;
-  unsigned char* bufs[2] = {slot_base, slot_base + Y::kBuf};
-  float* Sacc = reinterpret_cast<float*>(slot_base + 2 * Y::kBuf + Y::kHiLo);
-  float2* tab = reinterpret_cast<float2*>(slot_base + 2 * Y::kBuf + Y::kHiLo + Y::kS);
+  constexpr int kSlotBytes = STAGES == 2 ? Y::kSlot : Y::kSlot1;
+  unsigned char* slot_base = smem_raw + (size_t)slot * kSlotBytes;
+  unsigned char* bufs[2] = {slot_base, slot_base + (STAGES - 1) * Y::kBuf};
+  float* Sacc = reinterpret_cast<float*>(slot_base + STAGES * Y::kBuf + Y::kHiLo);
+  float2* tab = reinterpret_cast<float2*>(slot_base + STAGES * Y::kBuf + Y::kHiLo + Y::kS);
   const int ta = t % N, tb = t / N;
   const uint64_t kLimitNs = 2000000000ull;  // 2 s per wait
 
@@ -159,7 +169,7 @@ __global__ void __launch_bounds__(N * N * EPB)
     for (int s = 0; s < EPB; ++s) {
       const int64_t e = g * EPB + s;
       if (e >= L.n_elem) break;
-      unsigned char* dst = smem_raw + (size_t)s * Y::kSlot + (size_t)b * Y::kBuf;
+      unsigned char* dst = smem_raw + (size_t)s * kSlotBytes + (size_t)b * Y::kBuf;
       if (COMP)
         bulk_g2s(dst, L.x64 + e * VS + NP, Y::kXBytes, &bars[b]);
       else
@@ -206,11 +216,12 @@ __global__ void __launch_bounds__(N * N * EPB)
   }
   const float alpha = (float)L.alpha, beta = (float)L.beta, cf = (float)L.c;
   for (int k = 0; g < n_groups; ++k, g += G) {
-    const int b = k & 1;
+    const int b = STAGES == 2 ? (k & 1) : 0;
+    const uint32_t parity = STAGES == 2 ? (uint32_t)((k >> 1) & 1) : (uint32_t)(k & 1);
     const int64_t gn = g + G;
     const int64_t e = g * EPB + slot;
     const bool active = e < L.n_elem;
-    if (threadIdx.x == 0 && gn < n_groups) issue_group(gn, b ^ 1);
+    if (STAGES == 2 && threadIdx.x == 0 && gn < n_groups) issue_group(gn, b ^ 1);
     // scaled split tables for this element (depend only on its Jacobian)
     double jd[3] = {0.0, 0.0, 0.0};
     if (active) {
@@ -228,17 +239,33 @@ __global__ void __launch_bounds__(N * N * EPB)
               make_float2(__double2float_rn(va - (double)ah), __double2float_rn(vb - (double)bh));
       }
     }
-    const bool landed = mbar_wait(&bars[b], (uint32_t)((k >> 1) & 1), kLimitNs);
+    const bool landed = mbar_wait(&bars[b], parity, kLimitNs);
     cp_async_wait_all();
     if (__syncthreads_or(!landed)) {
       // a copy did not land in time: record it, give copies still in flight
       // one more bounded wait, and leave together
       if (threadIdx.x == 0 && L.err) atomicExch(L.err, 1);
-      if (!landed) mbar_wait(&bars[b], (uint32_t)((k >> 1) & 1), kLimitNs);
+      if (!landed) mbar_wait(&bars[b], parity, kLimitNs);
+      if (STAGES == 2 && threadIdx.x == 0 && gn < n_groups)
+        mbar_wait(&bars[b ^ 1], (uint32_t)(((k + 1) >> 1) & 1), kLimitNs);
       return;
     }
     const unsigned char* buf = bufs[b];
+    if (COMP) {
+      // each FP64 value of the staged X becomes its (hi, lo) FP32 pair in
+      // place, so that the passes split each value once
+      if (active) {
+        double* Xs = reinterpret_cast<double*>(bufs[b]);
+        for (int q = t; q < 4 * NP; q += NN) {
+          float hi, lo;
+          split_df(Xs[q], hi, lo);
+          reinterpret_cast<float2*>(Xs)[q] = make_float2(hi, lo);
+        }
+      }
+      __syncthreads();
+    }
     const FT* X = reinterpret_cast<const FT*>(buf);
+    const float2* X2 = reinterpret_cast<const float2*>(buf);
     const float* Yb = reinterpret_cast<const float*>(buf + Y::kX);
     const double* Bb = reinterpret_cast<const double*>(buf + Y::kX + Y::kY);
     const FT* face = reinterpret_cast<const FT*>(buf + Y::kX + Y::kY + Y::kB);
@@ -262,11 +289,14 @@ __global__ void __launch_bounds__(N * N * EPB)
         float dF[N], dP[N], pih[N], fh[N];
         float pil[N], fl[N];
         if (COMP) {
-          // X holds Pi, Phi_x, Phi_y, Phi_z in FP64; split as read
+          // X holds Pi, Phi_x, Phi_y, Phi_z as (hi, lo) FP32 pairs
 #pragma unroll
           for (int i = 0; i < N; ++i) {
-            split_df((double)X[base + i * stride], pih[i], pil[i]);
-            split_df((double)X[(1 + d) * NP + base + i * stride], fh[i], fl[i]);
+            const float2 vp = X2[base + i * stride], vf = X2[(1 + d) * NP + base + i * stride];
+            pih[i] = vp.x;
+            pil[i] = vp.y;
+            fh[i] = vf.x;
+            fl[i] = vf.y;
           }
           eo_line_pdf<N>(fh, fl, dF, th, tl);
           eo_line_pdf<N>(pih, pil, dP, th, tl);
@@ -368,10 +398,20 @@ __global__ void __launch_bounds__(N * N * EPB)
       }
       if (d < 2) __syncthreads();
     }
-    // neighbour faces of the next group, then release this buffer
-    if (gn < n_groups) issue_faces(gn * EPB + slot, b ^ 1);
-    cp_async_commit();
+    // neighbour faces of the next group, then release this buffer (the
+    // in-place split wrote it: order those generic writes before the next
+    // TMA writes into it)
+    if (STAGES == 2) {
+      if (gn < n_groups) issue_faces(gn * EPB + slot, b ^ 1);
+      cp_async_commit();
+    }
+    if (COMP) fence_proxy_async_smem();
     __syncthreads();
+    if (STAGES == 1 && gn < n_groups) {
+      if (threadIdx.x == 0) issue_group(gn, 0);
+      issue_faces(gn * EPB + slot, 0);
+      cp_async_commit();
+    }
   }
   cp_async_wait_all();
 }
@@ -391,14 +431,30 @@ constexpr int pipe_epb() {
   return fit < pipe_epb_target<N>() ? fit : pipe_epb_target<N>();
 }
 
+// Launch shapes: 0 two pipeline buffers, 1 one buffer and MINB = 4 resident
+// CTAs asked of the register allocator (the FP32 stages ask for 6).
+template <int N, bool COMP, bool HAS_Y, bool HAS_B, int V>
+cudaError_t launch_pipe_v(const MixedLaunch& L, cudaStream_t s);
+
 template <int N, bool COMP, bool HAS_Y, bool HAS_B>
 cudaError_t launch_pipe(const MixedLaunch& L, cudaStream_t s) {
+  // the single-buffered shape is compiled for the step's three stages only
+  if constexpr (!HAS_B) {
+    if (L.variant == 1) return launch_pipe_v<N, COMP, HAS_Y, HAS_B, 1>(L, s);
+  }
+  return launch_pipe_v<N, COMP, HAS_Y, HAS_B, 0>(L, s);
+}
+
+template <int N, bool COMP, bool HAS_Y, bool HAS_B, int V>
+cudaError_t launch_pipe_v(const MixedLaunch& L, cudaStream_t s) {
   constexpr int EPB_FIT = pipe_epb<N, COMP, HAS_Y, HAS_B>();
   if (EPB_FIT < 1) return launch_stage_mixed(L, s);  // too large to double-buffer
   constexpr int EPB = EPB_FIT < 1 ? 1 : EPB_FIT;
+  constexpr int STAGES = V == 1 ? 1 : 2;
+  constexpr int MINB = V == 1 ? (COMP ? 4 : 6) : 1;
   using Y = Lay<N, COMP, HAS_Y, HAS_B>;
-  const size_t smem = (size_t)EPB * Y::kSlot;
-  auto k = stage_mixed_pipe_kernel<N, EPB, COMP, HAS_Y, HAS_B>;
+  const size_t smem = (size_t)EPB * (STAGES == 2 ? Y::kSlot : Y::kSlot1);
+  auto k = stage_mixed_pipe_kernel<N, EPB, COMP, HAS_Y, HAS_B, STAGES, MINB>;
   cudaError_t err = cudaFuncSetAttribute(k, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
   if (err != cudaSuccess) return err;
   err = cudaFuncSetAttribute(k, cudaFuncAttributePreferredSharedMemoryCarveout,

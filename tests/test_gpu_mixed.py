@@ -108,3 +108,28 @@ def test_mixed_rejects_gamma2():
     with pytest.raises(dgsw.DgswError) as ei:
         DgEvolution([Brick((2, 2, 2))], 4, precision=PRECISION_MIXED, gamma2=1.0)
     assert ei.value.status == -3
+
+
+@pytest.mark.parametrize("n", [6, 8])
+def test_mixed_pipe_launch_shapes_agree(oracle, n):
+    # the pipelined kernel's two launch shapes (dgsw_tune): same bits, and
+    # both within the mixed bar of the FP64 oracle
+    bricks = [Brick((4, 4, 3))]
+    dt, steps = 1e-3, 30
+    u0 = oracle.initial_data(bricks, n, "plane_wave", [1, 1, 1])
+    ref = oracle.evolve(bricks, n, u0, dt, steps)
+    out = []
+    with DgEvolution(bricks, n, precision=PRECISION_MIXED) as ev:
+        ev.set_state(u0)
+        info = ev.tune()
+        assert info["family"] == "mixed_pipe"
+        assert np.array_equal(ev.get_state(), u0)
+        assert all(ms > 0 for ms in info["ms_per_step"])
+        for v in range(len(info["ms_per_step"])):
+            assert ev.tune(force_variant=v)["variant"] == v
+            ev.set_state(u0)
+            ev.step(steps, dt)
+            out.append(ev.get_state())
+    for got in out:
+        assert rel_l2(got, ref) <= 1e-6
+    np.testing.assert_array_equal(out[0], out[1])

@@ -83,12 +83,11 @@ struct DgswHandle_ {
   float* bt_fw1 = nullptr;
   float* bt_fw2 = nullptr;
   float* bt_fw3 = nullptr;
-  EoTable* bt_eo = nullptr;
+  float* bt_dtab = nullptr;
   // per variant and precision (0: FP64 input, 1: FP32): shared-memory regions
   // and resident grid
   static constexpr int kBtVariants = 8;
-  int bt_buf[kBtVariants][2] = {}, bt_s[kBtVariants][2] = {}, bt_tab[kBtVariants][2] = {},
-      bt_grid[kBtVariants][2] = {};
+  int bt_buf[kBtVariants][2] = {}, bt_s[kBtVariants][2] = {}, bt_grid[kBtVariants][2] = {};
   double bt_tune_ms[kBtVariants] = {};
   bool bt_tuned = false;
   // launch shape of the uniform-extent pipelined mixed kernel (stage_mixed_pipe.cu)
@@ -316,14 +315,13 @@ BatchLaunch base_batch(DgswHandle h, bool comp) {
   B.elem_n = h->elem_n;
   B.nbr = h->nbr;
   B.jac = h->jac;
-  B.eo = h->bt_eo;
+  B.dtab = h->bt_dtab;
   B.op_hi = h->op_hi;
   B.op_off = h->op_off;
   B.err = h->dev_err;
   const int i = comp ? 0 : 1;
   B.buf_bytes = h->bt_buf[v][i];
   B.s_bytes = h->bt_s[v][i];
-  B.tab_bytes = h->bt_tab[v][i];
   B.grid = h->bt_grid[v][i];
   return B;
 }
@@ -1830,9 +1828,9 @@ int batch_init(DgswHandle h) {
       (e = cudaMemset(h->bt_fw2, 0, h->bt_fsize * sizeof(float) + pad)) != cudaSuccess ||
       (e = cudaMemset(h->bt_fw3, 0, h->bt_fsize * sizeof(float) + pad)) != cudaSuccess)
     return cuda_fail(h, e, "clear face buffers");
-  std::vector<EoTable> eo(kMaxN + 1);
-  for (int n = kMinN; n <= kMaxN; ++n) lgl_eo_table(n, &eo[n]);
-  if ((e = upload(&h->bt_eo, eo)) != cudaSuccess) return cuda_fail(h, e, "upload split tables");
+  std::vector<float> dtab;
+  batch_split_tables(&dtab);
+  if ((e = upload(&h->bt_dtab, dtab)) != cudaSuccess) return cuda_fail(h, e, "upload split tables");
   constexpr int64_t kWindow = 256;
   bool present[kMaxN + 1] = {};
   for (int64_t el = 0; el < E; ++el) present[h->dom.elem_n[el]] = true;
@@ -1867,21 +1865,19 @@ int batch_init(DgswHandle h) {
   for (int v = 0; v < batch_variants(); ++v) {
     if (h->bt_nmax > batch_max_extent(v)) continue;
     for (int i = 0; i < 2; ++i) {
-      size_t buf = 0, sb = 0, tb = 0;
+      size_t buf = 0, sb = 0;
       for (int n = kMinN; n <= kMaxN; ++n) {
         if (!present[n]) continue;
-        size_t b1, s1, t1;
-        batch_smem_bytes(n, i == 0, v, &b1, &s1, &t1);
+        size_t b1, s1;
+        batch_smem_bytes(n, i == 0, v, &b1, &s1);
         buf = std::max(buf, b1);
         sb = std::max(sb, s1);
-        tb = std::max(tb, t1);
       }
-      const size_t total = batch_smem_total(v, buf, sb, tb);
+      const size_t total = batch_smem_total(v, buf, sb);
       if (total > 227 * 1024)
         return fail(h, DGSW_ERR_UNSUPPORTED, "batch stage: shared memory of a task exceeds 227 KB");
       h->bt_buf[v][i] = (int)buf;
       h->bt_s[v][i] = (int)sb;
-      h->bt_tab[v][i] = (int)tb;
       if ((e = batch_grid(i == 0, v, total, &h->bt_grid[v][i])) != cudaSuccess)
         return cuda_fail(h, e, "batch stage occupancy");
     }
@@ -2183,7 +2179,7 @@ int dgsw_destroy(DgswHandle h) {
   }
   if (h->pnc_face_idx) cudaFree(h->pnc_face_idx);
   void* bt[] = {h->bt_tasks[0], h->bt_tasks[1], h->bt_elems[0], h->bt_elems[1], h->bt_foff,
-                h->bt_fu, h->bt_fw1, h->bt_fw2, h->bt_fw3, h->bt_eo};
+                h->bt_fu, h->bt_fw1, h->bt_fw2, h->bt_fw3, h->bt_dtab};
   for (void* p : bt)
     if (p) cudaFree(p);
   if (h->op64) cudaFree(h->op64);

@@ -4,6 +4,7 @@
 
 #include <atomic>
 #include <cstdint>
+#include <vector>
 #include <cuda_runtime.h>
 
 #include "adams.hpp"
@@ -155,7 +156,8 @@ struct BatchLaunch {
   const int32_t* elem_n = nullptr;
   const int32_t* nbr = nullptr;
   const double* jac = nullptr;
-  const EoTable* eo = nullptr;      // device, [kMaxN + 1]
+  const float* dtab = nullptr;      // device: unscaled split tables of every extent
+                                    // (batch_split_tables), hi then lo
   const float* op_hi = nullptr;     // face operators T (n x nn) at op_off[n (kMaxN+1) + nn]
   const int32_t* op_off = nullptr;
   const double* x64 = nullptr;      // X (kPrecComp): FP64 state
@@ -166,21 +168,25 @@ struct BatchLaunch {
   float* fw32 = nullptr;            // optional: face values of W for the next stage
   double alpha = 0.0, c = 1.0;
   int* err = nullptr;               // device error word (bounded waits that timed out)
-  int buf_bytes = 0, s_bytes = 0, tab_bytes = 0;  // shared-memory regions
+  int buf_bytes = 0, s_bytes = 0;   // shared-memory regions
   int grid = 0;
 };
 cudaError_t launch_stage_batch(const BatchLaunch& L, cudaStream_t s);
 // The compiled launch shapes (variants): threads per CTA and largest extent;
-// elements per task of extent n; shared-memory bytes of a launch whose tasks
-// have extent n (its regions in *buf, *s, *tab).
+// elements per task of extent n; the shared-memory regions a launch whose
+// tasks have extent n needs (*buf pipeline buffer, *s accumulator).
 int batch_variants();
 int batch_threads(int variant);
 int batch_max_extent(int variant);
 int batch_task_elements(int n, int variant);
-void batch_smem_bytes(int n, bool comp, int variant, size_t* buf, size_t* s, size_t* tab);
-// the launch's shared memory for the given region sizes (pipeline buffers,
-// accumulator, tables and the face maps' scratch)
-size_t batch_smem_total(int variant, size_t buf, size_t s, size_t tab);
+void batch_smem_bytes(int n, bool comp, int variant, size_t* buf, size_t* s);
+// the launch's dynamic shared memory for the given region sizes (pipeline
+// buffers, accumulator and the face maps' scratch)
+size_t batch_smem_total(int variant, size_t buf, size_t s);
+// The split tables the batch kernels read (BatchLaunch.dtab): for every
+// extent 2..12 the even/odd split of the LGL D as FP32 hi parts, then the lo
+// parts; its length in floats.
+void batch_split_tables(std::vector<float>* out);
 // resident grid of the batch kernel with smem bytes of shared memory
 cudaError_t batch_grid(bool comp, int variant, size_t smem, int* grid);
 // The step's update of the FP64 state u (n values) by (double)(w + beta y),

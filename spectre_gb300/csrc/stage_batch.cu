@@ -52,6 +52,7 @@
 
 #include "common.cuh"
 #include "dg_device.cuh"
+#include "host_setup.hpp"
 #include "launch.hpp"
 #include "pipe.cuh"
 
@@ -74,6 +75,17 @@ constexpr uint64_t kLimitNs = 2000000000ull;  // 2 s per bounded wait
 __host__ __device__ constexpr int tab_stride(int n) {
   return 2 * (n / 2) * (n / 2) + ((n & 1) ? 2 * (n / 2) : 0);
 }
+
+// The unscaled split tables of every extent 2..12, one after another (the
+// hi parts, then the lo parts at kTabTotal): held once per CTA in shared
+// memory; the element's -c dxi/dx of each axis scales the contraction's
+// result instead.
+__host__ __device__ constexpr int tab_offset(int n) {
+  int o = 0;
+  for (int k = kMinN; k < n; ++k) o += tab_stride(k);
+  return o;
+}
+constexpr int kTabTotal = tab_offset(kMaxN + 1);
 
 // packed plain contraction (lanes: x = even part P, y = odd part Q)
 template <int N>
@@ -241,8 +253,8 @@ __device__ __forceinline__ int w_index(int f, int p, int np) {
 template <int N, bool COMP>
 __device__ __forceinline__ void task_passes(const BatchLaunch& L, const TaskView<COMP>& V,
                                             float* S, const float* tabs, const int g,
-                                            const float cf, const float* G) {
-  constexpr int NN = N * N, NP = NN * N, TS = tab_stride(N);
+                                            const float cf, const float* G, const float* F) {
+  constexpr int NN = N * N, NP = NN * N;
   const int slot = threadIdx.x / NN;
   const int t = threadIdx.x - slot * NN;
   const bool active = slot < g;
@@ -251,7 +263,8 @@ __device__ __forceinline__ void task_passes(const BatchLaunch& L, const TaskView
   unsigned char* xb = active ? V.x(slot) : nullptr;
   const unsigned char* fbk = active ? V.f(slot) : nullptr;
   float* Sl = S + slot * NP;
-  const float* th_all = tabs + slot * (COMP ? 2 : 1) * 3 * TS;
+  const float* th = tabs + tab_offset(N);
+  const float* tl = tabs + kTabTotal + tab_offset(N);
   const int64_t off = active ? V.offs[slot] : 0;
 #pragma unroll 1
   for (int d = 0; d < 3; ++d) {
@@ -268,9 +281,8 @@ __device__ __forceinline__ void task_passes(const BatchLaunch& L, const TaskView
         stride = NN;
       }
       const int fidx = ta + N * tb;
-      const float* th = th_all + d * TS;
-      const float* tl = th_all + 3 * TS + d * TS;
       const float Gd = G[slot * 3 + d];
+      const float Fd = F[slot * 3 + d];  // -c dxi/dx along this axis
       // the two lines one after the other (fewer live registers): Phi_d,
       // keeping its end values, then Pi
       float dF[N], dP[N], pih[N], pil[N];
@@ -288,6 +300,8 @@ __device__ __forceinline__ void task_passes(const BatchLaunch& L, const TaskView
             fl[i] = v.y;
           }
           eo_line_pdfg<N>(fh, fl, dF, th, tl);
+#pragma unroll
+          for (int i = 0; i < N; ++i) dF[i] *= Fd;
           f0h = fh[0];
           f0l = fl[0];
           f1h = fh[N - 1];
@@ -300,6 +314,8 @@ __device__ __forceinline__ void task_passes(const BatchLaunch& L, const TaskView
           pil[i] = v.y;
         }
         eo_line_pdfg<N>(pih, pil, dP, th, tl);
+#pragma unroll
+        for (int i = 0; i < N; ++i) dP[i] *= Fd;
         const float2* ext = reinterpret_cast<const float2*>(fbk);
         const float2 elo = ext[(2 * d) * NN + fidx], ehi = ext[(2 * d + 1) * NN + fidx];
         float wh, wl, t0, dh;
@@ -319,6 +335,8 @@ __device__ __forceinline__ void task_passes(const BatchLaunch& L, const TaskView
 #pragma unroll
           for (int i = 0; i < N; ++i) fh[i] = X[(2 + d) * NP + base + i * stride];
           eo_line_pg<N>(fh, dF, th);
+#pragma unroll
+          for (int i = 0; i < N; ++i) dF[i] *= Fd;
           f0h = fh[0];
           f1h = fh[N - 1];
           // alpha X_Phi_d enters the Phi_d output
@@ -334,7 +352,7 @@ __device__ __forceinline__ void task_passes(const BatchLaunch& L, const TaskView
           float dd[N];
           eo_line_pg<N>(pih, dd, th);
 #pragma unroll
-          for (int i = 0; i < N; ++i) dP[i] += dd[i];
+          for (int i = 0; i < N; ++i) dP[i] = fmaf(Fd, dd[i], dP[i]);
         }
         const float* ext = reinterpret_cast<const float*>(fbk);
         dw_lo = (pih[0] + f0h) - ext[(2 * d) * NN + fidx];
@@ -401,13 +419,18 @@ __device__ __forceinline__ void split_x(const TaskView<true>& V, int g, int bt) 
 // T (m x n, m the neighbour's extent) onto the neighbour's face points and
 // stored into the neighbour's slot opposite dir.  One warp per face; T, w and
 // the first sweep sit in the warp's scratch.
-template <bool COMP, int BT>
+// q / m for q < 144, 2 <= m <= 12 (exact: checked for every q and m)
+__device__ __forceinline__ int div_small(int q, int m) {
+  return (q * ((65536 + m - 1) / m)) >> 16;
+}
+
+template <int n, bool COMP, int BT>
 __device__ void task_faces(const BatchLaunch& L, const TaskView<COMP>& V, const int32_t* elems,
                            float* scratch) {
   constexpr int kWarps = BT / 32;
-  const int n = V.n, g = V.g;
+  constexpr int nn = n * n, np = nn * n;
+  const int g = V.g;
   const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
-  const int nn = n * n, np = nn * n;
   float* Ts = scratch + warp * kScratchFloats;
   float* wv = Ts + kMaxN * kMaxN;
   float* tv = wv + kMaxN * kMaxN;
@@ -435,14 +458,16 @@ __device__ void task_faces(const BatchLaunch& L, const TaskView<COMP>& V, const 
       for (int q = lane; q < n * m; q += 32) {
         const int pp = q % n, b = q / n;
         float acc = 0.0f;
+#pragma unroll
         for (int k = 0; k < n; ++k) acc = fmaf(Ts[b * n + k], wv[pp + n * k], acc);
         tv[q] = acc;
       }
       __syncwarp();
       // wv[a + m b] = sum_k T(a, k) tv[k + n b]
       for (int q = lane; q < m * m; q += 32) {
-        const int a = q % m, b = q / m;
+        const int b = div_small(q, m), a = q - b * m;
         float acc = 0.0f;
+#pragma unroll
         for (int k = 0; k < n; ++k) acc = fmaf(Ts[a * n + k], tv[k + n * b], acc);
         wv[q] = acc;
       }
@@ -455,29 +480,36 @@ __device__ void task_faces(const BatchLaunch& L, const TaskView<COMP>& V, const 
 
 template <int N, bool COMP, int BT>
 __device__ __forceinline__ void run_task(const BatchLaunch& L, const TaskView<COMP>& V, float* S,
-                                         const float* tabs, const float* G) {
+                                         const float* tabs, const float* G, const float* F,
+                                         const int32_t* elems, float* scratch) {
   if constexpr (COMP) {
     split_x<N>(V, V.g, BT);
     __syncthreads();
   }
-  task_passes<N, COMP>(L, V, S, tabs, V.g, (float)L.c, G);
+  task_passes<N, COMP>(L, V, S, tabs, V.g, (float)L.c, G, F);
+  if (L.fw32 != nullptr) {
+    __syncthreads();
+    task_faces<N, COMP, BT>(L, V, elems, scratch);
+  }
 }
 
 template <bool COMP, int BT, int NMAX>
 __device__ __forceinline__ void dispatch_task(const BatchLaunch& L, const TaskView<COMP>& V,
-                                              float* S, const float* tabs, const float* G) {
+                                              float* S, const float* tabs, const float* G,
+                                              const float* F, const int32_t* elems,
+                                              float* scratch) {
   switch (V.n) {
-    case 2: run_task<2, COMP, BT>(L, V, S, tabs, G); break;
-    case 3: run_task<3, COMP, BT>(L, V, S, tabs, G); break;
-    case 4: run_task<4, COMP, BT>(L, V, S, tabs, G); break;
-    case 5: run_task<5, COMP, BT>(L, V, S, tabs, G); break;
-    case 6: run_task<6, COMP, BT>(L, V, S, tabs, G); break;
-    case 7: run_task<7, COMP, BT>(L, V, S, tabs, G); break;
-    case 8: run_task<8, COMP, BT>(L, V, S, tabs, G); break;
-    case 9: if (NMAX >= 9) run_task<(NMAX >= 9 ? 9 : 2), COMP, BT>(L, V, S, tabs, G); break;
-    case 10: if (NMAX >= 10) run_task<(NMAX >= 10 ? 10 : 2), COMP, BT>(L, V, S, tabs, G); break;
-    case 11: if (NMAX >= 11) run_task<(NMAX >= 11 ? 11 : 2), COMP, BT>(L, V, S, tabs, G); break;
-    case 12: if (NMAX >= 12) run_task<(NMAX >= 12 ? 12 : 2), COMP, BT>(L, V, S, tabs, G); break;
+    case 2: run_task<2, COMP, BT>(L, V, S, tabs, G, F, elems, scratch); break;
+    case 3: run_task<3, COMP, BT>(L, V, S, tabs, G, F, elems, scratch); break;
+    case 4: run_task<4, COMP, BT>(L, V, S, tabs, G, F, elems, scratch); break;
+    case 5: run_task<5, COMP, BT>(L, V, S, tabs, G, F, elems, scratch); break;
+    case 6: run_task<6, COMP, BT>(L, V, S, tabs, G, F, elems, scratch); break;
+    case 7: run_task<7, COMP, BT>(L, V, S, tabs, G, F, elems, scratch); break;
+    case 8: run_task<8, COMP, BT>(L, V, S, tabs, G, F, elems, scratch); break;
+    case 9: if (NMAX >= 9) run_task<(NMAX >= 9 ? 9 : 2), COMP, BT>(L, V, S, tabs, G, F, elems, scratch); break;
+    case 10: if (NMAX >= 10) run_task<(NMAX >= 10 ? 10 : 2), COMP, BT>(L, V, S, tabs, G, F, elems, scratch); break;
+    case 11: if (NMAX >= 11) run_task<(NMAX >= 11 ? 11 : 2), COMP, BT>(L, V, S, tabs, G, F, elems, scratch); break;
+    case 12: if (NMAX >= 12) run_task<(NMAX >= 12 ? 12 : 2), COMP, BT>(L, V, S, tabs, G, F, elems, scratch); break;
     default: break;
   }
 }
@@ -495,11 +527,13 @@ __global__ void __launch_bounds__(BT, MINB) stage_batch_kernel(BatchLaunch L) {
   __shared__ int32_t s_elems[kMaxG];
   __shared__ int64_t s_offs[kMaxG];
   __shared__ float s_G[3 * kMaxG];
+  __shared__ float s_F[3 * kMaxG];
+  __shared__ __align__(16) float s_tab[2 * kTabTotal];
   unsigned char* bufs[2] = {smem, smem + (STAGES - 1) * L.buf_bytes};
   unsigned char* rest = smem + STAGES * L.buf_bytes;
   float* S = reinterpret_cast<float*>(rest);
-  float* tabs = reinterpret_cast<float*>(rest + L.s_bytes);
-  float* scratch = reinterpret_cast<float*>(rest + L.s_bytes + L.tab_bytes);
+  float* scratch = reinterpret_cast<float*>(rest + L.s_bytes);
+  for (int q = threadIdx.x; q < 2 * kTabTotal; q += BT) s_tab[q] = L.dtab[q];
 
   if (threadIdx.x == 0) {
     mbar_init(&bars[0], 1);
@@ -519,36 +553,15 @@ __global__ void __launch_bounds__(BT, MINB) stage_batch_kernel(BatchLaunch L) {
       issue_task<COMP>(L, L.tasks[next], bufs[b ^ 1], &bars[b ^ 1]);
     const int2 tk = L.tasks[task];
     const int n = tk.x & 0xff, g = tk.x >> 8;
-    const int ts = tab_stride(n);
-    // per-element data and the scaled split tables (overlap the copies)
+    // per-element data (overlaps the copies)
     if (threadIdx.x < g) {
       const int32_t e = L.task_elems[tk.y + threadIdx.x];
       s_elems[threadIdx.x] = e;
       s_offs[threadIdx.x] = L.offset[e];
-      for (int d = 0; d < 3; ++d)
-        s_G[3 * threadIdx.x + d] = (float)(-0.25 * c * (double)(n * (n - 1)) * L.jac[3 * (int64_t)e + d]);
-    }
-    {
-      const EoTable& eo = L.eo[n];
-      const int h = n / 2, odd = n & 1;
-      const int per = 3 * ts;
-      for (int q = threadIdx.x; q < g * per; q += BT) {
-        const int s = q / per, r = q - s * per, d = r / ts, rr = r - d * ts;
-        const int32_t e = L.task_elems[tk.y + s];
-        double v;
-        if (rr < 2 * h * h) {
-          const int pi = rr >> 1, i = pi / h, j = pi - i * h;
-          v = (rr & 1) ? eo.B[i][j] : eo.A[i][j];
-        } else if (odd && rr < 2 * h * h + h) {
-          v = eo.M[rr - 2 * h * h];
-        } else {
-          v = eo.B[h][rr - 2 * h * h - h];
-        }
-        const double sv = (-c * L.jac[3 * (int64_t)e + d]) * v;
-        const float hi = __double2float_rn(sv);
-        float* base = tabs + s * (COMP ? 2 : 1) * per;
-        base[r] = hi;
-        if (COMP) base[per + r] = __double2float_rn(sv - (double)hi);
+      for (int d = 0; d < 3; ++d) {
+        const double jd = L.jac[3 * (int64_t)e + d];
+        s_G[3 * threadIdx.x + d] = (float)(-0.25 * c * (double)(n * (n - 1)) * jd);
+        s_F[3 * threadIdx.x + d] = (float)(-c * jd);
       }
     }
     const bool landed = mbar_wait(&bars[b], parity, kLimitNs);
@@ -567,11 +580,7 @@ __global__ void __launch_bounds__(BT, MINB) stage_batch_kernel(BatchLaunch L) {
     V.L = &L;
     V.n = n;
     V.g = g;
-    dispatch_task<COMP, BT, NMAX>(L, V, S, tabs, s_G);
-    if (L.fw32 != nullptr) {
-      __syncthreads();
-      task_faces<COMP, BT>(L, V, s_elems, scratch);
-    }
+    dispatch_task<COMP, BT, NMAX>(L, V, S, s_tab, s_G, s_F, s_elems, scratch);
     // generic-proxy accesses of this buffer before the next TMA writes into it
     fence_proxy_async_smem();
     __syncthreads();
@@ -743,16 +752,38 @@ int batch_max_extent(int variant) { return kShapes[variant].nmax; }
 
 int batch_task_elements(int n, int variant) { return task_g(n, batch_threads(variant)); }
 
-void batch_smem_bytes(int n, bool comp, int variant, size_t* buf, size_t* s, size_t* tab) {
+void batch_smem_bytes(int n, bool comp, int variant, size_t* buf, size_t* s) {
   const int g = task_g(n, batch_threads(variant));
   *buf = (size_t)g * (x_slot(n, comp) + f_slot(n, comp));
   *s = (size_t)round128(g * n * n * n * 4);
-  *tab = (size_t)round128(g * (comp ? 2 : 1) * 3 * tab_stride(n) * 4);
 }
 
-size_t batch_smem_total(int variant, size_t buf, size_t s, size_t tab) {
-  return (size_t)kShapes[variant].stages * buf + s + tab +
+size_t batch_smem_total(int variant, size_t buf, size_t s) {
+  return (size_t)kShapes[variant].stages * buf + s +
          (size_t)(batch_threads(variant) / 32) * kScratchFloats * 4;
+}
+
+void batch_split_tables(std::vector<float>* out) {
+  out->assign(2 * kTabTotal, 0.0f);
+  for (int n = kMinN; n <= kMaxN; ++n) {
+    EoTable eo;
+    lgl_eo_table(n, &eo);
+    const int h = n / 2, ts = tab_stride(n), o = tab_offset(n);
+    for (int rr = 0; rr < ts; ++rr) {
+      double v;
+      if (rr < 2 * h * h) {
+        const int pi = rr >> 1, i = pi / h, j = pi - i * h;
+        v = (rr & 1) ? eo.B[i][j] : eo.A[i][j];
+      } else if (rr < 2 * h * h + h) {
+        v = eo.M[rr - 2 * h * h];
+      } else {
+        v = eo.B[h][rr - 2 * h * h - h];
+      }
+      const float hi = (float)v;
+      (*out)[o + rr] = hi;
+      (*out)[kTabTotal + o + rr] = (float)(v - (double)hi);
+    }
+  }
 }
 
 cudaError_t launch_stage_batch(const BatchLaunch& L, cudaStream_t s) {
@@ -762,7 +793,7 @@ cudaError_t launch_stage_batch(const BatchLaunch& L, cudaStream_t s) {
     return cudaErrorInvalidValue;
   if (L.w32 == nullptr) return cudaErrorInvalidValue;
   if (L.variant < 0 || L.variant >= kNumShapes) return cudaErrorInvalidValue;
-  const size_t smem = batch_smem_total(L.variant, L.buf_bytes, L.s_bytes, L.tab_bytes);
+  const size_t smem = batch_smem_total(L.variant, L.buf_bytes, L.s_bytes);
   return launch_any<0>(comp, L, smem, s);
 }
 

@@ -55,7 +55,7 @@ struct Lay {
   static constexpr int kBuf = kX + kY + kB + kFace;  // one pipeline buffer
   static constexpr int kHiLo = 0;  // the double-float split is done as values are read
   static constexpr int kS = round128(S::NP * 4);
-  static constexpr int kTab = round128((COMP ? 2 : 1) * 3 * S::TAB2 * 8);
+  static constexpr int kTab = 128;  // per axis: lift factor G and derivative scale F
   static constexpr int kSlot = 2 * kBuf + kHiLo + kS + kTab;  // two pipeline buffers
   static constexpr int kSlot1 = kBuf + kHiLo + kS + kTab;     // one
   // bytes the TMA copies of one element move (unpadded)
@@ -144,7 +144,10 @@ __global__ void __launch_bounds__(N * N * EPB, MINB)
   unsigned char* slot_base = smem_raw + (size_t)slot * kSlotBytes;
   unsigned char* bufs[2] = {slot_base, slot_base + (STAGES - 1) * Y::kBuf};
   float* Sacc = reinterpret_cast<float*>(slot_base + STAGES * Y::kBuf + Y::kHiLo);
-  float2* tab = reinterpret_cast<float2*>(slot_base + STAGES * Y::kBuf + Y::kHiLo + Y::kS);
+  float* GF = reinterpret_cast<float*>(slot_base + STAGES * Y::kBuf + Y::kHiLo + Y::kS);
+  // the unscaled split of D as (A, B) pairs, hi then lo, once per CTA; each
+  // element's -c dxi/dx scales the contractions' results per axis
+  __shared__ float2 s_tab[2 * TAB2];
   const int ta = t % N, tb = t / N;
   const uint64_t kLimitNs = 2000000000ull;  // 2 s per wait
 
@@ -152,6 +155,14 @@ __global__ void __launch_bounds__(N * N * EPB, MINB)
     mbar_init(&bars[0], 1);
     mbar_init(&bars[1], 1);
     fence_mbar_init();
+  }
+  for (int q = threadIdx.x; q < TAB2; q += blockDim.x) {
+    const int i = q / h, j = q - (q / h) * h;
+    const double va = L.eo.A[i][j], vb = L.eo.B[i][j];
+    const float ah = __double2float_rn(va), bh = __double2float_rn(vb);
+    s_tab[q] = make_float2(ah, bh);
+    s_tab[TAB2 + q] =
+        make_float2(__double2float_rn(va - (double)ah), __double2float_rn(vb - (double)bh));
   }
   __syncthreads();
 
@@ -222,22 +233,11 @@ __global__ void __launch_bounds__(N * N * EPB, MINB)
     const int64_t e = g * EPB + slot;
     const bool active = e < L.n_elem;
     if (STAGES == 2 && threadIdx.x == 0 && gn < n_groups) issue_group(gn, b ^ 1);
-    // scaled split tables for this element (depend only on its Jacobian)
-    double jd[3] = {0.0, 0.0, 0.0};
-    if (active) {
-      jd[0] = L.jac[3 * e];
-      jd[1] = L.jac[3 * e + 1];
-      jd[2] = L.jac[3 * e + 2];
-      for (int q = t; q < 3 * TAB2; q += NN) {
-        const int d = q / TAB2, r = q - d * TAB2, i = r / h, j = r % h;
-        const double f = -L.c * jd[d];
-        const double va = f * L.eo.A[i][j], vb = f * L.eo.B[i][j];
-        const float ah = __double2float_rn(va), bh = __double2float_rn(vb);
-        tab[q] = make_float2(ah, bh);
-        if (COMP)
-          tab[3 * TAB2 + q] =
-              make_float2(__double2float_rn(va - (double)ah), __double2float_rn(vb - (double)bh));
-      }
+    // the element's lift factors and derivative scales per axis
+    if (active && t < 3) {
+      const double jd = L.jac[3 * e + t];
+      GF[t] = (float)(-0.25 * L.c * (double)(N * (N - 1)) * jd);
+      GF[3 + t] = (float)(-L.c * jd);
     }
     const bool landed = mbar_wait(&bars[b], parity, kLimitNs);
     cp_async_wait_all();
@@ -284,8 +284,9 @@ __global__ void __launch_bounds__(N * N * EPB, MINB)
           base = ta + N * tb;
           stride = NN;
         }
-        const float2* th = tab + d * TAB2;
-        const float2* tl = tab + 3 * TAB2 + d * TAB2;
+        const float2* th = s_tab;
+        const float2* tl = s_tab + TAB2;
+        const float Fd = GF[3 + d];
         float dF[N], dP[N], pih[N], fh[N];
         float pil[N], fl[N];
         if (COMP) {
@@ -300,6 +301,11 @@ __global__ void __launch_bounds__(N * N * EPB, MINB)
           }
           eo_line_pdf<N>(fh, fl, dF, th, tl);
           eo_line_pdf<N>(pih, pil, dP, th, tl);
+#pragma unroll
+          for (int i = 0; i < N; ++i) {
+            dF[i] *= Fd;
+            dP[i] *= Fd;
+          }
         } else {
 #pragma unroll
           for (int i = 0; i < N; ++i) {
@@ -310,9 +316,14 @@ __global__ void __launch_bounds__(N * N * EPB, MINB)
           }
           eo_line_p<N>(fh, dF, th);
           eo_line_p<N>(pih, dP, th);
+#pragma unroll
+          for (int i = 0; i < N; ++i) {
+            dF[i] *= Fd;
+            dP[i] *= Fd;
+          }
         }
         // UpwindPenalty corrections at both ends of the line (see stage_mixed.cu)
-        const float G2 = (float)(-0.25 * L.c * (double)(N * (N - 1)) * jd[d]);
+        const float G2 = GF[d];
         const FT* fc = face + (4 * d) * NN + t;
         float dw_lo, dw_hi;
         if (COMP) {

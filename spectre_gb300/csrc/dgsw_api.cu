@@ -83,6 +83,11 @@ struct DgswHandle_ {
   float* bt_fw1 = nullptr;
   float* bt_fw2 = nullptr;
   float* bt_fw3 = nullptr;
+  float* bt_raw = nullptr;           // a stage's face values in each element's own resolution
+  int4* bt_chunks = nullptr;         // face-map chunks, one (n, m) pair each
+  int64_t bt_nchunks = 0;
+  int64_t* bt_face_src = nullptr;    // per producer face, sorted by (n, m)
+  int64_t* bt_face_dst = nullptr;
   float* bt_dtab = nullptr;
   // per variant and precision (0: FP64 input, 1: FP32): shared-memory regions
   // and resident grid
@@ -326,6 +331,20 @@ BatchLaunch base_batch(DgswHandle h, bool comp) {
   return B;
 }
 
+// The exterior face values of the next stage from the raw face values.
+cudaError_t batch_face_map(DgswHandle h, float* out) {
+  FaceMapLaunch M;
+  M.chunks = h->bt_chunks;
+  M.n_chunks = h->bt_nchunks;
+  M.face_src = h->bt_face_src;
+  M.face_dst = h->bt_face_dst;
+  M.op_hi = h->op_hi;
+  M.op_off = h->op_off;
+  M.raw = h->bt_raw;
+  M.out = out;
+  return launch_face_map(M, h->stream);
+}
+
 // The double-float face values of the state, formed from it.
 cudaError_t batch_state_faces(DgswHandle h) {
   BatchFaceLaunch F;
@@ -350,18 +369,20 @@ cudaError_t enqueue_batch_step(DgswHandle h, double dt) {
   A.x64 = h->state;
   A.fx2 = h->bt_fu;
   A.w32 = h->w1;
-  A.fw32 = h->bt_fw1;
+  A.raw32 = h->bt_raw;
   A.c = dt;
   cudaError_t e = launch_stage_batch(A, h->stream);
+  if (e == cudaSuccess) e = batch_face_map(h, h->bt_fw1);
   if (e != cudaSuccess) return e;
   BatchLaunch B = base_batch(h, false);
   B.x32 = h->w1;
   B.fx32 = h->bt_fw1;
   B.w32 = h->w2;
-  B.fw32 = h->bt_fw2;
+  B.raw32 = h->bt_raw;
   B.alpha = 0.5;
   B.c = 0.25 * dt;
   if ((e = launch_stage_batch(B, h->stream)) != cudaSuccess) return e;
+  if ((e = batch_face_map(h, h->bt_fw2)) != cudaSuccess) return e;
   // W3 = 2/3 W2 + 2dt/3 L(W2) in place of W2 (each element's block is read
   // only by the CTA that overwrites it) with its face values, then in one
   // stream u = u0 + W3 + 2/3 W1 and the state's face values += those of
@@ -370,10 +391,11 @@ cudaError_t enqueue_batch_step(DgswHandle h, double dt) {
   C.x32 = h->w2;
   C.fx32 = h->bt_fw2;
   C.w32 = h->w2;
-  C.fw32 = h->bt_fw3;
+  C.raw32 = h->bt_raw;
   C.alpha = 2.0 / 3.0;
   C.c = (2.0 / 3.0) * dt;
   if ((e = launch_stage_batch(C, h->stream)) != cudaSuccess) return e;
+  if ((e = batch_face_map(h, h->bt_fw3)) != cudaSuccess) return e;
   return launch_accumulate_step(h->state, h->w2, h->w1, 2.0 / 3.0, h->dom.offset.back(), h->bt_fu,
                                 h->bt_fw3, h->bt_fw1, h->bt_fsize, h->stream);
 }
@@ -1820,14 +1842,52 @@ int batch_init(DgswHandle h) {
   if ((e = cudaMalloc(&h->bt_fu, h->bt_fsize * sizeof(float2) + pad)) != cudaSuccess ||
       (e = cudaMalloc(&h->bt_fw1, h->bt_fsize * sizeof(float) + pad)) != cudaSuccess ||
       (e = cudaMalloc(&h->bt_fw2, h->bt_fsize * sizeof(float) + pad)) != cudaSuccess ||
-      (e = cudaMalloc(&h->bt_fw3, h->bt_fsize * sizeof(float) + pad)) != cudaSuccess)
+      (e = cudaMalloc(&h->bt_fw3, h->bt_fsize * sizeof(float) + pad)) != cudaSuccess ||
+      (e = cudaMalloc(&h->bt_raw, h->bt_fsize * sizeof(float) + pad)) != cudaSuccess)
     return cuda_fail(h, e, "allocate face buffers");
   // the rounding pads are read by the copies: keep them finite
   if ((e = cudaMemset(h->bt_fu, 0, h->bt_fsize * sizeof(float2) + pad)) != cudaSuccess ||
       (e = cudaMemset(h->bt_fw1, 0, h->bt_fsize * sizeof(float) + pad)) != cudaSuccess ||
       (e = cudaMemset(h->bt_fw2, 0, h->bt_fsize * sizeof(float) + pad)) != cudaSuccess ||
-      (e = cudaMemset(h->bt_fw3, 0, h->bt_fsize * sizeof(float) + pad)) != cudaSuccess)
+      (e = cudaMemset(h->bt_fw3, 0, h->bt_fsize * sizeof(float) + pad)) != cudaSuccess ||
+      (e = cudaMemset(h->bt_raw, 0, h->bt_fsize * sizeof(float) + pad)) != cudaSuccess)
     return cuda_fail(h, e, "clear face buffers");
+  // the producer faces sorted by (own extent, neighbour's extent), cut into
+  // chunks of at most kFacesPerChunk faces of one pair
+  {
+    constexpr int kFacesPerChunk = 16;
+    std::vector<std::vector<std::pair<int64_t, int64_t>>> by_pair((kMaxN + 1) * (kMaxN + 1));
+    for (int64_t el = 0; el < E; ++el) {
+      const int n = h->dom.elem_n[el];
+      for (int dir = 0; dir < 6; ++dir) {
+        const int64_t nb = h->dom.neighbor[6 * el + dir];
+        const int m = h->dom.elem_n[nb];
+        by_pair[n * (kMaxN + 1) + m].emplace_back(foff[el] + (int64_t)dir * n * n,
+                                                  foff[nb] + (int64_t)(dir ^ 1) * m * m);
+      }
+    }
+    std::vector<int4> chunks;
+    std::vector<int64_t> src, dst;
+    src.reserve(6 * E);
+    dst.reserve(6 * E);
+    for (int n = kMinN; n <= kMaxN; ++n)
+      for (int m = kMinN; m <= kMaxN; ++m) {
+        const auto& fl = by_pair[n * (kMaxN + 1) + m];
+        for (size_t i = 0; i < fl.size(); i += kFacesPerChunk) {
+          const int cnt = (int)std::min<size_t>(kFacesPerChunk, fl.size() - i);
+          chunks.push_back(make_int4(n | (m << 8), (int)src.size(), cnt, 0));
+          for (int k = 0; k < cnt; ++k) {
+            src.push_back(fl[i + k].first);
+            dst.push_back(fl[i + k].second);
+          }
+        }
+      }
+    h->bt_nchunks = (int64_t)chunks.size();
+    if ((e = upload(&h->bt_chunks, chunks)) != cudaSuccess ||
+        (e = upload(&h->bt_face_src, src)) != cudaSuccess ||
+        (e = upload(&h->bt_face_dst, dst)) != cudaSuccess)
+      return cuda_fail(h, e, "upload face maps");
+  }
   std::vector<float> dtab;
   batch_split_tables(&dtab);
   if ((e = upload(&h->bt_dtab, dtab)) != cudaSuccess) return cuda_fail(h, e, "upload split tables");
@@ -2179,7 +2239,8 @@ int dgsw_destroy(DgswHandle h) {
   }
   if (h->pnc_face_idx) cudaFree(h->pnc_face_idx);
   void* bt[] = {h->bt_tasks[0], h->bt_tasks[1], h->bt_elems[0], h->bt_elems[1], h->bt_foff,
-                h->bt_fu, h->bt_fw1, h->bt_fw2, h->bt_fw3, h->bt_dtab};
+                h->bt_fu, h->bt_fw1, h->bt_fw2, h->bt_fw3, h->bt_dtab, h->bt_raw,
+                h->bt_chunks, h->bt_face_src, h->bt_face_dst};
   for (void* p : bt)
     if (p) cudaFree(p);
   if (h->op64) cudaFree(h->op64);

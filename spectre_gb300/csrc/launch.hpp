@@ -165,7 +165,8 @@ struct BatchLaunch {
   const float2* fx2 = nullptr;      // exterior face values of X (kPrecComp, double-float)
   const float* fx32 = nullptr;      // exterior face values of X (kPrecF32)
   float* w32 = nullptr;             // FP32 output W (may be X's own buffer)
-  float* fw32 = nullptr;            // optional: face values of W for the next stage
+  float* raw32 = nullptr;           // optional: W's face values in the element's own
+                                    // resolution, at its face-buffer offsets
   double alpha = 0.0, c = 1.0;
   int* err = nullptr;               // device error word (bounded waits that timed out)
   int buf_bytes = 0, s_bytes = 0;   // shared-memory regions
@@ -194,6 +195,21 @@ cudaError_t batch_grid(bool comp, int variant, size_t smem, int* grid);
 cudaError_t launch_accumulate_step(double* u, const float* w, const float* y, double beta,
                                    int64_t n, float2* fu, const float* fw, const float* fy,
                                    int64_t nf, cudaStream_t s);
+// The next stage's exterior face values from the raw face values of a stage:
+// each producer face mapped onto its neighbour's points (stage_batch.cu).
+// chunks: (n | m << 8, first face, faces, 0), one (n, m) pair per chunk;
+// face_src / face_dst: per face, offsets into raw / out.
+struct FaceMapLaunch {
+  const int4* chunks = nullptr;
+  int64_t n_chunks = 0;
+  const int64_t* face_src = nullptr;
+  const int64_t* face_dst = nullptr;
+  const float* op_hi = nullptr;
+  const int32_t* op_off = nullptr;
+  const float* raw = nullptr;
+  float* out = nullptr;
+};
+cudaError_t launch_face_map(const FaceMapLaunch& L, cudaStream_t s);
 // Double-float exterior face values of an FP64 state for the first stage.
 struct BatchFaceLaunch {
   int64_t n_elem = 0;

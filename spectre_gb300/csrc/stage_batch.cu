@@ -181,8 +181,6 @@ __host__ __device__ constexpr int x_slot(int n, bool comp) { return round128(x_b
 __host__ __device__ constexpr int f_slot(int n, bool comp) { return round128(f_bytes(n, comp) + 32); }
 // elements per task of extent n with bt threads per CTA (one per grid line)
 __host__ __device__ constexpr int task_g(int n, int bt) { return bt / (n * n); }
-// per-warp scratch of the face maps: T (m x n), w and the first sweep
-constexpr int kScratchFloats = 3 * kMaxN * kMaxN;
 
 // face coordinates (a, b) of face direction dir -> volume index of extent n
 __device__ __forceinline__ int face_point(int n, int d, int slice, int a, int b) {
@@ -414,102 +412,58 @@ __device__ __forceinline__ void split_x(const TaskView<true>& V, int g, int bt) 
   }
 }
 
-// The next stage's exterior values from the faces of W: for face dir of the
-// element in slot s, w = Pi + s_e Phi_d (s_e = +1 upper, -1 lower) mapped by
-// T (m x n, m the neighbour's extent) onto the neighbour's face points and
-// stored into the neighbour's slot opposite dir.  One warp per face; T, w and
-// the first sweep sit in the warp's scratch.
-// q / m for q < 144, 2 <= m <= 12 (exact: checked for every q and m)
-__device__ __forceinline__ int div_small(int q, int m) {
-  return (q * ((65536 + m - 1) / m)) >> 16;
-}
-
+// The face values of W in the element's own resolution: for each face dir,
+// w = Pi + s_e Phi_d (s_e = +1 upper, -1 lower) at its N^2 points, into the
+// element's own slots of the raw face buffer (coalesced); the face-map
+// kernel then maps them onto the neighbours' points.
 template <int n, bool COMP, int BT>
-__device__ void task_faces(const BatchLaunch& L, const TaskView<COMP>& V, const int32_t* elems,
-                           float* scratch) {
-  constexpr int kWarps = BT / 32;
-  constexpr int nn = n * n, np = nn * n;
-  const int g = V.g;
-  const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
-  float* Ts = scratch + warp * kScratchFloats;
-  float* wv = Ts + kMaxN * kMaxN;
-  float* tv = wv + kMaxN * kMaxN;
-  for (int fc = warp; fc < 6 * g; fc += kWarps) {
-    const int s = fc / 6, dir = fc - 6 * s, d = dir >> 1;
-    const bool upper = dir & 1;
-    const int slice = upper ? n - 1 : 0;
+__device__ __forceinline__ void task_raw_faces(const BatchLaunch& L, const TaskView<COMP>& V,
+                                               const int32_t* elems) {
+  constexpr int nn = n * n, np = nn * n, F6 = 6 * nn;
+  for (int s = 0; s < V.g; ++s) {
     const float* W = reinterpret_cast<const float*>(V.x(s));
-    const int64_t e = elems[s];
-    const int64_t nb = L.nbr[6 * e + dir];
-    const int m = L.elem_n[nb];
-    const int64_t dst = L.foff[nb] + (int64_t)(dir ^ 1) * m * m;
-    if (m != n) {
-      const float* T = L.op_hi + L.op_off[m * (kMaxN + 1) + n];  // m x n, row-major
-      for (int q = lane; q < m * n; q += 32) Ts[q] = __ldg(T + q);
-    }
-    for (int q = lane; q < nn; q += 32) {
-      const int p = face_point(n, d, slice, q % n, q / n);
+    float* dst = L.raw32 + L.foff[elems[s]];
+    for (int q = threadIdx.x; q < F6; q += BT) {
+      const int dir = q / nn, r = q - dir * nn, d = dir >> 1;
+      const bool upper = dir & 1;
+      const int p = face_point(n, d, upper ? n - 1 : 0, r % n, r / n);
       const float pi = W[w_index<COMP>(1, p, np)], ph = W[w_index<COMP>(2 + d, p, np)];
-      wv[q] = upper ? pi + ph : pi - ph;
+      dst[q] = upper ? pi + ph : pi - ph;
     }
-    __syncwarp();
-    if (m != n) {
-      // tv[pp + n b] = sum_k T(b, k) wv[pp + n k], b < m
-      for (int q = lane; q < n * m; q += 32) {
-        const int pp = q % n, b = q / n;
-        float acc = 0.0f;
-#pragma unroll
-        for (int k = 0; k < n; ++k) acc = fmaf(Ts[b * n + k], wv[pp + n * k], acc);
-        tv[q] = acc;
-      }
-      __syncwarp();
-      // wv[a + m b] = sum_k T(a, k) tv[k + n b]
-      for (int q = lane; q < m * m; q += 32) {
-        const int b = div_small(q, m), a = q - b * m;
-        float acc = 0.0f;
-#pragma unroll
-        for (int k = 0; k < n; ++k) acc = fmaf(Ts[a * n + k], tv[k + n * b], acc);
-        wv[q] = acc;
-      }
-      __syncwarp();
-    }
-    for (int q = lane; q < m * m; q += 32) L.fw32[dst + q] = wv[q];
-    __syncwarp();
   }
 }
 
 template <int N, bool COMP, int BT>
 __device__ __forceinline__ void run_task(const BatchLaunch& L, const TaskView<COMP>& V, float* S,
                                          const float* tabs, const float* G, const float* F,
-                                         const int32_t* elems, float* scratch) {
+                                         const int32_t* elems) {
   if constexpr (COMP) {
     split_x<N>(V, V.g, BT);
     __syncthreads();
   }
   task_passes<N, COMP>(L, V, S, tabs, V.g, (float)L.c, G, F);
-  if (L.fw32 != nullptr) {
+  if (L.raw32 != nullptr) {
     __syncthreads();
-    task_faces<N, COMP, BT>(L, V, elems, scratch);
+    task_raw_faces<N, COMP, BT>(L, V, elems);
   }
 }
 
 template <bool COMP, int BT, int NMAX>
 __device__ __forceinline__ void dispatch_task(const BatchLaunch& L, const TaskView<COMP>& V,
                                               float* S, const float* tabs, const float* G,
-                                              const float* F, const int32_t* elems,
-                                              float* scratch) {
+                                              const float* F, const int32_t* elems) {
   switch (V.n) {
-    case 2: run_task<2, COMP, BT>(L, V, S, tabs, G, F, elems, scratch); break;
-    case 3: run_task<3, COMP, BT>(L, V, S, tabs, G, F, elems, scratch); break;
-    case 4: run_task<4, COMP, BT>(L, V, S, tabs, G, F, elems, scratch); break;
-    case 5: run_task<5, COMP, BT>(L, V, S, tabs, G, F, elems, scratch); break;
-    case 6: run_task<6, COMP, BT>(L, V, S, tabs, G, F, elems, scratch); break;
-    case 7: run_task<7, COMP, BT>(L, V, S, tabs, G, F, elems, scratch); break;
-    case 8: run_task<8, COMP, BT>(L, V, S, tabs, G, F, elems, scratch); break;
-    case 9: if (NMAX >= 9) run_task<(NMAX >= 9 ? 9 : 2), COMP, BT>(L, V, S, tabs, G, F, elems, scratch); break;
-    case 10: if (NMAX >= 10) run_task<(NMAX >= 10 ? 10 : 2), COMP, BT>(L, V, S, tabs, G, F, elems, scratch); break;
-    case 11: if (NMAX >= 11) run_task<(NMAX >= 11 ? 11 : 2), COMP, BT>(L, V, S, tabs, G, F, elems, scratch); break;
-    case 12: if (NMAX >= 12) run_task<(NMAX >= 12 ? 12 : 2), COMP, BT>(L, V, S, tabs, G, F, elems, scratch); break;
+    case 2: run_task<2, COMP, BT>(L, V, S, tabs, G, F, elems); break;
+    case 3: run_task<3, COMP, BT>(L, V, S, tabs, G, F, elems); break;
+    case 4: run_task<4, COMP, BT>(L, V, S, tabs, G, F, elems); break;
+    case 5: run_task<5, COMP, BT>(L, V, S, tabs, G, F, elems); break;
+    case 6: run_task<6, COMP, BT>(L, V, S, tabs, G, F, elems); break;
+    case 7: run_task<7, COMP, BT>(L, V, S, tabs, G, F, elems); break;
+    case 8: run_task<8, COMP, BT>(L, V, S, tabs, G, F, elems); break;
+    case 9: if (NMAX >= 9) run_task<(NMAX >= 9 ? 9 : 2), COMP, BT>(L, V, S, tabs, G, F, elems); break;
+    case 10: if (NMAX >= 10) run_task<(NMAX >= 10 ? 10 : 2), COMP, BT>(L, V, S, tabs, G, F, elems); break;
+    case 11: if (NMAX >= 11) run_task<(NMAX >= 11 ? 11 : 2), COMP, BT>(L, V, S, tabs, G, F, elems); break;
+    case 12: if (NMAX >= 12) run_task<(NMAX >= 12 ? 12 : 2), COMP, BT>(L, V, S, tabs, G, F, elems); break;
     default: break;
   }
 }
@@ -532,7 +486,6 @@ __global__ void __launch_bounds__(BT, MINB) stage_batch_kernel(BatchLaunch L) {
   unsigned char* bufs[2] = {smem, smem + (STAGES - 1) * L.buf_bytes};
   unsigned char* rest = smem + STAGES * L.buf_bytes;
   float* S = reinterpret_cast<float*>(rest);
-  float* scratch = reinterpret_cast<float*>(rest + L.s_bytes);
   for (int q = threadIdx.x; q < 2 * kTabTotal; q += BT) s_tab[q] = L.dtab[q];
 
   if (threadIdx.x == 0) {
@@ -580,7 +533,7 @@ __global__ void __launch_bounds__(BT, MINB) stage_batch_kernel(BatchLaunch L) {
     V.L = &L;
     V.n = n;
     V.g = g;
-    dispatch_task<COMP, BT, NMAX>(L, V, S, s_tab, s_G, s_F, s_elems, scratch);
+    dispatch_task<COMP, BT, NMAX>(L, V, S, s_tab, s_G, s_F, s_elems);
     // generic-proxy accesses of this buffer before the next TMA writes into it
     fence_proxy_async_smem();
     __syncthreads();
@@ -690,6 +643,78 @@ __global__ void __launch_bounds__(32 * kFaceWarps) batch_faces_kernel(BatchFaceL
   }
 }
 
+// ---------------------------------------------------------------- face maps
+// The next stage's exterior values: every producer face (element e, face
+// dir) of the raw face buffer mapped by T (m x n, m the neighbour's extent;
+// a copy when m = n) onto the neighbour's points, into its slot opposite
+// dir.  The faces are sorted by (n, m) and cut into chunks of one pair; a
+// CTA takes one chunk, holds its T in shared memory, and each warp maps one
+// face at a time: w into the warp's scratch, the first sweep, then the
+// second sweep straight to the output.
+constexpr int kMapWarps = 4;
+
+template <int n>
+__device__ __forceinline__ void map_chunk(const FaceMapLaunch& L, int4 ch, float* Ts, float* wv,
+                                          float* tv) {
+  constexpr int nn = n * n;
+  const int m = (ch.x >> 8) & 0xff;
+  const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+  if (m != n) {
+    const float* T = L.op_hi + L.op_off[m * (kMaxN + 1) + n];  // m x n, row-major
+    for (int q = threadIdx.x; q < m * n; q += 32 * kMapWarps) Ts[q] = T[q];
+  }
+  __syncthreads();
+  for (int f = warp; f < ch.z; f += kMapWarps) {
+    const int64_t src = L.face_src[ch.y + f], dst = L.face_dst[ch.y + f];
+    if (m == n) {
+      for (int q = lane; q < nn; q += 32) L.out[dst + q] = L.raw[src + q];
+      continue;
+    }
+    for (int q = lane; q < nn; q += 32) wv[q] = L.raw[src + q];
+    __syncwarp();
+    // tv[pp + n b] = sum_k T(b, k) wv[pp + n k], b < m
+    for (int q = lane; q < n * m; q += 32) {
+      const int pp = q % n, b = q / n;
+      float acc = 0.0f;
+#pragma unroll
+      for (int k = 0; k < n; ++k) acc = fmaf(Ts[b * n + k], wv[pp + n * k], acc);
+      tv[q] = acc;
+    }
+    __syncwarp();
+    // out[a + m b] = sum_k T(a, k) tv[k + n b]
+    for (int q = lane; q < m * m; q += 32) {
+      const int b = (q * ((65536 + m - 1) / m)) >> 16, a = q - b * m;  // q / m, exact here
+      float acc = 0.0f;
+#pragma unroll
+      for (int k = 0; k < n; ++k) acc = fmaf(Ts[a * n + k], tv[k + n * b], acc);
+      L.out[dst + q] = acc;
+    }
+    __syncwarp();
+  }
+}
+
+__global__ void __launch_bounds__(32 * kMapWarps) face_map_kernel(FaceMapLaunch L) {
+  __shared__ float Ts[kMaxN * kMaxN];
+  __shared__ float wv[kMapWarps][kMaxN * kMaxN];
+  __shared__ float tv[kMapWarps][kMaxN * kMaxN];
+  const int4 ch = L.chunks[blockIdx.x];
+  const int n = ch.x & 0xff, warp = threadIdx.x >> 5;
+  switch (n) {
+    case 2: map_chunk<2>(L, ch, Ts, wv[warp], tv[warp]); break;
+    case 3: map_chunk<3>(L, ch, Ts, wv[warp], tv[warp]); break;
+    case 4: map_chunk<4>(L, ch, Ts, wv[warp], tv[warp]); break;
+    case 5: map_chunk<5>(L, ch, Ts, wv[warp], tv[warp]); break;
+    case 6: map_chunk<6>(L, ch, Ts, wv[warp], tv[warp]); break;
+    case 7: map_chunk<7>(L, ch, Ts, wv[warp], tv[warp]); break;
+    case 8: map_chunk<8>(L, ch, Ts, wv[warp], tv[warp]); break;
+    case 9: map_chunk<9>(L, ch, Ts, wv[warp], tv[warp]); break;
+    case 10: map_chunk<10>(L, ch, Ts, wv[warp], tv[warp]); break;
+    case 11: map_chunk<11>(L, ch, Ts, wv[warp], tv[warp]); break;
+    case 12: map_chunk<12>(L, ch, Ts, wv[warp], tv[warp]); break;
+    default: break;
+  }
+}
+
 // The compiled launch shapes (variants): threads per CTA, resident CTAs
 // asked of the register allocator for the FP64-input and the FP32 stages,
 // largest extent, pipeline buffers.
@@ -759,8 +784,7 @@ void batch_smem_bytes(int n, bool comp, int variant, size_t* buf, size_t* s) {
 }
 
 size_t batch_smem_total(int variant, size_t buf, size_t s) {
-  return (size_t)kShapes[variant].stages * buf + s +
-         (size_t)(batch_threads(variant) / 32) * kScratchFloats * 4;
+  return (size_t)kShapes[variant].stages * buf + s;
 }
 
 void batch_split_tables(std::vector<float>* out) {
@@ -814,6 +838,12 @@ cudaError_t launch_batch_faces(const BatchFaceLaunch& L, cudaStream_t s) {
   if (faces <= 0) return cudaSuccess;
   const int64_t blocks = (faces + kFaceWarps - 1) / kFaceWarps;
   batch_faces_kernel<<<(unsigned)blocks, 32 * kFaceWarps, 0, s>>>(L);
+  return cudaGetLastError();
+}
+
+cudaError_t launch_face_map(const FaceMapLaunch& L, cudaStream_t s) {
+  if (L.n_chunks <= 0) return cudaSuccess;
+  face_map_kernel<<<(unsigned)L.n_chunks, 32 * kMapWarps, 0, s>>>(L);
   return cudaGetLastError();
 }
 

@@ -1853,9 +1853,9 @@ int batch_init(DgswHandle h) {
       (e = cudaMemset(h->bt_raw, 0, h->bt_fsize * sizeof(float) + pad)) != cudaSuccess)
     return cuda_fail(h, e, "clear face buffers");
   // the producer faces sorted by (own extent, neighbour's extent), cut into
-  // chunks of at most kFacesPerChunk faces of one pair
+  // chunks of at most kBatchMapFaces faces of one pair
   {
-    constexpr int kFacesPerChunk = 16;
+    constexpr int kFacesPerChunk = kBatchMapFaces;
     std::vector<std::vector<std::pair<int64_t, int64_t>>> by_pair((kMaxN + 1) * (kMaxN + 1));
     for (int64_t el = 0; el < E; ++el) {
       const int n = h->dom.elem_n[el];

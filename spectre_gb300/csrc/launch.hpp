@@ -199,6 +199,7 @@ cudaError_t launch_accumulate_step(double* u, const float* w, const float* y, do
 // each producer face mapped onto its neighbour's points (stage_batch.cu).
 // chunks: (n | m << 8, first face, faces, 0), one (n, m) pair per chunk;
 // face_src / face_dst: per face, offsets into raw / out.
+constexpr int kBatchMapFaces = 32;  // faces per chunk at most
 struct FaceMapLaunch {
   const int4* chunks = nullptr;
   int64_t n_chunks = 0;

@@ -545,20 +545,28 @@ __global__ void __launch_bounds__(BT, MINB) stage_batch_kernel(BatchLaunch L) {
 // The step's update of the FP64 state and of its face values, as streams:
 // u = u + (W + beta Y) for every value (FP64 add), and every face value
 // fu += fw + beta fy in double-float.
-__global__ void accumulate_step_kernel(double* u, const float* w, const float* y, float beta,
-                                       int64_t n, float2* fu, const float* fw, const float* fy,
-                                       int64_t nf) {
+__global__ void __launch_bounds__(256) accumulate_step_kernel(double* u, const float* w,
+                                                              const float* y, float beta, int64_t n,
+                                                              float2* fu, const float* fw,
+                                                              const float* fy, int64_t nf) {
   const int64_t stride = (int64_t)gridDim.x * blockDim.x;
   const int64_t i0 = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
-  const int64_t n2 = n / 2;
-  for (int64_t i = i0; i < n2; i += stride) {
-    const double2 b = reinterpret_cast<const double2*>(u)[i];
-    const float2 x = reinterpret_cast<const float2*>(w)[i];
-    const float2 v = reinterpret_cast<const float2*>(y)[i];
-    reinterpret_cast<double2*>(u)[i] =
-        make_double2(b.x + widen(fmaf(beta, v.x, x.x)), b.y + widen(fmaf(beta, v.y, x.y)));
+  // four values per thread and iteration: one 16-byte load of W and of Y,
+  // two of u, streamed past the caches
+  const int64_t n4 = n / 4;
+  const float4* w4 = reinterpret_cast<const float4*>(w);
+  const float4* y4 = reinterpret_cast<const float4*>(y);
+  double2* u2 = reinterpret_cast<double2*>(u);
+  for (int64_t i = i0; i < n4; i += stride) {
+    const float4 x = __ldcs(w4 + i);
+    const float4 v = __ldcs(y4 + i);
+    const double2 a = __ldcs(u2 + 2 * i);
+    const double2 b = __ldcs(u2 + 2 * i + 1);
+    __stcs(u2 + 2 * i, make_double2(a.x + widen(fmaf(beta, v.x, x.x)), a.y + widen(fmaf(beta, v.y, x.y))));
+    __stcs(u2 + 2 * i + 1,
+           make_double2(b.x + widen(fmaf(beta, v.z, x.z)), b.y + widen(fmaf(beta, v.w, x.w))));
   }
-  if (i0 == 0 && (n & 1)) u[n - 1] = u[n - 1] + widen(fmaf(beta, y[n - 1], w[n - 1]));
+  for (int64_t i = 4 * n4 + i0; i < n; i += stride) u[i] = u[i] + widen(fmaf(beta, y[i], w[i]));
   for (int64_t i = i0; i < nf; i += stride) {
     const float v = fmaf(beta, fy[i], fw[i]);
     const float2 o = fu[i];
@@ -647,31 +655,44 @@ __global__ void __launch_bounds__(32 * kFaceWarps) batch_faces_kernel(BatchFaceL
 // The next stage's exterior values: every producer face (element e, face
 // dir) of the raw face buffer mapped by T (m x n, m the neighbour's extent;
 // a copy when m = n) onto the neighbour's points, into its slot opposite
-// dir.  The faces are sorted by (n, m) and cut into chunks of one pair; a
-// CTA takes one chunk, holds its T in shared memory, and each warp maps one
-// face at a time: w into the warp's scratch, the first sweep, then the
-// second sweep straight to the output.
-constexpr int kMapWarps = 4;
+// dir.  The faces are sorted by (n, m) and cut into chunks of at most
+// kMapFaces faces of one pair; a CTA takes one chunk, holds its T and all of
+// its faces' values in shared memory, and each warp maps one face at a time:
+// the first sweep into the warp's scratch, the second straight to the
+// output.
+constexpr int kMapWarps = 8;
+
+constexpr int kMapFaces = kBatchMapFaces;
 
 template <int n>
-__device__ __forceinline__ void map_chunk(const FaceMapLaunch& L, int4 ch, float* Ts, float* wv,
-                                          float* tv) {
+__device__ __forceinline__ void map_chunk(const FaceMapLaunch& L, int4 ch, float* Ts,
+                                          float (*wall)[kMaxN * kMaxN], float* tv,
+                                          int64_t* s_src, int64_t* s_dst) {
   constexpr int nn = n * n;
   const int m = (ch.x >> 8) & 0xff;
   const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+  if (threadIdx.x < ch.z) {
+    s_src[threadIdx.x] = L.face_src[ch.y + threadIdx.x];
+    s_dst[threadIdx.x] = L.face_dst[ch.y + threadIdx.x];
+  }
   if (m != n) {
     const float* T = L.op_hi + L.op_off[m * (kMaxN + 1) + n];  // m x n, row-major
     for (int q = threadIdx.x; q < m * n; q += 32 * kMapWarps) Ts[q] = T[q];
   }
   __syncthreads();
+  // every face of the chunk into shared memory at once (one load latency)
+  for (int q = threadIdx.x; q < ch.z * nn; q += 32 * kMapWarps) {
+    const int f = q / nn, r = q - f * nn;
+    wall[f][r] = L.raw[s_src[f] + r];
+  }
+  __syncthreads();
   for (int f = warp; f < ch.z; f += kMapWarps) {
-    const int64_t src = L.face_src[ch.y + f], dst = L.face_dst[ch.y + f];
+    const float* wv = wall[f];
+    const int64_t dst = s_dst[f];
     if (m == n) {
-      for (int q = lane; q < nn; q += 32) L.out[dst + q] = L.raw[src + q];
+      for (int q = lane; q < nn; q += 32) L.out[dst + q] = wv[q];
       continue;
     }
-    for (int q = lane; q < nn; q += 32) wv[q] = L.raw[src + q];
-    __syncwarp();
     // tv[pp + n b] = sum_k T(b, k) wv[pp + n k], b < m
     for (int q = lane; q < n * m; q += 32) {
       const int pp = q % n, b = q / n;
@@ -695,22 +716,23 @@ __device__ __forceinline__ void map_chunk(const FaceMapLaunch& L, int4 ch, float
 
 __global__ void __launch_bounds__(32 * kMapWarps) face_map_kernel(FaceMapLaunch L) {
   __shared__ float Ts[kMaxN * kMaxN];
-  __shared__ float wv[kMapWarps][kMaxN * kMaxN];
+  __shared__ float wall[kMapFaces][kMaxN * kMaxN];
   __shared__ float tv[kMapWarps][kMaxN * kMaxN];
+  __shared__ int64_t s_src[kMapFaces], s_dst[kMapFaces];
   const int4 ch = L.chunks[blockIdx.x];
   const int n = ch.x & 0xff, warp = threadIdx.x >> 5;
   switch (n) {
-    case 2: map_chunk<2>(L, ch, Ts, wv[warp], tv[warp]); break;
-    case 3: map_chunk<3>(L, ch, Ts, wv[warp], tv[warp]); break;
-    case 4: map_chunk<4>(L, ch, Ts, wv[warp], tv[warp]); break;
-    case 5: map_chunk<5>(L, ch, Ts, wv[warp], tv[warp]); break;
-    case 6: map_chunk<6>(L, ch, Ts, wv[warp], tv[warp]); break;
-    case 7: map_chunk<7>(L, ch, Ts, wv[warp], tv[warp]); break;
-    case 8: map_chunk<8>(L, ch, Ts, wv[warp], tv[warp]); break;
-    case 9: map_chunk<9>(L, ch, Ts, wv[warp], tv[warp]); break;
-    case 10: map_chunk<10>(L, ch, Ts, wv[warp], tv[warp]); break;
-    case 11: map_chunk<11>(L, ch, Ts, wv[warp], tv[warp]); break;
-    case 12: map_chunk<12>(L, ch, Ts, wv[warp], tv[warp]); break;
+    case 2: map_chunk<2>(L, ch, Ts, wall, tv[warp], s_src, s_dst); break;
+    case 3: map_chunk<3>(L, ch, Ts, wall, tv[warp], s_src, s_dst); break;
+    case 4: map_chunk<4>(L, ch, Ts, wall, tv[warp], s_src, s_dst); break;
+    case 5: map_chunk<5>(L, ch, Ts, wall, tv[warp], s_src, s_dst); break;
+    case 6: map_chunk<6>(L, ch, Ts, wall, tv[warp], s_src, s_dst); break;
+    case 7: map_chunk<7>(L, ch, Ts, wall, tv[warp], s_src, s_dst); break;
+    case 8: map_chunk<8>(L, ch, Ts, wall, tv[warp], s_src, s_dst); break;
+    case 9: map_chunk<9>(L, ch, Ts, wall, tv[warp], s_src, s_dst); break;
+    case 10: map_chunk<10>(L, ch, Ts, wall, tv[warp], s_src, s_dst); break;
+    case 11: map_chunk<11>(L, ch, Ts, wall, tv[warp], s_src, s_dst); break;
+    case 12: map_chunk<12>(L, ch, Ts, wall, tv[warp], s_src, s_dst); break;
     default: break;
   }
 }
@@ -851,15 +873,15 @@ cudaError_t launch_accumulate_step(double* u, const float* w, const float* y, do
                                    int64_t n, float2* fu, const float* fw, const float* fy,
                                    int64_t nf, cudaStream_t s) {
   if (n <= 0) return cudaSuccess;
-  if ((reinterpret_cast<uintptr_t>(u) & 15u) != 0 ||
-      ((reinterpret_cast<uintptr_t>(w) | reinterpret_cast<uintptr_t>(y)) & 7u) != 0)
+  if (((reinterpret_cast<uintptr_t>(u) | reinterpret_cast<uintptr_t>(w) |
+        reinterpret_cast<uintptr_t>(y)) & 15u) != 0)
     return cudaErrorInvalidValue;
   int dev = 0, sms = 0;
   cudaError_t e = cudaGetDevice(&dev);
   if (e == cudaSuccess) e = cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
   if (e != cudaSuccess) return e;
-  const int64_t want = (n / 2 + 255) / 256;
-  const int64_t grid = want < (int64_t)sms * 8 ? (want > 0 ? want : 1) : (int64_t)sms * 8;
+  const int64_t want = (n / 4 + 255) / 256;
+  const int64_t grid = want < (int64_t)sms * 16 ? (want > 0 ? want : 1) : (int64_t)sms * 16;
   accumulate_step_kernel<<<(unsigned)grid, 256, 0, s>>>(u, w, y, (float)beta, n, fu, fw, fy, nf);
   return cudaGetLastError();
 }

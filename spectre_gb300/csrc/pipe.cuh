@@ -46,6 +46,20 @@ __device__ __forceinline__ bool mbar_try_wait(uint64_t* bar, uint32_t parity) {
   return ok != 0u;
 }
 
+// the same with a suspend-time hint: the thread may sleep in the barrier
+// unit for up to hint_ns before the test returns, instead of spinning
+__device__ __forceinline__ bool mbar_try_wait_sleep(uint64_t* bar, uint32_t parity,
+                                                    uint32_t hint_ns) {
+  uint32_t ok;
+  asm volatile(
+      "{\n .reg .pred p;\n mbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2, %3;\n"
+      " selp.u32 %0, 1, 0, p;\n}"
+      : "=r"(ok)
+      : "r"(saddr(bar)), "r"(parity), "r"(hint_ns)
+      : "memory");
+  return ok != 0u;
+}
+
 // orders this thread's earlier generic-proxy accesses of shared memory before
 // later async-proxy (TMA) writes to it
 __device__ __forceinline__ void fence_proxy_async_smem() {
@@ -62,7 +76,7 @@ __device__ __forceinline__ uint64_t global_ns() {
 __device__ __forceinline__ bool mbar_wait(uint64_t* bar, uint32_t parity, uint64_t limit_ns) {
   if (mbar_try_wait(bar, parity)) return true;
   const uint64_t t0 = global_ns();
-  while (!mbar_try_wait(bar, parity)) {
+  while (!mbar_try_wait_sleep(bar, parity, 2000u)) {
     if (global_ns() - t0 > limit_ns) return false;
   }
   return true;

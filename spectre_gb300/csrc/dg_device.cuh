@@ -130,6 +130,16 @@ __device__ __forceinline__ void dot2_first(float ah, float al, float xh, float x
   c = fmaf(ah, xl, c);
 }
 
+// w - gamma2 Psi in double-float: (wh, wl) -= (gh + gl)(ph + pl), gamma2 =
+// gh + gl and Psi = ph + pl split into FP32 pairs
+__device__ __forceinline__ void sub_g2psi(float& wh, float& wl, float gh, float gl, float ph,
+                                          float pl) {
+  float qh, qc, t;
+  dot2_first(gh, gl, ph, pl, qh, qc);
+  two_sum(wh, -qh, wh, t);
+  wl = wl + (t - qc);
+}
+
 // compensated (scaled D) x line in double-float, FP32 result (odd N allowed)
 template <int N>
 __device__ __forceinline__ void eo_line_df(const float (&xh)[N], const float (&xl)[N],

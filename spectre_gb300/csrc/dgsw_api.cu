@@ -324,6 +324,7 @@ BatchLaunch base_batch(DgswHandle h, bool comp) {
   B.op_hi = h->op_hi;
   B.op_off = h->op_off;
   B.err = h->dev_err;
+  B.gamma2 = h->cfg.gamma2;
   const int i = comp ? 0 : 1;
   B.buf_bytes = h->bt_buf[v][i];
   B.s_bytes = h->bt_s[v][i];
@@ -358,6 +359,7 @@ cudaError_t batch_state_faces(DgswHandle h) {
   F.op_off = h->op_off;
   F.x64 = h->state;
   F.fu2 = h->bt_fu;
+  F.gamma2 = h->cfg.gamma2;
   return launch_batch_faces(F, h->stream);
 }
 
@@ -1929,7 +1931,7 @@ int batch_init(DgswHandle h) {
       for (int n = kMinN; n <= kMaxN; ++n) {
         if (!present[n]) continue;
         size_t b1, s1;
-        batch_smem_bytes(n, i == 0, v, &b1, &s1);
+        batch_smem_bytes(n, i == 0, h->cfg.gamma2 != 0.0, v, &b1, &s1);
         buf = std::max(buf, b1);
         sb = std::max(sb, s1);
       }
@@ -1938,7 +1940,7 @@ int batch_init(DgswHandle h) {
         return fail(h, DGSW_ERR_UNSUPPORTED, "batch stage: shared memory of a task exceeds 227 KB");
       h->bt_buf[v][i] = (int)buf;
       h->bt_s[v][i] = (int)sb;
-      if ((e = batch_grid(i == 0, v, total, &h->bt_grid[v][i])) != cudaSuccess)
+      if ((e = batch_grid(i == 0, h->cfg.gamma2 != 0.0, v, total, &h->bt_grid[v][i])) != cudaSuccess)
         return cuda_fail(h, e, "batch stage occupancy");
     }
   }
@@ -1990,10 +1992,7 @@ int dgsw_create(const DgswConfig* cfg, DgswHandle* out) {
     return fail(nullptr, DGSW_ERR_UNSUPPORTED,
                 "Gauss quadrature: flat system, one extent for every element, FP64 precision");
   }
-  if (!h->curved && cfg->precision == DGSW_PRECISION_MIXED && cfg->gamma2 != 0.0) {
-    delete h;
-    return fail(nullptr, DGSW_ERR_UNSUPPORTED, "mixed precision needs gamma2 = 0");
-  }
+
   if (cfg->time_stepper == DGSW_STEPPER_ADAMS_BASHFORTH) {
     // checked before any device work, so that a bad request fails the same
     // way with or without a GPU
@@ -2113,7 +2112,9 @@ int dgsw_create(const DgswConfig* cfg, DgswHandle* out) {
       return fail(nullptr, rc, msg);
     }
   }
-  if (!h->dom.uniform) {
+  // mixed precision with gamma2 != 0 runs the kernels of differing extents
+  // (their gamma2 terms) on uniform meshes too
+  if (!h->dom.uniform || (mixed(h) && !h->curved && h->cfg.gamma2 != 0.0)) {
     h->general = true;
     std::vector<int32_t> lists[kMaxN + 1];
     for (int64_t el = 0; el < h->dom.n_elem; ++el) lists[h->dom.elem_n[el]].push_back((int32_t)el);

@@ -168,6 +168,7 @@ struct BatchLaunch {
   float* raw32 = nullptr;           // optional: W's face values in the element's own
                                     // resolution, at its face-buffer offsets
   double alpha = 0.0, c = 1.0;
+  double gamma2 = 0.0;              // ScalarWave's constraint damping (Psi staged too when != 0)
   int* err = nullptr;               // device error word (bounded waits that timed out)
   int buf_bytes = 0, s_bytes = 0;   // shared-memory regions
   int grid = 0;
@@ -180,7 +181,7 @@ int batch_variants();
 int batch_threads(int variant);
 int batch_max_extent(int variant);
 int batch_task_elements(int n, int variant);
-void batch_smem_bytes(int n, bool comp, int variant, size_t* buf, size_t* s);
+void batch_smem_bytes(int n, bool comp, bool g2, int variant, size_t* buf, size_t* s);
 // the launch's dynamic shared memory for the given region sizes (pipeline
 // buffers, accumulator and the face maps' scratch)
 size_t batch_smem_total(int variant, size_t buf, size_t s);
@@ -189,7 +190,7 @@ size_t batch_smem_total(int variant, size_t buf, size_t s);
 // parts; its length in floats.
 void batch_split_tables(std::vector<float>* out);
 // resident grid of the batch kernel with smem bytes of shared memory
-cudaError_t batch_grid(bool comp, int variant, size_t smem, int* grid);
+cudaError_t batch_grid(bool comp, bool g2, int variant, size_t smem, int* grid);
 // The step's update of the FP64 state u (n values) by (double)(w + beta y),
 // and of its double-float face values fu (nf values) by fw + beta fy.
 cudaError_t launch_accumulate_step(double* u, const float* w, const float* y, double beta,
@@ -223,6 +224,7 @@ struct BatchFaceLaunch {
   const int32_t* op_off = nullptr;
   const double* x64 = nullptr;
   float2* fu2 = nullptr;
+  double gamma2 = 0.0;
 };
 cudaError_t launch_batch_faces(const BatchFaceLaunch& L, cudaStream_t s);
 

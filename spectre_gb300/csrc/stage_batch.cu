@@ -63,6 +63,7 @@ using namespace pipe;
 using dev::dot2_first;
 using dev::dot2_term;
 using dev::split_df;
+using dev::sub_g2psi;
 using dev::two_sum;
 using dev::widen;
 
@@ -170,14 +171,17 @@ __device__ __forceinline__ void eo_line_pdfg(const float (&xh)[N], const float (
 // --------------------------------------------------------- buffer layout
 // Bytes of one element's X block, its face block, and their shared-memory
 // slots (room for the 16-byte alignment shift of the copy).
-__host__ __device__ constexpr int x_bytes(int n, bool comp) {
-  return comp ? 4 * 8 * n * n * n : 5 * 4 * n * n * n;
+// (COMP stages X's FP64 Pi and Phi -- and Psi too when gamma2 != 0, G2)
+__host__ __device__ constexpr int x_bytes(int n, bool comp, bool g2 = false) {
+  return comp ? (g2 ? 5 : 4) * 8 * n * n * n : 5 * 4 * n * n * n;
 }
 __host__ __device__ constexpr int f_bytes(int n, bool comp) {
   return comp ? 6 * 8 * n * n : (6 * 4 * n * n + 15) / 16 * 16;
 }
 __host__ __device__ constexpr int round128(int b) { return (b + 127) / 128 * 128; }
-__host__ __device__ constexpr int x_slot(int n, bool comp) { return round128(x_bytes(n, comp) + 32); }
+__host__ __device__ constexpr int x_slot(int n, bool comp, bool g2 = false) {
+  return round128(x_bytes(n, comp, g2) + 32);
+}
 __host__ __device__ constexpr int f_slot(int n, bool comp) { return round128(f_bytes(n, comp) + 32); }
 // elements per task of extent n with bt threads per CTA (one per grid line)
 __host__ __device__ constexpr int task_g(int n, int bt) { return bt / (n * n); }
@@ -188,32 +192,32 @@ __device__ __forceinline__ int face_point(int n, int d, int slice, int a, int b)
 }
 
 // copy source of element e's X block
-template <bool COMP>
+template <bool COMP, bool G2>
 __device__ __forceinline__ const unsigned char* x_src(const BatchLaunch& L, int64_t off, int np) {
-  return COMP ? reinterpret_cast<const unsigned char*>(L.x64 + off + np)
+  return COMP ? reinterpret_cast<const unsigned char*>(L.x64 + off + (G2 ? 0 : np))
               : reinterpret_cast<const unsigned char*>(L.x32 + off);
 }
 
 // issue the TMA copies of task tk into buffer buf (one thread)
-template <bool COMP>
+template <bool COMP, bool G2>
 __device__ void issue_task(const BatchLaunch& L, int2 tk, unsigned char* buf, uint64_t* bar) {
   const int n = tk.x & 0xff, g = tk.x >> 8;
   const int np = n * n * n;
-  const int xs = x_slot(n, COMP), fb = f_bytes(n, COMP);
+  const int xs = x_slot(n, COMP, G2), fb = f_bytes(n, COMP);
   uint32_t total = 0;
   for (int s = 0; s < g; ++s) {
     const int64_t e = L.task_elems[tk.y + s];
-    const uintptr_t src = reinterpret_cast<uintptr_t>(x_src<COMP>(L, L.offset[e], np));
+    const uintptr_t src = reinterpret_cast<uintptr_t>(x_src<COMP, G2>(L, L.offset[e], np));
     const uintptr_t a0 = src & ~(uintptr_t)15;
-    const uintptr_t a1 = (src + (uintptr_t)x_bytes(n, COMP) + 15) & ~(uintptr_t)15;
+    const uintptr_t a1 = (src + (uintptr_t)x_bytes(n, COMP, G2) + 15) & ~(uintptr_t)15;
     total += (uint32_t)(a1 - a0) + (uint32_t)fb;
   }
   mbar_arrive_expect_tx(bar, total);
   for (int s = 0; s < g; ++s) {
     const int64_t e = L.task_elems[tk.y + s];
-    const uintptr_t src = reinterpret_cast<uintptr_t>(x_src<COMP>(L, L.offset[e], np));
+    const uintptr_t src = reinterpret_cast<uintptr_t>(x_src<COMP, G2>(L, L.offset[e], np));
     const uintptr_t a0 = src & ~(uintptr_t)15;
-    const uintptr_t a1 = (src + (uintptr_t)x_bytes(n, COMP) + 15) & ~(uintptr_t)15;
+    const uintptr_t a1 = (src + (uintptr_t)x_bytes(n, COMP, G2) + 15) & ~(uintptr_t)15;
     bulk_g2s(buf + s * xs, reinterpret_cast<const void*>(a0), (uint32_t)(a1 - a0), bar);
     const unsigned char* fsrc = COMP ? reinterpret_cast<const unsigned char*>(L.fx2 + L.foff[e])
                                      : reinterpret_cast<const unsigned char*>(L.fx32 + L.foff[e]);
@@ -222,37 +226,44 @@ __device__ void issue_task(const BatchLaunch& L, int2 tk, unsigned char* buf, ui
 }
 
 // Where the element in slot s of the current task sits in shared memory.
-template <bool COMP>
+template <bool COMP, bool G2>
 struct TaskView {
   unsigned char* buf;   // the task's pipeline buffer
   const int64_t* offs;  // value offset of each slot's element (shared memory)
   const BatchLaunch* L;
   int n, g;
   __device__ __forceinline__ unsigned char* x(int s) const {
-    const uintptr_t src = reinterpret_cast<uintptr_t>(x_src<COMP>(*L, offs[s], n * n * n));
-    return buf + s * x_slot(n, COMP) + (int)(src & 15);
+    const uintptr_t src = reinterpret_cast<uintptr_t>(x_src<COMP, G2>(*L, offs[s], n * n * n));
+    return buf + s * x_slot(n, COMP, G2) + (int)(src & 15);
   }
   __device__ __forceinline__ const unsigned char* f(int s) const {
-    return buf + g * x_slot(n, COMP) + s * f_slot(n, COMP);
+    return buf + g * x_slot(n, COMP, G2) + s * f_slot(n, COMP);
   }
 };
 
 // ------------------------------------------------------------- one task
 // W of slot s, field f (Psi, Pi, Phi_x, Phi_y, Phi_z), point p: where the
 // passes leave it inside the X block.  F32: in place of X.  COMP (X holds
-// Pi, Phi_x, Phi_y, Phi_z as (hi, lo) FP32 pairs): Phi_d in the first word of
-// X's Phi_d pair, Pi in the first and Psi in the second word of X's Pi pair.
-template <bool COMP>
+// Pi, Phi_x, Phi_y, Phi_z -- preceded by Psi when G2 -- as (hi, lo) FP32
+// pairs): each field in the first word of its pair, except Psi without G2,
+// in the second word of X's Pi pair.
+template <bool COMP, bool G2>
 __device__ __forceinline__ int w_index(int f, int p, int np) {
   if (!COMP) return f * np + p;
+  if (G2) return 2 * (f * np + p);
   return f <= 1 ? 2 * p + (f == 0 ? 1 : 0) : 2 * ((f - 1) * np + p);
 }
 
-template <int N, bool COMP>
-__device__ __forceinline__ void task_passes(const BatchLaunch& L, const TaskView<COMP>& V,
+
+template <int N, bool COMP, bool G2>
+__device__ __forceinline__ void task_passes(const BatchLaunch& L, const TaskView<COMP, G2>& V,
                                             float* S, const float* tabs, const int g,
                                             const float cf, const float* G, const float* F) {
   constexpr int NN = N * N, NP = NN * N;
+  // pair index of Pi and of Phi_x in the COMP block
+  constexpr int PI0 = (COMP && G2) ? NP : 0, PHI0 = (COMP && G2) ? 2 * NP : NP;
+  const float g2 = (float)L.gamma2;
+  const float g2h = g2, g2l = (float)(L.gamma2 - (double)g2);
   const int slot = threadIdx.x / NN;
   const int t = threadIdx.x - slot * NN;
   const bool active = slot < g;
@@ -289,11 +300,12 @@ __device__ __forceinline__ void task_passes(const BatchLaunch& L, const TaskView
         // X holds each FP64 value as its (hi, lo) FP32 pair (split_x)
         const float2* X = reinterpret_cast<const float2*>(xb);
         float f0h, f0l, f1h, f1l;
+        float ps0h = 0.0f, ps0l = 0.0f, ps1h = 0.0f, ps1l = 0.0f;
         {
           float fh[N], fl[N];
 #pragma unroll
           for (int i = 0; i < N; ++i) {
-            const float2 v = X[(1 + d) * NP + base + i * stride];
+            const float2 v = X[PHI0 + d * NP + base + i * stride];
             fh[i] = v.x;
             fl[i] = v.y;
           }
@@ -304,30 +316,52 @@ __device__ __forceinline__ void task_passes(const BatchLaunch& L, const TaskView
           f0l = fl[0];
           f1h = fh[N - 1];
           f1l = fl[N - 1];
+          if (G2) {
+            // the gamma2 (d_d Psi - Phi_d) term of the Phi_d output
+            float psh[N], psl[N], dps[N];
+#pragma unroll
+            for (int i = 0; i < N; ++i) {
+              const float2 v = X[base + i * stride];
+              psh[i] = v.x;
+              psl[i] = v.y;
+            }
+            eo_line_pdfg<N>(psh, psl, dps, th, tl);
+#pragma unroll
+            for (int i = 0; i < N; ++i) dP[i] = -g2 * fmaf(Fd, dps[i], cf * (fh[i] + fl[i]));
+            ps0h = psh[0];
+            ps0l = psl[0];
+            ps1h = psh[N - 1];
+            ps1l = psl[N - 1];
+          }
         }
 #pragma unroll
         for (int i = 0; i < N; ++i) {
-          const float2 v = X[base + i * stride];
+          const float2 v = X[PI0 + base + i * stride];
           pih[i] = v.x;
           pil[i] = v.y;
         }
-        eo_line_pdfg<N>(pih, pil, dP, th, tl);
+        {
+          float dd[N];
+          eo_line_pdfg<N>(pih, pil, dd, th, tl);
 #pragma unroll
-        for (int i = 0; i < N; ++i) dP[i] *= Fd;
+          for (int i = 0; i < N; ++i) dP[i] = G2 ? fmaf(Fd, dd[i], dP[i]) : Fd * dd[i];
+        }
         const float2* ext = reinterpret_cast<const float2*>(fbk);
         const float2 elo = ext[(2 * d) * NN + fidx], ehi = ext[(2 * d + 1) * NN + fidx];
         float wh, wl, t0, dh;
         two_sum(pih[0], f0h, wh, t0);
         wl = t0 + (pil[0] + f0l);
+        if (G2) sub_g2psi(wh, wl, g2h, g2l, ps0h, ps0l);
         two_sum(wh, -elo.x, dh, t0);
         dw_lo = dh + (t0 + (wl - elo.y));
         two_sum(pih[N - 1], -f1h, wh, t0);
         wl = t0 + (pil[N - 1] - f1l);
+        if (G2) sub_g2psi(wh, wl, g2h, g2l, ps1h, ps1l);
         two_sum(wh, -ehi.x, dh, t0);
         dw_hi = dh + (t0 + (wl - ehi.y));
       } else {
         const float* X = reinterpret_cast<const float*>(xb);
-        float f0h, f1h;
+        float f0h, f1h, ps0 = 0.0f, ps1 = 0.0f;
         {
           float fh[N];
 #pragma unroll
@@ -340,6 +374,17 @@ __device__ __forceinline__ void task_passes(const BatchLaunch& L, const TaskView
           // alpha X_Phi_d enters the Phi_d output
 #pragma unroll
           for (int i = 0; i < N; ++i) dP[i] = alpha * fh[i];
+          if (G2) {
+            // the gamma2 (d_d Psi - Phi_d) term of the Phi_d output
+            float ps[N], dps[N];
+#pragma unroll
+            for (int i = 0; i < N; ++i) ps[i] = X[base + i * stride];
+            eo_line_pg<N>(ps, dps, th);
+#pragma unroll
+            for (int i = 0; i < N; ++i) dP[i] = fmaf(-g2, fmaf(Fd, dps[i], cf * fh[i]), dP[i]);
+            ps0 = ps[0];
+            ps1 = ps[N - 1];
+          }
         }
 #pragma unroll
         for (int i = 0; i < N; ++i) {
@@ -353,8 +398,13 @@ __device__ __forceinline__ void task_passes(const BatchLaunch& L, const TaskView
           for (int i = 0; i < N; ++i) dP[i] = fmaf(Fd, dd[i], dP[i]);
         }
         const float* ext = reinterpret_cast<const float*>(fbk);
-        dw_lo = (pih[0] + f0h) - ext[(2 * d) * NN + fidx];
-        dw_hi = (pih[N - 1] - f1h) - ext[(2 * d + 1) * NN + fidx];
+        float wi_lo = pih[0] + f0h, wi_hi = pih[N - 1] - f1h;
+        if (G2) {
+          wi_lo = fmaf(-g2, ps0, wi_lo);
+          wi_hi = fmaf(-g2, ps1, wi_hi);
+        }
+        dw_lo = wi_lo - ext[(2 * d) * NN + fidx];
+        dw_hi = wi_hi - ext[(2 * d + 1) * NN + fidx];
       }
       dF[0] = fmaf(Gd, dw_lo, dF[0]);
       dP[0] = fmaf(Gd, dw_lo, dP[0]);
@@ -365,7 +415,7 @@ __device__ __forceinline__ void task_passes(const BatchLaunch& L, const TaskView
       // Phi_d output: to the output and, in place, for the face maps
 #pragma unroll
       for (int i = 0; i < N; ++i) {
-        W[w_index<COMP>(2 + d, base + i * stride, NP)] = dP[i];
+        W[w_index<COMP, G2>(2 + d, base + i * stride, NP)] = dP[i];
         Wg[(2 + d) * NP + base + i * stride] = dP[i];
       }
       if (d < 2) {
@@ -386,8 +436,8 @@ __device__ __forceinline__ void task_passes(const BatchLaunch& L, const TaskView
             wpi = fmaf(alpha, pih[i], wpi);
             wpsi = fmaf(alpha, reinterpret_cast<const float*>(xb)[p], wpsi);
           }
-          W[w_index<COMP>(1, p, NP)] = wpi;
-          W[w_index<COMP>(0, p, NP)] = wpsi;
+          W[w_index<COMP, G2>(1, p, NP)] = wpi;
+          W[w_index<COMP, G2>(0, p, NP)] = wpsi;
           Wg[NP + p] = wpi;
           Wg[p] = wpsi;
         }
@@ -399,9 +449,9 @@ __device__ __forceinline__ void task_passes(const BatchLaunch& L, const TaskView
 
 // COMP: each FP64 value of the staged X becomes its (hi, lo) FP32 pair in
 // place (the same 8 bytes), so that the passes split each value once.
-template <int N>
-__device__ __forceinline__ void split_x(const TaskView<true>& V, int g, int bt) {
-  constexpr int NP4 = 4 * N * N * N;
+template <int N, bool G2>
+__device__ __forceinline__ void split_x(const TaskView<true, G2>& V, int g, int bt) {
+  constexpr int NP4 = (G2 ? 5 : 4) * N * N * N;
   for (int s = 0; s < g; ++s) {
     double* X = reinterpret_cast<double*>(V.x(s));
     for (int q = threadIdx.x; q < NP4; q += bt) {
@@ -413,13 +463,15 @@ __device__ __forceinline__ void split_x(const TaskView<true>& V, int g, int bt) 
 }
 
 // The face values of W in the element's own resolution: for each face dir,
-// w = Pi + s_e Phi_d (s_e = +1 upper, -1 lower) at its N^2 points, into the
+// w = Pi + s_e Phi_d - gamma2 Psi (s_e = +1 upper, -1 lower) at its N^2
+// points, into the
 // element's own slots of the raw face buffer (coalesced); the face-map
 // kernel then maps them onto the neighbours' points.
-template <int n, bool COMP, int BT>
-__device__ __forceinline__ void task_raw_faces(const BatchLaunch& L, const TaskView<COMP>& V,
+template <int n, bool COMP, bool G2, int BT>
+__device__ __forceinline__ void task_raw_faces(const BatchLaunch& L, const TaskView<COMP, G2>& V,
                                                const int32_t* elems) {
   constexpr int nn = n * n, np = nn * n, F6 = 6 * nn;
+  const float g2 = (float)L.gamma2;
   for (int s = 0; s < V.g; ++s) {
     const float* W = reinterpret_cast<const float*>(V.x(s));
     float* dst = L.raw32 + L.foff[elems[s]];
@@ -427,43 +479,45 @@ __device__ __forceinline__ void task_raw_faces(const BatchLaunch& L, const TaskV
       const int dir = q / nn, r = q - dir * nn, d = dir >> 1;
       const bool upper = dir & 1;
       const int p = face_point(n, d, upper ? n - 1 : 0, r % n, r / n);
-      const float pi = W[w_index<COMP>(1, p, np)], ph = W[w_index<COMP>(2 + d, p, np)];
-      dst[q] = upper ? pi + ph : pi - ph;
+      const float pi = W[w_index<COMP, G2>(1, p, np)], ph = W[w_index<COMP, G2>(2 + d, p, np)];
+      float w = upper ? pi + ph : pi - ph;
+      if (G2) w = fmaf(-g2, W[w_index<COMP, G2>(0, p, np)], w);
+      dst[q] = w;
     }
   }
 }
 
-template <int N, bool COMP, int BT>
-__device__ __forceinline__ void run_task(const BatchLaunch& L, const TaskView<COMP>& V, float* S,
-                                         const float* tabs, const float* G, const float* F,
-                                         const int32_t* elems) {
+template <int N, bool COMP, int BT, bool G2>
+__device__ __forceinline__ void run_task(const BatchLaunch& L, const TaskView<COMP, G2>& V,
+                                         float* S, const float* tabs, const float* G,
+                                         const float* F, const int32_t* elems) {
   if constexpr (COMP) {
-    split_x<N>(V, V.g, BT);
+    split_x<N, G2>(V, V.g, BT);
     __syncthreads();
   }
-  task_passes<N, COMP>(L, V, S, tabs, V.g, (float)L.c, G, F);
+  task_passes<N, COMP, G2>(L, V, S, tabs, V.g, (float)L.c, G, F);
   if (L.raw32 != nullptr) {
     __syncthreads();
-    task_raw_faces<N, COMP, BT>(L, V, elems);
+    task_raw_faces<N, COMP, G2, BT>(L, V, elems);
   }
 }
 
-template <bool COMP, int BT, int NMAX>
-__device__ __forceinline__ void dispatch_task(const BatchLaunch& L, const TaskView<COMP>& V,
+template <bool COMP, int BT, int NMAX, bool G2>
+__device__ __forceinline__ void dispatch_task(const BatchLaunch& L, const TaskView<COMP, G2>& V,
                                               float* S, const float* tabs, const float* G,
                                               const float* F, const int32_t* elems) {
   switch (V.n) {
-    case 2: run_task<2, COMP, BT>(L, V, S, tabs, G, F, elems); break;
-    case 3: run_task<3, COMP, BT>(L, V, S, tabs, G, F, elems); break;
-    case 4: run_task<4, COMP, BT>(L, V, S, tabs, G, F, elems); break;
-    case 5: run_task<5, COMP, BT>(L, V, S, tabs, G, F, elems); break;
-    case 6: run_task<6, COMP, BT>(L, V, S, tabs, G, F, elems); break;
-    case 7: run_task<7, COMP, BT>(L, V, S, tabs, G, F, elems); break;
-    case 8: run_task<8, COMP, BT>(L, V, S, tabs, G, F, elems); break;
-    case 9: if (NMAX >= 9) run_task<(NMAX >= 9 ? 9 : 2), COMP, BT>(L, V, S, tabs, G, F, elems); break;
-    case 10: if (NMAX >= 10) run_task<(NMAX >= 10 ? 10 : 2), COMP, BT>(L, V, S, tabs, G, F, elems); break;
-    case 11: if (NMAX >= 11) run_task<(NMAX >= 11 ? 11 : 2), COMP, BT>(L, V, S, tabs, G, F, elems); break;
-    case 12: if (NMAX >= 12) run_task<(NMAX >= 12 ? 12 : 2), COMP, BT>(L, V, S, tabs, G, F, elems); break;
+    case 2: run_task<2, COMP, BT, G2>(L, V, S, tabs, G, F, elems); break;
+    case 3: run_task<3, COMP, BT, G2>(L, V, S, tabs, G, F, elems); break;
+    case 4: run_task<4, COMP, BT, G2>(L, V, S, tabs, G, F, elems); break;
+    case 5: run_task<5, COMP, BT, G2>(L, V, S, tabs, G, F, elems); break;
+    case 6: run_task<6, COMP, BT, G2>(L, V, S, tabs, G, F, elems); break;
+    case 7: run_task<7, COMP, BT, G2>(L, V, S, tabs, G, F, elems); break;
+    case 8: run_task<8, COMP, BT, G2>(L, V, S, tabs, G, F, elems); break;
+    case 9: if (NMAX >= 9) run_task<(NMAX >= 9 ? 9 : 2), COMP, BT, G2>(L, V, S, tabs, G, F, elems); break;
+    case 10: if (NMAX >= 10) run_task<(NMAX >= 10 ? 10 : 2), COMP, BT, G2>(L, V, S, tabs, G, F, elems); break;
+    case 11: if (NMAX >= 11) run_task<(NMAX >= 11 ? 11 : 2), COMP, BT, G2>(L, V, S, tabs, G, F, elems); break;
+    case 12: if (NMAX >= 12) run_task<(NMAX >= 12 ? 12 : 2), COMP, BT, G2>(L, V, S, tabs, G, F, elems); break;
     default: break;
   }
 }
@@ -473,7 +527,7 @@ __device__ __forceinline__ void dispatch_task(const BatchLaunch& L, const TaskVi
 // allocator, extents up to NMAX compiled in, STAGES pipeline buffers (2:
 // the next task's copies land while this one computes; 1: they are issued
 // when this one is done, and other resident CTAs cover the wait).
-template <bool COMP, int BT, int MINB, int NMAX, int STAGES>
+template <bool COMP, int BT, int MINB, int NMAX, int STAGES, bool G2>
 __global__ void __launch_bounds__(BT, MINB) stage_batch_kernel(BatchLaunch L) {
   constexpr int kMaxG = BT / (kMinN * kMinN);  // elements per task at most (N = 2)
   extern __shared__ __align__(128) unsigned char smem[];
@@ -496,14 +550,14 @@ __global__ void __launch_bounds__(BT, MINB) stage_batch_kernel(BatchLaunch L) {
   __syncthreads();
   const int64_t Gd = gridDim.x;
   int64_t task = blockIdx.x;
-  if (task < L.n_tasks && threadIdx.x == 0) issue_task<COMP>(L, L.tasks[task], bufs[0], &bars[0]);
+  if (task < L.n_tasks && threadIdx.x == 0) issue_task<COMP, G2>(L, L.tasks[task], bufs[0], &bars[0]);
   const double c = L.c;
   for (int k = 0; task < L.n_tasks; ++k, task += Gd) {
     const int b = STAGES == 2 ? (k & 1) : 0;
     const uint32_t parity = STAGES == 2 ? (uint32_t)((k >> 1) & 1) : (uint32_t)(k & 1);
     const int64_t next = task + Gd;
     if (STAGES == 2 && threadIdx.x == 0 && next < L.n_tasks)
-      issue_task<COMP>(L, L.tasks[next], bufs[b ^ 1], &bars[b ^ 1]);
+      issue_task<COMP, G2>(L, L.tasks[next], bufs[b ^ 1], &bars[b ^ 1]);
     const int2 tk = L.tasks[task];
     const int n = tk.x & 0xff, g = tk.x >> 8;
     // per-element data (overlaps the copies)
@@ -527,18 +581,18 @@ __global__ void __launch_bounds__(BT, MINB) stage_batch_kernel(BatchLaunch L) {
         mbar_wait(&bars[b ^ 1], (uint32_t)(((k + 1) >> 1) & 1), kLimitNs);
       return;
     }
-    TaskView<COMP> V;
+    TaskView<COMP, G2> V;
     V.buf = bufs[b];
     V.offs = s_offs;
     V.L = &L;
     V.n = n;
     V.g = g;
-    dispatch_task<COMP, BT, NMAX>(L, V, S, s_tab, s_G, s_F, s_elems);
+    dispatch_task<COMP, BT, NMAX, G2>(L, V, S, s_tab, s_G, s_F, s_elems);
     // generic-proxy accesses of this buffer before the next TMA writes into it
     fence_proxy_async_smem();
     __syncthreads();
     if (STAGES == 1 && threadIdx.x == 0 && next < L.n_tasks)
-      issue_task<COMP>(L, L.tasks[next], bufs[0], &bars[0]);
+      issue_task<COMP, G2>(L, L.tasks[next], bufs[0], &bars[0]);
   }
 }
 
@@ -580,7 +634,7 @@ __global__ void __launch_bounds__(256) accumulate_step_kernel(double* u, const f
 
 // ---------------------------------------------------------------- faces of u
 // Double-float exterior values of an FP64 state: one warp per (element,
-// face): w = Pi + s_e Phi_d split into hi + lo, mapped by T (compensated
+// face): w = Pi + s_e Phi_d - gamma2 Psi split into hi + lo, mapped by T (compensated
 // products and sums, hi + lo tables) onto the neighbour's face points.
 constexpr int kFaceWarps = 4;
 
@@ -607,6 +661,7 @@ __global__ void __launch_bounds__(32 * kFaceWarps) batch_faces_kernel(BatchFaceL
     const int oo = L.op_off[m * (kMaxN + 1) + n];
     for (int q = lane; q < m * n; q += 32) T[q] = make_float2(L.op_hi[oo + q], L.op_lo[oo + q]);
   }
+  const float g2h = (float)L.gamma2, g2l = (float)(L.gamma2 - (double)g2h);
   for (int q = lane; q < nn; q += 32) {
     const int p = face_point(n, d, slice, q % n, q / n);
     float ph, pl, qh, ql, wh, t0;
@@ -618,6 +673,11 @@ __global__ void __launch_bounds__(32 * kFaceWarps) batch_faces_kernel(BatchFaceL
     } else {
       two_sum(ph, -qh, wh, t0);
       t0 += pl - ql;
+    }
+    if (L.gamma2 != 0.0) {
+      float sh, sl;
+      split_df(L.x64[off + p], sh, sl);
+      sub_g2psi(wh, t0, g2h, g2l, sh, sl);
     }
     float hi, lo;
     two_sum(wh, t0, hi, lo);
@@ -752,40 +812,48 @@ constexpr ShapeSpec kShapes[] = {
 };
 constexpr int kNumShapes = sizeof(kShapes) / sizeof(kShapes[0]);
 
-template <bool COMP, int V>
+template <bool COMP, int V, bool G2>
 constexpr auto kernel_of() {
   constexpr ShapeSpec S = kShapes[V];
-  return stage_batch_kernel<COMP, S.bt, COMP ? S.minb_comp : S.minb_f32, S.nmax, S.stages>;
+  return stage_batch_kernel<COMP, S.bt, COMP ? S.minb_comp : S.minb_f32, S.nmax, S.stages, G2>;
 }
 
-template <bool COMP, int V>
+template <bool COMP, int V, bool G2>
 cudaError_t launch_v(const BatchLaunch& L, size_t smem, cudaStream_t s) {
-  constexpr auto k = kernel_of<COMP, V>();
+  constexpr auto k = kernel_of<COMP, V, G2>();
   cudaError_t e = set_kernel_smem<k>((int)smem, true);
   if (e != cudaSuccess) return e;
   k<<<(unsigned)L.grid, kShapes[V].bt, smem, s>>>(L);
   return cudaGetLastError();
 }
 
-template <bool COMP, int V>
+template <bool COMP, int V, bool G2>
 cudaError_t grid_v(size_t smem, int* per_sm) {
-  constexpr auto k = kernel_of<COMP, V>();
+  constexpr auto k = kernel_of<COMP, V, G2>();
   cudaError_t e = set_kernel_smem<k>((int)smem, true);
   if (e != cudaSuccess) return e;
   return cudaOccupancyMaxActiveBlocksPerMultiprocessor(per_sm, k, kShapes[V].bt, smem);
 }
 
+template <int V, bool G2>
+cudaError_t launch_g(bool comp, const BatchLaunch& L, size_t smem, cudaStream_t s) {
+  return comp ? launch_v<true, V, G2>(L, smem, s) : launch_v<false, V, G2>(L, smem, s);
+}
+
 template <int V>
-cudaError_t launch_any(bool comp, const BatchLaunch& L, size_t smem, cudaStream_t s) {
-  if (L.variant == V) return comp ? launch_v<true, V>(L, smem, s) : launch_v<false, V>(L, smem, s);
-  if constexpr (V + 1 < kNumShapes) return launch_any<V + 1>(comp, L, smem, s);
+cudaError_t launch_any(bool comp, bool g2, const BatchLaunch& L, size_t smem, cudaStream_t s) {
+  if (L.variant == V) return g2 ? launch_g<V, true>(comp, L, smem, s) : launch_g<V, false>(comp, L, smem, s);
+  if constexpr (V + 1 < kNumShapes) return launch_any<V + 1>(comp, g2, L, smem, s);
   return cudaErrorInvalidValue;
 }
 
 template <int V>
-cudaError_t grid_any(bool comp, int variant, size_t smem, int* per_sm) {
-  if (variant == V) return comp ? grid_v<true, V>(smem, per_sm) : grid_v<false, V>(smem, per_sm);
-  if constexpr (V + 1 < kNumShapes) return grid_any<V + 1>(comp, variant, smem, per_sm);
+cudaError_t grid_any(bool comp, bool g2, int variant, size_t smem, int* per_sm) {
+  if (variant == V) {
+    if (g2) return comp ? grid_v<true, V, true>(smem, per_sm) : grid_v<false, V, true>(smem, per_sm);
+    return comp ? grid_v<true, V, false>(smem, per_sm) : grid_v<false, V, false>(smem, per_sm);
+  }
+  if constexpr (V + 1 < kNumShapes) return grid_any<V + 1>(comp, g2, variant, smem, per_sm);
   return cudaErrorInvalidValue;
 }
 
@@ -799,9 +867,9 @@ int batch_max_extent(int variant) { return kShapes[variant].nmax; }
 
 int batch_task_elements(int n, int variant) { return task_g(n, batch_threads(variant)); }
 
-void batch_smem_bytes(int n, bool comp, int variant, size_t* buf, size_t* s) {
+void batch_smem_bytes(int n, bool comp, bool g2, int variant, size_t* buf, size_t* s) {
   const int g = task_g(n, batch_threads(variant));
-  *buf = (size_t)g * (x_slot(n, comp) + f_slot(n, comp));
+  *buf = (size_t)g * (x_slot(n, comp, g2) + f_slot(n, comp));
   *s = (size_t)round128(g * n * n * n * 4);
 }
 
@@ -840,16 +908,16 @@ cudaError_t launch_stage_batch(const BatchLaunch& L, cudaStream_t s) {
   if (L.w32 == nullptr) return cudaErrorInvalidValue;
   if (L.variant < 0 || L.variant >= kNumShapes) return cudaErrorInvalidValue;
   const size_t smem = batch_smem_total(L.variant, L.buf_bytes, L.s_bytes);
-  return launch_any<0>(comp, L, smem, s);
+  return launch_any<0>(comp, L.gamma2 != 0.0, L, smem, s);
 }
 
-cudaError_t batch_grid(bool comp, int variant, size_t smem, int* grid) {
+cudaError_t batch_grid(bool comp, bool g2, int variant, size_t smem, int* grid) {
   int dev = 0, sms = 0, per_sm = 0;
   cudaError_t e;
   if ((e = cudaGetDevice(&dev)) != cudaSuccess) return e;
   if ((e = cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev)) != cudaSuccess) return e;
   if (variant < 0 || variant >= kNumShapes) return cudaErrorInvalidValue;
-  if ((e = grid_any<0>(comp, variant, smem, &per_sm)) != cudaSuccess) return e;
+  if ((e = grid_any<0>(comp, g2, variant, smem, &per_sm)) != cudaSuccess) return e;
   if (per_sm < 1) return cudaErrorInvalidConfiguration;
   *grid = sms * per_sm;
   return cudaSuccess;

@@ -41,6 +41,7 @@ using dev::Eo;
 using dev::eo_line;
 using dev::eo_line_df;
 using dev::split_df;
+using dev::sub_g2psi;
 using dev::two_sum;
 using dev::widen;
 
@@ -159,7 +160,8 @@ __global__ void __launch_bounds__(N * N * EPB) stage_general_kernel(GeneralLaunc
         const int v = face_point(nn, d, nslice, a, b);
         const int64_t np_n = (int64_t)nn * nn * nn;
         if (kF32) {
-          const float w = L.x32[noff + np_n + v] - (float)s * L.x32[noff + (2 + d) * np_n + v];
+          float w = L.x32[noff + np_n + v] - (float)s * L.x32[noff + (2 + d) * np_n + v];
+          if (L.gamma2 != 0.0) w = fmaf(-(float)L.gamma2, L.x32[noff + v], w);
           float* dst = reinterpret_cast<float*>(nn == N ? ex : t1) + (nn == N ? dir * NN : dir * kNmax * kNmax);
           dst[q] = w;
         } else if (kF64) {
@@ -177,6 +179,12 @@ __global__ void __launch_bounds__(N * N * EPB) stage_general_kernel(GeneralLaunc
           } else {
             two_sum(ph, qh, wh, t0);
             t0 += pl + ql;
+          }
+          if (L.gamma2 != 0.0) {
+            float sh, sl;
+            split_df(L.x64[noff + v], sh, sl);
+            const float gh = (float)L.gamma2;
+            sub_g2psi(wh, t0, gh, (float)(L.gamma2 - (double)gh), sh, sl);
           }
           float2* dst = reinterpret_cast<float2*>(nn == N ? ex : t1) + (nn == N ? dir * NN : dir * kNmax * kNmax);
           dst[q] = make_float2(wh, t0);
@@ -357,13 +365,40 @@ __global__ void __launch_bounds__(N * N * EPB) stage_general_kernel(GeneralLaunc
           }
         }
         const float* th = T32 + d * TAB;
+        // Psi at the line's ends, for the gamma2 Psi part of w
+        float ps0h = 0.0f, ps0l = 0.0f, ps1h = 0.0f, ps1l = 0.0f;
         if (kComp) {
           const float* tl = T32 + 3 * TAB + d * TAB;
           eo_line_df<N>(fh, fl, dF, th, tl);
           eo_line_df<N>(pih, pil, dP, th, tl);
+          if (L.gamma2 != 0.0) {
+            // the gamma2 (d_d Psi - Phi_d) term of the Phi_d output
+            float psh[N], psl[N], dps[N];
+#pragma unroll
+            for (int i = 0; i < N; ++i) split_df(L.x64[off + base + i * stride], psh[i], psl[i]);
+            eo_line_df<N>(psh, psl, dps, th, tl);
+            const float g2 = (float)L.gamma2, cc = (float)c;
+#pragma unroll
+            for (int i = 0; i < N; ++i) dP[i] = fmaf(-g2, dps[i] + cc * (fh[i] + fl[i]), dP[i]);
+            ps0h = psh[0];
+            ps0l = psl[0];
+            ps1h = psh[N - 1];
+            ps1l = psl[N - 1];
+          }
         } else {
           eo_line<N, float>(fh, dF, th);
           eo_line<N, float>(pih, dP, th);
+          if (L.gamma2 != 0.0) {
+            float ps[N], dps[N];
+#pragma unroll
+            for (int i = 0; i < N; ++i) ps[i] = L.x32[off + base + i * stride];
+            eo_line<N, float>(ps, dps, th);
+            const float g2 = (float)L.gamma2, cc = (float)c;
+#pragma unroll
+            for (int i = 0; i < N; ++i) dP[i] = fmaf(-g2, dps[i] + cc * fh[i], dP[i]);
+            ps0h = ps[0];
+            ps1h = ps[N - 1];
+          }
         }
         if (L.boundary) {
           const float G = (float)(-0.25 * c * (double)(N * (N - 1)) * jd[d]);
@@ -372,18 +407,22 @@ __global__ void __launch_bounds__(N * N * EPB) stage_general_kernel(GeneralLaunc
             const float2* ext = reinterpret_cast<const float2*>(ex);
             const float2 elo = ext[(2 * d) * NN + fidx], ehi = ext[(2 * d + 1) * NN + fidx];
             float wh, wl, t0, dh;
+            const float gh = (float)L.gamma2, gl = (float)(L.gamma2 - (double)gh);
             two_sum(pih[0], fh[0], wh, t0);
             wl = t0 + (pil[0] + fl[0]);
+            if (L.gamma2 != 0.0) sub_g2psi(wh, wl, gh, gl, ps0h, ps0l);
             two_sum(wh, -elo.x, dh, t0);
             dw_lo = dh + (t0 + (wl - elo.y));
             two_sum(pih[N - 1], -fh[N - 1], wh, t0);
             wl = t0 + (pil[N - 1] - fl[N - 1]);
+            if (L.gamma2 != 0.0) sub_g2psi(wh, wl, gh, gl, ps1h, ps1l);
             two_sum(wh, -ehi.x, dh, t0);
             dw_hi = dh + (t0 + (wl - ehi.y));
           } else {
             const float* ext = reinterpret_cast<const float*>(ex);
-            dw_lo = (pih[0] + fh[0]) - ext[(2 * d) * NN + fidx];
-            dw_hi = (pih[N - 1] - fh[N - 1]) - ext[(2 * d + 1) * NN + fidx];
+            const float g2 = (float)L.gamma2;
+            dw_lo = fmaf(-g2, ps0h, pih[0] + fh[0]) - ext[(2 * d) * NN + fidx];
+            dw_hi = fmaf(-g2, ps1h, pih[N - 1] - fh[N - 1]) - ext[(2 * d + 1) * NN + fidx];
           }
           dF[0] = fmaf(G, dw_lo, dF[0]);
           dP[0] = fmaf(G, dw_lo, dP[0]);

@@ -56,9 +56,17 @@ __device__ __forceinline__ void line_geometry(int a, int line, int& base, int& s
 
 // Resident blocks per SM asked of the register allocator: three for the
 // plain FP32 stages, whose split tables are read from shared memory where
-// used (fewer registers); two for the compensated stage.
+// used (fewer registers); two for the compensated stage.  Extents 11 and 12
+// ask one fewer: with three (two) their lines spill 150-230 (110-160) bytes
+// (ptxas), at two (one) nothing.
 template <int N, bool COMP>
-__global__ void __launch_bounds__(kThreads, COMP ? 2 : 3) csw_stage_mixed_kernel(CswMixedLaunch L) {
+constexpr int csw_mixed_min_blocks() {
+  return (COMP ? 2 : 3) - (N >= 11 ? 1 : 0);
+}
+
+template <int N, bool COMP>
+__global__ void __launch_bounds__(kThreads, csw_mixed_min_blocks<N, COMP>())
+    csw_stage_mixed_kernel(CswMixedLaunch L) {
   using S = CmShape<N, COMP>;
   constexpr int NN = S::NN, NP = S::NP, PTS = S::PTS, TAB = S::TAB;
   extern __shared__ float fsm[];

@@ -184,6 +184,9 @@ struct DgswHandle_ {
   double filter_alpha = 0.0;
   int filter_half_power = 0;
   double* filt = nullptr;  // [kMaxN + 1][kMaxN * kMaxN], matrix of extent n at n
+  float* filt32 = nullptr;  // the same in FP32 hi parts, then lo parts (mixed precision)
+  float* fr32 = nullptr;    // mixed precision with the filter: R = (F - I) u0
+  float* fw3 = nullptr;     //   and the third stage's dt L(D2)
   // graphs of whole steps
   cudaGraphExec_t graph_one = nullptr;
   cudaGraphExec_t graph_many = nullptr;
@@ -654,6 +657,104 @@ cudaError_t apply_filter(DgswHandle h, double* u) {
   return launch_filter(F, h->stream);
 }
 
+// W = c L(X) on the handle's mixed-precision kernels: X the FP64 state
+// (x64, compensated double-float arithmetic) or an FP32 increment (x32).
+cudaError_t mixed_apply_L(DgswHandle h, const double* x64, const float* x32, double c, float* w32) {
+  if (h->curved) {
+    CswMixedLaunch L = base_csw_mixed(h);
+    L.x64 = x64;
+    L.x32 = x32;
+    L.c = c;
+    L.w32 = w32;
+    return launch_csw_mixed(L, h->stream);
+  }
+  if (h->general) {
+    GeneralLaunch G = base_general(h);
+    G.prec = x64 ? kPrecComp : kPrecF32;
+    G.x64 = x64;
+    G.x32 = x32;
+    G.c = c;
+    G.w32 = w32;
+    return launch_general_classes(h, G);
+  }
+  MixedLaunch L = base_mixed(h);
+  L.x64 = x64;
+  L.x32 = x32;
+  L.c = c;
+  L.w32 = w32;
+  return launch_mixed(h, L);
+}
+
+// A filter launch (residual or combine) over every element of the handle.
+template <typename Launch>
+cudaError_t mixed_filter_all(DgswHandle h, MixedFilterLaunch F, Launch launch) {
+  const size_t stride = (size_t)kMaxN * kMaxN, half = (size_t)(kMaxN + 1) * stride;
+  if (h->general) {
+    F.offset = h->offset;
+    for (int n = kMinN; n <= kMaxN; ++n) {
+      if (h->class_count[n] == 0) continue;
+      F.n = n;
+      F.tasks = h->class_tasks[n];
+      F.n_tasks = h->class_count[n];
+      F.Fh = h->filt32 + (size_t)n * stride;
+      F.Fl = h->filt32 + half + (size_t)n * stride;
+      cudaError_t e = launch(F, h->stream);
+      if (e != cudaSuccess) return e;
+    }
+    return cudaSuccess;
+  }
+  F.n = h->dom.elem_n[0];
+  F.n_tasks = h->dom.n_elem;
+  F.Fh = h->filt32 + (size_t)F.n * stride;
+  F.Fl = h->filt32 + half + (size_t)F.n * stride;
+  return launch(F, h->stream);
+}
+
+// Substep k of the mixed-precision SSP-RK3 step with the filter after every
+// substep (filter_mixed.cu): with R = (F - I) u0,
+//   k = 0: W1 = dt L u0,  D1 = R + F W1                       (w1)
+//   k = 1: W2 = dt L D1,  D2 = 3/4 R + 1/4 D1 + 1/4 F(D1 + W2) (w2)
+//   k = 2: W3 = dt L D2,  u = u0 + 1/3 R + 2/3 D1 + 2/3 F(D2 + W3)
+// out (k < 2, optional) receives u0 + D_k; k = 2 writes out.
+cudaError_t mixed_filtered_stage(DgswHandle h, int k, double dt, const double* u0, double* out) {
+  cudaError_t e = cudaSuccess;
+  MixedFilterLaunch F;
+  F.r32 = h->fr32;
+  if (k == 0) {
+    if ((e = mixed_apply_L(h, u0, nullptr, dt, h->w1)) != cudaSuccess) return e;
+    MixedFilterLaunch R;
+    R.u64 = u0;
+    R.r32 = h->fr32;
+    if ((e = mixed_filter_all(h, R, launch_filter_residual)) != cudaSuccess) return e;
+    F.x32 = h->w1;
+    F.ar = 1.0;
+    F.b = 1.0;
+    F.w32 = h->w1;
+  } else if (k == 1) {
+    if ((e = mixed_apply_L(h, nullptr, h->w1, dt, h->w2)) != cudaSuccess) return e;
+    F.x32 = h->w1;
+    F.y32 = h->w2;
+    F.d32 = h->w1;
+    F.ar = 0.75;
+    F.ad = 0.25;
+    F.b = 0.25;
+    F.w32 = h->w2;
+  } else {
+    if ((e = mixed_apply_L(h, nullptr, h->w2, dt, h->fw3)) != cudaSuccess) return e;
+    F.x32 = h->w2;
+    F.y32 = h->fw3;
+    F.d32 = h->w1;
+    F.ar = 1.0 / 3.0;
+    F.ad = 2.0 / 3.0;
+    F.b = 2.0 / 3.0;
+  }
+  if (out) {
+    F.out64 = out;
+    F.base64 = u0;
+  }
+  return mixed_filter_all(h, F, launch_filter_combine);
+}
+
 // ---- launch autotuner ------------------------------------------------------
 // The FP64 stage kernel is compiled in two launch configurations per N
 // (elements per block and resident blocks asked of the register allocator).
@@ -964,6 +1065,12 @@ cudaError_t enqueue_mixed_stage(DgswHandle h, int k, double dt, const double* u0
 //   u  = 1/3 u + 2/3 t2 + 2dt/3 L(t2)   (in place: each element reads only
 //   its own u, neighbours' faces come from t2).
 cudaError_t enqueue_step(DgswHandle h, double dt) {
+  if (mixed(h) && h->filter_on) {
+    cudaError_t e = mixed_filtered_stage(h, 0, dt, h->state, nullptr);
+    if (e == cudaSuccess) e = mixed_filtered_stage(h, 1, dt, h->state, nullptr);
+    if (e == cudaSuccess) e = mixed_filtered_stage(h, 2, dt, h->state, h->state);
+    return e;
+  }
   if (h->batch) return enqueue_batch_step(h, dt);
   if (mixed(h)) {
     cudaError_t e = enqueue_mixed_stage(h, 0, dt, h->state, nullptr);
@@ -2214,6 +2321,9 @@ int dgsw_destroy(DgswHandle h) {
   if (h->c_F32) cudaFree(h->c_F32);
   if (h->c_X) cudaFree(h->c_X);
   if (h->filt) cudaFree(h->filt);
+  if (h->filt32) cudaFree(h->filt32);
+  if (h->fr32) cudaFree(h->fr32);
+  if (h->fw3) cudaFree(h->fw3);
   if (h->lgl_w) cudaFree(h->lgl_w);
   if (h->norm_partial) cudaFree(h->norm_partial);
   if (h->r_faces) cudaFree(h->r_faces);
@@ -2479,7 +2589,10 @@ int dgsw_substep(DgswHandle h, int k, double dt) {
   if (mixed(h)) {
     if (k == 0)
       DGSW_CUDA(h, cudaMemcpyAsync(h->u0s, h->state, bytes, cudaMemcpyDeviceToDevice, h->stream));
-    DGSW_CUDA(h, enqueue_mixed_stage(h, k, dt, h->u0s, h->state));
+    if (h->filter_on)
+      DGSW_CUDA(h, mixed_filtered_stage(h, k, dt, h->u0s, h->state));
+    else
+      DGSW_CUDA(h, enqueue_mixed_stage(h, k, dt, h->u0s, h->state));
     return DGSW_OK;
   }
   if (h->gauss) {
@@ -2721,9 +2834,6 @@ int dgsw_set_exponential_filter(DgswHandle h, double alpha, int half_power, int 
   }
   if (!std::isfinite(alpha) || alpha < 0.0 || half_power < 0 || half_power > 64)
     return fail(h, DGSW_ERR_ARGUMENT, "need a finite alpha >= 0 and half_power in [0, 64]");
-  if (mixed(h))
-    return fail(h, DGSW_ERR_UNSUPPORTED,
-                "the filter acts on FP64 substep states; use FP64 precision");
   if (h->gauss)
     return fail(h, DGSW_ERR_UNSUPPORTED, "the filter is built for Gauss-Lobatto meshes");
   if (int rc = select_device(h)) return rc;
@@ -2734,6 +2844,20 @@ int dgsw_set_exponential_filter(DgswHandle h, double alpha, int half_power, int 
   if (!h->filt) DGSW_CUDA(h, cudaMalloc(&h->filt, mats.size() * sizeof(double)));
   DGSW_CUDA(h, cudaMemcpy(h->filt, mats.data(), mats.size() * sizeof(double),
                           cudaMemcpyHostToDevice));
+  if (mixed(h)) {
+    // FP32 hi and lo parts of the matrices, the residual and third-stage buffers
+    std::vector<float> m32(2 * mats.size(), 0.0f);
+    for (size_t i = 0; i < mats.size(); ++i) {
+      m32[i] = (float)mats[i];
+      m32[mats.size() + i] = (float)(mats[i] - (double)m32[i]);
+    }
+    if (!h->filt32) DGSW_CUDA(h, cudaMalloc(&h->filt32, m32.size() * sizeof(float)));
+    DGSW_CUDA(h, cudaMemcpy(h->filt32, m32.data(), m32.size() * sizeof(float),
+                            cudaMemcpyHostToDevice));
+    const size_t b32 = (size_t)h->dom.offset.back() * sizeof(float) + 64;
+    if (!h->fr32) DGSW_CUDA(h, cudaMalloc(&h->fr32, b32));
+    if (!h->fw3) DGSW_CUDA(h, cudaMalloc(&h->fw3, b32));
+  }
   destroy_graphs(h);
   h->filter_on = true;
   h->filter_alpha = alpha;

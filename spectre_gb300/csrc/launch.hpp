@@ -446,6 +446,31 @@ struct FilterLaunch {
 };
 cudaError_t launch_filter(const FilterLaunch& L, cudaStream_t s);
 
+// The exponential filter on the mixed-precision path (filter_mixed.cu).
+// residual: r32 = (F - I) u64, compensated; combine: out = ar r32 + ad d32 +
+// b F(x32 + y32), to w32 and / or out64 = base64 + out.  tasks / offset null:
+// elements 0..n_tasks-1 of extent n, packed; else the listed elements at
+// their value offsets.  Fh, Fl: the n x n filter matrix, FP32 hi and lo.
+struct MixedFilterLaunch {
+  int n = 0;
+  int64_t n_tasks = 0;
+  const int32_t* tasks = nullptr;
+  const int64_t* offset = nullptr;
+  const float* Fh = nullptr;
+  const float* Fl = nullptr;
+  const double* u64 = nullptr;
+  float* r32 = nullptr;          // residual output / combine input
+  const float* x32 = nullptr;
+  const float* y32 = nullptr;
+  const float* d32 = nullptr;
+  double ar = 0.0, ad = 0.0, b = 1.0;
+  float* w32 = nullptr;
+  double* out64 = nullptr;
+  const double* base64 = nullptr;
+};
+cudaError_t launch_filter_residual(const MixedFilterLaunch& L, cudaStream_t s);
+cudaError_t launch_filter_combine(const MixedFilterLaunch& L, cudaStream_t s);
+
 // ObserveNorms partial sums per element and their fixed-order total
 // (norms.cu).  Flat elements: width (3 per element) gives det J; curved:
 // ij (9 x N^3 per element) gives det J = 1 / det(inverse Jacobian).

@@ -6,7 +6,9 @@ CPU: the oracle's 1D filter matrix against the reference's known answer
 exp(-alpha (k/(N-1))^(2 half_power)), 2e-12), and the product's host matrix
 against the oracle's (1e-13).  GPU: filtered SSP-RK3 steps of the flat,
 the mixed-extent and the curved paths against the oracle stepped substep by
-substep with the filter (<= 1e-11 relative per variable).
+substep with the filter (<= 1e-11 relative per variable); the same in mixed
+precision (<= 1e-6), and the configuration-5 shell over 1000 filtered steps,
+mixed against FP64 (rel L2 <= 1e-6).
 """
 import numpy as np
 import pytest
@@ -124,7 +126,81 @@ def test_curved_filtered_steps_match_oracle(oracle):
 
 
 @pytest.mark.gpu
-def test_filter_refused_for_mixed_precision():
-    with DgEvolution([Brick((2, 2, 2))], 6, precision=dgsw.PRECISION_MIXED) as ev:
-        with pytest.raises(dgsw.DgswError, match="FP64"):
+@pytest.mark.parametrize("n", [6, 7])
+def test_mixed_filtered_steps_match_oracle(oracle, n):
+    # mixed precision with the filter after every substep (filter_mixed.cu):
+    # the residual (F - I) u0 in double-float, the filters of the increments
+    # in FP32; against the oracle's FP64 filtered steps
+    bricks = [Brick((3, 2, 4))]
+    dt = 2e-3
+    rng = np.random.default_rng(13 + n)
+    en = oracle.elem_points(bricks, n)
+    u = rng.uniform(-1, 1, int(oracle.offsets(en)[-1]))
+    ref = _oracle_filtered(oracle, lambda x: oracle.rhs(bricks, n, x), u, dt, 4, en)
+    with DgEvolution(bricks, n, precision=dgsw.PRECISION_MIXED) as ev:
+        ev.set_exponential_filter(ALPHA, HALF_POWER)
+        ev.set_state(u)
+        ev.step(4, dt)
+        a = ev.get_state()
+        assert _rel(a, ref, en) <= 1e-6
+        # one substep at a time gives the same states
+        ev.set_state(u)
+        for _ in range(4):
+            for k in range(3):
+                ev.substep(k, dt)
+        np.testing.assert_array_equal(ev.get_state(), a)
+
+
+@pytest.mark.gpu
+def test_mixed_extent_mixed_filtered_steps_match_oracle(oracle):
+    bricks = [Brick((2, 3, 2))]
+    rng = np.random.default_rng(6)
+    pts = rng.integers(4, 11, size=12).astype(np.int32)
+    dt = 1e-3
+    en = oracle.elem_points(bricks, pts)
+    u = rng.uniform(-1, 1, int(oracle.offsets(en)[-1]))
+    ref = _oracle_filtered(oracle, lambda x: oracle.rhs(bricks, pts, x, gamma2=0.5), u, dt, 3, en)
+    with DgEvolution(bricks, pts, precision=dgsw.PRECISION_MIXED, gamma2=0.5) as ev:
+        ev.set_exponential_filter(ALPHA, HALF_POWER)
+        ev.set_state(u)
+        ev.step(3, dt)
+        assert _rel(ev.get_state(), ref, en) <= 1e-6
+
+
+@pytest.mark.gpu
+def test_curved_mixed_filtered_steps_match_oracle(oracle):
+    n, dt = 6, 1e-2
+    s = oracle.shell(1.9, 20.0, 1, 1, n, 1.0, 0.0, 1.0)
+    u = oracle.shell_initial_data(s, 8.0, 1.0)
+    E = u.shape[0]
+    en = np.full(E, n, dtype=np.int32)
+    rhs = lambda x: oracle.shell_rhs(s, x.reshape(u.shape))[0].ravel()  # noqa: E731
+    ref = _oracle_filtered(oracle, rhs, u, dt, 5, en)
+    with CurvedDgEvolution(Shell(1.9, 20.0, 1, 1), n, gamma2=1.0,
+                           precision=dgsw.PRECISION_MIXED) as ev:
+        ev.set_exponential_filter(ALPHA, HALF_POWER)
+        ev.set_state(u.ravel())
+        ev.step(5, dt)
+        assert _rel(ev.get_state(), ref, en) <= 1e-6
+
+
+@pytest.mark.gpu
+@pytest.mark.slow
+def test_curved_mixed_filtered_config5_full_run():
+    # the configuration-5 shell (768 elements x 10^3 points, Kerr-Schild M = 1,
+    # gamma1 = 0, gamma2 = 1, dt = 1e-3) over its 1000 steps with the filter
+    # after every substep, as the reference's curved executable's step
+    # actions apply it: mixed precision against FP64, rel L2 <= 1e-6
+    states = []
+    for prec in (dgsw.PRECISION_FP64, dgsw.PRECISION_MIXED):
+        sh = Shell(1.9, 20.0, 2, 3, "logarithmic", 1.0, 0.0)
+        with CurvedDgEvolution(sh, 10, precision=prec, gamma2=1.0) as ev:
             ev.set_exponential_filter(ALPHA, HALF_POWER)
+            ev.set_gaussian_shell(1.0, 8.0, 1.0)
+            ev.step(1000, 1e-3)
+            states.append(ev.get_state())
+    a, m = states
+    assert np.isfinite(m).all()
+    err = float(np.linalg.norm(m - a) / np.linalg.norm(a))
+    print("curved mixed vs FP64, both filtered, 1000 steps: rel L2 %.3e" % err)
+    assert err <= 1e-6

@@ -603,6 +603,7 @@ def time_curved(args, dev, with_cpu):
            "rel_l2_mixed_vs_fp64_after_steps": float(np.linalg.norm(m - a) / np.linalg.norm(a)),
            "max_abs_mixed_vs_fp64": float(np.abs(m - a).max())}
     out["adams"] = time_curved_adams(shell, n, dt, steps, dev)
+    out["filtered"] = time_curved_filtered(shell, n, dt, steps, dev)
     if with_cpu:
         s_orc = pyoracle.shell(1.9, 20.0, 2, 3, n, 1.0, 0.0, 1.0)
         u = pyoracle.shell_initial_data(s_orc, 8.0, 1.0)
@@ -619,6 +620,41 @@ def time_curved(args, dev, with_cpu):
                                          "%d evaluations, %.2f s each (includes its geometry "
                                          "set-up)" % (cpu_flags(), reps, el)}
     return out
+
+
+def time_curved_filtered(shell, n, dt, steps, dev):
+    """The curved case with the exponential filter (alpha 36, half power 8)
+    after every substep, as the reference's curved executable applies it:
+    FP64 and mixed over the same steps, and their rel L2 difference."""
+    import torch
+    from spectre_gb300.dgsw import CurvedDgEvolution, PRECISION_FP64, PRECISION_MIXED
+    res, states = {}, {}
+    for name, prec in (("fp64", PRECISION_FP64), ("mixed", PRECISION_MIXED)):
+        with CurvedDgEvolution(shell, n, precision=prec, gamma2=1.0, device=dev) as ev:
+            ev.set_exponential_filter(36.0, 8)
+            ev.set_gaussian_shell(1.0, 8.0, 1.0)
+            u0 = ev.get_state()
+            ev.step(16, dt)
+            ev.step(1, dt)
+            ev.set_state(u0)
+            stream = torch.cuda.ExternalStream(ev.stream_ptr(), device=dev)
+            e0 = torch.cuda.Event(enable_timing=True)
+            e1 = torch.cuda.Event(enable_timing=True)
+            torch.cuda.synchronize()
+            e0.record(stream)
+            ev.step(steps, dt, sync=False)
+            e1.record(stream)
+            e1.synchronize()
+            ms = e0.elapsed_time(e1)
+            states[name] = ev.get_state()
+            res[name] = {"value": ev.grid_points * 3 * steps / (ms * 1e-3), "unit": UNIT,
+                         "ms_per_step": ms / steps}
+    a, m = states["fp64"], states["mixed"]
+    res["filter"] = "Filters::Exponential alpha=36, half_power=8, after every substep"
+    res["steps"] = steps
+    res["mixed_speedup_vs_fp64"] = res["fp64"]["ms_per_step"] / res["mixed"]["ms_per_step"]
+    res["rel_l2_mixed_vs_fp64_after_steps"] = float(np.linalg.norm(m - a) / np.linalg.norm(a))
+    return res
 
 
 def ab_bytes_per_point(order, n):

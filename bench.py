@@ -306,11 +306,13 @@ def time_path(args, precision, dev, rank, ws, sample_clocks):
     """Times args.steps SSP-RK3 steps of one precision; returns the numbers
     and the final state (host copy)."""
     import torch
-    from spectre_gb300 import Brick, DgEvolution
+    from spectre_gb300 import Brick, DgEvolution, PRECISION_MIXED
     bricks = [Brick((args.elements, args.elements, args.elements))]
     params = np.array([[1.0, 0.5, math.pi, math.pi, math.pi]])
     ev = DgEvolution(bricks, N_PTS, precision=precision, device=dev)
     ev.set_initial_data("gaussian", params)
+    if precision == PRECISION_MIXED and args.mixed_variant >= 0:
+        ev.tune(force_variant=args.mixed_variant)
     stream = torch.cuda.ExternalStream(ev.stream_ptr(), device=dev)
     warm = max(args.warmup, 3)
     for _ in range(warm):
@@ -903,6 +905,9 @@ def main():
     ap.add_argument("--batched-precision", default="both", choices=["both", "fp64", "mixed"],
                     help="which precision paths the 256-instance workload times (both by "
                          "default; one alone only for profiling captures)")
+    ap.add_argument("--mixed-variant", type=int, default=-1,
+                    help="impose one launch candidate of the uniform mixed path (dgsw_tune) "
+                         "instead of the fastest; for profiling captures")
     ap.add_argument("--elements", type=int, default=ELEMS,
                     help="elements per axis (default 32: the benchmark workload; smaller "
                          "values only for profiling captures)")

@@ -369,8 +369,10 @@ int dgsw_autotune(DgswHandle h, int force_variant, int* variant, double* ms_per_
  * on elements of differing extents: the persistent batch kernels' compiled
  * launch shapes -- threads per CTA, resident CTAs per SM, pipeline buffers,
  * largest extent), DGSW_TUNE_MIXED_PIPE (mixed precision on one even extent:
- * the pipelined kernel with two pipeline buffers, or one buffer and more
- * resident CTAs), or DGSW_TUNE_NONE (fixed configurations).  Re-times every
+ * four candidates, the pipelined kernel with two pipeline buffers or one
+ * buffer and more resident CTAs (bit 0), each with the step's FP64 update
+ * u0 + W as a separate stream or in the last stage's epilogue (bit 1)), or
+ * DGSW_TUNE_NONE (fixed configurations).  Re-times every
  * candidate now on the handle's own state (saved and restored), keeps the
  * fastest (force_variant >= 0 imposes one instead) and returns the number of
  * candidates, the choice and ms per step of each (ms_per_step holds

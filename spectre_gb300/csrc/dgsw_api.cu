@@ -98,7 +98,7 @@ struct DgswHandle_ {
   // launch shape of the uniform-extent pipelined mixed kernel (stage_mixed_pipe.cu)
   int pipe_variant = 0;
   bool pipe_tuned = false;
-  double pipe_tune_ms[2] = {0.0, 0.0};
+  double pipe_tune_ms[4] = {0.0, 0.0, 0.0, 0.0};
   int bt_fu_age = 0;  // steps since the state's face values were formed from it
   // misfit objective and discrete adjoint (uniform FP64 path)
   EoTable eoT{};
@@ -287,7 +287,7 @@ MixedLaunch base_mixed(DgswHandle h) {
   L.jac = h->jac;
   L.eo = h->eo;
   L.err = h->dev_err;
-  L.variant = h->pipe_variant;
+  L.variant = h->pipe_variant & 1;
   return L;
 }
 
@@ -906,9 +906,11 @@ int batch_autotune(DgswHandle h, bool force) {
   return DGSW_OK;
 }
 
-// The uniform-extent mixed path on the pipelined kernel (even extents): its
-// two launch shapes (two pipeline buffers, or one with more resident CTAs)
-// timed the same way, cached per (extent, elements).
+// The uniform-extent mixed path on the pipelined kernel (even extents): four
+// candidates timed the same way, cached per (extent, elements).  Bit 0: two
+// pipeline buffers, or one with more resident CTAs; bit 1: the last stage
+// writes W for a separate FP64 accumulate stream, or forms u0 + W in its own
+// epilogue.
 bool pipe_tunable(DgswHandle h) {
   return mixed(h) && !h->batch && !h->curved && !h->general && !h->gauss && !h->refined &&
          !h->adams && mixed_pipe_supported(h->dom.elem_n[0]);
@@ -931,7 +933,7 @@ int pipe_autotune(DgswHandle h, bool force) {
   const int keep = h->pipe_variant;
   int best = -1;
   cudaError_t err = time_step_shapes(
-      h, 2,
+      h, 4,
       [&](int v) {
         h->pipe_variant = v;
         return true;
@@ -1043,6 +1045,14 @@ cudaError_t enqueue_mixed_stage(DgswHandle h, int k, double dt, const double* u0
     L.alpha = 2.0 / 3.0;
     L.beta = 2.0 / 3.0;
     L.c = (2.0 / 3.0) * dt;
+    if (out && mixed_pipe_supported(L.n) && (h->pipe_variant & 2)) {
+      // u0 + W formed in the stage's epilogue, one coalesced pass over each
+      // element's block after its W is complete in shared memory
+      L.out64 = out;
+      L.base64 = u0;
+      L.fuse_acc = true;
+      return launch_mixed(h, L);
+    }
     if (out) {
       // W lands in d1 (each point's d1 is read only by the thread that
       // overwrites it), then one stream forms u0 + W in FP64: the stage then
@@ -2785,15 +2795,14 @@ int dgsw_tune(DgswHandle h, int force_variant, int* family, int* n_variants, int
     for (int i = 0; i < nv && i < DGSW_TUNE_MAX_VARIANTS; ++i) ms[i] = h->bt_tune_ms[i];
   } else if (pipe_tunable(h)) {
     fam = DGSW_TUNE_MIXED_PIPE;
-    nv = 2;
+    nv = 4;
     if (force_variant >= nv || force_variant < -1)
       return fail(h, DGSW_ERR_ARGUMENT, "force_variant out of range");
     destroy_graphs(h);
     if (int rc = pipe_autotune(h, true)) return rc;
     if (force_variant >= 0) h->pipe_variant = force_variant;
     v = h->pipe_variant;
-    ms[0] = h->pipe_tune_ms[0];
-    ms[1] = h->pipe_tune_ms[1];
+    for (int i = 0; i < nv; ++i) ms[i] = h->pipe_tune_ms[i];
   } else if (tunable(h)) {
     fam = DGSW_TUNE_FP64_STAGE;
     nv = 2;

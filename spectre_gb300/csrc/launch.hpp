@@ -128,6 +128,9 @@ struct MixedLaunch {
   EoTable eo{};
   int* err = nullptr;  // device error word (bounded waits that timed out)
   int variant = 0;     // launch shape of the pipelined kernel (0 or 1)
+  // pipelined kernel, FP32 stage with y32, out64 and base64: out64 = base64
+  // + W formed in the kernel's epilogue (no w32)
+  bool fuse_acc = false;
 };
 
 cudaError_t launch_stage_mixed(const MixedLaunch& L, cudaStream_t s);

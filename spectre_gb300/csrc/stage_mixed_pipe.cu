@@ -127,9 +127,16 @@ __device__ __forceinline__ void eo_line_pdf(const float (&xh)[N], const float (&
 // while this one computes; 1: they are issued when this one is done, and the
 // other resident CTAs -- MINB asked of the register allocator -- cover the
 // wait).
-template <int N, int EPB, bool COMP, bool HAS_Y, bool HAS_B, int STAGES, int MINB>
+// ACC (FP32 stages with Y, no staged base): W is written in place into the
+// staged X (each line's values are read into registers before its outputs
+// land, and the pointwise reads of X and Y at a point precede its write),
+// then one coalesced pass over the element's contiguous block forms
+// out64 = base64 + W in FP64 with 16-byte loads and stores.
+template <int N, int EPB, bool COMP, bool HAS_Y, bool HAS_B, int STAGES, int MINB,
+          bool ACC = false>
 __global__ void __launch_bounds__(N * N * EPB, MINB)
     stage_mixed_pipe_kernel(MixedLaunch L, int64_t n_groups) {
+  static_assert(!ACC || (!COMP && HAS_Y && !HAS_B), "the fused accumulate is the last stage's");
   using S = P<N>;
   using Y = Lay<N, COMP, HAS_Y, HAS_B>;
   constexpr int NN = S::NN, NP = S::NP, h = S::h, TAB2 = S::TAB2;
@@ -251,6 +258,7 @@ __global__ void __launch_bounds__(N * N * EPB, MINB)
       return;
     }
     const unsigned char* buf = bufs[b];
+    float* Xw = reinterpret_cast<float*>(bufs[b]);  // W in place (ACC)
     if (COMP) {
       // each FP64 value of the staged X becomes its (hi, lo) FP32 pair in
       // place, so that the passes split each value once
@@ -361,6 +369,10 @@ __global__ void __launch_bounds__(N * N * EPB, MINB)
             w = fmaf(alpha, fh[i], w);
             if (HAS_Y) w = fmaf(beta, Yb[(2 + d) * NP + base + i * stride], w);
           }
+          if (ACC) {
+            Xw[(2 + d) * NP + base + i * stride] = w;
+            continue;
+          }
           if (L.w32) L.w32[vo + i * stride] = w;
           if (L.out64) {
             if (HAS_B)
@@ -391,6 +403,11 @@ __global__ void __launch_bounds__(N * N * EPB, MINB)
                 wpsi = fmaf(beta, Yb[p], wpsi);
               }
             }
+            if (ACC) {
+              Xw[NP + p] = wpi;
+              Xw[p] = wpsi;
+              continue;
+            }
             if (L.w32) {
               L.w32[e * VS + NP + p] = wpi;
               L.w32[e * VS + p] = wpsi;
@@ -409,6 +426,39 @@ __global__ void __launch_bounds__(N * N * EPB, MINB)
       }
       if (d < 2) __syncthreads();
     }
+    if (ACC) {
+      // out64 = base64 + W over the element's contiguous block: 4 values per
+      // thread and step, KB steps' loads issued before their stores (out64
+      // may alias base64; every value is read and written by one thread)
+      __syncthreads();
+      if (active) {
+        constexpr int Q4 = kVars * NP / 4, KB = N == 8 ? 5 : 3;
+        const float4* W4 = reinterpret_cast<const float4*>(bufs[b]);
+        const double2* B2 = reinterpret_cast<const double2*>(L.base64 + e * VS);
+        double2* O2 = reinterpret_cast<double2*>(L.out64 + e * VS);
+#pragma unroll 1
+        for (int q0 = t; q0 < Q4; q0 += KB * NN) {
+          double2 lo[KB], hi[KB];
+#pragma unroll
+          for (int k2 = 0; k2 < KB; ++k2) {
+            const int q = q0 + k2 * NN;
+            if (q < Q4) {
+              lo[k2] = B2[2 * q];
+              hi[k2] = B2[2 * q + 1];
+            }
+          }
+#pragma unroll
+          for (int k2 = 0; k2 < KB; ++k2) {
+            const int q = q0 + k2 * NN;
+            if (q < Q4) {
+              const float4 w = W4[q];
+              O2[2 * q] = make_double2(lo[k2].x + widen(w.x), lo[k2].y + widen(w.y));
+              O2[2 * q + 1] = make_double2(hi[k2].x + widen(w.z), hi[k2].y + widen(w.w));
+            }
+          }
+        }
+      }
+    }
     // neighbour faces of the next group, then release this buffer (the
     // in-place split wrote it: order those generic writes before the next
     // TMA writes into it)
@@ -416,7 +466,7 @@ __global__ void __launch_bounds__(N * N * EPB, MINB)
       if (gn < n_groups) issue_faces(gn * EPB + slot, b ^ 1);
       cp_async_commit();
     }
-    if (COMP) fence_proxy_async_smem();
+    if (COMP || ACC) fence_proxy_async_smem();
     __syncthreads();
     if (STAGES == 1 && gn < n_groups) {
       if (threadIdx.x == 0) issue_group(gn, 0);
@@ -444,7 +494,7 @@ constexpr int pipe_epb() {
 
 // Launch shapes: 0 two pipeline buffers, 1 one buffer and MINB = 4 resident
 // CTAs asked of the register allocator (the FP32 stages ask for 6).
-template <int N, bool COMP, bool HAS_Y, bool HAS_B, int V>
+template <int N, bool COMP, bool HAS_Y, bool HAS_B, int V, bool ACC = false>
 cudaError_t launch_pipe_v(const MixedLaunch& L, cudaStream_t s);
 
 template <int N, bool COMP, bool HAS_Y, bool HAS_B>
@@ -456,7 +506,7 @@ cudaError_t launch_pipe(const MixedLaunch& L, cudaStream_t s) {
   return launch_pipe_v<N, COMP, HAS_Y, HAS_B, 0>(L, s);
 }
 
-template <int N, bool COMP, bool HAS_Y, bool HAS_B, int V>
+template <int N, bool COMP, bool HAS_Y, bool HAS_B, int V, bool ACC>
 cudaError_t launch_pipe_v(const MixedLaunch& L, cudaStream_t s) {
   constexpr int EPB_FIT = pipe_epb<N, COMP, HAS_Y, HAS_B>();
   if (EPB_FIT < 1) return launch_stage_mixed(L, s);  // too large to double-buffer
@@ -465,7 +515,7 @@ cudaError_t launch_pipe_v(const MixedLaunch& L, cudaStream_t s) {
   constexpr int MINB = V == 1 ? (COMP ? 4 : 6) : 1;
   using Y = Lay<N, COMP, HAS_Y, HAS_B>;
   const size_t smem = (size_t)EPB * (STAGES == 2 ? Y::kSlot : Y::kSlot1);
-  auto k = stage_mixed_pipe_kernel<N, EPB, COMP, HAS_Y, HAS_B, STAGES, MINB>;
+  auto k = stage_mixed_pipe_kernel<N, EPB, COMP, HAS_Y, HAS_B, STAGES, MINB, ACC>;
   cudaError_t err = cudaFuncSetAttribute(k, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
   if (err != cudaSuccess) return err;
   err = cudaFuncSetAttribute(k, cudaFuncAttributePreferredSharedMemoryCarveout,
@@ -490,6 +540,12 @@ cudaError_t launch_pipe_v(const MixedLaunch& L, cudaStream_t s) {
 template <int N>
 cudaError_t launch_pipe_n(const MixedLaunch& L, cudaStream_t s) {
   const bool y = L.y32 != nullptr, bb = L.base64 != nullptr && L.out64 != nullptr;
+  if (L.fuse_acc) {
+    // the last stage with u0 + W formed in its epilogue
+    if (L.x64 || !y || !bb || L.w32) return cudaErrorInvalidValue;
+    return L.variant == 1 ? launch_pipe_v<N, false, true, false, 1, true>(L, s)
+                          : launch_pipe_v<N, false, true, false, 0, true>(L, s);
+  }
   if (L.x64) {
     if (y) return cudaErrorInvalidValue;
     return bb ? launch_pipe<N, true, false, true>(L, s) : launch_pipe<N, true, false, false>(L, s);

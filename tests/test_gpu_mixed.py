@@ -173,8 +173,9 @@ def test_mixed_gamma2_differing_extents_matches_oracle(oracle):
 
 @pytest.mark.parametrize("n", [6, 8])
 def test_mixed_pipe_launch_shapes_agree(oracle, n):
-    # the pipelined kernel's two launch shapes (dgsw_tune): same bits, and
-    # both within the mixed bar of the FP64 oracle
+    # the pipelined kernel's four candidates (dgsw_tune: one or two pipeline
+    # buffers, the FP64 update as a separate stream or in the last stage's
+    # epilogue): same bits, and all within the mixed bar of the FP64 oracle
     bricks = [Brick((4, 4, 3))]
     dt, steps = 1e-3, 30
     u0 = oracle.initial_data(bricks, n, "plane_wave", [1, 1, 1])
@@ -185,6 +186,7 @@ def test_mixed_pipe_launch_shapes_agree(oracle, n):
         info = ev.tune()
         assert info["family"] == "mixed_pipe"
         assert np.array_equal(ev.get_state(), u0)
+        assert len(info["ms_per_step"]) == 4
         assert all(ms > 0 for ms in info["ms_per_step"])
         for v in range(len(info["ms_per_step"])):
             assert ev.tune(force_variant=v)["variant"] == v
@@ -193,4 +195,5 @@ def test_mixed_pipe_launch_shapes_agree(oracle, n):
             out.append(ev.get_state())
     for got in out:
         assert rel_l2(got, ref) <= 1e-6
-    np.testing.assert_array_equal(out[0], out[1])
+    for got in out[1:]:
+        np.testing.assert_array_equal(out[0], got)

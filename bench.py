@@ -582,6 +582,9 @@ def time_curved(args, dev, with_cpu):
         res[name] = {"value": ev.grid_points * 3 * steps / (ms * 1e-3), "unit": UNIT,
                      "ms_per_step": ms / steps}
         points = ev.grid_points
+        if name == "mixed":
+            # the launch shape the tuner chose, re-timed after the timed region
+            res["mixed"]["tune"] = ev.tune()
         if name == "fp64":
             # FP64 against the oracle over the first steps
             k = 3

@@ -371,8 +371,11 @@ int dgsw_autotune(DgswHandle h, int force_variant, int* variant, double* ms_per_
  * largest extent), DGSW_TUNE_MIXED_PIPE (mixed precision on one even extent:
  * four candidates, the pipelined kernel with two pipeline buffers or one
  * buffer and more resident CTAs (bit 0), each with the step's FP64 update
- * u0 + W as a separate stream or in the last stage's epilogue (bit 1)), or
- * DGSW_TUNE_NONE (fixed configurations).  Re-times every
+ * u0 + W as a separate stream or in the last stage's epilogue (bit 1)),
+ * DGSW_TUNE_MIXED_CURVED (mixed precision on the curved shell: the stage
+ * kernel at 256 threads per block with its default or one more resident
+ * block per SM, or at 512 threads), or DGSW_TUNE_NONE (fixed
+ * configurations).  Re-times every
  * candidate now on the handle's own state (saved and restored), keeps the
  * fastest (force_variant >= 0 imposes one instead) and returns the number of
  * candidates, the choice and ms per step of each (ms_per_step holds
@@ -384,7 +387,8 @@ enum {
   DGSW_TUNE_NONE = 0,
   DGSW_TUNE_FP64_STAGE = 1,
   DGSW_TUNE_MIXED_BATCH = 2,
-  DGSW_TUNE_MIXED_PIPE = 3
+  DGSW_TUNE_MIXED_PIPE = 3,
+  DGSW_TUNE_MIXED_CURVED = 4
 };
 #define DGSW_TUNE_MAX_VARIANTS 8
 int dgsw_tune(DgswHandle h, int force_variant, int* family, int* n_variants, int* variant,

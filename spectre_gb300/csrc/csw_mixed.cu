@@ -1,379 +1,20 @@
-// csw_mixed.cu -- mixed-precision CurvedScalarWave stage on the shell.
-//
-// The curved operator L (TimeDerivative + UpwindPenalty + lift + the
-// radiation condition on the outer sphere) is linear in (Psi, Pi, Phi) on a
-// static background and mesh, so SSP-RK3 (Rk3HesthavenSsp.cpp:63-80) takes
-// the incremental form
-//   d1 = dt L(u0),  s2 = d1/2 + dt/4 L(d1),  u3 = u0 + 2/3 (s2 + d1) + 2dt/3 L(s2)
-// and only the first stage differentiates the full FP64 state.  One kernel
-// serves every stage:  W = alpha X + beta Y + c L(X), with
-//  - X FP64 (first stage): split exactly into hi + lo FP32 parts; the
-//    logical derivatives are compensated double-float dot products with the
-//    hi + lo split of D, and the jumps across faces are formed from the
-//    hi + lo parts, so no cancellation loses more than FP32 rounding of the
-//    result;
-//  - X FP32 (increments): plain FP32.
-// The background/geometry coefficients are the FP64 set-up tables rounded to
-// FP32 (formed once from the FP64 inverse Jacobian and FP64 background); the
-// FP64 state is touched only by the first stage's read and the last stage's
-// u0 + W.  Outputs: w32 = W, and/or out64 = base64 + W (out64 = W without a
-// base).  The work split is the FP64 kernel's (csw_fp64.cu): one element
-// per block, one round per logical axis.
-#include "common.cuh"
-#include "dg_device.cuh"
-#include "launch.hpp"
+// csw_mixed.cu -- launch shape 0 of the mixed-precision CurvedScalarWave
+// stage (csw_mixed.cuh) and the entry point that picks the shape.
+#include "csw_mixed.cuh"
 
 namespace dgsw {
-namespace {
+namespace csw_mixed {
+cudaError_t launch_shape0(const CswMixedLaunch& L, cudaStream_t s) { return launch_shape<0>(L, s); }
+}  // namespace csw_mixed
 
-constexpr int kThreads = 256;
-
-template <int N, bool COMP>
-struct CmShape {
-  static constexpr int NN = N * N;
-  static constexpr int NP = N * N * N;
-  static constexpr int TAB = 2 * dev::Eo<N>::H * dev::Eo<N>::h + dev::Eo<N>::H;
-  static constexpr int PTS = (NP + kThreads - 1) / kThreads;
-  // floats: hi state, lo state (COMP), one axis of derivatives, outer-layer
-  // derivatives, hi and lo tables
-  static constexpr int SMEM = 5 * NP + (COMP ? 5 * NP : 0) + 5 * NP + 12 * NN + 2 * TAB;
-};
-
-template <int N>
-__device__ __forceinline__ void line_geometry(int a, int line, int& base, int& stride) {
-  const int ta = line % N, tb = line / N;
-  if (a == 0) {
-    base = N * ta + N * N * tb;
-    stride = 1;
-  } else if (a == 1) {
-    base = ta + N * N * tb;
-    stride = N;
-  } else {
-    base = ta + N * tb;
-    stride = N * N;
-  }
-}
-
-// Resident blocks per SM asked of the register allocator: three for the
-// plain FP32 stages, whose split tables are read from shared memory where
-// used (fewer registers); two for the compensated stage.  Extents 11 and 12
-// ask one fewer: with three (two) their lines spill 150-230 (110-160) bytes
-// (ptxas), at two (one) nothing.
-template <int N, bool COMP>
-constexpr int csw_mixed_min_blocks() {
-  return (COMP ? 2 : 3) - (N >= 11 ? 1 : 0);
-}
-
-template <int N, bool COMP>
-__global__ void __launch_bounds__(kThreads, csw_mixed_min_blocks<N, COMP>())
-    csw_stage_mixed_kernel(CswMixedLaunch L) {
-  using S = CmShape<N, COMP>;
-  constexpr int NN = S::NN, NP = S::NP, PTS = S::PTS, TAB = S::TAB;
-  extern __shared__ float fsm[];
-  float* Uh = fsm;
-  float* Ul = Uh + 5 * NP;  // COMP only
-  float* Ga = Ul + (COMP ? 5 * NP : 0);
-  float* Go = Ga + 5 * NP;
-  float* th = Go + 12 * NN;
-  float* tl = th + TAB;
-  const int64_t e = blockIdx.x;
-  const int tid = threadIdx.x;
-  const int64_t off = e * (int64_t)(kVars * NP);
-  const bool outer = L.nbr[6 * e + 5] == -2;
-  // state of the element: vector loads when every element block starts on a
-  // 16-byte boundary (even N and an aligned base pointer), else scalar loads
-  if (COMP) {
-    if (NP % 2 == 0 && (reinterpret_cast<uintptr_t>(L.x64) & 15u) == 0) {
-      const double2* src = reinterpret_cast<const double2*>(L.x64 + off);
-      constexpr int Q = 5 * NP / 2;
-#pragma unroll 4
-      for (int q = tid; q < Q; q += kThreads) {
-        const double2 v = __ldg(src + q);
-        float h0, l0, h1, l1;
-        dev::split_df(v.x, h0, l0);
-        dev::split_df(v.y, h1, l1);
-        Uh[2 * q] = h0;
-        Ul[2 * q] = l0;
-        Uh[2 * q + 1] = h1;
-        Ul[2 * q + 1] = l1;
-      }
-    } else {
-      for (int q = tid; q < 5 * NP; q += kThreads) {
-        float hi, lo;
-        dev::split_df(L.x64[off + q], hi, lo);
-        Uh[q] = hi;
-        Ul[q] = lo;
-      }
-    }
-  } else {
-    if (NP % 4 == 0 && (reinterpret_cast<uintptr_t>(L.x32) & 15u) == 0) {
-      const float4* src = reinterpret_cast<const float4*>(L.x32 + off);
-      float4* dst = reinterpret_cast<float4*>(Uh);
-      constexpr int Q = 5 * NP / 4;
-#pragma unroll 4
-      for (int q = tid; q < Q; q += kThreads) dst[q] = __ldg(src + q);
-    } else {
-      for (int q = tid; q < 5 * NP; q += kThreads) Uh[q] = L.x32[off + q];
-    }
-  }
-  for (int q = tid; q < TAB; q += kThreads) {
-    constexpr int h = dev::Eo<N>::h, H = dev::Eo<N>::H;
-    double v;
-    if (q < H * h)
-      v = L.eo.A[q / h][q % h];
-    else if (q < 2 * H * h)
-      v = L.eo.B[(q - H * h) / h][(q - H * h) % h];
-    else
-      v = L.eo.M[q - 2 * H * h];
-    const float hv = (float)v;
-    th[q] = hv;
-    tl[q] = (float)(v - (double)hv);
-  }
-  const float* T = L.T + e * (int64_t)kCswT * NP;
-  const float g1 = L.gamma1, g2 = L.gamma2;
-
-  float acc[PTS][5];
-#pragma unroll
-  for (int r = 0; r < PTS; ++r)
-#pragma unroll
-    for (int v = 0; v < 5; ++v) acc[r][v] = 0.0f;
-
-#pragma unroll 1
-  for (int a = 0; a < 3; ++a) {
-    // this round's coefficients (B^a, G^a., A_a.) for the owned points are
-    // loaded before the derivative work, which then hides their latency
-    float cf[PTS][7];
-#pragma unroll
-    for (int r = 0; r < PTS; ++r) {
-      const int p = tid + r * kThreads;
-      if (p < NP) {
-        cf[r][0] = __ldg(T + (kTB + a) * NP + p);
-#pragma unroll
-        for (int j = 0; j < 3; ++j) {
-          cf[r][1 + j] = __ldg(T + (kTG + 3 * a + j) * NP + p);
-          cf[r][4 + j] = __ldg(T + (kTA + 3 * a + j) * NP + p);
-        }
-      }
-    }
-    __syncthreads();
-    for (int task = tid; task < 5 * NN; task += kThreads) {
-      const int v = task / NN, line = task - v * NN;
-      int base, stride;
-      line_geometry<N>(a, line, base, stride);
-      float uh[N], du[N];
-#pragma unroll
-      for (int i = 0; i < N; ++i) uh[i] = Uh[v * NP + base + i * stride];
-      if (COMP) {
-        float ul[N];
-#pragma unroll
-        for (int i = 0; i < N; ++i) ul[i] = Ul[v * NP + base + i * stride];
-        dev::eo_line_df<N>(uh, ul, du, th, tl);
-      } else {
-        dev::eo_line<N, float, true>(uh, du, th);
-      }
-#pragma unroll
-      for (int i = 0; i < N; ++i) Ga[v * NP + base + i * stride] = du[i];
-    }
-    __syncthreads();
-#pragma unroll
-    for (int r = 0; r < PTS; ++r) {
-      const int p = tid + r * kThreads;
-      if (p < NP) {
-        const float gpsi = Ga[p], gpi = Ga[NP + p];
-        const float gf[3] = {Ga[2 * NP + p], Ga[3 * NP + p], Ga[4 * NP + p]};
-        const float B = cf[r][0];
-        acc[r][0] = fmaf(B, gpsi, acc[r][0]);
-        float s = B * fmaf(g1 * g2, gpsi, gpi);
-#pragma unroll
-        for (int j = 0; j < 3; ++j) s = fmaf(-cf[r][1 + j], gf[j], s);
-        acc[r][1] += s;
-        const float hh = fmaf(g2, gpsi, -gpi);
-#pragma unroll
-        for (int i = 0; i < 3; ++i)
-          acc[r][2 + i] = fmaf(cf[r][4 + i], hh, fmaf(B, gf[i], acc[r][2 + i]));
-        if (outer && p >= NP - NN) {
-          const int q = p - (NP - NN);
-          Go[(4 * a + 0) * NN + q] = gpsi;
-#pragma unroll
-          for (int j = 0; j < 3; ++j) Go[(4 * a + 1 + j) * NN + q] = gf[j];
-        }
-      }
-    }
-  }
-  __syncthreads();
-
-#pragma unroll
-  for (int r = 0; r < PTS; ++r) {
-    const int p = tid + r * kThreads;
-    if (p >= NP) continue;
-    float ui[5];
-#pragma unroll
-    for (int v = 0; v < 5; ++v) ui[v] = COMP ? Uh[v * NP + p] + Ul[v * NP + p] : Uh[v * NP + p];
-    const float psi = ui[0], pi = ui[1];
-    const float phi[3] = {ui[2], ui[3], ui[4]};
-    const float lapse = T[kTLapse * NP + p];
-    float dt[5];
-    float bphi = 0.0f;
-    if (g1 != 0.0f)
-      for (int i = 0; i < 3; ++i) bphi = fmaf(T[(kTBeta + i) * NP + p], phi[i], bphi);
-    dt[0] = fmaf(-g1, bphi, fmaf(1.0f + g1, acc[r][0], -lapse * pi));
-    float s = fmaf(T[kTK * NP + p], pi, acc[r][1]);
-    for (int i = 0; i < 3; ++i) s = fmaf(T[(kTC + i) * NP + p], phi[i], s);
-    dt[1] = fmaf(-g1 * g2, bphi, s);
-    for (int i = 0; i < 3; ++i) {
-      float v = fmaf(-g2 * lapse, phi[i], acc[r][2 + i]);
-      v = fmaf(-pi, T[(kTDl + i) * NP + p], v);
-      for (int j = 0; j < 3; ++j) v = fmaf(T[(kTDs + 3 * i + j) * NP + p], phi[j], v);
-      dt[2 + i] = v;
-    }
-    const int i = p % N, j = (p / N) % N, k = p / NN;
-    float corr[5] = {0.0f, 0.0f, 0.0f, 0.0f, 0.0f};
-    const int dirs[6] = {i == 0 ? 0 : -1, i == N - 1 ? 1 : -1, j == 0 ? 2 : -1,
-                         j == N - 1 ? 3 : -1, k == 0 ? 4 : -1, k == N - 1 ? 5 : -1};
-    const int fq[3] = {j + N * k, i + N * k, i + N * j};
-#pragma unroll
-    for (int s6 = 0; s6 < 6; ++s6) {
-      const int dir = dirs[s6];
-      if (dir < 0) continue;
-      const int q = fq[dir >> 1];
-      const int64_t ef = e * 6 + dir;
-      const int32_t x = L.X[ef * NN + q];
-      const float* f = L.F + ef * kCswF * NN + q;
-      if (x >= 0) {
-        // jumps d = exterior - interior
-        float dv[5];
-#pragma unroll
-        for (int v = 0; v < 5; ++v) {
-          if (COMP) {
-            float eh, el;
-            dev::split_df(L.x64[x + (int64_t)v * NP], eh, el);
-            dv[v] = (eh - Uh[v * NP + p]) + (el - Ul[v * NP + p]);
-          } else {
-            dv[v] = L.x32[x + (int64_t)v * NP] - Uh[v * NP + p];
-          }
-        }
-        float ndp = 0.0f;
-#pragma unroll
-        for (int c = 0; c < 3; ++c) ndp = fmaf(f[(kFv + c) * NN], dv[2 + c], ndp);
-        const float m0 = f[(kFm + 0) * NN], m1 = f[(kFm + 1) * NN];
-        const float m2 = f[(kFm + 2) * NN], m3 = f[(kFm + 3) * NN];
-        const float g2p = g2 * dv[0];
-        const float t1 = m3 * (dv[1] - ndp - g2p);
-        const float t2 = -m2 * (dv[1] + ndp - g2p);
-        const float cpsi = m0 * dv[0];
-        corr[0] += cpsi;
-        corr[1] += fmaf(g2, cpsi, 0.5f * (t1 - t2));
-        const float hh = -0.5f * (t1 + t2);
-#pragma unroll
-        for (int c = 0; c < 3; ++c) {
-          const float nc = f[(kFn + c) * NN];
-          corr[2 + c] += fmaf(hh, nc, m1 * fmaf(-nc, ndp, dv[2 + c]));
-        }
-      } else if (x == -2) {
-        // ConstraintPreservingSphericalRadiation from the volume dt
-        const double* J = L.ij + e * 9 * (int64_t)NP + p;
-        float dpsi[3], dphi[3][3];
-#pragma unroll
-        for (int ii = 0; ii < 3; ++ii) {
-          float s0 = 0.0f, s1 = 0.0f, s2 = 0.0f, s3 = 0.0f;
-#pragma unroll
-          for (int a = 0; a < 3; ++a) {
-            const float Jai = (float)J[(3 * a + ii) * NP];
-            s0 = fmaf(Jai, Go[(4 * a + 0) * NN + q], s0);
-            s1 = fmaf(Jai, Go[(4 * a + 1) * NN + q], s1);
-            s2 = fmaf(Jai, Go[(4 * a + 2) * NN + q], s2);
-            s3 = fmaf(Jai, Go[(4 * a + 3) * NN + q], s3);
-          }
-          dpsi[ii] = s0;
-          dphi[ii][0] = s1;
-          dphi[ii][1] = s2;
-          dphi[ii][2] = s3;
-        }
-        const double* X3 = L.xyz + e * 3 * (int64_t)NP + p;
-        const float rr = (float)sqrt(X3[0] * X3[0] + X3[NP] * X3[NP] + X3[2 * NP] * X3[2 * NP]);
-        const float ir = 1.0f / rr;
-        float nv[3], nc[3], beta[3], bn = 0.0f;
-#pragma unroll
-        for (int c = 0; c < 3; ++c) {
-          nv[c] = f[(kFv + c) * NN];
-          nc[c] = f[(kFn + c) * NN];
-          beta[c] = T[(kTBeta + c) * NP + p];
-          bn = fmaf(beta[c], nc[c], bn);
-        }
-        const float l0 = fminf(-(1.0f + g1) * bn, 0.0f), l1 = fminf(-bn, 0.0f);
-        float cpsi = 0.0f;
-#pragma unroll
-        for (int c = 0; c < 3; ++c) cpsi = fmaf(nv[c], dpsi[c] - phi[c], cpsi);
-        cpsi *= l0;
-        corr[0] += cpsi;
-#pragma unroll
-        for (int c = 0; c < 3; ++c) {
-          float v = 0.0f;
-#pragma unroll
-          for (int jj = 0; jj < 3; ++jj) v = fmaf(nv[jj], dphi[jj][c] - dphi[c][jj], v);
-          corr[2 + c] += l1 * v;
-        }
-        float cpi = fmaf(2.0f * ir, psi, 4.0f * dt[0]) * ir;
-#pragma unroll
-        for (int c = 0; c < 3; ++c) {
-          cpi = fmaf(nv[c], fmaf(2.0f, dt[2 + c], 4.0f * ir * phi[c]), cpi);
-          cpi = fmaf(beta[c], dt[2 + c], cpi);
-#pragma unroll
-          for (int jj = 0; jj < 3; ++jj) cpi = fmaf(nv[c] * nv[jj], dphi[c][jj], cpi);
-        }
-        cpi /= lapse;
-        corr[1] += fmaf(g2, cpsi, cpi - dt[1]);
-      }
-    }
-    const float al = (float)L.alpha, be = (float)L.beta, cc = (float)L.c;
-#pragma unroll
-    for (int v = 0; v < 5; ++v) {
-      const int64_t o = off + v * NP + p;
-      float w = cc * (dt[v] + corr[v]);
-      if (L.alpha != 0.0) w = fmaf(al, ui[v], w);
-      if (L.y32) w = fmaf(be, L.y32[o], w);
-      if (L.w32) L.w32[o] = w;
-      if (L.out64) L.out64[o] = L.base64 ? L.base64[o] + dev::widen(w) : dev::widen(w);
-    }
-  }
-}
-
-template <int N, bool COMP>
-cudaError_t launch_mixed_n(const CswMixedLaunch& L, cudaStream_t s) {
-  const size_t smem = (size_t)CmShape<N, COMP>::SMEM * sizeof(float);
-  auto k = csw_stage_mixed_kernel<N, COMP>;
-  cudaError_t err =
-      cudaFuncSetAttribute(k, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
-  if (err != cudaSuccess) return err;
-  err = cudaFuncSetAttribute(k, cudaFuncAttributePreferredSharedMemoryCarveout,
-                             cudaSharedmemCarveoutMaxShared);
-  if (err != cudaSuccess) return err;
-  if (L.n_elem <= 0) return cudaSuccess;
-  k<<<(unsigned)L.n_elem, kThreads, smem, s>>>(L);
-  return cudaGetLastError();
-}
-
-template <int N>
-cudaError_t launch_mixed_mode(const CswMixedLaunch& L, cudaStream_t s) {
-  return L.x64 ? launch_mixed_n<N, true>(L, s) : launch_mixed_n<N, false>(L, s);
-}
-
-}  // namespace
+int csw_mixed_shapes() { return csw_mixed::kShapes; }
 
 cudaError_t launch_csw_mixed(const CswMixedLaunch& L, cudaStream_t s) {
   if ((L.x64 == nullptr) == (L.x32 == nullptr)) return cudaErrorInvalidValue;
-  switch (L.n) {
-    case 2: return launch_mixed_mode<2>(L, s);
-    case 3: return launch_mixed_mode<3>(L, s);
-    case 4: return launch_mixed_mode<4>(L, s);
-    case 5: return launch_mixed_mode<5>(L, s);
-    case 6: return launch_mixed_mode<6>(L, s);
-    case 7: return launch_mixed_mode<7>(L, s);
-    case 8: return launch_mixed_mode<8>(L, s);
-    case 9: return launch_mixed_mode<9>(L, s);
-    case 10: return launch_mixed_mode<10>(L, s);
-    case 11: return launch_mixed_mode<11>(L, s);
-    case 12: return launch_mixed_mode<12>(L, s);
+  switch (L.variant) {
+    case 0: return csw_mixed::launch_shape0(L, s);
+    case 1: return csw_mixed::launch_shape1(L, s);
+    case 2: return csw_mixed::launch_shape2(L, s);
     default: return cudaErrorInvalidValue;
   }
 }

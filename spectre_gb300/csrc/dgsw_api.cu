@@ -99,6 +99,9 @@ struct DgswHandle_ {
   int pipe_variant = 0;
   bool pipe_tuned = false;
   double pipe_tune_ms[4] = {0.0, 0.0, 0.0, 0.0};
+  int csw_variant = 0;  // launch shape of the mixed curved stage kernel
+  bool csw_tuned = false;
+  double csw_tune_ms[DGSW_TUNE_MAX_VARIANTS] = {};
   int bt_fu_age = 0;  // steps since the state's face values were formed from it
   // misfit objective and discrete adjoint (uniform FP64 path)
   EoTable eoT{};
@@ -184,7 +187,6 @@ struct DgswHandle_ {
   double filter_alpha = 0.0;
   int filter_half_power = 0;
   double* filt = nullptr;  // [kMaxN + 1][kMaxN * kMaxN], matrix of extent n at n
-  float* filt32 = nullptr;  // the same in FP32 hi parts, then lo parts (mixed precision)
   float* fr32 = nullptr;    // mixed precision with the filter: R = (F - I) u0
   float* fw3 = nullptr;     //   and the third stage's dt L(D2)
   // graphs of whole steps
@@ -555,6 +557,7 @@ CswMixedLaunch base_csw_mixed(DgswHandle h) {
   L.gamma1 = (float)h->shell.gamma1;
   L.gamma2 = (float)h->cfg.gamma2;
   L.eo = h->eo;
+  L.variant = h->csw_variant;
   return L;
 }
 
@@ -688,7 +691,7 @@ cudaError_t mixed_apply_L(DgswHandle h, const double* x64, const float* x32, dou
 // A filter launch (residual or combine) over every element of the handle.
 template <typename Launch>
 cudaError_t mixed_filter_all(DgswHandle h, MixedFilterLaunch F, Launch launch) {
-  const size_t stride = (size_t)kMaxN * kMaxN, half = (size_t)(kMaxN + 1) * stride;
+  const size_t stride = (size_t)kMaxN * kMaxN;
   if (h->general) {
     F.offset = h->offset;
     for (int n = kMinN; n <= kMaxN; ++n) {
@@ -696,8 +699,7 @@ cudaError_t mixed_filter_all(DgswHandle h, MixedFilterLaunch F, Launch launch) {
       F.n = n;
       F.tasks = h->class_tasks[n];
       F.n_tasks = h->class_count[n];
-      F.Fh = h->filt32 + (size_t)n * stride;
-      F.Fl = h->filt32 + half + (size_t)n * stride;
+      F.F = h->filt + (size_t)n * stride;
       cudaError_t e = launch(F, h->stream);
       if (e != cudaSuccess) return e;
     }
@@ -705,8 +707,7 @@ cudaError_t mixed_filter_all(DgswHandle h, MixedFilterLaunch F, Launch launch) {
   }
   F.n = h->dom.elem_n[0];
   F.n_tasks = h->dom.n_elem;
-  F.Fh = h->filt32 + (size_t)F.n * stride;
-  F.Fl = h->filt32 + half + (size_t)F.n * stride;
+  F.F = h->filt + (size_t)F.n * stride;
   return launch(F, h->stream);
 }
 
@@ -917,6 +918,45 @@ bool pipe_tunable(DgswHandle h) {
 }
 
 std::map<std::pair<int, int64_t>, int> g_pipe_tuned;
+
+// The mixed curved path: the stage kernel's launch shapes (threads per
+// block, resident blocks asked of the register allocator) timed the same
+// way, cached per (extent, elements).
+bool csw_tunable(DgswHandle h) { return mixed(h) && h->curved && !h->adams; }
+
+std::map<std::pair<int, int64_t>, int> g_csw_tuned;
+
+int csw_autotune(DgswHandle h, bool force) {
+  if (!csw_tunable(h) || (h->csw_tuned && !force)) return DGSW_OK;
+  const std::pair<int, int64_t> key(h->dom.elem_n[0], h->dom.n_elem);
+  if (!force) {
+    std::lock_guard<std::mutex> lk(g_tune_mu);
+    auto it = g_csw_tuned.find(key);
+    if (it != g_csw_tuned.end()) {
+      h->csw_variant = it->second;
+      h->csw_tuned = true;
+      return DGSW_OK;
+    }
+  }
+  const int keep = h->csw_variant;
+  int best = -1;
+  cudaError_t err = time_step_shapes(
+      h, csw_mixed_shapes(),
+      [&](int v) {
+        h->csw_variant = v;
+        return true;
+      },
+      h->csw_tune_ms, &best);
+  if (err != cudaSuccess) {
+    h->csw_variant = keep;
+    return cuda_fail(h, err, "curved launch autotune");
+  }
+  h->csw_variant = best >= 0 ? best : keep;
+  h->csw_tuned = true;
+  std::lock_guard<std::mutex> lk(g_tune_mu);
+  g_csw_tuned[key] = h->csw_variant;
+  return DGSW_OK;
+}
 
 int pipe_autotune(DgswHandle h, bool force) {
   if (!pipe_tunable(h) || (h->pipe_tuned && !force)) return DGSW_OK;
@@ -2331,7 +2371,6 @@ int dgsw_destroy(DgswHandle h) {
   if (h->c_F32) cudaFree(h->c_F32);
   if (h->c_X) cudaFree(h->c_X);
   if (h->filt) cudaFree(h->filt);
-  if (h->filt32) cudaFree(h->filt32);
   if (h->fr32) cudaFree(h->fr32);
   if (h->fw3) cudaFree(h->fw3);
   if (h->lgl_w) cudaFree(h->lgl_w);
@@ -2793,6 +2832,16 @@ int dgsw_tune(DgswHandle h, int force_variant, int* family, int* n_variants, int
     if (force_variant >= 0) h->bt_variant = force_variant;
     v = h->bt_variant;
     for (int i = 0; i < nv && i < DGSW_TUNE_MAX_VARIANTS; ++i) ms[i] = h->bt_tune_ms[i];
+  } else if (csw_tunable(h)) {
+    fam = DGSW_TUNE_MIXED_CURVED;
+    nv = csw_mixed_shapes();
+    if (force_variant >= nv || force_variant < -1)
+      return fail(h, DGSW_ERR_ARGUMENT, "force_variant out of range");
+    destroy_graphs(h);
+    if (int rc = csw_autotune(h, true)) return rc;
+    if (force_variant >= 0) h->csw_variant = force_variant;
+    v = h->csw_variant;
+    for (int i = 0; i < nv; ++i) ms[i] = h->csw_tune_ms[i];
   } else if (pipe_tunable(h)) {
     fam = DGSW_TUNE_MIXED_PIPE;
     nv = 4;
@@ -2854,15 +2903,8 @@ int dgsw_set_exponential_filter(DgswHandle h, double alpha, int half_power, int 
   DGSW_CUDA(h, cudaMemcpy(h->filt, mats.data(), mats.size() * sizeof(double),
                           cudaMemcpyHostToDevice));
   if (mixed(h)) {
-    // FP32 hi and lo parts of the matrices, the residual and third-stage buffers
-    std::vector<float> m32(2 * mats.size(), 0.0f);
-    for (size_t i = 0; i < mats.size(); ++i) {
-      m32[i] = (float)mats[i];
-      m32[mats.size() + i] = (float)(mats[i] - (double)m32[i]);
-    }
-    if (!h->filt32) DGSW_CUDA(h, cudaMalloc(&h->filt32, m32.size() * sizeof(float)));
-    DGSW_CUDA(h, cudaMemcpy(h->filt32, m32.data(), m32.size() * sizeof(float),
-                            cudaMemcpyHostToDevice));
+    // the residual and third-stage buffers (the kernels split the FP64
+    // matrices themselves)
     const size_t b32 = (size_t)h->dom.offset.back() * sizeof(float) + 64;
     if (!h->fr32) DGSW_CUDA(h, cudaMalloc(&h->fr32, b32));
     if (!h->fw3) DGSW_CUDA(h, cudaMalloc(&h->fw3, b32));
@@ -3001,6 +3043,10 @@ static int step_impl(DgswHandle h, int n_steps, double dt) {
   if (pipe_tunable(h) && !h->pipe_tuned) {
     destroy_graphs(h);
     if (int rc = pipe_autotune(h, false)) return rc;
+  }
+  if (csw_tunable(h) && !h->csw_tuned) {
+    destroy_graphs(h);
+    if (int rc = csw_autotune(h, false)) return rc;
   }
   if (!(h->graph_dt == dt)) {
     destroy_graphs(h);

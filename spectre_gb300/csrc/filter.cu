@@ -4,75 +4,60 @@
 // with the 1D filter matrix F (Spectral/Filtering.cpp:18-31) along each of
 // the three logical axes, in place, FP64.
 //
-// One block per element: the five variables are staged in shared memory,
-// then three passes (one per axis) apply F to every line, ping-ponging
-// between two shared buffers, and the result is written back.  The filter is
-// an element-local N^3 x N^3 tensor-product operator: it reads and writes the
-// state once (80 B per point) and costs 3 N FP64 FMAs per value.
+// One block per (element, variable), one thread per line: the variable's
+// N^3 block is staged in shared memory, then three passes (one per axis)
+// each read every thread's line into registers, synchronise, and write F
+// times the line back in place; the result is written back to the state.
+// F's mirror symmetry halves the multiply-adds (filter_line.cuh): the filter
+// reads and writes the state once (80 B per point) and costs about 3 N / 2
+// FP64 FMAs per value, which bind it on GB300.
 #include "common.cuh"
+#include "filter_line.cuh"
 #include "launch.hpp"
 
 namespace dgsw {
 namespace {
 
-constexpr int kThreads = 256;
-
 template <int N>
-__global__ void __launch_bounds__(kThreads) filter_kernel(FilterLaunch L) {
-  constexpr int NN = N * N, NP = N * N * N;
-  extern __shared__ double fbuf[];
-  double* A = fbuf;
-  double* B = fbuf + 5 * NP;
-  double* F = B + 5 * NP;
-  const int64_t e = L.tasks ? (int64_t)L.tasks[blockIdx.x] : (int64_t)blockIdx.x;
-  const int64_t off = L.offset ? L.offset[e] : e * (int64_t)(kVars * NP);
+__global__ void __launch_bounds__(filt::line_threads<N>()) filter_kernel(FilterLaunch L) {
+  constexpr int NN = N * N, NP = N * N * N, TS = filt::SymTab<N>::SIZE;
+  constexpr int T = filt::line_threads<N>();
+  __shared__ double S[NP];
+  __shared__ double tab[TS];
+  const int64_t slot = blockIdx.x / kVars;
+  const int v = (int)(blockIdx.x - slot * kVars);
+  const int64_t e = L.tasks ? (int64_t)L.tasks[slot] : slot;
+  const int64_t off = (L.offset ? L.offset[e] : e * (int64_t)(kVars * NP)) + (int64_t)v * NP;
   double* u = L.u + off;
-  for (int q = threadIdx.x; q < 5 * NP; q += kThreads) A[q] = u[q];
-  for (int q = threadIdx.x; q < NN; q += kThreads) F[q] = L.F[q];
+  const int tid = threadIdx.x;
+  for (int q = tid; q < NP; q += T) S[q] = u[q];
+  for (int q = tid; q < TS; q += T) tab[q] = filt::sym_entry<N>(L.F, q);
   __syncthreads();
+  const bool has = tid < NN;
 #pragma unroll 1
   for (int a = 0; a < 3; ++a) {
-    const double* src = (a == 1) ? B : A;
-    double* dst = (a == 1) ? A : B;
-    for (int task = threadIdx.x; task < 5 * NN; task += kThreads) {
-      const int v = task / NN, line = task - v * NN;
-      const int ta = line % N, tb = line / N;
-      int base, stride;
-      if (a == 0) {
-        base = N * ta + NN * tb;
-        stride = 1;
-      } else if (a == 1) {
-        base = ta + NN * tb;
-        stride = N;
-      } else {
-        base = ta + N * tb;
-        stride = NN;
-      }
-      double x[N];
+    int base = 0, stride = 0;
+    double x[N], y[N];
+    if (has) {
+      filt::axis_line<N>(a, tid, base, stride);
 #pragma unroll
-      for (int i = 0; i < N; ++i) x[i] = src[v * NP + base + i * stride];
+      for (int i = 0; i < N; ++i) x[i] = S[base + i * stride];
+    }
+    __syncthreads();  // every line read before any is overwritten
+    if (has) {
+      filt::sym_line<N, double>(x, y, tab);
 #pragma unroll
-      for (int i = 0; i < N; ++i) {
-        double s = F[i * N] * x[0];
-#pragma unroll
-        for (int j = 1; j < N; ++j) s = fma(F[i * N + j], x[j], s);
-        dst[v * NP + base + i * stride] = s;
-      }
+      for (int i = 0; i < N; ++i) S[base + i * stride] = y[i];
     }
     __syncthreads();
   }
-  // three passes: A -> B -> A -> B
-  for (int q = threadIdx.x; q < 5 * NP; q += kThreads) u[q] = B[q];
+  for (int q = tid; q < NP; q += T) u[q] = S[q];
 }
 
 template <int N>
 cudaError_t launch_n(const FilterLaunch& L, cudaStream_t s) {
-  const size_t smem = (size_t)(10 * N * N * N + N * N) * sizeof(double);
-  auto k = filter_kernel<N>;
-  cudaError_t err = cudaFuncSetAttribute(k, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
-  if (err != cudaSuccess) return err;
   if (L.n_tasks <= 0) return cudaSuccess;
-  k<<<(unsigned)L.n_tasks, kThreads, smem, s>>>(L);
+  filter_kernel<N><<<(unsigned)(L.n_tasks * kVars), filt::line_threads<N>(), 0, s>>>(L);
   return cudaGetLastError();
 }
 

@@ -12,136 +12,115 @@
 // formed from the FP64 state in double-float arithmetic (hi + lo FP32
 // values and tables, compensated products and sums) and rounded once.
 //
-// filter_residual_kernel: R for one element per block: u split into (hi, lo)
-// pairs in shared memory, three sweeps of F, then (F u) - u.
-// filter_combine_kernel: out = ar R + ad D + b F(X + Y) for one element per
-// block (X + Y staged in shared memory, three FP32 sweeps), written as FP32
-// and / or added to an FP64 base.
+// Both kernels run one block per (element, variable) and one thread per
+// line, with F's mirror symmetry (filter_line.cuh); each axis pass reads every
+// thread's line into registers, synchronises and writes the result in place.
+// filter_residual_kernel: R = (F u) - u, u split into (hi, lo) FP32 pairs,
+// three compensated sweeps with the hi + lo split tables, rounded once.
+// filter_combine_kernel: out = ar R + ad D + b F(X + Y), X + Y staged, three
+// FP32 sweeps, written as FP32 and / or added to an FP64 base.
 #include "common.cuh"
 #include "dg_device.cuh"
+#include "filter_line.cuh"
 #include "launch.hpp"
 
 namespace dgsw {
 namespace {
 
-using dev::dot2_first;
-using dev::dot2_term;
 using dev::split_df;
 using dev::two_sum;
 using dev::widen;
 
-constexpr int kThreads = 256;
-
-__device__ __forceinline__ void line_of(int N, int a, int line, int* base, int* stride) {
-  const int NN = N * N, ta = line % N, tb = line / N;
-  if (a == 0) {
-    *base = N * ta + NN * tb;
-    *stride = 1;
-  } else if (a == 1) {
-    *base = ta + NN * tb;
-    *stride = N;
-  } else {
-    *base = ta + N * tb;
-    *stride = NN;
-  }
-}
-
 template <int N>
-__global__ void __launch_bounds__(kThreads) filter_residual_kernel(MixedFilterLaunch L) {
-  constexpr int NN = N * N, NP = N * N * N;
-  extern __shared__ float2 rbuf[];
-  float2* A = rbuf;
-  float2* B = rbuf + 5 * NP;
-  float* Fh = reinterpret_cast<float*>(B + 5 * NP);
-  float* Fl = Fh + NN;
-  const int64_t e = L.tasks ? (int64_t)L.tasks[blockIdx.x] : (int64_t)blockIdx.x;
-  const int64_t off = L.offset ? L.offset[e] : e * (int64_t)(kVars * NP);
+__global__ void __launch_bounds__(filt::line_threads<N>())
+    filter_residual_kernel(MixedFilterLaunch L) {
+  constexpr int NN = N * N, NP = N * N * N, TS = filt::SymTab<N>::SIZE;
+  constexpr int T = filt::line_threads<N>();
+  __shared__ float Sh[NP], Sl[NP];
+  __shared__ float th[TS], tl[TS];
+  const int64_t slot = blockIdx.x / kVars;
+  const int v = (int)(blockIdx.x - slot * kVars);
+  const int64_t e = L.tasks ? (int64_t)L.tasks[slot] : slot;
+  const int64_t off = (L.offset ? L.offset[e] : e * (int64_t)(kVars * NP)) + (int64_t)v * NP;
   const double* u = L.u64 + off;
-  for (int q = threadIdx.x; q < 5 * NP; q += kThreads) {
-    float hi, lo;
-    split_df(u[q], hi, lo);
-    A[q] = make_float2(hi, lo);
-  }
-  for (int q = threadIdx.x; q < NN; q += kThreads) {
-    Fh[q] = L.Fh[q];
-    Fl[q] = L.Fl[q];
+  const int tid = threadIdx.x;
+  for (int q = tid; q < NP; q += T) split_df(u[q], Sh[q], Sl[q]);
+  for (int q = tid; q < TS; q += T) {
+    const double t = filt::sym_entry<N>(L.F, q);
+    const float hi = __double2float_rn(t);
+    th[q] = hi;
+    tl[q] = __double2float_rn(t - (double)hi);
   }
   __syncthreads();
+  const bool has = tid < NN;
 #pragma unroll 1
   for (int a = 0; a < 3; ++a) {
-    const float2* src = (a == 1) ? B : A;
-    float2* dst = (a == 1) ? A : B;
-    for (int task = threadIdx.x; task < 5 * NN; task += kThreads) {
-      const int v = task / NN, line = task - v * NN;
-      int base, stride;
-      line_of(N, a, line, &base, &stride);
-      float xh[N], xl[N];
+    int base = 0, stride = 0;
+    float xh[N], xl[N], yh[N], yl[N];
+    if (has) {
+      filt::axis_line<N>(a, tid, base, stride);
 #pragma unroll
       for (int i = 0; i < N; ++i) {
-        const float2 x = src[v * NP + base + i * stride];
-        xh[i] = x.x;
-        xl[i] = x.y;
+        xh[i] = Sh[base + i * stride];
+        xl[i] = Sl[base + i * stride];
       }
+    }
+    __syncthreads();  // every line read before any is overwritten
+    if (has) {
+      filt::sym_line_df<N>(xh, xl, yh, yl, th, tl);
 #pragma unroll
       for (int i = 0; i < N; ++i) {
-        float s, c;
-        dot2_first(Fh[i * N], Fl[i * N], xh[0], xl[0], s, c);
-#pragma unroll
-        for (int j = 1; j < N; ++j) dot2_term(Fh[i * N + j], Fl[i * N + j], xh[j], xl[j], s, c);
-        float h, l;
-        two_sum(s, c, h, l);
-        dst[v * NP + base + i * stride] = make_float2(h, l);
+        Sh[base + i * stride] = yh[i];
+        Sl[base + i * stride] = yl[i];
       }
     }
     __syncthreads();
   }
-  // three sweeps: A -> B -> A -> B; R = (F u) - u, rounded once
-  for (int q = threadIdx.x; q < 5 * NP; q += kThreads) {
+  // R = (F u) - u, rounded once
+  for (int q = tid; q < NP; q += T) {
     float uh, ul, s, t;
     split_df(u[q], uh, ul);
-    const float2 f = B[q];
-    two_sum(f.x, -uh, s, t);
-    L.r32[off + q] = s + (t + (f.y - ul));
+    two_sum(Sh[q], -uh, s, t);
+    L.r32[off + q] = s + (t + (Sl[q] - ul));
   }
 }
 
 template <int N>
-__global__ void __launch_bounds__(kThreads) filter_combine_kernel(MixedFilterLaunch L) {
-  constexpr int NN = N * N, NP = N * N * N;
-  extern __shared__ float cbuf[];
-  float* A = cbuf;
-  float* B = cbuf + 5 * NP;
-  float* F = B + 5 * NP;
-  const int64_t e = L.tasks ? (int64_t)L.tasks[blockIdx.x] : (int64_t)blockIdx.x;
-  const int64_t off = L.offset ? L.offset[e] : e * (int64_t)(kVars * NP);
-  for (int q = threadIdx.x; q < 5 * NP; q += kThreads)
-    A[q] = L.x32[off + q] + (L.y32 ? L.y32[off + q] : 0.0f);
-  for (int q = threadIdx.x; q < NN; q += kThreads) F[q] = L.Fh[q];
+__global__ void __launch_bounds__(filt::line_threads<N>())
+    filter_combine_kernel(MixedFilterLaunch L) {
+  constexpr int NN = N * N, NP = N * N * N, TS = filt::SymTab<N>::SIZE;
+  constexpr int T = filt::line_threads<N>();
+  __shared__ float S[NP];
+  __shared__ float tab[TS];
+  const int64_t slot = blockIdx.x / kVars;
+  const int v = (int)(blockIdx.x - slot * kVars);
+  const int64_t e = L.tasks ? (int64_t)L.tasks[slot] : slot;
+  const int64_t off = (L.offset ? L.offset[e] : e * (int64_t)(kVars * NP)) + (int64_t)v * NP;
+  const int tid = threadIdx.x;
+  for (int q = tid; q < NP; q += T) S[q] = L.x32[off + q] + (L.y32 ? L.y32[off + q] : 0.0f);
+  for (int q = tid; q < TS; q += T) tab[q] = (float)filt::sym_entry<N>(L.F, q);
   __syncthreads();
+  const bool has = tid < NN;
 #pragma unroll 1
   for (int a = 0; a < 3; ++a) {
-    const float* src = (a == 1) ? B : A;
-    float* dst = (a == 1) ? A : B;
-    for (int task = threadIdx.x; task < 5 * NN; task += kThreads) {
-      const int v = task / NN, line = task - v * NN;
-      int base, stride;
-      line_of(N, a, line, &base, &stride);
-      float x[N];
+    int base = 0, stride = 0;
+    float x[N], y[N];
+    if (has) {
+      filt::axis_line<N>(a, tid, base, stride);
 #pragma unroll
-      for (int i = 0; i < N; ++i) x[i] = src[v * NP + base + i * stride];
+      for (int i = 0; i < N; ++i) x[i] = S[base + i * stride];
+    }
+    __syncthreads();  // every line read before any is overwritten
+    if (has) {
+      filt::sym_line<N, float>(x, y, tab);
 #pragma unroll
-      for (int i = 0; i < N; ++i) {
-        float s = F[i * N] * x[0];
-#pragma unroll
-        for (int j = 1; j < N; ++j) s = fmaf(F[i * N + j], x[j], s);
-        dst[v * NP + base + i * stride] = s;
-      }
+      for (int i = 0; i < N; ++i) S[base + i * stride] = y[i];
     }
     __syncthreads();
   }
   const float ar = (float)L.ar, ad = (float)L.ad, b = (float)L.b;
-  for (int q = threadIdx.x; q < 5 * NP; q += kThreads) {
-    float w = b * B[q];
+  for (int q = tid; q < NP; q += T) {
+    float w = b * S[q];
     if (L.r32) w = fmaf(ar, L.r32[off + q], w);
     if (L.d32) w = fmaf(ad, L.d32[off + q], w);
     if (L.w32) L.w32[off + q] = w;
@@ -152,20 +131,11 @@ __global__ void __launch_bounds__(kThreads) filter_combine_kernel(MixedFilterLau
 template <int N>
 cudaError_t launch_n(const MixedFilterLaunch& L, bool residual, cudaStream_t s) {
   if (L.n_tasks <= 0) return cudaSuccess;
-  constexpr int NP = N * N * N, NN = N * N;
-  if (residual) {
-    const size_t smem = (size_t)10 * NP * sizeof(float2) + 2 * NN * sizeof(float);
-    auto k = filter_residual_kernel<N>;
-    cudaError_t err = set_kernel_smem<filter_residual_kernel<N>>((int)smem, false);
-    if (err != cudaSuccess) return err;
-    k<<<(unsigned)L.n_tasks, kThreads, smem, s>>>(L);
-  } else {
-    const size_t smem = (size_t)(10 * NP + NN) * sizeof(float);
-    auto k = filter_combine_kernel<N>;
-    cudaError_t err = set_kernel_smem<filter_combine_kernel<N>>((int)smem, false);
-    if (err != cudaSuccess) return err;
-    k<<<(unsigned)L.n_tasks, kThreads, smem, s>>>(L);
-  }
+  const unsigned blocks = (unsigned)(L.n_tasks * kVars);
+  if (residual)
+    filter_residual_kernel<N><<<blocks, filt::line_threads<N>(), 0, s>>>(L);
+  else
+    filter_combine_kernel<N><<<blocks, filt::line_threads<N>(), 0, s>>>(L);
   return cudaGetLastError();
 }
 
@@ -189,12 +159,12 @@ cudaError_t launch_any(const MixedFilterLaunch& L, bool residual, cudaStream_t s
 }  // namespace
 
 cudaError_t launch_filter_residual(const MixedFilterLaunch& L, cudaStream_t s) {
-  if (!L.u64 || !L.r32 || !L.Fh || !L.Fl) return cudaErrorInvalidValue;
+  if (!L.u64 || !L.r32 || !L.F) return cudaErrorInvalidValue;
   return launch_any(L, true, s);
 }
 
 cudaError_t launch_filter_combine(const MixedFilterLaunch& L, cudaStream_t s) {
-  if (!L.x32 || !L.Fh || (!L.w32 && !L.out64) || (L.out64 && !L.base64)) return cudaErrorInvalidValue;
+  if (!L.x32 || !L.F || (!L.w32 && !L.out64) || (L.out64 && !L.base64)) return cudaErrorInvalidValue;
   return launch_any(L, false, s);
 }
 

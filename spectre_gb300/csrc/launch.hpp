@@ -396,8 +396,10 @@ struct CswMixedLaunch {
   const int32_t* nbr = nullptr;
   float gamma1 = 0.0f, gamma2 = 0.0f;
   EoTable eo{};
+  int variant = 0;  // launch shape (csw_mixed.cuh), < csw_mixed_shapes()
 };
 cudaError_t launch_csw_mixed(const CswMixedLaunch& L, cudaStream_t s);
+int csw_mixed_shapes();
 
 struct CswSetup {
   int n = 0;
@@ -453,14 +455,13 @@ cudaError_t launch_filter(const FilterLaunch& L, cudaStream_t s);
 // residual: r32 = (F - I) u64, compensated; combine: out = ar r32 + ad d32 +
 // b F(x32 + y32), to w32 and / or out64 = base64 + out.  tasks / offset null:
 // elements 0..n_tasks-1 of extent n, packed; else the listed elements at
-// their value offsets.  Fh, Fl: the n x n filter matrix, FP32 hi and lo.
+// their value offsets.  F: the n x n filter matrix (FP64, row-major).
 struct MixedFilterLaunch {
   int n = 0;
   int64_t n_tasks = 0;
   const int32_t* tasks = nullptr;
   const int64_t* offset = nullptr;
-  const float* Fh = nullptr;
-  const float* Fl = nullptr;
+  const double* F = nullptr;
   const double* u64 = nullptr;
   float* r32 = nullptr;          // residual output / combine input
   const float* x32 = nullptr;

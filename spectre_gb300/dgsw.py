@@ -798,7 +798,8 @@ class DgEvolution:
                self._h)
         return v.value, ms
 
-    TUNE_FAMILIES = {0: "none", 1: "fp64_stage", 2: "mixed_batch", 3: "mixed_pipe"}
+    TUNE_FAMILIES = {0: "none", 1: "fp64_stage", 2: "mixed_batch", 3: "mixed_pipe",
+                     4: "mixed_curved"}
 
     def tune(self, force_variant: int = -1):
         """Re-times the launch shapes of the handle's step kernels on its own

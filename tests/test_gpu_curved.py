@@ -141,3 +141,35 @@ def test_curved_mixed_n12(oracle):
     assert rel_l2(evm.get_state(), ev64.get_state()) < 1e-7
     ev64.close()
     evm.close()
+
+
+@pytest.mark.parametrize("n", [5, 10, 12])
+def test_curved_mixed_launch_shapes_agree(oracle, n):
+    # the mixed curved stage kernel's launch shapes (dgsw_tune family
+    # mixed_curved: 256 threads at two occupancies, 512 threads): the tuner
+    # restores the state it times on, every shape gives the same bits, and
+    # all stay within the mixed bar of FP64 over 20 steps
+    ev64, _ = make(oracle, 1, 2, n)
+    ev64.set_gaussian_shell(1.0, 8.0, 1.0)
+    u0 = ev64.get_state()
+    ev64.step(20, 1e-3)
+    ref = ev64.get_state()
+    ev64.close()
+    out = []
+    evm, _ = make(oracle, 1, 2, n, precision=dgsw.PRECISION_MIXED)
+    evm.set_state(u0)
+    info = evm.tune()
+    assert info["family"] == "mixed_curved"
+    assert len(info["ms_per_step"]) == 3
+    assert all(ms > 0 for ms in info["ms_per_step"])
+    np.testing.assert_array_equal(evm.get_state(), u0)
+    for v in range(3):
+        assert evm.tune(force_variant=v)["variant"] == v
+        evm.set_state(u0)
+        evm.step(20, 1e-3)
+        out.append(evm.get_state())
+    evm.close()
+    for got in out:
+        assert rel_l2(got, ref) < 1e-6
+    for got in out[1:]:
+        np.testing.assert_array_equal(out[0], got)

@@ -287,12 +287,11 @@ struct Run {
   // history, face packages into the own local and the neighbours' remote
   // boundary histories
   void record(const double* u, const std::vector<int64_t>& who, Id id, int order) {
-    std::vector<double> dudt((size_t)sys.E * kVarsA * sys.np);
+    std::vector<double> dudt((size_t)sys.total_values());
     sys.volume_rhs(u, dudt.data());
-    const int64_t per = kVarsA * sys.np;
     for (int64_t e : who) {
-      el[e].vol.push_back(
-          {id, order, std::vector<double>(dudt.begin() + e * per, dudt.begin() + (e + 1) * per)});
+      const int64_t o = sys.offset_of(e), per = (int64_t)kVarsA * sys.n_of(e) * sys.n_of(e) * sys.n_of(e);
+      el[e].vol.push_back({id, order, std::vector<double>(dudt.begin() + o, dudt.begin() + o + per)});
       for (int dir = 0; dir < 6; ++dir) {
         const int64_t nb = sys.neighbor(e, dir);
         if (nb < 0) continue;
@@ -315,9 +314,10 @@ struct Run {
     std::vector<int64_t> t;
     for (const VolEntry& v : h) t.push_back(v.id.tick);
     const std::vector<double> c = coefficients(t, start, end, clk);
-    double* ue = u + e * kVarsA * sys.np;
+    double* ue = u + sys.offset_of(e);
+    const int64_t per = (int64_t)h.back().dt.size();
     for (int j = 0; j < order; ++j)
-      for (int64_t p = 0; p < kVarsA * sys.np; ++p) ue[p] += c[j] * h[j].dt[p];
+      for (int64_t p = 0; p < per; ++p) ue[p] += c[j] * h[j].dt[p];
     return 0;
   }
 
@@ -325,8 +325,9 @@ struct Run {
   // coupling being dg_boundary_terms lifted onto the GLL face; then
   // add_slice_to_data
   int boundary_delta(double* u, int64_t e, int64_t start, int64_t end) const {
-    const int n = sys.n, nf = n * n;
-    double* ue = u + e * kVarsA * sys.np;
+    const int n = sys.n_of(e), nf = n * n;
+    const int64_t np = (int64_t)nf * n;
+    double* ue = u + sys.offset_of(e);
     const double slice_factor = -0.5 * (double)(n * (n - 1));
     for (int dir = 0; dir < 6; ++dir) {
       if (sys.neighbor(e, dir) < 0) continue;
@@ -339,9 +340,13 @@ struct Run {
       const int rc = lts_coefficients(lid, rid, start, end, ord, ord, ord, clk, &terms);
       if (rc) return rc;
       std::vector<double> lifted((size_t)kVarsA * nf, 0.0), bc((size_t)kVarsA * nf);
+      std::vector<double> bc_m;
       for (const Term& t : terms) {
         const LocalEntry& L = m.local[t.local];
-        sys.boundary_terms(L.pkg, m.remote[t.remote].pkg, bc.data());
+        const int nm = sys.mortar_n(e, dir);
+        bc_m.assign((size_t)kVarsA * nm * nm, 0.0);
+        sys.boundary_terms(L.pkg, m.remote[t.remote].pkg, bc_m.data());
+        sys.mortar_to_face(e, dir, bc_m.data(), bc.data());
         for (int v = 0; v < kVarsA; ++v)
           for (int f = 0; f < nf; ++f)
             lifted[(size_t)v * nf + f] += t.coef * (bc[(size_t)v * nf + f] * (slice_factor * L.mag[f]));
@@ -350,7 +355,7 @@ struct Run {
       for (int b = 0; b < n; ++b)
         for (int a = 0; a < n; ++a) {
           const int64_t vi = face_volume_index(n, d, slice, a, b);
-          for (int v = 0; v < kVarsA; ++v) ue[v * sys.np + vi] += lifted[(size_t)v * nf + a + n * b];
+          for (int v = 0; v < kVarsA; ++v) ue[v * np + vi] += lifted[(size_t)v * nf + a + n * b];
         }
     }
     return 0;
@@ -418,6 +423,121 @@ struct FlatSystem : System {
   }
 };
 
+// M (rows x cols, row-major) applied along both axes of nfields face blocks
+// of cols^2 values: out[f][ip + rows bp] = sum M[ip][i] M[bp][b] in[f][i + cols b]
+void face_matrix(int rows, int cols, const double* M, int nfields, const double* in, double* out) {
+  std::vector<double> tmp((size_t)rows * cols);
+  for (int f = 0; f < nfields; ++f) {
+    const double* src = in + (size_t)f * cols * cols;
+    double* dst = out + (size_t)f * rows * rows;
+    for (int b = 0; b < cols; ++b)
+      for (int ip = 0; ip < rows; ++ip) {
+        double s = 0.0;
+        for (int i = 0; i < cols; ++i) s += M[ip * cols + i] * src[i + cols * b];
+        tmp[ip + (size_t)rows * b] = s;
+      }
+    for (int bp = 0; bp < rows; ++bp)
+      for (int ip = 0; ip < rows; ++ip) {
+        double s = 0.0;
+        for (int b = 0; b < cols; ++b) s += M[bp * cols + b] * tmp[ip + (size_t)rows * b];
+        dst[ip + (size_t)rows * bp] = s;
+      }
+  }
+}
+
+// Flat scalar wave on conforming periodic bricks whose elements have their own
+// LGL extents (p-nonconforming faces).  The mortar of a face has the larger of
+// the two extents (mortar_mesh, MortarHelpers.cpp:21-47); each side's package
+// is interpolated onto it where it is finer than the face
+// (projection_matrix_parent_to_child, Projection.cpp:310-330), and the
+// corrections come back by Legendre truncation (projection_matrix_child_to_
+// parent, Projection.cpp:97-130), as ApplyBoundaryCorrections.hpp:880-937
+// does for every (local, remote) record pair.
+struct MixedFlatSystem : System {
+  int n_inst = 0;
+  const OrcBrick* br = nullptr;
+  double gamma2 = 0.0;
+  int threads = 0;
+  std::vector<int32_t> elem_n, nbr, inst;
+  std::vector<int64_t> off;     // n_elem + 1 block offsets
+  std::vector<double> invjac;  // 3 per element
+
+  int n_of(int64_t e) const override { return elem_n[e]; }
+  int64_t offset_of(int64_t e) const override { return off[e]; }
+  int64_t total_values() const override { return off[E]; }
+  int64_t neighbor(int64_t e, int dir) const override { return nbr[6 * e + dir]; }
+  int back_dir(int64_t, int dir) const override { return dir ^ 1; }
+  void volume_rhs(const double* u, double* dudt) override {
+    orc_volume_rhs(n_inst, br, elem_n.data(), gamma2, u, dudt, threads);
+  }
+  int mortar_n(int64_t e, int dir) const override {
+    return std::max(elem_n[e], elem_n[nbr[6 * e + dir]]);
+  }
+  // dg_package_data on e's own face points
+  void face_package(const double* u, int64_t e, int dir, std::vector<double>* pkg,
+                    std::vector<double>* mag) const {
+    const int ne = elem_n[e], d = dir / 2, nf = ne * ne;
+    const int64_t np_e = (int64_t)nf * ne;
+    const bool upper = dir % 2;
+    const int slice = upper ? ne - 1 : 0;
+    const double* ue = u + off[e];
+    std::vector<double> psi(nf), pi(nf), phi(3 * nf), g2(nf, gamma2), nrm(3 * nf, 0.0);
+    mag->assign(nf, invjac[3 * e + d]);
+    for (int b = 0; b < ne; ++b)
+      for (int a = 0; a < ne; ++a) {
+        const int f = a + ne * b;
+        const int64_t v = face_volume_index(ne, d, slice, a, b);
+        psi[f] = ue[v];
+        pi[f] = ue[np_e + v];
+        for (int i = 0; i < 3; ++i) phi[i * nf + f] = ue[(2 + i) * np_e + v];
+        nrm[d * nf + f] = upper ? 1.0 : -1.0;
+      }
+    pkg->assign((size_t)16 * nf, 0.0);
+    double ms;
+    orc_package(nf, psi.data(), pi.data(), phi.data(), g2.data(), nrm.data(), nullptr, pkg->data(),
+                &ms);
+  }
+  // a face package of extent nf_n onto the mortar of extent nm
+  static void to_mortar(int nf_n, int nm, const std::vector<double>& f, std::vector<double>* out) {
+    if (nm == nf_n) {
+      *out = f;
+      return;
+    }
+    std::vector<double> P((size_t)nm * nf_n);
+    orc_proj_face_to_mortar(nf_n, nm, P.data());
+    out->assign((size_t)16 * nm * nm, 0.0);
+    face_matrix(nm, nf_n, P.data(), 16, f.data(), out->data());
+  }
+  void package(const double* u, int64_t e, int dir, std::vector<double>* pkg,
+               std::vector<double>* mag) const override {
+    std::vector<double> f;
+    face_package(u, e, dir, &f, mag);
+    to_mortar(elem_n[e], mortar_n(e, dir), f, pkg);
+  }
+  void exterior_package(const double* u, int64_t e, int dir,
+                        std::vector<double>* pkg) const override {
+    // aligned bricks: the neighbour's face points run in e's order
+    const int64_t nb = nbr[6 * e + dir];
+    std::vector<double> f, mag;
+    face_package(u, nb, dir ^ 1, &f, &mag);
+    to_mortar(elem_n[nb], mortar_n(e, dir), f, pkg);
+  }
+  void boundary_terms(const std::vector<double>& pi, const std::vector<double>& pe,
+                      double* out) const override {
+    orc_boundary_terms((int)(pi.size() / 16), pi.data(), pe.data(), out);
+  }
+  void mortar_to_face(int64_t e, int dir, const double* on_mortar, double* on_face) const override {
+    const int ne = elem_n[e], nm = mortar_n(e, dir);
+    if (nm == ne) {
+      std::copy(on_mortar, on_mortar + (size_t)kVarsA * ne * ne, on_face);
+      return;
+    }
+    std::vector<double> R((size_t)ne * nm);
+    orc_proj_mortar_to_face(ne, nm, R.data());
+    face_matrix(ne, nm, R.data(), kVarsA, on_mortar, on_face);
+  }
+};
+
 }  // namespace
 
 int lts_evolve(System& sys, int order, const int32_t* levels, double slab, int n_slabs, double* u) {
@@ -441,7 +561,7 @@ int lts_evolve(System& sys, int order, const int32_t* levels, double slab, int n
     return t < switch_tick ? first_step : (S >> (levels ? levels[e] : 0));
   };
   R.clk = Clock{slab, S, 0.0};
-  const int64_t total = (int64_t)kVarsA * sys.np * sys.E;
+  const int64_t total = sys.total_values();
   std::vector<double> u0(u, u + total);
   std::vector<int64_t> all(sys.E);
   for (int64_t e = 0; e < sys.E; ++e) all[e] = e;
@@ -559,6 +679,40 @@ int orc_evolve_adams(int n_inst, const OrcBrick* br, int n, double gamma2, int o
   sys.gamma2 = gamma2;
   sys.threads = n_threads;
   sys.elem_n.assign(sys.E, n);
+  sys.nbr.resize(6 * sys.E);
+  sys.inst.resize(sys.E);
+  std::vector<uint64_t> ids(sys.E);
+  std::vector<int32_t> ijk(3 * sys.E);
+  const int mrc = orc_index_maps(n_inst, br, ids.data(), sys.nbr.data(), ijk.data(), sys.inst.data());
+  if (mrc != 0 && mrc != -2) return -1;
+  sys.invjac.resize(3 * sys.E);
+  for (int64_t e = 0; e < sys.E; ++e)
+    for (int d = 0; d < 3; ++d) {
+      const OrcBrick& b = br[sys.inst[e]];
+      sys.invjac[3 * e + d] = 2.0 / ((b.hi[d] - b.lo[d]) / b.n[d]);
+    }
+  return orc_adams::lts_evolve(sys, order, levels, slab, n_slabs, u);
+}
+
+int orc_evolve_adams_extents(int n_inst, const OrcBrick* br, const int32_t* elem_n, double gamma2,
+                             int order, const int32_t* levels, double slab, int n_slabs, double* u,
+                             int n_threads) {
+  if (n_inst < 1 || !br || !elem_n) return -1;
+  orc_adams::MixedFlatSystem sys;
+  sys.n_inst = n_inst;
+  sys.br = br;
+  sys.E = orc_num_elements(n_inst, br);
+  sys.gamma2 = gamma2;
+  sys.threads = n_threads;
+  sys.elem_n.assign(elem_n, elem_n + sys.E);
+  sys.off.assign(sys.E + 1, 0);
+  for (int64_t e = 0; e < sys.E; ++e) {
+    const int ne = sys.elem_n[e];
+    if (ne < 2 || ne > 20) return -1;
+    sys.off[e + 1] = sys.off[e] + (int64_t)5 * ne * ne * ne;
+  }
+  sys.n = sys.elem_n[0];
+  sys.np = (int64_t)sys.n * sys.n * sys.n;
   sys.nbr.resize(6 * sys.E);
   sys.inst.resize(sys.E);
   std::vector<uint64_t> ids(sys.E);

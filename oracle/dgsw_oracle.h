@@ -296,6 +296,12 @@ int orc_lts_coefficients(int n_local, const int64_t* local_slab, const int64_t* 
  * steps at the finest step.  u in place. */
 int orc_evolve_adams(int n_inst, const OrcBrick* bricks, int n, double gamma2, int order,
                      const int32_t* levels, double slab, int n_slabs, double* u, int n_threads);
+/* The same on bricks whose elements have their own extents elem_n[e]
+ * (p-nonconforming faces through mortars at the larger extent); u in the
+ * layout of orc_offsets. */
+int orc_evolve_adams_extents(int n_inst, const OrcBrick* bricks, const int32_t* elem_n,
+                             double gamma2, int order, const int32_t* levels, double slab,
+                             int n_slabs, double* u, int n_threads);
 
 #ifdef __cplusplus
 }

@@ -101,6 +101,7 @@ def _load(path):
         "orc_adams_coefficients": [I, P, I64, I64, D, I64, P],
         "orc_lts_coefficients": [I, P, P, I, P, P, I64, I64, D, I64, I, I, I, I, P, P, P],
         "orc_evolve_adams": [I, P, I, D, I, P, D, I, P, I],
+        "orc_evolve_adams_extents": [I, P, P, D, I, P, D, I, P, I],
         "orc_shell_evolve_adams": [P, I, P, D, I, P, I],
     }
     for name, args in sig.items():
@@ -596,6 +597,19 @@ def evolve_adams(bricks, n, u, slab, n_slabs, order, levels=None, gamma2=0.0, th
     lv = None if levels is None else np.ascontiguousarray(levels, dtype=np.int32)
     _check(lib().orc_evolve_adams(len(bricks), ctypes.addressof(arr), n, gamma2, order, _p(lv),
                                   slab, n_slabs, _p(u), threads))
+    return u
+
+
+def evolve_adams_extents(bricks, elem_n, u, slab, n_slabs, order, levels=None, gamma2=0.0,
+                         threads=0):
+    """AdamsBashforth(order) with local time stepping on bricks whose
+    elements have their own extents (p-nonconforming mortars)."""
+    u = np.array(u, dtype=np.float64, copy=True)
+    arr = _bricks(bricks)
+    en = np.ascontiguousarray(elem_n, dtype=np.int32)
+    lv = None if levels is None else np.ascontiguousarray(levels, dtype=np.int32)
+    _check(lib().orc_evolve_adams_extents(len(bricks), ctypes.addressof(arr), _p(en), gamma2,
+                                          order, _p(lv), slab, n_slabs, _p(u), threads))
     return u
 
 

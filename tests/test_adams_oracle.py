@@ -114,3 +114,30 @@ def test_curved_shell_order(oracle, order, lts):
     errs = [np.abs(oracle.shell_evolve_adams(s, u0, T / k, k, order, levels=levels).ravel()
                    - ref.ravel()).max() for k in (8, 16)]
     assert math.log2(errs[0] / errs[1]) > order - 0.5
+
+
+def test_extents_path_of_one_extent_is_the_uniform_path(oracle):
+    # the oracle's per-element-extent system with every extent equal runs the
+    # same arithmetic as the uniform one
+    n = 4
+    bricks, u0 = _plane_wave_case(oracle, n)
+    levels = [0, 1, 0, 1, 1, 0, 1, 0]
+    a = oracle.evolve_adams(bricks, n, u0, 0.05, 3, 3, levels=levels)
+    b = oracle.evolve_adams_extents(bricks, [n] * 8, u0, 0.05, 3, 3, levels=levels)
+    np.testing.assert_array_equal(a, b)
+
+
+@pytest.mark.parametrize("levels", [None, [0, 1, 0, 1, 1, 0, 1, 0], [2, 1, 1, 0, 1, 0, 0, 0]])
+@pytest.mark.parametrize("order", [2, 3])
+def test_extents_local_stepping_order(oracle, levels, order):
+    # p-nonconforming faces (mortars at the larger extent) with 1:1, 2:1 and
+    # 4:1 step ratios keep the order of the method against a time-resolved
+    # SSP-RK3 run of the same semi-discrete system
+    elem_n = [4, 5, 6, 4, 5, 4, 6, 5]
+    T = 0.4
+    bricks = [Brick((2, 2, 2), (0.0, 0.0, 0.0), (2 * math.pi,) * 3)]
+    u0 = oracle.initial_data(bricks, elem_n, "plane_wave", [1.0, 1.0, 1.0])
+    ref = oracle.evolve(bricks, elem_n, u0, T / 800, 800)
+    errs = [np.abs(oracle.evolve_adams_extents(bricks, elem_n, u0, T / s, s, order,
+                                               levels=levels) - ref).max() for s in (8, 16)]
+    assert math.log2(errs[0] / errs[1]) > order - 0.5

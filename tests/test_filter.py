@@ -39,6 +39,31 @@ def test_product_filter_matrix_matches_oracle(dgsw_lib, oracle, n):
                                    oracle.exponential_filter(n, alpha, hp), rtol=0, atol=1e-13)
 
 
+@pytest.mark.parametrize("n", range(2, 13))
+def test_filter_matrix_mirror_symmetry(dgsw_lib, n):
+    # the filter kernels apply F through its mirror symmetry F[N-1-i][N-1-j]
+    # = F[i][j] (symmetric LGL nodes, Legendre parity); the host matrices
+    # hold it to rounding, and the even/odd form reproduces F x
+    rng = np.random.default_rng(n)
+    for alpha, hp in ((12.0, 32), (36.0, 8), (0.0, 4)):
+        F = dgsw.exponential_filter_matrix(n, alpha, hp)
+        np.testing.assert_allclose(F[::-1, ::-1], F, rtol=0, atol=1e-14)
+        h = n // 2
+        A = 0.5 * (F[:h, :h] + F[:h, ::-1][:, :h])
+        B = 0.5 * (F[:h, :h] - F[:h, ::-1][:, :h])
+        for x in rng.standard_normal((4, n)):
+            e = x[:h] + x[::-1][:h]
+            o = x[:h] - x[::-1][:h]
+            P = A @ e + (F[:h, h] * x[h] if n % 2 else 0.0)
+            Q = B @ o
+            y = np.empty(n)
+            y[:h] = P + Q
+            y[n - h:] = (P - Q)[::-1]
+            if n % 2:
+                y[h] = 0.5 * (F[h, :h] + F[h, ::-1][:h]) @ e + F[h, h] * x[h]
+            np.testing.assert_allclose(y, F @ x, rtol=0, atol=1e-13 * (1 + np.abs(x).sum()))
+
+
 def _rel(a, b, elem_n):
     a = np.asarray(a).ravel()
     b = np.asarray(b).ravel()

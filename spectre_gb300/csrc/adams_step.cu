@@ -31,6 +31,17 @@
 // Work split as stage_fp64.cu: N*N threads per element, one line per thread
 // in each of the three axis passes; the element's state is staged in shared
 // memory.
+//
+// Elements of differing extents (GEN): one launch per extent class; each
+// element's blocks sit at its own offsets in the state, the F ring and the B
+// ring.  The reference couples a p-nonconforming face on the mortar at the
+// larger extent for every (local, remote) record pair and projects the
+// correction back (ApplyBoundaryCorrections.hpp:816-937); the coupling is
+// linear and restriction after interpolation is the identity, so the sum of
+// pairs equals (W_int - T W_ext) / 2 with W_ext the neighbour's weighted
+// records on its own grid and T = R P the separable face map (as
+// stage_general.cu).  ab_pnc_faces_kernel forms T W_ext per such face before
+// the class launches.
 #include "common.cuh"
 #include "dg_device.cuh"
 #include "launch.hpp"
@@ -53,11 +64,11 @@ constexpr int ab_epb() {
   return N <= 4 ? 8 : (N <= 6 ? 4 : (N <= 10 ? 2 : 1));
 }
 
-// face record of element rec's face dir at point t: side 0 is the element's
-// own w there, side 1 the w of the neighbour's sign
-__device__ __forceinline__ double face_w(const double* __restrict__ B, int64_t rec, int dir, int t,
-                                         int NN, int side) {
-  return __ldg(B + ((rec * 6 + dir) * 2 + side) * (int64_t)NN + t);
+// an element's face record (B at its block) for face dir at point t: side 0
+// is the element's own w there, side 1 the w of the neighbour's sign
+__device__ __forceinline__ double face_w(const double* __restrict__ B, int dir, int t, int NN,
+                                         int side) {
+  return __ldg(B + (int64_t)(dir * 2 + side) * NN + t);
 }
 
 // resident blocks per SM asked of the register allocator: the FP64 pipe binds
@@ -69,7 +80,7 @@ constexpr int ab_min_blocks() {
   return N == 8 ? 4 : 1;
 }
 
-template <int N, int EPB>
+template <int N, int EPB, bool GEN>
 __global__ void __launch_bounds__(N * N * EPB, ab_min_blocks<N>())
     ab_step_kernel(const __grid_constant__ AbArgs A) {
   using S = AbShape<N>;
@@ -93,9 +104,17 @@ __global__ void __launch_bounds__(N * N * EPB, ab_min_blocks<N>())
   double* U = smem + slot * S::SLOT;  // Psi, Pi, Phi_x, Phi_y, Phi_z
   double* Sacc = U + 5 * NP;          // running dt Pi
   double* T = Sacc + NP;              // three scaled split tables
-  const int64_t off = e * (int64_t)(kVars * NP);
+  const int64_t off = GEN ? A.offset[e] : e * (int64_t)(kVars * NP);
   const int64_t E = A.n_elem;
   const double g2 = A.gamma2;
+  // element el's volume record in slot s of F, and its face records in slot
+  // s of B
+  auto frec = [&](int s) -> int64_t {
+    return GEN ? (int64_t)s * A.total + off : ((int64_t)s * E + e) * (kVars * NP);
+  };
+  auto brec = [&](int s, int64_t el) -> int64_t {
+    return GEN ? (int64_t)s * A.total_b + A.boff[el] : ((int64_t)s * E + el) * 12 * (int64_t)NN;
+  };
 
   double jd[3] = {0.0, 0.0, 0.0};
   if (active)
@@ -126,9 +145,14 @@ __global__ void __launch_bounds__(N * N * EPB, ab_min_blocks<N>())
       const AbFaceTable& f = J.face[A.level[nb]];
       double wi = 0.0, we = 0.0;
       for (int i = 0; i < f.n_loc; ++i)
-        wi = fma(f.loc_c[i], face_w(A.B, (int64_t)f.loc_slot[i] * E + e, dir, t, NN, 0), wi);
-      for (int i = 0; i < f.n_rem; ++i)
-        we = fma(f.rem_c[i], face_w(A.B, (int64_t)f.rem_slot[i] * E + nb, dir ^ 1, t, NN, 1), we);
+        wi = fma(f.loc_c[i], face_w(A.B + brec(f.loc_slot[i], e), dir, t, NN, 0), wi);
+      const int32_t pr = GEN ? A.face_idx[6 * e + dir] : -1;
+      if (pr >= 0) {
+        we = __ldg(A.wext + (int64_t)pr * NN + t);
+      } else {
+        for (int i = 0; i < f.n_rem; ++i)
+          we = fma(f.rem_c[i], face_w(A.B + brec(f.rem_slot[i], nb), dir ^ 1, t, NN, 1), we);
+      }
       dwf[dir] = -0.25 * (double)(N * (N - 1)) * jd[dir >> 1] * (wi - we);
     }
   }
@@ -142,7 +166,7 @@ __global__ void __launch_bounds__(N * N * EPB, ab_min_blocks<N>())
     if (update)
       for (int i = 0; i < J.n_vol; ++i) {
         const double c = J.vol_c[i];
-        const double* Fi = A.F + ((int64_t)J.vol_slot[i] * E + e) * (kVars * NP);
+        const double* Fi = A.F + frec(J.vol_slot[i]);
         for (int q = t; q < 5 * NP; q += NN) U[q] = fma(c, __ldg(Fi + q), U[q]);
       }
     for (int q = t; q < 3 * TAB; q += NN) {
@@ -179,8 +203,8 @@ __global__ void __launch_bounds__(N * N * EPB, ab_min_blocks<N>())
     for (int q = t; q < 5 * NP; q += NN) A.u[off + q] = U[q];
 
   // 3. record: volume time derivative and face data of the new state
-  double* Fo = A.F + ((int64_t)(active ? J.rec_slot : 0) * E + e) * (kVars * NP);
-  double* Bo = A.B + ((int64_t)(active ? J.rec_slot : 0) * E + e) * 12 * (int64_t)NN;
+  double* Fo = A.F + frec(active ? J.rec_slot : 0);
+  double* Bo = A.B + brec(active ? J.rec_slot : 0, e);
 #pragma unroll 1
   for (int d = 0; d < 3; ++d) {
     if (active) {
@@ -238,11 +262,11 @@ __global__ void __launch_bounds__(N * N * EPB, ab_min_blocks<N>())
   }
 }
 
-template <int N>
-cudaError_t launch_n(const AbArgs& A, cudaStream_t s) {
+template <int N, bool GEN>
+cudaError_t launch_nv(const AbArgs& A, cudaStream_t s) {
   constexpr int EPB = ab_epb<N>();
   const size_t smem = (size_t)EPB * AbShape<N>::SLOT * sizeof(double);
-  constexpr auto k = ab_step_kernel<N, EPB>;
+  constexpr auto k = ab_step_kernel<N, EPB, GEN>;
   cudaError_t err = set_kernel_smem<k>((int)smem, false);
   if (err != cudaSuccess) return err;
   int64_t total = 0;
@@ -250,6 +274,82 @@ cudaError_t launch_n(const AbArgs& A, cudaStream_t s) {
   const int64_t blocks = (total + EPB - 1) / EPB;
   if (blocks <= 0) return cudaSuccess;
   k<<<(unsigned)blocks, N * N * EPB, smem, s>>>(A);
+  return cudaGetLastError();
+}
+
+template <int N>
+cudaError_t launch_n(const AbArgs& A, cudaStream_t s) {
+  if (A.offset) {
+    if (!A.boff || !A.face_idx || A.total <= 0 || A.total_b <= 0) return cudaErrorInvalidValue;
+    return launch_nv<N, true>(A, s);
+  }
+  return launch_nv<N, false>(A, s);
+}
+
+// One warp per face record: the neighbour's weighted records (its own grid)
+// in shared memory, then T along the face's second axis and its first, as
+// pnc_faces_kernel (stage_general.cu) maps a state's exterior w.
+constexpr int kAbPncWarps = 4;
+
+template <int N>
+__global__ void __launch_bounds__(32 * kAbPncWarps)
+    ab_pnc_faces_kernel(const __grid_constant__ AbPncLaunch P) {
+  constexpr int NN = N * N;
+  __shared__ double sw[kAbPncWarps][kMaxN * kMaxN];
+  __shared__ double s2[kAbPncWarps][kMaxN * N];
+  const int warp = threadIdx.x / 32, lane = threadIdx.x % 32;
+  const int64_t r = (int64_t)blockIdx.x * kAbPncWarps + warp;
+  if (r >= P.n_rec) return;  // whole warps leave; only warp barriers follow
+  const int64_t face = P.rec_face[r];
+  const int64_t e = face / 6;
+  const int dir = (int)(face - 6 * e);
+  // the job of e's level, if it finishes a step in this launch
+  const int l = P.level[e];
+  int j = -1;
+  for (int q = 0; q < P.L.n_jobs; ++q)
+    if (P.L.job[q].level == l) {
+      j = q;
+      break;
+    }
+  if (j < 0) return;
+  const AbLevelJob& J = P.L.job[j];
+  if (!J.update || J.reset) return;
+  const int64_t nb = P.nbr[face];
+  const int nn = P.elem_n[nb], mm = nn * nn;
+  const AbFaceTable& f = J.face[P.level[nb]];
+  // side 1 of the neighbour's record of its face dir ^ 1: the w this face
+  // forms from the neighbour's data, on the neighbour's face points
+  const int64_t side = P.boff[nb] + (int64_t)((dir ^ 1) * 2 + 1) * mm;
+  double* w = sw[warp];
+  double* t2 = s2[warp];
+  for (int q = lane; q < mm; q += 32) {
+    double acc = 0.0;
+    for (int i = 0; i < f.n_rem; ++i)
+      acc = fma(f.rem_c[i], __ldg(P.B + (int64_t)f.rem_slot[i] * P.total_b + side + q), acc);
+    w[q] = acc;
+  }
+  __syncwarp();
+  const double* T = P.op64 + P.op_off[N * (kMaxN + 1) + nn];  // N x nn, row-major
+  for (int q = lane; q < nn * N; q += 32) {
+    const int pp = q % nn, b = q / nn;
+    double acc = 0.0;
+    for (int k = 0; k < nn; ++k) acc = fma(T[b * nn + k], w[pp + nn * k], acc);
+    t2[q] = acc;
+  }
+  __syncwarp();
+  for (int q = lane; q < NN; q += 32) {
+    const int a = q % N, b = q / N;
+    double acc = 0.0;
+    for (int k = 0; k < nn; ++k) acc = fma(T[a * nn + k], t2[k + nn * b], acc);
+    P.wext[r * NN + q] = acc;
+  }
+}
+
+template <int N>
+cudaError_t launch_pnc_n(const AbPncLaunch& P, cudaStream_t s) {
+  const int64_t blocks = (P.n_rec + kAbPncWarps - 1) / kAbPncWarps;
+  if (blocks <= 0) return cudaSuccess;
+  ab_pnc_faces_kernel<N><<<(unsigned)blocks, 32 * kAbPncWarps, 0, s>>>(P);
   return cudaGetLastError();
 }
 
@@ -268,6 +368,26 @@ cudaError_t launch_adams_step(const AbArgs& A, int n, cudaStream_t s) {
     case 10: return launch_n<10>(A, s);
     case 11: return launch_n<11>(A, s);
     case 12: return launch_n<12>(A, s);
+    default: return cudaErrorInvalidValue;
+  }
+}
+
+cudaError_t launch_adams_pnc_faces(const AbPncLaunch& P, cudaStream_t s) {
+  if (!P.rec_face || !P.elem_n || !P.nbr || !P.level || !P.boff || !P.B || !P.op64 || !P.op_off ||
+      !P.wext || P.total_b <= 0)
+    return cudaErrorInvalidValue;
+  switch (P.n) {
+    case 2: return launch_pnc_n<2>(P, s);
+    case 3: return launch_pnc_n<3>(P, s);
+    case 4: return launch_pnc_n<4>(P, s);
+    case 5: return launch_pnc_n<5>(P, s);
+    case 6: return launch_pnc_n<6>(P, s);
+    case 7: return launch_pnc_n<7>(P, s);
+    case 8: return launch_pnc_n<8>(P, s);
+    case 9: return launch_pnc_n<9>(P, s);
+    case 10: return launch_pnc_n<10>(P, s);
+    case 11: return launch_pnc_n<11>(P, s);
+    case 12: return launch_pnc_n<12>(P, s);
     default: return cudaErrorInvalidValue;
   }
 }

@@ -155,6 +155,14 @@ struct DgswHandle_ {
   int8_t* ab_level = nullptr;   // step level per element
   double* ab_F = nullptr;       // ring of volume time derivatives
   double* ab_B = nullptr;       // ring of face data
+  int64_t ab_points[kAbMaxLevels] = {};  // grid points of each level's elements
+  // elements of differing extents: the level list is sorted by (level,
+  // extent); each (level, extent) range, every element's block in a slot of
+  // the face-data ring and that slot's length
+  int32_t ab_cls_begin[kAbMaxLevels][kMaxN + 1] = {};
+  int32_t ab_cls_count[kAbMaxLevels][kMaxN + 1] = {};
+  int64_t* ab_boff = nullptr;
+  int64_t ab_total_b = 0;
   double ab_slab = std::nan("");
   // steps of a host-resident state with the copies overlapped (dgsw_step_host)
   cudaStream_t pipe_in = nullptr, pipe_out = nullptr;
@@ -1265,9 +1273,9 @@ cudaError_t capture_steps(DgswHandle h, double dt, int steps, cudaGraphExec_t* o
 // AdamsBashforth handle set-up: step levels, the level-sorted element list,
 // the schedule (whose dry run sizes the history rings) and the rings.
 int adams_init(DgswHandle h, const DgswConfig& cfg) {
-  if (h->refined || h->gauss || !h->dom.uniform || mixed(h))
+  if (h->refined || h->gauss || mixed(h) || (!h->dom.uniform && h->curved))
     return fail(h, DGSW_ERR_UNSUPPORTED,
-                "AdamsBashforth: Gauss-Lobatto, one extent, conforming elements, FP64");
+                "AdamsBashforth: Gauss-Lobatto, conforming elements (of any extents on bricks), FP64");
   const int64_t E = h->dom.n_elem;
   std::vector<int8_t> level(E, 0);
   for (int64_t e = 0; e < E; ++e) {
@@ -1283,11 +1291,19 @@ int adams_init(DgswHandle h, const DgswConfig& cfg) {
       if (nb >= 0) adj[level[e]][level[nb]] = true;  // < 0: the shell's boundary spheres
     }
   }
+  // the level list, each level's elements grouped by extent
   std::vector<int32_t> list;
   list.reserve(E);
   for (int l = 0; l < kAbMaxLevels; ++l)
-    for (int64_t e = 0; e < E; ++e)
-      if (level[e] == l) list.push_back((int32_t)e);
+    for (int n = kMinN; n <= kMaxN; ++n) {
+      h->ab_cls_begin[l][n] = (int32_t)list.size();
+      for (int64_t e = 0; e < E; ++e)
+        if (level[e] == l && h->dom.elem_n[e] == n) {
+          list.push_back((int32_t)e);
+          h->ab_points[l] += (int64_t)n * n * n;
+        }
+      h->ab_cls_count[l][n] = (int32_t)list.size() - h->ab_cls_begin[l][n];
+    }
   std::string err;
   const int order = cfg.stepper_order ? cfg.stepper_order : 3;
   if (!h->ab.init(order, adj, h->ab_count, &err)) return fail(h, DGSW_ERR_ARGUMENT, err);
@@ -1297,12 +1313,22 @@ int adams_init(DgswHandle h, const DgswConfig& cfg) {
   h->ab_level_host = level;
   const int n = h->dom.elem_n[0];
   const size_t slots = (size_t)h->ab.ring_slots();
-  if ((e = cudaMalloc(&h->ab_F, slots * E * kVars * n * n * n * sizeof(double))) != cudaSuccess)
+  if ((e = cudaMalloc(&h->ab_F, slots * h->dom.offset.back() * sizeof(double))) != cudaSuccess)
     return cuda_fail(h, e, "cudaMalloc time-derivative ring");
   // the shell records the whole state (its exterior points are reached
   // through the face offsets of the volume layout); bricks record the face w's
-  const size_t rec = h->curved ? (size_t)kVars * n * n * n : (size_t)12 * n * n;
-  if ((e = cudaMalloc(&h->ab_B, slots * E * rec * sizeof(double))) != cudaSuccess)
+  // (12 n^2 per element: 6 faces x (own w, the neighbour's w))
+  if (h->curved) {
+    h->ab_total_b = E * (int64_t)kVars * n * n * n;
+  } else {
+    std::vector<int64_t> boff(E + 1, 0);
+    for (int64_t el = 0; el < E; ++el)
+      boff[el + 1] = boff[el] + 12 * (int64_t)h->dom.elem_n[el] * h->dom.elem_n[el];
+    h->ab_total_b = boff[E];
+    if (h->general && (e = upload(&h->ab_boff, boff)) != cudaSuccess)
+      return cuda_fail(h, e, "upload face-record offsets");
+  }
+  if ((e = cudaMalloc(&h->ab_B, slots * h->ab_total_b * sizeof(double))) != cudaSuccess)
     return cuda_fail(h, e, "cudaMalloc face-data ring");
   h->adams = true;
   return DGSW_OK;
@@ -1341,9 +1367,53 @@ int adams_step(DgswHandle h, int n_steps, double dt) {
       DGSW_CUDA(h, cudaMemcpyAsync(h->t1, h->state, bytes, cudaMemcpyDeviceToDevice, h->stream));
     if (!h->ab.slab(&launches, &err)) return fail(h, DGSW_ERR_ARGUMENT, err);
     for (const AbLaunch& L : launches) {
-      if (!h->curved) {
+      if (!h->curved && !h->general) {
         A.L = L;
         DGSW_CUDA(h, launch_adams_step(A, n, h->stream));
+        continue;
+      }
+      if (!h->curved) {
+        // elements of differing extents: the exterior w of the faces whose
+        // neighbour has another extent, then one launch per extent class
+        for (int c = kMinN; c <= kMaxN; ++c) {
+          if (h->class_count[c] == 0 || h->pnc_count[c] == 0) continue;
+          AbPncLaunch P;
+          P.n = c;
+          P.n_rec = h->pnc_count[c];
+          P.rec_face = h->pnc_rec[c];
+          P.elem_n = h->elem_n;
+          P.nbr = h->nbr;
+          P.level = h->ab_level;
+          P.boff = h->ab_boff;
+          P.total_b = h->ab_total_b;
+          P.B = h->ab_B;
+          P.op64 = h->op64;
+          P.op_off = h->op_off;
+          P.wext = h->pnc_wext[c];
+          P.L = L;
+          DGSW_CUDA(h, launch_adams_pnc_faces(P, h->stream));
+        }
+        for (int c = kMinN; c <= kMaxN; ++c) {
+          if (h->class_count[c] == 0) continue;
+          AbArgs G = A;
+          G.L = L;
+          int64_t total = 0;
+          for (int j = 0; j < L.n_jobs; ++j) {
+            const int l = L.job[j].level;
+            G.L.job[j].begin = h->ab_cls_begin[l][c];
+            G.L.job[j].count = h->ab_cls_count[l][c];
+            total += G.L.job[j].count;
+          }
+          if (total == 0) continue;
+          G.eo = h->class_eo[c];
+          G.offset = h->offset;
+          G.boff = h->ab_boff;
+          G.total = h->dom.offset.back();
+          G.total_b = h->ab_total_b;
+          G.face_idx = h->pnc_face_idx;
+          G.wext = h->pnc_wext[c];
+          DGSW_CUDA(h, launch_adams_step(G, c, h->stream));
+        }
         continue;
       }
       // shell: update (volume part and boundary delta), then the records
@@ -1681,12 +1751,11 @@ int dgsw_adams_info(DgswHandle h, int* ring_slots, int64_t* ticks_per_slab,
                     int64_t* rhs_points_per_slab, int* launches_per_slab) {
   if (!h) return fail(nullptr, DGSW_ERR_ARGUMENT, "null handle");
   if (!h->adams) return fail(h, DGSW_ERR_UNSUPPORTED, "not an AdamsBashforth handle");
-  const int64_t np = (int64_t)h->dom.elem_n[0] * h->dom.elem_n[0] * h->dom.elem_n[0];
   int64_t pts = 0;
   int finest = 0;
   for (int l = 0; l < kAbMaxLevels; ++l)
     if (h->ab_count[l]) {
-      pts += h->ab_count[l] * np * h->ab.steps_per_slab(l);
+      pts += h->ab_points[l] * h->ab.steps_per_slab(l);
       finest = l;
     }
   if (ring_slots) *ring_slots = h->ab.ring_slots();
@@ -2155,9 +2224,10 @@ int dgsw_create(const DgswConfig* cfg, DgswHandle* out) {
     // way with or without a GPU
     int code = DGSW_OK;
     const char* why = nullptr;
-    if (h->refined || h->gauss || !h->dom.uniform || cfg->precision != DGSW_PRECISION_FP64) {
+    if (h->refined || h->gauss || (!h->dom.uniform && h->curved) ||
+        cfg->precision != DGSW_PRECISION_FP64) {
       code = DGSW_ERR_UNSUPPORTED;
-      why = "AdamsBashforth: Gauss-Lobatto, one extent, conforming elements, FP64";
+      why = "AdamsBashforth: Gauss-Lobatto, conforming elements (of any extents on bricks), FP64";
     } else if (cfg->stepper_order < 0 || cfg->stepper_order > kAbMaxOrder) {
       code = DGSW_ERR_ARGUMENT;
       why = "AdamsBashforth order must be in [1, 8] (0: 3)";
@@ -2392,6 +2462,7 @@ int dgsw_destroy(DgswHandle h) {
   if (h->ab_level) cudaFree(h->ab_level);
   if (h->ab_F) cudaFree(h->ab_F);
   if (h->ab_B) cudaFree(h->ab_B);
+  if (h->ab_boff) cudaFree(h->ab_boff);
   for (int n = 0; n <= kMaxN; ++n) {
     if (h->class_tasks[n]) cudaFree(h->class_tasks[n]);
     if (h->pnc_rec[n]) cudaFree(h->pnc_rec[n]);

@@ -90,8 +90,41 @@ struct AbArgs {
   double gamma2 = 0.0;
   EoTable eo{};
   AbLaunch L{};
+  // elements of differing extents (offset non-null): the launch covers the
+  // elements of extent n in the jobs' ranges; offset / boff give each
+  // element's block in the state (and in a ring slot of F, total values per
+  // slot) and in a ring slot of B (total_b values per slot); faces whose
+  // neighbour has another extent (face_idx >= 0) read their exterior w,
+  // already weighted over the records and mapped onto this face, from wext
+  const int64_t* offset = nullptr;
+  const int64_t* boff = nullptr;
+  int64_t total = 0, total_b = 0;
+  const int32_t* face_idx = nullptr;
+  const double* wext = nullptr;
 };
 cudaError_t launch_adams_step(const AbArgs& A, int n, cudaStream_t s);
+
+// The exterior w of the faces (records rec_face, 6 e + dir, of elements of
+// extent n) whose neighbour has another extent, for the elements that finish
+// a step in launch L: sum_r b_r of the neighbour's recorded w (its own grid),
+// mapped onto this face by T = R P (op64 / op_off as PncFaceLaunch); wext
+// gets n^2 values per record (adams_step.cu).
+struct AbPncLaunch {
+  int n = 0;
+  int64_t n_rec = 0;
+  const int32_t* rec_face = nullptr;
+  const int32_t* elem_n = nullptr;
+  const int32_t* nbr = nullptr;
+  const int8_t* level = nullptr;
+  const int64_t* boff = nullptr;
+  int64_t total_b = 0;
+  const double* B = nullptr;
+  const double* op64 = nullptr;
+  const int32_t* op_off = nullptr;
+  double* wext = nullptr;
+  AbLaunch L{};
+};
+cudaError_t launch_adams_pnc_faces(const AbPncLaunch& P, cudaStream_t s);
 
 // Exterior w = Pi - s Phi_d - gamma2 Psi of every 2:1 face of a refined
 // lattice (refined_faces.cu): the coarse neighbour's face interpolated to this

@@ -181,3 +181,69 @@ def test_curved_shell_matches_oracle(oracle, order, L):
         got = ev.get_state()
     want = oracle.shell_evolve_adams(s, u0, slab, slabs, order, levels=levels).ravel()
     assert per_var_rel(got, want, E, n) <= tol(order, slabs, L)
+
+
+def per_var_rel_extents(a, b, elem_n):
+    """per_var_rel on the layout of per-element extents."""
+    num, den = np.zeros(5), np.zeros(5)
+    off = 0
+    for n in elem_n:
+        npt = int(n) ** 3
+        for v in range(5):
+            sl = slice(off + v * npt, off + (v + 1) * npt)
+            num[v] = max(num[v], np.abs(a[sl] - b[sl]).max())
+            den[v] = max(den[v], np.abs(b[sl]).max())
+        off += 5 * npt
+    return float(max(num[v] / den[v] for v in range(5)))
+
+
+@pytest.mark.parametrize("order,L,gamma2", [(1, 0, 0.0), (3, 0, 0.6), (2, 1, 0.0), (3, 1, 0.6),
+                                            (4, 2, 0.0), (3, 3, 0.0)])
+def test_local_stepping_differing_extents_matches_oracle(oracle, order, L, gamma2):
+    # p-nonconforming faces (extents 3..9 per element, mortars at the larger
+    # extent) with step ratios up to 2^L against the oracle's literal
+    # per-mortar, per-record-pair evolution
+    bricks = [Brick((3, 3, 2), (0.0, 0.0, 0.0), (2.0, 2.0, 1.5)),
+              Brick((2, 2, 2), (0.0, 0.0, 0.0), (1.5, 1.5, 1.5))]
+    E = oracle.num_elements(bricks)
+    rng = np.random.default_rng(100 * order + L)
+    elem_n = rng.integers(3, 10, size=E).astype(np.int32)
+    levels = pattern(E, L, seed=order + 7) if L else None
+    u0 = oracle.initial_data(bricks, elem_n, "gaussian",
+                             oracle.gaussian_params(len(bricks), width=0.7,
+                                                    center=(0.9, 0.8, 0.7)))
+    slab, slabs = 0.004, 3
+    with DgEvolution(bricks, elem_n, gamma2=gamma2, time_stepper="adams_bashforth", order=order,
+                     step_levels=levels) as ev:
+        ev.set_state(u0)
+        ev.step(slabs, slab)
+        got = ev.get_state()
+        info = ev.adams_info()
+    want = oracle.evolve_adams_extents(bricks, elem_n, u0, slab, slabs, order, levels=levels,
+                                       gamma2=gamma2)
+    assert per_var_rel_extents(got, want, elem_n) <= tol(order, slabs, L)
+    lv = np.zeros(E, np.int64) if levels is None else levels.astype(np.int64)
+    assert info["rhs_points_per_slab"] == int(np.sum(2 ** lv * elem_n.astype(np.int64) ** 3))
+
+
+def test_local_stepping_differing_extents_converges(oracle):
+    # the product's LTS run on a p-nonconforming mesh against a time-resolved
+    # SSP-RK3 run of the same semi-discrete system: AB3 error shrinks at
+    # third order with the slab
+    bricks = [Brick((2, 2, 2), (0.0, 0.0, 0.0), (2 * math.pi,) * 3)]
+    elem_n = np.array([4, 5, 6, 4, 5, 4, 6, 5], np.int32)
+    levels = np.array([0, 1, 0, 1, 1, 0, 1, 0], np.int32)
+    T = 0.4
+    u0 = oracle.initial_data(bricks, elem_n, "plane_wave", [1.0, 1.0, 1.0])
+    with DgEvolution(bricks, elem_n) as rk:
+        rk.set_state(u0)
+        rk.step(800, T / 800)
+        ref = rk.get_state()
+    errs = []
+    for s in (8, 16):
+        with DgEvolution(bricks, elem_n, time_stepper="adams_bashforth", order=3,
+                         step_levels=levels) as ev:
+            ev.set_state(u0)
+            ev.step(s, T / s)
+            errs.append(float(np.abs(ev.get_state() - ref).max()))
+    assert math.log2(errs[0] / errs[1]) > 2.5

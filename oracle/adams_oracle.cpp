@@ -576,6 +576,7 @@ int lts_evolve(System& sys, int order, const int32_t* levels, double slab, int n
         for (int64_t e : all) {
           if ((rc = R.boundary_delta(u, e, j - 1, j))) return rc;
           R.clean(e);
+          sys.filter_element(u, e);
         }
       if (j == 0) std::copy(u0.begin(), u0.end(), u);
       R.record(u, all, Id{sn, j}, j < o ? o : o + 1);
@@ -604,6 +605,7 @@ int lts_evolve(System& sys, int order, const int32_t* levels, double slab, int n
     for (int64_t e : fin) {
       if ((rc = R.boundary_delta(u, e, R.el[e].start, P))) return rc;
       R.clean(e);
+      sys.filter_element(u, e);
     }
     if (P == final_tick) break;
     R.record(u, fin, Id{P / S, P}, order);

@@ -46,6 +46,12 @@ struct System {
     (void)dir;
     return n_of(e);
   }
+  // dg::Actions::Filter on element e after each of its steps (the curved
+  // executable's step actions end with it; none unless overridden)
+  virtual void filter_element(double* u, int64_t e) const {
+    (void)u;
+    (void)e;
+  }
   // project_from_mortar of the 5 corrections onto e's face dir (a copy where
   // the mortar is the face)
   virtual void mortar_to_face(int64_t e, int dir, const double* on_mortar, double* on_face) const {

@@ -2201,6 +2201,14 @@ int shell_rhs_impl(const ShellMesh& m, const double* u, double* dudt, bool morta
 // background, and the curved UpwindPenalty boundary terms.
 struct ShellSystem : orc_adams::System {
   ShellMesh m;
+  bool filter = false;  // the exponential filter after every step
+  double filter_alpha = 0.0;
+  int filter_half_power = 0;
+  void filter_element(double* u, int64_t e) const override {
+    if (!filter) return;
+    const int32_t ne = n;
+    orc_filter_elements(1, &ne, filter_alpha, filter_half_power, u + e * 5 * np);
+  }
   int64_t neighbor(int64_t e, int dir) const override { return m.nbr[6 * e + dir]; }
   int back_dir(int64_t e, int dir) const override {
     return shell_back_dir(m, e, m.nbr[6 * e + dir]);
@@ -2350,6 +2358,25 @@ int orc_shell_evolve_adams(const OrcShell* s, int order, const int32_t* levels, 
   sys.E = sys.m.E;
   sys.n = s->n;
   sys.np = (int64_t)s->n * s->n * s->n;
+  return orc_adams::lts_evolve(sys, order, levels, slab, n_slabs, u);
+}
+
+int orc_shell_evolve_adams_filtered(const OrcShell* s, int order, const int32_t* levels,
+                                    double slab, int n_slabs, double alpha, int half_power,
+                                    double* u, int n_threads) {
+  if (check_shell(s) || !u || !(alpha >= 0.0) || half_power < 0) return -1;
+#ifdef _OPENMP
+  if (n_threads > 0) omp_set_num_threads(n_threads);
+#endif
+  (void)n_threads;
+  ShellSystem sys;
+  build_shell(*s, &sys.m);
+  sys.E = sys.m.E;
+  sys.n = s->n;
+  sys.np = (int64_t)s->n * s->n * s->n;
+  sys.filter = true;
+  sys.filter_alpha = alpha;
+  sys.filter_half_power = half_power;
   return orc_adams::lts_evolve(sys, order, levels, slab, n_slabs, u);
 }
 

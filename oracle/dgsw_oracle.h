@@ -269,6 +269,12 @@ int orc_shell_evolve(const OrcShell* s, double dt, int n_steps, double* u, int n
  * through the boundary histories (adams_oracle.cpp) */
 int orc_shell_evolve_adams(const OrcShell* s, int order, const int32_t* levels, double slab,
                            int n_slabs, double* u, int n_threads);
+/* The same with dg::Actions::Filter (the exponential filter of
+ * orc_filter_elements) applied to each element after every one of its
+ * steps, as the curved executable's step actions end. */
+int orc_shell_evolve_adams_filtered(const OrcShell* s, int order, const int32_t* levels,
+                                    double slab, int n_slabs, double alpha, int half_power,
+                                    double* u, int n_threads);
 /* ObserveNorms (as orc_observe_norms) of a shell state */
 int orc_shell_observe_norms(const OrcShell* s, const double* u, double* out);
 

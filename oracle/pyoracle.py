@@ -103,6 +103,7 @@ def _load(path):
         "orc_evolve_adams": [I, P, I, D, I, P, D, I, P, I],
         "orc_evolve_adams_extents": [I, P, P, D, I, P, D, I, P, I],
         "orc_shell_evolve_adams": [P, I, P, D, I, P, I],
+        "orc_shell_evolve_adams_filtered": [P, I, P, D, I, D, I, P, I],
     }
     for name, args in sig.items():
         fn = getattr(L, name)
@@ -613,12 +614,19 @@ def evolve_adams_extents(bricks, elem_n, u, slab, n_slabs, order, levels=None, g
     return u
 
 
-def shell_evolve_adams(s, u, slab, n_slabs, order, levels=None, threads=0):
-    """AdamsBashforth(order) with local time stepping on the shell."""
+def shell_evolve_adams(s, u, slab, n_slabs, order, levels=None, threads=0, filter=None):
+    """AdamsBashforth(order) with local time stepping on the shell; filter =
+    (alpha, half_power) applies the exponential filter to each element after
+    every one of its steps."""
     u = np.array(u, dtype=np.float64, copy=True)
     lv = None if levels is None else np.ascontiguousarray(levels, dtype=np.int32)
-    _check(lib().orc_shell_evolve_adams(ctypes.addressof(s), order, _p(lv), slab, n_slabs, _p(u),
-                                        threads))
+    if filter is None:
+        _check(lib().orc_shell_evolve_adams(ctypes.addressof(s), order, _p(lv), slab, n_slabs,
+                                            _p(u), threads))
+    else:
+        _check(lib().orc_shell_evolve_adams_filtered(ctypes.addressof(s), order, _p(lv), slab,
+                                                     n_slabs, float(filter[0]), int(filter[1]),
+                                                     _p(u), threads))
     return u
 
 

@@ -1358,8 +1358,10 @@ int adams_step(DgswHandle h, int n_steps, double dt) {
   A.eo = h->eo;
   const int n = h->dom.elem_n[0];
   const int64_t per = (int64_t)kVars * n * n * n;
-  if (h->filter_on)
-    return fail(h, DGSW_ERR_UNSUPPORTED, "the exponential filter is not applied with AdamsBashforth");
+  if (h->filter_on && !h->curved)
+    return fail(h, DGSW_ERR_UNSUPPORTED,
+                "AdamsBashforth applies the exponential filter on the curved shell only (the "
+                "flat 3D scalar-wave executable does not filter)");
   std::vector<AbLaunch> launches;
   std::string err;
   for (int s = 0; s < n_steps; ++s) {
@@ -1432,6 +1434,22 @@ int adams_step(DgswHandle h, int n_steps, double dt) {
       C.gamma2 = h->cfg.gamma2;
       C.L = L;
       DGSW_CUDA(h, launch_csw_ab_update(C, h->stream));
+      if (h->filter_on) {
+        // dg::Actions::Filter after the step of every element that finished
+        // one (the curved executable's step actions end with it), before
+        // its new state is recorded
+        for (int j = 0; j < L.n_jobs; ++j) {
+          const AbLevelJob& J = L.job[j];
+          if (!J.update || J.reset || J.count == 0) continue;
+          FilterLaunch F;
+          F.n = n;
+          F.n_tasks = J.count;
+          F.tasks = h->ab_list + J.begin;
+          F.u = h->state;
+          F.F = h->filt + (size_t)n * kMaxN * kMaxN;
+          DGSW_CUDA(h, launch_filter(F, h->stream));
+        }
+      }
       for (int j = 0; j < L.n_jobs; ++j) {
         const AbLevelJob& J = L.job[j];
         CswLaunch R = base_csw(h);

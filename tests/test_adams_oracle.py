@@ -141,3 +141,35 @@ def test_extents_local_stepping_order(oracle, levels, order):
     errs = [np.abs(oracle.evolve_adams_extents(bricks, elem_n, u0, T / s, s, order,
                                                levels=levels) - ref).max() for s in (8, 16)]
     assert math.log2(errs[0] / errs[1]) > order - 0.5
+
+
+def test_filtered_shell_alpha_zero_is_unfiltered(oracle):
+    # alpha = 0 keeps every Legendre mode (F = I to rounding): the filtered
+    # run of the curved executable's step actions equals the plain one
+    s = oracle.shell(1.9, 20.0, 0, 1, 5, 1.0, 0.0, 1.0)
+    E = oracle.shell_num_elements(s)
+    u0 = oracle.shell_initial_data(s, 8.0, 1.5)
+    levels = np.array([i % 2 for i in range(E)], np.int32)
+    a = oracle.shell_evolve_adams(s, u0, 0.02, 3, 3, levels=levels)
+    b = oracle.shell_evolve_adams(s, u0, 0.02, 3, 3, levels=levels, filter=(0.0, 8))
+    assert np.abs(a - b).max() <= 1e-12 * np.abs(a).max()
+
+
+def test_filtered_shell_damps_the_top_modes(oracle):
+    # the filter after every step removes the top Legendre mode of every
+    # element's state (exp(-36) ~ 2e-16), which the unfiltered run keeps
+    n = 5
+    s = oracle.shell(1.9, 20.0, 0, 1, n, 1.0, 0.0, 1.0)
+    E = oracle.shell_num_elements(s)
+    u0 = oracle.shell_initial_data(s, 8.0, 1.5)
+    a = oracle.shell_evolve_adams(s, u0, 0.02, 3, 3)
+    b = oracle.shell_evolve_adams(s, u0, 0.02, 3, 3, filter=(36.0, 8))
+    Vi = oracle.inv_vandermonde(n)
+
+    def top(u):
+        modal = np.einsum("ai,bj,ck,evkji->evcba", Vi, Vi, Vi, u.reshape(E, 5, n, n, n))
+        return max(np.abs(modal[..., n - 1]).max(), np.abs(modal[..., n - 1, :]).max(),
+                   np.abs(modal[..., n - 1, :, :]).max())
+
+    assert top(b) <= 1e-12 * np.abs(b).max()
+    assert top(a) >= 1e-6 * np.abs(a).max()

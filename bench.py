@@ -516,9 +516,14 @@ def time_curved_adams(shell, n, dt, steps, dev):
     layer = np.arange(E) % 8  # radial segment: the innermost index of a wedge's elements
     levels = np.where(layer < 2, 2, np.where(layer < 5, 1, 0)).astype(np.int32)
     res, states = {}, {}
-    for name, lv, slab, slabs in (("gts", None, dt, steps), ("lts", levels, 4 * dt, steps // 4)):
+    for name, lv, slab, slabs, filt in (("gts", None, dt, steps, False),
+                                        ("lts", levels, 4 * dt, steps // 4, False),
+                                        ("lts_filtered", levels, 4 * dt, steps // 4, True)):
         ev = CurvedDgEvolution(shell, n, gamma2=1.0, device=dev, time_stepper="adams_bashforth",
                                order=3, step_levels=lv)
+        if filt:
+            # the executable's step actions end with the filter on every element
+            ev.set_exponential_filter(36.0, 8)
         ev.set_gaussian_shell(1.0, 8.0, 1.0)
         u0 = ev.get_state()
         ev.step(2, slab)  # start-up and switch
@@ -538,6 +543,7 @@ def time_curved_adams(shell, n, dt, steps, dev):
                      "ms_per_unit_time": ms / (slabs * slab), "slab": slab, "slabs": slabs,
                      "launches_per_slab": 2 * info["launches_per_slab"]}
         ev.close()
+    res["lts_filtered"]["filter"] = "Filters::Exponential alpha=36, half_power=8, after every element step"
     res["lts_speedup_vs_gts"] = res["gts"]["ms_per_unit_time"] / res["lts"]["ms_per_unit_time"]
     a, b = states["gts"], states["lts"]
     res["max_abs_lts_vs_gts"] = float(np.abs(a - b).max())

@@ -377,7 +377,9 @@ int dgsw_autotune(DgswHandle h, int force_variant, int* variant, double* ms_per_
  * u0 + W as a separate stream or in the last stage's epilogue (bit 1)),
  * DGSW_TUNE_MIXED_CURVED (mixed precision on the curved shell: the stage
  * kernel at 256 threads per block with its default or one more resident
- * block per SM, or at 512 threads), or DGSW_TUNE_NONE (fixed
+ * block per SM, or at 512 threads (candidates 0-2), each with the step's
+ * FP64 update in the last stage's epilogue or as a separate stream (3-5)),
+ * or DGSW_TUNE_NONE (fixed
  * configurations).  Re-times every
  * candidate now on the handle's own state (saved and restored), keeps the
  * fastest (force_variant >= 0 imposes one instead) and returns the number of

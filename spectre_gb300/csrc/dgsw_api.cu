@@ -565,7 +565,7 @@ CswMixedLaunch base_csw_mixed(DgswHandle h) {
   L.gamma1 = (float)h->shell.gamma1;
   L.gamma2 = (float)h->cfg.gamma2;
   L.eo = h->eo;
-  L.variant = h->csw_variant;
+  L.variant = h->csw_variant % csw_mixed_shapes();
   return L;
 }
 
@@ -928,8 +928,9 @@ bool pipe_tunable(DgswHandle h) {
 std::map<std::pair<int, int64_t>, int> g_pipe_tuned;
 
 // The mixed curved path: the stage kernel's launch shapes (threads per
-// block, resident blocks asked of the register allocator) timed the same
-// way, cached per (extent, elements).
+// block, resident blocks asked of the register allocator), each with the
+// step's FP64 update in the last stage's epilogue or as a separate stream,
+// timed the same way, cached per (extent, elements).
 bool csw_tunable(DgswHandle h) { return mixed(h) && h->curved && !h->adams; }
 
 std::map<std::pair<int, int64_t>, int> g_csw_tuned;
@@ -949,7 +950,7 @@ int csw_autotune(DgswHandle h, bool force) {
   const int keep = h->csw_variant;
   int best = -1;
   cudaError_t err = time_step_shapes(
-      h, csw_mixed_shapes(),
+      h, 2 * csw_mixed_shapes(),
       [&](int v) {
         h->csw_variant = v;
         return true;
@@ -1034,6 +1035,16 @@ cudaError_t enqueue_mixed_stage(DgswHandle h, int k, double dt, const double* u0
       L.alpha = 2.0 / 3.0;
       L.beta = 2.0 / 3.0;
       L.c = (2.0 / 3.0) * dt;
+      if (out && h->csw_variant >= csw_mixed_shapes()) {
+        // tuning candidates of the second half: W in place into d1 (each
+        // point's d1 is read only by the thread that overwrites it), then
+        // u0 + W as one FP64 stream, so that the stage's epilogue waits on no
+        // FP64 loads
+        L.w32 = h->w1;
+        cudaError_t e = launch_csw_mixed(L, h->stream);
+        if (e != cudaSuccess) return e;
+        return launch_accumulate(out, u0, h->w1, h->dom.offset.back(), h->stream);
+      }
     }
     if (out) {
       L.out64 = out;
@@ -2923,7 +2934,7 @@ int dgsw_tune(DgswHandle h, int force_variant, int* family, int* n_variants, int
     for (int i = 0; i < nv && i < DGSW_TUNE_MAX_VARIANTS; ++i) ms[i] = h->bt_tune_ms[i];
   } else if (csw_tunable(h)) {
     fam = DGSW_TUNE_MIXED_CURVED;
-    nv = csw_mixed_shapes();
+    nv = 2 * csw_mixed_shapes();
     if (force_variant >= nv || force_variant < -1)
       return fail(h, DGSW_ERR_ARGUMENT, "force_variant out of range");
     destroy_graphs(h);

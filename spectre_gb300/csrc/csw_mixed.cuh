@@ -26,6 +26,7 @@
 #include "common.cuh"
 #include "dg_device.cuh"
 #include "launch.hpp"
+#include "pipe.cuh"
 
 namespace dgsw {
 namespace csw_mixed {
@@ -92,6 +93,16 @@ __global__ void __launch_bounds__(kThreads, MINB) csw_stage_mixed_kernel(CswMixe
   const int tid = threadIdx.x;
   const int64_t off = e * (int64_t)(kVars * NP);
   const bool outer = L.nbr[6 * e + 5] == -2;
+  if (tid == 0) {
+    // L2 prefetch of what the element reads after its derivative rounds --
+    // the coefficient rows of the pointwise terms, its face table and the
+    // pointwise inputs -- so that those loads meet L2, not DRAM
+    pipe::prefetch_l2(L.T + (e * (int64_t)kCswT + kTK) * NP,
+                      (size_t)(kCswT - kTK) * NP * sizeof(float));
+    pipe::prefetch_l2(L.F + e * 6 * (int64_t)kCswF * NN, (size_t)6 * kCswF * NN * sizeof(float));
+    if (L.y32) pipe::prefetch_l2(L.y32 + off, (size_t)kVars * NP * sizeof(float));
+    if (L.base64) pipe::prefetch_l2(L.base64 + off, (size_t)kVars * NP * sizeof(double));
+  }
   // state of the element: vector loads when every element block starts on a
   // 16-byte boundary (even N and an aligned base pointer), else scalar loads
   if (COMP) {

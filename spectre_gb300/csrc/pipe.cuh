@@ -38,6 +38,16 @@ __device__ __forceinline__ void bulk_g2s(void* dst, const void* src, uint32_t by
       : "memory");
 }
 
+// L2 prefetch hint of [p, p + bytes): the 16-byte aligned part of the range
+// (the start rounded up, the end down), so nothing outside it is touched
+__device__ __forceinline__ void prefetch_l2(const void* p, size_t bytes) {
+  const uintptr_t a = reinterpret_cast<uintptr_t>(p);
+  const uintptr_t b = (a + 15u) & ~(uintptr_t)15u, end = (a + bytes) & ~(uintptr_t)15u;
+  if (end <= b) return;
+  asm volatile("cp.async.bulk.prefetch.L2.global [%0], %1;" ::"l"(b), "r"((uint32_t)(end - b))
+               : "memory");
+}
+
 __device__ __forceinline__ bool mbar_try_wait(uint64_t* bar, uint32_t parity) {
   uint32_t ok;
   asm volatile(

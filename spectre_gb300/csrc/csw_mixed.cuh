@@ -25,6 +25,7 @@
 
 #include "common.cuh"
 #include "dg_device.cuh"
+#include "eo_packed.cuh"
 #include "launch.hpp"
 #include "pipe.cuh"
 
@@ -35,11 +36,12 @@ template <int N, bool COMP, int kThreads>
 struct CmShape {
   static constexpr int NN = N * N;
   static constexpr int NP = N * N * N;
-  static constexpr int TAB = 2 * dev::Eo<N>::H * dev::Eo<N>::h + dev::Eo<N>::H;
+  static constexpr int TAB = pipe::tab_stride(N);  // packed split of D (eo_packed.cuh)
   static constexpr int PTS = (NP + kThreads - 1) / kThreads;
   // floats: hi state, lo state (COMP), one axis of derivatives, outer-layer
-  // derivatives, hi and lo tables
-  static constexpr int SMEM = 5 * NP + (COMP ? 5 * NP : 0) + 5 * NP + 12 * NN + 2 * TAB;
+  // derivatives, then (at a 16-byte boundary) the hi and lo tables
+  static constexpr int TAB0 = (5 * NP + (COMP ? 5 * NP : 0) + 5 * NP + 12 * NN + 3) / 4 * 4;
+  static constexpr int SMEM = TAB0 + 2 * ((TAB + 3) / 4 * 4);
 };
 
 template <int N>
@@ -87,8 +89,8 @@ __global__ void __launch_bounds__(kThreads, MINB) csw_stage_mixed_kernel(CswMixe
   float* Ul = Uh + 5 * NP;  // COMP only
   float* Ga = Ul + (COMP ? 5 * NP : 0);
   float* Go = Ga + 5 * NP;
-  float* th = Go + 12 * NN;
-  float* tl = th + TAB;
+  float* th = fsm + S::TAB0;
+  float* tl = th + (TAB + 3) / 4 * 4;
   const int64_t e = blockIdx.x;
   const int tid = threadIdx.x;
   const int64_t off = e * (int64_t)(kVars * NP);
@@ -139,15 +141,19 @@ __global__ void __launch_bounds__(kThreads, MINB) csw_stage_mixed_kernel(CswMixe
       for (int q = tid; q < 5 * NP; q += kThreads) Uh[q] = L.x32[off + q];
     }
   }
+  // the unscaled split of D in the packed layout: (A, B) pairs, then for odd
+  // N the middle column and the middle row; hi and lo FP32 parts
   for (int q = tid; q < TAB; q += kThreads) {
-    constexpr int h = dev::Eo<N>::h, H = dev::Eo<N>::H;
+    constexpr int h = N / 2;
     double v;
-    if (q < H * h)
-      v = L.eo.A[q / h][q % h];
-    else if (q < 2 * H * h)
-      v = L.eo.B[(q - H * h) / h][(q - H * h) % h];
-    else
-      v = L.eo.M[q - 2 * H * h];
+    if (q < 2 * h * h) {
+      const int pr = q >> 1, i = pr / h, j = pr - (pr / h) * h;
+      v = (q & 1) ? L.eo.B[i][j] : L.eo.A[i][j];
+    } else if (q < 2 * h * h + h) {
+      v = L.eo.M[q - 2 * h * h];
+    } else {
+      v = L.eo.B[h][q - 2 * h * h - h];
+    }
     const float hv = (float)v;
     th[q] = hv;
     tl[q] = (float)(v - (double)hv);
@@ -190,9 +196,9 @@ __global__ void __launch_bounds__(kThreads, MINB) csw_stage_mixed_kernel(CswMixe
         float ul[N];
 #pragma unroll
         for (int i = 0; i < N; ++i) ul[i] = Ul[v * NP + base + i * stride];
-        dev::eo_line_df<N>(uh, ul, du, th, tl);
+        pipe::eo_line_pdfg<N>(uh, ul, du, th, tl);
       } else {
-        dev::eo_line<N, float, true>(uh, du, th);
+        pipe::eo_line_pg<N>(uh, du, th);
       }
 #pragma unroll
       for (int i = 0; i < N; ++i) Ga[v * NP + base + i * stride] = du[i];

@@ -54,6 +54,7 @@
 #include "dg_device.cuh"
 #include "host_setup.hpp"
 #include "launch.hpp"
+#include "eo_packed.cuh"
 #include "pipe.cuh"
 
 namespace dgsw {
@@ -70,13 +71,6 @@ using dev::widen;
 constexpr uint64_t kLimitNs = 2000000000ull;  // 2 s per bounded wait
 
 // ------------------------------------------------------------ split tables
-// Per direction, the scaled even/odd split of D (h = N/2):
-//   pairs (A_ij, B_ij), i, j < h, as float2 [h*h], then for odd N the
-//   middle-point column M_i (i < h) and the middle row B_hj (j < h).
-__host__ __device__ constexpr int tab_stride(int n) {
-  return 2 * (n / 2) * (n / 2) + ((n & 1) ? 2 * (n / 2) : 0);
-}
-
 // The unscaled split tables of every extent 2..12, one after another (the
 // hi parts, then the lo parts at kTabTotal): held once per CTA in shared
 // memory; the element's -c dxi/dx of each axis scales the contraction's
@@ -87,86 +81,6 @@ __host__ __device__ constexpr int tab_offset(int n) {
   return o;
 }
 constexpr int kTabTotal = tab_offset(kMaxN + 1);
-
-// packed plain contraction (lanes: x = even part P, y = odd part Q)
-template <int N>
-__device__ __forceinline__ void eo_line_pg(const float (&x)[N], float (&out)[N],
-                                           const float* __restrict__ tab) {
-  constexpr int h = N / 2, odd = N & 1;
-  const float2* pr = reinterpret_cast<const float2*>(tab);
-  float2 eo[h];
-#pragma unroll
-  for (int j = 0; j < h; ++j) eo[j] = make_float2(x[j] + x[N - 1 - j], x[j] - x[N - 1 - j]);
-#pragma unroll
-  for (int i = 0; i < h; ++i) {
-    float2 acc = mul2(pr[i * h], eo[0]);
-#pragma unroll
-    for (int j = 1; j < h; ++j) acc = fma2(pr[i * h + j], eo[j], acc);
-    float P = acc.x;
-    if (odd) P = fmaf(tab[2 * h * h + i], x[h], P);
-    out[i] = P + acc.y;
-    out[N - 1 - i] = acc.y - P;
-  }
-  if (odd) {
-    const float* bm = tab + 2 * h * h + h;
-    float Q = bm[0] * eo[0].y;
-#pragma unroll
-    for (int j = 1; j < h; ++j) Q = fmaf(bm[j], eo[j].y, Q);
-    out[h] = Q;
-  }
-}
-
-// packed compensated contraction of a double-float line (hi + lo tables)
-template <int N>
-__device__ __forceinline__ void eo_line_pdfg(const float (&xh)[N], const float (&xl)[N],
-                                             float (&out)[N], const float* __restrict__ th,
-                                             const float* __restrict__ tl) {
-  constexpr int h = N / 2, odd = N & 1;
-  const float2* ph = reinterpret_cast<const float2*>(th);
-  const float2* pl = reinterpret_cast<const float2*>(tl);
-  float2 eoh[h], eol[h];
-#pragma unroll
-  for (int j = 0; j < h; ++j) {
-    float2 s, t;
-    two_sum2(make_float2(xh[j], xh[j]), make_float2(xh[N - 1 - j], -xh[N - 1 - j]), s, t);
-    eoh[j] = s;
-    eol[j] = add2(t, make_float2(xl[j] + xl[N - 1 - j], xl[j] - xl[N - 1 - j]));
-  }
-#pragma unroll
-  for (int i = 0; i < h; ++i) {
-    // s: the running sum of the products' high parts; the corrections are
-    // three independent sums (rounding errors of s and of the products; the
-    // table's low parts; the data's low parts), added at the end
-    float2 s = mul2(ph[i * h], eoh[0]);
-    float2 c1 = fma2(ph[i * h], eoh[0], neg2(s));
-    float2 c2 = mul2(pl[i * h], eoh[0]);
-    float2 c3 = mul2(ph[i * h], eol[0]);
-#pragma unroll
-    for (int j = 1; j < h; ++j) {
-      const float2 a = ph[i * h + j];
-      const float2 p = mul2(a, eoh[j]);
-      const float2 pe = fma2(a, eoh[j], neg2(p));
-      float2 t;
-      two_sum2(s, p, s, t);
-      c1 = add2(c1, add2(t, pe));
-      c2 = fma2(pl[i * h + j], eoh[j], c2);
-      c3 = fma2(a, eol[j], c3);
-    }
-    float2 c = add2(c1, add2(c2, c3));
-    if (odd) dot2_term(th[2 * h * h + i], tl[2 * h * h + i], xh[h], xl[h], s.x, c.x);
-    out[i] = (s.x + s.y) + (c.x + c.y);
-    out[N - 1 - i] = (s.y - s.x) + (c.y - c.x);
-  }
-  if (odd) {
-    const float* bh = th + 2 * h * h + h;
-    const float* bl = tl + 2 * h * h + h;
-    float qs, qc;
-    dot2_first(bh[0], bl[0], eoh[0].y, eol[0].y, qs, qc);
-#pragma unroll
-    for (int j = 1; j < h; ++j) dot2_term(bh[j], bl[j], eoh[j].y, eol[j].y, qs, qc);
-    out[h] = qs + qc;
-  }
-}
 
 // --------------------------------------------------------- buffer layout
 // Bytes of one element's X block, its face block, and their shared-memory

@@ -517,8 +517,8 @@ def time_curved_adams(shell, n, dt, steps, dev):
     levels = np.where(layer < 2, 2, np.where(layer < 5, 1, 0)).astype(np.int32)
     res, states = {}, {}
     for name, lv, slab, slabs, filt in (("gts", None, dt, steps, False),
-                                        ("lts", levels, 4 * dt, steps // 4, False),
-                                        ("lts_filtered", levels, 4 * dt, steps // 4, True)):
+                                        ("lts", levels, 4 * dt, max(1, steps // 4), False),
+                                        ("lts_filtered", levels, 4 * dt, max(1, steps // 4), True)):
         ev = CurvedDgEvolution(shell, n, gamma2=1.0, device=dev, time_stepper="adams_bashforth",
                                order=3, step_levels=lv)
         if filt:
@@ -570,6 +570,8 @@ def time_curved(args, dev, with_cpu):
     for name, prec in (("fp64", PRECISION_FP64), ("mixed", PRECISION_MIXED)):
         ev = CurvedDgEvolution(shell, n, precision=prec, gamma2=1.0, device=dev)
         ev.set_gaussian_shell(1.0, 8.0, 1.0)
+        if prec == PRECISION_MIXED and args.curved_variant >= 0:
+            ev.tune(force_variant=args.curved_variant)
         u0 = ev.get_state()
         # warm-up: graphs captured, then the state reset to t = 0
         ev.step(16, dt)
@@ -916,6 +918,9 @@ def main():
                          "default; one alone only for profiling captures)")
     ap.add_argument("--mixed-variant", type=int, default=-1,
                     help="impose one launch candidate of the uniform mixed path (dgsw_tune) "
+                         "instead of the fastest; for profiling captures")
+    ap.add_argument("--curved-variant", type=int, default=-1,
+                    help="impose one launch candidate of the mixed curved path (dgsw_tune) "
                          "instead of the fastest; for profiling captures")
     ap.add_argument("--elements", type=int, default=ELEMS,
                     help="elements per axis (default 32: the benchmark workload; smaller "

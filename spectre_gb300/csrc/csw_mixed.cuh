@@ -110,17 +110,29 @@ __global__ void __launch_bounds__(kThreads, MINB) csw_stage_mixed_kernel(CswMixe
   if (COMP) {
     if (NP % 2 == 0 && (reinterpret_cast<uintptr_t>(L.x64) & 15u) == 0) {
       const double2* src = reinterpret_cast<const double2*>(L.x64 + off);
-      constexpr int Q = 5 * NP / 2;
-#pragma unroll 4
-      for (int q = tid; q < Q; q += kThreads) {
-        const double2 v = __ldg(src + q);
-        float h0, l0, h1, l1;
-        dev::split_df(v.x, h0, l0);
-        dev::split_df(v.y, h1, l1);
-        Uh[2 * q] = h0;
-        Ul[2 * q] = l0;
-        Uh[2 * q + 1] = h1;
-        Ul[2 * q + 1] = l1;
+      constexpr int Q = 5 * NP / 2, KQ = (Q + kThreads - 1) / kThreads, KB = 8;
+      // batches of KB loads in flight per thread before their splits
+#pragma unroll
+      for (int k0 = 0; k0 < KQ; k0 += KB) {
+        double2 v[KB];
+#pragma unroll
+        for (int k = 0; k < KB; ++k) {
+          const int q = tid + (k0 + k) * kThreads;
+          if (k0 + k < KQ && q < Q) v[k] = __ldg(src + q);
+        }
+#pragma unroll
+        for (int k = 0; k < KB; ++k) {
+          const int q = tid + (k0 + k) * kThreads;
+          if (k0 + k < KQ && q < Q) {
+            float h0, l0, h1, l1;
+            dev::split_df(v[k].x, h0, l0);
+            dev::split_df(v[k].y, h1, l1);
+            Uh[2 * q] = h0;
+            Ul[2 * q] = l0;
+            Uh[2 * q + 1] = h1;
+            Ul[2 * q + 1] = l1;
+          }
+        }
       }
     } else {
       for (int q = tid; q < 5 * NP; q += kThreads) {
@@ -134,9 +146,21 @@ __global__ void __launch_bounds__(kThreads, MINB) csw_stage_mixed_kernel(CswMixe
     if (NP % 4 == 0 && (reinterpret_cast<uintptr_t>(L.x32) & 15u) == 0) {
       const float4* src = reinterpret_cast<const float4*>(L.x32 + off);
       float4* dst = reinterpret_cast<float4*>(Uh);
-      constexpr int Q = 5 * NP / 4;
-#pragma unroll 4
-      for (int q = tid; q < Q; q += kThreads) dst[q] = __ldg(src + q);
+      constexpr int Q = 5 * NP / 4, KQ = (Q + kThreads - 1) / kThreads, KB = 8;
+#pragma unroll
+      for (int k0 = 0; k0 < KQ; k0 += KB) {
+        float4 v[KB];
+#pragma unroll
+        for (int k = 0; k < KB; ++k) {
+          const int q = tid + (k0 + k) * kThreads;
+          if (k0 + k < KQ && q < Q) v[k] = __ldg(src + q);
+        }
+#pragma unroll
+        for (int k = 0; k < KB; ++k) {
+          const int q = tid + (k0 + k) * kThreads;
+          if (k0 + k < KQ && q < Q) dst[q] = v[k];
+        }
+      }
     } else {
       for (int q = tid; q < 5 * NP; q += kThreads) Uh[q] = L.x32[off + q];
     }

@@ -39,8 +39,10 @@ struct CmShape {
   static constexpr int TAB = pipe::tab_stride(N);  // packed split of D (eo_packed.cuh)
   static constexpr int PTS = (NP + kThreads - 1) / kThreads;
   // floats: hi state, lo state (COMP), one axis of derivatives, outer-layer
-  // derivatives, then (at a 16-byte boundary) the hi and lo tables
-  static constexpr int TAB0 = (5 * NP + (COMP ? 5 * NP : 0) + 5 * NP + 12 * NN + 3) / 4 * 4;
+  // derivatives, the internal-face corrections [6][5][N^2], then (at a
+  // 16-byte boundary) the hi and lo tables
+  static constexpr int TAB0 =
+      (5 * NP + (COMP ? 5 * NP : 0) + 5 * NP + 12 * NN + 30 * NN + 3) / 4 * 4;
   static constexpr int SMEM = TAB0 + 2 * ((TAB + 3) / 4 * 4);
 };
 
@@ -89,6 +91,7 @@ __global__ void __launch_bounds__(kThreads, MINB) csw_stage_mixed_kernel(CswMixe
   float* Ul = Uh + 5 * NP;  // COMP only
   float* Ga = Ul + (COMP ? 5 * NP : 0);
   float* Go = Ga + 5 * NP;
+  float* Cf = Go + 12 * NN;
   float* th = fsm + S::TAB0;
   float* tl = th + (TAB + 3) / 4 * 4;
   const int64_t e = blockIdx.x;
@@ -184,6 +187,55 @@ __global__ void __launch_bounds__(kThreads, MINB) csw_stage_mixed_kernel(CswMixe
   }
   const float* T = L.T + e * (int64_t)kCswT * NP;
   const float g1 = L.gamma1, g2 = L.gamma2;
+  __syncthreads();
+
+  // UpwindPenalty corrections of the internal faces, one thread per face
+  // point: they need only the jumps of the state across the face, so their
+  // gathers of the exterior values are issued here, all at once, rather than
+  // point by point after the derivative rounds
+  for (int fp = tid; fp < 6 * NN; fp += kThreads) {
+    const int dir = fp / NN, q = fp - (fp / NN) * NN, d = dir >> 1;
+    const int sl = (dir & 1) ? N - 1 : 0, fa = q % N, fb = q / N;
+    const int p = d == 0 ? sl + N * (fa + N * fb)
+                         : (d == 1 ? fa + N * (sl + N * fb) : fa + N * (fb + N * sl));
+    const int64_t ef = e * 6 + dir;
+    const int32_t x = L.X[ef * NN + q];
+    float corr[5] = {0.0f, 0.0f, 0.0f, 0.0f, 0.0f};
+    if (x >= 0) {
+      const float* f = L.F + ef * kCswF * NN + q;
+      // jumps d = exterior - interior
+      float dv[5];
+#pragma unroll
+      for (int v = 0; v < 5; ++v) {
+        if (COMP) {
+          float eh, el;
+          dev::split_df(L.x64[x + (int64_t)v * NP], eh, el);
+          dv[v] = (eh - Uh[v * NP + p]) + (el - Ul[v * NP + p]);
+        } else {
+          dv[v] = L.x32[x + (int64_t)v * NP] - Uh[v * NP + p];
+        }
+      }
+      float ndp = 0.0f;
+#pragma unroll
+      for (int c = 0; c < 3; ++c) ndp = fmaf(f[(kFv + c) * NN], dv[2 + c], ndp);
+      const float m0 = f[(kFm + 0) * NN], m1 = f[(kFm + 1) * NN];
+      const float m2 = f[(kFm + 2) * NN], m3 = f[(kFm + 3) * NN];
+      const float g2p = g2 * dv[0];
+      const float t1 = m3 * (dv[1] - ndp - g2p);
+      const float t2 = -m2 * (dv[1] + ndp - g2p);
+      const float cpsi = m0 * dv[0];
+      corr[0] = cpsi;
+      corr[1] = fmaf(g2, cpsi, 0.5f * (t1 - t2));
+      const float hh = -0.5f * (t1 + t2);
+#pragma unroll
+      for (int c = 0; c < 3; ++c) {
+        const float nc = f[(kFn + c) * NN];
+        corr[2 + c] = fmaf(hh, nc, m1 * fmaf(-nc, ndp, dv[2 + c]));
+      }
+    }
+#pragma unroll
+    for (int v = 0; v < 5; ++v) Cf[(dir * 5 + v) * NN + q] = corr[v];
+  }
 
   float acc[PTS][5];
 #pragma unroll
@@ -290,40 +342,11 @@ __global__ void __launch_bounds__(kThreads, MINB) csw_stage_mixed_kernel(CswMixe
       if (dir < 0) continue;
       const int q = fq[dir >> 1];
       const int64_t ef = e * 6 + dir;
-      const int32_t x = L.X[ef * NN + q];
-      const float* f = L.F + ef * kCswF * NN + q;
-      if (x >= 0) {
-        // jumps d = exterior - interior
-        float dv[5];
 #pragma unroll
-        for (int v = 0; v < 5; ++v) {
-          if (COMP) {
-            float eh, el;
-            dev::split_df(L.x64[x + (int64_t)v * NP], eh, el);
-            dv[v] = (eh - Uh[v * NP + p]) + (el - Ul[v * NP + p]);
-          } else {
-            dv[v] = L.x32[x + (int64_t)v * NP] - Uh[v * NP + p];
-          }
-        }
-        float ndp = 0.0f;
-#pragma unroll
-        for (int c = 0; c < 3; ++c) ndp = fmaf(f[(kFv + c) * NN], dv[2 + c], ndp);
-        const float m0 = f[(kFm + 0) * NN], m1 = f[(kFm + 1) * NN];
-        const float m2 = f[(kFm + 2) * NN], m3 = f[(kFm + 3) * NN];
-        const float g2p = g2 * dv[0];
-        const float t1 = m3 * (dv[1] - ndp - g2p);
-        const float t2 = -m2 * (dv[1] + ndp - g2p);
-        const float cpsi = m0 * dv[0];
-        corr[0] += cpsi;
-        corr[1] += fmaf(g2, cpsi, 0.5f * (t1 - t2));
-        const float hh = -0.5f * (t1 + t2);
-#pragma unroll
-        for (int c = 0; c < 3; ++c) {
-          const float nc = f[(kFn + c) * NN];
-          corr[2 + c] += fmaf(hh, nc, m1 * fmaf(-nc, ndp, dv[2 + c]));
-        }
-      } else if (x == -2) {
+      for (int v = 0; v < 5; ++v) corr[v] += Cf[(dir * 5 + v) * NN + q];
+      if (dir == 5 && outer) {
         // ConstraintPreservingSphericalRadiation from the volume dt
+        const float* f = L.F + ef * kCswF * NN + q;
         const double* J = L.ij + e * 9 * (int64_t)NP + p;
         float dpsi[3], dphi[3][3];
 #pragma unroll

@@ -224,9 +224,11 @@ struct CswShape {
   static constexpr int NP = N * N * N;
   static constexpr int TAB = 2 * dev::Eo<N>::H * dev::Eo<N>::h + dev::Eo<N>::H;
   static constexpr int PTS = (NP + kThreads - 1) / kThreads;  // points per thread
-  // shared doubles: state, one axis of derivatives, the outer layer's
-  // logical derivatives of Psi and Phi (for the radiation condition), table
-  static constexpr int SMEM = 5 * NP + 5 * NP + 12 * NN + TAB;
+  // shared doubles: state, one axis of derivatives (afterwards the
+  // internal-face corrections [6][5][N^2]), the outer layer's logical
+  // derivatives of Psi and Phi (for the radiation condition), table
+  static constexpr int GA = 5 * NP > 30 * NN ? 5 * NP : 30 * NN;
+  static constexpr int SMEM = 5 * NP + GA + 12 * NN + TAB;
 };
 
 template <int N>
@@ -287,7 +289,7 @@ __global__ void __launch_bounds__(kThreads, CswShape<N>::SMEM * 8 <= 113 * 1024 
   extern __shared__ double smem[];
   double* U = smem;          // 5 * NP: ucur of this element
   double* Ga = U + 5 * NP;   // 5 * NP: d_a of the five fields, one axis at a time
-  double* Go = Ga + 5 * NP;  // 12 * NN: outer layer d_a Psi, d_a Phi_j ([a][4][NN])
+  double* Go = Ga + S::GA;   // 12 * NN: outer layer d_a Psi, d_a Phi_j ([a][4][NN])
   double* tab = Go + 12 * NN;
   const int64_t e = L.list ? (int64_t)L.list[blockIdx.x] : (int64_t)blockIdx.x;
   const int tid = threadIdx.x;
@@ -355,7 +357,36 @@ __global__ void __launch_bounds__(kThreads, CswShape<N>::SMEM * 8 <= 113 * 1024 
       }
     }
   }
-  __syncthreads();  // Go complete
+  __syncthreads();  // Go complete, Ga free
+
+  // UpwindPenalty corrections of the internal faces, one thread per face
+  // point, into Ga ([dir][var][N^2]): every exterior gather of the element
+  // issued together rather than point by point
+  double* Cf = Ga;
+  const bool internal = kBoundary && L.internal;
+  if (internal) {
+    for (int fp = tid; fp < 6 * NN; fp += kThreads) {
+      const int dir = fp / NN, q = fp - (fp / NN) * NN, d = dir >> 1;
+      const int sl = (dir & 1) ? N - 1 : 0, fa = q % N, fb = q / N;
+      const int p = d == 0 ? sl + N * (fa + N * fb)
+                           : (d == 1 ? fa + N * (sl + N * fb) : fa + N * (fb + N * sl));
+      const int64_t ef = e * 6 + dir;
+      const int32_t x = L.X[ef * NN + q];
+      double c[5] = {0.0, 0.0, 0.0, 0.0, 0.0};
+      if (x >= 0) {
+        double ui[5], ue[5];
+#pragma unroll
+        for (int v = 0; v < 5; ++v) {
+          ui[v] = U[v * NP + p];
+          ue[v] = L.ucur[x + (int64_t)v * NP];
+        }
+        upwind_face<double>(ui, ue, L.F + ef * kCswF * NN + q, NN, g2, c);
+      }
+#pragma unroll
+      for (int v = 0; v < 5; ++v) Cf[(dir * 5 + v) * NN + q] = c[v];
+    }
+    __syncthreads();
+  }
 
 #pragma unroll
   for (int r = 0; r < PTS; ++r) {
@@ -381,7 +412,6 @@ __global__ void __launch_bounds__(kThreads, CswShape<N>::SMEM * 8 <= 113 * 1024 
     if (kBoundary) {
       const int i = p % N, j = (p / N) % N, k = p / NN;
       double corr[5] = {0.0, 0.0, 0.0, 0.0, 0.0};
-      const double ui[5] = {psi, pi, phi[0], phi[1], phi[2]};
       const int dirs[6] = {i == 0 ? 0 : -1, i == N - 1 ? 1 : -1, j == 0 ? 2 : -1,
                            j == N - 1 ? 3 : -1, k == 0 ? 4 : -1, k == N - 1 ? 5 : -1};
       const int fq[3] = {j + N * k, i + N * k, i + N * j};
@@ -391,15 +421,12 @@ __global__ void __launch_bounds__(kThreads, CswShape<N>::SMEM * 8 <= 113 * 1024 
         if (dir < 0) continue;
         const int q = fq[dir >> 1];
         const int64_t ef = e * 6 + dir;
-        const int32_t x = L.X[ef * NN + q];
         const double* f = L.F + ef * kCswF * NN + q;
-        if (x >= 0) {
-          if (!L.internal) continue;
-          double ue[5];
+        if (internal) {
 #pragma unroll
-          for (int v = 0; v < 5; ++v) ue[v] = L.ucur[x + (int64_t)v * NP];
-          upwind_face<double>(ui, ue, f, NN, g2, corr);
-        } else if (x == -2) {
+          for (int v = 0; v < 5; ++v) corr[v] += Cf[(dir * 5 + v) * NN + q];
+        }
+        if (dir == 5 && outer) {
           // ConstraintPreservingSphericalRadiation::dg_time_derivative from
           // the volume dt (only zeta-upper faces lie on the outer sphere)
           const double* J = L.ij + e * 9 * (int64_t)NP + p;
@@ -489,7 +516,7 @@ __global__ void __launch_bounds__(kThreads) csw_ab_update_kernel(const __grid_co
     }
     g -= A.L.job[q].count;
   }
-  if (j < 0) return;  // no barrier in this kernel
+  if (j < 0) return;  // uniform over the block, before its one barrier
   const AbLevelJob& J = A.L.job[j];
   const int64_t e = A.list[J.begin + g];
   const int64_t per = (int64_t)kVars * NP, E = A.n_elem;
@@ -497,6 +524,39 @@ __global__ void __launch_bounds__(kThreads) csw_ab_update_kernel(const __grid_co
   const bool update = J.update && !J.reset;
   if (!update && !J.reset) return;
   const double* src = J.reset ? A.u0 : A.u;
+  // the boundary delta of every internal face point first, one thread per
+  // face point, into shared memory ([dir][var][N^2]): the record gathers of
+  // the whole element issued together
+  __shared__ double Cf[6 * 5 * NN];
+  if (update) {
+    for (int fp = threadIdx.x; fp < 6 * NN; fp += kThreads) {
+      const int dir = fp / NN, q = fp - (fp / NN) * NN, d = dir >> 1;
+      const int sl = (dir & 1) ? N - 1 : 0, fa = q % N, fb = q / N;
+      const int p = d == 0 ? sl + N * (fa + N * fb)
+                           : (d == 1 ? fa + N * (sl + N * fb) : fa + N * (fb + N * sl));
+      const int64_t ef = e * 6 + dir;
+      const int32_t x = A.X[ef * NN + q];
+      double corr[5] = {0.0, 0.0, 0.0, 0.0, 0.0};
+      if (x >= 0) {  // external faces: their condition is in the time derivative
+        const AbFaceTable& f = J.face[A.level[x / per]];
+        double ui[5] = {0.0, 0.0, 0.0, 0.0, 0.0}, ue[5] = {0.0, 0.0, 0.0, 0.0, 0.0};
+        for (int i = 0; i < f.n_loc; ++i) {
+          const double* Ul = A.U + ((int64_t)f.loc_slot[i] * E + e) * per + p;
+#pragma unroll
+          for (int v = 0; v < 5; ++v) ui[v] = fma(f.loc_c[i], Ul[v * NP], ui[v]);
+        }
+        for (int i = 0; i < f.n_rem; ++i) {
+          const double* Ur = A.U + (int64_t)f.rem_slot[i] * E * per + x;
+#pragma unroll
+          for (int v = 0; v < 5; ++v) ue[v] = fma(f.rem_c[i], Ur[v * NP], ue[v]);
+        }
+        upwind_face<double>(ui, ue, A.Fc + ef * kCswF * NN + q, NN, A.gamma2, corr);
+      }
+#pragma unroll
+      for (int v = 0; v < 5; ++v) Cf[(dir * 5 + v) * NN + q] = corr[v];
+    }
+    __syncthreads();  // update is uniform over the block
+  }
   for (int p = threadIdx.x; p < NP; p += kThreads) {
     double val[5];
 #pragma unroll
@@ -517,22 +577,8 @@ __global__ void __launch_bounds__(kThreads) csw_ab_update_kernel(const __grid_co
         const int dir = dirs[s6];
         if (dir < 0) continue;
         const int q = fq[dir >> 1];
-        const int64_t ef = e * 6 + dir;
-        const int32_t x = A.X[ef * NN + q];
-        if (x < 0) continue;  // external: its condition is in the time derivative
-        const AbFaceTable& f = J.face[A.level[x / per]];
-        double ui[5] = {0.0, 0.0, 0.0, 0.0, 0.0}, ue[5] = {0.0, 0.0, 0.0, 0.0, 0.0};
-        for (int i = 0; i < f.n_loc; ++i) {
-          const double* Ul = A.U + ((int64_t)f.loc_slot[i] * E + e) * per + p;
 #pragma unroll
-          for (int v = 0; v < 5; ++v) ui[v] = fma(f.loc_c[i], Ul[v * NP], ui[v]);
-        }
-        for (int i = 0; i < f.n_rem; ++i) {
-          const double* Ur = A.U + (int64_t)f.rem_slot[i] * E * per + x;
-#pragma unroll
-          for (int v = 0; v < 5; ++v) ue[v] = fma(f.rem_c[i], Ur[v * NP], ue[v]);
-        }
-        upwind_face<double>(ui, ue, A.Fc + ef * kCswF * NN + q, NN, A.gamma2, corr);
+        for (int v = 0; v < 5; ++v) corr[v] += Cf[(dir * 5 + v) * NN + q];
       }
 #pragma unroll
       for (int v = 0; v < 5; ++v) val[v] += corr[v];

@@ -690,6 +690,89 @@ AB3_FP64_INST_PER_POINT = (156.672e6 + 76.8e6 + 30.048e6) / 4096000
 AB3_TRAFFIC_PER_POINT = (814.1e6 + 415.1e6) / 4096000
 
 
+def time_next_rows(args, dev):
+    """The rows built around the path, each timed once at the 32^3 x 8^3 size
+    (or the refined lattice below) with CUDA events on the handle's stream:
+    Gauss-point quadrature, an h-refined lattice with 2:1 faces, ObserveNorms,
+    the exponential filter on the flat path, and the AMR p-projection of every
+    element.  Achieved GB/s are algorithmic bytes / time."""
+    import torch
+    from spectre_gb300 import Brick, DgEvolution
+    from spectre_gb300.dgsw import RefinedBrick, amr_project
+    E = args.elements
+    params = np.array([[1.0, 0.5, math.pi, math.pi, math.pi]])
+    res = {}
+
+    def timed(ev, fn, reps):
+        stream = torch.cuda.ExternalStream(ev.stream_ptr(), device=dev)
+        fn()
+        torch.cuda.synchronize()
+        e0 = torch.cuda.Event(enable_timing=True)
+        e1 = torch.cuda.Event(enable_timing=True)
+        e0.record(stream)
+        for _ in range(reps):
+            fn()
+        e1.record(stream)
+        e1.synchronize()
+        return e0.elapsed_time(e1) / reps
+
+    steps = 20
+    with DgEvolution([Brick((E, E, E))], N_PTS, device=dev) as ev:
+        ev.set_initial_data("gaussian", params)
+        ms_gll = timed(ev, lambda: ev.step(steps, DT, sync=False), 1) / steps
+        pts = ev.grid_points
+        ev.set_exponential_filter(36.0, 8)
+        ms_f = timed(ev, lambda: ev.step(steps, DT, sync=False), 1) / steps
+        ev.set_exponential_filter(36.0, 8, enable=False)
+        # ObserveNorms of the state: one reduction launch pair and the
+        # 27-value result copied to the host
+        ms_norms = timed(ev, lambda: ev.observe_norms(), 10)
+        # AMR p-projection of every element 8 -> 9 (ProjectVariables)
+        st = torch.from_numpy(ev.get_state()).to("cuda:%d" % dev)
+        ne = ev.n_elements
+        src = np.arange(ne, dtype=np.int32)
+        se = np.full((ne, 3), N_PTS, np.int32)
+        de = np.full((ne, 3), N_PTS + 1, np.int32)
+        ch = np.zeros((ne, 3), np.int8)
+        ino = np.arange(ne, dtype=np.int64) * 5 * N_PTS ** 3
+        ms_amr = timed(ev, lambda: amr_project(ev, 5, st, ino, src, se, de, ch), 3)
+        amr_bytes = ne * 5 * (N_PTS ** 3 + (N_PTS + 1) ** 3) * 8
+    filt_app = (ms_f - ms_gll) / 3
+    res["gll_fp64_ms_per_step"] = ms_gll
+    res["exponential_filter"] = {
+        "ms_per_application": filt_app,
+        "achieved_gbs": 80.0 * pts / (filt_app * 1e-3) / 1e9 if filt_app > 0 else None,
+        "note": "Filters::Exponential alpha=36 half_power=8 after every substep on the FP64 "
+                "path; cost = (filtered step - plain step) / 3; 80 B per point algorithmic"}
+    res["observe_norms"] = {
+        "ms_per_call": ms_norms,
+        "achieved_gbs": 40.0 * pts / (ms_norms * 1e-3) / 1e9,
+        "note": "Max, Min, L2Norm, L2IntegralNorm, VolumeIntegral of the five variables, "
+                "result on the host; 40 B per point read"}
+    res["amr_p_projection"] = {
+        "ms": ms_amr, "achieved_gbs": amr_bytes / (ms_amr * 1e-3) / 1e9,
+        "note": "amr::projectors::ProjectVariables p-refinement 8 -> 9 of every element "
+                "(read 8^3, write 9^3 values x 5 variables)"}
+    with DgEvolution([Brick((E, E, E))], N_PTS, device=dev, quadrature="gauss") as ev:
+        ev.set_initial_data("gaussian", params)
+        ms_g = timed(ev, lambda: ev.step(steps, DT, sync=False), 1) / steps
+        res["gauss_quadrature"] = {
+            "value": ev.grid_points * 3 / (ms_g * 1e-3), "unit": UNIT, "ms_per_step": ms_g,
+            "vs_gll": ms_gll / ms_g,
+            "workload": "%d^3 elements x %d^3 Legendre-Gauss points, FP64, SSP-RK3" % (E, N_PTS)}
+    # 4 x 4 x 4 blocks, checkerboard levels 2 / 3 (every face 2:1)
+    lv = [2 + ((i + j + k) % 2) for k in range(4) for j in range(4) for i in range(4)]
+    with DgEvolution(RefinedBrick((4, 4, 4), lv), N_PTS, device=dev) as ev:
+        ev.set_initial_data("gaussian", params)
+        ms_r = timed(ev, lambda: ev.step(steps, DT, sync=False), 1) / steps
+        res["h_refined"] = {
+            "value": ev.grid_points * 3 / (ms_r * 1e-3), "unit": UNIT, "ms_per_step": ms_r,
+            "elements": ev.n_elements,
+            "workload": "4^3 blocks, levels 2/3 in a checkerboard (2:1 mortars on every block "
+                        "face), %d^3 LGL points, FP64, SSP-RK3" % N_PTS}
+    return res
+
+
 def time_adams(args, dev):
     """AdamsBashforth(3) on the 32^3-element mesh (8^3 points,
     Gaussian pulse, slab = step = 2e-4): global stepping, and local time
@@ -846,6 +929,9 @@ def run_ours(args):
     curved = None
     if not args.no_curved:
         curved = time_curved(args, dev, rank == 0 and not args.no_cpu_baseline)
+    next_rows = None
+    if not args.no_next_rows:
+        next_rows = time_next_rows(args, dev)
 
     cpu = None
     if rank == 0 and not args.no_cpu_baseline:
@@ -879,7 +965,7 @@ def run_ours(args):
                                   "DFMA/DADD throughput probe on this pool's GB300"},
             "autotune": autotune,
             "mixed": mixed, "batched": batched, "adjoint": adjoint, "curved": curved,
-            "adams": adams,
+            "adams": adams, "next_rows": next_rows,
             "cpu_baseline": cpu, "e2e": e2e, "clocks": clocks,
             "gpu_launches": 3 * args.steps,
             "gpu_launches_note": "stage kernels of the timed FP64 region (one launch per stage)",
@@ -902,6 +988,8 @@ def main():
     ap.add_argument("--no-adjoint", action="store_true")
     ap.add_argument("--no-curved", action="store_true")
     ap.add_argument("--no-adams", action="store_true")
+    ap.add_argument("--no-next-rows", action="store_true",
+                    help="skip the Gauss / h-refined / ObserveNorms / filter / AMR timings")
     ap.add_argument("--curved-steps", type=int, default=0,
                     help="SSP-RK3 steps of the curved shell run (default 1000)")
     ap.add_argument("--curved-only", action="store_true",

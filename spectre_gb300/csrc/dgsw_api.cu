@@ -2586,11 +2586,14 @@ int dgsw_set_initial_data(DgswHandle h, int kind, const double* params, double t
   }
   if (kind != 0 && kind != 1) return fail(h, DGSW_ERR_ARGUMENT, "unknown initial data kind");
   if (int rc = select_device(h)) return rc;
-  const size_t count = kind == 0 ? 3 : 5 * (size_t)h->dom.bricks.size();
+  // one Gaussian per instance; a refined lattice is one instance (its
+  // elements' instance index is 0) and keeps no brick list
+  const size_t n_inst = h->dom.bricks.empty() ? 1 : h->dom.bricks.size();
+  const size_t count = kind == 0 ? 3 : 5 * n_inst;
   for (size_t i = 0; i < count; ++i)
     if (!std::isfinite(params[i])) return fail(h, DGSW_ERR_ARGUMENT, "non-finite parameter");
   if (kind == 1)
-    for (size_t i = 0; i < h->dom.bricks.size(); ++i)
+    for (size_t i = 0; i < n_inst; ++i)
       if (!(params[5 * i + 1] > 0.0)) return fail(h, DGSW_ERR_ARGUMENT, "width must be positive");
   if (count > h->params_cap) {
     DGSW_CUDA(h, cudaStreamSynchronize(h->stream));

@@ -93,3 +93,23 @@ def test_gpu_refined_plane_wave_converges():
             errs.append(ev.observe_plane_wave_errors([1.0, 1.0, 1.0], 50 * 5e-4)
                         ["L2Norm(Error(Psi))"])
     assert errs[0] > 10 * errs[1] > 100 * errs[2], errs
+
+
+@pytest.mark.gpu
+def test_gpu_refined_gaussian_initial_data(oracle):
+    # a refined lattice is one instance: one (A, width, centre) row sets the
+    # Gaussian pulse on every element (evaluated at the oracle's coordinates)
+    blocks, levels = LATTICES[0]
+    n = 5
+    r = oracle.refined(blocks, levels)
+    xyz = r.coords(n)
+    A, w, c = 1.3, 0.8, np.array([1.0, 2.0, 3.0])
+    dx = xyz - c[None, :, None]
+    psi = A * np.exp(-(dx ** 2).sum(axis=1) / (w * w))
+    want = np.zeros((xyz.shape[0], 5, n ** 3))
+    want[:, 0] = psi
+    for d in range(3):
+        want[:, 2 + d] = -2.0 * dx[:, d] / (w * w) * psi
+    with DgEvolution(RefinedBrick(blocks, levels), n) as ev:
+        ev.set_initial_data("gaussian", np.array([[A, w, *c]]))
+        np.testing.assert_allclose(ev.get_state(), want.ravel(), rtol=0, atol=1e-13)

@@ -2826,7 +2826,8 @@ static int observe_norms(DgswHandle h, const double* dev_u, const double* dev_su
       }
     }
     DGSW_CUDA(h, upload(&h->lgl_w, w));
-    DGSW_CUDA(h, cudaMalloc(&h->norm_partial, ((size_t)E * 26 + 32) * sizeof(double)));
+    DGSW_CUDA(h, cudaMalloc(&h->norm_partial,
+                            ((size_t)(E + kNormsBlocks) * 26 + 32) * sizeof(double)));
   }
   NormsLaunch L;
   L.n_elem = E;
@@ -2841,7 +2842,7 @@ static int observe_norms(DgswHandle h, const double* dev_u, const double* dev_su
   L.u = dev_u ? dev_u : h->state;
   L.subtract = dev_sub;
   L.partial = h->norm_partial;
-  L.result = h->norm_partial + (size_t)E * 26;
+  L.result = h->norm_partial + (size_t)(E + kNormsBlocks) * 26;
   DGSW_CUDA(h, launch_norms(L, h->stream));
   double r[26];
   DGSW_CUDA(h, cudaMemcpyAsync(r, L.result, sizeof(r), cudaMemcpyDeviceToHost, h->stream));

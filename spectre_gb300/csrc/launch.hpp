@@ -521,9 +521,10 @@ struct NormsLaunch {
   const double* lgl_w = nullptr;    // [kMaxN + 1][kMaxN] LGL weights
   const double* u = nullptr;
   const double* subtract = nullptr;
-  double* partial = nullptr;        // n_elem x 26
+  double* partial = nullptr;        // 26 x n_elem, then 26 x kNormsBlocks scratch
   double* result = nullptr;         // 26
 };
+constexpr int kNormsBlocks = 256;  // blocks of the second reduction level
 cudaError_t launch_norms(const NormsLaunch& L, cudaStream_t s);
 
 // UpwindPenalty pointwise kernels (face_kernels.cu).

@@ -511,16 +511,20 @@ def time_curved_adams(shell, n, dt, steps, dev):
     logarithmic radial map makes the inner layers smallest: layers 0-1 step
     dt, 2-4 2 dt, 5-7 4 dt).  Both cover the same simulated time."""
     import torch
-    from spectre_gb300.dgsw import CurvedDgEvolution
+    from spectre_gb300.dgsw import CurvedDgEvolution, PRECISION_FP64, PRECISION_MIXED
     E = 768
     layer = np.arange(E) % 8  # radial segment: the innermost index of a wedge's elements
     levels = np.where(layer < 2, 2, np.where(layer < 5, 1, 0)).astype(np.int32)
     res, states = {}, {}
-    for name, lv, slab, slabs, filt in (("gts", None, dt, steps, False),
-                                        ("lts", levels, 4 * dt, max(1, steps // 4), False),
-                                        ("lts_filtered", levels, 4 * dt, max(1, steps // 4), True)):
-        ev = CurvedDgEvolution(shell, n, gamma2=1.0, device=dev, time_stepper="adams_bashforth",
-                               order=3, step_levels=lv)
+    nl = max(1, steps // 4)
+    for name, lv, slab, slabs, filt, prec in (
+            ("gts", None, dt, steps, False, PRECISION_FP64),
+            ("lts", levels, 4 * dt, nl, False, PRECISION_FP64),
+            ("lts_filtered", levels, 4 * dt, nl, True, PRECISION_FP64),
+            ("gts_mixed", None, dt, steps, False, PRECISION_MIXED),
+            ("lts_filtered_mixed", levels, 4 * dt, nl, True, PRECISION_MIXED)):
+        ev = CurvedDgEvolution(shell, n, precision=prec, gamma2=1.0, device=dev,
+                               time_stepper="adams_bashforth", order=3, step_levels=lv)
         if filt:
             # the executable's step actions end with the filter on every element
             ev.set_exponential_filter(36.0, 8)
@@ -545,6 +549,10 @@ def time_curved_adams(shell, n, dt, steps, dev):
         ev.close()
     res["lts_filtered"]["filter"] = "Filters::Exponential alpha=36, half_power=8, after every element step"
     res["lts_speedup_vs_gts"] = res["gts"]["ms_per_unit_time"] / res["lts"]["ms_per_unit_time"]
+    for m, f in (("gts_mixed", "gts"), ("lts_filtered_mixed", "lts_filtered")):
+        res[m]["speedup_vs_fp64"] = res[f]["ms_per_unit_time"] / res[m]["ms_per_unit_time"]
+        res[m]["rel_l2_vs_fp64"] = float(np.linalg.norm(states[m] - states[f]) /
+                                         np.linalg.norm(states[f]))
     a, b = states["gts"], states["lts"]
     res["max_abs_lts_vs_gts"] = float(np.abs(a - b).max())
     res["note"] = ("AdamsBashforth(3); value counts each element's own steps; the start-up "

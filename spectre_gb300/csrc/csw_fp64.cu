@@ -563,9 +563,14 @@ __global__ void __launch_bounds__(kThreads) csw_ab_update_kernel(const __grid_co
     for (int v = 0; v < 5; ++v) val[v] = src[off + v * NP + p];
     if (update) {
       for (int i = 0; i < J.n_vol; ++i) {
-        const double* Fi = A.F + ((int64_t)J.vol_slot[i] * E + e) * per + p;
+        const int64_t fo = ((int64_t)J.vol_slot[i] * E + e) * per + p;
+        if (A.F32) {
 #pragma unroll
-        for (int v = 0; v < 5; ++v) val[v] = fma(J.vol_c[i], Fi[v * NP], val[v]);
+          for (int v = 0; v < 5; ++v) val[v] = fma(J.vol_c[i], (double)A.F32[fo + v * NP], val[v]);
+        } else {
+#pragma unroll
+          for (int v = 0; v < 5; ++v) val[v] = fma(J.vol_c[i], A.F[fo + v * NP], val[v]);
+        }
       }
       const int i0 = p % N, j0 = (p / N) % N, k0 = p / NN;
       const int dirs[6] = {i0 == 0 ? 0 : -1, i0 == N - 1 ? 1 : -1, j0 == 0 ? 2 : -1,

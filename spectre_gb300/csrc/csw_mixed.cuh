@@ -94,9 +94,13 @@ __global__ void __launch_bounds__(kThreads, MINB) csw_stage_mixed_kernel(CswMixe
   float* Cf = Go + 12 * NN;
   float* th = fsm + S::TAB0;
   float* tl = th + (TAB + 3) / 4 * 4;
-  const int64_t e = blockIdx.x;
+  const int64_t e = L.list ? (int64_t)L.list[blockIdx.x] : (int64_t)blockIdx.x;
   const int tid = threadIdx.x;
   const int64_t off = e * (int64_t)(kVars * NP);
+  if (L.ucopy && COMP) {
+    // AdamsBashforth record: the element's FP64 state as it is
+    for (int q = tid; q < kVars * NP; q += kThreads) L.ucopy[off + q] = L.x64[off + q];
+  }
   const bool outer = L.nbr[6 * e + 5] == -2;
   if (tid == 0) {
     // L2 prefetch of what the element reads after its derivative rounds --
@@ -193,7 +197,7 @@ __global__ void __launch_bounds__(kThreads, MINB) csw_stage_mixed_kernel(CswMixe
   // point: they need only the jumps of the state across the face, so their
   // gathers of the exterior values are issued here, all at once, rather than
   // point by point after the derivative rounds
-  for (int fp = tid; fp < 6 * NN; fp += kThreads) {
+  for (int fp = tid; fp < (L.internal ? 6 * NN : 0); fp += kThreads) {
     const int dir = fp / NN, q = fp - (fp / NN) * NN, d = dir >> 1;
     const int sl = (dir & 1) ? N - 1 : 0, fa = q % N, fb = q / N;
     const int p = d == 0 ? sl + N * (fa + N * fb)
@@ -342,8 +346,10 @@ __global__ void __launch_bounds__(kThreads, MINB) csw_stage_mixed_kernel(CswMixe
       if (dir < 0) continue;
       const int q = fq[dir >> 1];
       const int64_t ef = e * 6 + dir;
+      if (L.internal) {
 #pragma unroll
-      for (int v = 0; v < 5; ++v) corr[v] += Cf[(dir * 5 + v) * NN + q];
+        for (int v = 0; v < 5; ++v) corr[v] += Cf[(dir * 5 + v) * NN + q];
+      }
       if (dir == 5 && outer) {
         // ConstraintPreservingSphericalRadiation from the volume dt
         const float* f = L.F + ef * kCswF * NN + q;
@@ -425,8 +431,9 @@ cudaError_t launch_shape_n(const CswMixedLaunch& L, cudaStream_t s) {
   err = cudaFuncSetAttribute(k, cudaFuncAttributePreferredSharedMemoryCarveout,
                              cudaSharedmemCarveoutMaxShared);
   if (err != cudaSuccess) return err;
-  if (L.n_elem <= 0) return cudaSuccess;
-  k<<<(unsigned)L.n_elem, T, smem, s>>>(L);
+  const int64_t blocks = L.list ? L.list_count : L.n_elem;
+  if (blocks <= 0) return cudaSuccess;
+  k<<<(unsigned)blocks, T, smem, s>>>(L);
   return cudaGetLastError();
 }
 

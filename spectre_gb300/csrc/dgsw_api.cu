@@ -154,6 +154,7 @@ struct DgswHandle_ {
   int32_t* ab_list = nullptr;   // element ids sorted by step level
   int8_t* ab_level = nullptr;   // step level per element
   double* ab_F = nullptr;       // ring of volume time derivatives
+  float* ab_F32 = nullptr;      // the same in FP32 (mixed precision on the shell)
   double* ab_B = nullptr;       // ring of face data
   int64_t ab_points[kAbMaxLevels] = {};  // grid points of each level's elements
   // elements of differing extents: the level list is sorted by (level,
@@ -1284,9 +1285,10 @@ cudaError_t capture_steps(DgswHandle h, double dt, int steps, cudaGraphExec_t* o
 // AdamsBashforth handle set-up: step levels, the level-sorted element list,
 // the schedule (whose dry run sizes the history rings) and the rings.
 int adams_init(DgswHandle h, const DgswConfig& cfg) {
-  if (h->refined || h->gauss || mixed(h) || (!h->dom.uniform && h->curved))
+  if (h->refined || h->gauss || (mixed(h) && !h->curved) || (!h->dom.uniform && h->curved))
     return fail(h, DGSW_ERR_UNSUPPORTED,
-                "AdamsBashforth: Gauss-Lobatto, conforming elements (of any extents on bricks), FP64");
+                "AdamsBashforth: Gauss-Lobatto, conforming elements (of any extents on bricks), FP64 "
+                "(mixed precision on the shell)");
   const int64_t E = h->dom.n_elem;
   std::vector<int8_t> level(E, 0);
   for (int64_t e = 0; e < E; ++e) {
@@ -1324,8 +1326,13 @@ int adams_init(DgswHandle h, const DgswConfig& cfg) {
   h->ab_level_host = level;
   const int n = h->dom.elem_n[0];
   const size_t slots = (size_t)h->ab.ring_slots();
-  if ((e = cudaMalloc(&h->ab_F, slots * h->dom.offset.back() * sizeof(double))) != cudaSuccess)
+  if (mixed(h)) {
+    if ((e = cudaMalloc(&h->ab_F32, slots * h->dom.offset.back() * sizeof(float))) != cudaSuccess)
+      return cuda_fail(h, e, "cudaMalloc time-derivative ring");
+  } else if ((e = cudaMalloc(&h->ab_F, slots * h->dom.offset.back() * sizeof(double))) !=
+             cudaSuccess) {
     return cuda_fail(h, e, "cudaMalloc time-derivative ring");
+  }
   // the shell records the whole state (its exterior points are reached
   // through the face offsets of the volume layout); bricks record the face w's
   // (12 n^2 per element: 6 faces x (own w, the neighbour's w))
@@ -1435,6 +1442,7 @@ int adams_step(DgswHandle h, int n_steps, double dt) {
       C.u = h->state;
       C.u0 = h->t1;
       C.F = h->ab_F;
+      C.F32 = h->ab_F32;
       C.U = h->ab_B;
       C.Fc = h->c_F;
       C.X = h->c_X;
@@ -1452,6 +1460,18 @@ int adams_step(DgswHandle h, int n_steps, double dt) {
         for (int j = 0; j < L.n_jobs; ++j) {
           const AbLevelJob& J = L.job[j];
           if (!J.update || J.reset || J.count == 0) continue;
+          if (mixed(h)) {
+            // u + (F - I) u with the residual in double-float FP32
+            MixedFilterLaunch R;
+            R.n = n;
+            R.n_tasks = J.count;
+            R.tasks = h->ab_list + J.begin;
+            R.F = h->filt + (size_t)n * kMaxN * kMaxN;
+            R.u64 = h->state;
+            R.out64 = h->state;
+            DGSW_CUDA(h, launch_filter_residual(R, h->stream));
+            continue;
+          }
           FilterLaunch F;
           F.n = n;
           F.n_tasks = J.count;
@@ -1463,6 +1483,21 @@ int adams_step(DgswHandle h, int n_steps, double dt) {
       }
       for (int j = 0; j < L.n_jobs; ++j) {
         const AbLevelJob& J = L.job[j];
+        if (mixed(h)) {
+          // the record in mixed precision: dt u = L(u) by the compensated
+          // double-float stage (FP32 result), the state copied as it is
+          CswMixedLaunch M = base_csw_mixed(h);
+          M.x64 = h->state;
+          M.alpha = 0.0;
+          M.c = 1.0;
+          M.w32 = h->ab_F32 + (int64_t)J.rec_slot * h->dom.n_elem * per;
+          M.ucopy = h->ab_B + (int64_t)J.rec_slot * h->dom.n_elem * per;
+          M.internal = 0;
+          M.list = h->ab_list + J.begin;
+          M.list_count = J.count;
+          DGSW_CUDA(h, launch_csw_mixed(M, h->stream));
+          continue;
+        }
         CswLaunch R = base_csw(h);
         R.ucur = h->state;
         R.unext = h->ab_F + (int64_t)J.rec_slot * h->dom.n_elem * per;
@@ -2254,9 +2289,10 @@ int dgsw_create(const DgswConfig* cfg, DgswHandle* out) {
     int code = DGSW_OK;
     const char* why = nullptr;
     if (h->refined || h->gauss || (!h->dom.uniform && h->curved) ||
-        cfg->precision != DGSW_PRECISION_FP64) {
+        (cfg->precision != DGSW_PRECISION_FP64 && !h->curved)) {
       code = DGSW_ERR_UNSUPPORTED;
-      why = "AdamsBashforth: Gauss-Lobatto, conforming elements (of any extents on bricks), FP64";
+      why = "AdamsBashforth: Gauss-Lobatto, conforming elements (of any extents on bricks), FP64 "
+            "(mixed precision on the shell)";
     } else if (cfg->stepper_order < 0 || cfg->stepper_order > kAbMaxOrder) {
       code = DGSW_ERR_ARGUMENT;
       why = "AdamsBashforth order must be in [1, 8] (0: 3)";
@@ -2491,6 +2527,7 @@ int dgsw_destroy(DgswHandle h) {
   if (h->ab_level) cudaFree(h->ab_level);
   if (h->ab_F) cudaFree(h->ab_F);
   if (h->ab_B) cudaFree(h->ab_B);
+  if (h->ab_F32) cudaFree(h->ab_F32);
   if (h->ab_boff) cudaFree(h->ab_boff);
   for (int n = 0; n <= kMaxN; ++n) {
     if (h->class_tasks[n]) cudaFree(h->class_tasks[n]);

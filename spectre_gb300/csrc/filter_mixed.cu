@@ -76,12 +76,17 @@ __global__ void __launch_bounds__(filt::line_threads<N>())
     }
     __syncthreads();
   }
-  // R = (F u) - u, rounded once
+  // R = (F u) - u, rounded once; with out64 the filtered state u + R itself
   for (int q = tid; q < NP; q += T) {
     float uh, ul, s, t;
-    split_df(u[q], uh, ul);
+    const double uq = u[q];
+    split_df(uq, uh, ul);
     two_sum(Sh[q], -uh, s, t);
-    L.r32[off + q] = s + (t + (Sl[q] - ul));
+    const float r = s + (t + (Sl[q] - ul));
+    if (L.out64)
+      L.out64[off + q] = uq + widen(r);
+    else
+      L.r32[off + q] = r;
   }
 }
 
@@ -159,7 +164,7 @@ cudaError_t launch_any(const MixedFilterLaunch& L, bool residual, cudaStream_t s
 }  // namespace
 
 cudaError_t launch_filter_residual(const MixedFilterLaunch& L, cudaStream_t s) {
-  if (!L.u64 || !L.r32 || !L.F) return cudaErrorInvalidValue;
+  if (!L.u64 || (!L.r32 && !L.out64) || !L.F) return cudaErrorInvalidValue;
   return launch_any(L, true, s);
 }
 

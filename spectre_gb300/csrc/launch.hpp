@@ -396,6 +396,7 @@ struct CswAbArgs {
   double* u = nullptr;
   const double* u0 = nullptr;
   const double* F = nullptr;  // ring slots x elements x 5 N^3 time derivatives
+  const float* F32 = nullptr; // the same in FP32 (mixed precision; F null)
   const double* U = nullptr;  // ring slots x elements x 5 N^3 recorded states
   const double* Fc = nullptr; // face table (kCswF per face point)
   const int32_t* X = nullptr; // exterior point offsets
@@ -430,6 +431,12 @@ struct CswMixedLaunch {
   float gamma1 = 0.0f, gamma2 = 0.0f;
   EoTable eo{};
   int variant = 0;  // launch shape (csw_mixed.cuh), < csw_mixed_shapes()
+  // AdamsBashforth records: only the listed elements (list non-null), no
+  // internal mortar terms (internal = 0), and the FP64 x64 copied to ucopy
+  const int32_t* list = nullptr;
+  int64_t list_count = 0;
+  int internal = 1;
+  double* ucopy = nullptr;
 };
 cudaError_t launch_csw_mixed(const CswMixedLaunch& L, cudaStream_t s);
 int csw_mixed_shapes();
@@ -485,7 +492,8 @@ struct FilterLaunch {
 cudaError_t launch_filter(const FilterLaunch& L, cudaStream_t s);
 
 // The exponential filter on the mixed-precision path (filter_mixed.cu).
-// residual: r32 = (F - I) u64, compensated; combine: out = ar r32 + ad d32 +
+// residual: r32 = (F - I) u64, compensated (or, with out64, out64 = u64 +
+// that residual: the filtered state); combine: out = ar r32 + ad d32 +
 // b F(x32 + y32), to w32 and / or out64 = base64 + out.  tasks / offset null:
 // elements 0..n_tasks-1 of extent n, packed; else the listed elements at
 // their value offsets.  F: the n x n filter matrix (FP64, row-major).

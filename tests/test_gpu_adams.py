@@ -282,3 +282,34 @@ def test_flat_adams_refuses_the_filter(oracle):
         ev.set_initial_data("plane_wave", [1.0, 1.0, 1.0])
         with pytest.raises(DgswError):
             ev.step(1, 0.01)
+
+
+def rel_l2(a, b):
+    return float(np.linalg.norm((a - b).ravel()) / np.linalg.norm(b.ravel()))
+
+
+@pytest.mark.parametrize("order,L,filt", [(1, 0, False), (3, 0, False), (2, 1, False),
+                                          (3, 2, False), (3, 2, True)])
+def test_curved_shell_mixed_adams_close_to_fp64(oracle, order, L, filt):
+    # AdamsBashforth with local time stepping in mixed precision: each record
+    # dt u = L(u) by the compensated double-float stage (FP32 result), the
+    # FP64 state and the FP64 state records for the face coupling; against
+    # the FP64 run of the same schedule (filtered or not) over 40 slabs
+    from spectre_gb300.dgsw import CurvedDgEvolution, Shell, PRECISION_FP64, PRECISION_MIXED
+    n = 6
+    s = oracle.shell(1.9, 20.0, 1, 1, n, 1.0, 0.0, 1.0)
+    E = oracle.shell_num_elements(s)
+    u0 = oracle.shell_initial_data(s, 8.0, 1.5).ravel()
+    levels = pattern(E, L, seed=order + 11) if L else None
+    out = {}
+    for prec in (PRECISION_FP64, PRECISION_MIXED):
+        with CurvedDgEvolution(Shell(1.9, 20.0, 1, 1), n, precision=prec, gamma2=1.0,
+                               time_stepper="adams_bashforth", order=order,
+                               step_levels=levels) as ev:
+            if filt:
+                ev.set_exponential_filter(36.0, 8)
+            ev.set_state(u0)
+            ev.step(40, 0.02)
+            out[prec] = ev.get_state()
+    assert np.isfinite(out[PRECISION_MIXED]).all()
+    assert rel_l2(out[PRECISION_MIXED], out[PRECISION_FP64]) <= 1e-6

@@ -309,6 +309,18 @@ __global__ void __launch_bounds__(kThreads, CswShape<N>::SMEM * 8 <= 113 * 1024 
   }
   const double* T = L.T + e * (int64_t)kCswT * NP;
   const double g1 = L.gamma1, g2 = L.gamma2;
+  if (L.frec) {
+    // AdamsBashforth record: the element's face values, [6][5][N^2]
+    __syncthreads();  // U staged
+    for (int fp = tid; fp < 6 * NN; fp += kThreads) {
+      const int dir = fp / NN, q = fp - (fp / NN) * NN, d = dir >> 1;
+      const int sl = (dir & 1) ? N - 1 : 0, fa = q % N, fb = q / N;
+      const int p = d == 0 ? sl + N * (fa + N * fb)
+                           : (d == 1 ? fa + N * (sl + N * fb) : fa + N * (fb + N * sl));
+#pragma unroll
+      for (int v = 0; v < 5; ++v) L.frec[e * 30 * NN + (dir * 5 + v) * NN + q] = U[v * NP + p];
+    }
+  }
 
   double acc[PTS][5];
 #pragma unroll
@@ -492,7 +504,6 @@ __global__ void __launch_bounds__(kThreads, CswShape<N>::SMEM * 8 <= 113 * 1024 
       double o = fma(L.b, uc, L.c * dt[v]);
       if (L.a != 0.0) o = fma(L.a, L.u0[off + v * NP + p], o);
       L.unext[off + v * NP + p] = o;
-      if (L.ucopy) L.ucopy[off + v * NP + p] = uc;
     }
   }
 }
@@ -502,8 +513,9 @@ __global__ void __launch_bounds__(kThreads, CswShape<N>::SMEM * 8 <= 113 * 1024 
 // face point the curved UpwindPenalty of the marginal-weighted records.
 // The correction is linear in the exterior-minus-interior jump with static
 // weights (csw_face_kernel), so sum_{l,r} c_lr C(L_l, R_r) =
-// C(sum_l a_l L_l, sum_r b_r R_r).  The exterior record point is the
-// neighbour's offset X of the face point in the same ring slot layout.
+// C(sum_l a_l L_l, sum_r b_r R_r).  The records hold each element's face
+// values ([6][5][N^2]); the exterior record point is the offset X of the
+// neighbour's matching face point in the same ring slot.
 template <int N>
 __global__ void __launch_bounds__(kThreads) csw_ab_update_kernel(const __grid_constant__ CswAbArgs A) {
   constexpr int NN = N * N, NP = NN * N;
@@ -530,25 +542,23 @@ __global__ void __launch_bounds__(kThreads) csw_ab_update_kernel(const __grid_co
   __shared__ double Cf[6 * 5 * NN];
   if (update) {
     for (int fp = threadIdx.x; fp < 6 * NN; fp += kThreads) {
-      const int dir = fp / NN, q = fp - (fp / NN) * NN, d = dir >> 1;
-      const int sl = (dir & 1) ? N - 1 : 0, fa = q % N, fb = q / N;
-      const int p = d == 0 ? sl + N * (fa + N * fb)
-                           : (d == 1 ? fa + N * (sl + N * fb) : fa + N * (fb + N * sl));
+      const int dir = fp / NN, q = fp - (fp / NN) * NN;
       const int64_t ef = e * 6 + dir;
       const int32_t x = A.X[ef * NN + q];
       double corr[5] = {0.0, 0.0, 0.0, 0.0, 0.0};
       if (x >= 0) {  // external faces: their condition is in the time derivative
-        const AbFaceTable& f = J.face[A.level[x / per]];
+        const int64_t rs = E * 30 * (int64_t)NN;  // one ring slot of face records
+        const AbFaceTable& f = J.face[A.level[x / (30 * NN)]];
         double ui[5] = {0.0, 0.0, 0.0, 0.0, 0.0}, ue[5] = {0.0, 0.0, 0.0, 0.0, 0.0};
         for (int i = 0; i < f.n_loc; ++i) {
-          const double* Ul = A.U + ((int64_t)f.loc_slot[i] * E + e) * per + p;
+          const double* Ul = A.U + (int64_t)f.loc_slot[i] * rs + e * 30 * NN + dir * 5 * NN + q;
 #pragma unroll
-          for (int v = 0; v < 5; ++v) ui[v] = fma(f.loc_c[i], Ul[v * NP], ui[v]);
+          for (int v = 0; v < 5; ++v) ui[v] = fma(f.loc_c[i], Ul[v * NN], ui[v]);
         }
         for (int i = 0; i < f.n_rem; ++i) {
-          const double* Ur = A.U + (int64_t)f.rem_slot[i] * E * per + x;
+          const double* Ur = A.U + (int64_t)f.rem_slot[i] * rs + x;
 #pragma unroll
-          for (int v = 0; v < 5; ++v) ue[v] = fma(f.rem_c[i], Ur[v * NP], ue[v]);
+          for (int v = 0; v < 5; ++v) ue[v] = fma(f.rem_c[i], Ur[v * NN], ue[v]);
         }
         upwind_face<double>(ui, ue, A.Fc + ef * kCswF * NN + q, NN, A.gamma2, corr);
       }
@@ -557,21 +567,38 @@ __global__ void __launch_bounds__(kThreads) csw_ab_update_kernel(const __grid_co
     }
     __syncthreads();  // update is uniform over the block
   }
-  for (int p = threadIdx.x; p < NP; p += kThreads) {
-    double val[5];
+  // every point of this thread at once: the state loads, then each
+  // record's loads, issued together (the stores alias the state)
+  constexpr int PTS = (NP + kThreads - 1) / kThreads;
+  double val[PTS][5];
 #pragma unroll
-    for (int v = 0; v < 5; ++v) val[v] = src[off + v * NP + p];
-    if (update) {
-      for (int i = 0; i < J.n_vol; ++i) {
-        const int64_t fo = ((int64_t)J.vol_slot[i] * E + e) * per + p;
+  for (int r = 0; r < PTS; ++r) {
+    const int p = threadIdx.x + r * kThreads;
+    if (p < NP)
+#pragma unroll
+      for (int v = 0; v < 5; ++v) val[r][v] = src[off + v * NP + p];
+  }
+  if (update) {
+    for (int i = 0; i < J.n_vol; ++i) {
+      const double c = J.vol_c[i];
+      const int64_t fo = ((int64_t)J.vol_slot[i] * E + e) * per;
+#pragma unroll
+      for (int r = 0; r < PTS; ++r) {
+        const int p = threadIdx.x + r * kThreads;
+        if (p >= NP) continue;
         if (A.F32) {
 #pragma unroll
-          for (int v = 0; v < 5; ++v) val[v] = fma(J.vol_c[i], (double)A.F32[fo + v * NP], val[v]);
+          for (int v = 0; v < 5; ++v) val[r][v] = fma(c, (double)A.F32[fo + v * NP + p], val[r][v]);
         } else {
 #pragma unroll
-          for (int v = 0; v < 5; ++v) val[v] = fma(J.vol_c[i], A.F[fo + v * NP], val[v]);
+          for (int v = 0; v < 5; ++v) val[r][v] = fma(c, A.F[fo + v * NP + p], val[r][v]);
         }
       }
+    }
+#pragma unroll
+    for (int r = 0; r < PTS; ++r) {
+      const int p = threadIdx.x + r * kThreads;
+      if (p >= NP) continue;
       const int i0 = p % N, j0 = (p / N) % N, k0 = p / NN;
       const int dirs[6] = {i0 == 0 ? 0 : -1, i0 == N - 1 ? 1 : -1, j0 == 0 ? 2 : -1,
                            j0 == N - 1 ? 3 : -1, k0 == 0 ? 4 : -1, k0 == N - 1 ? 5 : -1};
@@ -586,10 +613,15 @@ __global__ void __launch_bounds__(kThreads) csw_ab_update_kernel(const __grid_co
         for (int v = 0; v < 5; ++v) corr[v] += Cf[(dir * 5 + v) * NN + q];
       }
 #pragma unroll
-      for (int v = 0; v < 5; ++v) val[v] += corr[v];
+      for (int v = 0; v < 5; ++v) val[r][v] += corr[v];
     }
+  }
 #pragma unroll
-    for (int v = 0; v < 5; ++v) A.u[off + v * NP + p] = val[v];
+  for (int r = 0; r < PTS; ++r) {
+    const int p = threadIdx.x + r * kThreads;
+    if (p < NP)
+#pragma unroll
+      for (int v = 0; v < 5; ++v) A.u[off + v * NP + p] = val[r][v];
   }
 }
 

@@ -97,9 +97,17 @@ __global__ void __launch_bounds__(kThreads, MINB) csw_stage_mixed_kernel(CswMixe
   const int64_t e = L.list ? (int64_t)L.list[blockIdx.x] : (int64_t)blockIdx.x;
   const int tid = threadIdx.x;
   const int64_t off = e * (int64_t)(kVars * NP);
-  if (L.ucopy && COMP) {
-    // AdamsBashforth record: the element's FP64 state as it is
-    for (int q = tid; q < kVars * NP; q += kThreads) L.ucopy[off + q] = L.x64[off + q];
+  if (L.frec && COMP) {
+    // AdamsBashforth record: the element's FP64 face values as they are
+    for (int fp = tid; fp < 6 * NN; fp += kThreads) {
+      const int dir = fp / NN, q = fp - (fp / NN) * NN, d = dir >> 1;
+      const int sl = (dir & 1) ? N - 1 : 0, fa = q % N, fb = q / N;
+      const int p = d == 0 ? sl + N * (fa + N * fb)
+                           : (d == 1 ? fa + N * (sl + N * fb) : fa + N * (fb + N * sl));
+#pragma unroll
+      for (int v = 0; v < 5; ++v)
+        L.frec[e * 30 * NN + (dir * 5 + v) * NN + q] = L.x64[off + (int64_t)v * NP + p];
+    }
   }
   const bool outer = L.nbr[6 * e + 5] == -2;
   if (tid == 0) {

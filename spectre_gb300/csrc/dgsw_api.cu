@@ -128,6 +128,7 @@ struct DgswHandle_ {
   float* c_T32 = nullptr;
   float* c_F32 = nullptr;
   int32_t* c_X = nullptr;
+  int32_t* c_Xf = nullptr;  // per face point: the exterior point in the face records
   // launch autotuner: the FP64 stage's launch-configuration variant
   bool tuned = false;
   int stage_variant = 0;
@@ -596,6 +597,26 @@ std::vector<int32_t> shell_face_offsets(const Domain& dom, const ShellGeometry& 
   return X;
 }
 
+// The same exterior points in the AdamsBashforth face records ([6][5][N^2]
+// values per element): (nb 6 + nd) 5 N^2 + the neighbour's face point.
+std::vector<int32_t> shell_face_record_offsets(const Domain& dom, const ShellGeometry& geo) {
+  const int n = geo.n, nn = n * n;
+  std::vector<int32_t> X(6 * (size_t)nn * dom.n_elem);
+  for (int64_t e = 0; e < dom.n_elem; ++e)
+    for (int dir = 0; dir < 6; ++dir) {
+      const int32_t nb = dom.neighbor[6 * e + dir];
+      int32_t* out = &X[(6 * e + dir) * (size_t)nn];
+      if (nb < 0) {
+        for (int q = 0; q < nn; ++q) out[q] = nb;
+        continue;
+      }
+      const int nd = geo.back_dir[6 * e + dir];
+      for (int q = 0; q < nn; ++q)
+        out[q] = (int32_t)(((int64_t)nb * 6 + nd) * 5 * nn + geo.face_perm[(6 * e + dir) * (size_t)nn + q]);
+    }
+  return X;
+}
+
 // Uploads the shell geometry and forms the background, the operator tables
 // and the face geometry on the device (FP64).  Fails if a characteristic
 // speed on the inner (excision) sphere is incoming.
@@ -609,6 +630,10 @@ int csw_init(DgswHandle h, const ShellGeometry& geo) {
     return cuda_fail(h, e, "upload inverse Jacobian");
   if ((e = upload(&h->c_X, shell_face_offsets(h->dom, geo))) != cudaSuccess)
     return cuda_fail(h, e, "upload face offsets");
+  if (E * 30 * nn >= ((int64_t)1 << 31))
+    return fail(h, DGSW_ERR_ARGUMENT, "shell too large for 32-bit face record offsets");
+  if ((e = upload(&h->c_Xf, shell_face_record_offsets(h->dom, geo))) != cudaSuccess)
+    return cuda_fail(h, e, "upload face record offsets");
   DGSW_CUDA(h, cudaMalloc(&h->c_T, (size_t)E * kCswT * np * sizeof(double)));
   DGSW_CUDA(h, cudaMalloc(&h->c_F, (size_t)E * 6 * kCswF * nn * sizeof(double)));
   if (mixed(h)) {
@@ -1337,7 +1362,7 @@ int adams_init(DgswHandle h, const DgswConfig& cfg) {
   // through the face offsets of the volume layout); bricks record the face w's
   // (12 n^2 per element: 6 faces x (own w, the neighbour's w))
   if (h->curved) {
-    h->ab_total_b = E * (int64_t)kVars * n * n * n;
+    h->ab_total_b = E * 30 * (int64_t)n * n;  // face records, [6][5][N^2] per element
   } else {
     std::vector<int64_t> boff(E + 1, 0);
     for (int64_t el = 0; el < E; ++el)
@@ -1445,7 +1470,7 @@ int adams_step(DgswHandle h, int n_steps, double dt) {
       C.F32 = h->ab_F32;
       C.U = h->ab_B;
       C.Fc = h->c_F;
-      C.X = h->c_X;
+      C.X = h->c_Xf;
       C.list = h->ab_list;
       C.level = h->ab_level;
       C.n = n;
@@ -1491,7 +1516,7 @@ int adams_step(DgswHandle h, int n_steps, double dt) {
           M.alpha = 0.0;
           M.c = 1.0;
           M.w32 = h->ab_F32 + (int64_t)J.rec_slot * h->dom.n_elem * per;
-          M.ucopy = h->ab_B + (int64_t)J.rec_slot * h->dom.n_elem * per;
+          M.frec = h->ab_B + (int64_t)J.rec_slot * h->ab_total_b;
           M.internal = 0;
           M.list = h->ab_list + J.begin;
           M.list_count = J.count;
@@ -1501,7 +1526,7 @@ int adams_step(DgswHandle h, int n_steps, double dt) {
         CswLaunch R = base_csw(h);
         R.ucur = h->state;
         R.unext = h->ab_F + (int64_t)J.rec_slot * h->dom.n_elem * per;
-        R.ucopy = h->ab_B + (int64_t)J.rec_slot * h->dom.n_elem * per;
+        R.frec = h->ab_B + (int64_t)J.rec_slot * h->ab_total_b;
         R.a = 0.0;
         R.b = 0.0;
         R.c = 1.0;
@@ -2505,6 +2530,7 @@ int dgsw_destroy(DgswHandle h) {
   if (h->c_T32) cudaFree(h->c_T32);
   if (h->c_F32) cudaFree(h->c_F32);
   if (h->c_X) cudaFree(h->c_X);
+  if (h->c_Xf) cudaFree(h->c_Xf);
   if (h->filt) cudaFree(h->filt);
   if (h->fr32) cudaFree(h->fr32);
   if (h->fw3) cudaFree(h->fw3);

@@ -381,11 +381,12 @@ struct CswLaunch {
   double gamma1 = 0.0, gamma2 = 0.0;
   EoTable eo{};
   // AdamsBashforth records: only the listed elements (list non-null), no
-  // internal mortar terms (internal = 0), and a copy of ucur written to ucopy
+  // internal mortar terms (internal = 0), and ucur's face values written to
+  // frec ([6][5][N^2] per element at e * 30 N^2)
   const int32_t* list = nullptr;
   int64_t list_count = 0;
   int internal = 1;
-  double* ucopy = nullptr;
+  double* frec = nullptr;
 };
 cudaError_t launch_csw_fp64(const CswLaunch& L, cudaStream_t s);
 
@@ -397,9 +398,10 @@ struct CswAbArgs {
   const double* u0 = nullptr;
   const double* F = nullptr;  // ring slots x elements x 5 N^3 time derivatives
   const float* F32 = nullptr; // the same in FP32 (mixed precision; F null)
-  const double* U = nullptr;  // ring slots x elements x 5 N^3 recorded states
+  const double* U = nullptr;  // ring slots x elements x [6][5][N^2] recorded face values
   const double* Fc = nullptr; // face table (kCswF per face point)
-  const int32_t* X = nullptr; // exterior point offsets
+  const int32_t* X = nullptr; // per face point: the exterior point's offset in a
+                              // slot of U ((nb 6 + nd) 5 N^2 + point), < 0 external
   const int32_t* list = nullptr;
   const int8_t* level = nullptr;
   int n = 0;
@@ -432,11 +434,12 @@ struct CswMixedLaunch {
   EoTable eo{};
   int variant = 0;  // launch shape (csw_mixed.cuh), < csw_mixed_shapes()
   // AdamsBashforth records: only the listed elements (list non-null), no
-  // internal mortar terms (internal = 0), and the FP64 x64 copied to ucopy
+  // internal mortar terms (internal = 0), and the FP64 x64's face values
+  // written to frec ([6][5][N^2] per element at e * 30 N^2)
   const int32_t* list = nullptr;
   int64_t list_count = 0;
   int internal = 1;
-  double* ucopy = nullptr;
+  double* frec = nullptr;
 };
 cudaError_t launch_csw_mixed(const CswMixedLaunch& L, cudaStream_t s);
 int csw_mixed_shapes();

@@ -235,11 +235,13 @@ int dgsw_substep(DgswHandle h, int k, double dt);
 int dgsw_step_host(DgswHandle h, double* host_u, int n_steps, double dt);
 
 /* ---- TimeStepper (AdamsBashforth, local time stepping) -------------------
- * Handles with time_stepper DGSW_STEPPER_ADAMS_BASHFORTH: Gauss-Lobatto,
- * FP64; the flat system on conforming bricks of one extent or of
+ * Handles with time_stepper DGSW_STEPPER_ADAMS_BASHFORTH: Gauss-Lobatto;
+ * the flat system (FP64) on conforming bricks of one extent or of
  * per-element extents (p-nonconforming faces coupled on the mortar at the
  * larger extent for every pair of records, ApplyBoundaryCorrections.hpp:
- * 816-937), or the curved shell of one extent.  dgsw_step
+ * 816-937), or the curved shell of one extent in FP64 or mixed precision
+ * (each record dt u in compensated FP32 arithmetic, FP64 state), with the
+ * exponential filter after each element step when it is set.  dgsw_step
  * advances n_steps slabs of duration dt (the same dt on every call); within a
  * slab an element of step level l takes 2^l steps, and the UpwindPenalty
  * coupling across faces between levels is integrated by

@@ -560,7 +560,18 @@ __global__ void __launch_bounds__(kThreads) csw_ab_update_kernel(const __grid_co
 #pragma unroll
           for (int v = 0; v < 5; ++v) ue[v] = fma(f.rem_c[i], Ur[v * NN], ue[v]);
         }
-        upwind_face<double>(ui, ue, A.Fc + ef * kCswF * NN + q, NN, A.gamma2, corr);
+        if (A.Fc32) {
+          // mixed precision: the jumps rounded to FP32 once, the correction
+          // in FP32 with the FP32 face table
+          float z[5] = {0.0f, 0.0f, 0.0f, 0.0f, 0.0f}, dv[5], c32[5] = {0.0f, 0.0f, 0.0f, 0.0f, 0.0f};
+#pragma unroll
+          for (int v = 0; v < 5; ++v) dv[v] = (float)(ue[v] - ui[v]);
+          upwind_face<float>(z, dv, A.Fc32 + ef * kCswF * NN + q, NN, (float)A.gamma2, c32);
+#pragma unroll
+          for (int v = 0; v < 5; ++v) corr[v] = c32[v];
+        } else {
+          upwind_face<double>(ui, ue, A.Fc + ef * kCswF * NN + q, NN, A.gamma2, corr);
+        }
       }
 #pragma unroll
       for (int v = 0; v < 5; ++v) Cf[(dir * 5 + v) * NN + q] = corr[v];
@@ -579,31 +590,14 @@ __global__ void __launch_bounds__(kThreads) csw_ab_update_kernel(const __grid_co
       for (int v = 0; v < 5; ++v) val[r][v] = src[off + v * NP + p];
   }
   if (update) {
-    for (int i = 0; i < J.n_vol; ++i) {
-      const double c = J.vol_c[i];
-      const int64_t fo = ((int64_t)J.vol_slot[i] * E + e) * per;
-#pragma unroll
-      for (int r = 0; r < PTS; ++r) {
-        const int p = threadIdx.x + r * kThreads;
-        if (p >= NP) continue;
-        if (A.F32) {
-#pragma unroll
-          for (int v = 0; v < 5; ++v) val[r][v] = fma(c, (double)A.F32[fo + v * NP + p], val[r][v]);
-        } else {
-#pragma unroll
-          for (int v = 0; v < 5; ++v) val[r][v] = fma(c, A.F[fo + v * NP + p], val[r][v]);
-        }
-      }
-    }
-#pragma unroll
-    for (int r = 0; r < PTS; ++r) {
-      const int p = threadIdx.x + r * kThreads;
-      if (p >= NP) continue;
+    // the 0-3 face corrections of point p, summed in a fixed order
+    auto face_sum = [&](int p, double (&corr)[5]) {
       const int i0 = p % N, j0 = (p / N) % N, k0 = p / NN;
       const int dirs[6] = {i0 == 0 ? 0 : -1, i0 == N - 1 ? 1 : -1, j0 == 0 ? 2 : -1,
                            j0 == N - 1 ? 3 : -1, k0 == 0 ? 4 : -1, k0 == N - 1 ? 5 : -1};
       const int fq[3] = {j0 + N * k0, i0 + N * k0, i0 + N * j0};
-      double corr[5] = {0.0, 0.0, 0.0, 0.0, 0.0};
+#pragma unroll
+      for (int v = 0; v < 5; ++v) corr[v] = 0.0;
 #pragma unroll
       for (int s6 = 0; s6 < 6; ++s6) {
         const int dir = dirs[s6];
@@ -612,8 +606,57 @@ __global__ void __launch_bounds__(kThreads) csw_ab_update_kernel(const __grid_co
 #pragma unroll
         for (int v = 0; v < 5; ++v) corr[v] += Cf[(dir * 5 + v) * NN + q];
       }
+    };
+    if (A.F32) {
+      // mixed precision: the increment sum_j c_j F_j and the face
+      // corrections in FP32 (the records' own precision), added to the FP64
+      // state once
+      float inc[PTS][5];
 #pragma unroll
-      for (int v = 0; v < 5; ++v) val[r][v] += corr[v];
+      for (int r = 0; r < PTS; ++r)
+#pragma unroll
+        for (int v = 0; v < 5; ++v) inc[r][v] = 0.0f;
+      for (int i = 0; i < J.n_vol; ++i) {
+        const float c = (float)J.vol_c[i];
+        const int64_t fo = ((int64_t)J.vol_slot[i] * E + e) * per;
+#pragma unroll
+        for (int r = 0; r < PTS; ++r) {
+          const int p = threadIdx.x + r * kThreads;
+          if (p >= NP) continue;
+#pragma unroll
+          for (int v = 0; v < 5; ++v) inc[r][v] = fmaf(c, A.F32[fo + v * NP + p], inc[r][v]);
+        }
+      }
+#pragma unroll
+      for (int r = 0; r < PTS; ++r) {
+        const int p = threadIdx.x + r * kThreads;
+        if (p >= NP) continue;
+        double corr[5];
+        face_sum(p, corr);  // FP32 values: their sums below are FP32 sums
+#pragma unroll
+        for (int v = 0; v < 5; ++v) val[r][v] += dev::widen(inc[r][v] + (float)corr[v]);
+      }
+    } else {
+      for (int i = 0; i < J.n_vol; ++i) {
+        const double c = J.vol_c[i];
+        const int64_t fo = ((int64_t)J.vol_slot[i] * E + e) * per;
+#pragma unroll
+        for (int r = 0; r < PTS; ++r) {
+          const int p = threadIdx.x + r * kThreads;
+          if (p >= NP) continue;
+#pragma unroll
+          for (int v = 0; v < 5; ++v) val[r][v] = fma(c, A.F[fo + v * NP + p], val[r][v]);
+        }
+      }
+#pragma unroll
+      for (int r = 0; r < PTS; ++r) {
+        const int p = threadIdx.x + r * kThreads;
+        if (p >= NP) continue;
+        double corr[5];
+        face_sum(p, corr);
+#pragma unroll
+        for (int v = 0; v < 5; ++v) val[r][v] += corr[v];
+      }
     }
   }
 #pragma unroll

@@ -1468,6 +1468,7 @@ int adams_step(DgswHandle h, int n_steps, double dt) {
       C.u0 = h->t1;
       C.F = h->ab_F;
       C.F32 = h->ab_F32;
+      C.Fc32 = mixed(h) ? h->c_F32 : nullptr;
       C.U = h->ab_B;
       C.Fc = h->c_F;
       C.X = h->c_Xf;

@@ -400,6 +400,7 @@ struct CswAbArgs {
   const float* F32 = nullptr; // the same in FP32 (mixed precision; F null)
   const double* U = nullptr;  // ring slots x elements x [6][5][N^2] recorded face values
   const double* Fc = nullptr; // face table (kCswF per face point)
+  const float* Fc32 = nullptr; // its FP32 copy (mixed precision: FP32 face corrections)
   const int32_t* X = nullptr; // per face point: the exterior point's offset in a
                               // slot of U ((nb 6 + nd) 5 N^2 + point), < 0 external
   const int32_t* list = nullptr;

@@ -64,6 +64,54 @@ struct Lay {
   static constexpr uint32_t kBBytes = HAS_B ? 5 * S::NP * 8 : 0;
 };
 
+// A contiguous row of N floats (an x line; N even, the row 8-byte aligned,
+// 16-byte aligned when N % 4 == 0) moved with the widest vector accesses:
+// neighbouring threads' x lines are N floats apart, so scalar accesses
+// would conflict on the shared-memory banks N-fold.
+template <int N, typename P>
+__device__ __forceinline__ void load_row(const P* p, float (&x)[N]) {
+  if constexpr (N % 4 == 0) {
+#pragma unroll
+    for (int k = 0; k < N / 4; ++k) {
+      const float4 v = reinterpret_cast<const float4*>(p)[k];
+      x[4 * k] = v.x;
+      x[4 * k + 1] = v.y;
+      x[4 * k + 2] = v.z;
+      x[4 * k + 3] = v.w;
+    }
+  } else {
+#pragma unroll
+    for (int k = 0; k < N / 2; ++k) {
+      const float2 v = reinterpret_cast<const float2*>(p)[k];
+      x[2 * k] = v.x;
+      x[2 * k + 1] = v.y;
+    }
+  }
+}
+template <int N, typename P>
+__device__ __forceinline__ void store_row(P* p, const float (&x)[N]) {
+  if constexpr (N % 4 == 0) {
+#pragma unroll
+    for (int k = 0; k < N / 4; ++k)
+      reinterpret_cast<float4*>(p)[k] = make_float4(x[4 * k], x[4 * k + 1], x[4 * k + 2], x[4 * k + 3]);
+  } else {
+#pragma unroll
+    for (int k = 0; k < N / 2; ++k) reinterpret_cast<float2*>(p)[k] = make_float2(x[2 * k], x[2 * k + 1]);
+  }
+}
+// a contiguous row of N (hi, lo) pairs, two pairs per 16-byte access
+template <int N>
+__device__ __forceinline__ void load_row2(const float2* p, float (&h)[N], float (&l)[N]) {
+#pragma unroll
+  for (int k = 0; k < N / 2; ++k) {
+    const float4 v = reinterpret_cast<const float4*>(p)[k];
+    h[2 * k] = v.x;
+    l[2 * k] = v.y;
+    h[2 * k + 1] = v.z;
+    l[2 * k + 1] = v.w;
+  }
+}
+
 // packed even/odd contraction, plain FP32 (lanes: x = even part P, y = odd Q)
 template <int N>
 __device__ __forceinline__ void eo_line_p(const float (&x)[N], float (&out)[N],
@@ -299,13 +347,18 @@ __global__ void __launch_bounds__(N * N * EPB, MINB)
         float pil[N], fl[N];
         if (COMP) {
           // X holds Pi, Phi_x, Phi_y, Phi_z as (hi, lo) FP32 pairs
+          if (d == 0) {
+            load_row2<N>(X2 + base, pih, pil);
+            load_row2<N>(X2 + NP + base, fh, fl);
+          } else {
 #pragma unroll
-          for (int i = 0; i < N; ++i) {
-            const float2 vp = X2[base + i * stride], vf = X2[(1 + d) * NP + base + i * stride];
-            pih[i] = vp.x;
-            pil[i] = vp.y;
-            fh[i] = vf.x;
-            fl[i] = vf.y;
+            for (int i = 0; i < N; ++i) {
+              const float2 vp = X2[base + i * stride], vf = X2[(1 + d) * NP + base + i * stride];
+              pih[i] = vp.x;
+              pil[i] = vp.y;
+              fh[i] = vf.x;
+              fl[i] = vf.y;
+            }
           }
           eo_line_pdf<N>(fh, fl, dF, th, tl);
           eo_line_pdf<N>(pih, pil, dP, th, tl);
@@ -315,10 +368,18 @@ __global__ void __launch_bounds__(N * N * EPB, MINB)
             dP[i] *= Fd;
           }
         } else {
+          if (d == 0) {
+            load_row<N>(X + NP + base, pih);
+            load_row<N>(X + 2 * NP + base, fh);
+          } else {
+#pragma unroll
+            for (int i = 0; i < N; ++i) {
+              pih[i] = X[NP + base + i * stride];
+              fh[i] = X[(2 + d) * NP + base + i * stride];
+            }
+          }
 #pragma unroll
           for (int i = 0; i < N; ++i) {
-            pih[i] = X[NP + base + i * stride];
-            fh[i] = X[(2 + d) * NP + base + i * stride];
             pil[i] = 0.0f;
             fl[i] = 0.0f;
           }
@@ -362,32 +423,57 @@ __global__ void __launch_bounds__(N * N * EPB, MINB)
         dP[N - 1] = fmaf(-G2, dw_hi, dP[N - 1]);
         // Phi_d output
         const int64_t vo = e * VS + (2 + d) * NP + base;
+        float yv[N];
+        if (!COMP && HAS_Y) {
+          if (d == 0) {
+            load_row<N>(Yb + 2 * NP + base, yv);
+          } else {
+#pragma unroll
+            for (int i = 0; i < N; ++i) yv[i] = Yb[(2 + d) * NP + base + i * stride];
+          }
+        }
+        float wv[N];
 #pragma unroll
         for (int i = 0; i < N; ++i) {
           float w = dP[i];
           if (!COMP) {
             w = fmaf(alpha, fh[i], w);
-            if (HAS_Y) w = fmaf(beta, Yb[(2 + d) * NP + base + i * stride], w);
+            if (HAS_Y) w = fmaf(beta, yv[i], w);
           }
-          if (ACC) {
-            Xw[(2 + d) * NP + base + i * stride] = w;
-            continue;
+          wv[i] = w;
+        }
+        if (ACC) {
+          if (d == 0) {
+            store_row<N>(Xw + 2 * NP + base, wv);
+          } else {
+#pragma unroll
+            for (int i = 0; i < N; ++i) Xw[(2 + d) * NP + base + i * stride] = wv[i];
           }
-          if (L.w32) L.w32[vo + i * stride] = w;
+        } else {
+          if (L.w32) {
+            if (d == 0) {
+              store_row<N>(L.w32 + vo, wv);
+            } else {
+#pragma unroll
+              for (int i = 0; i < N; ++i) L.w32[vo + i * stride] = wv[i];
+            }
+          }
           if (L.out64) {
-            if (HAS_B)
-              L.out64[vo + i * stride] = Bb[(2 + d) * NP + base + i * stride] + widen(w);
-            else
-              L.out64[vo + i * stride] = widen(w);
+#pragma unroll
+            for (int i = 0; i < N; ++i) {
+              if (HAS_B)
+                L.out64[vo + i * stride] = Bb[(2 + d) * NP + base + i * stride] + widen(wv[i]);
+              else
+                L.out64[vo + i * stride] = widen(wv[i]);
+            }
           }
         }
         if (d < 2) {
+          if (d == 0) {
+            store_row<N>(Sacc + base, dF);
+          } else {
 #pragma unroll
-          for (int i = 0; i < N; ++i) {
-            if (d == 0)
-              Sacc[base + i * stride] = dF[i];
-            else
-              Sacc[base + i * stride] += dF[i];
+            for (int i = 0; i < N; ++i) Sacc[base + i * stride] += dF[i];
           }
         } else {
 #pragma unroll

@@ -44,8 +44,28 @@ struct Shape {
   static constexpr int NN = N * N;
   static constexpr int NP = N * N * N;
   static constexpr int TAB = 2 * H * h + H;  // doubles of one scaled table
-  static constexpr int SLOT = 5 * NP + 3 * TAB;  // smem doubles per element
+  // smem doubles per element, even so that every slot starts 16-byte aligned
+  static constexpr int SLOT = (5 * NP + 3 * TAB + 1) / 2 * 2;
 };
+
+// A contiguous row of N doubles (an x line; even N, 16-byte aligned) moved
+// two at a time: neighbouring threads' x lines are N doubles apart, so scalar
+// accesses would conflict on the shared-memory banks.
+template <int N>
+__device__ __forceinline__ void load_row(const double* p, double (&x)[N]) {
+#pragma unroll
+  for (int k = 0; k < N / 2; ++k) {
+    const double2 v = reinterpret_cast<const double2*>(p)[k];
+    x[2 * k] = v.x;
+    x[2 * k + 1] = v.y;
+  }
+}
+template <int N>
+__device__ __forceinline__ void store_row(double* p, const double (&x)[N]) {
+#pragma unroll
+  for (int k = 0; k < N / 2; ++k)
+    reinterpret_cast<double2*>(p)[k] = make_double2(x[2 * k], x[2 * k + 1]);
+}
 
 template <int N>
 __device__ __forceinline__ void eo_line(const double (&u)[N], double (&out)[N],
@@ -116,10 +136,15 @@ __global__ void __launch_bounds__(N * N * EPB, MINB)
         stride = NN;
       }
       double up[N], uf[N], dF[N], dP[N];
+      if (N % 2 == 0 && d == 0) {
+        load_row<N>(F + base, up);
+        load_row<N>(F + NP + base, uf);
+      } else {
 #pragma unroll
-      for (int i = 0; i < N; ++i) {
-        up[i] = F[base + i * stride];
-        uf[i] = F[(1 + d) * NP + base + i * stride];
+        for (int i = 0; i < N; ++i) {
+          up[i] = F[base + i * stride];
+          uf[i] = F[(1 + d) * NP + base + i * stride];
+        }
       }
       const double* tab = T + d * TAB;
       eo_line<N>(uf, dF, tab);  // -c J_d D Phi_d : c * (dt Pi) part
@@ -179,27 +204,48 @@ __global__ void __launch_bounds__(N * N * EPB, MINB)
 #pragma unroll
         for (int i = 0; i < N; ++i) dP[i] = fma(-gamma2, dpsi[i] + c * uf[i], dP[i]);
       }
-      // Phi_d update
+      // Phi_d update (x lines: contiguous, moved two doubles at a time when
+      // the element blocks are 16-byte aligned)
       double* outF = unext + off + (2 + d) * NP + base;
+      const bool row = N % 2 == 0 && d == 0 && (reinterpret_cast<uintptr_t>(outF) & 15u) == 0;
+      double ua[N];
+      if (MODE == kModeStage) {
+        if (N % 2 == 0 && d == 0 &&
+            (reinterpret_cast<uintptr_t>(u0 + off + 2 * NP + base) & 15u) == 0) {
+          load_row<N>(u0 + off + 2 * NP + base, ua);
+        } else {
+#pragma unroll
+          for (int i = 0; i < N; ++i) ua[i] = u0[off + (2 + d) * NP + base + i * stride];
+        }
+      }
+      double ov[N];
 #pragma unroll
       for (int i = 0; i < N; ++i) {
-        double v;
         if (MODE == kModeRhs || MODE == kModeVolume) {
-          v = dP[i];
+          ov[i] = dP[i];
         } else if (MODE == kModeStageFirst) {
-          v = uf[i] + dP[i];
+          ov[i] = uf[i] + dP[i];
         } else {
-          v = fma(coef.a, u0[off + (2 + d) * NP + base + i * stride], fma(coef.b, uf[i], dP[i]));
+          ov[i] = fma(coef.a, ua[i], fma(coef.b, uf[i], dP[i]));
         }
-        outF[i * stride] = v;
+      }
+      if (row) {
+        store_row<N>(outF, ov);
+      } else {
+#pragma unroll
+        for (int i = 0; i < N; ++i) outF[i * stride] = ov[i];
       }
       if (d < 2) {
+        if (N % 2 == 0 && d == 0) {
+          store_row<N>(Sacc + base, dF);
+        } else {
 #pragma unroll
-        for (int i = 0; i < N; ++i) {
-          if (d == 0)
-            Sacc[base + i * stride] = dF[i];
-          else
-            Sacc[base + i * stride] += dF[i];
+          for (int i = 0; i < N; ++i) {
+            if (d == 0)
+              Sacc[base + i * stride] = dF[i];
+            else
+              Sacc[base + i * stride] += dF[i];
+          }
         }
       } else {
         // z pass: dt Pi complete on this line; Pi and Psi updates

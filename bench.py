@@ -464,44 +464,81 @@ def config2_full_length(dev, steps=500):
             "rel_l2_mixed_vs_fp64": float(np.linalg.norm(m - a) / np.linalg.norm(a))}
 
 
+def _time_gradient(p, psi0, reps=3):
+    """(J, gradient, s per gradient, s per forward misfit run) of a MisfitProblem."""
+    import torch
+    p.value_and_gradient(psi0)  # warm-up (tuning, graph capture)
+    torch.cuda.synchronize()
+    t0 = time.perf_counter()
+    for _ in range(reps):
+        J, g = p.value_and_gradient(psi0)
+    torch.cuda.synchronize()
+    s_per_grad = (time.perf_counter() - t0) / reps
+    t0 = time.perf_counter()
+    for _ in range(reps):
+        p.value(psi0)
+    torch.cuda.synchronize()
+    return J, g, s_per_grad, (time.perf_counter() - t0) / reps
+
+
 def time_adjoint(dev):
     """The adjoint case: 8^3 elements x 8^3 points, dt 5e-4, 2000 SSP-RK3 steps, 64
     samples every 10 steps; seconds per gradient (forward misfit run + the
-    discrete adjoint sweep), with central-difference and tangent-linear checks
-    along seeded directions."""
+    discrete adjoint sweep) in FP64 and in mixed precision (FP64 states, FP32
+    increments), with central-difference checks against the FP64 objective
+    and tangent-linear checks along seeded directions, and the mixed
+    gradient's error against the FP64 one."""
     import torch
     from spectre_gb300.adjoint import MisfitProblem
     p = MisfitProblem(device=dev)
+    pm = MisfitProblem(device=dev, precision="mixed")
     try:
         psi0 = p.initial_psi()
-        p.value_and_gradient(psi0)  # warm-up (graph capture)
-        torch.cuda.synchronize()
-        reps = 3
-        t0 = time.perf_counter()
-        for _ in range(reps):
-            J, g = p.value_and_gradient(psi0)
-        torch.cuda.synchronize()
-        s_per_grad = (time.perf_counter() - t0) / reps
+        J, g, s_grad, s_fwd = _time_gradient(p, psi0)
+        Jm, gm, s_grad_m, s_fwd_m = _time_gradient(pm, psi0)
+        split, split_ms = p.ev.adjoint_autotune()
+        stage_variant, stage_ms = p.ev.autotune()
         rng = torch.Generator(device="cuda").manual_seed(11)
         eps = 1e-6
-        fd_err = 0.0
+        fd_err = fd_err_m = 0.0
         for _ in range(2):
             v = torch.randn(psi0.shape, dtype=torch.float64, device="cuda", generator=rng)
             fd = (p.value(psi0 + eps * v) - p.value(psi0 - eps * v)) / (2 * eps)
-            ad = float(torch.sum(g * v))
-            fd_err = max(fd_err, abs(fd - ad) / abs(ad))
+            fd_err = max(fd_err, abs(fd - float(torch.sum(g * v))) / abs(fd))
+            fd_err_m = max(fd_err_m, abs(fd - float(torch.sum(gm * v))) / abs(fd))
         v = torch.randn(psi0.shape, dtype=torch.float64, device="cuda", generator=rng)
         tl = p.tangent_linear(psi0, v)
         tl_err = abs(tl - float(torch.sum(g * v))) / abs(tl)
-        return {"workload": "ScalarWave 8^3 elements x 8^3 LGL points, FP64, SSP-RK3 dt=5e-4, "
+        tl_err_m = abs(tl - float(torch.sum(gm * v))) / abs(tl)
+        mixed_max = float((gm - g).abs().max()) / float(g.abs().max())
+        mixed_l2 = float(torch.linalg.norm(gm - g)) / float(torch.linalg.norm(g))
+        return {"workload": "ScalarWave 8^3 elements x 8^3 LGL points, SSP-RK3 dt=5e-4, "
                             "2000 steps, 64 seeded samples of Psi every 10 steps; control Psi(t=0)",
-                "s_per_grad": s_per_grad, "J": J,
-                "fd_max_rel_err_2_dirs": fd_err, "tangent_linear_rel_err": tl_err,
-                "note": "forward misfit run + hand-written discrete adjoint sweep (3 L^T "
-                        "launches per step); the step map is linear, so no forward states "
-                        "are stored"}
+                "s_per_grad": s_grad_m, "s_per_grad_precision": "mixed",
+                "fp64": {"s_per_grad": s_grad, "s_forward": s_fwd,
+                         "s_adjoint_sweep": s_grad - s_fwd, "J": J,
+                         "fd_max_rel_err_2_dirs": fd_err, "tangent_linear_rel_err": tl_err,
+                         "forward_stage_variant": stage_variant,
+                         "forward_ms_per_stage_variants": [float(x) for x in stage_ms],
+                         "adjoint_split": split,
+                         "adjoint_ms_per_launch_splits": [float(x) for x in split_ms]},
+                "mixed": {"s_per_grad": s_grad_m, "s_forward": s_fwd_m,
+                          "s_adjoint_sweep": s_grad_m - s_fwd_m, "J": Jm,
+                          "J_rel_err_vs_fp64": abs(Jm - J) / abs(J),
+                          "grad_max_rel_err_vs_fp64": mixed_max,
+                          "grad_l2_rel_err_vs_fp64": mixed_l2,
+                          "fd_max_rel_err_2_dirs": fd_err_m,
+                          "tangent_linear_rel_err": tl_err_m,
+                          "speedup_vs_fp64": s_grad / s_grad_m},
+                "note": "forward misfit run + hand-written discrete adjoint sweep; the step "
+                        "map is linear, so no forward states are stored.  FP64: 3 L^T launches "
+                        "per step (reverse SSP-RK3 stages).  Mixed: mixed forward, and "
+                        "W1 = dt L^T l (double-float), W2, W3 (FP32), l += W1 + W2/2 + W3/6. "
+                        "Central differences and the tangent-linear run use the FP64 "
+                        "objective."}
     finally:
         p.close()
+        pm.close()
 
 
 def time_curved_adams(shell, n, dt, steps, dev):

@@ -39,7 +39,7 @@
 extern "C" {
 #endif
 
-#define DGSW_ABI_VERSION 8
+#define DGSW_ABI_VERSION 9
 
 typedef enum {
   DGSW_OK = 0,
@@ -357,19 +357,24 @@ int dgsw_set_guards(DgswHandle h, double cfl_safety_factor, int check_finite);
 int dgsw_check_finite(DgswHandle h, int64_t* first_element);
 
 /* ---- launch autotuner -------------------------------------------------------
- * The plain FP64 stage kernel exists in two launch configurations per N
- * (elements per block, resident blocks per SM).  The first dgsw_step of a
- * handle times both on the handle's own data (without touching its state),
- * keeps the faster and reuses the choice for handles of the same shape.
- * dgsw_autotune re-runs the timing now and returns the chosen variant and
- * the measured ms per stage launch of each (zeros where nothing is tuned:
- * mixed, curved, Gauss and mixed-extent handles use fixed configurations);
- * force_variant 0 or 1 then imposes that variant (-1 keeps the faster).
- * No counterpart in the reference. */
+ * The plain FP64 stage kernel exists in DGSW_STAGE_VARIANTS launch
+ * configurations per N: two of elements per block and resident blocks per SM
+ * (0, 1), and two that run the three axis passes of one element at once (2, 3:
+ * three times the threads for the same work, for grids too small to fill the
+ * GPU; 3 asks for one more resident block per SM than 2).
+ * All give the same bits.  The first dgsw_step of a handle times each on the
+ * handle's own data (without touching its state), keeps the fastest and
+ * reuses the choice for handles of the same shape.  dgsw_autotune re-runs
+ * the timing now and returns the chosen variant and the measured ms per
+ * stage launch of each (ms_per_launch holds DGSW_STAGE_VARIANTS values; zeros
+ * where nothing is tuned: mixed, curved, Gauss and mixed-extent handles use
+ * fixed configurations); force_variant >= 0 then imposes that variant (-1
+ * keeps the fastest).  No counterpart in the reference. */
+#define DGSW_STAGE_VARIANTS 4
 int dgsw_autotune(DgswHandle h, int force_variant, int* variant, double* ms_per_launch);
 
 /* The launch autotuner of whichever step kernels the handle runs.
- * family: DGSW_TUNE_FP64_STAGE (the plain FP64 stage kernel's two
+ * family: DGSW_TUNE_FP64_STAGE (the plain FP64 stage kernel's
  * configurations, as dgsw_autotune), DGSW_TUNE_MIXED_BATCH (mixed precision
  * on elements of differing extents: the persistent batch kernels' compiled
  * launch shapes -- threads per CTA, resident CTAs per SM, pipeline buffers,
@@ -465,11 +470,19 @@ int dgsw_amr_project_device(DgswHandle h, int n_vars, int64_t n_in, const int64_
                             const int8_t* child, const int64_t* out_offset, double* dev_out);
 
 /* ---- discrete adjoint and the misfit objective -----------------------------
- * FP64, one brick of uniform extent, gamma2 = 0.  The step map of this path
- * is linear (fixed normals and char speeds), so the reverse sweep needs only
- * the recorded residuals, not the forward states.
- * dgsw_adjoint_rhs_device: lambda -> L^T lambda, the exact transpose of the
- * operator dgsw_rhs_device applies.
+ * One brick of uniform extent, gamma2 = 0, Rk3HesthavenSsp, no filter.  The
+ * step map of this path is linear (fixed normals and char speeds), so the
+ * reverse sweep needs only the recorded residuals, not the forward states.
+ * FP64 handles run dgsw_step forward and the FP64 adjoint (three L^T
+ * launches per step, the reverse stages of Rk3HesthavenSsp).  Mixed-precision
+ * handles run both sweeps as the step's Taylor polynomial 1 + dt L +
+ * (dt L)^2/2 + (dt L)^3/6 (the same map): W1 = dt L u, W2 = dt L W1,
+ * W3 = dt L W2, u += W1 + W2/2 + W3/6 (L^T and the adjoint state backwards),
+ * with FP64 states and double-float increments formed in FP32 arithmetic
+ * (not the FP32 increments of dgsw_step: the residuals and the rough adjoint
+ * field need ~1e-8 of themselves over thousands of steps).
+ * dgsw_adjoint_rhs_device: lambda -> L^T lambda (FP64), the exact transpose
+ * of the operator dgsw_rhs_device applies.
  * dgsw_set_samples: points (x, y, z per point) where Psi is sampled by
  * barycentric Lagrange interpolation on the element's LGL nodes
  * (Spectral.cpp:625-670 weights; the role of IrregularInterpolant,
@@ -487,6 +500,14 @@ int dgsw_sample_psi(DgswHandle h, double* host_out);
 int dgsw_misfit_forward(DgswHandle h, int n_windows, int steps_per_window, double dt,
                         const double* host_targets, double* J);
 int dgsw_misfit_adjoint(DgswHandle h, double* dev_grad);
+/* The adjoint kernel's two work splits (N^2 threads per element with the
+ * three axes in turn, or 3 N^2 threads with the axes at once; the same bits).
+ * The first dgsw_misfit_adjoint times both on the handle's state and keeps the
+ * faster; dgsw_adjoint_autotune re-times them now and returns the choice and
+ * ms per L^T launch of each (ms_per_launch: 2 values); force_variant 0 or 1
+ * imposes a split afterwards (-1 keeps the faster).  No counterpart in the
+ * reference. */
+int dgsw_adjoint_autotune(DgswHandle h, int force_variant, int* variant, double* ms_per_launch);
 
 /* ---- host-only setup (no GPU) ---------------------------------------------
  * Spectral::collocation_points / quadrature_weights <Legendre, GaussLobatto>

@@ -1,11 +1,13 @@
 """Misfit objective and its discrete adjoint behind torch.autograd.Function.
 
 The control is the initial Psi field of one evolution (one periodic brick,
-uniform LGL extent, plain FP64).  J(Psi0) = sum over windows m and sample
-points s of (Psi(x_s, t_m) - target_ms)^2, with Psi sampled every
-`steps_per_window` SSP-RK3 steps.  The gradient comes from the hand-written
-discrete adjoint of the DG step (dgsw_misfit_adjoint); the step map is
-linear, so the reverse sweep needs the recorded residuals only.
+uniform LGL extent).  J(Psi0) = sum over windows m and sample points s of
+(Psi(x_s, t_m) - target_ms)^2, with Psi sampled every `steps_per_window`
+SSP-RK3 steps.  The gradient comes from the hand-written discrete adjoint of
+the DG step (dgsw_misfit_adjoint); the step map is linear, so the reverse
+sweep needs the recorded residuals only.  precision="mixed" runs the forward
+and the adjoint sweep in mixed precision (FP64 states, FP32 increments); the
+targets and the base state always come from an FP64 run.
 """
 from __future__ import annotations
 
@@ -13,7 +15,7 @@ import math
 
 import numpy as np
 
-from .dgsw import Brick, DgEvolution, PRECISION_FP64
+from .dgsw import Brick, DgEvolution, PRECISION_FP64, PRECISION_MIXED
 
 TWO_PI = 2.0 * math.pi
 
@@ -24,12 +26,14 @@ def psi_view(state, n_elem: int, n: int):
 
 
 class MisfitProblem:
-    """Owns one FP64 DgEvolution, the fixed (Pi, Phi) of the initial state,
-    the sample points and the target trace."""
+    """Owns one DgEvolution (FP64 or mixed precision), the fixed (Pi, Phi) of
+    the initial state, the sample points and the target trace."""
 
     def __init__(self, elements=(8, 8, 8), points=8, dt=5e-4, steps=2000, steps_per_window=10,
-                 n_samples=64, seed=4, device=0):
+                 n_samples=64, seed=4, device=0, precision="fp64"):
         import torch
+        prec = {"fp64": PRECISION_FP64, "mixed": PRECISION_MIXED}[precision]
+        self.precision = precision
         self.ev = DgEvolution([Brick(elements)], points, precision=PRECISION_FP64, device=device)
         self.n = points
         self.dt = dt
@@ -55,6 +59,10 @@ class MisfitProblem:
         self.base_state = torch.tensor(self.ev.get_state(), dtype=torch.float64,
                                        device="cuda:%d" % device)
         self.n_elem = self.ev.n_elements
+        if prec != PRECISION_FP64:
+            self.ev.close()
+            self.ev = DgEvolution([Brick(elements)], points, precision=prec, device=device)
+            self.ev.set_samples(self.xyz)
 
     def initial_psi(self):
         return psi_view(self.base_state, self.n_elem, self.n).clone()

@@ -110,6 +110,7 @@ struct DgswHandle_ {
   double* samp_w = nullptr;
   double* adj = nullptr;   // adjoint state
   double* adjz = nullptr;  // adjoint stage combination
+  float2* adj32 = nullptr;  // mixed precision: the increments W1, W2 (double-float pairs)
   double* targets = nullptr;
   double* residuals = nullptr;
   int64_t record_cap = 0;  // windows x samples the two buffers above hold
@@ -117,6 +118,13 @@ struct DgswHandle_ {
   double rec_dt = 0.0;
   cudaGraphExec_t graph_adj = nullptr;
   int graph_adj_steps = 0;
+  cudaGraphExec_t graph_tf = nullptr;  // mixed precision: the misfit forward's window of steps
+  int graph_tf_steps = 0;
+  double graph_tf_dt = std::nan("");
+  // the adjoint kernel's work split (AdjointLaunch::variant), timed on first use
+  bool adj_tuned = false;
+  int adj_variant = 0;
+  double adj_tune_ms[2] = {0.0, 0.0};
   double graph_adj_dt = std::nan("");
   // CurvedScalarWave on the shell: static tables (csw_fp64.cu)
   bool curved = false;
@@ -132,7 +140,7 @@ struct DgswHandle_ {
   // launch autotuner: the FP64 stage's launch-configuration variant
   bool tuned = false;
   int stage_variant = 0;
-  double tune_ms[2] = {0.0, 0.0};
+  double tune_ms[DGSW_STAGE_VARIANTS] = {};
   // refined block lattice (h-nonconforming 2:1 faces)
   bool refined = false;
   DgswRefinedBrick rbrick{};
@@ -791,11 +799,13 @@ cudaError_t mixed_filtered_stage(DgswHandle h, int k, double dt, const double* u
 }
 
 // ---- launch autotuner ------------------------------------------------------
-// The FP64 stage kernel is compiled in two launch configurations per N
-// (elements per block and resident blocks asked of the register allocator).
-// Before the first step the handle times both on its own data (the stage
-// input copied to t1, output to t2: the state is untouched) and keeps the
-// faster; the choice is cached per (N, elements) for later handles.
+// The FP64 stage kernel is compiled in DGSW_STAGE_VARIANTS launch
+// configurations per N (elements per block and resident blocks asked of the
+// register allocator; variants 2 and 3 run the three axis passes at once, for
+// grids too small to fill the GPU).  Before the first step the handle times each on its own data
+// (the stage input copied to t1, output to t2: the state is untouched) and
+// keeps the fastest; the choice is cached per (N, elements) for later
+// handles.
 bool tunable(DgswHandle h) { return !mixed(h) && !h->curved && !h->gauss && !h->general; }
 
 std::mutex g_tune_mu;
@@ -821,7 +831,7 @@ int autotune(DgswHandle h, bool force) {
   float best = -1.0f;
   int choice = 0;
   cudaError_t err = cudaSuccess;
-  for (int v = 0; v < 2 && err == cudaSuccess; ++v) {
+  for (int v = 0; v < DGSW_STAGE_VARIANTS && err == cudaSuccess; ++v) {
     StageLaunch L = base_launch(h);
     L.variant = v;
     L.mode = kModeStage;
@@ -1236,7 +1246,50 @@ AdjointLaunch base_adjoint(DgswHandle h) {
   A.nbr = h->nbr;
   A.jac = h->jac;
   A.eoT = h->eoT;
+  A.variant = h->adj_variant;
   return A;
+}
+
+// Times both work splits of the adjoint kernel on the handle's state (read
+// only; the output goes to t1) and keeps the faster.  Both give the same bits.
+cudaError_t adjoint_autotune(DgswHandle h) {
+  cudaEvent_t e0, e1;
+  cudaError_t err = cudaEventCreate(&e0);
+  if (err != cudaSuccess) return err;
+  err = cudaEventCreate(&e1);
+  if (err != cudaSuccess) {
+    cudaEventDestroy(e0);
+    return err;
+  }
+  float best = -1.0f;
+  int choice = 0;
+  for (int v = 0; v < 2 && err == cudaSuccess; ++v) {
+    AdjointLaunch A = base_adjoint(h);
+    A.variant = v;
+    A.x = h->state;
+    A.out = h->t1;
+    A.alpha = 1.0;
+    A.c = 1e-4;
+    err = launch_adjoint_fp64(A, h->stream);  // warm-up
+    if (err == cudaSuccess) err = cudaEventRecord(e0, h->stream);
+    for (int r = 0; r < 5 && err == cudaSuccess; ++r) err = launch_adjoint_fp64(A, h->stream);
+    if (err == cudaSuccess) err = cudaEventRecord(e1, h->stream);
+    if (err == cudaSuccess) err = cudaEventSynchronize(e1);
+    float ms = 0.0f;
+    if (err == cudaSuccess) err = cudaEventElapsedTime(&ms, e0, e1);
+    h->adj_tune_ms[v] = ms / 5.0;
+    if (err == cudaSuccess && (best < 0.0f || ms < best)) {
+      best = ms;
+      choice = v;
+    }
+  }
+  cudaEventDestroy(e0);
+  cudaEventDestroy(e1);
+  if (err == cudaSuccess) {
+    h->adj_variant = choice;
+    h->adj_tuned = true;
+  }
+  return err;
 }
 
 // One step of the discrete adjoint of Rk3HesthavenSsp (Rk3HesthavenSsp.cpp:63-80)
@@ -1273,12 +1326,80 @@ cudaError_t enqueue_adjoint_step(DgswHandle h, double dt) {
   return launch_adjoint_fp64(A, h->stream);
 }
 
+// One mixed-precision step of the plain operator (taylor_df.cu) or of its
+// adjoint: the step map is the Taylor polynomial 1 + dt L + (dt L)^2/2 +
+// (dt L)^3/6, so
+//   W1 = dt L u,  W2 = dt L W1,  W3 = dt L W2,  u += W1 + W2/2 + W3/6
+// (L^T and the adjoint state for the adjoint), with double-float increments
+// formed in FP32 arithmetic.  The misfit forward of a mixed-precision handle
+// steps with it (its residuals must hold ~1e-8 of themselves over thousands
+// of steps), on the state; the adjoint on h->adj.
+cudaError_t enqueue_taylor_step(DgswHandle h, double dt, bool transpose) {
+  const int64_t size = h->dom.offset.back();
+  float2* w1 = h->adj32;
+  float2* w2 = h->adj32 + size;
+  double* u = transpose ? h->adj : h->state;
+  TaylorLaunch A;
+  A.n = h->dom.elem_n[0];
+  A.n_elem = h->dom.n_elem;
+  A.transpose = transpose;
+  A.dt = dt;
+  A.nbr = h->nbr;
+  A.jac = h->jac;
+  A.eo = transpose ? h->eoT : h->eo;
+  A.kind = 0;
+  A.x64 = u;
+  A.outp = w1;
+  cudaError_t e = launch_taylor_df(A, h->stream);
+  if (e != cudaSuccess) return e;
+  A.kind = 1;
+  A.x64 = nullptr;
+  A.xp = w1;
+  A.outp = w2;
+  e = launch_taylor_df(A, h->stream);
+  if (e != cudaSuccess) return e;
+  A.kind = 2;
+  A.xp = w2;
+  A.outp = nullptr;
+  A.l64 = u;
+  A.w1 = w1;
+  return launch_taylor_df(A, h->stream);
+}
+
 cudaError_t capture_adjoint_steps(DgswHandle h, double dt, int steps, cudaGraphExec_t* out) {
   cudaGraph_t g = nullptr;
   cudaError_t e = cudaStreamBeginCapture(h->stream, cudaStreamCaptureModeThreadLocal);
   if (e != cudaSuccess) return e;
   cudaError_t le = cudaSuccess;
-  for (int s = 0; s < steps && le == cudaSuccess; ++s) le = enqueue_adjoint_step(h, dt);
+  for (int s = 0; s < steps && le == cudaSuccess; ++s)
+    le = mixed(h) ? enqueue_taylor_step(h, dt, true) : enqueue_adjoint_step(h, dt);
+  e = cudaStreamEndCapture(h->stream, &g);
+  if (le != cudaSuccess) {
+    if (g) cudaGraphDestroy(g);
+    return le;
+  }
+  if (e != cudaSuccess) return e;
+  e = cudaGraphInstantiate(out, g, 0);
+  cudaGraphDestroy(g);
+  return e;
+}
+
+// the two increment blocks of the mixed-precision Taylor step
+int taylor_buffers(DgswHandle h) {
+  if (h->adj32) return DGSW_OK;
+  DGSW_CUDA(h, cudaStreamSynchronize(h->stream));
+  DGSW_CUDA(h, cudaMalloc(&h->adj32, 2 * h->dom.offset.back() * sizeof(float2)));
+  return DGSW_OK;
+}
+
+// steps mixed-precision Taylor steps of the state (the misfit forward of a
+// mixed-precision handle)
+cudaError_t capture_taylor_steps(DgswHandle h, double dt, int steps, cudaGraphExec_t* out) {
+  cudaGraph_t g = nullptr;
+  cudaError_t e = cudaStreamBeginCapture(h->stream, cudaStreamCaptureModeThreadLocal);
+  if (e != cudaSuccess) return e;
+  cudaError_t le = cudaSuccess;
+  for (int s = 0; s < steps && le == cudaSuccess; ++s) le = enqueue_taylor_step(h, dt, false);
   e = cudaStreamEndCapture(h->stream, &g);
   if (le != cudaSuccess) {
     if (g) cudaGraphDestroy(g);
@@ -2521,9 +2642,11 @@ int dgsw_destroy(DgswHandle h) {
   for (double* p : dbl)
     if (p) cudaFree(p);
   if (h->graph_adj) cudaGraphExecDestroy(h->graph_adj);
+  if (h->graph_tf) cudaGraphExecDestroy(h->graph_tf);
   double* adjbufs[] = {h->samp_w, h->adj, h->adjz, h->targets, h->residuals};
   for (double* p : adjbufs)
     if (p) cudaFree(p);
+  if (h->adj32) cudaFree(h->adj32);
   if (h->samp_off) cudaFree(h->samp_off);
   double* cdbl[] = {h->c_xyz, h->c_ij, h->c_T, h->c_F};
   for (double* p : cdbl)
@@ -2966,8 +3089,8 @@ int dgsw_observe_plane_wave_errors(DgswHandle h, const double* k, double t, doub
 
 int dgsw_autotune(DgswHandle h, int force_variant, int* variant, double* ms_per_launch) {
   if (!h) return fail(nullptr, DGSW_ERR_ARGUMENT, "null handle");
-  if (force_variant < -1 || force_variant > 1)
-    return fail(h, DGSW_ERR_ARGUMENT, "force_variant must be -1, 0 or 1");
+  if (force_variant < -1 || force_variant >= DGSW_STAGE_VARIANTS)
+    return fail(h, DGSW_ERR_ARGUMENT, "force_variant must be -1 or a variant index");
   if (int rc = select_device(h)) return rc;
   if (tunable(h)) {
     destroy_graphs(h);
@@ -2975,10 +3098,8 @@ int dgsw_autotune(DgswHandle h, int force_variant, int* variant, double* ms_per_
     if (force_variant >= 0) h->stage_variant = force_variant;
   }
   if (variant) *variant = h->stage_variant;
-  if (ms_per_launch) {
-    ms_per_launch[0] = h->tune_ms[0];
-    ms_per_launch[1] = h->tune_ms[1];
-  }
+  if (ms_per_launch)
+    for (int v = 0; v < DGSW_STAGE_VARIANTS; ++v) ms_per_launch[v] = h->tune_ms[v];
   return DGSW_OK;
 }
 
@@ -3022,15 +3143,14 @@ int dgsw_tune(DgswHandle h, int force_variant, int* family, int* n_variants, int
     for (int i = 0; i < nv; ++i) ms[i] = h->pipe_tune_ms[i];
   } else if (tunable(h)) {
     fam = DGSW_TUNE_FP64_STAGE;
-    nv = 2;
+    nv = DGSW_STAGE_VARIANTS;
     if (force_variant >= nv || force_variant < -1)
       return fail(h, DGSW_ERR_ARGUMENT, "force_variant out of range");
     destroy_graphs(h);
     if (int rc = autotune(h, true)) return rc;
     if (force_variant >= 0) h->stage_variant = force_variant;
     v = h->stage_variant;
-    ms[0] = 3.0 * h->tune_ms[0];
-    ms[1] = 3.0 * h->tune_ms[1];
+    for (int i = 0; i < nv; ++i) ms[i] = 3.0 * h->tune_ms[i];
   }
   if (family) *family = fam;
   if (n_variants) *n_variants = nv;
@@ -3323,7 +3443,10 @@ int dgsw_misfit_forward(DgswHandle h, int n_windows, int steps_per_window, doubl
   if (n_windows < 1 || steps_per_window < 1 || !std::isfinite(dt))
     return fail(h, DGSW_ERR_ARGUMENT, "bad window arguments");
   if (h->n_samples < 1) return fail(h, DGSW_ERR_ARGUMENT, "no sample points set");
-  if (mixed(h)) return fail(h, DGSW_ERR_UNSUPPORTED, "the misfit adjoint is FP64 only");
+  if (h->curved || h->refined || h->filter_on ||
+      h->cfg.time_stepper != DGSW_STEPPER_RK3_HESTHAVEN_SSP)
+    return fail(h, DGSW_ERR_UNSUPPORTED,
+                "the misfit adjoint needs the flat system, Rk3HesthavenSsp and no filter");
   if (int rc = select_device(h)) return rc;
   const int64_t need = (int64_t)n_windows * h->n_samples;
   if (h->record_cap < need) {
@@ -3338,8 +3461,22 @@ int dgsw_misfit_forward(DgswHandle h, int n_windows, int steps_per_window, doubl
   DGSW_CUDA(h, cudaMemcpyAsync(h->targets, host_targets, need * sizeof(double),
                                cudaMemcpyHostToDevice, h->stream));
   const int n = h->dom.elem_n[0];
+  if (mixed(h)) {
+    if (int rc = taylor_buffers(h)) return rc;
+    if (!(h->graph_tf_dt == dt) || h->graph_tf_steps != steps_per_window) {
+      if (h->graph_tf) cudaGraphExecDestroy(h->graph_tf);
+      h->graph_tf = nullptr;
+      DGSW_CUDA(h, capture_taylor_steps(h, dt, steps_per_window, &h->graph_tf));
+      h->graph_tf_dt = dt;
+      h->graph_tf_steps = steps_per_window;
+    }
+  }
   for (int m = 0; m < n_windows; ++m) {
-    if (int rc = dgsw_step(h, steps_per_window, dt)) return rc;
+    if (mixed(h)) {
+      DGSW_CUDA(h, cudaGraphLaunch(h->graph_tf, h->stream));
+    } else if (int rc = dgsw_step(h, steps_per_window, dt)) {
+      return rc;
+    }
     DGSW_CUDA(h, launch_sample(h->state, h->n_samples, n, h->samp_off, h->samp_w,
                                h->targets + (int64_t)m * h->n_samples,
                                h->residuals + (int64_t)m * h->n_samples, h->stream));
@@ -3357,13 +3494,38 @@ int dgsw_misfit_forward(DgswHandle h, int n_windows, int steps_per_window, doubl
   return check_device_error(h);
 }
 
+int dgsw_adjoint_autotune(DgswHandle h, int force_variant, int* variant, double* ms_per_launch) {
+  if (!h) return fail(nullptr, DGSW_ERR_ARGUMENT, "null handle");
+  if (force_variant < -1 || force_variant > 1)
+    return fail(h, DGSW_ERR_ARGUMENT, "force_variant must be -1, 0 or 1");
+  if (h->general || h->curved || h->gauss || h->refined || mixed(h) || h->cfg.gamma2 != 0.0)
+    return fail(h, DGSW_ERR_UNSUPPORTED,
+                "the FP64 adjoint needs the flat FP64 system, uniform extents and gamma2 = 0");
+  if (int rc = select_device(h)) return rc;
+  DGSW_CUDA(h, adjoint_autotune(h));
+  if (force_variant >= 0) h->adj_variant = force_variant;
+  // the captured sweep holds the old split
+  if (h->graph_adj) cudaGraphExecDestroy(h->graph_adj);
+  h->graph_adj = nullptr;
+  h->graph_adj_steps = 0;
+  if (variant) *variant = h->adj_variant;
+  if (ms_per_launch) {
+    ms_per_launch[0] = h->adj_tune_ms[0];
+    ms_per_launch[1] = h->adj_tune_ms[1];
+  }
+  return DGSW_OK;
+}
+
 int dgsw_misfit_adjoint(DgswHandle h, double* dev_grad) {
   if (!h || !dev_grad) return fail(h, DGSW_ERR_ARGUMENT, "null argument");
   if (h->rec_windows < 1) return fail(h, DGSW_ERR_ARGUMENT, "no recorded misfit run");
   if (int rc = select_device(h)) return rc;
   const size_t bytes = h->dom.offset.back() * sizeof(double);
+  if (mixed(h))
+    if (int rc = taylor_buffers(h)) return rc;
   const int K = h->rec_steps;
   const double dt = h->rec_dt;
+  if (!h->adj_tuned && !mixed(h)) DGSW_CUDA(h, adjoint_autotune(h));
   if (!(h->graph_adj_dt == dt) || h->graph_adj_steps != K) {
     if (h->graph_adj) cudaGraphExecDestroy(h->graph_adj);
     h->graph_adj = nullptr;

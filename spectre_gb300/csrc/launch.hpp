@@ -349,8 +349,32 @@ struct AdjointLaunch {
   const int32_t* nbr = nullptr;
   const double* jac = nullptr;
   EoTable eoT{};  // even/odd split of D^T
+  int variant = 0;  // 0: N^2 threads per element, axes in turn; 1: 3 N^2, axes at once
 };
 cudaError_t launch_adjoint_fp64(const AdjointLaunch& L, cudaStream_t s);
+// One launch of the mixed-precision Taylor step (taylor_df.cu) of the plain
+// operator L or (transpose) of L^T, increments as double-float (hi, lo) FP32
+// pairs in the state's layout: W1 = dt L u (kind 0, x64 = the FP64 state,
+// outp = W1), W2 = dt L W1 (kind 1, xp = W1, outp = W2), and kind 2:
+// W3 = dt L W2 (xp = W2) with state l64 += W1 + W2/2 + W3/6 (w1 = W1).  eo:
+// the split tables of D (forward) or D^T (transpose).
+struct TaylorLaunch {
+  int n = 0;
+  int kind = 0;
+  bool transpose = false;
+  int64_t n_elem = 0;
+  double dt = 0.0;
+  const double* x64 = nullptr;
+  const float2* xp = nullptr;
+  float2* outp = nullptr;
+  double* l64 = nullptr;
+  const float2* w1 = nullptr;
+  float sixth_h = 0.0f, sixth_l = 0.0f;  // 1/6 as a pair (set by the launcher)
+  const int32_t* nbr = nullptr;
+  const double* jac = nullptr;
+  EoTable eo{};
+};
+cudaError_t launch_taylor_df(const TaylorLaunch& L, cudaStream_t s);
 // Psi at sample points: out[s] = sample - target[s] (target may be null).
 cudaError_t launch_sample(const double* u, int n_samples, int n, const int64_t* elem_off,
                           const double* w, const double* target, double* out, cudaStream_t s);

@@ -41,6 +41,7 @@ PRECISION_FP64 = 0
 PRECISION_MIXED = 1
 N_VARS = 5  # Psi, Pi, Phi_x, Phi_y, Phi_z
 N_PACKAGED = 16  # UpwindPenalty dg_package_field_tags doubles per face point
+STAGE_VARIANTS = 4  # DGSW_STAGE_VARIANTS: launch configurations of the FP64 stage
 
 
 class DgswError(RuntimeError):
@@ -157,6 +158,7 @@ _SIGNATURES = {
     "dgsw_sample_psi": (_I, [_P, _P]),
     "dgsw_misfit_forward": (_I, [_P, _I, _I, _D, _P, ctypes.POINTER(_D)]),
     "dgsw_misfit_adjoint": (_I, [_P, _P]),
+    "dgsw_adjoint_autotune": (_I, [_P, _I, ctypes.POINTER(_I), _P]),
     "dgsw_step_noalloc": (_I, [ctypes.POINTER(DgswBrick), _I, _D, _P, _I, _D, _P]),
     "dgsw_adams_info": (_I, [_P, _P, _P, _P, _P]),
     "dgsw_cfl_steps": (_I, [ctypes.POINTER(DgswConfig), _D, _P, _P]),
@@ -790,10 +792,10 @@ class DgEvolution:
 
     def autotune(self, force_variant: int = -1):
         """Re-times the FP64 stage's launch variants on this handle; returns
-        (chosen variant, [ms per launch of each]).  force_variant 0 / 1
+        (chosen variant, [ms per launch of each]).  force_variant >= 0
         imposes a variant afterwards."""
         v = _I()
-        ms = np.zeros(2)
+        ms = np.zeros(STAGE_VARIANTS)
         _check(lib().dgsw_autotune(self._h, int(force_variant), ctypes.byref(v), _ptr(ms)),
                self._h)
         return v.value, ms
@@ -862,6 +864,16 @@ class DgEvolution:
         _check(lib().dgsw_adjoint_rhs_device(self._h, _ptr(lam_dev), _ptr(out)), self._h)
         self.synchronize()
         return out
+
+    def adjoint_autotune(self, force_variant: int = -1):
+        """Re-times the adjoint kernel's two work splits on this handle;
+        returns (chosen split, [ms per L^T launch of each]).  force_variant
+        0 / 1 imposes a split afterwards."""
+        v = _I()
+        ms = np.zeros(2)
+        _check(lib().dgsw_adjoint_autotune(self._h, int(force_variant), ctypes.byref(v),
+                                           _ptr(ms)), self._h)
+        return v.value, ms
 
     def set_samples(self, xyz):
         a = np.ascontiguousarray(xyz, dtype=np.float64).reshape(-1, 3)

@@ -12,7 +12,7 @@ import numpy as np
 import pytest
 
 from spectre_gb300 import dgsw
-from spectre_gb300.dgsw import Brick, DgEvolution
+from spectre_gb300.dgsw import STAGE_VARIANTS, Brick, DgEvolution
 
 pytestmark = pytest.mark.gpu
 HERE = os.path.dirname(os.path.abspath(__file__))
@@ -247,12 +247,15 @@ def test_errors_are_reported_not_fatal():
 
 
 def test_autotuned_variants_agree(oracle):
-    # both launch configurations of the FP64 stage match the oracle
+    # every launch configuration of the FP64 stage (two of elements per block,
+    # two with the three axis passes at once) matches the oracle, all with
+    # the same bits
     bricks = [Brick((3, 2, 4))]
-    for n in (4, 8, 11):
+    for n in (2, 4, 5, 8, 10, 11, 12):
         u = random_state(np.random.default_rng(n), bricks, n, oracle)
         ref = oracle.evolve(bricks, n, u, 1e-3, 2)
-        for force in (0, 1):
+        first = None
+        for force in range(STAGE_VARIANTS):
             with DgEvolution(bricks, n) as ev:
                 ev.set_state(u)
                 v, ms = ev.autotune(force)
@@ -260,3 +263,7 @@ def test_autotuned_variants_agree(oracle):
                 ev.step(2, 1e-3)
                 got = ev.get_state()
             assert rel_err_per_var(got, ref, oracle.elem_points(bricks, n)) <= 1e-12
+            if first is None:
+                first = got
+            else:
+                assert np.array_equal(got, first), (n, force)

@@ -30,7 +30,7 @@ def test_library_exports_every_header_symbol(dgsw_lib):
         assert hasattr(L, n), n
     # the Python binding declares a signature for every exported function
     assert set(names) <= set(dgsw.exported_symbols()) | {"dgsw_stream"}
-    assert L.dgsw_abi_version() == 8
+    assert L.dgsw_abi_version() == 9
 
 
 @pytest.mark.parametrize("n", sorted(int(k) for k in LGL["points_weights"]))

@@ -142,14 +142,71 @@ __device__ __forceinline__ void load_pair(const TaylorLaunch& L, int64_t q, floa
   }
 }
 
-// state[q] += W1 + W2/2 + W3/6 at value q, W3 = (w3h, w3l), in double-float
-__device__ __forceinline__ void step_sum(const TaylorLaunch& L, int64_t q, float w3h, float w3l) {
-  const float2 w1 = L.w1[q], w2 = L.xp[q];
+// A contiguous row of N floats (an x line) moved 16 or 8 bytes at a time
+template <int N>
+__device__ __forceinline__ void load_row(const float* p, float (&x)[N]) {
+  if constexpr (N % 4 == 0) {
+#pragma unroll
+    for (int k = 0; k < N / 4; ++k) {
+      const float4 v = reinterpret_cast<const float4*>(p)[k];
+      x[4 * k] = v.x;
+      x[4 * k + 1] = v.y;
+      x[4 * k + 2] = v.z;
+      x[4 * k + 3] = v.w;
+    }
+  } else if constexpr (N % 2 == 0) {
+#pragma unroll
+    for (int k = 0; k < N / 2; ++k) {
+      const float2 v = reinterpret_cast<const float2*>(p)[k];
+      x[2 * k] = v.x;
+      x[2 * k + 1] = v.y;
+    }
+  } else {
+#pragma unroll
+    for (int i = 0; i < N; ++i) x[i] = p[i];
+  }
+}
+template <int N>
+__device__ __forceinline__ void store_row(float* p, const float (&x)[N]) {
+  if constexpr (N % 4 == 0) {
+#pragma unroll
+    for (int k = 0; k < N / 4; ++k)
+      reinterpret_cast<float4*>(p)[k] = make_float4(x[4 * k], x[4 * k + 1], x[4 * k + 2], x[4 * k + 3]);
+  } else if constexpr (N % 2 == 0) {
+#pragma unroll
+    for (int k = 0; k < N / 2; ++k) reinterpret_cast<float2*>(p)[k] = make_float2(x[2 * k], x[2 * k + 1]);
+  } else {
+#pragma unroll
+    for (int i = 0; i < N; ++i) p[i] = x[i];
+  }
+}
+// a row of N (hi, lo) pairs, two pairs per 16-byte store (even N)
+template <int N>
+__device__ __forceinline__ void store_row_pairs(float2* p, const float (&h)[N], const float (&l)[N]) {
+  if constexpr (N % 2 == 0) {
+#pragma unroll
+    for (int k = 0; k < N / 2; ++k)
+      reinterpret_cast<float4*>(p)[k] = make_float4(h[2 * k], l[2 * k], h[2 * k + 1], l[2 * k + 1]);
+  } else {
+#pragma unroll
+    for (int i = 0; i < N; ++i) p[i] = make_float2(h[i], l[i]);
+  }
+}
+
+// W1 + W2/2 + W3/6 of one value in double-float, W3 = (w3h, w3l), widened
+__device__ __forceinline__ double step_inc(const TaylorLaunch& L, float2 w1, float2 w2, float w3h,
+                                           float w3l) {
   float sh, sl, uh, ul;
   df_mul(w3h, w3l, L.sixth_h, L.sixth_l, uh, ul);        // W3 / 6
   df_add(w1.x, w1.y, 0.5f * w2.x, 0.5f * w2.y, sh, sl);  // W1 + W2 / 2
   df_add(sh, sl, uh, ul, sh, sl);
-  L.l64[q] += widen(sh) + widen(sl);
+  return widen(sh) + widen(sl);
+}
+
+// state[q] += W1 + W2/2 + W3/6 at value q
+__device__ __forceinline__ void step_sum(const TaylorLaunch& L, int64_t q, float w3h, float w3l) {
+  const double v = L.l64[q];
+  L.l64[q] = v + step_inc(L, L.w1[q], L.xp[q], w3h, w3l);
 }
 
 // TR: L^T (else L).  FIRST: x = the FP64 state; otherwise x = W1 or W2
@@ -166,13 +223,57 @@ __global__ void __launch_bounds__(3 * N * N, MINB) taylor_df_kernel(TaylorLaunch
   float2* Sd = reinterpret_cast<float2*>(msm_ + 8 * NP);  // each axis's share of the Pi sum
   float* th = msm_ + 14 * NP;       // split tables of D (D^T), hi
   float* tl = th + TAB;             // and lo
+  constexpr int NT = 3 * NN;  // threads
   const int d = threadIdx.x / NN;
   const int t = threadIdx.x - d * NN;
   const int64_t e = blockIdx.x;
   const int64_t off = e * (int64_t)(kVars * NP);
   const double c = L.dt;
-  for (int q = threadIdx.x; q < 4 * NP; q += 3 * NN) load_pair<FIRST>(L, off + NP + q, Xh[q], Xl[q]);
-  for (int q = threadIdx.x; q < TAB; q += 3 * NN) {
+  const int ta = t % N, tb = t / N;
+  int base, stride;
+  if (d == 0) {
+    base = N * ta + NN * tb;
+    stride = 1;
+  } else if (d == 1) {
+    base = ta + NN * tb;
+    stride = N;
+  } else {
+    base = ta + N * tb;
+    stride = NN;
+  }
+  // the neighbours' values at this line's two face points, loaded first so
+  // that their latency overlaps the staging below
+  float nbh[4], nbl[4];
+  {
+    const int64_t nlo = (int64_t)L.nbr[6 * e + 2 * d] * (kVars * NP);
+    const int64_t nhi = (int64_t)L.nbr[6 * e + 2 * d + 1] * (kVars * NP);
+    const int64_t lo_pt = base + (N - 1) * stride;  // lower neighbour's upper face
+    const int64_t hi_pt = base;                     // upper neighbour's lower face
+    load_pair<FIRST>(L, nlo + NP + lo_pt, nbh[0], nbl[0]);
+    load_pair<FIRST>(L, nlo + (2 + d) * NP + lo_pt, nbh[1], nbl[1]);
+    load_pair<FIRST>(L, nhi + NP + hi_pt, nbh[2], nbl[2]);
+    load_pair<FIRST>(L, nhi + (2 + d) * NP + hi_pt, nbh[3], nbl[3]);
+  }
+  {
+    // the element's Pi and Phi, all of a thread's loads issued before any
+    // is used
+    constexpr int QPT = (4 * NP + NT - 1) / NT;
+    float vh[QPT], vl[QPT];
+#pragma unroll
+    for (int k = 0; k < QPT; ++k) {
+      const int q = threadIdx.x + k * NT;
+      if (q < 4 * NP) load_pair<FIRST>(L, off + NP + q, vh[k], vl[k]);
+    }
+#pragma unroll
+    for (int k = 0; k < QPT; ++k) {
+      const int q = threadIdx.x + k * NT;
+      if (q < 4 * NP) {
+        Xh[q] = vh[k];
+        Xl[q] = vl[k];
+      }
+    }
+  }
+  for (int q = threadIdx.x; q < TAB; q += NT) {
     double v;
     if (q < H * h)
       v = L.eo.A[q / h][q % h];
@@ -188,25 +289,22 @@ __global__ void __launch_bounds__(3 * N * N, MINB) taylor_df_kernel(TaylorLaunch
   const float Fh = __double2float_rn(fd), Fl = __double2float_rn(fd - (double)Fh);
   __syncthreads();
   {
-    const int ta = t % N, tb = t / N;
-    int base, stride;
-    if (d == 0) {
-      base = N * ta + NN * tb;
-      stride = 1;
-    } else if (d == 1) {
-      base = ta + NN * tb;
-      stride = N;
-    } else {
-      base = ta + N * tb;
-      stride = NN;
-    }
     float ph[N], pl[N], fh[N], fl[N];
+    if (d == 0) {
+      // x lines are contiguous rows N floats apart: vector accesses keep the
+      // shared-memory banks from serialising them
+      load_row<N>(Xh + base, ph);
+      load_row<N>(Xl + base, pl);
+      load_row<N>(Xh + NP + base, fh);
+      load_row<N>(Xl + NP + base, fl);
+    } else {
 #pragma unroll
-    for (int i = 0; i < N; ++i) {
-      ph[i] = Xh[base + i * stride];
-      pl[i] = Xl[base + i * stride];
-      fh[i] = Xh[(1 + d) * NP + base + i * stride];
-      fl[i] = Xl[(1 + d) * NP + base + i * stride];
+      for (int i = 0; i < N; ++i) {
+        ph[i] = Xh[base + i * stride];
+        pl[i] = Xl[base + i * stride];
+        fh[i] = Xh[(1 + d) * NP + base + i * stride];
+        fl[i] = Xl[(1 + d) * NP + base + i * stride];
+      }
     }
     float dFh[N], dFl[N], dPh[N], dPl[N];
     eo_line_pairs<N>(fh, fl, dFh, dFl, th, tl);  // D Phi_d : into Pi
@@ -218,26 +316,18 @@ __global__ void __launch_bounds__(3 * N * N, MINB) taylor_df_kernel(TaylorLaunch
     // l_Phi_d) of this element, q' = G (l_Pi,nbr + s l_Phi_d,nbr) of the
     // neighbour; dPi += q - q', dPhi_d += -s (q + q').
     constexpr float K = 0.25f * (float)(N * (N - 1));
-    const int64_t nlo = (int64_t)L.nbr[6 * e + 2 * d] * (kVars * NP);
-    const int64_t nhi = (int64_t)L.nbr[6 * e + 2 * d + 1] * (kVars * NP);
-    const int64_t lo_pt = base + (N - 1) * stride;  // lower neighbour's upper face
-    const int64_t hi_pt = base;                     // upper neighbour's lower face
     {
-      float ah, al, bh, bl, uh, ul, vh, vl, xh, xl;
+      float ah, al, bh, bl, xh, xl;
       // s = -1: a = Pi + Phi_d here; b = the neighbour's Pi -+ Phi_d
       df_add(ph[0], pl[0], fh[0], fl[0], ah, al);
-      load_pair<FIRST>(L, nlo + NP + lo_pt, uh, ul);
-      load_pair<FIRST>(L, nlo + (2 + d) * NP + lo_pt, vh, vl);
-      df_add(uh, ul, TR ? -vh : vh, TR ? -vl : vl, bh, bl);
+      df_add(nbh[0], nbl[0], TR ? -nbh[1] : nbh[1], TR ? -nbl[1] : nbl[1], bh, bl);
       df_add(ah, al, -bh, -bl, xh, xl);
       df_axpy(dFh[0], dFl[0], K, xh, xl);
       if (TR) df_add(ah, al, bh, bl, xh, xl);
       df_axpy(dPh[0], dPl[0], K, xh, xl);
       // s = +1: a = Pi - Phi_d here; b = the neighbour's Pi +- Phi_d
       df_add(ph[N - 1], pl[N - 1], -fh[N - 1], -fl[N - 1], ah, al);
-      load_pair<FIRST>(L, nhi + NP + hi_pt, uh, ul);
-      load_pair<FIRST>(L, nhi + (2 + d) * NP + hi_pt, vh, vl);
-      df_add(uh, ul, TR ? vh : -vh, TR ? vl : -vl, bh, bl);
+      df_add(nbh[2], nbl[2], TR ? nbh[3] : -nbh[3], TR ? nbl[3] : -nbl[3], bh, bl);
       df_add(ah, al, -bh, -bl, xh, xl);
       df_axpy(dFh[N - 1], dFl[N - 1], K, xh, xl);
       if (TR) df_add(ah, al, bh, bl, xh, xl);
@@ -248,22 +338,53 @@ __global__ void __launch_bounds__(3 * N * N, MINB) taylor_df_kernel(TaylorLaunch
       df_mul(dFh[i], dFl[i], Fh, Fl, dFh[i], dFl[i]);
       df_mul(dPh[i], dPl[i], Fh, Fl, dPh[i], dPl[i]);
     }
-    // Phi_d: the increment, or (last launch) the step's sum into the state
-    const int64_t vo = off + (2 + d) * NP + base;
+    // every line read: the Phi_d results replace Phi_d in shared memory, and
+    // the block writes all results out with coalesced accesses below
+    __syncthreads();
+    if (d == 0) {
+      store_row<N>(Xh + NP + base, dPh);
+      store_row<N>(Xl + NP + base, dPl);
+      store_row_pairs<N>(Sd + base, dFh, dFl);
+    } else {
 #pragma unroll
-    for (int i = 0; i < N; ++i) {
-      const int64_t q = vo + i * stride;
-      if (FINAL) {
-        step_sum(L, q, dPh[i], dPl[i]);
-      } else {
-        L.outp[q] = make_float2(dPh[i], dPl[i]);
+      for (int i = 0; i < N; ++i) {
+        Xh[(1 + d) * NP + base + i * stride] = dPh[i];
+        Xl[(1 + d) * NP + base + i * stride] = dPl[i];
+        Sd[d * NP + base + i * stride] = make_float2(dFh[i], dFl[i]);
       }
     }
-#pragma unroll
-    for (int i = 0; i < N; ++i) Sd[d * NP + base + i * stride] = make_float2(dFh[i], dFl[i]);
   }
   __syncthreads();
-  for (int p = threadIdx.x; p < NP; p += 3 * NN) {
+  // Phi: the increments, or (last launch) the step's sums into the state,
+  // with all of a thread's global loads issued before any is used
+  if (FINAL) {
+    constexpr int QPT = (3 * NP + NT - 1) / NT;
+    constexpr int KB = 4;  // loads in flight per thread
+#pragma unroll
+    for (int k0 = 0; k0 < QPT; k0 += KB) {
+      float2 a1[KB], a2[KB];
+      double lv[KB];
+#pragma unroll
+      for (int k = 0; k < KB; ++k) {
+        const int q = NP + threadIdx.x + (k0 + k) * NT;
+        if (k0 + k < QPT && q < 4 * NP) {
+          a1[k] = L.w1[off + NP + q];
+          a2[k] = L.xp[off + NP + q];
+          lv[k] = L.l64[off + NP + q];
+        }
+      }
+#pragma unroll
+      for (int k = 0; k < KB; ++k) {
+        const int q = NP + threadIdx.x + (k0 + k) * NT;
+        if (k0 + k < QPT && q < 4 * NP)
+          L.l64[off + NP + q] = lv[k] + step_inc(L, a1[k], a2[k], Xh[q], Xl[q]);
+      }
+    }
+  } else {
+    for (int q = NP + threadIdx.x; q < 4 * NP; q += NT)
+      L.outp[off + NP + q] = make_float2(Xh[q], Xl[q]);
+  }
+  for (int p = threadIdx.x; p < NP; p += NT) {
     const float2 s0 = Sd[p], s1 = Sd[NP + p], s2 = Sd[2 * NP + p];
     float wh, wl;
     df_add(s0.x, s0.y, s1.x, s1.y, wh, wl);

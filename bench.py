@@ -532,8 +532,10 @@ def time_adjoint(dev):
                           "speedup_vs_fp64": s_grad / s_grad_m},
                 "note": "forward misfit run + hand-written discrete adjoint sweep; the step "
                         "map is linear, so no forward states are stored.  FP64: 3 L^T launches "
-                        "per step (reverse SSP-RK3 stages).  Mixed: mixed forward, and "
-                        "W1 = dt L^T l (double-float), W2, W3 (FP32), l += W1 + W2/2 + W3/6. "
+                        "per step (reverse SSP-RK3 stages).  Mixed: both sweeps as the step's "
+                        "Taylor polynomial, W1 = dt L u, W2 = dt L W1, W3 = dt L W2, "
+                        "u += W1 + W2/2 + W3/6 (L^T backwards), FP64 states and double-float "
+                        "increments formed in FP32 arithmetic (taylor_df.cu). "
                         "Central differences and the tangent-linear run use the FP64 "
                         "objective."}
     finally:

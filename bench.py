@@ -958,6 +958,24 @@ def run_ours(args):
     if mixed is not None and not args.no_full_length and args.elements == ELEMS:
         mixed["full_length"] = config2_full_length(dev)
 
+    # double-float arithmetic on the FP64 state (Taylor form of the step,
+    # taylor_df.cu): FP64-level agreement at FP32-pipe rates
+    double_float = None
+    if not args.no_mixed:
+        from spectre_gb300 import PRECISION_DOUBLE_FLOAT
+        evd, msd, _, stated, _ = time_path(args, PRECISION_DOUBLE_FLOAT, dev, rank, ws, False)
+        evd.close()
+        double_float = {
+            "value": points * 3 * args.steps * ws / (msd * 1e-3), "unit": UNIT,
+            "ms_per_step": msd / args.steps, "speedup_vs_fp64": ms / msd,
+            "rel_l2_vs_fp64_after_steps": float(np.linalg.norm(stated - state64) /
+                                                np.linalg.norm(state64)),
+            "max_abs_vs_fp64_after_steps": float(np.max(np.abs(stated - state64))),
+            "steps_compared": warm + args.steps,
+            "dtype": "double-float (hi + lo f32 pairs, compensated products and sums), "
+                     "f64 state; step as its Taylor polynomial",
+            "launches_per_step": 3}
+
     batched = None
     if not args.no_batched:
         batched = time_batched(args, dev)
@@ -1011,7 +1029,8 @@ def run_ours(args):
                           "note": "FP64 pipe binds the plain path on GB300; peak from a "
                                   "DFMA/DADD throughput probe on this pool's GB300"},
             "autotune": autotune,
-            "mixed": mixed, "batched": batched, "adjoint": adjoint, "curved": curved,
+            "mixed": mixed, "double_float": double_float, "batched": batched, "adjoint": adjoint,
+            "curved": curved,
             "adams": adams, "next_rows": next_rows,
             "cpu_baseline": cpu, "e2e": e2e, "clocks": clocks,
             "gpu_launches": 3 * args.steps,

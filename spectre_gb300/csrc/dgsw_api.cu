@@ -298,6 +298,8 @@ cudaError_t launch_stage(DgswHandle h, const StageLaunch& L) {
 }
 
 bool mixed(DgswHandle h) { return h->cfg.precision == DGSW_PRECISION_MIXED; }
+// double-float arithmetic on an FP64 state (taylor_df.cu)
+bool dfloat(DgswHandle h) { return h->cfg.precision == DGSW_PRECISION_DOUBLE_FLOAT; }
 
 MixedLaunch base_mixed(DgswHandle h) {
   MixedLaunch L;
@@ -806,7 +808,9 @@ cudaError_t mixed_filtered_stage(DgswHandle h, int k, double dt, const double* u
 // (the stage input copied to t1, output to t2: the state is untouched) and
 // keeps the fastest; the choice is cached per (N, elements) for later
 // handles.
-bool tunable(DgswHandle h) { return !mixed(h) && !h->curved && !h->gauss && !h->general; }
+bool tunable(DgswHandle h) {
+  return !mixed(h) && !dfloat(h) && !h->curved && !h->gauss && !h->general;
+}
 
 std::mutex g_tune_mu;
 std::map<std::pair<int, int64_t>, int> g_tuned;
@@ -1169,7 +1173,10 @@ cudaError_t enqueue_mixed_stage(DgswHandle h, int k, double dt, const double* u0
 //   t1 = u + dt L(u); t2 = 3/4 u + 1/4 t1 + dt/4 L(t1);
 //   u  = 1/3 u + 2/3 t2 + 2dt/3 L(t2)   (in place: each element reads only
 //   its own u, neighbours' faces come from t2).
+cudaError_t enqueue_taylor_step(DgswHandle h, double dt, bool transpose);
+
 cudaError_t enqueue_step(DgswHandle h, double dt) {
+  if (dfloat(h)) return enqueue_taylor_step(h, dt, false);
   if (mixed(h) && h->filter_on) {
     cudaError_t e = mixed_filtered_stage(h, 0, dt, h->state, nullptr);
     if (e == cudaSuccess) e = mixed_filtered_stage(h, 1, dt, h->state, nullptr);
@@ -1372,7 +1379,7 @@ cudaError_t capture_adjoint_steps(DgswHandle h, double dt, int steps, cudaGraphE
   if (e != cudaSuccess) return e;
   cudaError_t le = cudaSuccess;
   for (int s = 0; s < steps && le == cudaSuccess; ++s)
-    le = mixed(h) ? enqueue_taylor_step(h, dt, true) : enqueue_adjoint_step(h, dt);
+    le = mixed(h) || dfloat(h) ? enqueue_taylor_step(h, dt, true) : enqueue_adjoint_step(h, dt);
   e = cudaStreamEndCapture(h->stream, &g);
   if (le != cudaSuccess) {
     if (g) cudaGraphDestroy(g);
@@ -1672,8 +1679,8 @@ int adams_step(DgswHandle h, int n_steps, double dt) {
 // other's tails, and the copies of some chunks overlap the stages of others
 // (the host link carries both directions at once).
 bool pipelinable(DgswHandle h) {
-  return !mixed(h) && !h->curved && !h->gauss && !h->general && !h->refined && !h->adams &&
-         !h->filter_on && h->dom.n_elem >= 4096;
+  return !mixed(h) && !dfloat(h) && !h->curved && !h->gauss && !h->general && !h->refined &&
+         !h->adams && !h->filter_on && h->dom.n_elem >= 4096;
 }
 
 // The issue order of the 3 C stage launches (3 c + stage).  The model: the
@@ -2429,6 +2436,13 @@ int dgsw_create(const DgswConfig* cfg, DgswHandle* out) {
     return fail(nullptr, DGSW_ERR_UNSUPPORTED,
                 "Gauss quadrature: flat system, one extent for every element, FP64 precision");
   }
+  if (cfg->precision == DGSW_PRECISION_DOUBLE_FLOAT &&
+      (h->curved || h->refined || h->gauss || !h->dom.uniform || cfg->gamma2 != 0.0 ||
+       cfg->time_stepper != DGSW_STEPPER_RK3_HESTHAVEN_SSP)) {
+    delete h;
+    return fail(nullptr, DGSW_ERR_UNSUPPORTED,
+                "double-float precision: flat system, one extent, gamma2 = 0, Rk3HesthavenSsp");
+  }
 
   if (cfg->time_stepper == DGSW_STEPPER_ADAMS_BASHFORTH) {
     // checked before any device work, so that a bad request fails the same
@@ -2489,6 +2503,11 @@ int dgsw_create(const DgswConfig* cfg, DgswHandle* out) {
   if ((e = cudaMemset(h->state, 0, bytes + pad)) != cudaSuccess) return bail(e, "cudaMemset");
   if ((e = cudaMalloc(&h->dev_err, sizeof(int))) != cudaSuccess) return bail(e, "cudaMalloc err");
   if ((e = cudaMemset(h->dev_err, 0, sizeof(int))) != cudaSuccess) return bail(e, "cudaMemset err");
+  if (cfg->precision == DGSW_PRECISION_DOUBLE_FLOAT) {
+    // the Taylor step's increments W1, W2 as double-float pairs
+    if ((e = cudaMalloc(&h->adj32, 2 * h->dom.offset.back() * sizeof(float2))) != cudaSuccess)
+      return bail(e, "cudaMalloc increments");
+  }
   if (cfg->precision == DGSW_PRECISION_MIXED) {
     if ((e = cudaMalloc(&h->w1, bytes / 2 + pad)) != cudaSuccess) return bail(e, "cudaMalloc w1");
     if ((e = cudaMalloc(&h->w2, bytes / 2 + pad)) != cudaSuccess) return bail(e, "cudaMalloc w2");
@@ -2923,6 +2942,9 @@ int dgsw_substep(DgswHandle h, int k, double dt) {
   if (h->adams)
     return fail(h, DGSW_ERR_UNSUPPORTED, "AdamsBashforth has no substeps; use dgsw_step");
   if (k < 0 || k > 2 || !std::isfinite(dt)) return fail(h, DGSW_ERR_ARGUMENT, "bad substep");
+  if (dfloat(h))
+    return fail(h, DGSW_ERR_UNSUPPORTED,
+                "double-float precision steps the Taylor form, which has no substeps");
   if (int rc = select_device(h)) return rc;
   const size_t bytes = h->dom.offset.back() * sizeof(double);
   if (mixed(h)) {
@@ -3182,6 +3204,8 @@ int dgsw_set_exponential_filter(DgswHandle h, double alpha, int half_power, int 
     return fail(h, DGSW_ERR_ARGUMENT, "need a finite alpha >= 0 and half_power in [0, 64]");
   if (h->gauss)
     return fail(h, DGSW_ERR_UNSUPPORTED, "the filter is built for Gauss-Lobatto meshes");
+  if (dfloat(h))
+    return fail(h, DGSW_ERR_UNSUPPORTED, "the filter is not built for double-float precision");
   if (int rc = select_device(h)) return rc;
   std::vector<double> mats((size_t)(kMaxN + 1) * kMaxN * kMaxN, 0.0);
   for (int n = kMinN; n <= kMaxN; ++n)
@@ -3498,7 +3522,8 @@ int dgsw_adjoint_autotune(DgswHandle h, int force_variant, int* variant, double*
   if (!h) return fail(nullptr, DGSW_ERR_ARGUMENT, "null handle");
   if (force_variant < -1 || force_variant > 1)
     return fail(h, DGSW_ERR_ARGUMENT, "force_variant must be -1, 0 or 1");
-  if (h->general || h->curved || h->gauss || h->refined || mixed(h) || h->cfg.gamma2 != 0.0)
+  if (h->general || h->curved || h->gauss || h->refined || mixed(h) || dfloat(h) ||
+      h->cfg.gamma2 != 0.0)
     return fail(h, DGSW_ERR_UNSUPPORTED,
                 "the FP64 adjoint needs the flat FP64 system, uniform extents and gamma2 = 0");
   if (int rc = select_device(h)) return rc;
@@ -3521,11 +3546,11 @@ int dgsw_misfit_adjoint(DgswHandle h, double* dev_grad) {
   if (h->rec_windows < 1) return fail(h, DGSW_ERR_ARGUMENT, "no recorded misfit run");
   if (int rc = select_device(h)) return rc;
   const size_t bytes = h->dom.offset.back() * sizeof(double);
-  if (mixed(h))
+  if (mixed(h) || dfloat(h))
     if (int rc = taylor_buffers(h)) return rc;
   const int K = h->rec_steps;
   const double dt = h->rec_dt;
-  if (!h->adj_tuned && !mixed(h)) DGSW_CUDA(h, adjoint_autotune(h));
+  if (!h->adj_tuned && !mixed(h) && !dfloat(h)) DGSW_CUDA(h, adjoint_autotune(h));
   if (!(h->graph_adj_dt == dt) || h->graph_adj_steps != K) {
     if (h->graph_adj) cudaGraphExecDestroy(h->graph_adj);
     h->graph_adj = nullptr;

@@ -325,7 +325,8 @@ bool build_domain(const DgswConfig& cfg, Domain* dom, std::string* err) {
     *err = "unsupported time stepper";
     return false;
   }
-  if (cfg.precision != DGSW_PRECISION_FP64 && cfg.precision != DGSW_PRECISION_MIXED) {
+  if (cfg.precision != DGSW_PRECISION_FP64 && cfg.precision != DGSW_PRECISION_MIXED &&
+      cfg.precision != DGSW_PRECISION_DOUBLE_FLOAT) {
     *err = "unknown precision";
     return false;
   }

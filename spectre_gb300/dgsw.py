@@ -39,6 +39,7 @@ STATUS_NAMES = {
 }
 PRECISION_FP64 = 0
 PRECISION_MIXED = 1
+PRECISION_DOUBLE_FLOAT = 2  # FP64 state, double-float (hi + lo FP32) arithmetic
 N_VARS = 5  # Psi, Pi, Phi_x, Phi_y, Phi_z
 N_PACKAGED = 16  # UpwindPenalty dg_package_field_tags doubles per face point
 STAGE_VARIANTS = 4  # DGSW_STAGE_VARIANTS: launch configurations of the FP64 stage

@@ -49,9 +49,24 @@ template <int N>
 struct MShape {
   static constexpr int NN = N * N, NP = N * N * N;
   static constexpr int TAB = Eo<N>::TAB;
-  // floats: X (Pi, Phi as hi and lo), three axis sums as (hi, lo), tables hi, lo
-  static constexpr int SIZE = 8 * NP + 6 * NP + 2 * TAB;
+  // floats: X (Pi, Phi as hi and lo), three axis sums as (hi, lo), tables hi,
+  // lo; rounded to 16 bytes
+  static constexpr int SIZE = (8 * NP + 6 * NP + 2 * TAB + 3) / 4 * 4;
+  // the last launch's prefetch regions (floats): the state block (FP64), W1
+  // and W2's Psi (pairs)
+  static constexpr int PF_EXTRA = 10 * NP + 10 * NP + 2 * NP;
+  static constexpr bool PF_FITS = (SIZE + PF_EXTRA) * 4 <= 200 * 1024;
 };
+
+// 8-byte asynchronous global -> shared copies (cp.async), and the wait for
+// all of this thread's
+__device__ __forceinline__ void cp_async8(void* smem_dst, const void* gsrc) {
+  const unsigned s = (unsigned)__cvta_generic_to_shared(smem_dst);
+  asm volatile("cp.async.ca.shared.global [%0], [%1], 8;\n" ::"r"(s), "l"(gsrc) : "memory");
+}
+__device__ __forceinline__ void cp_async_wait_all() {
+  asm volatile("cp.async.wait_all;\n" ::: "memory");
+}
 
 // double-float helpers: (h, l) with |l| <= ulp(h) / 2
 __device__ __forceinline__ void quick_two_sum(float a, float b, float& s, float& e) {
@@ -241,6 +256,23 @@ __global__ void __launch_bounds__(3 * N * N, MINB) taylor_df_kernel(TaylorLaunch
     base = ta + N * tb;
     stride = NN;
   }
+  // The last launch (where it fits): the values its update reads -- the
+  // state, W1 and (forward) W2's Psi -- copied to shared memory in the
+  // background while the block computes W3 (W2's Pi and Phi are staged
+  // below).
+  constexpr bool PF = FINAL && S::PF_FITS;
+  double* Us = reinterpret_cast<double*>(msm_ + S::SIZE);
+  float2* W1s = reinterpret_cast<float2*>(msm_ + S::SIZE + 10 * NP);
+  float2* W2ps = reinterpret_cast<float2*>(msm_ + S::SIZE + 20 * NP);
+  if (PF) {
+    // the adjoint leaves l_Psi unchanged (its increments' Psi is 0)
+    for (int q = TR ? NP + threadIdx.x : threadIdx.x; q < kVars * NP; q += NT) {
+      cp_async8(Us + q, L.l64 + off + q);
+      cp_async8(W1s + q, L.w1 + off + q);
+    }
+    if (!TR)
+      for (int q = threadIdx.x; q < NP; q += NT) cp_async8(W2ps + q, L.xp + off + q);
+  }
   // the neighbours' values at this line's two face points, loaded first so
   // that their latency overlaps the staging below
   float nbh[4], nbl[4];
@@ -338,9 +370,22 @@ __global__ void __launch_bounds__(3 * N * N, MINB) taylor_df_kernel(TaylorLaunch
       df_mul(dFh[i], dFl[i], Fh, Fl, dFh[i], dFl[i]);
       df_mul(dPh[i], dPl[i], Fh, Fl, dPh[i], dPl[i]);
     }
-    // every line read: the Phi_d results replace Phi_d in shared memory, and
-    // the block writes all results out with coalesced accesses below
+    // every line read: the Phi_d results replace Phi_d in shared memory (the
+    // last launch: the step's sum W1 + W2/2 + W3/6 on the line replaces W2),
+    // and the block writes all results out with coalesced accesses below
+    if (PF) cp_async_wait_all();
     __syncthreads();
+    if (PF) {
+#pragma unroll
+      for (int i = 0; i < N; ++i) {
+        const int q = (1 + d) * NP + base + i * stride;
+        float sh, sl, uh, ul;
+        const float2 w1 = W1s[NP + q];
+        df_mul(dPh[i], dPl[i], L.sixth_h, L.sixth_l, uh, ul);          // W3 / 6
+        df_add(w1.x, w1.y, 0.5f * Xh[q], 0.5f * Xl[q], sh, sl);        // W1 + W2 / 2
+        df_add(sh, sl, uh, ul, dPh[i], dPl[i]);
+      }
+    }
     if (d == 0) {
       store_row<N>(Xh + NP + base, dPh);
       store_row<N>(Xl + NP + base, dPl);
@@ -357,7 +402,10 @@ __global__ void __launch_bounds__(3 * N * N, MINB) taylor_df_kernel(TaylorLaunch
   __syncthreads();
   // Phi: the increments, or (last launch) the step's sums into the state,
   // with all of a thread's global loads issued before any is used
-  if (FINAL) {
+  if (PF) {
+    for (int q = NP + threadIdx.x; q < 4 * NP; q += NT)
+      L.l64[off + NP + q] = Us[NP + q] + (widen(Xh[q]) + widen(Xl[q]));
+  } else if (FINAL) {
     constexpr int QPT = (3 * NP + NT - 1) / NT;
     constexpr int KB = 4;  // loads in flight per thread
 #pragma unroll
@@ -402,7 +450,10 @@ __global__ void __launch_bounds__(3 * N * N, MINB) taylor_df_kernel(TaylorLaunch
     // forward: the Psi increment -c Pi of the input
     float sh = 0.0f, sl = 0.0f;
     if (!TR) df_mul(ch, cl, Xh[p], Xl[p], sh, sl);
-    if (FINAL) {
+    if (PF) {
+      L.l64[q] = Us[NP + p] + step_inc(L, W1s[NP + p], make_float2(Xh[p], Xl[p]), wh, wl);
+      if (!TR) L.l64[off + p] = Us[p] + step_inc(L, W1s[p], W2ps[p], sh, sl);
+    } else if (FINAL) {
       step_sum(L, q, wh, wl);
       if (!TR) step_sum(L, off + p, sh, sl);
     } else {
@@ -413,15 +464,20 @@ __global__ void __launch_bounds__(3 * N * N, MINB) taylor_df_kernel(TaylorLaunch
 }
 
 // resident blocks per SM asked of the register allocator
-template <int N>
+// (N = 8: the non-final kinds stay at 96-102 registers without spills when
+// asked for 2; asked for 3 they spill ~200 bytes.  The final kind, whose
+// shared-memory prefetch allows 3 blocks, measured 2.28 against 2.41 ms per
+// step at 32^3 with 3 and a 176-byte spill.)
+template <int N, bool FINAL>
 constexpr int mixed_minb() {
-  return N <= 4 ? 8 : (N <= 6 ? 4 : (N == 7 ? 3 : (N <= 9 ? 2 : 1)));
+  return N <= 4 ? 8 : (N <= 6 ? 4 : (N == 7 ? 3 : (N == 8 ? (FINAL ? 3 : 2) : (N == 9 ? 2 : 1))));
 }
 
 template <int N, bool TR, bool FIRST, bool FINAL>
 cudaError_t launch_k(const TaylorLaunch& L, cudaStream_t s) {
-  constexpr size_t smem = (size_t)MShape<N>::SIZE * sizeof(float);
-  constexpr auto k = taylor_df_kernel<N, TR, FIRST, FINAL, mixed_minb<N>()>;
+  using S = MShape<N>;
+  constexpr size_t smem = (size_t)(S::SIZE + (FINAL && S::PF_FITS ? S::PF_EXTRA : 0)) * sizeof(float);
+  constexpr auto k = taylor_df_kernel<N, TR, FIRST, FINAL, mixed_minb<N, FINAL>()>;
   cudaError_t err = set_kernel_smem<k>((int)smem, true);
   if (err != cudaSuccess) return err;
   TaylorLaunch A = L;

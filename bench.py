@@ -481,7 +481,7 @@ def _time_gradient(p, psi0, reps=3):
     return J, g, s_per_grad, (time.perf_counter() - t0) / reps
 
 
-def time_adjoint(dev):
+def time_adjoint(dev, steps=2000):
     """The adjoint case: 8^3 elements x 8^3 points, dt 5e-4, 2000 SSP-RK3 steps, 64
     samples every 10 steps; seconds per gradient (forward misfit run + the
     discrete adjoint sweep) in FP64 and in mixed precision (FP64 states, FP32
@@ -490,8 +490,8 @@ def time_adjoint(dev):
     gradient's error against the FP64 one."""
     import torch
     from spectre_gb300.adjoint import MisfitProblem
-    p = MisfitProblem(device=dev)
-    pm = MisfitProblem(device=dev, precision="mixed")
+    p = MisfitProblem(device=dev, steps=steps)
+    pm = MisfitProblem(device=dev, steps=steps, precision="mixed")
     try:
         psi0 = p.initial_psi()
         J, g, s_grad, s_fwd = _time_gradient(p, psi0)
@@ -513,7 +513,8 @@ def time_adjoint(dev):
         mixed_max = float((gm - g).abs().max()) / float(g.abs().max())
         mixed_l2 = float(torch.linalg.norm(gm - g)) / float(torch.linalg.norm(g))
         return {"workload": "ScalarWave 8^3 elements x 8^3 LGL points, SSP-RK3 dt=5e-4, "
-                            "2000 steps, 64 seeded samples of Psi every 10 steps; control Psi(t=0)",
+                            "%d steps, 64 seeded samples of Psi every 10 steps; control Psi(t=0)"
+                            % steps,
                 "s_per_grad": s_grad_m, "s_per_grad_precision": "mixed",
                 "fp64": {"s_per_grad": s_grad, "s_forward": s_fwd,
                          "s_adjoint_sweep": s_grad - s_fwd, "J": J,
@@ -1064,6 +1065,15 @@ def main():
     ap.add_argument("--batched-only", action="store_true",
                     help="run only the 256-instance mixed-extent workload and print its "
                          "numbers (for profiling captures)")
+    ap.add_argument("--adjoint-only", action="store_true",
+                    help="run only the misfit-gradient workload (FP64 and mixed) and print its "
+                         "numbers (for profiling captures)")
+    ap.add_argument("--adjoint-steps", type=int, default=2000,
+                    help="SSP-RK3 steps of the misfit-gradient workload (default 2000; fewer "
+                         "only for profiling captures)")
+    ap.add_argument("--double-float-only", action="store_true",
+                    help="run only the double-float path on the --elements cube and print its "
+                         "numbers (for profiling captures)")
     ap.add_argument("--no-full-length", action="store_true",
                     help="skip the accuracy runs over the configured step counts (500 steps "
                          "of the 32^3 case, 300 of the 256-instance case)")
@@ -1091,6 +1101,23 @@ def main():
         import torch
         torch.cuda.set_device(0)
         print(json.dumps(time_batched(args, 0)), flush=True)
+        return 0
+    if args.adjoint_only:
+        import torch
+        torch.cuda.set_device(0)
+        print(json.dumps(time_adjoint(0, args.adjoint_steps)), flush=True)
+        return 0
+    if args.double_float_only:
+        import torch
+        from spectre_gb300 import PRECISION_DOUBLE_FLOAT
+        torch.cuda.set_device(0)
+        ev, ms, _, _, _ = time_path(args, PRECISION_DOUBLE_FLOAT, 0, 0, 1, False)
+        pts = ev.grid_points
+        ev.close()
+        print(json.dumps({"precision": "double_float", "elements_per_axis": args.elements,
+                          "ms_per_step": ms / args.steps,
+                          "value": pts * 3 * args.steps / (ms * 1e-3), "unit": UNIT}),
+              flush=True)
         return 0
     return run_ours(args)
 

@@ -163,6 +163,29 @@ def test_adams_configs_rejected_before_any_device_work(dgsw_lib):
             L.dgsw_destroy(h)
 
 
+def test_double_float_configs_checked_before_any_device_work(dgsw_lib):
+    # double-float precision: flat, one extent, gamma2 = 0, SSP-RK3; other
+    # requests fail as unsupported, with or without a GPU
+    import ctypes
+    L = dgsw_lib.lib()
+    E = 2 * 2 * 2
+
+    def create(points=4, **kw):
+        holder = dgsw._ConfigHolder([dgsw.Brick((2, 2, 2))], points,
+                                    precision=dgsw.PRECISION_DOUBLE_FLOAT, **kw)
+        h = ctypes.c_void_p()
+        return L.dgsw_create(ctypes.byref(holder.cfg), ctypes.byref(h)), h
+
+    for bad in (dict(gamma2=1.0), dict(points=[4] * (E - 1) + [5]),
+                dict(time_stepper="adams_bashforth")):
+        rc, _ = create(**bad)
+        assert rc == -3 and b"double-float" in L.dgsw_last_error(None), bad
+    rc, h = create()
+    assert rc in (0, -5)  # ok with a GPU, no device without one
+    if rc == 0:
+        L.dgsw_destroy(h)
+
+
 # ---------------- curved shell: maps and geometry against the oracle ----------------
 
 SHELLS = [dict(ref_ang=0, ref_rad=0, n=4), dict(ref_ang=1, ref_rad=2, n=5),

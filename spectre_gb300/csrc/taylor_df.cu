@@ -321,55 +321,79 @@ __global__ void __launch_bounds__(3 * N * N, MINB) taylor_df_kernel(TaylorLaunch
   const float Fh = __double2float_rn(fd), Fl = __double2float_rn(fd - (double)Fh);
   __syncthreads();
   {
-    float ph[N], pl[N], fh[N], fl[N];
-    if (d == 0) {
-      // x lines are contiguous rows N floats apart: vector accesses keep the
-      // shared-memory banks from serialising them
-      load_row<N>(Xh + base, ph);
-      load_row<N>(Xl + base, pl);
-      load_row<N>(Xh + NP + base, fh);
-      load_row<N>(Xl + NP + base, fl);
-    } else {
-#pragma unroll
-      for (int i = 0; i < N; ++i) {
-        ph[i] = Xh[base + i * stride];
-        pl[i] = Xl[base + i * stride];
-        fh[i] = Xh[(1 + d) * NP + base + i * stride];
-        fl[i] = Xl[(1 + d) * NP + base + i * stride];
-      }
-    }
-    float dFh[N], dFl[N], dPh[N], dPl[N];
-    eo_line_pairs<N>(fh, fl, dFh, dFl, th, tl);  // D Phi_d : into Pi
-    eo_line_pairs<N>(ph, pl, dPh, dPl, th, tl);  // D Pi    : into Phi_d
     // UpwindPenalty at both ends of the line, lifted with G = fd K, K =
     // N(N-1)/4: the sums are formed unscaled, then scaled.  Forward
     // (stage_fp64.cu): dw = w_int - w_ext, w = Pi - s Phi_d, dPi += G dw,
     // dPhi_d += -s G dw.  Transposed (adjoint_fp64.cu): q = G (l_Pi - s
     // l_Phi_d) of this element, q' = G (l_Pi,nbr + s l_Phi_d,nbr) of the
-    // neighbour; dPi += q - q', dPhi_d += -s (q + q').
+    // neighbour; dPi += q - q', dPhi_d += -s (q + q').  The Phi_d line is
+    // differentiated first and its result leaves registers (into Sd) before
+    // the Pi line's: fewer live registers, more resident blocks.
     constexpr float K = 0.25f * (float)(N * (N - 1));
+    float e0h, e0l, e1h, e1l;  // the dF face terms: a - b at both ends
+    float g0h, g0l, g1h, g1l;  // the dP face terms (a - b forward, a + b transposed)
+    float ph[N], pl[N];
     {
-      float ah, al, bh, bl, xh, xl;
-      // s = -1: a = Pi + Phi_d here; b = the neighbour's Pi -+ Phi_d
-      df_add(ph[0], pl[0], fh[0], fl[0], ah, al);
-      df_add(nbh[0], nbl[0], TR ? -nbh[1] : nbh[1], TR ? -nbl[1] : nbl[1], bh, bl);
-      df_add(ah, al, -bh, -bl, xh, xl);
-      df_axpy(dFh[0], dFl[0], K, xh, xl);
-      if (TR) df_add(ah, al, bh, bl, xh, xl);
-      df_axpy(dPh[0], dPl[0], K, xh, xl);
-      // s = +1: a = Pi - Phi_d here; b = the neighbour's Pi +- Phi_d
-      df_add(ph[N - 1], pl[N - 1], -fh[N - 1], -fl[N - 1], ah, al);
-      df_add(nbh[2], nbl[2], TR ? nbh[3] : -nbh[3], TR ? nbl[3] : -nbl[3], bh, bl);
-      df_add(ah, al, -bh, -bl, xh, xl);
-      df_axpy(dFh[N - 1], dFl[N - 1], K, xh, xl);
-      if (TR) df_add(ah, al, bh, bl, xh, xl);
-      df_axpy(dPh[N - 1], dPl[N - 1], -K, xh, xl);
-    }
+      float fh[N], fl[N];
+      if (d == 0) {
+        // x lines are contiguous rows N floats apart: vector accesses keep
+        // the shared-memory banks from serialising them
+        load_row<N>(Xh + base, ph);
+        load_row<N>(Xl + base, pl);
+        load_row<N>(Xh + NP + base, fh);
+        load_row<N>(Xl + NP + base, fl);
+      } else {
 #pragma unroll
-    for (int i = 0; i < N; ++i) {
-      df_mul(dFh[i], dFl[i], Fh, Fl, dFh[i], dFl[i]);
-      df_mul(dPh[i], dPl[i], Fh, Fl, dPh[i], dPl[i]);
+        for (int i = 0; i < N; ++i) {
+          ph[i] = Xh[base + i * stride];
+          pl[i] = Xl[base + i * stride];
+          fh[i] = Xh[(1 + d) * NP + base + i * stride];
+          fl[i] = Xl[(1 + d) * NP + base + i * stride];
+        }
+      }
+      {
+        float ah, al, bh, bl;
+        // s = -1: a = Pi + Phi_d here; b = the neighbour's Pi -+ Phi_d
+        df_add(ph[0], pl[0], fh[0], fl[0], ah, al);
+        df_add(nbh[0], nbl[0], TR ? -nbh[1] : nbh[1], TR ? -nbl[1] : nbl[1], bh, bl);
+        df_add(ah, al, -bh, -bl, e0h, e0l);
+        if (TR) {
+          df_add(ah, al, bh, bl, g0h, g0l);
+        } else {
+          g0h = e0h;
+          g0l = e0l;
+        }
+        // s = +1: a = Pi - Phi_d here; b = the neighbour's Pi +- Phi_d
+        df_add(ph[N - 1], pl[N - 1], -fh[N - 1], -fl[N - 1], ah, al);
+        df_add(nbh[2], nbl[2], TR ? nbh[3] : -nbh[3], TR ? nbl[3] : -nbl[3], bh, bl);
+        df_add(ah, al, -bh, -bl, e1h, e1l);
+        if (TR) {
+          df_add(ah, al, bh, bl, g1h, g1l);
+        } else {
+          g1h = e1h;
+          g1l = e1l;
+        }
+      }
+      float dFh[N], dFl[N];
+      eo_line_pairs<N>(fh, fl, dFh, dFl, th, tl);  // D Phi_d : into Pi
+      df_axpy(dFh[0], dFl[0], K, e0h, e0l);
+      df_axpy(dFh[N - 1], dFl[N - 1], K, e1h, e1l);
+#pragma unroll
+      for (int i = 0; i < N; ++i) df_mul(dFh[i], dFl[i], Fh, Fl, dFh[i], dFl[i]);
+      // this axis's share of the Pi sum (Sd is read after the last barrier)
+      if (d == 0) {
+        store_row_pairs<N>(Sd + base, dFh, dFl);
+      } else {
+#pragma unroll
+        for (int i = 0; i < N; ++i) Sd[d * NP + base + i * stride] = make_float2(dFh[i], dFl[i]);
+      }
     }
+    float dPh[N], dPl[N];
+    eo_line_pairs<N>(ph, pl, dPh, dPl, th, tl);  // D Pi : into Phi_d
+    df_axpy(dPh[0], dPl[0], K, g0h, g0l);
+    df_axpy(dPh[N - 1], dPl[N - 1], -K, g1h, g1l);
+#pragma unroll
+    for (int i = 0; i < N; ++i) df_mul(dPh[i], dPl[i], Fh, Fl, dPh[i], dPl[i]);
     // every line read: the Phi_d results replace Phi_d in shared memory (the
     // last launch: the step's sum W1 + W2/2 + W3/6 on the line replaces W2),
     // and the block writes all results out with coalesced accesses below
@@ -389,13 +413,11 @@ __global__ void __launch_bounds__(3 * N * N, MINB) taylor_df_kernel(TaylorLaunch
     if (d == 0) {
       store_row<N>(Xh + NP + base, dPh);
       store_row<N>(Xl + NP + base, dPl);
-      store_row_pairs<N>(Sd + base, dFh, dFl);
     } else {
 #pragma unroll
       for (int i = 0; i < N; ++i) {
         Xh[(1 + d) * NP + base + i * stride] = dPh[i];
         Xl[(1 + d) * NP + base + i * stride] = dPl[i];
-        Sd[d * NP + base + i * stride] = make_float2(dFh[i], dFl[i]);
       }
     }
   }
@@ -464,13 +486,12 @@ __global__ void __launch_bounds__(3 * N * N, MINB) taylor_df_kernel(TaylorLaunch
 }
 
 // resident blocks per SM asked of the register allocator
-// (N = 8: the non-final kinds stay at 96-102 registers without spills when
-// asked for 2; asked for 3 they spill ~200 bytes.  The final kind, whose
-// shared-memory prefetch allows 3 blocks, measured 2.28 against 2.41 ms per
-// step at 32^3 with 3 and a 176-byte spill.)
+// (N = 8: with the Phi_d line finished before the Pi line, the non-final
+// kinds fit 80 registers, 4 blocks per SM; the final kind, whose
+// shared-memory prefetch allows 3 blocks, 91-93.)
 template <int N, bool FINAL>
 constexpr int mixed_minb() {
-  return N <= 4 ? 8 : (N <= 6 ? 4 : (N == 7 ? 3 : (N == 8 ? (FINAL ? 3 : 2) : (N == 9 ? 2 : 1))));
+  return N <= 4 ? 8 : (N <= 6 ? 4 : (N == 7 ? 3 : (N == 8 ? (FINAL ? 3 : 4) : (N == 9 ? 2 : 1))));
 }
 
 template <int N, bool TR, bool FIRST, bool FINAL>

@@ -10,7 +10,8 @@ double-float increments keep ~44 bits, so the measured differences are
 import numpy as np
 import pytest
 
-from spectre_gb300.dgsw import PRECISION_DOUBLE_FLOAT, PRECISION_FP64, Brick, DgEvolution, DgswError
+from spectre_gb300.dgsw import (PRECISION_DOUBLE_FLOAT, PRECISION_FP64, Brick, DgEvolution,
+                                DgswError)
 
 from test_gpu_parity_fp64 import RTOL, random_state, rel_err_per_var
 
@@ -90,7 +91,6 @@ def test_refusals():
 def test_misfit_gradient_matches_fp64():
     # a double-float handle runs the misfit forward and adjoint sweep on the
     # same Taylor kernels as the mixed-precision problem
-    import torch
     from spectre_gb300.adjoint import MisfitProblem
     kw = dict(elements=(4, 4, 4), points=6, dt=1e-3, steps=40, steps_per_window=10,
               n_samples=12, seed=5)
@@ -107,3 +107,17 @@ def test_misfit_gradient_matches_fp64():
         assert float((g - g64).abs().max()) <= 1e-10 * float(g64.abs().max())
     finally:
         pd.close()
+
+
+def test_step_host_equals_device_steps():
+    # the host-state call on a double-float handle: whole-state copies around
+    # the same device steps, bit-identical to set_state + step + get_state
+    bricks = [Brick((3, 3, 2))]
+    n, dt = 6, 1e-3
+    u = np.random.default_rng(3).uniform(-1, 1, 18 * 5 * n ** 3)
+    with DgEvolution(bricks, n, precision=PRECISION_DOUBLE_FLOAT) as ev:
+        ev.set_state(u)
+        ev.step(4, dt)
+        ref = ev.get_state()
+        got = ev.step_host(u.copy(), 4, dt)
+    np.testing.assert_array_equal(got, ref)

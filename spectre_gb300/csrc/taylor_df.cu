@@ -226,8 +226,11 @@ __device__ __forceinline__ void step_sum(const TaylorLaunch& L, int64_t q, float
 
 // TR: L^T (else L).  FIRST: x = the FP64 state; otherwise x = W1 or W2
 // (pairs).  FINAL: W3 = dt L W2 stays in registers and the state takes
-// W1 + W2/2 + W3/6; otherwise out = dt L x.
-template <int N, bool TR, bool FIRST, bool FINAL, int MINB>
+// W1 + W2/2 + W3/6; otherwise out = dt L x.  LW (grids of at most a few
+// blocks per SM, final launch): the state is not prefetched, so that the
+// block's shared memory allows one more resident block and the whole grid
+// runs in one wave.
+template <int N, bool TR, bool FIRST, bool FINAL, int MINB, bool LW = false>
 __global__ void __launch_bounds__(3 * N * N, MINB) taylor_df_kernel(TaylorLaunch L) {
   using S = MShape<N>;
   constexpr int NN = S::NN, NP = S::NP, TAB = S::TAB;
@@ -261,13 +264,14 @@ __global__ void __launch_bounds__(3 * N * N, MINB) taylor_df_kernel(TaylorLaunch
   // background while the block computes W3 (W2's Pi and Phi are staged
   // below).
   constexpr bool PF = FINAL && S::PF_FITS;
+  constexpr bool PFU = PF && !LW;  // the state prefetched too
   double* Us = reinterpret_cast<double*>(msm_ + S::SIZE);
-  float2* W1s = reinterpret_cast<float2*>(msm_ + S::SIZE + 10 * NP);
-  float2* W2ps = reinterpret_cast<float2*>(msm_ + S::SIZE + 20 * NP);
+  float2* W1s = reinterpret_cast<float2*>(msm_ + S::SIZE + (PFU ? 10 * NP : 0));
+  float2* W2ps = reinterpret_cast<float2*>(msm_ + S::SIZE + (PFU ? 20 * NP : 10 * NP));
   if (PF) {
     // the adjoint leaves l_Psi unchanged (its increments' Psi is 0)
     for (int q = TR ? NP + threadIdx.x : threadIdx.x; q < kVars * NP; q += NT) {
-      cp_async8(Us + q, L.l64 + off + q);
+      if (PFU) cp_async8(Us + q, L.l64 + off + q);
       cp_async8(W1s + q, L.w1 + off + q);
     }
     if (!TR)
@@ -424,9 +428,27 @@ __global__ void __launch_bounds__(3 * N * N, MINB) taylor_df_kernel(TaylorLaunch
   __syncthreads();
   // Phi: the increments, or (last launch) the step's sums into the state,
   // with all of a thread's global loads issued before any is used
-  if (PF) {
+  if (PFU) {
     for (int q = NP + threadIdx.x; q < 4 * NP; q += NT)
       L.l64[off + NP + q] = Us[NP + q] + (widen(Xh[q]) + widen(Xl[q]));
+  } else if (PF) {
+    constexpr int QPT = (3 * NP + NT - 1) / NT;
+    constexpr int KB = 4;  // loads in flight per thread
+#pragma unroll
+    for (int k0 = 0; k0 < QPT; k0 += KB) {
+      double lv[KB];
+#pragma unroll
+      for (int k = 0; k < KB; ++k) {
+        const int q = NP + threadIdx.x + (k0 + k) * NT;
+        if (k0 + k < QPT && q < 4 * NP) lv[k] = L.l64[off + NP + q];
+      }
+#pragma unroll
+      for (int k = 0; k < KB; ++k) {
+        const int q = NP + threadIdx.x + (k0 + k) * NT;
+        if (k0 + k < QPT && q < 4 * NP)
+          L.l64[off + NP + q] = lv[k] + (widen(Xh[q]) + widen(Xl[q]));
+      }
+    }
   } else if (FINAL) {
     constexpr int QPT = (3 * NP + NT - 1) / NT;
     constexpr int KB = 4;  // loads in flight per thread
@@ -473,8 +495,12 @@ __global__ void __launch_bounds__(3 * N * N, MINB) taylor_df_kernel(TaylorLaunch
     float sh = 0.0f, sl = 0.0f;
     if (!TR) df_mul(ch, cl, Xh[p], Xl[p], sh, sl);
     if (PF) {
-      L.l64[q] = Us[NP + p] + step_inc(L, W1s[NP + p], make_float2(Xh[p], Xl[p]), wh, wl);
-      if (!TR) L.l64[off + p] = Us[p] + step_inc(L, W1s[p], W2ps[p], sh, sl);
+      const double u1 = PFU ? Us[NP + p] : L.l64[q];
+      L.l64[q] = u1 + step_inc(L, W1s[NP + p], make_float2(Xh[p], Xl[p]), wh, wl);
+      if (!TR) {
+        const double u0 = PFU ? Us[p] : L.l64[off + p];
+        L.l64[off + p] = u0 + step_inc(L, W1s[p], W2ps[p], sh, sl);
+      }
     } else if (FINAL) {
       step_sum(L, q, wh, wl);
       if (!TR) step_sum(L, off + p, sh, sl);
@@ -499,11 +525,23 @@ constexpr int mixed_minb() {
                                               : (N == 9 ? 3 : (N <= 11 ? 2 : 1)))));
 }
 
-template <int N, bool TR, bool FIRST, bool FINAL>
+// multiprocessors of the current device (cached per device)
+int sm_count() {
+  static int cached[64] = {};
+  int dev = 0;
+  if (cudaGetDevice(&dev) != cudaSuccess || dev < 0 || dev >= 64) return 0;
+  if (cached[dev] == 0) cudaDeviceGetAttribute(&cached[dev], cudaDevAttrMultiProcessorCount, dev);
+  return cached[dev];
+}
+
+template <int N, bool TR, bool FIRST, bool FINAL, bool LW = false>
 cudaError_t launch_k(const TaylorLaunch& L, cudaStream_t s) {
   using S = MShape<N>;
-  constexpr size_t smem = (size_t)(S::SIZE + (FINAL && S::PF_FITS ? S::PF_EXTRA : 0)) * sizeof(float);
-  constexpr auto k = taylor_df_kernel<N, TR, FIRST, FINAL, mixed_minb<N, FINAL>()>;
+  constexpr int pf = FINAL && S::PF_FITS ? (LW ? S::PF_EXTRA - 10 * S::NP : S::PF_EXTRA) : 0;
+  constexpr size_t smem = (size_t)(S::SIZE + pf) * sizeof(float);
+  // LW at N = 8: 53 KB of shared memory and 80 registers, 4 blocks per SM
+  constexpr int minb = LW && N == 8 ? 4 : mixed_minb<N, FINAL>();
+  constexpr auto k = taylor_df_kernel<N, TR, FIRST, FINAL, minb, LW>;
   cudaError_t err = set_kernel_smem<k>((int)smem, true);
   if (err != cudaSuccess) return err;
   TaylorLaunch A = L;
@@ -519,7 +557,13 @@ cudaError_t launch_kind(const TaylorLaunch& L, cudaStream_t s) {
   switch (L.kind) {
     case 0: return launch_k<N, TR, true, false>(L, s);
     case 1: return launch_k<N, TR, false, false>(L, s);
-    case 2: return launch_k<N, TR, false, true>(L, s);
+    case 2:
+      // a grid that fits one wave with the smaller final-launch footprint
+      if constexpr (N == 8) {
+        const int sms = sm_count();
+        if (sms > 0 && L.n_elem <= (int64_t)4 * sms) return launch_k<N, TR, false, true, true>(L, s);
+      }
+      return launch_k<N, TR, false, true>(L, s);
     default: return cudaErrorInvalidValue;
   }
 }

@@ -226,10 +226,9 @@ __device__ __forceinline__ void step_sum(const TaylorLaunch& L, int64_t q, float
 
 // TR: L^T (else L).  FIRST: x = the FP64 state; otherwise x = W1 or W2
 // (pairs).  FINAL: W3 = dt L W2 stays in registers and the state takes
-// W1 + W2/2 + W3/6; otherwise out = dt L x.  LW (grids of at most a few
-// blocks per SM, final launch): the state is not prefetched, so that the
-// block's shared memory allows one more resident block and the whole grid
-// runs in one wave.
+// W1 + W2/2 + W3/6; otherwise out = dt L x.  LW (final launch): the state
+// is not prefetched, so that the block's shared memory allows one more
+// resident block; its loads are issued in batches in the epilogue.
 template <int N, bool TR, bool FIRST, bool FINAL, int MINB, bool LW = false>
 __global__ void __launch_bounds__(3 * N * N, MINB) taylor_df_kernel(TaylorLaunch L) {
   using S = MShape<N>;
@@ -525,15 +524,6 @@ constexpr int mixed_minb() {
                                               : (N == 9 ? 3 : (N <= 11 ? 2 : 1)))));
 }
 
-// multiprocessors of the current device (cached per device)
-int sm_count() {
-  static int cached[64] = {};
-  int dev = 0;
-  if (cudaGetDevice(&dev) != cudaSuccess || dev < 0 || dev >= 64) return 0;
-  if (cached[dev] == 0) cudaDeviceGetAttribute(&cached[dev], cudaDevAttrMultiProcessorCount, dev);
-  return cached[dev];
-}
-
 template <int N, bool TR, bool FIRST, bool FINAL, bool LW = false>
 cudaError_t launch_k(const TaylorLaunch& L, cudaStream_t s) {
   using S = MShape<N>;
@@ -558,11 +548,9 @@ cudaError_t launch_kind(const TaylorLaunch& L, cudaStream_t s) {
     case 0: return launch_k<N, TR, true, false>(L, s);
     case 1: return launch_k<N, TR, false, false>(L, s);
     case 2:
-      // a grid that fits one wave with the smaller final-launch footprint
-      if constexpr (N == 8) {
-        const int sms = sm_count();
-        if (sms > 0 && L.n_elem <= (int64_t)4 * sms) return launch_k<N, TR, false, true, true>(L, s);
-      }
+      // N = 8: the final launch without the state's prefetch (4 blocks per
+      // SM) measured faster on both the 512-element and the 32^3 grid
+      if constexpr (N == 8) return launch_k<N, TR, false, true, true>(L, s);
       return launch_k<N, TR, false, true>(L, s);
     default: return cudaErrorInvalidValue;
   }

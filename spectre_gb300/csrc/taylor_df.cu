@@ -512,15 +512,17 @@ __global__ void __launch_bounds__(3 * N * N, MINB) taylor_df_kernel(TaylorLaunch
 
 // resident blocks per SM asked of the register allocator
 // (N = 8: with the Phi_d line finished before the Pi line, the non-final
-// kinds fit 80 registers, 4 blocks per SM; the final kind, whose
-// shared-memory prefetch allows 3 blocks, 91-93.  N = 9: 80 registers; 10:
+// kinds fit 80 registers without a spill (4 blocks per SM) or 64 with a
+// 28-44 byte spill (5 blocks per SM: 1.80 against 1.90 ms per double-float
+// step at 32^3); the final kind, whose shared-memory prefetch allows 3
+// blocks, 91-93.  N = 9: 80 registers; 10:
 // 96; 11: 80 with a 72-92 byte spill; 12: ~120.)
 template <int N, bool FINAL>
 constexpr int mixed_minb() {
   return N <= 4 ? 8
                 : (N <= 6 ? 4
                           : (N == 7 ? 3
-                                    : (N == 8 ? (FINAL ? 3 : 4)
+                                    : (N == 8 ? (FINAL ? 3 : 5)
                                               : (N == 9 ? 3 : (N <= 11 ? 2 : 1)))));
 }
 

@@ -1,5 +1,7 @@
-// taylor_df.cu -- the plain DG step and its discrete adjoint in mixed
-// precision: FP64 states, double-float increments formed with FP32 arithmetic.
+// taylor_df.cu -- the plain DG step and its discrete adjoint with FP64
+// states and double-float increments formed with FP32 arithmetic: the step of
+// DGSW_PRECISION_DOUBLE_FLOAT handles, and both sweeps of the misfit gradient
+// on mixed-precision and double-float handles.
 //
 // The operator L of the flat ScalarWave system with gamma2 = 0 is linear and
 // does not change in time, so one Rk3HesthavenSsp step (Rk3HesthavenSsp.cpp:

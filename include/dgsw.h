@@ -76,8 +76,8 @@ typedef enum {
  * taken as its Taylor polynomial (identical to Rk3HesthavenSsp for this
  * linear, time-independent operator) and added to the FP64 state once per
  * step; results agree with FP64 to ~1e-14 relative.  Flat system, one brick
- * set of one extent, gamma2 = 0, Rk3HesthavenSsp, no filter; dgsw_substep is
- * not available (the Taylor form has no substeps). */
+ * set of one extent (gamma2 general), Rk3HesthavenSsp, no filter;
+ * dgsw_substep is not available (the Taylor form has no substeps). */
 typedef enum {
   DGSW_PRECISION_FP64 = 0,
   DGSW_PRECISION_MIXED = 1,

@@ -1354,6 +1354,7 @@ cudaError_t enqueue_taylor_step(DgswHandle h, double dt, bool transpose) {
   A.nbr = h->nbr;
   A.jac = h->jac;
   A.eo = transpose ? h->eoT : h->eo;
+  A.gamma2 = transpose ? 0.0 : h->cfg.gamma2;
   A.kind = 0;
   A.x64 = u;
   A.outp = w1;
@@ -2437,11 +2438,11 @@ int dgsw_create(const DgswConfig* cfg, DgswHandle* out) {
                 "Gauss quadrature: flat system, one extent for every element, FP64 precision");
   }
   if (cfg->precision == DGSW_PRECISION_DOUBLE_FLOAT &&
-      (h->curved || h->refined || h->gauss || !h->dom.uniform || cfg->gamma2 != 0.0 ||
+      (h->curved || h->refined || h->gauss || !h->dom.uniform ||
        cfg->time_stepper != DGSW_STEPPER_RK3_HESTHAVEN_SSP)) {
     delete h;
     return fail(nullptr, DGSW_ERR_UNSUPPORTED,
-                "double-float precision: flat system, one extent, gamma2 = 0, Rk3HesthavenSsp");
+                "double-float precision: flat system, one extent, Rk3HesthavenSsp");
   }
 
   if (cfg->time_stepper == DGSW_STEPPER_ADAMS_BASHFORTH) {

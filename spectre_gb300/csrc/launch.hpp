@@ -373,8 +373,11 @@ struct TaylorLaunch {
   const int32_t* nbr = nullptr;
   const double* jac = nullptr;
   EoTable eo{};
+  double gamma2 = 0.0;  // forward only: ScalarWave's constraint damping
 };
 cudaError_t launch_taylor_df(const TaylorLaunch& L, cudaStream_t s);
+// the gamma2 != 0 kernels (taylor_df_g2.cu); launch_taylor_df calls it
+cudaError_t launch_taylor_df_g2(const TaylorLaunch& L, cudaStream_t s);
 // Psi at sample points: out[s] = sample - target[s] (target may be null).
 cudaError_t launch_sample(const double* u, int n_samples, int n, const int64_t* elem_off,
                           const double* w, const double* target, double* out, cudaStream_t s);

@@ -164,8 +164,8 @@ def test_adams_configs_rejected_before_any_device_work(dgsw_lib):
 
 
 def test_double_float_configs_checked_before_any_device_work(dgsw_lib):
-    # double-float precision: flat, one extent, gamma2 = 0, SSP-RK3; other
-    # requests fail as unsupported, with or without a GPU
+    # double-float precision: flat, one extent, SSP-RK3; other requests fail
+    # as unsupported, with or without a GPU
     import ctypes
     L = dgsw_lib.lib()
     E = 2 * 2 * 2
@@ -176,14 +176,14 @@ def test_double_float_configs_checked_before_any_device_work(dgsw_lib):
         h = ctypes.c_void_p()
         return L.dgsw_create(ctypes.byref(holder.cfg), ctypes.byref(h)), h
 
-    for bad in (dict(gamma2=1.0), dict(points=[4] * (E - 1) + [5]),
-                dict(time_stepper="adams_bashforth")):
+    for bad in (dict(points=[4] * (E - 1) + [5]), dict(time_stepper="adams_bashforth")):
         rc, _ = create(**bad)
         assert rc == -3 and b"double-float" in L.dgsw_last_error(None), bad
-    rc, h = create()
-    assert rc in (0, -5)  # ok with a GPU, no device without one
-    if rc == 0:
-        L.dgsw_destroy(h)
+    for ok in (dict(), dict(gamma2=1.5)):
+        rc, h = create(**ok)
+        assert rc in (0, -5)  # ok with a GPU, no device without one
+        if rc == 0:
+            L.dgsw_destroy(h)
 
 
 # ---------------- curved shell: maps and geometry against the oracle ----------------

@@ -487,12 +487,13 @@ int dgsw_amr_project_device(DgswHandle h, int n_vars, int64_t n_in, const int64_
  * reverse sweep needs only the recorded residuals, not the forward states.
  * FP64 handles run dgsw_step forward and the FP64 adjoint (three L^T
  * launches per step, the reverse stages of Rk3HesthavenSsp).  Mixed-precision
- * handles run both sweeps as the step's Taylor polynomial 1 + dt L +
- * (dt L)^2/2 + (dt L)^3/6 (the same map): W1 = dt L u, W2 = dt L W1,
- * W3 = dt L W2, u += W1 + W2/2 + W3/6 (L^T and the adjoint state backwards),
- * with FP64 states and double-float increments formed in FP32 arithmetic
- * (not the FP32 increments of dgsw_step: the residuals and the rough adjoint
- * field need ~1e-8 of themselves over thousands of steps).
+ * and double-float handles run both sweeps as the step's Taylor polynomial
+ * 1 + dt L + (dt L)^2/2 + (dt L)^3/6 (the same map): W1 = dt L u,
+ * W2 = dt L W1, W3 = dt L W2, u += W1 + W2/2 + W3/6 (L^T and the adjoint
+ * state backwards), with FP64 states and double-float increments formed in
+ * FP32 arithmetic (on mixed-precision handles not the FP32 increments of
+ * dgsw_step: the residuals and the rough adjoint field need ~1e-8 of
+ * themselves over thousands of steps).
  * dgsw_adjoint_rhs_device: lambda -> L^T lambda (FP64), the exact transpose
  * of the operator dgsw_rhs_device applies.
  * dgsw_set_samples: points (x, y, z per point) where Psi is sampled by

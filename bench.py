@@ -973,6 +973,18 @@ def run_ours(args):
     if not args.no_mixed:
         from spectre_gb300 import PRECISION_DOUBLE_FLOAT
         evd, msd, _, stated, _ = time_path(args, PRECISION_DOUBLE_FLOAT, dev, rank, ws, False)
+        # host-resident state through dgsw_step_host, as the FP64 e2e leg
+        hostd = torch.empty(evd.state_size, dtype=torch.float64, pin_memory=True)
+        hd = hostd.numpy()
+        evd.get_state(hd)
+        for _ in range(max(args.warmup, 3)):
+            evd.step_host(hd, 1, DT)
+        torch.cuda.synchronize()
+        kd = max(1, min(args.steps, 20))
+        t0 = time.perf_counter()
+        for _ in range(kd):
+            evd.step_host(hd, 1, DT)
+        e2e_d_ms = (time.perf_counter() - t0) / kd * 1e3
         evd.close()
         double_float = {
             "value": points * 3 * args.steps * ws / (msd * 1e-3), "unit": UNIT,
@@ -980,6 +992,9 @@ def run_ours(args):
             "rel_l2_vs_fp64_after_steps": float(np.linalg.norm(stated - state64) /
                                                 np.linalg.norm(state64)),
             "max_abs_vs_fp64_after_steps": float(np.max(np.abs(stated - state64))),
+            "e2e": {"value": points * 3 * ws / (e2e_d_ms * 1e-3), "unit": UNIT,
+                    "ms_per_step": e2e_d_ms, "steps": kd,
+                    "call": "dgsw_step_host(h, pinned host state, 1, dt) per step"},
             "steps_compared": warm + args.steps,
             "dtype": "double-float (hi + lo f32 pairs, compensated products and sums), "
                      "f64 state; step as its Taylor polynomial",

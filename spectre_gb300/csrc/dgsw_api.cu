@@ -1341,6 +1341,39 @@ cudaError_t enqueue_adjoint_step(DgswHandle h, double dt) {
 // formed in FP32 arithmetic.  The misfit forward of a mixed-precision handle
 // steps with it (its residuals must hold ~1e-8 of themselves over thousands
 // of steps), on the state; the adjoint on h->adj.
+// One launch (kind 0, 1, 2) of the Taylor step over the elements
+// [begin, begin + count), on stream s.
+cudaError_t taylor_launch(DgswHandle h, double dt, bool transpose, int kind, int64_t begin,
+                          int64_t count, cudaStream_t s) {
+  const int64_t size = h->dom.offset.back();
+  float2* w1 = h->adj32;
+  float2* w2 = h->adj32 + size;
+  double* u = transpose ? h->adj : h->state;
+  TaylorLaunch A;
+  A.n = h->dom.elem_n[0];
+  A.n_elem = count;
+  A.elem_begin = begin;
+  A.transpose = transpose;
+  A.dt = dt;
+  A.nbr = h->nbr;
+  A.jac = h->jac;
+  A.eo = transpose ? h->eoT : h->eo;
+  A.gamma2 = transpose ? 0.0 : h->cfg.gamma2;
+  A.kind = kind;
+  if (kind == 0) {
+    A.x64 = u;
+    A.outp = w1;
+  } else if (kind == 1) {
+    A.xp = w1;
+    A.outp = w2;
+  } else {
+    A.xp = w2;
+    A.l64 = u;
+    A.w1 = w1;
+  }
+  return launch_taylor_df(A, s);
+}
+
 cudaError_t enqueue_taylor_step(DgswHandle h, double dt, bool transpose) {
   const int64_t size = h->dom.offset.back();
   float2* w1 = h->adj32;
@@ -1680,8 +1713,8 @@ int adams_step(DgswHandle h, int n_steps, double dt) {
 // other's tails, and the copies of some chunks overlap the stages of others
 // (the host link carries both directions at once).
 bool pipelinable(DgswHandle h) {
-  return !mixed(h) && !dfloat(h) && !h->curved && !h->gauss && !h->general && !h->refined &&
-         !h->adams && !h->filter_on && h->dom.n_elem >= 4096;
+  return !mixed(h) && !h->curved && !h->gauss && !h->general && !h->refined && !h->adams &&
+         !h->filter_on && h->dom.n_elem >= 4096;
 }
 
 // The issue order of the 3 C stage launches (3 c + stage).  The model: the
@@ -1788,8 +1821,10 @@ int pipe_init(DgswHandle h) {
   const int64_t pts = (int64_t)h->dom.elem_n[0] * h->dom.elem_n[0] * h->dom.elem_n[0];
   const double copy_s = kVars * pts * sizeof(double) / (h->pipe_link_gbs * 1e9);
   const double tuned_ms = h->tuned ? h->tune_ms[h->stage_variant] : 0.0;
+  // (double-float launches: ~3.6e-11 s per point, measured at 32^3 x 8^3)
   const double stage_s = h->pipe_stage_ns > 0.0 ? h->pipe_stage_ns * 1e-9
                          : tuned_ms > 0.0       ? tuned_ms * 1e-3 / E
+                         : dfloat(h)            ? pts * 3.6e-11
                                                 : pts * 1e-10;
   const int n_streams = std::max(1, h->pipe_streams);
   for (int k = 0; k < 2; ++k) {
@@ -1868,15 +1903,24 @@ int pipelined_step(DgswHandle h, double* host_u, double dt, bool copy_in, bool c
         if (src != s) DGSW_CUDA(h, cudaStreamWaitEvent(q, ev(st, d), 0));
       }
     }
-    StageLaunch L = base_launch(h);
-    L.mode = st == 0 ? kModeStageFirst : kModeStage;
-    L.ucur = in[st];
-    L.u0 = h->state;
-    L.unext = out[st];
-    L.coef = coef[st];
-    L.elem_begin = h->chunk_begin[c];
-    L.elem_count = h->chunk_begin[c + 1] - h->chunk_begin[c];
-    DGSW_CUDA(h, launch_stage_fp64(L, q));
+    if (dfloat(h)) {
+      // the Taylor step's three launches take the stages' places: W1 from
+      // the state, W2 from W1, W3 with the state's update in place (its
+      // readers, the W1 launches of the neighbouring chunks, precede it
+      // through the W2 launches it waits for)
+      DGSW_CUDA(h, taylor_launch(h, dt, false, st, h->chunk_begin[c],
+                                 h->chunk_begin[c + 1] - h->chunk_begin[c], q));
+    } else {
+      StageLaunch L = base_launch(h);
+      L.mode = st == 0 ? kModeStageFirst : kModeStage;
+      L.ucur = in[st];
+      L.u0 = h->state;
+      L.unext = out[st];
+      L.coef = coef[st];
+      L.elem_begin = h->chunk_begin[c];
+      L.elem_count = h->chunk_begin[c + 1] - h->chunk_begin[c];
+      DGSW_CUDA(h, launch_stage_fp64(L, q));
+    }
     DGSW_CUDA(h, cudaEventRecord(ev(st + 1, c), q));
     stream_of[3 * c + st] = s;
     if (st == 2 && copy_out) {

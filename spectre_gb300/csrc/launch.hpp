@@ -374,6 +374,9 @@ struct TaylorLaunch {
   const double* jac = nullptr;
   EoTable eo{};
   double gamma2 = 0.0;  // forward only: ScalarWave's constraint damping
+  // the elements [elem_begin, elem_begin + n_elem) only (neighbours are read
+  // wherever they are)
+  int64_t elem_begin = 0;
 };
 cudaError_t launch_taylor_df(const TaylorLaunch& L, cudaStream_t s);
 // the gamma2 != 0 kernels (taylor_df_g2.cu); launch_taylor_df calls it

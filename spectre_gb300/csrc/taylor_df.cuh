@@ -255,7 +255,7 @@ __global__ void __launch_bounds__(3 * N * N, MINB) taylor_df_kernel(TaylorLaunch
   constexpr int NT = 3 * NN;  // threads
   const int d = threadIdx.x / NN;
   const int t = threadIdx.x - d * NN;
-  const int64_t e = blockIdx.x;
+  const int64_t e = L.elem_begin + blockIdx.x;  // the grid covers the range exactly
   const int64_t off = e * (int64_t)(kVars * NP);
   const double c = L.dt;
   const int ta = t % N, tb = t / N;

@@ -135,3 +135,21 @@ def test_step_host_equals_device_steps():
         ref = ev.get_state()
         got = ev.step_host(u.copy(), 4, dt)
     np.testing.assert_array_equal(got, ref)
+
+
+@pytest.mark.parametrize("steps", [1, 2, 5])
+def test_pipelined_step_host_equals_device_steps(steps):
+    # 16^3 elements: enough for the chunked host-state path, whose copies
+    # overlap the first and last steps' launches chunk by chunk; the same
+    # bits as set_state + step + get_state
+    import torch
+    bricks = [Brick((16, 16, 16))]
+    n, dt = 4, 1e-3
+    with DgEvolution(bricks, n, precision=PRECISION_DOUBLE_FLOAT) as ev:
+        u = np.random.default_rng(steps).uniform(-1, 1, ev.state_size)
+        ev.set_state(u)
+        ev.step(steps, dt)
+        ref = ev.get_state()
+        host = torch.from_numpy(u.copy()).pin_memory()
+        got = ev.step_host(host.numpy(), steps, dt)
+    np.testing.assert_array_equal(got, ref)

@@ -153,3 +153,20 @@ def test_pipelined_step_host_equals_device_steps(steps):
         host = torch.from_numpy(u.copy()).pin_memory()
         got = ev.step_host(host.numpy(), steps, dt)
     np.testing.assert_array_equal(got, ref)
+
+
+def test_graph_chunks_equal_single_steps(oracle):
+    # dgsw_step replays windows of steps from CUDA graphs: 37 steps (two
+    # graphs of 16 and single steps) give the bits of 37 single calls
+    bricks = [Brick((2, 2, 2))]
+    n, dt = 6, 1e-3
+    u0 = oracle.initial_data(bricks, n, "gaussian", oracle.gaussian_params(1, width=1.0))
+    with DgEvolution(bricks, n, precision=PRECISION_DOUBLE_FLOAT) as ev:
+        ev.set_state(u0)
+        ev.step(37, dt)
+        a = ev.get_state()
+        ev.set_state(u0)
+        for _ in range(37):
+            ev.step(1, dt)
+        b = ev.get_state()
+    np.testing.assert_array_equal(a, b)
